@@ -1,0 +1,81 @@
+"""ctypes binding of libdepsolver_cuda.so (the in-tree CUDA library).
+
+There is no fallback: if the shared library is missing or fails to load,
+every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libdepsolver_cuda.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "depsolver_cuda.h")
+
+_lib = None
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_up = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
+
+
+class DscError(RuntimeError):
+    """A dsc_* entry point returned a non-zero status."""
+
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"status {status}: {msg}")
+        self.status = status
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run depsolver_gb300.build.build() first")
+        L = C.CDLL(LIB_PATH, mode=C.RTLD_LOCAL)
+        L.dsc_last_error.restype = C.c_char_p
+        L.dsc_device_count.restype = C.c_int
+        L.dsc_assemble.restype = C.c_int
+        L.dsc_assemble.argtypes = [C.c_int, C.c_int, C.c_uint, C.c_uint, C.c_uint, _dp, _up, _up,
+                                   C.c_void_p, C.c_void_p, C.c_double, _dp, C.c_void_p, C.c_size_t,
+                                   _dp]
+        L.dsc_gauss.restype = C.c_int
+        L.dsc_gauss.argtypes = [C.c_uint, _dp, C.c_size_t, _dp]
+        L.dsc_gmres.restype = C.c_int
+        L.dsc_gmres.argtypes = [C.c_uint, C.c_uint, C.c_double, C.c_uint, _dp, C.c_size_t, _dp,
+                                C.c_void_p, C.c_char_p, C.POINTER(C.c_uint)]
+        for nm in ("dsc_field_points", "dsc_potential_points"):
+            f = getattr(L, nm)
+            f.restype = C.c_int
+            f.argtypes = [C.c_int, C.c_uint, C.c_uint, _dp, _up, _dp, C.c_uint, _dp, _dp]
+        L.dsc_force_mst.restype = C.c_int
+        L.dsc_force_mst.argtypes = [C.c_int, C.c_uint, C.c_uint, _dp, _up, _up, _dp, C.c_double,
+                                    C.c_void_p, C.c_void_p, _dp, _dp]
+        _lib = L
+    return _lib
+
+
+def check(status: int) -> None:
+    if status != 0:
+        raise DscError(status, lib().dsc_last_error().decode(errors="replace"))
+
+
+def declared_symbols() -> list[str]:
+    """Function names declared in include/depsolver_cuda.h."""
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\(", text)
+    skip = {"if", "defined"}
+    return sorted({n for n in names if n not in skip})
+
+
+def declared_globals() -> list[str]:
+    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    out = []
+    for m in re.finditer(r"^extern\s+([^;({\"]*);", text, flags=re.M):
+        decl = m.group(1)
+        decl = re.sub(r"^(unsigned int|FILE\s*\*|double|int)\s*", "", decl)
+        out += [d.strip().lstrip("*") for d in decl.split(",")]
+    return out

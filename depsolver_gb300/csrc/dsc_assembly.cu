@@ -1,0 +1,310 @@
+// dsc_assembly.cu -- dense geometric matrix K of the collocation system.
+//
+// Restates the element loops of electricFormA_tria3/tria6
+// (src/assembly_el.c:63-307) without the frequency: K[c][i] (column-major)
+// holds C * int G N_c for conductor rows and int H N_c for interface rows.
+//
+// Regular pairs (row node not in the element) -- k_asm_regular:
+//   CTA = 32 collocation rows x one group of 32 elements (Morton order).
+//   Phase A: each warp takes one element at a time, lane = row; the 7-point
+//   rule (src/kernelIntegrals.c:109-142, :231-282) gives nen values per
+//   (row, element) pair, staged in shared memory as V[slot][row].
+//   Phase B: each footprint node of the group sums its slots and writes one
+//   coalesced 32-row segment of its K column (or of a partial-sum slot when
+//   other groups touch the node too).
+// Partial slots are added in group order by k_asm_fixup (deterministic).
+// Singular pairs -- k_asm_singular: one warp per row, the row's elements in
+// element order, quadrature points split over the lanes (dsc_singular.cuh).
+#include "dsc_common.cuh"
+#include "dsc_internal.h"
+#include "dsc_singular.cuh"
+
+namespace dsc {
+
+// Shape-function values at the 7 points of the regular rule.
+struct Shape7 {
+    double v[kTriPts][6];
+};
+
+constexpr double kT7[kTriPts][2] = {
+    {0.333333333333333, 0.333333333333333}, {0.470142064105115, 0.470142064105115},
+    {0.0597158717897700, 0.470142064105115}, {0.470142064105115, 0.0597158717897700},
+    {0.101286507323456, 0.101286507323456}, {0.797426985353088, 0.101286507323456},
+    {0.101286507323456, 0.797426985353088}};
+constexpr double kW7[kTriPts] = {0.1125, 0.066197076394253, 0.066197076394253, 0.066197076394253,
+                                 0.062969590272414, 0.062969590272414, 0.062969590272414};
+
+constexpr Shape7 make_shape(int nen)
+{
+    Shape7 s{};
+    for (int q = 0; q < kTriPts; q++) {
+        double l1 = kT7[q][0], l2 = kT7[q][1], l3 = 1.0 - l1 - l2;
+        if (nen == 3) {
+            s.v[q][0] = l1;
+            s.v[q][1] = l2;
+            s.v[q][2] = l3;
+        } else {
+            s.v[q][0] = l1 * (2.0 * l1 - 1.0);
+            s.v[q][1] = 4.0 * l1 * l2;
+            s.v[q][2] = l2 * (2.0 * l2 - 1.0);
+            s.v[q][3] = 4.0 * l2 * l3;
+            s.v[q][4] = l3 * (2.0 * l3 - 1.0);
+            s.v[q][5] = 4.0 * l1 * l3;
+        }
+    }
+    return s;
+}
+
+__constant__ Shape7 c_shape3 = make_shape(3);
+__constant__ Shape7 c_shape6 = make_shape(6);
+
+template <int NEN>
+__device__ __forceinline__ double shape_q(int q, int k)
+{
+    return NEN == 3 ? c_shape3.v[q][k] : c_shape6.v[q][k];
+}
+
+// Quadrature points of every element: x, y, z and w_q * J_q.
+template <int NEN>
+__global__ void k_elem_qp(const double *__restrict__ X, const double *__restrict__ Y,
+                          const double *__restrict__ Z, const int *__restrict__ elems, int E,
+                          double *__restrict__ qp)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= E * kTriPts) return;
+    int e = t / kTriPts, q = t % kTriPts;
+    double Xe[NEN][3], N[NEN], XL[3];
+#pragma unroll
+    for (int k = 0; k < NEN; k++) {
+        int v = elems[(size_t)e * NEN + k];
+        Xe[k][0] = X[v];
+        Xe[k][1] = Y[v];
+        Xe[k][2] = Z[v];
+    }
+    double l1 = c_tri7[q][0], l2 = c_tri7[q][1];
+    shape<NEN>(l1, l2, N);
+    double J = map_point<NEN>(Xe, l1, l2, N, XL);
+    double *o = qp + (size_t)t * 4;
+    o[0] = XL[0];
+    o[1] = XL[1];
+    o[2] = XL[2];
+    o[3] = c_tri7[q][2] * J;
+}
+
+struct AsmArgs {
+    const double *X, *Y, *Z, *normals, *row_fac, *qp;
+    const int *row_kind, *elems, *grp_elem, *fp_ptr, *fp_dest, *fp_sl_ptr;
+    const uint16_t *fp_sl;
+    int N, row_lo, row_hi;
+    size_t ld, ldp;
+};
+
+// MODE 0: every row of the warp is a conductor row (G = 1/r);
+// MODE 1: every row is an interface row (H = n.(x-y)/r^3); MODE 2: mixed.
+template <int NEN, int MODE>
+__device__ __forceinline__ void pair_regular_f64(const double *__restrict__ q7, double xi, double yi,
+                                                 double zi, double nx, double ny, double nz,
+                                                 bool isH, double *acc)
+{
+#pragma unroll
+    for (int q = 0; q < kTriPts; q++) {
+        const double *Q = q7 + q * 4;
+        double dx = xi - Q[0], dy = yi - Q[1], dz = zi - Q[2];
+        double r2 = dx * dx + dy * dy + dz * dz;
+        double inv = rsqrt(r2);
+        double w;
+        if (MODE == 0) {
+            w = Q[3] * inv;
+        } else {
+            double h = Q[3] * inv * inv * inv * (dx * nx + dy * ny + dz * nz);
+            w = (MODE == 1 || isH) ? h : Q[3] * inv;
+        }
+#pragma unroll
+        for (int k = 0; k < NEN; k++) acc[k] += w * shape_q<NEN>(q, k);
+    }
+}
+
+template <int NEN>
+__global__ void __launch_bounds__(128) k_asm_regular_f64(AsmArgs a, double *__restrict__ K,
+                                                         double *__restrict__ P)
+{
+    constexpr int R = kRowTile, EG = kGroup;
+    extern __shared__ double smem[];
+    double *s_qp = smem;                                   // EG * 28
+    double *s_V = smem + EG * kTriPts * 4;                 // EG * NEN * R
+    int *s_nodes = (int *)(s_V + EG * NEN * R);            // EG * NEN
+    const int g = blockIdx.y;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+
+    for (int t = threadIdx.x; t < EG * kTriPts * 4; t += blockDim.x) {
+        int e = a.grp_elem[g * EG + t / (kTriPts * 4)];
+        s_qp[t] = e >= 0 ? a.qp[(size_t)e * kTriPts * 4 + t % (kTriPts * 4)] : 0.0;
+    }
+    for (int t = threadIdx.x; t < EG * NEN; t += blockDim.x) {
+        int e = a.grp_elem[g * EG + t / NEN];
+        s_nodes[t] = e >= 0 ? a.elems[(size_t)e * NEN + t % NEN] : -1;
+    }
+    __syncthreads();
+
+    const int i = a.row_lo + blockIdx.x * R + lane;
+    const bool valid = i < a.row_hi;
+    const int ii = valid ? i : a.row_lo;
+    const double xi = a.X[ii], yi = a.Y[ii], zi = a.Z[ii];
+    const double nx = a.normals[3 * (size_t)ii], ny = a.normals[3 * (size_t)ii + 1],
+                 nz = a.normals[3 * (size_t)ii + 2];
+    const int kind = valid ? a.row_kind[ii] : 0;
+    const double fac = a.row_fac[ii];
+    const bool allG = __all_sync(0xffffffffu, kind == 0);
+    const bool allH = __all_sync(0xffffffffu, kind == 1);
+
+    for (int el = w; el < EG; el += 4) {
+        double acc[NEN];
+#pragma unroll
+        for (int k = 0; k < NEN; k++) acc[k] = 0.0;
+        const int *en = s_nodes + el * NEN;
+        bool drop = en[0] < 0;
+#pragma unroll
+        for (int k = 0; k < NEN; k++) drop |= en[k] == i;
+        if (en[0] >= 0) {
+            const double *q7 = s_qp + el * kTriPts * 4;
+            if (allG) pair_regular_f64<NEN, 0>(q7, xi, yi, zi, nx, ny, nz, false, acc);
+            else if (allH) pair_regular_f64<NEN, 1>(q7, xi, yi, zi, nx, ny, nz, true, acc);
+            else pair_regular_f64<NEN, 2>(q7, xi, yi, zi, nx, ny, nz, kind == 1, acc);
+        }
+#pragma unroll
+        for (int k = 0; k < NEN; k++) s_V[(el * NEN + k) * R + lane] = drop ? 0.0 : fac * acc[k];
+    }
+    __syncthreads();
+
+    const int f0 = a.fp_ptr[g], f1 = a.fp_ptr[g + 1];
+    for (int j = f0 + w; j < f1; j += 4) {
+        const int s0 = a.fp_sl_ptr[j], s1 = a.fp_sl_ptr[j + 1];
+        double sum = 0.0;
+        for (int m = s0; m < s1; m++) sum += s_V[a.fp_sl[m] * R + lane];
+        const int dest = a.fp_dest[j];
+        if (valid) {
+            if (dest >= 0) K[(size_t)dest * a.ld + i] = sum;
+            else P[(size_t)(-dest - 1) * a.ldp + (i - a.row_lo)] = sum;
+        }
+    }
+}
+
+// K column of every node shared by several groups = sum of its slots in
+// group order; nodes in no element get a zero column.
+template <typename T>
+__global__ void k_asm_fixup(const int *__restrict__ fix_ptr, const int *__restrict__ fix_slot,
+                            const int *__restrict__ fix_col, int n_fix, const T *__restrict__ P,
+                            size_t ldp, T *__restrict__ K, size_t ld, int row_lo, int nrows)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrows) return;
+    for (int b = blockIdx.y; b < n_fix; b += gridDim.y) {
+        T sum = 0;
+        for (int t = fix_ptr[b]; t < fix_ptr[b + 1]; t++) sum += P[(size_t)fix_slot[t] * ldp + r];
+        K[(size_t)fix_col[b] * ld + row_lo + r] = sum;
+    }
+}
+
+// Singular pairs: warp per row, adds into K (FP64 sums, stored as T).
+template <int NEN, typename T>
+__global__ void __launch_bounds__(128) k_asm_singular(const double *__restrict__ X,
+                                                      const double *__restrict__ Y,
+                                                      const double *__restrict__ Z,
+                                                      const double *__restrict__ normals,
+                                                      const int *__restrict__ row_kind,
+                                                      const double *__restrict__ row_fac,
+                                                      const int *__restrict__ elems,
+                                                      const int *__restrict__ ne_ptr,
+                                                      const int *__restrict__ ne_elem,
+                                                      const int *__restrict__ ne_pos, int row_lo,
+                                                      int row_hi, T *__restrict__ K, size_t ld)
+{
+    const int i = row_lo + (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (i >= row_hi) return;
+    const double xe[3] = {X[i], Y[i], Z[i]};
+    const double n[3] = {normals[3 * (size_t)i], normals[3 * (size_t)i + 1],
+                         normals[3 * (size_t)i + 2]};
+    const int kind = row_kind[i];
+    const double fac = row_fac[i];
+    for (int t = ne_ptr[i]; t < ne_ptr[i + 1]; t++) {
+        const int e = ne_elem[t], s = ne_pos[t] + 1;
+        double Xe[NEN][3], out[NEN];
+#pragma unroll
+        for (int k = 0; k < NEN; k++) {
+            int v = elems[(size_t)e * NEN + k];
+            Xe[k][0] = X[v];
+            Xe[k][1] = Y[v];
+            Xe[k][2] = Z[v];
+        }
+        if (kind == 0) warp_singular_G<NEN>(s, Xe, xe, out);
+        else warp_singular_H<NEN, 0>(s, Xe, xe, n, out);
+        if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < NEN; k++) {
+                size_t o = (size_t)elems[(size_t)e * NEN + k] * ld + i;
+                K[o] = (T)((double)K[o] + fac * out[k]);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+static size_t regular_smem(int nen)
+{
+    return (size_t)kGroup * kTriPts * 4 * sizeof(double) +
+           (size_t)kGroup * nen * kRowTile * sizeof(double) + (size_t)kGroup * nen * sizeof(int);
+}
+
+template <int NEN>
+static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStream_t st)
+{
+    k_elem_qp<NEN><<<(m.E * kTriPts + 255) / 256, 256, 0, st>>>(m.x.p, m.y.p, m.z.p, m.elems.p, m.E,
+                                                                  m.qp.p);
+    DSC_CUDA(cudaGetLastError());
+    // Partial-sum buffer: n_slots columns of a row chunk, at most ~1 GiB.
+    const size_t budget = (size_t)1 << 30;
+    int rc = m.N;
+    if (m.n_slots > 0) {
+        size_t per_row = (size_t)m.n_slots * sizeof(double);
+        size_t fit = budget / per_row;
+        if (fit < (size_t)rc) rc = (int)std::max<size_t>(kRowTile, fit / kRowTile * kRowTile);
+    }
+    DevBuf<double> P;
+    DSC_TRY(P.alloc((size_t)std::max(m.n_slots, 1) * rc));
+    const size_t smem = regular_smem(NEN);
+    DSC_CUDA(cudaFuncSetAttribute(k_asm_regular_f64<NEN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem));
+    AsmArgs a{m.x.p, m.y.p, m.z.p, m.normals.p, m.row_fac.p, m.qp.p, m.row_kind.p, m.elems.p,
+              m.grp_elem.p, m.fp_ptr.p, m.fp_dest.p, m.fp_sl_ptr.p, m.fp_sl.p, m.N, 0, 0, ld,
+              (size_t)rc};
+    for (int lo = 0; lo < m.N; lo += rc) {
+        int hi = std::min(m.N, lo + rc);
+        a.row_lo = lo;
+        a.row_hi = hi;
+        dim3 grid((hi - lo + kRowTile - 1) / kRowTile, m.G);
+        k_asm_regular_f64<NEN><<<grid, 128, smem, st>>>(a, K, P.p);
+        DSC_CUDA(cudaGetLastError());
+        if (m.n_fix > 0) {
+            dim3 fg((hi - lo + 255) / 256, std::min(m.n_fix, 65535));
+            k_asm_fixup<double><<<fg, 256, 0, st>>>(m.fix_ptr.p, m.fix_slot.p, m.fix_col.p, m.n_fix,
+                                                    P.p, (size_t)rc, K, ld, lo, hi - lo);
+            DSC_CUDA(cudaGetLastError());
+        }
+        int warps = hi - lo;
+        k_asm_singular<NEN, double><<<(warps * 32 + 127) / 128, 128, 0, st>>>(
+            m.x.p, m.y.p, m.z.p, m.normals.p, m.row_kind.p, m.row_fac.p, m.elems.p, m.ne_ptr.p,
+            m.ne_elem.p, m.ne_pos.p, lo, hi, K, ld);
+        DSC_CUDA(cudaGetLastError());
+    }
+    // P is released at scope exit: wait for the kernels that read it.
+    DSC_CUDA(cudaStreamSynchronize(st));
+    return kOk;
+}
+
+int assemble_K_fp64(const DeviceMesh &m, double *K, size_t ld, cudaStream_t st)
+{
+    return m.nen == 6 ? assemble_fp64_impl<6>(m, K, ld, st) : assemble_fp64_impl<3>(m, K, ld, st);
+}
+
+}  // namespace dsc

@@ -1,0 +1,59 @@
+// dsc_blas.cuh -- small deterministic vector kernels shared by the solvers.
+#pragma once
+
+#include "dsc_common.cuh"
+
+namespace dsc {
+
+// Fixed grid so that every reduction adds the same partials in the same
+// order on every run and every device.
+constexpr int kRedBlocks = 256;
+constexpr int kRedThreads = 256;
+
+// Workspace of one reduction: kRedBlocks partials and a completion counter.
+struct RedWork {
+    double *partials;  // kRedBlocks
+    unsigned *counter; // 1, zero between uses
+};
+
+__device__ __forceinline__ double block_sum(double v, double *sh)
+{
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (w == 0) {
+        r = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
+        r = warp_sum(r);
+    }
+    __syncthreads();
+    return r;  // valid in warp 0
+}
+
+// The last block to finish adds the partials (in block order) and writes
+// *out; the counter is reset for the next reduction.
+__device__ __forceinline__ void finish_reduction(double v, RedWork rw, double *out, double *sh)
+{
+    double b = block_sum(v, sh);
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        rw.partials[blockIdx.x] = b;
+        __threadfence();
+        unsigned done = atomicAdd(rw.counter, 1u);
+        last = done == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last && threadIdx.x < 32) {
+        __threadfence();
+        double s = 0.0;
+        for (int t = threadIdx.x; t < (int)gridDim.x; t += 32) s += ((volatile double *)rw.partials)[t];
+        s = warp_sum(s);
+        if (threadIdx.x == 0) {
+            *out = s;
+            *rw.counter = 0;
+        }
+    }
+}
+
+}  // namespace dsc

@@ -1,0 +1,680 @@
+// dsc_capi.cu -- the exported C ABI (include/depsolver_cuda.h).
+//
+// Drop-in entry points keep the reference's names, signatures, globals and
+// error behaviour; dsc_* entry points take flat arrays and return status
+// codes.  Both run the same device code.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <memory>
+#include <mutex>
+#include <vector>
+
+#include "../../include/depsolver_cuda.h"
+#include "dsc_common.cuh"
+#include "dsc_field.h"
+#include "dsc_gmres.h"
+#include "dsc_internal.h"
+
+// Globals read by the drop-in entry points (the reference defines them in
+// src/depSolver.c:46-50; a host program's definitions take precedence).
+unsigned int nNodes, nElems, nInterfaces;
+FILE *file_log;
+
+namespace dsc {
+
+// ---------------------------------------------------------------- context
+struct MeshEntry {
+    uint64_t key = 0;
+    HostPlan plan;
+    DeviceMesh dev;
+};
+
+struct Context {
+    std::mutex mu;
+    cudaStream_t st = nullptr;
+    std::unique_ptr<MeshEntry> mesh;
+    uint64_t sigma_key = 0;
+    DevBuf<double> sigma;
+    double *pinned = nullptr;
+    size_t pinned_bytes = 0;
+};
+
+static Context &ctx()
+{
+    static Context c;
+    return c;
+}
+
+static int ensure_stream()
+{
+    Context &c = ctx();
+    if (!c.st) {
+        int n = 0;
+        if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+            cudaGetLastError();
+            set_error("no CUDA device available");
+            return kErrCuda;
+        }
+        DSC_CUDA(cudaStreamCreateWithFlags(&c.st, cudaStreamNonBlocking));
+    }
+    return kOk;
+}
+
+static int ensure_pinned(size_t bytes)
+{
+    Context &c = ctx();
+    if (c.pinned_bytes >= bytes) return kOk;
+    if (c.pinned) cudaFreeHost(c.pinned);
+    c.pinned = nullptr;
+    c.pinned_bytes = 0;
+    DSC_CUDA(cudaHostAlloc((void **)&c.pinned, bytes, cudaHostAllocDefault));
+    c.pinned_bytes = bytes;
+    return kOk;
+}
+
+static uint64_t mix(uint64_t h, uint64_t v)
+{
+    h ^= v + 0x9e3779b97f4a7c15ULL + (h << 6) + (h >> 2);
+    return h * 0xff51afd7ed558ccdULL;
+}
+
+static uint64_t hash_bytes(uint64_t h, const void *p, size_t n)
+{
+    const unsigned char *b = (const unsigned char *)p;
+    size_t w = n / 8;
+    for (size_t i = 0; i < w; i++) {
+        uint64_t v;
+        memcpy(&v, b + 8 * i, 8);
+        h = mix(h, v);
+    }
+    for (size_t i = 8 * w; i < n; i++) h = mix(h, b[i]);
+    return mix(h, n);
+}
+
+// Geometry (and its device copy) for these nodes and 0-based elements,
+// rebuilt only when the content changes.
+static int get_mesh(int nen, int N, int E, const double *nodes, const int *elems0,
+                    MeshEntry **out)
+{
+    DSC_TRY(ensure_stream());
+    Context &c = ctx();
+    uint64_t key = mix(mix(mix(0x243f6a8885a308d3ULL, nen), N), E);
+    key = hash_bytes(key, nodes, (size_t)N * 3 * sizeof(double));
+    key = hash_bytes(key, elems0, (size_t)E * nen * sizeof(int));
+    if (!c.mesh || c.mesh->key != key) {
+        auto m = std::make_unique<MeshEntry>();
+        DSC_TRY(build_plan(nen, N, E, nodes, elems0, nullptr, m->plan));
+        DSC_TRY(m->dev.upload(m->plan, c.st));
+        m->key = key;
+        c.mesh = std::move(m);
+        c.sigma_key = 0;
+    }
+    *out = c.mesh.get();
+    return kOk;
+}
+
+static int get_sigma(int N, const double *vB, const double **dsig)
+{
+    Context &c = ctx();
+    uint64_t key = hash_bytes(0x13198a2e03707344ULL ^ c.mesh->key, vB, (size_t)2 * N * sizeof(double));
+    if (c.sigma_key != key) {
+        DSC_TRY(c.sigma.upload(vB, (size_t)2 * N, c.st));
+        DSC_CUDA(cudaStreamSynchronize(c.st));
+        c.sigma_key = key;
+    }
+    *dsig = c.sigma.p;
+    return kOk;
+}
+
+// Flattened copies of the reference's row-pointer inputs.
+struct FlatMesh {
+    std::vector<double> nodes;
+    std::vector<int> elems0;
+};
+
+static void flatten(int nen, int N, int E, double **mNodes, unsigned **mElems, FlatMesh &f)
+{
+    f.nodes.resize((size_t)N * 3);
+    f.elems0.resize((size_t)E * nen);
+    for (int i = 0; i < N; i++)
+        for (int d = 0; d < 3; d++) f.nodes[3 * (size_t)i + d] = mNodes[i][d];
+    for (int e = 0; e < E; e++)
+        for (int k = 0; k < nen; k++) f.elems0[(size_t)e * nen + k] = (int)mElems[e][k] - 1;
+}
+
+static int elems_to0(int nen, int E, const unsigned *elems1, std::vector<int> &out)
+{
+    out.resize((size_t)E * nen);
+    for (size_t t = 0; t < out.size(); t++) out[t] = (int)elems1[t] - 1;
+    return kOk;
+}
+
+// ---------------------------------------------------------------- assembly
+// Rows [r0, r1) of the compact (full = 0) or full (full = 1) system from K:
+// top rows i:    [a_i K_i + d_i e_i | b_i K_i]
+// bottom rows N+i (full only): [-b_i K_i | a_i K_i + d_i e_(N+i)]
+// K is column-major; a 32 x 32 shared tile turns its columns into rows.
+__global__ void k_form_rows(const double *__restrict__ K, size_t ld, int N, int full, int r0,
+                            int r1, const double *__restrict__ ca, const double *__restrict__ cb,
+                            const double *__restrict__ cd, double *__restrict__ out)
+{
+    __shared__ double t[32][33];
+    const int c0 = blockIdx.x * 32, rr0 = r0 + blockIdx.y * 32;
+    const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+    for (int k = ty; k < 32; k += 8) {
+        int c = c0 + k, r = rr0 + tx;
+        int i = r < N ? r : r - N;
+        t[k][tx] = (c < N && r < r1) ? K[(size_t)c * ld + i] : 0.0;
+    }
+    __syncthreads();
+    const size_t ncol = 2 * (size_t)N;
+    for (int k = ty; k < 32; k += 8) {
+        int r = rr0 + k, c = c0 + tx;
+        if (r >= r1 || c >= N) continue;
+        const bool top = r < N;
+        const int i = top ? r : r - N;
+        const double kv = t[tx][k];
+        const double a = ca[i], b = cb[i], d = cd[i];
+        double left, right;
+        if (top) {
+            left = a * kv + (c == i ? d : 0.0);
+            right = b * kv;
+        } else {
+            left = -b * kv;
+            right = a * kv + (c == i ? d : 0.0);
+        }
+        double *o = out + (size_t)(r - r0) * ncol;
+        o[c] = left;
+        o[c + N] = right;
+    }
+}
+
+typedef void (*RowSinkFn)(void *user, int row, const double *vals, size_t n);
+
+// Assembles K in FP64 and streams the requested form out row-chunk by
+// row-chunk: device transpose into a staging block, copy to pinned host
+// memory, then sink(row, values) for every row.
+static int assemble_impl(int nen, int full, unsigned N, unsigned E, unsigned nIf,
+                         const double *nodes, const int *elems0, const unsigned *bctype,
+                         const unsigned *ifaces, const double *mat, double freq, const double *mbc,
+                         RowSinkFn sink, void *user)
+{
+    MeshEntry *m;
+    DSC_TRY(get_mesh(nen, (int)N, (int)E, nodes, elems0, &m));
+    DSC_TRY(set_rows(m->plan, bctype));
+    cudaStream_t st = ctx().st;
+    DSC_TRY(m->dev.upload_rows(m->plan, st));
+    // Per-row coefficients: conductor rows a = 1 (K holds C int G N);
+    // interface rows a = A_k, b = B_k, d = -1/(2 eps0) with k the row's
+    // interface id mBC[i][1] (src/assembly_el.c:245-256).
+    std::vector<double> Ak(nIf ? nIf : 1), Bk(nIf ? nIf : 1);
+    if (nIf) interface_coeffs(nIf, ifaces, mat, freq, Ak.data(), Bk.data());
+    std::vector<double> ca(N), cb(N), cd(N);
+    for (unsigned i = 0; i < N; i++) {
+        if (m->plan.row_kind[i] == 0) {
+            ca[i] = 1.0;
+            cb[i] = 0.0;
+            cd[i] = 0.0;
+        } else {
+            unsigned k = (unsigned)mbc[3 * (size_t)i + 1] - 1;
+            if (k >= nIf) {
+                set_error("node %u: interface id %g outside 1..%u", i + 1, mbc[3 * (size_t)i + 1], nIf);
+                return kErrArg;
+            }
+            ca[i] = Ak[k];
+            cb[i] = Bk[k];
+            cd[i] = -0.5 / kEps0;
+        }
+    }
+    DevBuf<double> dca, dcb, dcd, K, stage;
+    DSC_TRY(dca.upload(ca, st));
+    DSC_TRY(dcb.upload(cb, st));
+    DSC_TRY(dcd.upload(cd, st));
+    const size_t ld = ((size_t)N + 31) / 32 * 32;
+    DSC_TRY(K.alloc(ld * N));
+    DSC_TRY(assemble_K_fp64(m->dev, K.p, ld, st));
+
+    const size_t ncol = 2 * (size_t)N;
+    const int nrows = full ? 2 * (int)N : (int)N;
+    // staging block of at most 64 MiB (and at least 32 rows)
+    int rows_per = (int)std::max<size_t>(32, ((size_t)64 << 20) / (ncol * sizeof(double)) / 32 * 32);
+    rows_per = std::min(rows_per, (nrows + 31) / 32 * 32);
+    DSC_TRY(stage.alloc((size_t)rows_per * ncol));
+    DSC_TRY(ensure_pinned((size_t)rows_per * ncol * sizeof(double)));
+    double *host = ctx().pinned;
+    for (int r0 = 0; r0 < nrows; r0 += rows_per) {
+        const int r1 = std::min(nrows, r0 + rows_per);
+        dim3 grid(((int)N + 31) / 32, (r1 - r0 + 31) / 32), blk(32, 8);
+        k_form_rows<<<grid, blk, 0, st>>>(K.p, ld, (int)N, full, r0, r1, dca.p, dcb.p, dcd.p, stage.p);
+        DSC_CUDA(cudaGetLastError());
+        DSC_CUDA(cudaMemcpyAsync(host, stage.p, (size_t)(r1 - r0) * ncol * sizeof(double),
+                                 cudaMemcpyDeviceToHost, st));
+        DSC_CUDA(cudaStreamSynchronize(st));
+        for (int r = r0; r < r1; r++) sink(user, r, host + (size_t)(r - r0) * ncol, ncol);
+    }
+    return kOk;
+}
+
+struct RowPtrSink {
+    double **rows;
+};
+
+static void add_to_rowptr(void *u, int r, const double *v, size_t n)
+{
+    double *row = ((RowPtrSink *)u)->rows[r];
+    for (size_t c = 0; c < n; c++) row[c] += v[c];
+}
+
+struct FlatSink {
+    double *A;
+    size_t lda;
+};
+
+static void add_to_flat(void *u, int r, const double *v, size_t n)
+{
+    FlatSink *f = (FlatSink *)u;
+    double *row = f->A + (size_t)r * f->lda;
+    for (size_t c = 0; c < n; c++) row[c] += v[c];
+}
+
+// ---------------------------------------------------------------- solvers
+static int gauss_impl(unsigned n, const double *const *rows, const double *flat, size_t lda,
+                      double *B, int *bad_row)
+{
+    DSC_TRY(ensure_stream());
+    cudaStream_t st = ctx().st;
+    const size_t ldd = ((size_t)n + 1 + 31) / 32 * 32;
+    DevBuf<double> A;
+    DSC_TRY(A.alloc(ldd * n));
+    // pack rows (plus B as column n) through pinned memory, 64 MiB at a time
+    const size_t chunk = std::max<size_t>(1, ((size_t)64 << 20) / (ldd * sizeof(double)));
+    DSC_TRY(ensure_pinned(chunk * ldd * sizeof(double)));
+    double *host = ctx().pinned;
+    for (size_t r0 = 0; r0 < n; r0 += chunk) {
+        size_t r1 = std::min<size_t>(n, r0 + chunk);
+        for (size_t r = r0; r < r1; r++) {
+            const double *src = rows ? rows[r] : flat + r * lda;
+            double *dst = host + (r - r0) * ldd;
+            memcpy(dst, src, n * sizeof(double));
+            dst[n] = B[r];
+        }
+        DSC_CUDA(cudaMemcpyAsync(A.p + r0 * ldd, host, (r1 - r0) * ldd * sizeof(double),
+                                 cudaMemcpyHostToDevice, st));
+        DSC_CUDA(cudaStreamSynchronize(st));
+    }
+    DSC_TRY(lu_solve_augmented_fp64((int)n, A.p, ldd, bad_row, st));
+    DevBuf<double> x;
+    DSC_TRY(x.alloc(n));
+    DSC_TRY(lu_extract_solution((int)n, A.p, ldd, x.p, st));
+    DSC_CUDA(cudaMemcpyAsync(B, x.p, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    DSC_CUDA(cudaStreamSynchronize(st));
+    return kOk;
+}
+
+static int gmres_impl(unsigned N, unsigned preCond, double tol, unsigned maxit,
+                      const double *const *rows, const double *flat, size_t lda, double *B,
+                      const double *x0, FILE *log, unsigned *iters)
+{
+    DSC_TRY(ensure_stream());
+    cudaStream_t st = ctx().st;
+    const size_t ncol = 2 * (size_t)N;
+    const size_t ldd = (ncol + 31) / 32 * 32;
+    DevBuf<double> A, dB, dx0;
+    DSC_TRY(A.alloc(ldd * N));
+    const size_t chunk = std::max<size_t>(1, ((size_t)64 << 20) / (ldd * sizeof(double)));
+    DSC_TRY(ensure_pinned(chunk * ldd * sizeof(double)));
+    double *host = ctx().pinned;
+    for (size_t r0 = 0; r0 < N; r0 += chunk) {
+        size_t r1 = std::min<size_t>(N, r0 + chunk);
+        for (size_t r = r0; r < r1; r++)
+            memcpy(host + (r - r0) * ldd, rows ? rows[r] : flat + r * lda, ncol * sizeof(double));
+        DSC_CUDA(cudaMemcpyAsync(A.p + r0 * ldd, host, (r1 - r0) * ldd * sizeof(double),
+                                 cudaMemcpyHostToDevice, st));
+        DSC_CUDA(cudaStreamSynchronize(st));
+    }
+    DSC_TRY(dB.upload(B, ncol, st));
+    if (x0) DSC_TRY(dx0.upload(x0, ncol, st));
+    int rc = gmres_compact_fp64((int)N, A.p, ldd, dB.p, x0 ? dx0.p : nullptr, preCond, tol, maxit,
+                                log, iters, st);
+    if (rc == kOk) {
+        DSC_CUDA(cudaMemcpyAsync(B, dB.p, ncol * sizeof(double), cudaMemcpyDeviceToHost, st));
+        DSC_CUDA(cudaStreamSynchronize(st));
+    }
+    return rc;
+}
+
+static int points_impl(int nen, unsigned N, unsigned E, const double *nodes, const int *elems0,
+                       const double *vB, unsigned npts, const double *pts, int field, double *out)
+{
+    MeshEntry *m;
+    DSC_TRY(get_mesh(nen, (int)N, (int)E, nodes, elems0, &m));
+    const double *dsig;
+    DSC_TRY(get_sigma((int)N, vB, &dsig));
+    cudaStream_t st = ctx().st;
+    PointSet ps;
+    DSC_TRY(ps.build(m->plan, (int)npts, pts));
+    DevBuf<double> dout;
+    const int nv = field ? 6 : 2;
+    DSC_TRY(dout.alloc((size_t)npts * nv));
+    DSC_TRY(eval_points(m->dev, ps, dsig, field, dout.p, st));
+    DSC_CUDA(cudaMemcpyAsync(out, dout.p, (size_t)npts * nv * sizeof(double), cudaMemcpyDeviceToHost,
+                             st));
+    DSC_CUDA(cudaStreamSynchronize(st));
+    return kOk;
+}
+
+static int force_impl(int nen, unsigned N, unsigned E, const double *nodes, const int *elems0,
+                      const unsigned *bctype, const double *vB, double eps, double *Fce,
+                      double *Xce, double *Fcm, double *Xcm)
+{
+    MeshEntry *m;
+    DSC_TRY(get_mesh(nen, (int)N, (int)E, nodes, elems0, &m));
+    const double *dsig;
+    DSC_TRY(get_sigma((int)N, vB, &dsig));
+    return force_mst(m->dev, m->plan, bctype, dsig, eps, Fce, Xce, Fcm, Xcm, ctx().st);
+}
+
+// ---------------------------------------------------------------- fatal
+// The reference's errorHandler (src/errorHandler.c:42-52): message on
+// stderr and in bem.log, then exit(1).
+static void fatal(const char *msg)
+{
+    fprintf(stderr, "\nERROR: %s\n", msg);
+    fprintf(stderr, "*** PROGRAM TERMINATED ***\n\n");
+    if (file_log) {
+        fprintf(file_log, "\nERROR: %s\n", msg);
+        fprintf(file_log, "*** PROGRAM TERMINATED ***\n\n");
+        fclose(file_log);
+    }
+    exit(1);
+}
+
+static void check_or_die(int rc)
+{
+    if (rc != kOk) fatal(last_error());
+}
+
+// Material table size implied by the interfaces (ids are 1-based).
+static unsigned n_materials(unsigned nIf, unsigned **vInterfaces)
+{
+    unsigned m = 0;
+    for (unsigned i = 0; i < nIf; i++) m = std::max(m, std::max(vInterfaces[i][0], vInterfaces[i][1]));
+    return m;
+}
+
+static int electric_form(int nen, int full, double **mNodes, unsigned **mElems, unsigned *vBCType,
+                         unsigned **vInterfaces, double **vMatParam, double *vProbParam, double **mA,
+                         double **mBC, double *vB)
+{
+    std::lock_guard<std::mutex> lk(ctx().mu);
+    const unsigned N = nNodes, E = nElems, nIf = nInterfaces;
+    FlatMesh f;
+    flatten(nen, (int)N, (int)E, mNodes, mElems, f);
+    std::vector<unsigned> ifc((size_t)nIf * 2);
+    for (unsigned i = 0; i < nIf; i++) {
+        ifc[2 * i] = vInterfaces[i][0];
+        ifc[2 * i + 1] = vInterfaces[i][1];
+    }
+    unsigned nm = n_materials(nIf, vInterfaces);
+    std::vector<double> mat((size_t)std::max(nm, 1u) * 2, 0.0);
+    for (unsigned i = 0; i < nm; i++) {
+        mat[2 * i] = vMatParam[i][0];
+        mat[2 * i + 1] = vMatParam[i][1];
+    }
+    std::vector<double> mbc((size_t)2 * N * 3);
+    for (size_t j = 0; j < 2 * (size_t)N; j++)
+        for (int d = 0; d < 3; d++) mbc[3 * j + d] = mBC[j][d];
+    RowPtrSink sink{mA};
+    check_or_die(assemble_impl(nen, full, N, E, nIf, f.nodes.data(), f.elems0.data(), vBCType,
+                               ifc.data(), mat.data(), vProbParam[0], mbc.data(), add_to_rowptr,
+                               &sink));
+    // right-hand side (src/assembly_el.c:296-298)
+    for (unsigned i = 0; i < N; i++) {
+        vB[i] = mBC[i][0];
+        vB[i + N] = mBC[i + N][0];
+    }
+    return 0;
+}
+
+}  // namespace dsc
+
+using namespace dsc;
+
+// ================================================================ drop-in
+
+extern "C" int electricFormA_tria3(double **mNodes, unsigned int **mElems, unsigned int *vBCType,
+                                   unsigned int **vInterfaces, double **vMatParam,
+                                   double *vProbParam, double **mA, double **mBC, double *vB)
+{
+    return electric_form(3, 0, mNodes, mElems, vBCType, vInterfaces, vMatParam, vProbParam, mA, mBC, vB);
+}
+
+extern "C" int electricFormA_tria6(double **mNodes, unsigned int **mElems, unsigned int *vBCType,
+                                   unsigned int **vInterfaces, double **vMatParam,
+                                   double *vProbParam, double **mA, double **mBC, double *vB)
+{
+    return electric_form(6, 0, mNodes, mElems, vBCType, vInterfaces, vMatParam, vProbParam, mA, mBC, vB);
+}
+
+extern "C" int electricFormFullA_tria3(double **mNodes, unsigned int **mElems,
+                                       unsigned int *vBCType, unsigned int **vInterfaces,
+                                       double **vMatParam, double *vProbParam, double **mA,
+                                       double **mBC, double *vB)
+{
+    return electric_form(3, 1, mNodes, mElems, vBCType, vInterfaces, vMatParam, vProbParam, mA, mBC, vB);
+}
+
+extern "C" int electricFormFullA_tria6(double **mNodes, unsigned int **mElems,
+                                       unsigned int *vBCType, unsigned int **vInterfaces,
+                                       double **vMatParam, double *vProbParam, double **mA,
+                                       double **mBC, double *vB)
+{
+    return electric_form(6, 1, mNodes, mElems, vBCType, vInterfaces, vMatParam, vProbParam, mA, mBC, vB);
+}
+
+extern "C" int gaussBksb(unsigned int N, double **A, double *B)
+{
+    std::lock_guard<std::mutex> lk(ctx().mu);
+    int bad = -1;
+    int rc = gauss_impl(N, A, nullptr, 0, B, &bad);
+    if (rc == kErrSingular) {
+        // the reference's message and exit (src/gaussBksb.c:68-69)
+        printf("\nSingularity in row %d in system matrix", bad);
+        exit(1);
+    }
+    check_or_die(rc);
+    return 0;
+}
+
+extern "C" void solverGMRES_el(unsigned int preCond, unsigned int nInit, double **A, double *B)
+{
+    std::lock_guard<std::mutex> lk(ctx().mu);
+    const unsigned N = nNodes;
+    std::vector<double> x0;
+    if (nInit != 0) {
+        // initial guess (src/gmres_el.c:80-84)
+        x0.assign(2 * (size_t)N, 0.0);
+        FILE *fin = fopen("solution.init", "r");
+        if (!fin) fatal("Can't open solution.init");
+        for (unsigned i = 0; i < nInit && i < 2 * N; i++)
+            if (fscanf(fin, "%le", &x0[i]) != 1) break;
+        fclose(fin);
+    }
+    FILE *fg = fopen("gmres.log", "w");
+    unsigned iters = 0;
+    int rc = gmres_impl(N, preCond, 1.0E-6, 600, A, nullptr, 0, B, x0.empty() ? nullptr : x0.data(),
+                        fg, &iters);
+    if (rc == kErrNoConverge) {
+        if (fg) fclose(fg);
+        fatal("Linear system may be ill-conditioned");
+    }
+    if (rc == kErrStagnation) {
+        if (fg) fclose(fg);
+        fatal("CONVERGENCE RATE TOO SLOW");
+    }
+    check_or_die(rc);
+    if (fg) fclose(fg);
+}
+
+static int field_dropin(int nen, int field, double *Xin, double **mNodes, unsigned **mElems,
+                        double *vB, double *out)
+{
+    std::lock_guard<std::mutex> lk(ctx().mu);
+    FlatMesh f;
+    flatten(nen, (int)nNodes, (int)nElems, mNodes, mElems, f);
+    check_or_die(points_impl(nen, nNodes, nElems, f.nodes.data(), f.elems0.data(), vB, 1, Xin, field, out));
+    return 0;
+}
+
+extern "C" int field_tria3(double *Xin, double **mNodes, unsigned int **mElems, double *vB, double *mE)
+{
+    return field_dropin(3, 1, Xin, mNodes, mElems, vB, mE);
+}
+
+extern "C" int field_tria6(double *Xin, double **mNodes, unsigned int **mElems, double *vB, double *mE)
+{
+    return field_dropin(6, 1, Xin, mNodes, mElems, vB, mE);
+}
+
+extern "C" int potential_tria3(double *Xin, double **mNodes, unsigned int **mElems, double *vB,
+                               double *mPot)
+{
+    return field_dropin(3, 0, Xin, mNodes, mElems, vB, mPot);
+}
+
+extern "C" int potential_tria6(double *Xin, double **mNodes, unsigned int **mElems, double *vB,
+                               double *mPot)
+{
+    return field_dropin(6, 0, Xin, mNodes, mElems, vB, mPot);
+}
+
+static int force_dropin(int nen, double **mNodes, unsigned **mElems, unsigned *vBCType, double *vB,
+                        double Eps, double **Fce, double **Xce, double *Fcm, double *Xcm)
+{
+    std::lock_guard<std::mutex> lk(ctx().mu);
+    const unsigned N = nNodes, E = nElems;
+    FlatMesh f;
+    flatten(nen, (int)N, (int)E, mNodes, mElems, f);
+    std::vector<double> fce((size_t)E * 3, NAN), xce((size_t)E * 3, NAN);
+    check_or_die(force_impl(nen, N, E, f.nodes.data(), f.elems0.data(), vBCType, vB, Eps, fce.data(),
+                            xce.data(), Fcm, Xcm));
+    for (unsigned e = 0; e < E; e++) {
+        if (vBCType[mElems[e][0] - 1] != 6) continue;
+        for (int d = 0; d < 3; d++) {
+            Fce[e][d] = fce[3 * (size_t)e + d];
+            Xce[e][d] = xce[3 * (size_t)e + d];
+        }
+    }
+    return 0;
+}
+
+extern "C" int forceMST_tria3(double **mNodes, unsigned int **mElems, unsigned int *vBCType,
+                              double *vB, double Eps, double **Fce, double **Xce, double *Fcm,
+                              double *Xcm)
+{
+    return force_dropin(3, mNodes, mElems, vBCType, vB, Eps, Fce, Xce, Fcm, Xcm);
+}
+
+extern "C" int forceMST_tria6(double **mNodes, unsigned int **mElems, unsigned int *vBCType,
+                              double *vB, double Eps, double **Fce, double **Xce, double *Fcm,
+                              double *Xcm)
+{
+    return force_dropin(6, mNodes, mElems, vBCType, vB, Eps, Fce, Xce, Fcm, Xcm);
+}
+
+// ================================================================ dsc_ API
+
+extern "C" const char *dsc_last_error(void) { return last_error(); }
+
+extern "C" int dsc_device_count(void)
+{
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+extern "C" int dsc_assemble(int nen, int full, unsigned N, unsigned E, unsigned nIf,
+                            const double *nodes, const unsigned *elems, const unsigned *bctype,
+                            const unsigned *ifaces, const double *mat, double freq,
+                            const double *mbc, double *A, size_t lda, double *B)
+{
+    std::lock_guard<std::mutex> lk(ctx().mu);
+    if ((nen != 3 && nen != 6) || !nodes || !elems || !bctype || !mbc || !A || !B ||
+        lda < 2 * (size_t)N) {
+        set_error("dsc_assemble: bad arguments");
+        return kErrArg;
+    }
+    std::vector<int> e0;
+    elems_to0(nen, (int)E, elems, e0);
+    FlatSink sink{A, lda};
+    DSC_TRY(assemble_impl(nen, full, N, E, nIf, nodes, e0.data(), bctype, ifaces, mat, freq, mbc,
+                          add_to_flat, &sink));
+    for (unsigned i = 0; i < N; i++) {
+        B[i] = mbc[3 * (size_t)i];
+        B[i + N] = mbc[3 * (size_t)(i + N)];
+    }
+    return kOk;
+}
+
+extern "C" int dsc_gauss(unsigned n, const double *A, size_t lda, double *B)
+{
+    std::lock_guard<std::mutex> lk(ctx().mu);
+    if (!A || !B || lda < n || n == 0) {
+        set_error("dsc_gauss: bad arguments");
+        return kErrArg;
+    }
+    int bad = -1;
+    return gauss_impl(n, nullptr, A, lda, B, &bad);
+}
+
+extern "C" int dsc_gmres(unsigned N, unsigned preCond, double tol, unsigned max_iters,
+                         const double *A, size_t lda, double *B, const double *x0,
+                         const char *log_path, unsigned *iters)
+{
+    std::lock_guard<std::mutex> lk(ctx().mu);
+    if (!A || !B || lda < 2 * (size_t)N || N == 0 || max_iters == 0) {
+        set_error("dsc_gmres: bad arguments");
+        return kErrArg;
+    }
+    FILE *log = log_path ? fopen(log_path, "w") : nullptr;
+    int rc = gmres_impl(N, preCond, tol, max_iters, nullptr, A, lda, B, x0, log, iters);
+    if (log) fclose(log);
+    return rc;
+}
+
+extern "C" int dsc_field_points(int nen, unsigned N, unsigned E, const double *nodes,
+                                const unsigned *elems, const double *vB, unsigned npts,
+                                const double *pts, double *mE)
+{
+    std::lock_guard<std::mutex> lk(ctx().mu);
+    std::vector<int> e0;
+    elems_to0(nen, (int)E, elems, e0);
+    return points_impl(nen, N, E, nodes, e0.data(), vB, npts, pts, 1, mE);
+}
+
+extern "C" int dsc_potential_points(int nen, unsigned N, unsigned E, const double *nodes,
+                                    const unsigned *elems, const double *vB, unsigned npts,
+                                    const double *pts, double *mPot)
+{
+    std::lock_guard<std::mutex> lk(ctx().mu);
+    std::vector<int> e0;
+    elems_to0(nen, (int)E, elems, e0);
+    return points_impl(nen, N, E, nodes, e0.data(), vB, npts, pts, 0, mPot);
+}
+
+extern "C" int dsc_force_mst(int nen, unsigned N, unsigned E, const double *nodes,
+                             const unsigned *elems, const unsigned *bctype, const double *vB,
+                             double eps, double *Fce, double *Xce, double *Fcm, double *Xcm)
+{
+    std::lock_guard<std::mutex> lk(ctx().mu);
+    std::vector<int> e0;
+    elems_to0(nen, (int)E, elems, e0);
+    return force_impl(nen, N, E, nodes, e0.data(), bctype, vB, eps, Fce, Xce, Fcm, Xcm);
+}

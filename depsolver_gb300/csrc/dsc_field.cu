@@ -1,0 +1,521 @@
+// dsc_field.cu -- potential, field and Maxwell-stress force from the nodal
+// surface charge (field_tria*, potential_tria* src/field.c:57-200,
+// src/potential.c:55-179; forceMST_tria* src/force.c:348-552 with intF_*
+// src/forceIntegrals.c:632-723).
+//
+// Regular pairs: the 7 quadrature points of every element carry their
+// charge weights c_q = w_q J_q sum_k N_k(q) sigma_k (Re and Im), so a
+// (point, element) pair costs 7 kernel evaluations and no shape functions.
+// Two layouts: thread per point over a chunk of elements staged in shared
+// memory (many points), or thread per element with a block reduction (a
+// handful of points).  Partial sums per element chunk are reduced in chunk
+// order, so results do not depend on scheduling.
+// Singular pairs (the point coincides with a node of the element, by exact
+// coordinate equality as the reference tests it) use the FP64 subdivision
+// rule, one warp per point, plus the reference's jump term: once per such
+// element, sigma/(2 eps0) of the element's FIRST node times the averaged
+// normal of the coincident node (src/field.c:171-195), kept for parity.
+#include <math.h>
+
+#include <algorithm>
+
+#include "dsc_common.cuh"
+#include "dsc_field.h"
+#include "dsc_internal.h"
+#include "dsc_singular.cuh"
+
+namespace dsc {
+
+constexpr int kFieldChunk = 64;  // elements per chunk
+
+// Charge-weighted quadrature points: cq[(e*7+q)*5 + {x,y,z,re,im}].
+template <int NEN>
+__global__ void k_charge_qp(const double *__restrict__ X, const double *__restrict__ Y,
+                            const double *__restrict__ Z, const int *__restrict__ elems, int E, int N,
+                            const double *__restrict__ sigma, double *__restrict__ cq)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= E * kTriPts) return;
+    int e = t / kTriPts, q = t % kTriPts;
+    double Xe[NEN][3], N6[NEN], XL[3];
+    double sr = 0.0, si = 0.0;
+    double l1 = c_tri7[q][0], l2 = c_tri7[q][1];
+    shape<NEN>(l1, l2, N6);
+#pragma unroll
+    for (int k = 0; k < NEN; k++) {
+        int v = elems[(size_t)e * NEN + k];
+        Xe[k][0] = X[v];
+        Xe[k][1] = Y[v];
+        Xe[k][2] = Z[v];
+        sr += N6[k] * sigma[v];
+        si += N6[k] * sigma[v + N];
+    }
+    double J = map_point<NEN>(Xe, l1, l2, N6, XL);
+    double w = c_tri7[q][2] * J;
+    double *o = cq + (size_t)t * 5;
+    o[0] = XL[0];
+    o[1] = XL[1];
+    o[2] = XL[2];
+    o[3] = w * sr;
+    o[4] = w * si;
+}
+
+struct PointArgs {
+    const double *px, *py, *pz;   // points
+    const int4 *coinc;            // up to 4 coincident node ids per point (-1 pad)
+    int P;
+    const int *elems;
+    const double *cq;
+    int E;
+};
+
+template <int NEN>
+__device__ __forceinline__ bool is_singular(const int *en, int4 c)
+{
+    bool s = false;
+#pragma unroll
+    for (int k = 0; k < NEN; k++)
+        s |= (en[k] == c.x) | (en[k] == c.y) | (en[k] == c.z) | (en[k] == c.w);
+    return s && c.x >= 0;
+}
+
+// FIELD = 1: out has 6 values per point (Re/Im of E x, y, z without the
+// 1/(4 pi eps0) factor); FIELD = 0: 2 values (Re/Im potential).
+template <int NEN, int FIELD>
+__global__ void __launch_bounds__(128) k_point_regular(PointArgs a, double *__restrict__ part)
+{
+    constexpr int NV = FIELD ? 6 : 2;
+    __shared__ double s_cq[kFieldChunk * kTriPts * 5];
+    __shared__ int s_en[kFieldChunk * NEN];
+    const int chunk = blockIdx.y;
+    const int e0 = chunk * kFieldChunk;
+    const int ne = min(kFieldChunk, a.E - e0);
+    for (int t = threadIdx.x; t < ne * kTriPts * 5; t += blockDim.x)
+        s_cq[t] = a.cq[(size_t)e0 * kTriPts * 5 + t];
+    for (int t = threadIdx.x; t < ne * NEN; t += blockDim.x) s_en[t] = a.elems[(size_t)e0 * NEN + t];
+    __syncthreads();
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= a.P) return;
+    const double x = a.px[p], y = a.py[p], z = a.pz[p];
+    const int4 c = a.coinc[p];
+    double acc[NV];
+#pragma unroll
+    for (int v = 0; v < NV; v++) acc[v] = 0.0;
+    for (int e = 0; e < ne; e++) {
+        if (is_singular<NEN>(s_en + e * NEN, c)) continue;
+        const double *Q = s_cq + e * kTriPts * 5;
+#pragma unroll
+        for (int q = 0; q < kTriPts; q++) {
+            double dx = x - Q[q * 5], dy = y - Q[q * 5 + 1], dz = z - Q[q * 5 + 2];
+            double inv = rsqrt(dx * dx + dy * dy + dz * dz);
+            if (FIELD) {
+                double i3 = inv * inv * inv;
+                double gr = Q[q * 5 + 3] * i3, gi = Q[q * 5 + 4] * i3;
+                acc[0] += gr * dx; acc[1] += gi * dx;
+                acc[2] += gr * dy; acc[3] += gi * dy;
+                acc[4] += gr * dz; acc[5] += gi * dz;
+            } else {
+                acc[0] += Q[q * 5 + 3] * inv;
+                acc[1] += Q[q * 5 + 4] * inv;
+            }
+        }
+    }
+    double *o = part + ((size_t)chunk * a.P + p) * NV;
+#pragma unroll
+    for (int v = 0; v < NV; v++) o[v] = acc[v];
+}
+
+// Few points: thread per element, block reduction per point.
+template <int NEN, int FIELD>
+__global__ void __launch_bounds__(128) k_point_regular_few(PointArgs a, double *__restrict__ part)
+{
+    constexpr int NV = FIELD ? 6 : 2;
+    __shared__ double sh[32];
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int p = 0; p < a.P; p++) {
+        double acc[NV];
+#pragma unroll
+        for (int v = 0; v < NV; v++) acc[v] = 0.0;
+        if (e < a.E && !is_singular<NEN>(a.elems + (size_t)e * NEN, a.coinc[p])) {
+            const double x = a.px[p], y = a.py[p], z = a.pz[p];
+            const double *Q = a.cq + (size_t)e * kTriPts * 5;
+#pragma unroll
+            for (int q = 0; q < kTriPts; q++) {
+                double dx = x - Q[q * 5], dy = y - Q[q * 5 + 1], dz = z - Q[q * 5 + 2];
+                double inv = rsqrt(dx * dx + dy * dy + dz * dz);
+                if (FIELD) {
+                    double i3 = inv * inv * inv;
+                    double gr = Q[q * 5 + 3] * i3, gi = Q[q * 5 + 4] * i3;
+                    acc[0] += gr * dx; acc[1] += gi * dx;
+                    acc[2] += gr * dy; acc[3] += gi * dy;
+                    acc[4] += gr * dz; acc[5] += gi * dz;
+                } else {
+                    acc[0] += Q[q * 5 + 3] * inv;
+                    acc[1] += Q[q * 5 + 4] * inv;
+                }
+            }
+        }
+#pragma unroll
+        for (int v = 0; v < NV; v++) {
+            double s = warp_sum(acc[v]);
+            const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+            if (lane == 0) sh[w] = s;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                double t = 0.0;
+                for (int u = 0; u < (int)(blockDim.x >> 5); u++) t += sh[u];
+                part[((size_t)blockIdx.x * a.P + p) * NV + v] = t;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// Singular pairs of each point: tuples (element, local position s of the
+// coincident node, node whose averaged normal is used), in element order.
+template <int NEN, int FIELD>
+__global__ void __launch_bounds__(128) k_point_singular(
+    PointArgs a, const double *__restrict__ X, const double *__restrict__ Y,
+    const double *__restrict__ Z, const double *__restrict__ normals, int N,
+    const double *__restrict__ sigma, const int *__restrict__ sp_ptr, const int4 *__restrict__ sp,
+    double *__restrict__ out)
+{
+    constexpr int NV = FIELD ? 6 : 2;
+    const int p = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (p >= a.P) return;
+    const double xe[3] = {a.px[p], a.py[p], a.pz[p]};
+    // field: (0.5/eps0)/(2 pi) as src/field.c:149-150; potential:
+    // 1/(4 pi eps0) as src/potential.c:138
+    const double A = FIELD ? 0.5 / kEps0 / kPi2 : 1.0 / (kPi4 * kEps0), B = 0.5 / kEps0;
+    double acc[NV];
+#pragma unroll
+    for (int v = 0; v < NV; v++) acc[v] = 0.0;
+    for (int t = sp_ptr[p]; t < sp_ptr[p + 1]; t++) {
+        const int4 tu = sp[t];  // x: element, y: position (1-based), z: normal node
+        const int e = tu.x, s = tu.y;
+        double Xe[NEN][3];
+        int nodes[NEN];
+#pragma unroll
+        for (int k = 0; k < NEN; k++) {
+            int v = a.elems[(size_t)e * NEN + k];
+            nodes[k] = v;
+            Xe[k][0] = X[v];
+            Xe[k][1] = Y[v];
+            Xe[k][2] = Z[v];
+        }
+        if (FIELD) {
+            double n[3] = {normals[3 * (size_t)tu.z], normals[3 * (size_t)tu.z + 1],
+                           normals[3 * (size_t)tu.z + 2]};
+            double sub[3 * NEN];
+            warp_singular_H<NEN, 1>(s, Xe, xe, n, sub);
+#pragma unroll
+            for (int k = 0; k < NEN; k++) {
+                const double sr = sigma[nodes[k]], si = sigma[nodes[k] + N];
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    acc[2 * c] += A * sub[3 * k + c] * sr;
+                    acc[2 * c + 1] += A * sub[3 * k + c] * si;
+                }
+            }
+            const double sr0 = sigma[nodes[0]], si0 = sigma[nodes[0] + N];
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                acc[2 * c] += B * sr0 * n[c];
+                acc[2 * c + 1] += B * si0 * n[c];
+            }
+        } else {
+            double sub[NEN];
+            warp_singular_G<NEN>(s, Xe, xe, sub);
+#pragma unroll
+            for (int k = 0; k < NEN; k++) {
+                acc[0] += A * sub[k] * sigma[nodes[k]];
+                acc[1] += A * sub[k] * sigma[nodes[k] + N];
+            }
+        }
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int v = 0; v < NV; v++) out[(size_t)p * NV + v] = acc[v];
+    }
+}
+
+// result[p] = 1/(4 pi eps0) * sum_chunks part + singular part.
+template <int NV>
+__global__ void k_point_reduce(const double *__restrict__ part, int nchunk, int P,
+                               const double *__restrict__ sing, double *__restrict__ out)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= P * NV) return;
+    const double A = NV == 6 ? 0.5 / kEps0 / kPi2 : 1.0 / (kPi4 * kEps0);
+    double s = 0.0;
+    for (int c = 0; c < nchunk; c++) s += part[(size_t)c * P * NV + t];
+    out[t] = A * s + sing[t];
+}
+
+// Maxwell stress on the particle elements (first node of type 6):
+// Fce = eps/2 * int [E (E.n) - |E|^2 n / 2] dS with Re(E) interpolated from
+// the nodes, Xce = X(1/4, 1/4).
+template <int NEN>
+__global__ void k_mst(const double *__restrict__ X, const double *__restrict__ Y,
+                      const double *__restrict__ Z, const int *__restrict__ elems,
+                      const int *__restrict__ pel, int npel, const double *__restrict__ Enode,
+                      double eps, double *__restrict__ Fce, double *__restrict__ Xce)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= npel) return;
+    const int e = pel[t];
+    double Xe[NEN][3], En[NEN][3], N6[NEN], XL[3], n[3];
+#pragma unroll
+    for (int k = 0; k < NEN; k++) {
+        int v = elems[(size_t)e * NEN + k];
+        Xe[k][0] = X[v];
+        Xe[k][1] = Y[v];
+        Xe[k][2] = Z[v];
+        En[k][0] = Enode[3 * (size_t)v];
+        En[k][1] = Enode[3 * (size_t)v + 1];
+        En[k][2] = Enode[3 * (size_t)v + 2];
+    }
+    double I0 = 0.0, I1 = 0.0, I2 = 0.0;
+    for (int q = 0; q < kTriPts; q++) {
+        double l1 = c_tri7[q][0], l2 = c_tri7[q][1];
+        shape<NEN>(l1, l2, N6);
+        double J = map_point<NEN>(Xe, l1, l2, N6, XL);
+        local_normal<NEN>(Xe, l1, l2, n);
+        double Ex = 0.0, Ey = 0.0, Ez = 0.0;
+#pragma unroll
+        for (int k = 0; k < NEN; k++) {
+            Ex += En[k][0] * N6[k];
+            Ey += En[k][1] * N6[k];
+            Ez += En[k][2] * N6[k];
+        }
+        double NE = Ex * n[0] + Ey * n[1] + Ez * n[2];
+        double Esq = Ex * Ex + Ey * Ey + Ez * Ez;
+        double A = J * c_tri7[q][2];
+        I0 += A * (Ex * NE - 0.5 * Esq * n[0]);
+        I1 += A * (Ey * NE - 0.5 * Esq * n[1]);
+        I2 += A * (Ez * NE - 0.5 * Esq * n[2]);
+    }
+    const double A = 0.5 * eps;
+    Fce[3 * (size_t)t] = A * I0;
+    Fce[3 * (size_t)t + 1] = A * I1;
+    Fce[3 * (size_t)t + 2] = A * I2;
+    shape<NEN>(0.25, 0.25, N6);
+    map_point<NEN>(Xe, 0.25, 0.25, N6, XL);
+    Xce[3 * (size_t)t] = XL[0];
+    Xce[3 * (size_t)t + 1] = XL[1];
+    Xce[3 * (size_t)t + 2] = XL[2];
+}
+
+// Scatter Re(E) of each particle node into a node-indexed array.
+__global__ void k_scatter_re(const double *__restrict__ Ept, const int *__restrict__ ids, int P,
+                             double *__restrict__ Enode)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    const int v = ids[p];
+    Enode[3 * (size_t)v] = Ept[6 * (size_t)p];
+    Enode[3 * (size_t)v + 1] = Ept[6 * (size_t)p + 2];
+    Enode[3 * (size_t)v + 2] = Ept[6 * (size_t)p + 4];
+}
+
+// Totals: Fcm = sum Fce, Xcm = mean of the particle nodes (one warp,
+// lane-strided sums and a tree reduction: a fixed order).
+__global__ void k_mst_totals(const double *__restrict__ Fce, int npel, const double *__restrict__ X,
+                             const double *__restrict__ Y, const double *__restrict__ Z,
+                             const int *__restrict__ ids, int P, double *__restrict__ tot)
+{
+    const int lane = threadIdx.x;
+    double f[3] = {0, 0, 0}, x[3] = {0, 0, 0};
+    for (int t = lane; t < npel; t += 32)
+        for (int d = 0; d < 3; d++) f[d] += Fce[3 * (size_t)t + d];
+    for (int p = lane; p < P; p += 32) {
+        x[0] += X[ids[p]];
+        x[1] += Y[ids[p]];
+        x[2] += Z[ids[p]];
+    }
+    for (int d = 0; d < 3; d++) {
+        f[d] = warp_sum(f[d]);
+        x[d] = warp_sum(x[d]);
+    }
+    if (lane == 0) {
+        for (int d = 0; d < 3; d++) {
+            tot[d] = f[d];
+            tot[3 + d] = x[d] / P;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ host
+
+int PointSet::build(const HostPlan &plan, int P, const double *pts)
+{
+    this->P = P;
+    std::vector<double> xs(P), ys(P), zs(P);
+    std::vector<int4> co(P, make_int4(-1, -1, -1, -1));
+    std::vector<int> ptr(1, 0);
+    std::vector<int4> tup;
+    const int nen = plan.nen;
+    // exact-coordinate lookup of mesh nodes
+    for (int p = 0; p < P; p++) {
+        xs[p] = pts[3 * p];
+        ys[p] = pts[3 * p + 1];
+        zs[p] = pts[3 * p + 2];
+        auto it = plan_coords_find(plan, xs[p], ys[p], zs[p]);
+        int nco = 0;
+        int ids[4] = {-1, -1, -1, -1};
+        for (int v : it) {
+            if (nco == 4) {
+                set_error("more than 4 mesh nodes share the coordinates of point %d", p);
+                return kErrArg;
+            }
+            ids[nco++] = v;
+        }
+        co[p] = make_int4(ids[0], ids[1], ids[2], ids[3]);
+        // singular elements of this point, element order, first matching
+        // position within the element (src/field.c:164-173)
+        if (nco > 0) {
+            std::vector<int> cand;
+            for (int u = 0; u < nco; u++)
+                for (int t = plan.ne_ptr[ids[u]]; t < plan.ne_ptr[ids[u] + 1]; t++)
+                    cand.push_back(plan.ne_elem[t]);
+            std::sort(cand.begin(), cand.end());
+            cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
+            for (int e : cand) {
+                for (int k = 0; k < nen; k++) {
+                    int v = plan.elems[(size_t)e * nen + k];
+                    if (plan.nodes[3 * (size_t)v] == xs[p] && plan.nodes[3 * (size_t)v + 1] == ys[p] &&
+                        plan.nodes[3 * (size_t)v + 2] == zs[p]) {
+                        tup.push_back(make_int4(e, k + 1, v, 0));
+                        break;
+                    }
+                }
+            }
+        }
+        ptr.push_back((int)tup.size());
+    }
+    cudaStream_t st = 0;
+    DSC_TRY(px.upload(xs, st));
+    DSC_TRY(py.upload(ys, st));
+    DSC_TRY(pz.upload(zs, st));
+    DSC_TRY(coinc.upload(co, st));
+    DSC_TRY(sp_ptr.upload(ptr, st));
+    if (tup.empty()) tup.push_back(make_int4(0, 0, 0, 0));
+    DSC_TRY(sp.upload(tup, st));
+    DSC_CUDA(cudaStreamSynchronize(st));
+    return kOk;
+}
+
+template <int NEN>
+static int eval_points_impl(const DeviceMesh &m, const PointSet &ps, const double *dsigma,
+                            int field, double *dout, cudaStream_t st)
+{
+    const int NV = field ? 6 : 2;
+    DevBuf<double> cq, part, sing;
+    DSC_TRY(cq.alloc((size_t)m.E * kTriPts * 5));
+    k_charge_qp<NEN><<<(m.E * kTriPts + 255) / 256, 256, 0, st>>>(m.x.p, m.y.p, m.z.p, m.elems.p, m.E,
+                                                                    m.N, dsigma, cq.p);
+    PointArgs a{ps.px.p, ps.py.p, ps.pz.p, ps.coinc.p, ps.P, m.elems.p, cq.p, m.E};
+    int nchunk;
+    if (ps.P >= 64) {
+        nchunk = (m.E + kFieldChunk - 1) / kFieldChunk;
+        DSC_TRY(part.alloc((size_t)nchunk * ps.P * NV));
+        dim3 g((ps.P + 127) / 128, nchunk);
+        if (field) k_point_regular<NEN, 1><<<g, 128, 0, st>>>(a, part.p);
+        else k_point_regular<NEN, 0><<<g, 128, 0, st>>>(a, part.p);
+    } else {
+        nchunk = (m.E + 127) / 128;
+        DSC_TRY(part.alloc((size_t)nchunk * ps.P * NV));
+        if (field) k_point_regular_few<NEN, 1><<<nchunk, 128, 0, st>>>(a, part.p);
+        else k_point_regular_few<NEN, 0><<<nchunk, 128, 0, st>>>(a, part.p);
+    }
+    DSC_CUDA(cudaGetLastError());
+    DSC_TRY(sing.alloc((size_t)ps.P * NV));
+    const int sblocks = (ps.P * 32 + 127) / 128;
+    if (field)
+        k_point_singular<NEN, 1><<<sblocks, 128, 0, st>>>(a, m.x.p, m.y.p, m.z.p, m.normals.p, m.N,
+                                                          dsigma, ps.sp_ptr.p, ps.sp.p, sing.p);
+    else
+        k_point_singular<NEN, 0><<<sblocks, 128, 0, st>>>(a, m.x.p, m.y.p, m.z.p, m.normals.p, m.N,
+                                                          dsigma, ps.sp_ptr.p, ps.sp.p, sing.p);
+    DSC_CUDA(cudaGetLastError());
+    if (field) k_point_reduce<6><<<(ps.P * 6 + 255) / 256, 256, 0, st>>>(part.p, nchunk, ps.P, sing.p, dout);
+    else k_point_reduce<2><<<(ps.P * 2 + 255) / 256, 256, 0, st>>>(part.p, nchunk, ps.P, sing.p, dout);
+    DSC_CUDA(cudaGetLastError());
+    DSC_CUDA(cudaStreamSynchronize(st));
+    return kOk;
+}
+
+int eval_points(const DeviceMesh &m, const PointSet &ps, const double *dsigma, int field,
+                double *dout, cudaStream_t st)
+{
+    return m.nen == 6 ? eval_points_impl<6>(m, ps, dsigma, field, dout, st)
+                      : eval_points_impl<3>(m, ps, dsigma, field, dout, st);
+}
+
+int force_mst(const DeviceMesh &m, const HostPlan &plan, const unsigned *bctype,
+              const double *dsigma, double eps, double *Fce_host /*E x 3, may be null*/,
+              double *Xce_host, double *Fcm, double *Xcm, cudaStream_t st)
+{
+    std::vector<int> ids, pel;
+    std::vector<double> pts;
+    for (int i = 0; i < m.N; i++)
+        if (bctype[i] == 6) {
+            ids.push_back(i);
+            pts.push_back(plan.nodes[3 * (size_t)i]);
+            pts.push_back(plan.nodes[3 * (size_t)i + 1]);
+            pts.push_back(plan.nodes[3 * (size_t)i + 2]);
+        }
+    for (int e = 0; e < m.E; e++)
+        if (bctype[plan.elems[(size_t)e * m.nen]] == 6) pel.push_back(e);
+    const int P = (int)ids.size(), npel = (int)pel.size();
+    if (P == 0) {
+        // the reference divides by a zero count here; report zeros
+        for (int d = 0; d < 3; d++) Fcm[d] = Xcm[d] = 0.0;
+        return kOk;
+    }
+    PointSet ps;
+    DSC_TRY(ps.build(plan, P, pts.data()));
+    DevBuf<double> Ept, Enode, Fce, Xce, tot;
+    DevBuf<int> dids, dpel;
+    DSC_TRY(Ept.alloc((size_t)P * 6));
+    DSC_TRY(eval_points(m, ps, dsigma, 1, Ept.p, st));
+    DSC_TRY(Enode.alloc((size_t)m.N * 3));
+    DSC_CUDA(cudaMemsetAsync(Enode.p, 0, (size_t)m.N * 3 * sizeof(double), st));
+    DSC_TRY(dids.upload(ids, st));
+    DSC_TRY(dpel.upload(pel.empty() ? std::vector<int>{0} : pel, st));
+    k_scatter_re<<<(P + 255) / 256, 256, 0, st>>>(Ept.p, dids.p, P, Enode.p);
+    DSC_TRY(Fce.alloc((size_t)std::max(npel, 1) * 3));
+    DSC_TRY(Xce.alloc((size_t)std::max(npel, 1) * 3));
+    DSC_TRY(tot.alloc(6));
+    if (npel > 0) {
+        if (m.nen == 6)
+            k_mst<6><<<(npel + 127) / 128, 128, 0, st>>>(m.x.p, m.y.p, m.z.p, m.elems.p, dpel.p, npel,
+                                                         Enode.p, eps, Fce.p, Xce.p);
+        else
+            k_mst<3><<<(npel + 127) / 128, 128, 0, st>>>(m.x.p, m.y.p, m.z.p, m.elems.p, dpel.p, npel,
+                                                         Enode.p, eps, Fce.p, Xce.p);
+    }
+    k_mst_totals<<<1, 32, 0, st>>>(Fce.p, npel, m.x.p, m.y.p, m.z.p, dids.p, P, tot.p);
+    DSC_CUDA(cudaGetLastError());
+    double h[6];
+    DSC_CUDA(cudaMemcpyAsync(h, tot.p, sizeof h, cudaMemcpyDeviceToHost, st));
+    std::vector<double> f((size_t)npel * 3), x((size_t)npel * 3);
+    if (npel > 0 && (Fce_host || Xce_host)) {
+        DSC_CUDA(cudaMemcpyAsync(f.data(), Fce.p, f.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+        DSC_CUDA(cudaMemcpyAsync(x.data(), Xce.p, x.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    }
+    DSC_CUDA(cudaStreamSynchronize(st));
+    for (int d = 0; d < 3; d++) {
+        Fcm[d] = h[d];
+        Xcm[d] = h[3 + d];
+    }
+    for (int t = 0; t < npel; t++)
+        for (int d = 0; d < 3; d++) {
+            if (Fce_host) Fce_host[3 * (size_t)pel[t] + d] = f[3 * (size_t)t + d];
+            if (Xce_host) Xce_host[3 * (size_t)pel[t] + d] = x[3 * (size_t)t + d];
+        }
+    return kOk;
+}
+
+}  // namespace dsc

@@ -1,0 +1,23 @@
+// dsc_gmres.h -- solver entry points inside libdepsolver_cuda (not exported).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdio.h>
+
+namespace dsc {
+
+// Reference-faithful FP64 GMRES on the compact form (device A, N x 2N with
+// row stride lda, scaled in place when preCond == 1; device B overwritten
+// with the solution on success).  log (may be null) receives gmres.log.
+int gmres_compact_fp64(int N, double *dA, size_t lda, double *dB, const double *dx0,
+                       unsigned preCond, double tol_rel, unsigned max_iters, FILE *log,
+                       unsigned *iters, cudaStream_t st);
+
+// Un-pivoted blocked LU solve of a dense row-major FP64 system on the
+// device.  dA is n x (n + 1) with stride lda >= n + 1 and the right-hand
+// side in column n; on success column n holds the solution.  A pivot within
+// 1e-9 of zero stops the solve with kErrSingular (*bad_row receives it).
+int lu_solve_augmented_fp64(int n, double *dA, size_t lda, int *bad_row, cudaStream_t st);
+int lu_extract_solution(int n, const double *dA, size_t lda, double *dB, cudaStream_t st);
+
+}  // namespace dsc

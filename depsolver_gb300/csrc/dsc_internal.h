@@ -1,0 +1,145 @@
+// dsc_internal.h -- host-side structures of libdepsolver_cuda (not exported).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+namespace dsc {
+
+// ---------------------------------------------------------------- errors
+enum Status {
+    kOk = 0,
+    kErrCuda = 1,
+    kErrArg = 2,
+    kErrBcType = 3,      // boundary type the assembly does not define
+    kErrSingular = 4,    // pivot within 1e-9 of zero
+    kErrNoConverge = 5,  // GMRES hit its iteration cap
+    kErrStagnation = 6,  // "CONVERGENCE RATE TOO SLOW"
+    kErrMemory = 7,
+};
+
+void set_error(const char *fmt, ...);
+const char *last_error();
+
+#define DSC_CUDA(call)                                                                       \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess) {                                                             \
+            ::dsc::set_error("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_)); \
+            return ::dsc::kErrCuda;                                                          \
+        }                                                                                    \
+    } while (0)
+
+#define DSC_TRY(call)                     \
+    do {                                  \
+        int s_ = (call);                  \
+        if (s_ != ::dsc::kOk) return s_;  \
+    } while (0)
+
+// ---------------------------------------------------------------- buffers
+template <typename T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    int alloc(size_t count)
+    {
+        if (count <= n && p) return kOk;
+        release();
+        if (count == 0) count = 1;
+        if (cudaMalloc(&p, count * sizeof(T)) != cudaSuccess) {
+            cudaGetLastError();
+            set_error("cudaMalloc of %zu bytes failed", count * sizeof(T));
+            return kErrMemory;
+        }
+        n = count;
+        return kOk;
+    }
+    int upload(const T *h, size_t count, cudaStream_t st)
+    {
+        DSC_TRY(alloc(count));
+        DSC_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, st));
+        return kOk;
+    }
+    int upload(const std::vector<T> &v, cudaStream_t st) { return upload(v.data(), v.size(), st); }
+};
+
+// ---------------------------------------------------------------- mesh plan
+// Element groups: elements in Morton order of their centroids, cut into
+// groups of kGroup.  A group's footprint is the set of nodes its elements
+// touch; a footprint node that no other group touches is written straight
+// into K, the others go to partial-sum slots that a fix-up pass adds in
+// group order.
+constexpr int kGroup = 32;   // elements per group
+constexpr int kRowTile = 32; // collocation rows per assembly CTA
+
+struct HostPlan {
+    int nen = 6, N = 0, E = 0;
+    std::vector<double> nodes;    // N x 3
+    std::vector<int> elems;       // E x nen, 0-based
+    std::vector<int> row_kind;    // N: 0 conductor (G), 1 interface (H)
+    std::vector<double> row_fac;  // N: C for G rows, -1 for H rows
+    std::vector<double> normals;  // N x 3 averaged node normals
+    int G = 0;
+    std::vector<int> grp_elem;    // G x kGroup, -1 padded
+    std::vector<int> fp_ptr;      // G + 1
+    std::vector<int> fp_dest;     // >= 0: K column; < 0: -(slot + 1)
+    std::vector<int> fp_sl_ptr;   // entries + 1
+    std::vector<uint16_t> fp_sl;  // local slot e * nen + k
+    int n_slots = 0;
+    int max_fp = 0;
+    std::vector<int> fix_ptr, fix_slot, fix_col;  // boundary nodes
+    std::vector<int> ne_ptr, ne_elem, ne_pos;     // node -> (element, position)
+    std::vector<int> coord_order;                 // node ids sorted by (x, y, z)
+};
+
+// Builds everything above from 0-based connectivity; bctype (may be null)
+// has N entries (the real-equation rows).  Fails on boundary types other
+// than 0, 1, 6.
+int build_plan(int nen, int N, int E, const double *nodes, const int *elems0,
+               const unsigned *bctype, HostPlan &plan);
+int set_rows(HostPlan &plan, const unsigned *bctype);
+
+// Averaged node normals in element order (reference src/normals.c:120-319).
+void node_normals(int nen, int N, int E, const double *nodes, const int *elems0, double *out);
+
+// Interface coefficients (reference src/assembly_el.c:223-239).
+void interface_coeffs(unsigned nIf, const unsigned *ifaces, const double *mat, double freq,
+                      double *Ak, double *Bk);
+
+// Device copy of a plan plus the element quadrature data.
+struct DeviceMesh {
+    int nen = 6, N = 0, E = 0, G = 0, n_slots = 0, n_fix = 0;
+    DevBuf<double> x, y, z;        // node coordinates (SoA)
+    DevBuf<int> elems;             // E x nen
+    DevBuf<int> row_kind;
+    DevBuf<double> row_fac, normals;
+    DevBuf<int> grp_elem, fp_ptr, fp_dest, fp_sl_ptr;
+    DevBuf<uint16_t> fp_sl;
+    DevBuf<int> fix_ptr, fix_slot, fix_col;
+    DevBuf<int> ne_ptr, ne_elem, ne_pos;
+    DevBuf<double> qp;             // E x 7 x 4: x, y, z, w * J
+    int upload(const HostPlan &p, cudaStream_t st);
+    int upload_rows(const HostPlan &p, cudaStream_t st);
+};
+
+// K (N x N, column-major, leading dimension ld): K[c * ld + i] is the
+// geometric integral of row i against node c: C * int G N_c for conductor
+// rows, int H N_c (normal derivative, sign as the reference) for interface
+// rows.  The frequency enters only through per-row coefficients.
+int assemble_K_fp64(const DeviceMesh &m, double *K, size_t ld, cudaStream_t st);
+int assemble_K_fp32(const DeviceMesh &m, float *K, size_t ld, cudaStream_t st);
+
+}  // namespace dsc

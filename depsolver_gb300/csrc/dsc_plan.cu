@@ -1,0 +1,321 @@
+// dsc_plan.cu -- host-side mesh planning for the assembly kernels.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <numeric>
+
+#include "dsc_common.cuh"
+#include "dsc_field.h"
+#include "dsc_internal.h"
+
+namespace dsc {
+
+static thread_local char g_err[512];
+
+void set_error(const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof g_err, fmt, ap);
+    va_end(ap);
+}
+
+const char *last_error() { return g_err; }
+
+// Local coordinates of node position p of a tria6 (src/normals.c:240-264);
+// a tria3 normal is constant over the element.
+static const double kTria6NodeL[6][2] = {{1.0, 0.0}, {0.5, 0.5}, {0.0, 1.0},
+                                         {0.0, 0.5}, {0.0, 0.0}, {0.5, 0.0}};
+
+// One pass over the elements in order adds each element's unit normal at
+// the node's local position to the node's sum -- the same additions, in the
+// same order, as the reference's per-node scan (getNormal_tria6
+// src/normals.c:207-319) -- then normalises.
+void node_normals(int nen, int N, int E, const double *nodes, const int *el, double *out)
+{
+    std::vector<double> acc((size_t)N * 3, 0.0);
+    double X[6][3], n[3];
+    for (int e = 0; e < E; e++) {
+        const int *en = el + (size_t)e * nen;
+        for (int k = 0; k < nen; k++)
+            for (int d = 0; d < 3; d++) X[k][d] = nodes[3 * (size_t)en[k] + d];
+        for (int k = 0; k < nen; k++) {
+            bool first = true;
+            for (int j = 0; j < k; j++)
+                if (en[j] == en[k]) first = false;
+            if (!first) continue;
+            if (nen == 6) local_normal<6>(X, kTria6NodeL[k][0], kTria6NodeL[k][1], n);
+            else local_normal<3>(X, 0.0, 0.0, n);
+            double *a = &acc[3 * (size_t)en[k]];
+            a[0] += n[0];
+            a[1] += n[1];
+            a[2] += n[2];
+        }
+    }
+    for (int i = 0; i < N; i++) {
+        const double *a = &acc[3 * (size_t)i];
+        double inv = 1.0 / sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+        out[3 * (size_t)i + 0] = a[0] * inv;
+        out[3 * (size_t)i + 1] = a[1] * inv;
+        out[3 * (size_t)i + 2] = a[2] * inv;
+    }
+}
+
+void interface_coeffs(unsigned nIf, const unsigned *ifaces, const double *mat, double freq,
+                      double *Ak, double *Bk)
+{
+    const double C = 1.0 / (kPi4 * kEps0);
+    const double W = freq * kPi2 * kEps0;
+    for (unsigned i = 0; i < nIf; i++) {
+        unsigned m1 = ifaces[2 * i] - 1, m2 = ifaces[2 * i + 1] - 1;
+        double sigTot = mat[2 * m1] + mat[2 * m2];
+        double sigDif = mat[2 * m1] - mat[2 * m2];
+        double epsTot = W * (mat[2 * m1 + 1] + mat[2 * m2 + 1]);
+        double epsDif = W * (mat[2 * m1 + 1] - mat[2 * m2 + 1]);
+        double D = C / (sigTot * sigTot + epsTot * epsTot);
+        Ak[i] = D * (sigTot * sigDif + epsTot * epsDif);
+        Bk[i] = D * (sigDif * epsTot - sigTot * epsDif);
+    }
+}
+
+static uint64_t spread3(uint64_t v)
+{
+    v &= 0x1fffff;
+    v = (v | v << 32) & 0x1f00000000ffffULL;
+    v = (v | v << 16) & 0x1f0000ff0000ffULL;
+    v = (v | v << 8) & 0x100f00f00f00f00fULL;
+    v = (v | v << 4) & 0x10c30c30c30c30c3ULL;
+    v = (v | v << 2) & 0x1249249249249249ULL;
+    return v;
+}
+
+int set_rows(HostPlan &p, const unsigned *bctype)
+{
+    const double C = 1.0 / (kPi4 * kEps0);
+    p.row_kind.resize(p.N);
+    p.row_fac.resize(p.N);
+    for (int i = 0; i < p.N; i++) {
+        unsigned t = bctype[i];
+        if (t == 1) { p.row_kind[i] = 0; p.row_fac[i] = C; }
+        else if (t == 0 || t == 6) { p.row_kind[i] = 1; p.row_fac[i] = -1.0; }
+        else {
+            set_error("node %d has boundary type %u; the assembly defines only 0, 1 and 6", i + 1, t);
+            return kErrBcType;
+        }
+    }
+    return kOk;
+}
+
+int build_plan(int nen, int N, int E, const double *nodes, const int *el,
+               const unsigned *bctype, HostPlan &p)
+{
+    if ((nen != 3 && nen != 6) || N <= 0 || E <= 0) {
+        set_error("bad mesh sizes (nen %d, N %d, E %d)", nen, N, E);
+        return kErrArg;
+    }
+    for (size_t t = 0; t < (size_t)E * nen; t++)
+        if (el[t] < 0 || el[t] >= N) {
+            set_error("element %zu references node %d outside 1..%d", t / nen, el[t] + 1, N);
+            return kErrArg;
+        }
+    p.nen = nen;
+    p.N = N;
+    p.E = E;
+    p.nodes.assign(nodes, nodes + (size_t)N * 3);
+    p.elems.assign(el, el + (size_t)E * nen);
+    p.row_kind.assign(N, 1);
+    p.row_fac.assign(N, -1.0);
+    if (bctype) DSC_TRY(set_rows(p, bctype));
+    p.normals.resize((size_t)N * 3);
+    node_normals(nen, N, E, nodes, el, p.normals.data());
+
+    // Morton order of element centroids.
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int i = 0; i < N; i++)
+        for (int d = 0; d < 3; d++) {
+            lo[d] = std::min(lo[d], nodes[3 * (size_t)i + d]);
+            hi[d] = std::max(hi[d], nodes[3 * (size_t)i + d]);
+        }
+    std::vector<uint64_t> code(E);
+    for (int e = 0; e < E; e++) {
+        uint64_t c = 0;
+        for (int d = 0; d < 3; d++) {
+            double s = 0.0;
+            for (int k = 0; k < nen; k++) s += nodes[3 * (size_t)el[(size_t)e * nen + k] + d];
+            s /= nen;
+            double span = hi[d] - lo[d];
+            double f = span > 0 ? (s - lo[d]) / span : 0.0;
+            uint64_t q = (uint64_t)std::min(2097151.0, std::max(0.0, f * 2097151.0));
+            c |= spread3(q) << d;
+        }
+        code[e] = c;
+    }
+    std::vector<int> order(E);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return code[a] < code[b]; });
+
+    p.G = (E + kGroup - 1) / kGroup;
+    p.grp_elem.assign((size_t)p.G * kGroup, -1);
+    for (int t = 0; t < E; t++) p.grp_elem[t] = order[t];
+
+    // Footprints: (node, slot) pairs of each group sorted by node.
+    std::vector<std::vector<std::pair<int, int>>> fps(p.G);
+    std::vector<int> ngroups(N, 0), lastg(N, -1);
+    for (int g = 0; g < p.G; g++) {
+        auto &f = fps[g];
+        for (int j = 0; j < kGroup; j++) {
+            int e = p.grp_elem[(size_t)g * kGroup + j];
+            if (e < 0) continue;
+            for (int k = 0; k < nen; k++) f.push_back({el[(size_t)e * nen + k], j * nen + k});
+        }
+        std::sort(f.begin(), f.end());
+        for (size_t t = 0; t < f.size(); t++) {
+            int v = f[t].first;
+            if (lastg[v] != g) {
+                lastg[v] = g;
+                ngroups[v]++;
+            }
+        }
+    }
+    std::vector<std::vector<int>> node_slots(N);
+    p.fp_ptr.assign(1, 0);
+    p.fp_dest.clear();
+    p.fp_sl_ptr.assign(1, 0);
+    p.fp_sl.clear();
+    p.n_slots = 0;
+    p.max_fp = 0;
+    for (int g = 0; g < p.G; g++) {
+        auto &f = fps[g];
+        int nfp = 0;
+        for (size_t t = 0; t < f.size();) {
+            int v = f[t].first;
+            size_t u = t;
+            while (u < f.size() && f[u].first == v) p.fp_sl.push_back((uint16_t)f[u++].second);
+            if (ngroups[v] == 1) p.fp_dest.push_back(v);
+            else {
+                node_slots[v].push_back(p.n_slots);
+                p.fp_dest.push_back(-(p.n_slots + 1));
+                p.n_slots++;
+            }
+            p.fp_sl_ptr.push_back((int)p.fp_sl.size());
+            nfp++;
+            t = u;
+        }
+        p.max_fp = std::max(p.max_fp, nfp);
+        p.fp_ptr.push_back((int)p.fp_dest.size());
+    }
+    p.fix_ptr.assign(1, 0);
+    p.fix_slot.clear();
+    p.fix_col.clear();
+    for (int v = 0; v < N; v++) {
+        if (ngroups[v] == 1) continue;
+        p.fix_col.push_back(v);
+        for (int s : node_slots[v]) p.fix_slot.push_back(s);
+        p.fix_ptr.push_back((int)p.fix_slot.size());
+    }
+    // node -> elements containing it, element order, first position
+    std::vector<int> cnt(N + 1, 0);
+    for (int e = 0; e < E; e++)
+        for (int k = 0; k < nen; k++) {
+            int v = el[(size_t)e * nen + k];
+            bool first = true;
+            for (int j = 0; j < k; j++)
+                if (el[(size_t)e * nen + j] == v) first = false;
+            if (first) cnt[v + 1]++;
+        }
+    for (int i = 0; i < N; i++) cnt[i + 1] += cnt[i];
+    p.ne_ptr = cnt;
+    p.ne_elem.assign(cnt[N], 0);
+    p.ne_pos.assign(cnt[N], 0);
+    std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+    for (int e = 0; e < E; e++)
+        for (int k = 0; k < nen; k++) {
+            int v = el[(size_t)e * nen + k];
+            bool first = true;
+            for (int j = 0; j < k; j++)
+                if (el[(size_t)e * nen + j] == v) first = false;
+            if (!first) continue;
+            p.ne_elem[fill[v]] = e;
+            p.ne_pos[fill[v]] = k;
+            fill[v]++;
+        }
+    p.coord_order.resize(N);
+    std::iota(p.coord_order.begin(), p.coord_order.end(), 0);
+    std::stable_sort(p.coord_order.begin(), p.coord_order.end(), [&](int a, int b) {
+        const double *u = &p.nodes[3 * (size_t)a], *v = &p.nodes[3 * (size_t)b];
+        if (u[0] != v[0]) return u[0] < v[0];
+        if (u[1] != v[1]) return u[1] < v[1];
+        return u[2] < v[2];
+    });
+    return kOk;
+}
+
+std::vector<int> plan_coords_find(const HostPlan &p, double x, double y, double z)
+{
+    const double key[3] = {x, y, z};
+    auto less = [&](const double *u, const double *v) {
+        if (u[0] != v[0]) return u[0] < v[0];
+        if (u[1] != v[1]) return u[1] < v[1];
+        return u[2] < v[2];
+    };
+    auto lo = std::lower_bound(p.coord_order.begin(), p.coord_order.end(), 0,
+                               [&](int a, int) { return less(&p.nodes[3 * (size_t)a], key); });
+    std::vector<int> out;
+    for (auto it = lo; it != p.coord_order.end(); ++it) {
+        const double *u = &p.nodes[3 * (size_t)*it];
+        if (u[0] == x && u[1] == y && u[2] == z) out.push_back(*it);
+        else break;
+    }
+    std::sort(out.begin(), out.end());
+    return out;
+}
+
+int DeviceMesh::upload_rows(const HostPlan &p, cudaStream_t st)
+{
+    DSC_TRY(row_kind.upload(p.row_kind, st));
+    DSC_TRY(row_fac.upload(p.row_fac, st));
+    DSC_CUDA(cudaStreamSynchronize(st));
+    return kOk;
+}
+
+int DeviceMesh::upload(const HostPlan &p, cudaStream_t st)
+{
+    nen = p.nen;
+    N = p.N;
+    E = p.E;
+    G = p.G;
+    n_slots = p.n_slots;
+    n_fix = (int)p.fix_col.size();
+    std::vector<double> xs(N), ys(N), zs(N);
+    for (int i = 0; i < N; i++) {
+        xs[i] = p.nodes[3 * (size_t)i];
+        ys[i] = p.nodes[3 * (size_t)i + 1];
+        zs[i] = p.nodes[3 * (size_t)i + 2];
+    }
+    DSC_TRY(x.upload(xs, st));
+    DSC_TRY(y.upload(ys, st));
+    DSC_TRY(z.upload(zs, st));
+    DSC_TRY(elems.upload(p.elems, st));
+    DSC_TRY(upload_rows(p, st));
+    DSC_TRY(normals.upload(p.normals, st));
+    DSC_TRY(grp_elem.upload(p.grp_elem, st));
+    DSC_TRY(fp_ptr.upload(p.fp_ptr, st));
+    DSC_TRY(fp_dest.upload(p.fp_dest, st));
+    DSC_TRY(fp_sl_ptr.upload(p.fp_sl_ptr, st));
+    DSC_TRY(fp_sl.upload(p.fp_sl, st));
+    DSC_TRY(fix_ptr.upload(p.fix_ptr, st));
+    DSC_TRY(fix_slot.upload(p.fix_slot.empty() ? std::vector<int>{0} : p.fix_slot, st));
+    DSC_TRY(fix_col.upload(p.fix_col.empty() ? std::vector<int>{0} : p.fix_col, st));
+    DSC_TRY(ne_ptr.upload(p.ne_ptr, st));
+    DSC_TRY(ne_elem.upload(p.ne_elem, st));
+    DSC_TRY(ne_pos.upload(p.ne_pos, st));
+    DSC_TRY(qp.alloc((size_t)E * kTriPts * 4));
+    // host vectors go out of scope: wait for the copies
+    DSC_CUDA(cudaStreamSynchronize(st));
+    return kOk;
+}
+
+}  // namespace dsc

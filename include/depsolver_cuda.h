@@ -1,0 +1,147 @@
+/*
+ * depsolver_cuda.h -- C ABI of libdepsolver_cuda, the GB300 (sm_103a)
+ * implementation of depSolver's boundary-element hot path.
+ *
+ * Two layers:
+ *
+ *  1. Drop-in entry points with the reference's exact names, signatures and
+ *     error behaviour.  A depSolver build links libdepsolver_cuda.so in place
+ *     of assembly_el.o, kernelIntegrals.o, gaussBksb.o, gmres_el.o, field.o,
+ *     potential.o, force.o (MST part) and forceIntegrals.o; the driver, input
+ *     parsing, normals and post-processing stay the reference's C code and
+ *     input decks and output files are unchanged.  Like the reference they
+ *     read the globals nNodes, nElems and nInterfaces and report fatal
+ *     errors on stderr and in bem.log before exit(1).
+ *
+ *  2. dsc_* entry points on flat row-major arrays that return a status
+ *     code (0 = success, see dsc_last_error()) instead of exiting.  Meshes
+ *     are passed as in the reference's input files: elems are 1-based node
+ *     ids, bctype and mbc have 2N rows.
+ *
+ * No torch or CUDA types appear in any signature.
+ */
+#ifndef DEPSOLVER_CUDA_H
+#define DEPSOLVER_CUDA_H
+
+#include <stddef.h>
+#include <stdio.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ globals
+ * Read by the drop-in entry points exactly where the reference reads them
+ * (defined in src/depSolver.c:46-50).  The library carries its own
+ * definitions; when linked into the depSolver executable, the executable's
+ * definitions take precedence. */
+extern unsigned int nNodes, nElems, nInterfaces;
+extern FILE *file_log;
+
+/* --------------------------------------------------------- drop-in: assembly
+ * Replace src/assembly_el.c:63 / :197 / :329 / :470 (declared in
+ * src/assembly_el.h:29-67).  Compact form (electricFormA_*): mA has nNodes
+ * rows of 2*nNodes; full form (electricFormFullA_*): 2*nNodes rows.  The
+ * assembled values are ADDED to mA (the reference accumulates into a
+ * zeroed matrix); vB receives the boundary values.  Boundary types other
+ * than 0, 1 and 6 (which the reference assembles with stale interface data)
+ * are reported as a fatal error. */
+int electricFormA_tria3(double **mNodes, unsigned int **mElems, unsigned int *vBCType,
+                        unsigned int **vInterfaces, double **vMatParam, double *vProbParam,
+                        double **mA, double **mBC, double *vB);
+int electricFormA_tria6(double **mNodes, unsigned int **mElems, unsigned int *vBCType,
+                        unsigned int **vInterfaces, double **vMatParam, double *vProbParam,
+                        double **mA, double **mBC, double *vB);
+int electricFormFullA_tria3(double **mNodes, unsigned int **mElems, unsigned int *vBCType,
+                            unsigned int **vInterfaces, double **vMatParam, double *vProbParam,
+                            double **mA, double **mBC, double *vB);
+int electricFormFullA_tria6(double **mNodes, unsigned int **mElems, unsigned int *vBCType,
+                            unsigned int **vInterfaces, double **vMatParam, double *vProbParam,
+                            double **mA, double **mBC, double *vB);
+
+/* ----------------------------------------------------------- drop-in: solve
+ * gaussBksb replaces src/gaussBksb.c:39 (src/gaussBksb.h:29): N x N system,
+ * solution returned in B.  A's contents after the call are unspecified (the
+ * reference leaves its eliminated matrix there; no caller reads it).
+ * solverGMRES_el replaces src/gmres_el.c:66 (src/gmres_el.h:29): compact
+ * nNodes x 2nNodes system, Jacobi scaling when preCond == 1, initial guess
+ * from solution.init when nInit != 0, gmres.log written in the working
+ * directory in the reference's format, solution returned in B. */
+int gaussBksb(unsigned int N, double **A, double *B);
+void solverGMRES_el(unsigned int preCond, unsigned int nInit, double **A, double *B);
+
+/* ---------------------------------------------------- drop-in: post-process
+ * field_* replace src/field.c:57 / :137 (src/field.h:30-41):
+ *   mE = {Re Ex, Im Ex, Re Ey, Im Ey, Re Ez, Im Ez} at Xin.
+ * potential_* replace src/potential.c:55 / :126 (src/potential.h:29-40):
+ *   mPot = {Re, Im}.
+ * forceMST_* replace src/force.c:348 / :463 (src/force.h:54-73): Maxwell
+ * stress force on the elements whose first node has boundary type 6
+ * (rows of Fce / Xce written for those elements only), total Fcm and the
+ * mean Xcm of the type-6 nodes. */
+int field_tria3(double *Xin, double **mNodes, unsigned int **mElems, double *vB, double *mE);
+int field_tria6(double *Xin, double **mNodes, unsigned int **mElems, double *vB, double *mE);
+int potential_tria3(double *Xin, double **mNodes, unsigned int **mElems, double *vB, double *mPot);
+int potential_tria6(double *Xin, double **mNodes, unsigned int **mElems, double *vB, double *mPot);
+int forceMST_tria3(double **mNodes, unsigned int **mElems, unsigned int *vBCType, double *vB,
+                   double Eps, double **Fce, double **Xce, double *Fcm, double *Xcm);
+int forceMST_tria6(double **mNodes, unsigned int **mElems, unsigned int *vBCType, double *vB,
+                   double Eps, double **Fce, double **Xce, double *Fcm, double *Xcm);
+
+/* ------------------------------------------------------------ flat dsc_ API */
+
+/* Status codes. */
+#define DSC_OK 0
+#define DSC_ERR_CUDA 1
+#define DSC_ERR_ARG 2
+#define DSC_ERR_BCTYPE 3
+#define DSC_ERR_SINGULAR 4
+#define DSC_ERR_NOCONVERGE 5
+#define DSC_ERR_STAGNATION 6
+#define DSC_ERR_MEMORY 7
+
+/* Message of the last failure on this thread. */
+const char *dsc_last_error(void);
+
+/* Number of CUDA devices visible (0 when none; no error). */
+int dsc_device_count(void);
+
+/* Flat form of electricFormA_* (full = 0; A is N x 2N) and
+ * electricFormFullA_* (full = 1; A is 2N x 2N); rows of A are lda doubles
+ * apart and receive A += assembled values; B (2N) = boundary values.
+ * nen = 3 or 6; elems 1-based (E x nen); bctype 2N; ifaces nIf x 2; mat
+ * has at least max(ifaces) rows of (sigma, eps_r); mbc 2N x 3. */
+int dsc_assemble(int nen, int full, unsigned N, unsigned E, unsigned nIf, const double *nodes,
+                 const unsigned *elems, const unsigned *bctype, const unsigned *ifaces,
+                 const double *mat, double freq, const double *mbc, double *A, size_t lda,
+                 double *B);
+
+/* Flat form of gaussBksb: row-major n x n (stride lda), B overwritten with
+ * the solution; A is left unchanged. */
+int dsc_gauss(unsigned n, const double *A, size_t lda, double *B);
+
+/* Flat form of solverGMRES_el with the tolerance (relative to |B|, the
+ * reference compiles 1e-6) and the iteration cap (600) as arguments.
+ * A (N x 2N, stride lda) is left unchanged; B is overwritten with the
+ * solution on success; x0 (2N) may be NULL; log_path may be NULL (no log);
+ * *iters receives the iteration count. */
+int dsc_gmres(unsigned N, unsigned preCond, double tol, unsigned max_iters, const double *A,
+              size_t lda, double *B, const double *x0, const char *log_path, unsigned *iters);
+
+/* Field (mE: npts x 6) or potential (mPot: npts x 2) at npts points
+ * (pts: npts x 3), from the nodal solution vB (2N). */
+int dsc_field_points(int nen, unsigned N, unsigned E, const double *nodes, const unsigned *elems,
+                     const double *vB, unsigned npts, const double *pts, double *mE);
+int dsc_potential_points(int nen, unsigned N, unsigned E, const double *nodes,
+                         const unsigned *elems, const double *vB, unsigned npts,
+                         const double *pts, double *mPot);
+
+/* Flat form of forceMST_*: Fce, Xce are E x 3 (may be NULL). */
+int dsc_force_mst(int nen, unsigned N, unsigned E, const double *nodes, const unsigned *elems,
+                  const unsigned *bctype, const double *vB, double eps, double *Fce, double *Xce,
+                  double *Fcm, double *Xcm);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

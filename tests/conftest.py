@@ -1,0 +1,58 @@
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+REFERENCE = os.environ.get("DSC_REFERENCE", "/root/reference")
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA device (GB300, sm_103a)")
+
+
+@pytest.fixture(scope="session")
+def port():
+    from oracle.checker import Port, build_port
+    build_port()
+    return Port()
+
+
+@pytest.fixture(scope="session")
+def ref():
+    from oracle import checker
+    if checker.build_ref() is None:
+        pytest.skip("reference sources not present")
+    return checker.Ref()
+
+
+@pytest.fixture(scope="session")
+def native():
+    """The CUDA library; built if missing.  Never a fallback."""
+    from depsolver_gb300 import _native, build
+    if not os.path.exists(_native.LIB_PATH):
+        build.build()
+    return _native.lib()
+
+
+@pytest.fixture(scope="session")
+def gpu(native):
+    if native.dsc_device_count() < 1:
+        pytest.skip("no CUDA device")
+    return native
+
+
+def golden(name):
+    return np.load(os.path.join(GOLDEN, name), allow_pickle=False)
+
+
+def relerr(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    scale = np.abs(b).max()
+    return float(np.abs(a - b).max() / (scale if scale > 0 else 1.0))

@@ -1,0 +1,38 @@
+"""The C ABI: the library loads, exports every function and global that
+include/depsolver_cuda.h declares, and has no CPU fallback (without a GPU
+every compute entry point fails with a CUDA status)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from depsolver_gb300 import _native, scenes
+
+
+def test_exports_every_declared_symbol(native):
+    names = _native.declared_symbols()
+    assert "electricFormA_tria6" in names and "solverGMRES_el" in names and "dsc_assemble" in names
+    missing = [n for n in names if not hasattr(native, n)]
+    assert not missing, missing
+    for g in _native.declared_globals():
+        C.c_uint.in_dll(native, g) if g != "file_log" else C.c_void_p.in_dll(native, g)
+
+
+def test_header_matches_reference_dropin_set():
+    """Every hot-path entry point of the reference has a drop-in."""
+    expected = {
+        "electricFormA_tria3", "electricFormA_tria6", "electricFormFullA_tria3",
+        "electricFormFullA_tria6", "gaussBksb", "solverGMRES_el", "field_tria3", "field_tria6",
+        "potential_tria3", "potential_tria6", "forceMST_tria3", "forceMST_tria6",
+    }
+    assert expected <= set(_native.declared_symbols())
+
+
+def test_no_cpu_fallback_without_device(native):
+    if native.dsc_device_count() > 0:
+        pytest.skip("a device is present")
+    from depsolver_gb300 import api
+    sc = scenes.small(nen=3)
+    with pytest.raises(_native.DscError) as ei:
+        api.electric_form(sc)
+    assert ei.value.status == 1 and "device" in str(ei.value)
