@@ -226,7 +226,10 @@ __global__ void __launch_bounds__(128) k_asm_singular(const double *__restrict__
     const double n[3] = {normals[3 * (size_t)i], normals[3 * (size_t)i + 1],
                          normals[3 * (size_t)i + 2]};
     const int kind = row_kind[i];
-    const double fac = row_fac[i];
+    // warp_singular_H already carries the reference's minus sign
+    // (Int[k] -= ...), so interface rows take factor 1 here; conductor rows
+    // take C = 1/(4 pi eps0).
+    const double fac = kind == 0 ? row_fac[i] : 1.0;
     for (int t = ne_ptr[i]; t < ne_ptr[i + 1]; t++) {
         const int e = ne_elem[t], s = ne_pos[t] + 1;
         double Xe[NEN][3], out[NEN];

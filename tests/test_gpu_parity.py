@@ -129,9 +129,15 @@ def test_pure_conductor_scene(gpu, port):
     A, B = api.electric_form(sc)
     Ap, Bp = port.assemble(sc)
     assert relerr(A, Ap) < ASM_TOL
-    x, it = api.solver_gmres_el(A, B)
-    xp, itp, _ = port.gmres(Ap, Bp)
-    assert it == itp and relerr(x, xp) < SOL_TOL
+    # At the compiled 1e-6 tolerance this scene converges on a tie: the
+    # checker's residual at step 11 is within 9% of the tolerance and a
+    # different summation order stops one step earlier, so compare the
+    # tight-tolerance and direct solutions instead.
+    x, it = api.solver_gmres_el(A, B, tol=1e-12)
+    xp, itp, _ = port.gmres(Ap, Bp, tol=1e-12)
+    assert abs(it - itp) <= 1 and relerr(x, xp) < SOL_TOL
+    Af, Bf = api.electric_form(sc, full=True)
+    assert relerr(api.gauss_bksb(Af, Bf), xp) < 1e-9
 
 
 def test_errors_are_reported_not_faked(gpu):
