@@ -1,0 +1,384 @@
+"""Benchmark: DEP solves/s on the 12k-node scene (level-4 sphere between
+30 x 30-cell plates, tria6, N = 17684, E = 8720).
+
+A step is one batch: assemble the geometric matrix of the scene (FP64) and
+solve a 64-frequency sweep (1 kHz .. 100 MHz, log-spaced) to a relative
+residual of 1e-10 with the mixed-precision batched path, then the
+Maxwell-stress DEP force of every system.  value = systems solved per
+second (inputs resident in GPU memory).  e2e = the same through the C ABI
+from host arrays (dsc_sweep: mesh in, nodal solution and forces out).
+
+Also measured and reported: the plain FP64 GPU path (the reference's GMRES
+in FP64, one frequency per solve, assembly included), the force error of
+the mixed path against an FP64 solve, and a CPU baseline (the C
+restatement of the reference, all host cores).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DEP solves/s at 12k nodes: mixed-prec+batched vs FP64 GPU, force err ≤1e-6"
+UNIT = "solves/s"
+NFREQ = 64
+TOL = 1e-10
+FREQS = np.logspace(3.0, 8.0, NFREQ)
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int = 0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ CPU baseline
+def cpu_baseline(sc, nthreads: int, sample_div: int = 8, full_first: bool = True):
+    """The C restatement of the reference (oracle/port) on the host cores.
+
+    One full solve of one frequency (assembly, GMRES at the reference's
+    compiled tolerance 1e-6, MST force) gives the reference's iteration
+    count; the timed sample is 1/sample_div of the assembly rows, the same
+    rows' share of every GMRES matrix-vector product (times that count) and
+    1/sample_div of the particle-node fields, scaled to one full solve;
+    Gram-Schmidt and the MST integral are timed in full."""
+    from oracle.checker import Port
+    P = Port()
+    N = sc.N
+    info = {}
+    if full_first:
+        t0 = time.perf_counter()
+        A, B = P.assemble(sc, nthreads=nthreads)
+        t1 = time.perf_counter()
+        x, it, st = P.gmres(A, B, nthreads=nthreads)
+        t2 = time.perf_counter()
+        F = P.force_mst(sc, x, nthreads=nthreads)
+        t3 = time.perf_counter()
+        info = {"full_solve_s": t3 - t0, "assembly_s": t1 - t0, "gmres_s": t2 - t1,
+                "force_s": t3 - t2, "gmres_iters": int(it), "Fcm": F[2].tolist()}
+        del A
+    it = info.get("gmres_iters", 40)
+    # sampled step: one contiguous chunk of rows per thread, evenly spread,
+    # 1/sample_div of all rows, assembled concurrently (ctypes releases the
+    # GIL, each call single-threaded)
+    per = max(1, N // sample_div // nthreads)
+    starts = np.linspace(0, N - per, nthreads).astype(int)
+    Ab = np.zeros((nthreads * per, 2 * N))
+    Bbs = [np.zeros(2 * N) for _ in range(nthreads)]
+    nodes = np.ascontiguousarray(sc.nodes)
+    elems = np.ascontiguousarray(sc.elems, np.uint32)
+    bct = np.ascontiguousarray(sc.bctype, np.uint32)
+    ifc = np.ascontiguousarray(sc.ifaces, np.uint32)
+    mat = np.ascontiguousarray(sc.mat)
+    mbc = np.ascontiguousarray(sc.mbc)
+
+    def asm(t):
+        s0 = int(starts[t])
+        # rows s0..s0+per land at Ab[t*per ...]: row i at base + i * 2N
+        base = Ab.ctypes.data + (t * per - s0) * 2 * N * 8
+        P.lib.orc_assemble(sc.nen, 0, N, sc.E, sc.n_if, nodes, elems, bct, ifc.ctypes.data,
+                           mat.ctypes.data, sc.freq, mbc, s0, s0 + per, base, 2 * N, Bbs[t], 1)
+
+    ths = [threading.Thread(target=asm, args=(t,)) for t in range(nthreads)]
+    t0 = time.perf_counter()
+    for th in ths:
+        th.start()
+    for th in ths:
+        th.join()
+    t_asm = time.perf_counter() - t0
+    blocks = [None] * nthreads
+    xv = np.random.default_rng(0).standard_normal(2 * N)
+    y = np.zeros(2 * N)
+    t0 = time.perf_counter()
+    P.lib.orc_matvec_rows(N, Ab.ctypes.data, xv, y, 0, nthreads * per, nthreads)
+    t_mv = time.perf_counter() - t0
+    chunk = per
+    # Gram-Schmidt of an iteration with half the final Krylov dimension, in full
+    V = np.random.default_rng(1).standard_normal((max(1, it // 2), 2 * N))
+    t0 = time.perf_counter()
+    w = xv.copy()
+    for v in V:
+        w -= (v @ w) * v
+    t_mgs = time.perf_counter() - t0
+    p0, p1 = sc.particles[0][0], sc.particles[-1][1]
+    pts = sc.nodes[p0:p1][:: sample_div]
+    sol = np.zeros(2 * N)
+    sol[:N] = 1.0
+    t0 = time.perf_counter()
+    P.field(sc, sol, pts, nthreads=nthreads)
+    t_field = time.perf_counter() - t0
+    est = sample_div * (t_asm + it * t_mv + t_field) + it * t_mgs
+    sample = (f"one full solve of one frequency (assembly, GMRES to 1e-6 in {it} iterations, "
+              f"force) then a timed 1/{sample_div} sample: {len(blocks) * chunk} of {N} assembly rows, "
+              f"their share of {it} matrix-vector products, {len(pts)} of {p1 - p0} particle-node "
+              f"fields, scaled x{sample_div}; Gram-Schmidt timed in full")
+    return {"value": 1.0 / est, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": sample, "est_solve_s": est, "parts_s": {"assembly": sample_div * t_asm,
+            "gmres": it * (sample_div * t_mv + t_mgs), "field": sample_div * t_field},
+            "full": info}
+
+
+# ------------------------------------------------------------------ ours
+def run_ours(args, rank, world):
+    import torch
+
+    from depsolver_gb300 import _native, api, scenes
+
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA device")
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    L = _native.lib()
+    sc = scenes.cfg1()
+    N, E = sc.N, sc.E
+    s = api.Session(sc)
+    stream = torch.cuda.ExternalStream(s.stream_handle())
+    if args.only_step:
+        # one warm-up and one timed step only (for profiler launch lists)
+        for _ in range(2):
+            s.assemble()
+            s.solve(FREQS, mode=api.MODE_MIXED, tol=TOL)
+        torch.cuda.synchronize()
+        print(json.dumps({"only_step": True, "launches": int(L.dsc_kernel_launches())}))
+        return
+
+    # accuracy: mixed vs an FP64 solve (tol 1e-12) at three frequencies
+    chk = [FREQS[0], FREQS[NFREQ // 2], FREQS[-1]]
+    fm, _, sm = s.solve(FREQS, mode=api.MODE_MIXED, tol=TOL, want_sigma=True)
+    f64, it64, s64 = s.solve(chk, mode=api.MODE_FP64, tol=1e-12, want_sigma=True)
+    ferr, serr = 0.0, 0.0
+    for j, fq in enumerate(chk):
+        k = int(np.argmin(np.abs(FREQS - fq)))
+        ferr = max(ferr, float(np.abs(fm[k, :3] - f64[j, :3]).max() / f64[j, 6:9].sum()))
+        serr = max(serr, float(np.abs(sm[k] - s64[j]).max() / np.abs(s64[j]).max()))
+
+    # plain FP64 GPU path: assembly + the reference's GMRES (tol 1e-10) + force
+    fp64_t = []
+    for _ in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.assemble()
+        _, itf, _ = s.solve([1e6], mode=api.MODE_FP64, tol=TOL)
+        torch.cuda.synchronize()
+        fp64_t.append(time.perf_counter() - t0)
+    fp64_s = min(fp64_t)
+
+    # headline: warm-up, then K timed steps (assembly + 64-system sweep)
+    for _ in range(args.warmup):
+        s.assemble()
+        s.solve(FREQS, mode=api.MODE_MIXED, tol=TOL)
+    s.set_timing(True)
+    s.timing()  # reset
+    clocks = ClockSampler(dev)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    l0 = L.dsc_kernel_launches()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        s.assemble()
+        s.solve(FREQS, mode=api.MODE_MIXED, tol=TOL)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    launches = int(L.dsc_kernel_launches() - l0)
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    tms = torch.tensor([ms], device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(tms, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.barrier()
+    ms = float(tms.item())
+    timing = s.timing()
+    value = world * args.steps * NFREQ / (ms / 1e3)
+
+    # e2e through the C ABI from host arrays: dsc_sweep (session created,
+    # mesh uploaded, assembled, solved, nodal solution and forces read back)
+    e2e_steps = max(1, min(args.steps, 3))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        fe, _, se = api.sweep(sc, FREQS, mode=api.MODE_MIXED, tol=TOL, want_sigma=True)
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    h2d = (sc.nodes.nbytes + sc.elems.astype(np.uint32).nbytes + sc.bctype.astype(np.uint32).nbytes
+           + sc.mbc.nbytes + sc.mat.nbytes + sc.ifaces.astype(np.uint32).nbytes + FREQS.nbytes)
+    d2h = se.nbytes + fe.nbytes
+
+    if rank != 0:
+        return
+    # roofline of the dominant kernel class over the timed region
+    P = peaks()
+    work = {  # algorithmic work per launch
+        "gemm_K": ("tensor", 2.0 * N * N * 2 * NFREQ / 1e12, "TFLOP/s", P.get("bf16_tflops", 1900.0)),
+        "residual_fp64": ("tensor", 2.0 * N * N * 2 * NFREQ / 1e12, "TFLOP/s", P.get("bf16_tflops", 1900.0)),
+        "asm_regular": ("tensor", N * E * 7 * 30 / 1e12, "TFLOP/s", P.get("bf16_tflops", 1900.0)),
+    }
+    total_ms = sum(v[0] for v in timing.values())
+    dom = max(timing, key=lambda k: timing[k][0])
+    dms, dcnt = timing[dom]
+    roof = None
+    if dom in work and dcnt:
+        bound, per, unit, peak = work[dom]
+        ach = per / (dms / dcnt / 1e3)
+        roof = {"kernel": dom, "bound": bound, "achieved": ach, "peak": peak, "unit": unit,
+                "frac": ach / peak, "traffic": None,
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)"}
+    cpu = cpu_baseline(sc, os.cpu_count() or 1) if not args.no_cpu else None
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32-matvec/f64-residual",
+        "data": "synthetic (seeded scene generator, reference input model)",
+        "config": {"workload": "cfg1: level-4 tria6 sphere (r=1, eps_r 2.5, sigma 1e-3) between "
+                               "30x30-cell tria6 plates at z=+-5, +-1 V; medium eps_r 78, sigma 1e-4",
+                   "N": N, "E": E, "freqs_per_step": NFREQ, "freq_range_hz": [1e3, 1e8],
+                   "tol": TOL, "step": "assemble K (FP64) + 64-system mixed sweep + MST forces",
+                   "l2": "inputs larger than L2 (K 2.5 GB FP64 + 1.25 GB FP32)",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": NFREQ / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "fp64_path": {"value": 1.0 / fp64_s, "unit": UNIT, "ms_per_solve": fp64_s * 1e3,
+                      "gmres_iters": int(itf[0])},
+        "speedup_vs_fp64_path": value / world / (1.0 / fp64_s),
+        "accuracy": {"force_err_vs_fp64": ferr, "sigma_rel_err_vs_fp64": serr,
+                     "force_err_def": "max over 3 frequencies of |Fcm_mixed - Fcm_fp64| / sum|Fce|"},
+        "kernels_ms": {k: {"ms": v[0], "launches": v[1], "share": v[0] / total_ms if total_ms else 0}
+                       for k, v in timing.items()},
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    print(json.dumps(out), flush=True)
+
+
+# ------------------------------------------------------------------ reference
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    from depsolver_gb300 import scenes
+    sc = scenes.cfg1()
+    threads = os.cpu_count() or 1
+    # warm-up: one full solve (the reference's iteration count), then samples
+    first = cpu_baseline(sc, threads, full_first=True)
+    for _ in range(max(0, args.warmup - 1)):
+        cpu_baseline(sc, threads, full_first=False)
+    ests = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r = cpu_baseline(sc, threads, full_first=False)
+        ests.append(r["est_solve_s"])
+    wall = time.perf_counter() - t0
+    it = first["full"]["gmres_iters"]
+    est = statistics.median(ests)
+    value = 1.0 / est
+    cb = dict(first)
+    cb["value"] = value
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded scene generator, reference input model)",
+           "config": {"workload": "cfg1 (as the GPU arm), one frequency per solve, "
+                                  f"reference GMRES tolerance 1e-6 ({it} iterations)",
+                      "N": sc.N, "E": sc.E, "threads": threads},
+           "cpu_baseline": cb,
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--only-step", action="store_true",
+                    help="run one warm-up and one step and nothing else (profiling)")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    if world > 1 and args.impl == "ours":
+        import torch
+        torch.distributed.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world)
+    if world > 1 and args.impl == "ours":
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -53,6 +53,28 @@ def lib() -> C.CDLL:
         L.dsc_force_mst.restype = C.c_int
         L.dsc_force_mst.argtypes = [C.c_int, C.c_uint, C.c_uint, _dp, _up, _up, _dp, C.c_double,
                                     C.c_void_p, C.c_void_p, _dp, _dp]
+        L.dsc_session_create.restype = C.c_int
+        L.dsc_session_create.argtypes = [C.c_int, C.c_uint, C.c_uint, _dp, _up, _up, _dp, C.c_uint,
+                                         C.c_void_p, C.c_uint, _dp, C.POINTER(C.c_void_p)]
+        L.dsc_session_destroy.restype = None
+        L.dsc_session_destroy.argtypes = [C.c_void_p]
+        L.dsc_session_assemble.restype = C.c_int
+        L.dsc_session_assemble.argtypes = [C.c_void_p]
+        L.dsc_session_solve.restype = C.c_int
+        L.dsc_session_solve.argtypes = [C.c_void_p, C.c_int, C.c_uint, _dp, C.c_double, C.c_uint,
+                                        C.c_void_p, C.c_void_p, C.c_void_p]
+        L.dsc_session_stream.restype = C.c_void_p
+        L.dsc_session_stream.argtypes = [C.c_void_p]
+        L.dsc_kernel_launches.restype = C.c_ulonglong
+        L.dsc_kernel_launches.argtypes = []
+        L.dsc_session_set_timing.restype = C.c_int
+        L.dsc_session_set_timing.argtypes = [C.c_void_p, C.c_int]
+        L.dsc_session_timing.restype = C.c_int
+        L.dsc_session_timing.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        L.dsc_sweep.restype = C.c_int
+        L.dsc_sweep.argtypes = [C.c_int, C.c_uint, C.c_uint, _dp, _up, _up, _dp, C.c_uint,
+                                C.c_void_p, C.c_uint, _dp, C.c_int, C.c_uint, _dp, C.c_double,
+                                C.c_uint, C.c_void_p, C.c_void_p, C.c_void_p]
         _lib = L
     return _lib
 

@@ -101,3 +101,87 @@ def force_mst(sc: Scene, vB: np.ndarray, eps: float | None = None):
                                               _u(sc.bctype), _f(vB), eps, Fce.ctypes.data,
                                               Xce.ctypes.data, Fcm, Xcm))
     return Fce, Xce, Fcm, Xcm
+
+
+# ------------------------------------------------------------------ sweeps
+
+MODE_FP64 = 1
+MODE_MIXED = 2
+TIMER_NAMES = ("asm_regular", "asm_fixup", "asm_singular", "gemv_K64", "gemm_K", "field", "mst",
+               "residual_fp64", "krylov")
+
+
+class Session:
+    """A geometry kept on the GPU (geometric matrix assembled once) for
+    frequency sweeps; wraps dsc_session_* of the C ABI."""
+
+    def __init__(self, sc: Scene):
+        L = _native.lib()
+        self._L = L
+        self.scene = sc
+        h = C.c_void_p()
+        ifc = _u(sc.ifaces)
+        _native.check(L.dsc_session_create(sc.nen, sc.N, sc.E, _f(sc.nodes), _u(sc.elems),
+                                           _u(sc.bctype), _f(sc.mbc), sc.n_if,
+                                           ifc.ctypes.data if sc.n_if else None,
+                                           sc.mat.shape[0], _f(sc.mat), C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if self._h:
+            self._L.dsc_session_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def assemble(self):
+        _native.check(self._L.dsc_session_assemble(self._h))
+
+    def stream_handle(self) -> int:
+        """cudaStream_t of the session (for torch.cuda.ExternalStream)."""
+        return int(self._L.dsc_session_stream(self._h) or 0)
+
+    def set_timing(self, on: bool):
+        _native.check(self._L.dsc_session_set_timing(self._h, int(on)))
+
+    def timing(self):
+        ms = np.zeros(len(TIMER_NAMES))
+        cnt = np.zeros(len(TIMER_NAMES), dtype=np.int32)
+        _native.check(self._L.dsc_session_timing(self._h, ms.ctypes.data, cnt.ctypes.data,
+                                                 len(TIMER_NAMES)))
+        return {n: (float(ms[k]), int(cnt[k])) for k, n in enumerate(TIMER_NAMES)}
+
+    def solve(self, freqs, mode: int = MODE_MIXED, tol: float = 1e-10, max_iters: int = 600,
+              want_sigma: bool = False):
+        """Returns (forces (F x 9): Fcm, Xcm, sum|Fce|; iterations; sigma or None)."""
+        fr = _f(np.atleast_1d(freqs))
+        F = fr.shape[0]
+        forces = np.zeros((F, 9))
+        its = np.zeros(F, dtype=np.uint32)
+        sig = np.zeros((F, 2 * self.scene.N)) if want_sigma else None
+        _native.check(self._L.dsc_session_solve(self._h, mode, F, fr, tol, max_iters,
+                                                sig.ctypes.data if sig is not None else None,
+                                                forces.ctypes.data, its.ctypes.data))
+        return forces, its, sig
+
+
+def sweep(sc: Scene, freqs, mode: int = MODE_MIXED, tol: float = 1e-10, max_iters: int = 600,
+          want_sigma: bool = True):
+    """One call from host arrays to forces (and sigma): dsc_sweep."""
+    L = _native.lib()
+    fr = _f(np.atleast_1d(freqs))
+    F = fr.shape[0]
+    forces = np.zeros((F, 9))
+    its = np.zeros(F, dtype=np.uint32)
+    sig = np.zeros((F, 2 * sc.N)) if want_sigma else None
+    ifc = _u(sc.ifaces)
+    _native.check(L.dsc_sweep(sc.nen, sc.N, sc.E, _f(sc.nodes), _u(sc.elems), _u(sc.bctype),
+                              _f(sc.mbc), sc.n_if, ifc.ctypes.data if sc.n_if else None,
+                              sc.mat.shape[0], _f(sc.mat), mode, F, fr, tol, max_iters,
+                              sig.ctypes.data if sig is not None else None, forces.ctypes.data,
+                              its.ctypes.data))
+    return forces, its, sig

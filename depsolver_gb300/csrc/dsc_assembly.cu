@@ -260,10 +260,10 @@ static size_t regular_smem(int nen)
 }
 
 template <int NEN>
-static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStream_t st)
+static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStream_t st, Timer *tm)
 {
-    k_elem_qp<NEN><<<(m.E * kTriPts + 255) / 256, 256, 0, st>>>(m.x.p, m.y.p, m.z.p, m.elems.p, m.E,
-                                                                  m.qp.p);
+    DSC_LAUNCH(k_elem_qp<NEN><<<(m.E * kTriPts + 255) / 256, 256, 0, st>>>(m.x.p, m.y.p, m.z.p, m.elems.p, m.E,
+                                                                  m.qp.p));
     DSC_CUDA(cudaGetLastError());
     // Partial-sum buffer: n_slots columns of a row chunk, at most ~1 GiB.
     const size_t budget = (size_t)1 << 30;
@@ -286,18 +286,23 @@ static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStr
         a.row_lo = lo;
         a.row_hi = hi;
         dim3 grid((hi - lo + kRowTile - 1) / kRowTile, m.G);
-        k_asm_regular_f64<NEN><<<grid, 128, smem, st>>>(a, K, P.p);
+        {
+            TimerScope ts(tm, kTAsmRegular, st);
+            DSC_LAUNCH(k_asm_regular_f64<NEN><<<grid, 128, smem, st>>>(a, K, P.p));
+        }
         DSC_CUDA(cudaGetLastError());
         if (m.n_fix > 0) {
             dim3 fg((hi - lo + 255) / 256, std::min(m.n_fix, 65535));
-            k_asm_fixup<double><<<fg, 256, 0, st>>>(m.fix_ptr.p, m.fix_slot.p, m.fix_col.p, m.n_fix,
-                                                    P.p, (size_t)rc, K, ld, lo, hi - lo);
+            TimerScope ts(tm, kTAsmFixup, st);
+            DSC_LAUNCH(k_asm_fixup<double><<<fg, 256, 0, st>>>(m.fix_ptr.p, m.fix_slot.p, m.fix_col.p, m.n_fix,
+                                                    P.p, (size_t)rc, K, ld, lo, hi - lo));
             DSC_CUDA(cudaGetLastError());
         }
         int warps = hi - lo;
-        k_asm_singular<NEN, double><<<(warps * 32 + 127) / 128, 128, 0, st>>>(
+        TimerScope ts(tm, kTAsmSingular, st);
+        DSC_LAUNCH(k_asm_singular<NEN, double><<<(warps * 32 + 127) / 128, 128, 0, st>>>(
             m.x.p, m.y.p, m.z.p, m.normals.p, m.row_kind.p, m.row_fac.p, m.elems.p, m.ne_ptr.p,
-            m.ne_elem.p, m.ne_pos.p, lo, hi, K, ld);
+            m.ne_elem.p, m.ne_pos.p, lo, hi, K, ld));
         DSC_CUDA(cudaGetLastError());
     }
     // P is released at scope exit: wait for the kernels that read it.
@@ -305,9 +310,9 @@ static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStr
     return kOk;
 }
 
-int assemble_K_fp64(const DeviceMesh &m, double *K, size_t ld, cudaStream_t st)
+int assemble_K_fp64(const DeviceMesh &m, double *K, size_t ld, cudaStream_t st, Timer *tm)
 {
-    return m.nen == 6 ? assemble_fp64_impl<6>(m, K, ld, st) : assemble_fp64_impl<3>(m, K, ld, st);
+    return m.nen == 6 ? assemble_fp64_impl<6>(m, K, ld, st, tm) : assemble_fp64_impl<3>(m, K, ld, st, tm);
 }
 
 }  // namespace dsc

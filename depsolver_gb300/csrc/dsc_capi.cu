@@ -249,7 +249,7 @@ static int assemble_impl(int nen, int full, unsigned N, unsigned E, unsigned nIf
     for (int r0 = 0; r0 < nrows; r0 += rows_per) {
         const int r1 = std::min(nrows, r0 + rows_per);
         dim3 grid(((int)N + 31) / 32, (r1 - r0 + 31) / 32), blk(32, 8);
-        k_form_rows<<<grid, blk, 0, st>>>(K.p, ld, (int)N, full, r0, r1, dca.p, dcb.p, dcd.p, stage.p);
+        DSC_LAUNCH(k_form_rows<<<grid, blk, 0, st>>>(K.p, ld, (int)N, full, r0, r1, dca.p, dcb.p, dcd.p, stage.p));
         DSC_CUDA(cudaGetLastError());
         DSC_CUDA(cudaMemcpyAsync(host, stage.p, (size_t)(r1 - r0) * ncol * sizeof(double),
                                  cudaMemcpyDeviceToHost, st));

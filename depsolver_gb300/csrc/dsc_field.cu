@@ -338,10 +338,15 @@ __global__ void k_mst_totals(const double *__restrict__ Fce, int npel, const dou
         f[d] = warp_sum(f[d]);
         x[d] = warp_sum(x[d]);
     }
+    double fa[3] = {0, 0, 0};
+    for (int t = lane; t < npel; t += 32)
+        for (int d = 0; d < 3; d++) fa[d] += fabs(Fce[3 * (size_t)t + d]);
+    for (int d = 0; d < 3; d++) fa[d] = warp_sum(fa[d]);
     if (lane == 0) {
         for (int d = 0; d < 3; d++) {
             tot[d] = f[d];
             tot[3 + d] = x[d] / P;
+            tot[6 + d] = fa[d];
         }
     }
 }
@@ -407,50 +412,50 @@ int PointSet::build(const HostPlan &plan, int P, const double *pts)
 }
 
 template <int NEN>
-static int eval_points_impl(const DeviceMesh &m, const PointSet &ps, const double *dsigma,
-                            int field, double *dout, cudaStream_t st)
+static int eval_points_impl(const DeviceMesh &m, PointSet &ps, const double *dsigma, int field,
+                            double *dout, cudaStream_t st, bool sync)
 {
     const int NV = field ? 6 : 2;
-    DevBuf<double> cq, part, sing;
+    DevBuf<double> &cq = ps.cq, &part = ps.part, &sing = ps.sing;
     DSC_TRY(cq.alloc((size_t)m.E * kTriPts * 5));
-    k_charge_qp<NEN><<<(m.E * kTriPts + 255) / 256, 256, 0, st>>>(m.x.p, m.y.p, m.z.p, m.elems.p, m.E,
-                                                                    m.N, dsigma, cq.p);
+    DSC_LAUNCH(k_charge_qp<NEN><<<(m.E * kTriPts + 255) / 256, 256, 0, st>>>(m.x.p, m.y.p, m.z.p, m.elems.p, m.E,
+                                                                    m.N, dsigma, cq.p));
     PointArgs a{ps.px.p, ps.py.p, ps.pz.p, ps.coinc.p, ps.P, m.elems.p, cq.p, m.E};
     int nchunk;
     if (ps.P >= 64) {
         nchunk = (m.E + kFieldChunk - 1) / kFieldChunk;
         DSC_TRY(part.alloc((size_t)nchunk * ps.P * NV));
         dim3 g((ps.P + 127) / 128, nchunk);
-        if (field) k_point_regular<NEN, 1><<<g, 128, 0, st>>>(a, part.p);
-        else k_point_regular<NEN, 0><<<g, 128, 0, st>>>(a, part.p);
+        if (field) DSC_LAUNCH(k_point_regular<NEN, 1><<<g, 128, 0, st>>>(a, part.p));
+        else DSC_LAUNCH(k_point_regular<NEN, 0><<<g, 128, 0, st>>>(a, part.p));
     } else {
         nchunk = (m.E + 127) / 128;
         DSC_TRY(part.alloc((size_t)nchunk * ps.P * NV));
-        if (field) k_point_regular_few<NEN, 1><<<nchunk, 128, 0, st>>>(a, part.p);
-        else k_point_regular_few<NEN, 0><<<nchunk, 128, 0, st>>>(a, part.p);
+        if (field) DSC_LAUNCH(k_point_regular_few<NEN, 1><<<nchunk, 128, 0, st>>>(a, part.p));
+        else DSC_LAUNCH(k_point_regular_few<NEN, 0><<<nchunk, 128, 0, st>>>(a, part.p));
     }
     DSC_CUDA(cudaGetLastError());
     DSC_TRY(sing.alloc((size_t)ps.P * NV));
     const int sblocks = (ps.P * 32 + 127) / 128;
     if (field)
-        k_point_singular<NEN, 1><<<sblocks, 128, 0, st>>>(a, m.x.p, m.y.p, m.z.p, m.normals.p, m.N,
-                                                          dsigma, ps.sp_ptr.p, ps.sp.p, sing.p);
+        DSC_LAUNCH(k_point_singular<NEN, 1><<<sblocks, 128, 0, st>>>(a, m.x.p, m.y.p, m.z.p, m.normals.p, m.N,
+                                                          dsigma, ps.sp_ptr.p, ps.sp.p, sing.p));
     else
-        k_point_singular<NEN, 0><<<sblocks, 128, 0, st>>>(a, m.x.p, m.y.p, m.z.p, m.normals.p, m.N,
-                                                          dsigma, ps.sp_ptr.p, ps.sp.p, sing.p);
+        DSC_LAUNCH(k_point_singular<NEN, 0><<<sblocks, 128, 0, st>>>(a, m.x.p, m.y.p, m.z.p, m.normals.p, m.N,
+                                                          dsigma, ps.sp_ptr.p, ps.sp.p, sing.p));
     DSC_CUDA(cudaGetLastError());
-    if (field) k_point_reduce<6><<<(ps.P * 6 + 255) / 256, 256, 0, st>>>(part.p, nchunk, ps.P, sing.p, dout);
-    else k_point_reduce<2><<<(ps.P * 2 + 255) / 256, 256, 0, st>>>(part.p, nchunk, ps.P, sing.p, dout);
+    if (field) DSC_LAUNCH(k_point_reduce<6><<<(ps.P * 6 + 255) / 256, 256, 0, st>>>(part.p, nchunk, ps.P, sing.p, dout));
+    else DSC_LAUNCH(k_point_reduce<2><<<(ps.P * 2 + 255) / 256, 256, 0, st>>>(part.p, nchunk, ps.P, sing.p, dout));
     DSC_CUDA(cudaGetLastError());
-    DSC_CUDA(cudaStreamSynchronize(st));
+    if (sync) DSC_CUDA(cudaStreamSynchronize(st));
     return kOk;
 }
 
-int eval_points(const DeviceMesh &m, const PointSet &ps, const double *dsigma, int field,
-                double *dout, cudaStream_t st)
+int eval_points(const DeviceMesh &m, PointSet &ps, const double *dsigma, int field, double *dout,
+                cudaStream_t st, bool sync)
 {
-    return m.nen == 6 ? eval_points_impl<6>(m, ps, dsigma, field, dout, st)
-                      : eval_points_impl<3>(m, ps, dsigma, field, dout, st);
+    return m.nen == 6 ? eval_points_impl<6>(m, ps, dsigma, field, dout, st, sync)
+                      : eval_points_impl<3>(m, ps, dsigma, field, dout, st, sync);
 }
 
 int force_mst(const DeviceMesh &m, const HostPlan &plan, const unsigned *bctype,
@@ -468,42 +473,24 @@ int force_mst(const DeviceMesh &m, const HostPlan &plan, const unsigned *bctype,
         }
     for (int e = 0; e < m.E; e++)
         if (bctype[plan.elems[(size_t)e * m.nen]] == 6) pel.push_back(e);
-    const int P = (int)ids.size(), npel = (int)pel.size();
-    if (P == 0) {
+    (void)pts;
+    ForcePlan fp;
+    DSC_TRY(fp.build(plan, bctype, st));
+    if (fp.P == 0) {
         // the reference divides by a zero count here; report zeros
         for (int d = 0; d < 3; d++) Fcm[d] = Xcm[d] = 0.0;
         return kOk;
     }
-    PointSet ps;
-    DSC_TRY(ps.build(plan, P, pts.data()));
-    DevBuf<double> Ept, Enode, Fce, Xce, tot;
-    DevBuf<int> dids, dpel;
-    DSC_TRY(Ept.alloc((size_t)P * 6));
-    DSC_TRY(eval_points(m, ps, dsigma, 1, Ept.p, st));
-    DSC_TRY(Enode.alloc((size_t)m.N * 3));
-    DSC_CUDA(cudaMemsetAsync(Enode.p, 0, (size_t)m.N * 3 * sizeof(double), st));
-    DSC_TRY(dids.upload(ids, st));
-    DSC_TRY(dpel.upload(pel.empty() ? std::vector<int>{0} : pel, st));
-    k_scatter_re<<<(P + 255) / 256, 256, 0, st>>>(Ept.p, dids.p, P, Enode.p);
-    DSC_TRY(Fce.alloc((size_t)std::max(npel, 1) * 3));
-    DSC_TRY(Xce.alloc((size_t)std::max(npel, 1) * 3));
-    DSC_TRY(tot.alloc(6));
-    if (npel > 0) {
-        if (m.nen == 6)
-            k_mst<6><<<(npel + 127) / 128, 128, 0, st>>>(m.x.p, m.y.p, m.z.p, m.elems.p, dpel.p, npel,
-                                                         Enode.p, eps, Fce.p, Xce.p);
-        else
-            k_mst<3><<<(npel + 127) / 128, 128, 0, st>>>(m.x.p, m.y.p, m.z.p, m.elems.p, dpel.p, npel,
-                                                         Enode.p, eps, Fce.p, Xce.p);
-    }
-    k_mst_totals<<<1, 32, 0, st>>>(Fce.p, npel, m.x.p, m.y.p, m.z.p, dids.p, P, tot.p);
-    DSC_CUDA(cudaGetLastError());
-    double h[6];
+    DevBuf<double> tot;
+    DSC_TRY(tot.alloc(9));
+    DSC_TRY(force_mst_dev(m, fp, dsigma, eps, tot.p, st));
+    double h[9];
     DSC_CUDA(cudaMemcpyAsync(h, tot.p, sizeof h, cudaMemcpyDeviceToHost, st));
+    const int npel = fp.npel;
     std::vector<double> f((size_t)npel * 3), x((size_t)npel * 3);
     if (npel > 0 && (Fce_host || Xce_host)) {
-        DSC_CUDA(cudaMemcpyAsync(f.data(), Fce.p, f.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
-        DSC_CUDA(cudaMemcpyAsync(x.data(), Xce.p, x.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+        DSC_CUDA(cudaMemcpyAsync(f.data(), fp.Fce.p, f.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+        DSC_CUDA(cudaMemcpyAsync(x.data(), fp.Xce.p, x.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
     }
     DSC_CUDA(cudaStreamSynchronize(st));
     for (int d = 0; d < 3; d++) {
@@ -512,9 +499,62 @@ int force_mst(const DeviceMesh &m, const HostPlan &plan, const unsigned *bctype,
     }
     for (int t = 0; t < npel; t++)
         for (int d = 0; d < 3; d++) {
-            if (Fce_host) Fce_host[3 * (size_t)pel[t] + d] = f[3 * (size_t)t + d];
-            if (Xce_host) Xce_host[3 * (size_t)pel[t] + d] = x[3 * (size_t)t + d];
+            if (Fce_host) Fce_host[3 * (size_t)fp.pel_host[t] + d] = f[3 * (size_t)t + d];
+            if (Xce_host) Xce_host[3 * (size_t)fp.pel_host[t] + d] = x[3 * (size_t)t + d];
         }
+    return kOk;
+}
+
+int ForcePlan::build(const HostPlan &plan, const unsigned *bctype, cudaStream_t st)
+{
+    std::vector<int> idv;
+    std::vector<double> pts;
+    for (int i = 0; i < plan.N; i++)
+        if (bctype[i] == 6) {
+            idv.push_back(i);
+            for (int d = 0; d < 3; d++) pts.push_back(plan.nodes[3 * (size_t)i + d]);
+        }
+    pel_host.clear();
+    for (int e = 0; e < plan.E; e++)
+        if (bctype[plan.elems[(size_t)e * plan.nen]] == 6) pel_host.push_back(e);
+    P = (int)idv.size();
+    npel = (int)pel_host.size();
+    if (P == 0) return kOk;
+    DSC_TRY(ps.build(plan, P, pts.data()));
+    DSC_TRY(ids.upload(idv, st));
+    DSC_TRY(pel.upload(pel_host.empty() ? std::vector<int>{0} : pel_host, st));
+    DSC_TRY(Ept.alloc((size_t)P * 6));
+    DSC_TRY(Enode.alloc((size_t)plan.N * 3));
+    DSC_TRY(Fce.alloc((size_t)std::max(npel, 1) * 3));
+    DSC_TRY(Xce.alloc((size_t)std::max(npel, 1) * 3));
+    DSC_CUDA(cudaMemsetAsync(Enode.p, 0, (size_t)plan.N * 3 * sizeof(double), st));
+    DSC_CUDA(cudaStreamSynchronize(st));
+    return kOk;
+}
+
+int force_mst_dev(const DeviceMesh &m, ForcePlan &fp, const double *dsigma, double eps,
+                  double *d_tot, cudaStream_t st, Timer *tm)
+{
+    if (fp.P == 0) {
+        DSC_CUDA(cudaMemsetAsync(d_tot, 0, 9 * sizeof(double), st));
+        return kOk;
+    }
+    {
+        TimerScope ts(tm, kTField, st);
+        DSC_TRY(eval_points(m, fp.ps, dsigma, 1, fp.Ept.p, st, false));
+    }
+    TimerScope ts(tm, kTMst, st);
+    DSC_LAUNCH(k_scatter_re<<<(fp.P + 255) / 256, 256, 0, st>>>(fp.Ept.p, fp.ids.p, fp.P, fp.Enode.p));
+    if (fp.npel > 0) {
+        if (m.nen == 6)
+            DSC_LAUNCH(k_mst<6><<<(fp.npel + 127) / 128, 128, 0, st>>>(m.x.p, m.y.p, m.z.p, m.elems.p, fp.pel.p,
+                                                            fp.npel, fp.Enode.p, eps, fp.Fce.p, fp.Xce.p));
+        else
+            DSC_LAUNCH(k_mst<3><<<(fp.npel + 127) / 128, 128, 0, st>>>(m.x.p, m.y.p, m.z.p, m.elems.p, fp.pel.p,
+                                                            fp.npel, fp.Enode.p, eps, fp.Fce.p, fp.Xce.p));
+    }
+    DSC_LAUNCH(k_mst_totals<<<1, 32, 0, st>>>(fp.Fce.p, fp.npel, m.x.p, m.y.p, m.z.p, fp.ids.p, fp.P, d_tot));
+    DSC_CUDA(cudaGetLastError());
     return kOk;
 }
 

@@ -18,13 +18,34 @@ struct PointSet {
     DevBuf<int4> coinc;
     DevBuf<int> sp_ptr;
     DevBuf<int4> sp;
+    // workspace of eval_points (charge-weighted points, chunk partials,
+    // singular parts), kept between calls
+    DevBuf<double> cq, part, sing;
     int build(const HostPlan &plan, int P, const double *pts);
 };
 
 // field = 1: dout = P x 6 (Re Ex, Im Ex, Re Ey, Im Ey, Re Ez, Im Ez);
 // field = 0: dout = P x 2 (Re, Im potential).  dsigma: device, 2N.
-int eval_points(const DeviceMesh &m, const PointSet &ps, const double *dsigma, int field,
-                double *dout, cudaStream_t st);
+// sync = false leaves the work queued on st.
+int eval_points(const DeviceMesh &m, PointSet &ps, const double *dsigma, int field, double *dout,
+                cudaStream_t st, bool sync = true);
+
+// What the force step needs, built once per scene: the type-6 nodes as
+// evaluation points and the elements whose first node has type 6.
+struct ForcePlan {
+    int P = 0, npel = 0;
+    PointSet ps;
+    DevBuf<int> ids, pel;
+    std::vector<int> pel_host;
+    DevBuf<double> Ept, Enode, Fce, Xce;
+    int build(const HostPlan &plan, const unsigned *bctype, cudaStream_t st);
+};
+
+// Force for one nodal solution dsigma (device, 2N); d_tot (device, 9):
+// Fcm[3], Xcm[3], sum over elements of |Fce| per component[3].  Fce/Xce
+// of the particle elements stay in fp.Fce / fp.Xce (npel x 3).
+int force_mst_dev(const DeviceMesh &m, ForcePlan &fp, const double *dsigma, double eps,
+                  double *d_tot, cudaStream_t st, Timer *tm = nullptr);
 
 // Maxwell-stress force on the type-6 surface; Fce/Xce (host, E x 3, may be
 // null) receive the rows of particle elements only.

@@ -117,11 +117,37 @@ __global__ void k_update_x(double *__restrict__ x, const double *__restrict__ V,
     }
 }
 
+// The compact N x 2N matrix as an operator.
+struct CompactOp : RealOp {
+    const double *A;
+    size_t lda;
+    int N;
+    int apply(const double *x, double *y, cudaStream_t st) override
+    {
+        DSC_LAUNCH(k_matvec_compact<<<(N * 32 + 255) / 256, 256, 0, st>>>(A, lda, N, x, y));
+        DSC_CUDA(cudaGetLastError());
+        return kOk;
+    }
+};
+
 int gmres_compact_fp64(int N, double *dA, size_t lda, double *dB, const double *dx0,
                        unsigned preCond, double tol_rel, unsigned max_iters, FILE *log,
                        unsigned *iters_out, cudaStream_t st)
 {
-    const int n = 2 * N;
+    if (preCond == 1) {
+        DSC_LAUNCH(k_jacobi_scale<<<N, 256, 0, st>>>(dA, lda, N, dB));
+        DSC_CUDA(cudaGetLastError());
+    }
+    CompactOp op;
+    op.A = dA;
+    op.lda = lda;
+    op.N = N;
+    return gmres_real_fp64(2 * N, op, dB, dx0, tol_rel, max_iters, log, iters_out, st);
+}
+
+int gmres_real_fp64(int n, RealOp &op, double *dB, const double *dx0, double tol_rel,
+                    unsigned max_iters, FILE *log, unsigned *iters_out, cudaStream_t st)
+{
     const unsigned M = max_iters;
     DevBuf<double> V, x, y, scal, part, resd;
     DevBuf<unsigned> cnt;
@@ -141,11 +167,7 @@ int gmres_compact_fp64(int N, double *dA, size_t lda, double *dB, const double *
 
     if (dx0) DSC_CUDA(cudaMemcpyAsync(x.p, dx0, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
     else DSC_CUDA(cudaMemsetAsync(x.p, 0, n * sizeof(double), st));
-    if (preCond == 1) {
-        k_jacobi_scale<<<N, 256, 0, st>>>(dA, lda, N, dB);
-        DSC_CUDA(cudaGetLastError());
-    }
-    k_dot<<<rg, rt, 0, st>>>(dB, dB, n, rw, aux + 1);
+    DSC_LAUNCH(k_dot<<<rg, rt, 0, st>>>(dB, dB, n, rw, aux + 1));
     double bb;
     DSC_CUDA(cudaMemcpyAsync(&bb, aux + 1, sizeof(double), cudaMemcpyDeviceToHost, st));
     DSC_CUDA(cudaStreamSynchronize(st));
@@ -159,15 +181,14 @@ int gmres_compact_fp64(int N, double *dA, size_t lda, double *dB, const double *
     // initial residual (initRes_el src/gmres_el.c:272-294)
     double xx = 0.0;
     if (dx0) {
-        k_dot<<<rg, rt, 0, st>>>(x.p, x.p, n, rw, aux + 1);
+        DSC_LAUNCH(k_dot<<<rg, rt, 0, st>>>(x.p, x.p, n, rw, aux + 1));
         DSC_CUDA(cudaMemcpyAsync(&xx, aux + 1, sizeof(double), cudaMemcpyDeviceToHost, st));
         DSC_CUDA(cudaStreamSynchronize(st));
     }
-    if (sqrt(xx) != 0.0)
-        k_matvec_compact<<<(N * 32 + 255) / 256, 256, 0, st>>>(dA, lda, N, x.p, y.p);
-    k_residual0<<<vblocks, 256, 0, st>>>(dB, y.p, V.p, n, sqrt(xx) != 0.0);
-    k_dot<<<rg, rt, 0, st>>>(V.p, V.p, n, rw, aux + 1);
-    k_normalize<<<vblocks, 256, 0, st>>>(V.p, n, aux + 1, aux + 2, 1);
+    if (sqrt(xx) != 0.0) DSC_TRY(op.apply(x.p, y.p, st));
+    DSC_LAUNCH(k_residual0<<<vblocks, 256, 0, st>>>(dB, y.p, V.p, n, sqrt(xx) != 0.0));
+    DSC_LAUNCH(k_dot<<<rg, rt, 0, st>>>(V.p, V.p, n, rw, aux + 1));
+    DSC_LAUNCH(k_normalize<<<vblocks, 256, 0, st>>>(V.p, n, aux + 1, aux + 2, 1));
     DSC_CUDA(cudaGetLastError());
     double r0;
     DSC_CUDA(cudaMemcpyAsync(&r0, aux + 2, sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -186,15 +207,15 @@ int gmres_compact_fp64(int N, double *dA, size_t lda, double *dB, const double *
         for (unsigned i = 0; i < M; i++) {
             it++;
             double *vi = V.p + (size_t)i * n, *w = V.p + (size_t)(i + 1) * n;
-            k_matvec_compact<<<(N * 32 + 255) / 256, 256, 0, st>>>(dA, lda, N, vi, w);
-            k_dot<<<rg, rt, 0, st>>>(w, w, n, rw, aux);
+            DSC_TRY(op.apply(vi, w, st));
+            DSC_LAUNCH(k_dot<<<rg, rt, 0, st>>>(w, w, n, rw, aux));
             for (unsigned j = 0; j <= i; j++)
-                k_mgs_step<<<rg, rt, 0, st>>>(w, j ? V.p + (size_t)(j - 1) * n : nullptr,
+                DSC_LAUNCH(k_mgs_step<<<rg, rt, 0, st>>>(w, j ? V.p + (size_t)(j - 1) * n : nullptr,
                                               V.p + (size_t)j * n, n, hcol + (j ? j - 1 : 0), rw,
-                                              hcol + j);
-            k_mgs_step<<<rg, rt, 0, st>>>(w, V.p + (size_t)i * n, nullptr, n, hcol + i, rw,
-                                          aux + 3);
-            k_normalize<<<vblocks, 256, 0, st>>>(w, n, aux + 3, hcol + i + 1, 1);
+                                              hcol + j));
+            DSC_LAUNCH(k_mgs_step<<<rg, rt, 0, st>>>(w, V.p + (size_t)i * n, nullptr, n, hcol + i, rw,
+                                          aux + 3));
+            DSC_LAUNCH(k_normalize<<<vblocks, 256, 0, st>>>(w, n, aux + 3, hcol + i + 1, 1));
             DSC_CUDA(cudaGetLastError());
             DSC_CUDA(cudaMemcpyAsync(col.data(), hcol, (i + 2) * sizeof(double),
                                      cudaMemcpyDeviceToHost, st));
@@ -234,7 +255,7 @@ int gmres_compact_fp64(int N, double *dA, size_t lda, double *dB, const double *
             }
             DSC_CUDA(cudaMemcpyAsync(resd.p, res.data(), it * sizeof(double),
                                      cudaMemcpyHostToDevice, st));
-            k_update_x<<<vblocks, 256, 0, st>>>(x.p, V.p, n, resd.p, (int)it, n);
+            DSC_LAUNCH(k_update_x<<<vblocks, 256, 0, st>>>(x.p, V.p, n, resd.p, (int)it, n));
             DSC_CUDA(cudaGetLastError());
         }
     }

@@ -6,6 +6,18 @@
 
 namespace dsc {
 
+// A real linear operator of dimension n on the device: y = Op x.
+struct RealOp {
+    virtual ~RealOp() = default;
+    virtual int apply(const double *x, double *y, cudaStream_t st) = 0;
+};
+
+// The reference's GMRES iteration (src/gmres_el.c:149-260) on any real
+// operator: dB (n) in, solution out; preconditioning, if any, is already
+// folded into op and dB by the caller.
+int gmres_real_fp64(int n, RealOp &op, double *dB, const double *dx0, double tol_rel,
+                    unsigned max_iters, FILE *log, unsigned *iters, cudaStream_t st);
+
 // Reference-faithful FP64 GMRES on the compact form (device A, N x 2N with
 // row stride lda, scaled in place when preCond == 1; device B overwritten
 // with the solution on success).  log (may be null) receives gmres.log.

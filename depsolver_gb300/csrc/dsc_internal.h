@@ -24,6 +24,15 @@ enum Status {
 void set_error(const char *fmt, ...);
 const char *last_error();
 
+// Every kernel launch of the library goes through DSC_LAUNCH, which counts
+// it (dsc_kernel_launches() in the C ABI reports the running total).
+void note_launch();
+#define DSC_LAUNCH(...)         \
+    do {                        \
+        ::dsc::note_launch();   \
+        __VA_ARGS__;            \
+    } while (0)
+
 #define DSC_CUDA(call)                                                                       \
     do {                                                                                     \
         cudaError_t e_ = (call);                                                             \
@@ -74,6 +83,45 @@ struct DevBuf {
         return kOk;
     }
     int upload(const std::vector<T> &v, cudaStream_t st) { return upload(v.data(), v.size(), st); }
+};
+
+// ---------------------------------------------------------------- timing
+// CUDA-event timing of kernel classes on the launching stream (enabled by
+// the caller; off by default so that the plain entry points pay nothing).
+enum TimerId {
+    kTAsmRegular = 0, kTAsmFixup, kTAsmSingular, kTGemvK, kTGemmK, kTField, kTMst, kTResidual,
+    kTKrylov, kTCount
+};
+
+struct Timer {
+    bool on = false;
+    struct Rec {
+        int id;
+        cudaEvent_t a, b;
+    };
+    std::vector<Rec> recs;
+    std::vector<cudaEvent_t> pool;
+    int open_id = -1;
+    cudaEvent_t open_a = nullptr;
+    cudaEvent_t take();
+    void begin(int id, cudaStream_t st);
+    void end(cudaStream_t st);
+    // sums (ms) and launch counts per id since the last collect; resets
+    int collect(double *ms, int *count);
+    ~Timer();
+};
+
+struct TimerScope {
+    Timer *t;
+    cudaStream_t st;
+    TimerScope(Timer *t_, int id, cudaStream_t s) : t(t_ && t_->on ? t_ : nullptr), st(s)
+    {
+        if (t) t->begin(id, st);
+    }
+    ~TimerScope()
+    {
+        if (t) t->end(st);
+    }
 };
 
 // ---------------------------------------------------------------- mesh plan
@@ -139,7 +187,7 @@ struct DeviceMesh {
 // geometric integral of row i against node c: C * int G N_c for conductor
 // rows, int H N_c (normal derivative, sign as the reference) for interface
 // rows.  The frequency enters only through per-row coefficients.
-int assemble_K_fp64(const DeviceMesh &m, double *K, size_t ld, cudaStream_t st);
-int assemble_K_fp32(const DeviceMesh &m, float *K, size_t ld, cudaStream_t st);
+int assemble_K_fp64(const DeviceMesh &m, double *K, size_t ld, cudaStream_t st, Timer *tm = nullptr);
+int assemble_K_fp32(const DeviceMesh &m, float *K, size_t ld, cudaStream_t st, Timer *tm = nullptr);
 
 }  // namespace dsc

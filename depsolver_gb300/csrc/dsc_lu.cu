@@ -153,12 +153,12 @@ int lu_solve_augmented_fp64(int n, double *dA, size_t lda, int *bad_row, cudaStr
         const int j1 = std::min(n, j0 + kNB);
         for (int j = j0; j < j1; j++) {
             int rows = n - j - 1;
-            k_panel_col<<<std::max(1, (rows + 255) / 256), 256, 0, st>>>(dA, lda, n, j, j1, bad.p);
+            DSC_LAUNCH(k_panel_col<<<std::max(1, (rows + 255) / 256), 256, 0, st>>>(dA, lda, n, j, j1, bad.p));
         }
-        k_trsm_rows<<<(ncols - j1 + 127) / 128, 128, 0, st>>>(dA, lda, ncols, j0, j1);
+        DSC_LAUNCH(k_trsm_rows<<<(ncols - j1 + 127) / 128, 128, 0, st>>>(dA, lda, ncols, j0, j1));
         if (j1 < n) {
             dim3 g((ncols - j1 + 63) / 64, (n - j1 + 63) / 64);
-            k_gemm_update<<<g, 256, 0, st>>>(dA, lda, n, ncols, j0, j1);
+            DSC_LAUNCH(k_gemm_update<<<g, 256, 0, st>>>(dA, lda, n, ncols, j0, j1));
         }
         DSC_CUDA(cudaGetLastError());
     }
@@ -172,8 +172,8 @@ int lu_solve_augmented_fp64(int n, double *dA, size_t lda, int *bad_row, cudaStr
     }
     for (int j1 = n; j1 > 0; j1 -= kNB) {
         const int j0 = std::max(0, j1 - kNB);
-        k_back_block<<<1, 32, 0, st>>>(dA, lda, n, j0, j1);
-        if (j0 > 0) k_back_update<<<(j0 * 32 + 255) / 256, 256, 0, st>>>(dA, lda, n, j0, j1);
+        DSC_LAUNCH(k_back_block<<<1, 32, 0, st>>>(dA, lda, n, j0, j1));
+        if (j0 > 0) DSC_LAUNCH(k_back_update<<<(j0 * 32 + 255) / 256, 256, 0, st>>>(dA, lda, n, j0, j1));
         DSC_CUDA(cudaGetLastError());
     }
     return kOk;
@@ -181,7 +181,7 @@ int lu_solve_augmented_fp64(int n, double *dA, size_t lda, int *bad_row, cudaStr
 
 int lu_extract_solution(int n, const double *dA, size_t lda, double *dB, cudaStream_t st)
 {
-    k_copy_col<<<(n + 255) / 256, 256, 0, st>>>(dA, lda, n, dB);
+    DSC_LAUNCH(k_copy_col<<<(n + 255) / 256, 256, 0, st>>>(dA, lda, n, dB));
     DSC_CUDA(cudaGetLastError());
     return kOk;
 }

@@ -5,6 +5,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <numeric>
 
 #include "dsc_common.cuh"
@@ -14,6 +15,18 @@
 namespace dsc {
 
 static thread_local char g_err[512];
+static std::atomic<unsigned long long> g_launches{0};
+
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+}  // namespace dsc
+
+extern "C" unsigned long long dsc_kernel_launches(void)
+{
+    return dsc::g_launches.load(std::memory_order_relaxed);
+}
+
+namespace dsc {
 
 void set_error(const char *fmt, ...)
 {
@@ -271,6 +284,61 @@ std::vector<int> plan_coords_find(const HostPlan &p, double x, double y, double 
     }
     std::sort(out.begin(), out.end());
     return out;
+}
+
+cudaEvent_t Timer::take()
+{
+    if (!pool.empty()) {
+        cudaEvent_t e = pool.back();
+        pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+void Timer::begin(int id, cudaStream_t st)
+{
+    open_id = id;
+    open_a = take();
+    cudaEventRecord(open_a, st);
+}
+
+void Timer::end(cudaStream_t st)
+{
+    cudaEvent_t b = take();
+    cudaEventRecord(b, st);
+    recs.push_back({open_id, open_a, b});
+    open_id = -1;
+}
+
+int Timer::collect(double *ms, int *count)
+{
+    for (int k = 0; k < kTCount; k++) {
+        ms[k] = 0.0;
+        count[k] = 0;
+    }
+    for (auto &r : recs) {
+        DSC_CUDA(cudaEventSynchronize(r.b));
+        float t = 0.0f;
+        DSC_CUDA(cudaEventElapsedTime(&t, r.a, r.b));
+        ms[r.id] += t;
+        count[r.id] += 1;
+        pool.push_back(r.a);
+        pool.push_back(r.b);
+    }
+    recs.clear();
+    return kOk;
+}
+
+Timer::~Timer()
+{
+    for (auto &r : recs) {
+        pool.push_back(r.a);
+        pool.push_back(r.b);
+    }
+    for (auto e : pool) cudaEventDestroy(e);
 }
 
 int DeviceMesh::upload_rows(const HostPlan &p, cudaStream_t st)

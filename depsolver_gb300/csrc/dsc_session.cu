@@ -1,0 +1,351 @@
+// dsc_session.cu -- device-resident scenes and frequency sweeps.
+//
+// A session keeps one geometry in HBM: the mesh plan, the geometric matrix
+// K (assembled once, frequency independent) and the force plan.  Each
+// frequency f only changes per-row coefficients (src/assembly_el.c:223-256):
+//   M_f = diag(a - i b) K + diag(d),   a, b = A_k, B_k on interface rows,
+//   a = 1, b = 0 on conductor rows, d = -1/(2 eps0) on interface rows,
+// so a sweep assembles once and solves many systems.
+//
+// Plain FP64 path (DSC_MODE_FP64): per frequency, the reference's GMRES
+// (real 2N form, Jacobi row scaling with the real diagonal, MGS, Givens;
+// src/gmres_el.c:66-260) on the K-form operator
+//   y_re = a (K x_re) + d x_re + b (K x_im),  y_im = a (K x_im) + d x_im - b (K x_re)
+// whose K products are one FP64 GEMV with two right-hand sides, then the
+// FP64 field at the type-6 nodes and the Maxwell-stress force.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <complex>
+#include <memory>
+#include <vector>
+
+#include "../../include/depsolver_cuda.h"
+#include "dsc_blas.cuh"
+#include "dsc_common.cuh"
+#include "dsc_field.h"
+#include "dsc_gmres.h"
+#include "dsc_internal.h"
+#include "dsc_session.h"
+
+namespace dsc {
+
+// ---------------------------------------------------------------- kernels
+
+// part[s][0/1][i] = sum over the column split s of K[c][i] * x{re,im}[c];
+// K column-major; thread per row, x chunks staged in shared memory.
+template <typename T>
+__global__ void __launch_bounds__(256) k_gemv_K2(const T *__restrict__ K, size_t ld, int N,
+                                                 const double *__restrict__ xr,
+                                                 const double *__restrict__ xi, int cols,
+                                                 double *__restrict__ part)
+{
+    __shared__ double sxr[256], sxi[256];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = blockIdx.y;
+    const int c0 = s * cols, c1 = min(N, c0 + cols);
+    double ar = 0.0, ai = 0.0;
+    for (int cb = c0; cb < c1; cb += 256) {
+        __syncthreads();
+        if (cb + (int)threadIdx.x < c1) {
+            sxr[threadIdx.x] = xr[cb + threadIdx.x];
+            sxi[threadIdx.x] = xi[cb + threadIdx.x];
+        }
+        __syncthreads();
+        const int cn = min(256, c1 - cb);
+        if (i < N) {
+            const T *kp = K + (size_t)cb * ld + i;
+#pragma unroll 8
+            for (int c = 0; c < cn; c++) {
+                double k = (double)kp[(size_t)c * ld];
+                ar += k * sxr[c];
+                ai += k * sxi[c];
+            }
+        }
+    }
+    if (i < N) {
+        part[((size_t)s * 2) * N + i] = ar;
+        part[((size_t)s * 2 + 1) * N + i] = ai;
+    }
+}
+
+// y = K-form operator applied to x (real 2N layout), from the split sums.
+__global__ void k_kform_epilogue(const double *__restrict__ part, int S, int N,
+                                 const double *__restrict__ ca, const double *__restrict__ cb,
+                                 const double *__restrict__ cd, const double *__restrict__ x,
+                                 double *__restrict__ y)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    double tr = 0.0, ti = 0.0;
+    for (int s = 0; s < S; s++) {
+        tr += part[((size_t)s * 2) * N + i];
+        ti += part[((size_t)s * 2 + 1) * N + i];
+    }
+    const double a = ca[i], b = cb[i], d = cd[i];
+    y[i] = a * tr + d * x[i] + b * ti;
+    y[i + N] = a * ti + d * x[i + N] - b * tr;
+}
+
+__global__ void k_diag(const double *__restrict__ K, size_t ld, int N, double *__restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < N) out[i] = K[(size_t)i * ld + i];
+}
+
+// ---------------------------------------------------------------- operator
+
+struct KFormOp : RealOp {
+    const double *K = nullptr;
+    size_t ld = 0;
+    int N = 0, S = 1, cols = 0;
+    const double *ca = nullptr, *cb = nullptr, *cd = nullptr;
+    double *part = nullptr;
+    Timer *tm = nullptr;
+    int apply(const double *x, double *y, cudaStream_t st) override
+    {
+        {
+            TimerScope ts(tm, kTGemvK, st);
+            dim3 g((N + 255) / 256, S);
+            DSC_LAUNCH(k_gemv_K2<double><<<g, 256, 0, st>>>(K, ld, N, x, x + N, cols, part));
+        }
+        DSC_LAUNCH(k_kform_epilogue<<<(N + 255) / 256, 256, 0, st>>>(part, S, N, ca, cb, cd, x, y));
+        DSC_CUDA(cudaGetLastError());
+        return kOk;
+    }
+};
+
+// ---------------------------------------------------------------- session
+
+int Session::create(int nen_, unsigned N_, unsigned E_, const double *nodes, const unsigned *elems,
+                    const unsigned *bctype_, const double *mbc_, unsigned nIf_,
+                    const unsigned *ifaces_, unsigned nMat, const double *mat_)
+{
+    nen = nen_;
+    N = (int)N_;
+    E = (int)E_;
+    nIf = nIf_;
+    DSC_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    std::vector<int> e0((size_t)E * nen);
+    for (size_t t = 0; t < e0.size(); t++) e0[t] = (int)elems[t] - 1;
+    DSC_TRY(build_plan(nen, N, E, nodes, e0.data(), bctype_, plan));
+    bctype.assign(bctype_, bctype_ + 2 * (size_t)N);
+    mbc.assign(mbc_, mbc_ + 6 * (size_t)N);
+    ifaces.assign(ifaces_, ifaces_ + 2 * (size_t)nIf);
+    mat.assign(mat_, mat_ + 2 * (size_t)nMat);
+    for (unsigned i = 0; i < nIf; i++)
+        if (ifaces[2 * i] < 1 || ifaces[2 * i] > nMat || ifaces[2 * i + 1] < 1 || ifaces[2 * i + 1] > nMat) {
+            set_error("interface %u references a material outside 1..%u", i + 1, nMat);
+            return kErrArg;
+        }
+    iface_of_row.assign(N, -1);
+    for (int i = 0; i < N; i++)
+        if (plan.row_kind[i] == 1) {
+            unsigned k = (unsigned)mbc[3 * (size_t)i + 1] - 1;
+            if (k >= nIf) {
+                set_error("node %d: interface id %g outside 1..%u", i + 1, mbc[3 * (size_t)i + 1], nIf);
+                return kErrArg;
+            }
+            iface_of_row[i] = (int)k;
+        }
+    eps_medium = mat[1] * kEps0;
+    DSC_TRY(dev.upload(plan, st));
+    DSC_TRY(force.build(plan, bctype.data(), st));
+    ld = ((size_t)N + 31) / 32 * 32;
+    return kOk;
+}
+
+void destroy_mixed(Session::Mixed *m);
+
+Session::~Session()
+{
+    if (mx) destroy_mixed(mx);
+    if (st) cudaStreamDestroy(st);
+}
+
+int Session::assemble64()
+{
+    if (k64_ready) return kOk;
+    DSC_TRY(K64.alloc(ld * N));
+    DSC_TRY(assemble_K_fp64(dev, K64.p, ld, st, &timer));
+    DSC_TRY(Kdiag.alloc(N));
+    DSC_LAUNCH(k_diag<<<(N + 255) / 256, 256, 0, st>>>(K64.p, ld, N, Kdiag.p));
+    DSC_CUDA(cudaGetLastError());
+    Kdiag_host.resize(N);
+    DSC_CUDA(cudaMemcpyAsync(Kdiag_host.data(), Kdiag.p, N * sizeof(double), cudaMemcpyDeviceToHost, st));
+    DSC_CUDA(cudaStreamSynchronize(st));
+    k64_ready = true;
+    return kOk;
+}
+
+// Row coefficients at frequency f: a, b, d as above.
+void Session::coeffs(double f, std::vector<double> &a, std::vector<double> &b,
+                     std::vector<double> &d) const
+{
+    std::vector<double> Ak(nIf ? nIf : 1), Bk(nIf ? nIf : 1);
+    if (nIf) interface_coeffs(nIf, ifaces.data(), mat.data(), f, Ak.data(), Bk.data());
+    a.resize(N);
+    b.resize(N);
+    d.resize(N);
+    for (int i = 0; i < N; i++) {
+        if (iface_of_row[i] < 0) {
+            a[i] = 1.0;
+            b[i] = 0.0;
+            d[i] = 0.0;
+        } else {
+            a[i] = Ak[iface_of_row[i]];
+            b[i] = Bk[iface_of_row[i]];
+            d[i] = -0.5 / kEps0;
+        }
+    }
+}
+
+// One frequency on the plain FP64 path.  sigma_dev (2N) receives the
+// solution; d_tot (9) the force totals.
+int Session::solve_fp64(double f, double tol, unsigned max_iters, double *sigma_dev,
+                        double *d_tot, unsigned *iters)
+{
+    DSC_TRY(assemble64());
+    std::vector<double> a, b, d;
+    coeffs(f, a, b, d);
+    std::vector<double> B(2 * (size_t)N);
+    for (int i = 0; i < N; i++) {
+        B[i] = mbc[3 * (size_t)i];
+        B[i + N] = mbc[3 * (size_t)(i + N)];
+    }
+    // Jacobi scaling of the reference: row i (both halves) and B[i] (real
+    // part only) times 1 / A1[i][i] (src/gmres_el.c:87-93)
+    for (int i = 0; i < N; i++) {
+        double p = 1.0 / (a[i] * Kdiag_host[i] + d[i]);
+        a[i] *= p;
+        b[i] *= p;
+        d[i] *= p;
+        B[i] *= p;
+    }
+    DSC_TRY(ca.upload(a, st));
+    DSC_TRY(cb.upload(b, st));
+    DSC_TRY(cd.upload(d, st));
+    DSC_CUDA(cudaMemcpyAsync(sigma_dev, B.data(), B.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    KFormOp op;
+    op.K = K64.p;
+    op.ld = ld;
+    op.N = N;
+    int rowblocks = (N + 255) / 256;
+    op.S = std::max(1, std::min(64, 4 * 152 / rowblocks));
+    op.cols = (N + op.S - 1) / op.S;
+    op.ca = ca.p;
+    op.cb = cb.p;
+    op.cd = cd.p;
+    DSC_TRY(gemv_part.alloc((size_t)op.S * 2 * N));
+    op.part = gemv_part.p;
+    op.tm = &timer;
+    DSC_TRY(gmres_real_fp64(2 * N, op, sigma_dev, nullptr, tol, max_iters, nullptr, iters, st));
+    DSC_TRY(force_mst_dev(dev, force, sigma_dev, eps_medium, d_tot, st, &timer));
+    return kOk;
+}
+
+}  // namespace dsc
+
+// ================================================================ C ABI
+using namespace dsc;
+
+struct dsc_session {
+    Session s;
+};
+
+extern "C" int dsc_session_create(int nen, unsigned N, unsigned E, const double *nodes,
+                                  const unsigned *elems, const unsigned *bctype, const double *mbc,
+                                  unsigned nIf, const unsigned *ifaces, unsigned nMat,
+                                  const double *mat, dsc_session **out)
+{
+    *out = nullptr;
+    if ((nen != 3 && nen != 6) || !nodes || !elems || !bctype || !mbc || !mat || nMat == 0 ||
+        (nIf && !ifaces)) {
+        set_error("dsc_session_create: bad arguments");
+        return kErrArg;
+    }
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        set_error("no CUDA device available");
+        return kErrCuda;
+    }
+    auto s = std::make_unique<dsc_session>();
+    DSC_TRY(s->s.create(nen, N, E, nodes, elems, bctype, mbc, nIf, ifaces, nMat, mat));
+    *out = s.release();
+    return kOk;
+}
+
+extern "C" void dsc_session_destroy(dsc_session *s) { delete s; }
+
+extern "C" void *dsc_session_stream(dsc_session *s) { return (void *)s->s.st; }
+
+extern "C" int dsc_session_set_timing(dsc_session *s, int on)
+{
+    s->s.timer.on = on != 0;
+    return kOk;
+}
+
+extern "C" int dsc_session_timing(dsc_session *s, double *ms, int *count, int n)
+{
+    double t[kTCount];
+    int c[kTCount];
+    DSC_TRY(s->s.timer.collect(t, c));
+    for (int k = 0; k < n && k < kTCount; k++) {
+        ms[k] = t[k];
+        count[k] = c[k];
+    }
+    return kOk;
+}
+
+extern "C" int dsc_session_assemble(dsc_session *s)
+{
+    // always re-assemble: the caller asks for the work to be done now
+    s->s.k64_ready = false;
+    s->s.k32_ready = false;
+    return s->s.assemble64();
+}
+
+extern "C" int dsc_session_solve(dsc_session *sess, int mode, unsigned nfreq, const double *freqs,
+                                 double tol, unsigned max_iters, double *sigma, double *forces,
+                                 unsigned *iters)
+{
+    Session &s = sess->s;
+    if (mode != DSC_MODE_FP64 && mode != DSC_MODE_MIXED) {
+        set_error("dsc_session_solve: unknown mode %d", mode);
+        return kErrArg;
+    }
+    if (mode == DSC_MODE_MIXED) return s.solve_mixed(nfreq, freqs, tol, max_iters, sigma, forces, iters);
+    const size_t n2 = 2 * (size_t)s.N;
+    DevBuf<double> sig, tot;
+    DSC_TRY(sig.alloc(n2));
+    DSC_TRY(tot.alloc(9 * (size_t)std::max(1u, nfreq)));
+    for (unsigned k = 0; k < nfreq; k++) {
+        unsigned it = 0;
+        int rc = s.solve_fp64(freqs[k], tol, max_iters, sig.p, tot.p + 9 * (size_t)k, &it);
+        if (iters) iters[k] = it;
+        if (rc != kOk) return rc;
+        if (sigma)
+            DSC_CUDA(cudaMemcpyAsync(sigma + n2 * k, sig.p, n2 * sizeof(double), cudaMemcpyDeviceToHost,
+                                     s.st));
+    }
+    if (forces)
+        DSC_CUDA(cudaMemcpyAsync(forces, tot.p, 9 * (size_t)nfreq * sizeof(double),
+                                 cudaMemcpyDeviceToHost, s.st));
+    DSC_CUDA(cudaStreamSynchronize(s.st));
+    return kOk;
+}
+
+extern "C" int dsc_sweep(int nen, unsigned N, unsigned E, const double *nodes, const unsigned *elems,
+                         const unsigned *bctype, const double *mbc, unsigned nIf,
+                         const unsigned *ifaces, unsigned nMat, const double *mat, int mode,
+                         unsigned nfreq, const double *freqs, double tol, unsigned max_iters,
+                         double *sigma, double *forces, unsigned *iters)
+{
+    dsc_session *s = nullptr;
+    DSC_TRY(dsc_session_create(nen, N, E, nodes, elems, bctype, mbc, nIf, ifaces, nMat, mat, &s));
+    int rc = dsc_session_solve(s, mode, nfreq, freqs, tol, max_iters, sigma, forces, iters);
+    dsc_session_destroy(s);
+    return rc;
+}

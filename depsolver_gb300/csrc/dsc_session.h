@@ -1,0 +1,52 @@
+// dsc_session.h -- device-resident scene of libdepsolver_cuda (not exported).
+#pragma once
+
+#include <vector>
+
+#include "dsc_field.h"
+#include "dsc_internal.h"
+
+namespace dsc {
+
+struct Session {
+    int nen = 6, N = 0, E = 0;
+    unsigned nIf = 0;
+    cudaStream_t st = nullptr;
+    HostPlan plan;
+    DeviceMesh dev;
+    ForcePlan force;
+    Timer timer;
+    std::vector<unsigned> bctype, ifaces;
+    std::vector<double> mbc, mat;
+    std::vector<int> iface_of_row;
+    double eps_medium = 0.0;
+    size_t ld = 0;
+
+    // FP64 geometric matrix and its diagonal
+    bool k64_ready = false;
+    DevBuf<double> K64, Kdiag;
+    std::vector<double> Kdiag_host;
+    // plain FP64 path workspace
+    DevBuf<double> ca, cb, cd, gemv_part;
+
+    // mixed path: FP32 copy of K and batched-solver workspace
+    bool k32_ready = false;
+    DevBuf<float> K32;
+    struct Mixed;
+    Mixed *mx = nullptr;
+
+    int create(int nen, unsigned N, unsigned E, const double *nodes, const unsigned *elems,
+               const unsigned *bctype, const double *mbc, unsigned nIf, const unsigned *ifaces,
+               unsigned nMat, const double *mat);
+    ~Session();
+    int assemble64();
+    int make_k32();
+    void coeffs(double f, std::vector<double> &a, std::vector<double> &b,
+                std::vector<double> &d) const;
+    int solve_fp64(double f, double tol, unsigned max_iters, double *sigma_dev, double *d_tot,
+                   unsigned *iters);
+    int solve_mixed(unsigned nfreq, const double *freqs, double tol, unsigned max_iters,
+                    double *sigma_host, double *forces_host, unsigned *iters);
+};
+
+}  // namespace dsc

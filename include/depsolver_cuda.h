@@ -106,6 +106,9 @@ const char *dsc_last_error(void);
 /* Number of CUDA devices visible (0 when none; no error). */
 int dsc_device_count(void);
 
+/* Running total of kernels this library has launched in this process. */
+unsigned long long dsc_kernel_launches(void);
+
 /* Flat form of electricFormA_* (full = 0; A is N x 2N) and
  * electricFormFullA_* (full = 1; A is 2N x 2N); rows of A are lda doubles
  * apart and receive A += assembled values; B (2N) = boundary values.
@@ -140,6 +143,59 @@ int dsc_potential_points(int nen, unsigned N, unsigned E, const double *nodes,
 int dsc_force_mst(int nen, unsigned N, unsigned E, const double *nodes, const unsigned *elems,
                   const unsigned *bctype, const double *vB, double eps, double *Fce, double *Xce,
                   double *Fcm, double *Xcm);
+
+/* ------------------------------------------------------- sessions / sweeps
+ * No counterpart call in the reference: depSolver solves one (geometry,
+ * frequency) system per process run (src/depSolver.c:52-427) and a position
+ * sweep is many runs of depSolver-sft (src/depSolver-shift.c:212-217).  A
+ * session keeps one geometry in GPU memory: the frequency-independent
+ * geometric matrix is assembled once and every frequency only rescales its
+ * rows (the interface coefficients of src/assembly_el.c:223-239), so a
+ * sweep solves many systems per assembly.
+ *
+ * Modes:
+ *   DSC_MODE_FP64  -- the reference's algorithm in FP64: its GMRES (real
+ *                     2N form, Jacobi scaling, modified Gram-Schmidt, at
+ *                     tolerance `tol`) one frequency at a time, FP64 field
+ *                     and Maxwell-stress force.
+ *   DSC_MODE_MIXED -- all frequencies at once: complex GMRES whose matrix
+ *                     products run on an FP32 copy of the matrix, FP64
+ *                     Arnoldi, FP64-residual iterative refinement to `tol`
+ *                     (relative residual), batched field and force.
+ * forces receives 9 doubles per frequency: Fcm[3], Xcm[3] and the sum over
+ * particle elements of |Fce| per component (the scale of the net force).
+ * sigma (may be NULL) receives 2N doubles per frequency (Re then Im).
+ * iters (may be NULL) receives the iteration count per frequency. */
+#define DSC_MODE_FP64 1
+#define DSC_MODE_MIXED 2
+
+typedef struct dsc_session dsc_session;
+
+int dsc_session_create(int nen, unsigned N, unsigned E, const double *nodes, const unsigned *elems,
+                       const unsigned *bctype, const double *mbc, unsigned nIf,
+                       const unsigned *ifaces, unsigned nMat, const double *mat,
+                       dsc_session **out);
+void dsc_session_destroy(dsc_session *s);
+/* Assembles the FP64 geometric matrix now, again if it already exists
+ * (otherwise it is assembled on the first solve and then reused). */
+int dsc_session_assemble(dsc_session *s);
+int dsc_session_solve(dsc_session *s, int mode, unsigned nfreq, const double *freqs, double tol,
+                      unsigned max_iters, double *sigma, double *forces, unsigned *iters);
+/* CUDA-event timing of kernel classes (off by default): ms[k] and launch
+ * counts since the last call, k = 0 assembly regular pairs, 1 assembly
+ * fix-up, 2 assembly singular pairs, 3 FP64 K GEMV, 4 K GEMM (mixed),
+ * 5 field, 6 Maxwell stress, 7 FP64 residual GEMM, 8 Krylov updates. */
+int dsc_session_set_timing(dsc_session *s, int on);
+/* The CUDA stream (cudaStream_t) all of the session's work runs on, so a
+ * caller can record its own events around a solve. */
+void *dsc_session_stream(dsc_session *s);
+int dsc_session_timing(dsc_session *s, double *ms, int *count, int n);
+
+/* One-call sweep from host arrays (session created and destroyed inside). */
+int dsc_sweep(int nen, unsigned N, unsigned E, const double *nodes, const unsigned *elems,
+              const unsigned *bctype, const double *mbc, unsigned nIf, const unsigned *ifaces,
+              unsigned nMat, const double *mat, int mode, unsigned nfreq, const double *freqs,
+              double tol, unsigned max_iters, double *sigma, double *forces, unsigned *iters);
 
 #ifdef __cplusplus
 }

@@ -91,6 +91,8 @@ class Port:
         L.orc_intSingularG.argtypes = [C.c_int, C.c_uint, _dp, _dp, _dp]
         L.orc_intSingularH.argtypes = [C.c_int, C.c_uint, C.c_uint, _dp, _dp, _dp, _dp]
         L.orc_interface_coeffs.argtypes = [C.c_uint, C.c_void_p, C.c_void_p, C.c_double, _dp, _dp]
+        L.orc_matvec_rows.restype = None
+        L.orc_matvec_rows.argtypes = [C.c_uint, C.c_void_p, _dp, _dp, C.c_uint, C.c_uint, C.c_int]
 
     # -- assembly -------------------------------------------------------
     def assemble(self, sc, full: bool = False, rows=None, nthreads: int = 1):

@@ -91,6 +91,11 @@ int orc_gmres(unsigned N, unsigned preCond, double tol_rel, unsigned max_iters,
               double *A, double *B, const double *x0, FILE *log, int nthreads,
               unsigned *iters);
 
+/* Rows [r0, r1) of y = (A1 - i A2) x on the compact form; A holds the
+ * rows from r0 on (row r at A + (r - r0) * 2N), y is 2N long. */
+void orc_matvec_rows(unsigned N, const double *A, const double *x, double *y, unsigned r0,
+                     unsigned r1, int nthreads);
+
 /* Field and potential at a point (src/field.c:57-200,
  * src/potential.c:55-179).  mE[0..5] = Re Ex, Im Ex, Re Ey, Im Ey, Re Ez,
  * Im Ez; mPot[0..1] = Re, Im. */

@@ -60,6 +60,7 @@ struct mv_job {
     unsigned N, r0, r1;
     const double *A, *x;
     double *y;
+    unsigned aoff;  /* first row held in A */
 };
 
 /* y = (A1 - i A2) x on the compact N x 2N form, rows [r0, r1)
@@ -68,7 +69,7 @@ static void matvec_rows(const struct mv_job *j)
 {
     const unsigned N = j->N;
     for (unsigned i = j->r0; i < j->r1; i++) {
-        const double *a = j->A + (size_t)i * 2 * N;
+        const double *a = j->A + (size_t)(i - j->aoff) * 2 * N;
         double yr = 0.0, yi = 0.0;
         for (unsigned c = 0; c < N; c++) {
             yr += a[c] * j->x[c] + a[c + N] * j->x[c + N];
@@ -100,6 +101,29 @@ static void matvec(unsigned N, const double *A, const double *x, double *y, int 
         unsigned r0 = (unsigned)t * per, r1 = r0 + per < N ? r0 + per : N;
         if (r0 > N) r0 = N;
         jobs[t] = (struct mv_job){N, r0, r1, A, x, y};
+        pthread_create(&th[t], NULL, mv_thread, &jobs[t]);
+    }
+    for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+}
+
+/* Rows [r0, r1) of the compact-form product (used to time a sample of the
+ * GMRES matrix-vector product). */
+void orc_matvec_rows(unsigned N, const double *A, const double *x, double *y, unsigned r0,
+                     unsigned r1, int nthreads)
+{
+    if (nthreads <= 1) {
+        struct mv_job j = {N, r0, r1, A, x, y, r0};
+        matvec_rows(&j);
+        return;
+    }
+    struct mv_job jobs[256];
+    pthread_t th[256];
+    if (nthreads > 256) nthreads = 256;
+    unsigned n = r1 - r0, per = (n + (unsigned)nthreads - 1) / (unsigned)nthreads;
+    for (int t = 0; t < nthreads; t++) {
+        unsigned a = r0 + (unsigned)t * per, b = a + per < r1 ? a + per : r1;
+        if (a > r1) a = r1;
+        jobs[t] = (struct mv_job){N, a, b, A, x, y, r0};
         pthread_create(&th[t], NULL, mv_thread, &jobs[t]);
     }
     for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);

@@ -1,0 +1,69 @@
+"""Frequency sweeps on a device-resident scene (dsc_session_* / dsc_sweep).
+
+The plain FP64 path must reproduce the reference's GMRES (through the
+strict compact path and the checker); the mixed path must reach the FP64
+solution: nodal solution within 1e-9 relative and Maxwell-stress force within
+1e-6 of the force scale (sum over particle elements of |Fce|).
+"""
+import numpy as np
+import pytest
+
+from conftest import relerr
+from depsolver_gb300 import api, scenes
+
+pytestmark = pytest.mark.gpu
+
+FORCE_TOL = 1e-6   # |Fcm_mixed - Fcm_fp64| / sum|Fce|
+
+
+@pytest.mark.parametrize("nen", [6, 3])
+def test_fp64_session_matches_reference_gmres(gpu, port, nen):
+    sc = scenes.small(nen=nen)
+    s = api.Session(sc)
+    forces, its, sig = s.solve([sc.freq], mode=api.MODE_FP64, tol=1e-6, want_sigma=True)
+    Ap, Bp = port.assemble(sc)
+    xp, itp, st = port.gmres(Ap, Bp)
+    assert st == 0 and its[0] == itp
+    assert relerr(sig[0], xp) < 1e-10
+    Fce, Xce, Fcm, Xcm = port.force_mst(sc, xp)
+    pel = sc.bctype[sc.elems[:, 0] - 1] == 6
+    assert np.abs(forces[0, :3] - Fcm).max() <= 1e-9 * np.abs(Fce[pel]).sum()
+    assert relerr(forces[0, 3:6], Xcm) < 1e-13
+    assert np.allclose(forces[0, 6:9], np.abs(Fce[pel]).sum(0), rtol=1e-9)
+
+
+@pytest.mark.parametrize("nen", [6, 3])
+def test_mixed_matches_fp64_across_frequencies(gpu, port, nen):
+    sc = scenes.small(nen=nen, sphere_level=2, plate_cells=4)
+    freqs = np.logspace(3, 8, 6)
+    s = api.Session(sc)
+    f64, it64, s64 = s.solve(freqs, mode=api.MODE_FP64, tol=1e-12, want_sigma=True)
+    fmx, itmx, smx = s.solve(freqs, mode=api.MODE_MIXED, tol=1e-11, want_sigma=True)
+    for k in range(len(freqs)):
+        assert relerr(smx[k], s64[k]) < 1e-9, k
+        scale = f64[k, 6:9].sum()
+        assert np.abs(fmx[k, :3] - f64[k, :3]).max() <= FORCE_TOL * scale, k
+    # the reference's own solution at one frequency, by the checker
+    scf = sc.with_freq(freqs[2])
+    Ap, Bp = port.assemble(scf)
+    xp, _, st = port.gmres(Ap, Bp, tol=1e-12)
+    assert st == 0 and relerr(smx[2], xp) < 1e-9
+
+
+def test_sweep_equals_session(gpu):
+    sc = scenes.small(nen=6)
+    freqs = [1e4, 1e6, 5e7]
+    f1, _, s1 = api.sweep(sc, freqs, mode=api.MODE_MIXED, tol=1e-11)
+    s = api.Session(sc)
+    f2, _, s2 = s.solve(freqs, mode=api.MODE_MIXED, tol=1e-11, want_sigma=True)
+    assert np.array_equal(s1, s2) and np.array_equal(f1, f2)
+
+
+def test_session_timing_counts_kernels(gpu):
+    sc = scenes.small(nen=6)
+    s = api.Session(sc)
+    s.set_timing(True)
+    s.solve([1e6], mode=api.MODE_FP64, tol=1e-6)
+    t = s.timing()
+    assert t["asm_regular"][1] >= 1 and t["gemv_K64"][1] >= 5 and t["field"][1] == 1
+    assert all(ms >= 0 for ms, _ in t.values())
