@@ -25,6 +25,7 @@
 #include "dsc_internal.h"
 #include "dsc_session.h"
 #include "dsc_singular.cuh"
+#include "dsc_tcgemm.h"
 
 namespace dsc {
 
@@ -463,9 +464,11 @@ __global__ void k_mst_batched_totals(const double *__restrict__ Fce, int npel, i
 // ------------------------------------------------------------ workspace
 
 struct Session::Mixed {
-    int F = 0;
+    int F = 0, S = 1;
     DevBuf<double> Vb;      // (kInnerMax + 1) blocks of N x 2F (FP64)
-    DevBuf<float> V32, Y32; // FP32 GEMM operand / product
+    DevBuf<float> Vh, Vl;   // tf32 pair of the current Krylov block
+    DevBuf<float> Yp;       // split-K partial products, S blocks
+    DevBuf<int> err;        // set by the tensor-core kernel when a wait gives up
     DevBuf<double> W, Xs, R, Y64;
     DevBuf<double2> cs, cd, bt, h, hacc, ycoef;
     DevBuf<double> nrm, scale;
@@ -478,11 +481,31 @@ int Session::make_k32()
 {
     if (k32_ready) return kOk;
     DSC_TRY(assemble64());
-    DSC_TRY(K32.alloc(ld * N));
-    DSC_LAUNCH(k_k_to_float<<<4 * 152, 256, 0, st>>>(K64.p, K32.p, ld * (size_t)N));
-    DSC_CUDA(cudaGetLastError());
+    DSC_TRY(Kth.alloc(ld * N));
+    DSC_TRY(Ktl.alloc(ld * N));
+    DSC_TRY(split_transpose_K(K64.p, ld, N, Kth.p, Ktl.p, ld, st));
     k32_ready = true;
     return kOk;
+}
+
+// w_f = cs_f o (sum of the split partials of K v)_f + cd_f o v_f
+__global__ void k_apply_epilogue_splits(const float *__restrict__ P, int S, size_t split_stride,
+                                        const double *__restrict__ V, const double2 *__restrict__ cs,
+                                        const double2 *__restrict__ cd, double *__restrict__ W, int N,
+                                        size_t ld, int F)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int f = blockIdx.y;
+    if (i >= N || f >= F) return;
+    double yr = 0.0, yi = 0.0;
+    for (int s = 0; s < S; s++) {
+        yr += (double)P[(size_t)s * split_stride + (size_t)(2 * f) * ld + i];
+        yi += (double)P[(size_t)s * split_stride + (size_t)(2 * f + 1) * ld + i];
+    }
+    const double vr = V[(size_t)(2 * f) * ld + i], vi = V[(size_t)(2 * f + 1) * ld + i];
+    const double2 s = cs[(size_t)f * N + i], d = cd[(size_t)f * N + i];
+    W[(size_t)(2 * f) * ld + i] = s.x * yr - s.y * yi + d.x * vr - d.y * vi;
+    W[(size_t)(2 * f + 1) * ld + i] = s.x * yi + s.y * yr + d.x * vi + d.y * vr;
 }
 
 template <typename TA, typename TB, typename TC>
@@ -585,11 +608,13 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
             double *vn = w.Vb.p + (size_t)(j + 1) * blk;
             {
                 TimerScope ts(tm, kTGemmK, st);
-                DSC_LAUNCH(k_to_float<<<4 * 152, 256, 0, st>>>(vj, w.V32.p, blk));
-                DSC_TRY((gemm<float, float, float>(s.K32.p, ld, w.V32.p, ld, w.Y32.p, ld, N, 2 * F, N, st)));
+                DSC_TRY(split_vec(vj, w.Vh.p, w.Vl.p, blk, st));
+                DSC_TRY(tc_gemm_3xtf32(s.Kth.p, s.Ktl.p, ld, w.Vh.p, w.Vl.p, ld, N, 2 * F, N, w.Yp.p, ld,
+                                       w.S, w.err.p, st));
             }
             TimerScope ts(tm, kTKrylov, st);
-            DSC_LAUNCH(k_apply_epilogue<float><<<vg, 256, 0, st>>>(w.Y32.p, vj, w.cs.p, w.cd.p, w.W.p, N, ld, F));
+            DSC_LAUNCH(k_apply_epilogue_splits<<<vg, 256, 0, st>>>(w.Yp.p, w.S, ld * 2 * (size_t)F, vj, w.cs.p,
+                                                                   w.cd.p, w.W.p, N, ld, F));
             DSC_CUDA(cudaMemsetAsync(w.hacc.p, 0, (size_t)(j + 1) * F * sizeof(double2), st));
             for (int pass = 0; pass < 2; pass++) {
                 DSC_LAUNCH(k_cgs_dots<<<dim3(F, j + 1), 256, 0, st>>>(w.Vb.p, blk, w.W.p, N, ld, F, w.active.p, w.h.p));
@@ -678,6 +703,15 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
     if (iters)
         for (int f = 0; f < F; f++) iters[f] = (unsigned)total_it[f];
     (void)max_iters;
+    {
+        int herr = 0;
+        DSC_CUDA(cudaMemcpyAsync(&herr, w.err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        DSC_CUDA(cudaStreamSynchronize(st));
+        if (herr) {
+            set_error("tensor-core GEMM: a pipeline wait gave up (code %d)", herr);
+            return kErrCuda;
+        }
+    }
 
     // ---- batched field at the particle nodes and Maxwell-stress force
     ForcePlan &fp = s.force;
@@ -758,8 +792,12 @@ int Session::solve_mixed(unsigned nfreq, const double *freqs, double tol, unsign
     if (w.F < Fmax) {
         const size_t blk = ld * 2 * (size_t)Fmax;
         DSC_TRY(w.Vb.alloc(blk * (kInnerMax + 1)));
-        DSC_TRY(w.V32.alloc(blk));
-        DSC_TRY(w.Y32.alloc(blk));
+        w.S = tc_gemm_splits_for(N, N);
+        DSC_TRY(w.Vh.alloc(blk));
+        DSC_TRY(w.Vl.alloc(blk));
+        DSC_TRY(w.Yp.alloc(blk * w.S));
+        DSC_TRY(w.err.alloc(1));
+        DSC_CUDA(cudaMemsetAsync(w.err.p, 0, sizeof(int), st));
         DSC_TRY(w.W.alloc(blk));
         DSC_TRY(w.Xs.alloc(blk));
         DSC_TRY(w.R.alloc(blk));

@@ -29,9 +29,10 @@ struct Session {
     // plain FP64 path workspace
     DevBuf<double> ca, cb, cd, gemv_part;
 
-    // mixed path: FP32 copy of K and batched-solver workspace
+    // mixed path: K as row-major tf32 pairs (Kth + Ktl) for the tensor-core
+    // products, and the batched-solver workspace
     bool k32_ready = false;
-    DevBuf<float> K32;
+    DevBuf<float> Kth, Ktl;
     struct Mixed;
     Mixed *mx = nullptr;
 

@@ -1,0 +1,478 @@
+// dsc_tcgemm.cu -- split-K 3xTF32 GEMM on the 5th-generation tensor cores.
+//
+//   Y[s] (Nc x M, per split s) = sum over the k-range of split s of
+//       A (M x Kd) * B^T,   A = Ah + Al,  B = Bh + Bl (tf32 pairs)
+//   with the three products Ah Bh + Ah Bl + Al Bh: about FP32 accuracy.
+//
+// A and B are K-major FP32 (row m of A and row n of B hold consecutive k).
+// One CTA computes a 128-row tile of one split: warp 0 lane 0 streams
+// 128-byte-wide k-blocks of Ah, Al, Bh, Bl into a 3-stage shared-memory ring
+// with TMA (128B swizzle), warp 1 lane 0 issues tcgen05.mma (kind::tf32,
+// M = 128, N = BN, K = 8) into an FP32 accumulator in tensor memory and
+// releases each stage with tcgen05.commit, and all four warps read the
+// accumulator back (tcgen05.ld, one TMEM lane per row) and store the
+// partial tile.  Every wait on an mbarrier gives up after ~2 s of clock,
+// sets *err and lets the CTA drain and free its tensor memory.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include "dsc_internal.h"
+#include "dsc_tcgemm.h"
+
+namespace dsc {
+
+constexpr int kTcBM = 128;
+constexpr int kTcBK = 32;          // fp32 elements per k-block = one 128-byte swizzle row
+constexpr int kTcStages = 3;
+constexpr long long kTcSpin = 4000000000LL;  // clock cycles before a wait gives up
+
+__device__ __forceinline__ uint32_t su32(const void *p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *b, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(b)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *b, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(b)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint64_t *b, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(su32(b)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait for the phase of parity `parity`; false (and *err = code)
+// after kTcSpin cycles or when another thread has already failed.
+__device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, int *err, int code)
+{
+    const long long t0 = clock64();
+    while (!mbar_try(b, parity)) {
+        if (*(volatile int *)err) return false;
+        if (clock64() - t0 > kTcSpin) {
+            atomicCAS(err, 0, code);
+            return false;
+        }
+    }
+    return true;
+}
+
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar, int x,
+                                            int y)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%3, %4}], [%2];" ::"r"(su32(dst)),
+        "l"((uint64_t)map), "r"(su32(bar)), "r"(x), "r"(y)
+        : "memory");
+}
+
+// Shared-memory matrix descriptor of a K-major tile in the 128B-swizzled
+// canonical layout: rows of 128 bytes, 8-row groups 1024 bytes apart.
+__device__ __forceinline__ uint64_t sw128_desc(const void *tile)
+{
+    const uint64_t a = su32(tile);
+    uint64_t d = (a >> 4) & 0x3FFFull;        // start address
+    d |= (uint64_t)1 << 16;                   // leading byte offset (unused when swizzled)
+    d |= (uint64_t)(1024 >> 4) << 32;         // stride byte offset: 8 rows x 128 B
+    d |= (uint64_t)1 << 46;                   // descriptor version
+    d |= (uint64_t)2 << 61;                   // 128-byte swizzle
+    return d;
+}
+
+// Instruction descriptor: D f32, A and B tf32, both K-major, N x M shape.
+__host__ __device__ constexpr uint32_t idesc_tf32(int n, int m)
+{
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) |
+           ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t acc)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t *bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     su32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before()
+{
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tc_fence_after()
+{
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// 32 consecutive accumulator columns of this warp's 32 TMEM lanes.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t *r)
+{
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+          "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+          "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+          "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(128, 1)
+    k_tc_gemm_3xtf32(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
+                     const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl,
+                     int M, int Nc, int BN, int nkb_total, int kb_per_split, float *__restrict__ Y,
+                     size_t ldy, size_t split_stride, int tmem_cols, int *err)
+{
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const uint32_t a_bytes = kTcBM * 128, b_bytes = (uint32_t)BN * 128;
+    const uint32_t stage_bytes = 2 * a_bytes + 2 * b_bytes;
+    uint64_t *full = (uint64_t *)(smem + kTcStages * stage_bytes);
+    uint64_t *empty = full + kTcStages;
+    uint64_t *accum = empty + kTcStages;
+    uint32_t *tmem_slot = (uint32_t *)(accum + 1);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.x * kTcBM, split = blockIdx.y;
+    const int kb0 = split * kb_per_split;
+    const int nkb = max(0, min(nkb_total, kb0 + kb_per_split) - kb0);
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kTcStages; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(accum, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         su32(tmem_slot)),
+                     "r"(tmem_cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0 && lane == 0 && nkb > 0) {
+        // ---- producer
+        int issued = 0;
+        for (int i = 0; i < nkb; i++) {
+            const int s = i % kTcStages;
+            if (i >= kTcStages && !mbar_wait(&empty[s], ((i / kTcStages) - 1) & 1, err, 1)) break;
+            uint8_t *st = smem + s * stage_bytes;
+            mbar_expect_tx(&full[s], stage_bytes);
+            const int kx = (kb0 + i) * kTcBK;
+            tma_load_2d(st, &tmAh, &full[s], kx, m0);
+            tma_load_2d(st + a_bytes, &tmAl, &full[s], kx, m0);
+            tma_load_2d(st + 2 * a_bytes, &tmBh, &full[s], kx, 0);
+            tma_load_2d(st + 2 * a_bytes + b_bytes, &tmBl, &full[s], kx, 0);
+            issued = i + 1;
+        }
+        // drain: the last loads of every stage have landed before the CTA
+        // may exit (immediate in the normal path, bounded otherwise)
+        for (int i = max(0, issued - kTcStages); i < issued; i++) {
+            const long long t0 = clock64();
+            while (!mbar_try(&full[i % kTcStages], (i / kTcStages) & 1) && clock64() - t0 < kTcSpin) {
+            }
+        }
+    } else if (warp == 1 && lane == 0 && nkb > 0) {
+        // ---- MMA issuer
+        const uint32_t idesc = idesc_tf32(BN, kTcBM);
+        for (int i = 0; i < nkb; i++) {
+            const int s = i % kTcStages;
+            if (!mbar_wait(&full[s], (i / kTcStages) & 1, err, 2)) break;
+            tc_fence_after();
+            uint8_t *st = smem + s * stage_bytes;
+            const uint64_t dah = sw128_desc(st), dal = sw128_desc(st + a_bytes);
+            const uint64_t dbh = sw128_desc(st + 2 * a_bytes), dbl = sw128_desc(st + 2 * a_bytes + b_bytes);
+#pragma unroll
+            for (int kk = 0; kk < kTcBK / 8; kk++) {
+                const uint64_t off = (uint64_t)(kk * 32) >> 4;  // 8 tf32 = 32 bytes
+                mma_tf32(tmem, dal + off, dbh + off, idesc, (i | kk) != 0);
+                mma_tf32(tmem, dah + off, dbl + off, idesc, 1);
+                mma_tf32(tmem, dah + off, dbh + off, idesc, 1);
+            }
+            mma_commit(&empty[s]);
+        }
+        mma_commit(accum);
+    }
+    __syncwarp();
+
+    // ---- epilogue: TMEM lanes 32w .. 32w + 31 = rows of this warp
+    bool have = nkb > 0;
+    if (have) have = mbar_wait(accum, 0, err, 3);
+    // tcgen05.ld is warp-collective: the whole warp reads or none of it
+    have = __all_sync(0xffffffffu, have);
+    tc_fence_after();
+    const int m = m0 + warp * 32 + lane;
+    float *Ys = Y + (size_t)split * split_stride;
+    for (int c0 = 0; c0 < BN; c0 += 32) {
+        uint32_t r[32];
+        if (have) {
+            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, r);
+        } else {
+#pragma unroll
+            for (int j = 0; j < 32; j++) r[j] = 0u;
+        }
+        if (m < M) {
+#pragma unroll
+            for (int j = 0; j < 32; j++) {
+                const int n = c0 + j;
+                if (n < Nc) Ys[(size_t)n * ldy + m] = __uint_as_float(r[j]);
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tmem_cols)
+                     : "memory");
+}
+
+// ---------------------------------------------------------------- host
+
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
+}
+
+// 2-D FP32 tensor: rows x k (k contiguous, row stride ld elements), boxes
+// of 32 k x box_rows rows, 128-byte swizzle, zero fill outside.
+static int make_map(CUtensorMap *map, const float *base, int rows, int k, size_t ld, int box_rows)
+{
+    auto fn = encode_fn();
+    if (!fn) {
+        set_error("cuTensorMapEncodeTiled is not available");
+        return kErrCuda;
+    }
+    if (((uintptr_t)base & 15) || ((ld * sizeof(float)) & 15)) {
+        set_error("TMA operand not 16-byte aligned");
+        return kErrArg;
+    }
+    cuuint64_t dims[2] = {(cuuint64_t)k, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)(ld * sizeof(float))};
+    cuuint32_t box[2] = {(cuuint32_t)kTcBK, (cuuint32_t)box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)base, dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+        return kErrCuda;
+    }
+    return kOk;
+}
+
+int tc_gemm_3xtf32(const float *Ah, const float *Al, size_t lda, const float *Bh, const float *Bl,
+                   size_t ldb, int M, int Nc, int Kd, float *Y, size_t ldy, int splits, int *d_err,
+                   cudaStream_t st)
+{
+    if (Nc < 1 || Nc > 256 || M < 1 || Kd < 1 || ldy < (size_t)M) {
+        set_error("tc_gemm_3xtf32: unsupported shape M %d Nc %d Kd %d", M, Nc, Kd);
+        return kErrArg;
+    }
+    const int BN = (Nc + 15) / 16 * 16;
+    const int tmem_cols = BN <= 32 ? 32 : BN <= 64 ? 64 : BN <= 128 ? 128 : 256;
+    CUtensorMap ah, al, bh, bl;
+    DSC_TRY(make_map(&ah, Ah, M, Kd, lda, kTcBM));
+    DSC_TRY(make_map(&al, Al, M, Kd, lda, kTcBM));
+    DSC_TRY(make_map(&bh, Bh, Nc, Kd, ldb, BN));
+    DSC_TRY(make_map(&bl, Bl, Nc, Kd, ldb, BN));
+    const int nkb = (Kd + kTcBK - 1) / kTcBK;
+    splits = std::max(1, std::min(splits, nkb));
+    const int kps = (nkb + splits - 1) / splits;
+    splits = (nkb + kps - 1) / kps;  // every split has at least one k-block
+    const size_t smem = 1024 + (size_t)kTcStages * (2 * kTcBM * 128 + 2 * BN * 128) + 256;
+    DSC_CUDA(cudaFuncSetAttribute(k_tc_gemm_3xtf32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid((M + kTcBM - 1) / kTcBM, splits);
+    DSC_LAUNCH(k_tc_gemm_3xtf32<<<grid, 128, smem, st>>>(ah, al, bh, bl, M, Nc, BN, nkb, kps, Y, ldy,
+                                                        ldy * (size_t)Nc, tmem_cols, d_err));
+    DSC_CUDA(cudaGetLastError());
+    return kOk;
+}
+
+int tc_gemm_splits_for(int M, int Kd)
+{
+    const int tiles = (M + kTcBM - 1) / kTcBM;
+    const int nkb = (Kd + kTcBK - 1) / kTcBK;
+    // about eleven waves of one CTA per SM, at least four k-blocks per split;
+    // normalised exactly as tc_gemm_3xtf32 does, so callers can size buffers
+    int s = std::max(1, (11 * 152) / std::max(1, tiles));
+    s = std::max(1, std::min(s, nkb / 4));
+    s = std::min(s, nkb);
+    const int kps = (nkb + s - 1) / s;
+    return (nkb + kps - 1) / kps;
+}
+
+// ---------------------------------------------------------- operand split
+// tf32 pair of a value: hi = round-to-nearest tf32, lo = value - hi.
+__device__ __forceinline__ void tf32_split(double v, float &hi, float &lo)
+{
+    float f = (float)v;
+    uint32_t h;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(f));
+    hi = __uint_as_float(h);
+    lo = (float)(v - (double)hi);
+}
+
+// Column-major FP64 K (entry (i, c) at c * ld + i) to row-major tf32 pairs
+// (entry (i, c) at i * ldt + c): a 32 x 32 shared tile per block.
+__global__ void k_split_transpose(const double *__restrict__ K, size_t ld, int N,
+                                  float *__restrict__ Th, float *__restrict__ Tl, size_t ldt)
+{
+    __shared__ double t[32][33];
+    const int i0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        int c = c0 + k, i = i0 + threadIdx.x;
+        t[k][threadIdx.x] = (c < N && i < N) ? K[(size_t)c * ld + i] : 0.0;
+    }
+    __syncthreads();
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        int i = i0 + k, c = c0 + threadIdx.x;
+        if (i < N && c < N) {
+            float h, l;
+            tf32_split(t[threadIdx.x][k], h, l);
+            Th[(size_t)i * ldt + c] = h;
+            Tl[(size_t)i * ldt + c] = l;
+        }
+    }
+}
+
+// FP64 vectors (any layout) to tf32 pairs, elementwise.
+__global__ void k_split_vec(const double *__restrict__ x, float *__restrict__ h,
+                            float *__restrict__ l, size_t n)
+{
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n;
+         t += (size_t)gridDim.x * blockDim.x) {
+        float a, b;
+        tf32_split(x[t], a, b);
+        h[t] = a;
+        l[t] = b;
+    }
+}
+
+int split_transpose_K(const double *K, size_t ld, int N, float *Th, float *Tl, size_t ldt,
+                      cudaStream_t st)
+{
+    dim3 g((N + 31) / 32, (N + 31) / 32), b(32, 8);
+    DSC_LAUNCH(k_split_transpose<<<g, b, 0, st>>>(K, ld, N, Th, Tl, ldt));
+    DSC_CUDA(cudaGetLastError());
+    return kOk;
+}
+
+int split_vec(const double *x, float *h, float *l, size_t n, cudaStream_t st)
+{
+    DSC_LAUNCH(k_split_vec<<<4 * 152, 256, 0, st>>>(x, h, l, n));
+    DSC_CUDA(cudaGetLastError());
+    return kOk;
+}
+
+// Y (M x Nc, row-major FP64) = sum over splits of the partial tiles.
+__global__ void k_sum_splits(const float *__restrict__ P, int S, size_t split_stride, size_t ldy,
+                             int M, int Nc, double *__restrict__ Y)
+{
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = blockIdx.y;
+    if (m >= M) return;
+    double s = 0.0;
+    for (int k = 0; k < S; k++) s += (double)P[(size_t)k * split_stride + (size_t)n * ldy + m];
+    Y[(size_t)m * Nc + n] = s;
+}
+
+}  // namespace dsc
+
+using namespace dsc;
+
+// Host-array entry point of the tensor-core product (row-major FP64 in and
+// out): Y (M x Nc) = A (M x Kd) * B^T (B: Nc x Kd) with 3xTF32 products.
+extern "C" int dsc_tc_gemm(int M, int Nc, int Kd, const double *A, const double *B, double *Y,
+                           int splits)
+{
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        set_error("no CUDA device available");
+        return kErrCuda;
+    }
+    if (M < 1 || Kd < 1 || Nc < 1 || Nc > 256) {
+        set_error("dsc_tc_gemm: unsupported shape");
+        return kErrArg;
+    }
+    cudaStream_t st = 0;
+    const size_t lda = ((size_t)Kd + 31) / 32 * 32;
+    DevBuf<double> dA, dB, dY;
+    DevBuf<float> Ah, Al, Bh, Bl, P;
+    DevBuf<int> err;
+    DSC_TRY(dA.alloc((size_t)M * lda));
+    DSC_TRY(dB.alloc((size_t)Nc * lda));
+    DSC_CUDA(cudaMemset(dA.p, 0, (size_t)M * lda * sizeof(double)));
+    DSC_CUDA(cudaMemset(dB.p, 0, (size_t)Nc * lda * sizeof(double)));
+    DSC_CUDA(cudaMemcpy2D(dA.p, lda * sizeof(double), A, Kd * sizeof(double), Kd * sizeof(double), M,
+                          cudaMemcpyHostToDevice));
+    DSC_CUDA(cudaMemcpy2D(dB.p, lda * sizeof(double), B, Kd * sizeof(double), Kd * sizeof(double), Nc,
+                          cudaMemcpyHostToDevice));
+    DSC_TRY(Ah.alloc((size_t)M * lda));
+    DSC_TRY(Al.alloc((size_t)M * lda));
+    DSC_TRY(Bh.alloc((size_t)Nc * lda));
+    DSC_TRY(Bl.alloc((size_t)Nc * lda));
+    DSC_TRY(split_vec(dA.p, Ah.p, Al.p, (size_t)M * lda, st));
+    DSC_TRY(split_vec(dB.p, Bh.p, Bl.p, (size_t)Nc * lda, st));
+    if (splits <= 0) splits = tc_gemm_splits_for(M, Kd);
+    const int nkb = (Kd + kTcBK - 1) / kTcBK;
+    const int S = std::min(splits, nkb);
+    DSC_TRY(P.alloc((size_t)S * Nc * M));
+    DSC_TRY(err.alloc(1));
+    DSC_CUDA(cudaMemset(err.p, 0, sizeof(int)));
+    DSC_CUDA(cudaMemset(P.p, 0, (size_t)S * Nc * M * sizeof(float)));
+    DSC_TRY(tc_gemm_3xtf32(Ah.p, Al.p, lda, Bh.p, Bl.p, lda, M, Nc, Kd, P.p, (size_t)M, S, err.p, st));
+    DSC_TRY(dY.alloc((size_t)M * Nc));
+    dim3 g((M + 255) / 256, Nc);
+    DSC_LAUNCH(k_sum_splits<<<g, 256, 0, st>>>(P.p, S, (size_t)M * Nc, (size_t)M, M, Nc, dY.p));
+    DSC_CUDA(cudaGetLastError());
+    int herr = 0;
+    DSC_CUDA(cudaMemcpy(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (herr) {
+        set_error("tensor-core GEMM: a pipeline wait gave up (code %d)", herr);
+        return kErrCuda;
+    }
+    DSC_CUDA(cudaMemcpy(Y, dY.p, (size_t)M * Nc * sizeof(double), cudaMemcpyDeviceToHost));
+    return kOk;
+}

@@ -1,0 +1,27 @@
+// dsc_tcgemm.h -- tensor-core GEMM of libdepsolver_cuda (not exported).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+namespace dsc {
+
+// Y[s][n][m] (split s, column n, row m; stride ldy per column and ldy * Nc
+// per split) = partial sums over split s's share of k of
+//   (Ah + Al)[m][k] * (Bh + Bl)[n][k]  with the three products hh + hl + lh.
+// A: M x Kd, B: Nc x Kd, both K-major FP32 holding tf32 pairs, row strides
+// lda / ldb (multiples of 4 elements, 16-byte aligned bases).  Nc <= 256.
+// *d_err (device, zero on entry) is set when a wait inside the kernel gives
+// up.  The caller adds the splits.
+int tc_gemm_3xtf32(const float *Ah, const float *Al, size_t lda, const float *Bh, const float *Bl,
+                   size_t ldb, int M, int Nc, int Kd, float *Y, size_t ldy, int splits, int *d_err,
+                   cudaStream_t st);
+int tc_gemm_splits_for(int M, int Kd);
+
+// Column-major FP64 N x N matrix (stride ld) to row-major tf32 pairs.
+int split_transpose_K(const double *K, size_t ld, int N, float *Th, float *Tl, size_t ldt,
+                      cudaStream_t st);
+// FP64 array to tf32 pairs, elementwise.
+int split_vec(const double *x, float *h, float *l, size_t n, cudaStream_t st);
+
+}  // namespace dsc

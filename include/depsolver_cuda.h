@@ -191,6 +191,15 @@ int dsc_session_set_timing(dsc_session *s, int on);
 void *dsc_session_stream(dsc_session *s);
 int dsc_session_timing(dsc_session *s, double *ms, int *count, int n);
 
+/* Tensor-core product of host FP64 matrices, the kernel behind the mixed
+ * sweep's matrix products (no counterpart call in the reference, whose
+ * GMRES product is the scalar loop of src/gmres_el.c:323-337):
+ * Y (M x Nc) = A (M x Kd) * B^T (B is Nc x Kd), all row-major; each operand
+ * is split into a TF32 pair and three products hi*hi + hi*lo + lo*hi are
+ * accumulated in FP32 per split of k and in FP64 across splits (about FP32
+ * accuracy).  Nc <= 256; splits <= 0 picks the split count. */
+int dsc_tc_gemm(int M, int Nc, int Kd, const double *A, const double *B, double *Y, int splits);
+
 /* One-call sweep from host arrays (session created and destroyed inside). */
 int dsc_sweep(int nen, unsigned N, unsigned E, const double *nodes, const unsigned *elems,
               const unsigned *bctype, const double *mbc, unsigned nIf, const unsigned *ifaces,
