@@ -92,6 +92,84 @@ __global__ void __launch_bounds__(256) k_gemm_cm(const TA *__restrict__ A, size_
     }
 }
 
+// C (M x Nc, FP64) = A (M x Kd) * B (Kd x Nc), all FP64 column-major, to
+// about FP64 accuracy on the FP32 pipes: each operand is split into an FP32
+// pair (hi, lo); the product hi*hi is made exact with an FMA (p + e), the
+// running sum is an unevaluated pair (s, c) kept exact by TwoSum, and the
+// cross terms hi*lo + lo*hi go into c.  64 x 64 tile, 4 x 4 outputs per
+// thread, k-steps of 16.
+__device__ __forceinline__ void df32_acc(float &s, float &c, float ah, float al, float bh, float bl)
+{
+    // the _rn intrinsics keep the compiler from fusing these operations,
+    // which would break the exactness of the product and of TwoSum
+    const float p = __fmul_rn(ah, bh);
+    const float e = fmaf(ah, bh, -p);
+    const float t = __fadd_rn(s, p);
+    const float bp = __fsub_rn(t, s);
+    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+    s = t;
+    c += err + e + fmaf(ah, bl, al * bh);
+}
+
+__global__ void __launch_bounds__(256) k_gemm_df32(const double *__restrict__ A, size_t lda,
+                                                   const double *__restrict__ B, size_t ldb,
+                                                   double *__restrict__ C, size_t ldc, int M, int Nc,
+                                                   int Kd)
+{
+    __shared__ float Ah[16][64 + 1], Al[16][64 + 1];
+    __shared__ float Bh[16][64 + 1], Bl[16][64 + 1];
+    const int m0 = blockIdx.x * 64, n0 = blockIdx.y * 64;
+    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+    float s[4][4], c[4][4];
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+#pragma unroll
+        for (int v = 0; v < 4; v++) s[u][v] = c[u][v] = 0.0f;
+    for (int k0 = 0; k0 < Kd; k0 += 16) {
+        for (int t = threadIdx.x; t < 16 * 64; t += 256) {
+            int kk = t / 64, mm = t % 64;
+            int m = m0 + mm, k = k0 + kk;
+            double a = (m < M && k < Kd) ? A[(size_t)k * lda + m] : 0.0;
+            float h = (float)a;
+            Ah[kk][mm] = h;
+            Al[kk][mm] = (float)(a - (double)h);
+            int nn = t / 16, kb = t % 16;
+            int n = n0 + nn, k2 = k0 + kb;
+            double b = (n < Nc && k2 < Kd) ? B[(size_t)n * ldb + k2] : 0.0;
+            float g = (float)b;
+            Bh[kb][nn] = g;
+            Bl[kb][nn] = (float)(b - (double)g);
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int kk = 0; kk < 16; kk++) {
+            float ah[4], al[4], bh[4], bl[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                ah[u] = Ah[kk][ty + 16 * u];
+                al[u] = Al[kk][ty + 16 * u];
+                bh[u] = Bh[kk][tx + 16 * u];
+                bl[u] = Bl[kk][tx + 16 * u];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+#pragma unroll
+                for (int v = 0; v < 4; v++) df32_acc(s[u][v], c[u][v], ah[u], al[u], bh[v], bl[v]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+        int m = m0 + ty + 16 * u;
+        if (m >= M) continue;
+#pragma unroll
+        for (int v = 0; v < 4; v++) {
+            int n = n0 + tx + 16 * v;
+            if (n < Nc) C[(size_t)n * ldc + m] = (double)s[u][v] + (double)c[u][v];
+        }
+    }
+}
+
 __global__ void k_to_float(const double *__restrict__ x, float *__restrict__ y, size_t n)
 {
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n;
@@ -140,6 +218,147 @@ __global__ void k_residual(const double *__restrict__ Y, const double *__restric
     R[(size_t)(2 * f + 1) * ld + i] = b.y - (s.x * yi + s.y * yr + d.x * xi + d.y * xr);
 }
 
+// ---- Givens rotations and triangular solves on the device, one thread per
+// system (complex GMRES; c real, s complex; G = [[c, s], [-conj(s), c]]).
+__device__ __forceinline__ double2 cmul(double2 a, double2 b)
+{
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+__device__ __forceinline__ double cabs2(double2 a) { return hypot(a.x, a.y); }
+__device__ __forceinline__ double2 cdiv(double2 a, double2 b)
+{
+    const double d = b.x * b.x + b.y * b.y;
+    return make_double2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+}
+
+struct GivensState {
+    double2 *H;   // [f][k][j], (kInnerMax + 1) x kInnerMax per system
+    double *c;    // [f][j]
+    double2 *s;   // [f][j]
+    double2 *g;   // [f][k], kInnerMax + 1 per system
+};
+
+__global__ void k_givens_init(GivensState gs, const double *__restrict__ beta, int F,
+                              int *__restrict__ mcount)
+{
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= F) return;
+    double2 *g = gs.g + (size_t)f * (kInnerMax + 1);
+    for (int k = 0; k <= kInnerMax; k++) g[k] = make_double2(0.0, 0.0);
+    g[0] = make_double2(beta[f], 0.0);
+    mcount[f] = 0;
+}
+
+// Column j of every active system: h[0..j] (complex, from the two Gram-
+// Schmidt passes) and h[j+1] = |w|; applies the previous rotations, forms
+// the new one, updates g, decides convergence (|g[j+1]| <= itol * beta)
+// and the scale of the next basis vector.
+__global__ void k_givens_step(GivensState gs, const double2 *__restrict__ hacc,
+                              const double *__restrict__ hn, int j, int F,
+                              const double *__restrict__ beta, const double *__restrict__ itol,
+                              int *__restrict__ active, double *__restrict__ scale,
+                              int *__restrict__ mcount)
+{
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= F) return;
+    if (!active[f]) {
+        scale[f] = 0.0;
+        return;
+    }
+    double2 *H = gs.H + (size_t)f * (kInnerMax + 1) * kInnerMax;
+    double *cr = gs.c + (size_t)f * kInnerMax;
+    double2 *sr = gs.s + (size_t)f * kInnerMax;
+    double2 *g = gs.g + (size_t)f * (kInnerMax + 1);
+    double2 prev = hacc[f];  // running entry k
+    for (int k = 0; k < j; k++) {
+        const double2 nxt = hacc[(size_t)(k + 1) * F + f];
+        const double2 t1 = cadd(cscale(prev, cr[k]), cmul(sr[k], nxt));
+        const double2 t2 = cadd(cscale(cmul(cconj(sr[k]), prev), -1.0), cscale(nxt, cr[k]));
+        H[(size_t)k * kInnerMax + j] = t1;
+        prev = t2;
+    }
+    const double2 a = prev;
+    const double b = hn[f];
+    const double aa = cabs2(a), nu = hypot(aa, b);
+    double c;
+    double2 s, top;
+    if (aa == 0.0) {
+        c = 0.0;
+        s = make_double2(1.0, 0.0);
+        top = make_double2(b, 0.0);
+    } else {
+        const double2 sgn = cscale(a, 1.0 / aa);
+        c = aa / nu;
+        s = cscale(sgn, b / nu);  // sgn * conj(b) / nu with b real
+        top = cscale(sgn, nu);
+    }
+    cr[j] = c;
+    sr[j] = s;
+    H[(size_t)j * kInnerMax + j] = top;
+    const double2 gj = g[j];
+    g[j + 1] = cscale(cmul(cconj(s), gj), -1.0);
+    g[j] = cscale(gj, c);
+    mcount[f] = j + 1;
+    const double est = cabs2(g[j + 1]);
+    if (est <= itol[f] * beta[f] || b == 0.0) {
+        active[f] = 0;
+        scale[f] = 0.0;
+    } else {
+        scale[f] = 1.0 / b;
+    }
+}
+
+// y = R^{-1} g[0..m) for the systems of this inner solve (act0).
+__global__ void k_backsolve(GivensState gs, const int *__restrict__ mcount,
+                            const int *__restrict__ act0, int F, double2 *__restrict__ y)
+{
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= F) return;
+    const int m = act0[f] ? mcount[f] : 0;
+    const double2 *H = gs.H + (size_t)f * (kInnerMax + 1) * kInnerMax;
+    const double2 *g = gs.g + (size_t)f * (kInnerMax + 1);
+    for (int k = m - 1; k >= 0; k--) {
+        double2 t = g[k];
+        for (int q = k + 1; q < m; q++) t = csub(t, cmul(H[(size_t)k * kInnerMax + q], y[(size_t)q * F + f]));
+        y[(size_t)k * F + f] = cdiv(t, H[(size_t)k * kInnerMax + k]);
+    }
+}
+
+// X += D (all 2F columns)
+__global__ void k_axpy_blocks(double *__restrict__ X, const double *__restrict__ D, int N, size_t ld,
+                              int F)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int f = blockIdx.y;
+    if (i >= N) return;
+    X[(size_t)(2 * f) * ld + i] += D[(size_t)(2 * f) * ld + i];
+    X[(size_t)(2 * f + 1) * ld + i] += D[(size_t)(2 * f + 1) * ld + i];
+}
+
+// r_f -= cs_f o (sum of split partials of K d)_f + cd_f o d_f
+__global__ void k_residual_update(const float *__restrict__ P, int S, size_t split_stride,
+                                  const double *__restrict__ D, const double2 *__restrict__ cs,
+                                  const double2 *__restrict__ cd, double *__restrict__ R, int N,
+                                  size_t ld, int F)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int f = blockIdx.y;
+    if (i >= N || f >= F) return;
+    double yr = 0.0, yi = 0.0;
+    for (int s = 0; s < S; s++) {
+        yr += (double)P[(size_t)s * split_stride + (size_t)(2 * f) * ld + i];
+        yi += (double)P[(size_t)s * split_stride + (size_t)(2 * f + 1) * ld + i];
+    }
+    const double dr = D[(size_t)(2 * f) * ld + i], di = D[(size_t)(2 * f + 1) * ld + i];
+    const double2 s = cs[(size_t)f * N + i], d = cd[(size_t)f * N + i];
+    R[(size_t)(2 * f) * ld + i] -= s.x * yr - s.y * yi + d.x * dr - d.y * di;
+    R[(size_t)(2 * f + 1) * ld + i] -= s.x * yi + s.y * yr + d.x * di + d.y * dr;
+}
+
 // Complex dots h[k][f] = <V_k,f, W_f> = sum conj(v) w, for k < nk; one block
 // per (f, k), fixed-order block reduction.
 __global__ void __launch_bounds__(256) k_cgs_dots(const double *__restrict__ Vb, size_t vstride,
@@ -163,24 +382,98 @@ __global__ void __launch_bounds__(256) k_cgs_dots(const double *__restrict__ Vb,
     if (threadIdx.x == 0) h[(size_t)k * F + f] = make_double2(a, b);
 }
 
+// One pass over the basis: block (row chunk, f) stages its chunk of W_f in
+// shared memory, each warp forms the chunk's dots with V_k,f for k = warp,
+// warp + 8, ...; k_cgs_dots_reduce adds the chunks in order.
+constexpr int kDotRows = 1024;
+
+__global__ void __launch_bounds__(256) k_cgs_dots_chunk(const double *__restrict__ Vb, size_t vstride,
+                                                        const double *__restrict__ W, int N, size_t ld,
+                                                        int F, int nk, const int *__restrict__ active,
+                                                        double2 *__restrict__ part)
+{
+    __shared__ double swr[kDotRows], swi[kDotRows];
+    const int chunk = blockIdx.x, f = blockIdx.y;
+    if (!active[f]) return;
+    const int r0 = chunk * kDotRows, nr = min(kDotRows, N - r0);
+    const double *wr = W + (size_t)(2 * f) * ld + r0, *wi = wr + ld;
+    for (int t = threadIdx.x; t < nr; t += blockDim.x) {
+        swr[t] = wr[t];
+        swi[t] = wi[t];
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int k = warp; k < nk; k += (int)(blockDim.x >> 5)) {
+        const double *vr = Vb + (size_t)k * vstride + (size_t)(2 * f) * ld + r0, *vi = vr + ld;
+        double sr = 0.0, si = 0.0;
+        // pairs of rows per lane (16-byte loads: r0 and ld are multiples of
+        // 32, so every pair is aligned), two pairs in flight per step
+        const int np = nr & ~1;
+        int t = 2 * lane;
+        for (; t + 64 < np; t += 128) {
+            const double2 a0 = *(const double2 *)(vr + t), b0 = *(const double2 *)(vi + t);
+            const double2 a1 = *(const double2 *)(vr + t + 64), b1 = *(const double2 *)(vi + t + 64);
+            sr += a0.x * swr[t] + b0.x * swi[t] + a0.y * swr[t + 1] + b0.y * swi[t + 1];
+            si += a0.x * swi[t] - b0.x * swr[t] + a0.y * swi[t + 1] - b0.y * swr[t + 1];
+            sr += a1.x * swr[t + 64] + b1.x * swi[t + 64] + a1.y * swr[t + 65] + b1.y * swi[t + 65];
+            si += a1.x * swi[t + 64] - b1.x * swr[t + 64] + a1.y * swi[t + 65] - b1.y * swr[t + 65];
+        }
+        for (; t < np; t += 64) {
+            const double2 a0 = *(const double2 *)(vr + t), b0 = *(const double2 *)(vi + t);
+            sr += a0.x * swr[t] + b0.x * swi[t] + a0.y * swr[t + 1] + b0.y * swi[t + 1];
+            si += a0.x * swi[t] - b0.x * swr[t] + a0.y * swi[t + 1] - b0.y * swr[t + 1];
+        }
+        if (lane == 0 && np < nr) {
+            const double a = vr[np], b = vi[np], c = swr[np], d = swi[np];
+            sr += a * c + b * d;
+            si += a * d - b * c;
+        }
+        sr = warp_sum(sr);
+        si = warp_sum(si);
+        if (lane == 0) part[((size_t)chunk * nk + k) * F + f] = make_double2(sr, si);
+    }
+}
+
+__global__ void k_cgs_dots_reduce(const double2 *__restrict__ part, int nchunk, int nk, int F,
+                                  const int *__restrict__ active, double2 *__restrict__ h)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nk * F) return;
+    const int f = t % F;
+    if (!active[f]) return;
+    double sr = 0.0, si = 0.0;
+    for (int c = 0; c < nchunk; c++) {
+        const double2 v = part[(size_t)c * nk * F + t];
+        sr += v.x;
+        si += v.y;
+    }
+    h[t] = make_double2(sr, si);
+}
+
 // W_f -= sum_k h[k][f] V_k,f  (and hacc += h)
 __global__ void k_cgs_update(const double *__restrict__ Vb, size_t vstride, double *__restrict__ W,
                              int N, size_t ld, int F, int nk, const int *__restrict__ active,
                              const double2 *__restrict__ h, double2 *__restrict__ hacc)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    // two consecutive rows per thread (16-byte loads; ld is a multiple of 32
+    // and the padding rows up to ld are allocated)
+    const int i = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     const int f = blockIdx.y;
     if (i >= N || !active[f]) return;
-    double wr = W[(size_t)(2 * f) * ld + i], wi = W[(size_t)(2 * f + 1) * ld + i];
+    double2 wr = *(const double2 *)(W + (size_t)(2 * f) * ld + i);
+    double2 wi = *(const double2 *)(W + (size_t)(2 * f + 1) * ld + i);
+#pragma unroll 4
     for (int k = 0; k < nk; k++) {
         const double2 c = h[(size_t)k * F + f];
-        const double vr = Vb[(size_t)k * vstride + (size_t)(2 * f) * ld + i];
-        const double vi = Vb[(size_t)k * vstride + (size_t)(2 * f + 1) * ld + i];
-        wr -= c.x * vr - c.y * vi;
-        wi -= c.x * vi + c.y * vr;
+        const double2 vr = *(const double2 *)(Vb + (size_t)k * vstride + (size_t)(2 * f) * ld + i);
+        const double2 vi = *(const double2 *)(Vb + (size_t)k * vstride + (size_t)(2 * f + 1) * ld + i);
+        wr.x -= c.x * vr.x - c.y * vi.x;
+        wi.x -= c.x * vi.x + c.y * vr.x;
+        wr.y -= c.x * vr.y - c.y * vi.y;
+        wi.y -= c.x * vi.y + c.y * vr.y;
     }
-    W[(size_t)(2 * f) * ld + i] = wr;
-    W[(size_t)(2 * f + 1) * ld + i] = wi;
+    *(double2 *)(W + (size_t)(2 * f) * ld + i) = wr;
+    *(double2 *)(W + (size_t)(2 * f + 1) * ld + i) = wi;
     if (hacc && i == 0)
         for (int k = 0; k < nk; k++) {
             double2 a = hacc[(size_t)k * F + f], c = h[(size_t)k * F + f];
@@ -316,6 +609,148 @@ __global__ void __launch_bounds__(128) k_field_batched(const double *__restrict_
     for (int ff = 0; ff < nf; ff++)
         for (int d = 0; d < 3; d++)
             part[(((size_t)chunk * F + f0 + ff) * P + p) * 3 + d] = acc[ff][d];
+}
+
+// ---- FP32 far field with FP64 near field
+// Per element: centroid as an FP32 (hi, lo) pair, squared near radius, and
+// the 7 quadrature points relative to the centroid.  A (point, element)
+// pair is "near" when the point lies within kNearFactor times the element's
+// quadrature radius of the centroid; near pairs run in FP64.
+constexpr float kNearFactor = 4.0f;
+
+__global__ void k_prepare_far(const double *__restrict__ qp, int E, float *__restrict__ ecent,
+                              float *__restrict__ qoff)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    double c[3] = {0.0, 0.0, 0.0};
+    for (int q = 0; q < kTriPts; q++)
+        for (int d = 0; d < 3; d++) c[d] += qp[((size_t)e * kTriPts + q) * 4 + d];
+    for (int d = 0; d < 3; d++) c[d] /= kTriPts;
+    double r2 = 0.0;
+    for (int q = 0; q < kTriPts; q++) {
+        double s = 0.0;
+        for (int d = 0; d < 3; d++) {
+            double o = qp[((size_t)e * kTriPts + q) * 4 + d] - c[d];
+            qoff[((size_t)e * kTriPts + q) * 3 + d] = (float)o;
+            s += o * o;
+        }
+        r2 = fmax(r2, s);
+    }
+    float *o = ecent + (size_t)e * 8;
+    for (int d = 0; d < 3; d++) {
+        float h = (float)c[d];
+        o[d] = h;
+        o[3 + d] = (float)(c[d] - (double)h);
+    }
+    o[6] = (float)(r2 * (double)(kNearFactor * kNearFactor));
+    o[7] = 0.0f;
+}
+
+__global__ void k_points_split(const double *__restrict__ px, const double *__restrict__ py,
+                               const double *__restrict__ pz, int P, float *__restrict__ phl)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    const double v[3] = {px[p], py[p], pz[p]};
+    for (int d = 0; d < 3; d++) {
+        float h = (float)v[d];
+        phl[(size_t)p * 6 + d] = h;
+        phl[(size_t)p * 6 + 3 + d] = (float)(v[d] - (double)h);
+    }
+}
+
+__global__ void k_to_f32(const double *__restrict__ x, float *__restrict__ y, size_t n)
+{
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n;
+         t += (size_t)gridDim.x * blockDim.x)
+        y[t] = (float)x[t];
+}
+
+// part[chunk][f][p][3]: as k_field_batched, far pairs in FP32 (rsqrt with a
+// Newton step, coordinates as centroid-relative offsets), near pairs in FP64.
+template <int NEN>
+__global__ void __launch_bounds__(128) k_field_batched_mixed(
+    const float *__restrict__ phl, const int4 *__restrict__ coinc, int P, const int *__restrict__ elems,
+    int E, const float *__restrict__ ecent, const float *__restrict__ qoff, const float *__restrict__ cf32,
+    const double *__restrict__ qp, const double *__restrict__ cf, int F, double *__restrict__ part)
+{
+    __shared__ float s_cent[kBChunk * 8];
+    __shared__ float s_off[kBChunk * kTriPts * 3];
+    __shared__ float s_c[kBF][kBChunk * kTriPts];
+    __shared__ int s_en[kBChunk * NEN];
+    const int chunk = blockIdx.y, fg = blockIdx.z;
+    const int e0 = chunk * kBChunk, ne = min(kBChunk, E - e0);
+    const int f0 = fg * kBF, nf = min(kBF, F - f0);
+    for (int t = threadIdx.x; t < ne * 8; t += blockDim.x) s_cent[t] = ecent[(size_t)e0 * 8 + t];
+    for (int t = threadIdx.x; t < ne * kTriPts * 3; t += blockDim.x)
+        s_off[t] = qoff[(size_t)e0 * kTriPts * 3 + t];
+    for (int t = threadIdx.x; t < kBF * ne * kTriPts; t += blockDim.x) {
+        int ff = t / (ne * kTriPts), r = t % (ne * kTriPts);
+        s_c[ff][r] = ff < nf ? cf32[(size_t)(f0 + ff) * E * kTriPts + (size_t)e0 * kTriPts + r] : 0.0f;
+    }
+    for (int t = threadIdx.x; t < ne * NEN; t += blockDim.x) s_en[t] = elems[(size_t)e0 * NEN + t];
+    __syncthreads();
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    const float ph[3] = {phl[(size_t)p * 6], phl[(size_t)p * 6 + 1], phl[(size_t)p * 6 + 2]};
+    const float pl[3] = {phl[(size_t)p * 6 + 3], phl[(size_t)p * 6 + 4], phl[(size_t)p * 6 + 5]};
+    const int4 c = coinc[p];
+    float acc[kBF][3];
+#pragma unroll
+    for (int ff = 0; ff < kBF; ff++) acc[ff][0] = acc[ff][1] = acc[ff][2] = 0.0f;
+    for (int e = 0; e < ne; e++) {
+        bool sing = false;
+#pragma unroll
+        for (int k = 0; k < NEN; k++) {
+            int v = s_en[e * NEN + k];
+            sing |= (v == c.x) | (v == c.y) | (v == c.z) | (v == c.w);
+        }
+        if (sing && c.x >= 0) continue;
+        const float *ce = s_cent + e * 8;
+        const float d0x = (ph[0] - ce[0]) + (pl[0] - ce[3]);
+        const float d0y = (ph[1] - ce[1]) + (pl[1] - ce[4]);
+        const float d0z = (ph[2] - ce[2]) + (pl[2] - ce[5]);
+        if (d0x * d0x + d0y * d0y + d0z * d0z < ce[6]) {
+            // near pair: FP64
+            const double p64[3] = {(double)ph[0] + (double)pl[0], (double)ph[1] + (double)pl[1],
+                                   (double)ph[2] + (double)pl[2]};
+            for (int q = 0; q < kTriPts; q++) {
+                const double *Q = qp + ((size_t)(e0 + e) * kTriPts + q) * 4;
+                double dx = p64[0] - Q[0], dy = p64[1] - Q[1], dz = p64[2] - Q[2];
+                double inv = rsqrt(dx * dx + dy * dy + dz * dz);
+                double i3 = inv * inv * inv;
+                double gx = dx * i3, gy = dy * i3, gz = dz * i3;
+                for (int ff = 0; ff < nf; ff++) {
+                    double cq = cf[(size_t)(f0 + ff) * E * kTriPts + (size_t)(e0 + e) * kTriPts + q];
+                    acc[ff][0] += (float)(cq * gx);
+                    acc[ff][1] += (float)(cq * gy);
+                    acc[ff][2] += (float)(cq * gz);
+                }
+            }
+            continue;
+        }
+        const float *O = s_off + e * kTriPts * 3;
+#pragma unroll
+        for (int q = 0; q < kTriPts; q++) {
+            const float dx = d0x - O[q * 3], dy = d0y - O[q * 3 + 1], dz = d0z - O[q * 3 + 2];
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            float inv = rsqrtf(r2);
+            inv = inv * (1.5f - 0.5f * r2 * inv * inv);
+            const float i3 = inv * inv * inv;
+            const float gx = dx * i3, gy = dy * i3, gz = dz * i3;
+#pragma unroll
+            for (int ff = 0; ff < kBF; ff++) {
+                const float cq = s_c[ff][e * kTriPts + q];
+                acc[ff][0] += cq * gx;
+                acc[ff][1] += cq * gy;
+                acc[ff][2] += cq * gz;
+            }
+        }
+    }
+    for (int ff = 0; ff < nf; ff++)
+        for (int d = 0; d < 3; d++)
+            part[(((size_t)chunk * F + f0 + ff) * P + p) * 3 + d] = (double)acc[ff][d];
 }
 
 // Singular elements of each point, FP64 subdivision once per (point,
@@ -469,12 +904,16 @@ struct Session::Mixed {
     DevBuf<float> Vh, Vl;   // tf32 pair of the current Krylov block
     DevBuf<float> Yp;       // split-K partial products, S blocks
     DevBuf<int> err;        // set by the tensor-core kernel when a wait gives up
-    DevBuf<double> W, Xs, R, Y64;
-    DevBuf<double2> cs, cd, bt, h, hacc, ycoef;
-    DevBuf<double> nrm, scale;
-    DevBuf<int> active, mcount;
+    DevBuf<double> W, Xs, R, Y64, D;
+    DevBuf<double2> cs, cd, bt, h, hacc, ycoef, dpart;
+    DevBuf<double> nrm, scale, betad, itold, gc;
+    DevBuf<double2> gH, gsn, gg;  // Givens state per system
+    DevBuf<int> active, act0, mcount;
     // batched field
     DevBuf<double> cf, part, sing, Enode, Fce, tot;
+    // FP32 far-field pass: element centroids / offsets, split points, weights
+    bool far_ready = false;
+    DevBuf<float> ecent, qoff, phl, cf32;
 };
 
 int Session::make_k32()
@@ -582,28 +1021,26 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
         }
         // ---- inner GMRES on M e = r for the active systems
         std::vector<int> act(F), mf(F, 0);
-        std::vector<double> beta(F), sc(F);
+        std::vector<double> beta(F), sc(F), itol(F);
         for (int f = 0; f < F; f++) {
             act[f] = !done[f];
             beta[f] = rn[f];
             sc[f] = act[f] && beta[f] > 0 ? 1.0 / beta[f] : 0.0;
+            // reduce the residual to a tenth of the target, but not below
+            // what FP32-accurate products can deliver
+            itol[f] = std::min(1e-2, std::max(kInnerTol, 0.1 * tol * bnorm[f] / std::max(rn[f], 1e-300)));
         }
         DSC_TRY(w.active.upload(act, st));
+        DSC_TRY(w.act0.upload(act, st));
         DSC_TRY(w.scale.upload(sc, st));
+        DSC_TRY(w.betad.upload(beta, st));
+        DSC_TRY(w.itold.upload(itol, st));
         DSC_LAUNCH(k_scale_into<<<vg, 256, 0, st>>>(w.R.p, w.Vb.p, N, ld, F, w.scale.p, w.active.p));
-        std::vector<std::vector<cplx>> H(F), g(F), cs_(F), sn(F);
-        for (int f = 0; f < F; f++) {
-            H[f].assign((size_t)(kInnerMax + 1) * kInnerMax, 0.0);
-            g[f].assign(kInnerMax + 1, 0.0);
-            g[f][0] = beta[f];
-            cs_[f].assign(kInnerMax, 0.0);
-            sn[f].assign(kInnerMax, 0.0);
-        }
-        std::vector<int> inner_act = act;
-        int j = 0;
-        std::vector<double2> hh((size_t)(kInnerMax + 1) * F);
-        std::vector<double> hn(F);
-        for (j = 0; j < kInnerMax; j++) {
+        GivensState gst{w.gH.p, w.gc.p, w.gsn.p, w.gg.p};
+        const int gb = (F + 63) / 64;
+        DSC_LAUNCH(k_givens_init<<<gb, 64, 0, st>>>(gst, w.betad.p, F, w.mcount.p));
+        std::vector<int> hact(F);
+        for (int j = 0; j < kInnerMax; j++) {
             const double *vj = w.Vb.p + (size_t)j * blk;
             double *vn = w.Vb.p + (size_t)(j + 1) * blk;
             {
@@ -617,86 +1054,55 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
                                                                    w.cd.p, w.W.p, N, ld, F));
             DSC_CUDA(cudaMemsetAsync(w.hacc.p, 0, (size_t)(j + 1) * F * sizeof(double2), st));
             for (int pass = 0; pass < 2; pass++) {
-                DSC_LAUNCH(k_cgs_dots<<<dim3(F, j + 1), 256, 0, st>>>(w.Vb.p, blk, w.W.p, N, ld, F, w.active.p, w.h.p));
-                DSC_LAUNCH(k_cgs_update<<<vg, 256, 0, st>>>(w.Vb.p, blk, w.W.p, N, ld, F, j + 1, w.active.p, w.h.p,
+                const int nchunk = (N + kDotRows - 1) / kDotRows;
+                DSC_LAUNCH(k_cgs_dots_chunk<<<dim3(nchunk, F), 256, 0, st>>>(w.Vb.p, blk, w.W.p, N, ld, F, j + 1,
+                                                                            w.active.p, w.dpart.p));
+                DSC_LAUNCH(k_cgs_dots_reduce<<<((j + 1) * F + 255) / 256, 256, 0, st>>>(w.dpart.p, nchunk, j + 1, F,
+                                                                                       w.active.p, w.h.p));
+                const dim3 vg2(((N + 1) / 2 + 255) / 256, F);
+                DSC_LAUNCH(k_cgs_update<<<vg2, 256, 0, st>>>(w.Vb.p, blk, w.W.p, N, ld, F, j + 1, w.active.p, w.h.p,
                                                  w.hacc.p));
             }
             DSC_LAUNCH(k_norms<<<F, 256, 0, st>>>(w.W.p, N, ld, F, w.nrm.p));
+            DSC_LAUNCH(k_givens_step<<<gb, 64, 0, st>>>(gst, w.hacc.p, w.nrm.p, j, F, w.betad.p, w.itold.p,
+                                                        w.active.p, w.scale.p, w.mcount.p));
             DSC_CUDA(cudaGetLastError());
-            DSC_CUDA(cudaMemcpyAsync(hh.data(), w.hacc.p, (size_t)(j + 1) * F * sizeof(double2),
-                                     cudaMemcpyDeviceToHost, st));
-            DSC_CUDA(cudaMemcpyAsync(hn.data(), w.nrm.p, F * sizeof(double), cudaMemcpyDeviceToHost, st));
-            DSC_CUDA(cudaStreamSynchronize(st));
-            int still = 0;
-            for (int f = 0; f < F; f++) {
-                sc[f] = 0.0;
-                if (!inner_act[f]) continue;
-                std::vector<cplx> col(j + 2);
-                for (int k = 0; k <= j; k++) col[k] = cplx(hh[(size_t)k * F + f].x, hh[(size_t)k * F + f].y);
-                col[j + 1] = hn[f];
-                for (int k = 0; k < j; k++) {
-                    cplx t1 = cs_[f][k] * col[k] + sn[f][k] * col[k + 1];
-                    cplx t2 = -std::conj(sn[f][k]) * col[k] + cs_[f][k] * col[k + 1];
-                    col[k] = t1;
-                    col[k + 1] = t2;
-                }
-                double aa = std::abs(col[j]), bb = std::abs(col[j + 1]);
-                double nu = sqrt(aa * aa + bb * bb);
-                cplx c, sgn;
-                if (aa == 0.0) {
-                    c = 0.0;
-                    sn[f][j] = 1.0;
-                    col[j] = col[j + 1];
-                } else {
-                    c = aa / nu;
-                    sgn = col[j] / aa;
-                    sn[f][j] = sgn * std::conj(col[j + 1]) / nu;
-                    col[j] = sgn * nu;
-                }
-                cs_[f][j] = c;
-                col[j + 1] = 0.0;
-                for (int k = 0; k <= j; k++) H[f][(size_t)k * kInnerMax + j] = col[k];
-                g[f][j + 1] = -std::conj(sn[f][j]) * g[f][j];
-                g[f][j] = cs_[f][j] * g[f][j];
-                mf[f] = j + 1;
-                double est = std::abs(g[f][j + 1]);
-                if (est <= kInnerTol * beta[f] || hn[f] == 0.0) inner_act[f] = 0;
-                else {
-                    still++;
-                    sc[f] = 1.0 / hn[f];
-                }
+            if ((j + 1) % 4 == 0 || j + 1 == kInnerMax) {
+                // poll the converged systems every few steps only
+                DSC_CUDA(cudaMemcpyAsync(hact.data(), w.active.p, F * sizeof(int), cudaMemcpyDeviceToHost, st));
+                DSC_CUDA(cudaStreamSynchronize(st));
+                int still = 0;
+                for (int f = 0; f < F; f++) still += hact[f];
+                if (still == 0) break;
             }
-            if (still == 0 || j + 1 == kInnerMax) break;
-            // next basis vector for the systems still iterating
-            DSC_TRY(w.scale.upload(sc, st));
-            DSC_TRY(w.active.upload(inner_act, st));
-            DSC_LAUNCH(k_scale_into<<<vg, 256, 0, st>>>(w.W.p, vn, N, ld, F, w.scale.p, w.active.p));
+            if (j + 1 < kInnerMax)
+                DSC_LAUNCH(k_scale_into<<<vg, 256, 0, st>>>(w.W.p, vn, N, ld, F, w.scale.p, w.active.p));
         }
-        // triangular solves and x += V y
-        std::vector<double2> yc((size_t)kInnerMax * F, make_double2(0.0, 0.0));
-        for (int f = 0; f < F; f++) {
-            if (!act[f]) {
-                mf[f] = 0;
-                continue;
-            }
-            int m = mf[f];
-            std::vector<cplx> yv(m);
-            for (int k = m - 1; k >= 0; k--) {
-                cplx t = g[f][k];
-                for (int q = k + 1; q < m; q++) t -= H[f][(size_t)k * kInnerMax + q] * yv[q];
-                yv[k] = t / H[f][(size_t)k * kInnerMax + k];
-            }
-            for (int k = 0; k < m; k++) yc[(size_t)k * F + f] = make_double2(yv[k].real(), yv[k].imag());
-            total_it[f] += m;
-        }
-        DSC_TRY(w.ycoef.upload(yc, st));
-        DSC_TRY(w.mcount.upload(mf, st));
-        DSC_LAUNCH(k_update_solution<<<vg, 256, 0, st>>>(w.Xs.p, w.Vb.p, blk, N, ld, F, w.ycoef.p, w.mcount.p));
-        // FP64 residual r = bt - M x
-        {
+        // triangular solves on the device, then x += V y below
+        DSC_LAUNCH(k_backsolve<<<gb, 64, 0, st>>>(gst, w.mcount.p, w.act0.p, F, w.ycoef.p));
+        DSC_CUDA(cudaMemcpyAsync(mf.data(), w.mcount.p, F * sizeof(int), cudaMemcpyDeviceToHost, st));
+        DSC_CUDA(cudaStreamSynchronize(st));
+        for (int f = 0; f < F; f++)
+            if (act[f]) total_it[f] += mf[f];
+        // correction d = V y, then x += d
+        DSC_CUDA(cudaMemsetAsync(w.D.p, 0, blk * sizeof(double), st));
+        DSC_LAUNCH(k_update_solution<<<vg, 256, 0, st>>>(w.D.p, w.Vb.p, blk, N, ld, F, w.ycoef.p, w.mcount.p));
+        DSC_LAUNCH(k_axpy_blocks<<<vg, 256, 0, st>>>(w.Xs.p, w.D.p, N, ld, F));
+        if (outer == 0) {
+            // the first residual in FP64: r = bt - M x
             TimerScope ts(tm, kTResidual, st);
-            DSC_TRY((gemm<double, double, double>(s.K64.p, ld, w.Xs.p, ld, w.Y64.p, ld, N, 2 * F, N, st)));
+            dim3 g((N + 63) / 64, (2 * F + 63) / 64);
+            DSC_LAUNCH(k_gemm_df32<<<g, 256, 0, st>>>(s.K64.p, ld, w.Xs.p, ld, w.Y64.p, ld, N, 2 * F, N));
             DSC_LAUNCH(k_residual<<<vg, 256, 0, st>>>(w.Y64.p, w.Xs.p, w.cs.p, w.cd.p, w.bt.p, w.R.p, N, ld, F));
+        } else {
+            // later residuals are updated, r -= M d: d is small, so the
+            // tensor-core product's error is relative to |r|, not to |b|
+            TimerScope ts(tm, kTGemmK, st);
+            DSC_TRY(split_vec(w.D.p, w.Vh.p, w.Vl.p, blk, st));
+            DSC_TRY(tc_gemm_3xtf32(s.Kth.p, s.Ktl.p, ld, w.Vh.p, w.Vl.p, ld, N, 2 * F, N, w.Yp.p, ld, w.S,
+                                   w.err.p, st));
+            DSC_LAUNCH(k_residual_update<<<vg, 256, 0, st>>>(w.Yp.p, w.S, ld * 2 * (size_t)F, w.D.p, w.cs.p,
+                                                             w.cd.p, w.R.p, N, ld, F));
         }
         DSC_CUDA(cudaGetLastError());
     }
@@ -729,12 +1135,26 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
             if (s.nen == 6) DSC_LAUNCH(k_charge_batched<6><<<cg, 256, 0, st>>>(s.dev.elems.p, E, s.dev.qp.p, w.Xs.p, ld, F, w.cf.p));
             else DSC_LAUNCH(k_charge_batched<3><<<cg, 256, 0, st>>>(s.dev.elems.p, E, s.dev.qp.p, w.Xs.p, ld, F, w.cf.p));
             dim3 fg((P + 127) / 128, nchunk, (F + kBF - 1) / kBF);
+            if (!w.far_ready) {
+                // geometry of the far-field pass (the session's mesh is fixed)
+                DSC_TRY(w.ecent.alloc((size_t)E * 8));
+                DSC_TRY(w.qoff.alloc((size_t)E * kTriPts * 3));
+                DSC_TRY(w.phl.alloc((size_t)P * 6));
+                DSC_LAUNCH(k_prepare_far<<<(E + 127) / 128, 128, 0, st>>>(s.dev.qp.p, E, w.ecent.p, w.qoff.p));
+                DSC_LAUNCH(k_points_split<<<(P + 127) / 128, 128, 0, st>>>(fp.ps.px.p, fp.ps.py.p, fp.ps.pz.p,
+                                                                           P, w.phl.p));
+                w.far_ready = true;
+            }
+            DSC_TRY(w.cf32.alloc((size_t)F * E * kTriPts));
+            DSC_LAUNCH(k_to_f32<<<4 * 152, 256, 0, st>>>(w.cf.p, w.cf32.p, (size_t)F * E * kTriPts));
             if (s.nen == 6)
-                DSC_LAUNCH(k_field_batched<6><<<fg, 128, 0, st>>>(fp.ps.px.p, fp.ps.py.p, fp.ps.pz.p, fp.ps.coinc.p, P,
-                                                       s.dev.elems.p, E, s.dev.qp.p, w.cf.p, F, w.part.p));
+                DSC_LAUNCH(k_field_batched_mixed<6><<<fg, 128, 0, st>>>(w.phl.p, fp.ps.coinc.p, P, s.dev.elems.p, E,
+                                                                        w.ecent.p, w.qoff.p, w.cf32.p,
+                                                                        s.dev.qp.p, w.cf.p, F, w.part.p));
             else
-                DSC_LAUNCH(k_field_batched<3><<<fg, 128, 0, st>>>(fp.ps.px.p, fp.ps.py.p, fp.ps.pz.p, fp.ps.coinc.p, P,
-                                                       s.dev.elems.p, E, s.dev.qp.p, w.cf.p, F, w.part.p));
+                DSC_LAUNCH(k_field_batched_mixed<3><<<fg, 128, 0, st>>>(w.phl.p, fp.ps.coinc.p, P, s.dev.elems.p, E,
+                                                                        w.ecent.p, w.qoff.p, w.cf32.p,
+                                                                        s.dev.qp.p, w.cf.p, F, w.part.p));
             const int sb = (P * 32 + 127) / 128;
             if (s.nen == 6)
                 DSC_LAUNCH(k_field_batched_singular<6><<<sb, 128, 0, st>>>(
@@ -802,12 +1222,21 @@ int Session::solve_mixed(unsigned nfreq, const double *freqs, double tol, unsign
         DSC_TRY(w.Xs.alloc(blk));
         DSC_TRY(w.R.alloc(blk));
         DSC_TRY(w.Y64.alloc(blk));
+        DSC_TRY(w.D.alloc(blk));
         DSC_TRY(w.h.alloc((size_t)(kInnerMax + 1) * Fmax));
+        DSC_TRY(w.dpart.alloc((size_t)((N + kDotRows - 1) / kDotRows) * (kInnerMax + 1) * Fmax));
         DSC_TRY(w.hacc.alloc((size_t)(kInnerMax + 1) * Fmax));
         DSC_TRY(w.ycoef.alloc((size_t)kInnerMax * Fmax));
         DSC_TRY(w.nrm.alloc(Fmax));
         DSC_TRY(w.scale.alloc(Fmax));
         DSC_TRY(w.active.alloc(Fmax));
+        DSC_TRY(w.act0.alloc(Fmax));
+        DSC_TRY(w.betad.alloc(Fmax));
+        DSC_TRY(w.itold.alloc(Fmax));
+        DSC_TRY(w.gc.alloc((size_t)Fmax * kInnerMax));
+        DSC_TRY(w.gsn.alloc((size_t)Fmax * kInnerMax));
+        DSC_TRY(w.gg.alloc((size_t)Fmax * (kInnerMax + 1)));
+        DSC_TRY(w.gH.alloc((size_t)Fmax * (kInnerMax + 1) * kInnerMax));
         DSC_TRY(w.mcount.alloc(Fmax));
         DSC_TRY(w.tot.alloc((size_t)Fmax * 9));
         // the padding rows of the blocks are never read but keep them finite
