@@ -64,7 +64,7 @@ def lib() -> C.CDLL:
         L.dsc_session_solve.argtypes = [C.c_void_p, C.c_int, C.c_uint, _dp, C.c_double, C.c_uint,
                                         C.c_void_p, C.c_void_p, C.c_void_p]
         L.dsc_tc_gemm.restype = C.c_int
-        L.dsc_tc_gemm.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, C.c_int]
+        L.dsc_tc_gemm.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, C.c_int, C.c_int]
         L.dsc_session_stream.restype = C.c_void_p
         L.dsc_session_stream.argtypes = [C.c_void_p]
         L.dsc_kernel_launches.restype = C.c_ulonglong

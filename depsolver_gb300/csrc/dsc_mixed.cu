@@ -481,6 +481,15 @@ __global__ void k_cgs_update(const double *__restrict__ Vb, size_t vstride, doub
         }
 }
 
+// act2[f]: system f needs the second Gram-Schmidt pass
+__global__ void k_dgks(const int *__restrict__ active, const double *__restrict__ n0,
+                       const double *__restrict__ n1, int F, int *__restrict__ act2)
+{
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= F) return;
+    act2[f] = active[f] && n1[f] < 0.7071067811865476 * n0[f];
+}
+
 // nrm[f] = |W_f| (one block per system)
 __global__ void __launch_bounds__(256) k_norms(const double *__restrict__ W, int N, size_t ld, int F,
                                                double *__restrict__ nrm)
@@ -906,9 +915,9 @@ struct Session::Mixed {
     DevBuf<int> err;        // set by the tensor-core kernel when a wait gives up
     DevBuf<double> W, Xs, R, Y64, D;
     DevBuf<double2> cs, cd, bt, h, hacc, ycoef, dpart;
-    DevBuf<double> nrm, scale, betad, itold, gc;
+    DevBuf<double> nrm, nrm0, scale, betad, itold, gc;
     DevBuf<double2> gH, gsn, gg;  // Givens state per system
-    DevBuf<int> active, act0, mcount;
+    DevBuf<int> active, act0, act2, mcount;
     // batched field
     DevBuf<double> cf, part, sing, Enode, Fce, tot;
     // FP32 far-field pass: element centroids / offsets, split points, weights
@@ -920,9 +929,8 @@ int Session::make_k32()
 {
     if (k32_ready) return kOk;
     DSC_TRY(assemble64());
-    DSC_TRY(Kth.alloc(ld * N));
-    DSC_TRY(Ktl.alloc(ld * N));
-    DSC_TRY(split_transpose_K(K64.p, ld, N, Kth.p, Ktl.p, ld, st));
+    DSC_TRY(Kt32.alloc(ld * N));
+    DSC_TRY(split_transpose_K(K64.p, ld, N, Kt32.p, nullptr, ld, st));
     k32_ready = true;
     return kOk;
 }
@@ -1046,21 +1054,30 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
             {
                 TimerScope ts(tm, kTGemmK, st);
                 DSC_TRY(split_vec(vj, w.Vh.p, w.Vl.p, blk, st));
-                DSC_TRY(tc_gemm_3xtf32(s.Kth.p, s.Ktl.p, ld, w.Vh.p, w.Vl.p, ld, N, 2 * F, N, w.Yp.p, ld,
+                DSC_TRY(tc_gemm_3xtf32(s.Kt32.p, nullptr, ld, w.Vh.p, w.Vl.p, ld, N, 2 * F, N, w.Yp.p, ld,
                                        w.S, w.err.p, st));
             }
             TimerScope ts(tm, kTKrylov, st);
             DSC_LAUNCH(k_apply_epilogue_splits<<<vg, 256, 0, st>>>(w.Yp.p, w.S, ld * 2 * (size_t)F, vj, w.cs.p,
                                                                    w.cd.p, w.W.p, N, ld, F));
             DSC_CUDA(cudaMemsetAsync(w.hacc.p, 0, (size_t)(j + 1) * F * sizeof(double2), st));
+            // classical Gram-Schmidt; the second pass only for the systems
+            // whose vector lost more than 1 - 1/sqrt(2) of its norm in the
+            // first (the DGKS criterion), decided on the device
+            DSC_LAUNCH(k_norms<<<F, 256, 0, st>>>(w.W.p, N, ld, F, w.nrm0.p));
             for (int pass = 0; pass < 2; pass++) {
+                const int *mask = pass == 0 ? w.active.p : w.act2.p;
                 const int nchunk = (N + kDotRows - 1) / kDotRows;
+                if (pass == 1) {
+                    DSC_LAUNCH(k_norms<<<F, 256, 0, st>>>(w.W.p, N, ld, F, w.nrm.p));
+                    DSC_LAUNCH(k_dgks<<<gb, 64, 0, st>>>(w.active.p, w.nrm0.p, w.nrm.p, F, w.act2.p));
+                }
                 DSC_LAUNCH(k_cgs_dots_chunk<<<dim3(nchunk, F), 256, 0, st>>>(w.Vb.p, blk, w.W.p, N, ld, F, j + 1,
-                                                                            w.active.p, w.dpart.p));
+                                                                            mask, w.dpart.p));
                 DSC_LAUNCH(k_cgs_dots_reduce<<<((j + 1) * F + 255) / 256, 256, 0, st>>>(w.dpart.p, nchunk, j + 1, F,
-                                                                                       w.active.p, w.h.p));
+                                                                                       mask, w.h.p));
                 const dim3 vg2(((N + 1) / 2 + 255) / 256, F);
-                DSC_LAUNCH(k_cgs_update<<<vg2, 256, 0, st>>>(w.Vb.p, blk, w.W.p, N, ld, F, j + 1, w.active.p, w.h.p,
+                DSC_LAUNCH(k_cgs_update<<<vg2, 256, 0, st>>>(w.Vb.p, blk, w.W.p, N, ld, F, j + 1, mask, w.h.p,
                                                  w.hacc.p));
             }
             DSC_LAUNCH(k_norms<<<F, 256, 0, st>>>(w.W.p, N, ld, F, w.nrm.p));
@@ -1099,7 +1116,7 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
             // tensor-core product's error is relative to |r|, not to |b|
             TimerScope ts(tm, kTGemmK, st);
             DSC_TRY(split_vec(w.D.p, w.Vh.p, w.Vl.p, blk, st));
-            DSC_TRY(tc_gemm_3xtf32(s.Kth.p, s.Ktl.p, ld, w.Vh.p, w.Vl.p, ld, N, 2 * F, N, w.Yp.p, ld, w.S,
+            DSC_TRY(tc_gemm_3xtf32(s.Kt32.p, nullptr, ld, w.Vh.p, w.Vl.p, ld, N, 2 * F, N, w.Yp.p, ld, w.S,
                                    w.err.p, st));
             DSC_LAUNCH(k_residual_update<<<vg, 256, 0, st>>>(w.Yp.p, w.S, ld * 2 * (size_t)F, w.D.p, w.cs.p,
                                                              w.cd.p, w.R.p, N, ld, F));
@@ -1231,6 +1248,8 @@ int Session::solve_mixed(unsigned nfreq, const double *freqs, double tol, unsign
         DSC_TRY(w.scale.alloc(Fmax));
         DSC_TRY(w.active.alloc(Fmax));
         DSC_TRY(w.act0.alloc(Fmax));
+        DSC_TRY(w.act2.alloc(Fmax));
+        DSC_TRY(w.nrm0.alloc(Fmax));
         DSC_TRY(w.betad.alloc(Fmax));
         DSC_TRY(w.itold.alloc(Fmax));
         DSC_TRY(w.gc.alloc((size_t)Fmax * kInnerMax));

@@ -144,6 +144,23 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t *r)
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t *b)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(b)) : "memory");
+}
+
+__device__ __forceinline__ float tf32_rna(float v)
+{
+    uint32_t h;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
+    return __uint_as_float(h);
+}
+
+// SPLIT_A = false: A arrives as a tf32 pair (tmAh, tmAl).
+// SPLIT_A = true: A arrives as plain FP32 through tmAh into the hi slot and
+// warps 2 and 3 split it in shared memory (hi rounded to tf32 in place, the
+// remainder into the lo slot) before the MMA issuer may read the stage.
+template <bool SPLIT_A>
 __global__ void __launch_bounds__(128, 1)
     k_tc_gemm_3xtf32(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
                      const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl,
@@ -156,7 +173,8 @@ __global__ void __launch_bounds__(128, 1)
     const uint32_t stage_bytes = 2 * a_bytes + 2 * b_bytes;
     uint64_t *full = (uint64_t *)(smem + kTcStages * stage_bytes);
     uint64_t *empty = full + kTcStages;
-    uint64_t *accum = empty + kTcStages;
+    uint64_t *splitb = empty + kTcStages;
+    uint64_t *accum = splitb + kTcStages;
     uint32_t *tmem_slot = (uint32_t *)(accum + 1);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int m0 = blockIdx.x * kTcBM, split = blockIdx.y;
@@ -167,6 +185,7 @@ __global__ void __launch_bounds__(128, 1)
         for (int s = 0; s < kTcStages; s++) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
+            mbar_init(&splitb[s], 64);  // the 64 threads of warps 2 and 3
         }
         mbar_init(accum, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -189,10 +208,10 @@ __global__ void __launch_bounds__(128, 1)
             const int s = i % kTcStages;
             if (i >= kTcStages && !mbar_wait(&empty[s], ((i / kTcStages) - 1) & 1, err, 1)) break;
             uint8_t *st = smem + s * stage_bytes;
-            mbar_expect_tx(&full[s], stage_bytes);
+            mbar_expect_tx(&full[s], SPLIT_A ? stage_bytes - a_bytes : stage_bytes);
             const int kx = (kb0 + i) * kTcBK;
             tma_load_2d(st, &tmAh, &full[s], kx, m0);
-            tma_load_2d(st + a_bytes, &tmAl, &full[s], kx, m0);
+            if (!SPLIT_A) tma_load_2d(st + a_bytes, &tmAl, &full[s], kx, m0);
             tma_load_2d(st + 2 * a_bytes, &tmBh, &full[s], kx, 0);
             tma_load_2d(st + 2 * a_bytes + b_bytes, &tmBl, &full[s], kx, 0);
             issued = i + 1;
@@ -209,7 +228,7 @@ __global__ void __launch_bounds__(128, 1)
         const uint32_t idesc = idesc_tf32(BN, kTcBM);
         for (int i = 0; i < nkb; i++) {
             const int s = i % kTcStages;
-            if (!mbar_wait(&full[s], (i / kTcStages) & 1, err, 2)) break;
+            if (!mbar_wait(SPLIT_A ? &splitb[s] : &full[s], (i / kTcStages) & 1, err, 2)) break;
             tc_fence_after();
             uint8_t *st = smem + s * stage_bytes;
             const uint64_t dah = sw128_desc(st), dal = sw128_desc(st + a_bytes);
@@ -224,6 +243,32 @@ __global__ void __launch_bounds__(128, 1)
             mma_commit(&empty[s]);
         }
         mma_commit(accum);
+    } else if (SPLIT_A && warp >= 2 && nkb > 0) {
+        // ---- splitters: FP32 A tile -> tf32 hi (in place) + lo
+        const int tid = threadIdx.x - 64;
+        for (int i = 0; i < nkb; i++) {
+            const int s = i % kTcStages;
+            if (!mbar_wait(&full[s], (i / kTcStages) & 1, err, 4)) break;
+            float4 *hi = (float4 *)(smem + s * stage_bytes);
+            float4 *lo = (float4 *)(smem + s * stage_bytes + a_bytes);
+            for (int t = tid; t < (int)(a_bytes / 16); t += 64) {
+                const float4 v = hi[t];
+                float4 h, l;
+                h.x = tf32_rna(v.x);
+                h.y = tf32_rna(v.y);
+                h.z = tf32_rna(v.z);
+                h.w = tf32_rna(v.w);
+                l.x = v.x - h.x;
+                l.y = v.y - h.y;
+                l.z = v.z - h.z;
+                l.w = v.w - h.w;
+                hi[t] = h;
+                lo[t] = l;
+            }
+            // generic-proxy writes must be visible to the tensor core's reads
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_arrive(&splitb[s]);
+        }
     }
     __syncwarp();
 
@@ -311,9 +356,11 @@ int tc_gemm_3xtf32(const float *Ah, const float *Al, size_t lda, const float *Bh
     }
     const int BN = (Nc + 15) / 16 * 16;
     const int tmem_cols = BN <= 32 ? 32 : BN <= 64 ? 64 : BN <= 128 ? 128 : 256;
+    const bool split_a = Al == nullptr;  // plain FP32 A, split in shared memory
     CUtensorMap ah, al, bh, bl;
     DSC_TRY(make_map(&ah, Ah, M, Kd, lda, kTcBM));
-    DSC_TRY(make_map(&al, Al, M, Kd, lda, kTcBM));
+    if (split_a) al = ah;
+    else DSC_TRY(make_map(&al, Al, M, Kd, lda, kTcBM));
     DSC_TRY(make_map(&bh, Bh, Nc, Kd, ldb, BN));
     DSC_TRY(make_map(&bl, Bl, Nc, Kd, ldb, BN));
     const int nkb = (Kd + kTcBK - 1) / kTcBK;
@@ -321,10 +368,18 @@ int tc_gemm_3xtf32(const float *Ah, const float *Al, size_t lda, const float *Bh
     const int kps = (nkb + splits - 1) / splits;
     splits = (nkb + kps - 1) / kps;  // every split has at least one k-block
     const size_t smem = 1024 + (size_t)kTcStages * (2 * kTcBM * 128 + 2 * BN * 128) + 256;
-    DSC_CUDA(cudaFuncSetAttribute(k_tc_gemm_3xtf32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid((M + kTcBM - 1) / kTcBM, splits);
-    DSC_LAUNCH(k_tc_gemm_3xtf32<<<grid, 128, smem, st>>>(ah, al, bh, bl, M, Nc, BN, nkb, kps, Y, ldy,
-                                                        ldy * (size_t)Nc, tmem_cols, d_err));
+    if (split_a) {
+        DSC_CUDA(cudaFuncSetAttribute(k_tc_gemm_3xtf32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+        DSC_LAUNCH(k_tc_gemm_3xtf32<true><<<grid, 128, smem, st>>>(ah, al, bh, bl, M, Nc, BN, nkb, kps, Y, ldy,
+                                                                  ldy * (size_t)Nc, tmem_cols, d_err));
+    } else {
+        DSC_CUDA(cudaFuncSetAttribute(k_tc_gemm_3xtf32<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+        DSC_LAUNCH(k_tc_gemm_3xtf32<false><<<grid, 128, smem, st>>>(ah, al, bh, bl, M, Nc, BN, nkb, kps, Y, ldy,
+                                                                   ldy * (size_t)Nc, tmem_cols, d_err));
+    }
     DSC_CUDA(cudaGetLastError());
     return kOk;
 }
@@ -368,6 +423,10 @@ __global__ void k_split_transpose(const double *__restrict__ K, size_t ld, int N
     for (int k = threadIdx.y; k < 32; k += blockDim.y) {
         int i = i0 + k, c = c0 + threadIdx.x;
         if (i < N && c < N) {
+            if (!Tl) {
+                Th[(size_t)i * ldt + c] = (float)t[threadIdx.x][k];  // plain FP32
+                continue;
+            }
             float h, l;
             tf32_split(t[threadIdx.x][k], h, l);
             Th[(size_t)i * ldt + c] = h;
@@ -405,6 +464,13 @@ int split_vec(const double *x, float *h, float *l, size_t n, cudaStream_t st)
     return kOk;
 }
 
+__global__ void k_to_f32_plain(const double *__restrict__ x, float *__restrict__ y, size_t n)
+{
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n;
+         t += (size_t)gridDim.x * blockDim.x)
+        y[t] = (float)x[t];
+}
+
 // Y (M x Nc, row-major FP64) = sum over splits of the partial tiles.
 __global__ void k_sum_splits(const float *__restrict__ P, int S, size_t split_stride, size_t ldy,
                              int M, int Nc, double *__restrict__ Y)
@@ -424,7 +490,7 @@ using namespace dsc;
 // Host-array entry point of the tensor-core product (row-major FP64 in and
 // out): Y (M x Nc) = A (M x Kd) * B^T (B: Nc x Kd) with 3xTF32 products.
 extern "C" int dsc_tc_gemm(int M, int Nc, int Kd, const double *A, const double *B, double *Y,
-                           int splits)
+                           int splits, int a_in_smem)
 {
     int n = 0;
     if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
@@ -453,7 +519,8 @@ extern "C" int dsc_tc_gemm(int M, int Nc, int Kd, const double *A, const double 
     DSC_TRY(Al.alloc((size_t)M * lda));
     DSC_TRY(Bh.alloc((size_t)Nc * lda));
     DSC_TRY(Bl.alloc((size_t)Nc * lda));
-    DSC_TRY(split_vec(dA.p, Ah.p, Al.p, (size_t)M * lda, st));
+    if (a_in_smem) DSC_LAUNCH(k_to_f32_plain<<<4 * 152, 256, 0, st>>>(dA.p, Ah.p, (size_t)M * lda));
+    else DSC_TRY(split_vec(dA.p, Ah.p, Al.p, (size_t)M * lda, st));
     DSC_TRY(split_vec(dB.p, Bh.p, Bl.p, (size_t)Nc * lda, st));
     if (splits <= 0) splits = tc_gemm_splits_for(M, Kd);
     const int nkb = (Kd + kTcBK - 1) / kTcBK;
@@ -462,7 +529,8 @@ extern "C" int dsc_tc_gemm(int M, int Nc, int Kd, const double *A, const double 
     DSC_TRY(err.alloc(1));
     DSC_CUDA(cudaMemset(err.p, 0, sizeof(int)));
     DSC_CUDA(cudaMemset(P.p, 0, (size_t)S * Nc * M * sizeof(float)));
-    DSC_TRY(tc_gemm_3xtf32(Ah.p, Al.p, lda, Bh.p, Bl.p, lda, M, Nc, Kd, P.p, (size_t)M, S, err.p, st));
+    DSC_TRY(tc_gemm_3xtf32(Ah.p, a_in_smem ? nullptr : Al.p, lda, Bh.p, Bl.p, lda, M, Nc, Kd, P.p,
+                           (size_t)M, S, err.p, st));
     DSC_TRY(dY.alloc((size_t)M * Nc));
     dim3 g((M + 255) / 256, Nc);
     DSC_LAUNCH(k_sum_splits<<<g, 256, 0, st>>>(P.p, S, (size_t)M * Nc, (size_t)M, M, Nc, dY.p));

@@ -197,8 +197,11 @@ int dsc_session_timing(dsc_session *s, double *ms, int *count, int n);
  * Y (M x Nc) = A (M x Kd) * B^T (B is Nc x Kd), all row-major; each operand
  * is split into a TF32 pair and three products hi*hi + hi*lo + lo*hi are
  * accumulated in FP32 per split of k and in FP64 across splits (about FP32
- * accuracy).  Nc <= 256; splits <= 0 picks the split count. */
-int dsc_tc_gemm(int M, int Nc, int Kd, const double *A, const double *B, double *Y, int splits);
+ * accuracy).  Nc <= 256; splits <= 0 picks the split count.  a_in_smem = 1
+ * stores A as plain FP32 and splits it inside the kernel (half the reads of
+ * A; the mixed sweep's mode), 0 stores the pair. */
+int dsc_tc_gemm(int M, int Nc, int Kd, const double *A, const double *B, double *Y, int splits,
+                int a_in_smem);
 
 /* One-call sweep from host arrays (session created and destroyed inside). */
 int dsc_sweep(int nen, unsigned N, unsigned E, const double *nodes, const unsigned *elems,

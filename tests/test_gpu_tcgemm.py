@@ -12,15 +12,16 @@ from depsolver_gb300 import _native
 pytestmark = pytest.mark.gpu
 
 
-def _run(L, A, B, splits):
+def _run(L, A, B, splits, a_in_smem=1):
     M, Kd = A.shape
     Nc = B.shape[0]
     Y = np.zeros((M, Nc))
     _native.check(L.dsc_tc_gemm(M, Nc, Kd, np.ascontiguousarray(A), np.ascontiguousarray(B), Y,
-                                splits))
+                                splits, a_in_smem))
     return Y
 
 
+@pytest.mark.parametrize("a_in_smem", [0, 1])
 @pytest.mark.parametrize("M,Nc,Kd,splits", [
     (128, 16, 32, 1),      # one tile, one k-block
     (300, 40, 1000, 1),    # ragged everything, one split
@@ -28,11 +29,11 @@ def _run(L, A, B, splits):
     (1000, 128, 2500, 0),  # automatic split count
     (257, 100, 77, 3),
 ])
-def test_tc_gemm_matches_fp64(gpu, M, Nc, Kd, splits):
+def test_tc_gemm_matches_fp64(gpu, M, Nc, Kd, splits, a_in_smem):
     rng = np.random.default_rng(M + Nc + Kd)
     A = rng.standard_normal((M, Kd)) * np.exp(rng.uniform(-3, 3, (M, 1)))
     B = rng.standard_normal((Nc, Kd))
-    Y = _run(gpu, A, B, splits)
+    Y = _run(gpu, A, B, splits, a_in_smem)
     ref = A @ B.T
     bound = np.abs(A) @ np.abs(B).T
     assert np.all(np.abs(Y - ref) <= 2e-6 * bound + 1e-300), float(np.max(np.abs(Y - ref) / bound))
