@@ -65,6 +65,10 @@ def lib() -> C.CDLL:
                                         C.c_void_p, C.c_void_p, C.c_void_p]
         L.dsc_tc_gemm.restype = C.c_int
         L.dsc_tc_gemm.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, C.c_int, C.c_int]
+        L.dsc_tc_gemm_noalloc.restype = C.c_int
+        L.dsc_tc_gemm_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_size_t,
+                                          C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.c_int,
+                                          C.c_void_p]
         L.dsc_session_stream.restype = C.c_void_p
         L.dsc_session_stream.argtypes = [C.c_void_p]
         L.dsc_kernel_launches.restype = C.c_ulonglong

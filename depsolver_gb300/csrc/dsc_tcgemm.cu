@@ -483,6 +483,60 @@ __global__ void k_sum_splits(const float *__restrict__ P, int S, size_t split_st
     Y[(size_t)m * Nc + n] = s;
 }
 
+// Rows of a row-major FP64 matrix (rows x k, row stride ld) to tf32 pairs
+// with row stride ldh; only the first k entries of each row are read and
+// written.
+__global__ void k_split_rows(const double *__restrict__ x, size_t ld, int rows, int k,
+                             float *__restrict__ h, float *__restrict__ l, size_t ldh)
+{
+    const size_t n = (size_t)rows * k;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n;
+         t += (size_t)gridDim.x * blockDim.x) {
+        const size_t r = t / k, c = t % k;
+        float a, b;
+        tf32_split(x[r * ld + c], a, b);
+        h[r * ldh + c] = a;
+        l[r * ldh + c] = b;
+    }
+}
+
+int split_rows(const double *x, size_t ld, int rows, int k, float *h, float *l, size_t ldh,
+               cudaStream_t st)
+{
+    DSC_LAUNCH(k_split_rows<<<4 * 152, 256, 0, st>>>(x, ld, rows, k, h, l, ldh));
+    DSC_CUDA(cudaGetLastError());
+    return kOk;
+}
+
+// Y[m * ldy + n] (FP64) = sum over the S partial tiles, in split order.
+__global__ void k_sum_splits_ld(const float *__restrict__ P, int S, size_t split_stride,
+                                size_t ldp, int M, int Nc, double *__restrict__ Y, size_t ldy)
+{
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = blockIdx.y;
+    if (m >= M) return;
+    double s = 0.0;
+    for (int k = 0; k < S; k++) s += (double)P[(size_t)k * split_stride + (size_t)n * ldp + m];
+    Y[(size_t)m * ldy + n] = s;
+}
+
+int sum_splits(const float *P, int S, size_t split_stride, size_t ldp, int M, int Nc, double *Y,
+               size_t ldy, cudaStream_t st)
+{
+    dim3 g((M + 255) / 256, Nc);
+    DSC_LAUNCH(k_sum_splits_ld<<<g, 256, 0, st>>>(P, S, split_stride, ldp, M, Nc, Y, ldy));
+    DSC_CUDA(cudaGetLastError());
+    return kOk;
+}
+
+int tc_gemm_splits_used(int Kd, int splits)
+{
+    const int nkb = (Kd + kTcBK - 1) / kTcBK;
+    splits = std::max(1, std::min(splits, nkb));
+    const int kps = (nkb + splits - 1) / splits;
+    return (nkb + kps - 1) / kps;
+}
+
 }  // namespace dsc
 
 using namespace dsc;

@@ -23,5 +23,14 @@ int split_transpose_K(const double *K, size_t ld, int N, float *Th, float *Tl, s
                       cudaStream_t st);
 // FP64 array to tf32 pairs, elementwise.
 int split_vec(const double *x, float *h, float *l, size_t n, cudaStream_t st);
+// Row-major FP64 rows x k (row stride ld) to tf32 pairs (row stride ldh).
+int split_rows(const double *x, size_t ld, int rows, int k, float *h, float *l, size_t ldh,
+               cudaStream_t st);
+// Y[m * ldy + n] = sum over S partial tiles of tc_gemm_3xtf32 (tile s,
+// column n, row m at s * split_stride + n * ldp + m), in split order.
+int sum_splits(const float *P, int S, size_t split_stride, size_t ldp, int M, int Nc, double *Y,
+               size_t ldy, cudaStream_t st);
+// The number of partial tiles tc_gemm_3xtf32 writes for `splits` (>= 1).
+int tc_gemm_splits_used(int Kd, int splits);
 
 }  // namespace dsc

@@ -203,6 +203,38 @@ int dsc_session_timing(dsc_session *s, double *ms, int *count, int n);
 int dsc_tc_gemm(int M, int Nc, int Kd, const double *A, const double *B, double *Y, int splits,
                 int a_in_smem);
 
+/* The same product on caller-owned device memory, allocating nothing (no
+ * counterpart in the reference, which has no GPU code).  For callers that
+ * cannot let a library allocate: one that sized its device memory up front
+ * (the FP32 matrix, the Krylov vectors) and keeps none free, and one that
+ * runs work on other streams while it calls, since cudaFree synchronises
+ * the whole device and cudaMalloc may as well.  This call makes no
+ * cudaMalloc/cudaFree or other allocating call: its scratch is one static
+ * device array of DSC_NOALLOC_SCRATCH_BYTES (32 MiB) per device, reserved
+ * when the library's module holding it loads there.
+ *
+ * Y (M x Nc, FP64, row stride ldy) = A (M x Kd, FP32, row stride lda) *
+ * B^T (B: Nc x Kd, FP64, row stride ldb); A, B, Y on the current device.
+ * A's base is 16-byte aligned and lda a multiple of 4 (the tensor-memory
+ * copy engine's rule).  Same 3xTF32 products, split of k and split order as
+ * dsc_tc_gemm: for A holding FP32 values the two give identical Y.
+ * splits <= 0 picks dsc_tc_gemm's split count, lowered until the scratch
+ * fits; a shape (or an explicit splits) needing more than the scratch,
+ * about 4 * Nc * (2 * round_up(Kd, 32) + splits * M) bytes, is rejected
+ * with DSC_ERR_ARG and a message naming both sizes.
+ *
+ * The work runs on `stream` (a cudaStream_t; NULL = the default stream) and
+ * the call returns once it has finished, with the status of the kernels'
+ * bounded waits.  The first call on each device looks up the scratch's
+ * address (cudaGetSymbolAddress) and keeps it: make that call during
+ * set-up, before any stream capture begins, and do not call again on a
+ * device after cudaDeviceReset.  All calls on a device share its scratch,
+ * so two calls that overlapped would race on it; the library prevents that
+ * with a process-wide lock held until a call's work has finished. */
+#define DSC_NOALLOC_SCRATCH_BYTES 33554432u /* 32 MiB */
+int dsc_tc_gemm_noalloc(int M, int Nc, int Kd, const float *A, size_t lda, const double *B,
+                        size_t ldb, double *Y, size_t ldy, int splits, void *stream);
+
 /* One-call sweep from host arrays (session created and destroyed inside). */
 int dsc_sweep(int nen, unsigned N, unsigned E, const double *nodes, const unsigned *elems,
               const unsigned *bctype, const double *mbc, unsigned nIf, const unsigned *ifaces,
