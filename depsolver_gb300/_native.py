@@ -76,7 +76,7 @@ def lib() -> C.CDLL:
         L.dsc_session_set_timing.restype = C.c_int
         L.dsc_session_set_timing.argtypes = [C.c_void_p, C.c_int]
         L.dsc_session_timing.restype = C.c_int
-        L.dsc_session_timing.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        L.dsc_session_timing.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         L.dsc_sweep.restype = C.c_int
         L.dsc_sweep.argtypes = [C.c_int, C.c_uint, C.c_uint, _dp, _up, _up, _dp, C.c_uint,
                                 C.c_void_p, C.c_uint, _dp, C.c_int, C.c_uint, _dp, C.c_double,

@@ -108,7 +108,7 @@ def force_mst(sc: Scene, vB: np.ndarray, eps: float | None = None):
 MODE_FP64 = 1
 MODE_MIXED = 2
 TIMER_NAMES = ("asm_regular", "asm_fixup", "asm_singular", "gemv_K64", "gemm_K", "field", "mst",
-               "residual_fp64", "krylov")
+               "residual_fp64", "krylov", "gram_schmidt")
 
 
 class Session:
@@ -149,11 +149,14 @@ class Session:
         _native.check(self._L.dsc_session_set_timing(self._h, int(on)))
 
     def timing(self):
+        """{class: (ms, timed scopes, algorithmic work)} since the last call
+        (work units per class in dsc_session_timing's header comment)."""
         ms = np.zeros(len(TIMER_NAMES))
         cnt = np.zeros(len(TIMER_NAMES), dtype=np.int32)
+        wk = np.zeros(len(TIMER_NAMES))
         _native.check(self._L.dsc_session_timing(self._h, ms.ctypes.data, cnt.ctypes.data,
-                                                 len(TIMER_NAMES)))
-        return {n: (float(ms[k]), int(cnt[k])) for k, n in enumerate(TIMER_NAMES)}
+                                                 wk.ctypes.data, len(TIMER_NAMES)))
+        return {n: (float(ms[k]), int(cnt[k]), float(wk[k])) for k, n in enumerate(TIMER_NAMES)}
 
     def solve(self, freqs, mode: int = MODE_MIXED, tol: float = 1e-10, max_iters: int = 600,
               want_sigma: bool = False):

@@ -289,6 +289,7 @@ static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStr
         {
             TimerScope ts(tm, kTAsmRegular, st);
             DSC_LAUNCH(k_asm_regular_f64<NEN><<<grid, 128, smem, st>>>(a, K, P.p));
+            if (tm) tm->add_work(kTAsmRegular, (double)(hi - lo) * m.E);  // (row, element) pairs
         }
         DSC_CUDA(cudaGetLastError());
         if (m.n_fix > 0) {

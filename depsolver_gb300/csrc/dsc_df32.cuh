@@ -1,0 +1,96 @@
+// dsc_df32.cuh -- double-FP32 arithmetic for the Krylov vectors of the
+// mixed sweep.
+//
+// A value is the unevaluated sum hi + lo of two floats (a float2: x = hi,
+// y = lo), a 48-bit significand.  Products are made exact with an FMA
+// (Dekker's product via fma: p = a*b, e = fma(a, b, -p)), sums with Knuth's
+// TwoSum; the cross terms hi*lo and lo*hi go into the low part and lo*lo is
+// dropped.  An accumulator keeps its error terms in .y without
+// renormalising; it is renormalised once at the end (df_norm), which keeps
+// the error of a length-n sum near n * 2^-48 of its largest partial sum.
+//
+// These run on the FP32 pipes, which on sm_103a issue 64 times as many
+// operations per clock as the FP64 pipe.  The _rn intrinsics stop the
+// compiler from contracting the error-free transforms into FMAs.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace dsc {
+
+__device__ __forceinline__ float2 df_two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return make_float2(s, e);
+}
+
+// (hi, lo) with |lo| <= ulp(hi) / 2, for |a| >= |b| or a == 0
+__device__ __forceinline__ float2 df_fast_two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    return make_float2(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+
+__device__ __forceinline__ float2 df_norm(float2 a)
+{
+    return df_two_sum(a.x, a.y);
+}
+
+// acc += a * b
+__device__ __forceinline__ void df_mac(float2 &acc, float2 a, float2 b)
+{
+    const float p = __fmul_rn(a.x, b.x);
+    float e = __fmaf_rn(a.x, b.x, -p);
+    e = __fmaf_rn(a.x, b.y, e);
+    e = __fmaf_rn(a.y, b.x, e);
+    const float2 s = df_two_sum(acc.x, p);
+    acc.x = s.x;
+    acc.y = __fadd_rn(acc.y, __fadd_rn(s.y, e));
+}
+
+// a * b, renormalised
+__device__ __forceinline__ float2 df_mul(float2 a, float2 b)
+{
+    const float p = __fmul_rn(a.x, b.x);
+    float e = __fmaf_rn(a.x, b.x, -p);
+    e = __fmaf_rn(a.x, b.y, e);
+    e = __fmaf_rn(a.y, b.x, e);
+    return df_fast_two_sum(p, e);
+}
+
+__device__ __forceinline__ float2 df_add(float2 a, float2 b)
+{
+    const float2 s = df_two_sum(a.x, b.x);
+    return df_fast_two_sum(s.x, __fadd_rn(s.y, __fadd_rn(a.y, b.y)));
+}
+
+__device__ __forceinline__ float2 df_neg(float2 a) { return make_float2(-a.x, -a.y); }
+
+// FP64 <-> double-FP32 (these conversions run on the FP64 pipe: use them
+// per block or per system, not per element, in the streaming kernels)
+__device__ __forceinline__ float2 df_from(double v)
+{
+    const float h = (float)v;
+    return make_float2(h, (float)(v - (double)h));
+}
+
+__device__ __forceinline__ double df_to(float2 a) { return (double)a.x + (double)a.y; }
+
+// Warp-wide sum of accumulators (fixed shuffle order).
+__device__ __forceinline__ float2 df_warp_sum(float2 v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        float2 u;
+        u.x = __shfl_xor_sync(0xffffffffu, v.x, o);
+        u.y = __shfl_xor_sync(0xffffffffu, v.y, o);
+        const float2 s = df_two_sum(v.x, u.x);
+        v.x = s.x;
+        v.y = __fadd_rn(s.y, __fadd_rn(v.y, u.y));
+    }
+    return v;
+}
+
+}  // namespace dsc

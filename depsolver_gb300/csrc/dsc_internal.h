@@ -90,7 +90,7 @@ struct DevBuf {
 // the caller; off by default so that the plain entry points pay nothing).
 enum TimerId {
     kTAsmRegular = 0, kTAsmFixup, kTAsmSingular, kTGemvK, kTGemmK, kTField, kTMst, kTResidual,
-    kTKrylov, kTCount
+    kTKrylov, kTCgs, kTCount
 };
 
 struct Timer {
@@ -103,11 +103,18 @@ struct Timer {
     std::vector<cudaEvent_t> pool;
     int open_id = -1;
     cudaEvent_t open_a = nullptr;
+    // algorithmic work per id since the last collect (units per id in the
+    // C ABI's dsc_session_timing)
+    double work[kTCount] = {};
     cudaEvent_t take();
     void begin(int id, cudaStream_t st);
     void end(cudaStream_t st);
-    // sums (ms) and launch counts per id since the last collect; resets
-    int collect(double *ms, int *count);
+    void add_work(int id, double w)
+    {
+        if (on) work[id] += w;
+    }
+    // sums (ms), scope counts and work per id since the last collect; resets
+    int collect(double *ms, int *count, double *wk);
     ~Timer();
 };
 

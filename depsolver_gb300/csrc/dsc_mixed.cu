@@ -21,6 +21,7 @@
 #include "../../include/depsolver_cuda.h"
 #include "dsc_blas.cuh"
 #include "dsc_common.cuh"
+#include "dsc_df32.cuh"
 #include "dsc_field.h"
 #include "dsc_internal.h"
 #include "dsc_session.h"
@@ -359,78 +360,61 @@ __global__ void k_residual_update(const float *__restrict__ P, int S, size_t spl
     R[(size_t)(2 * f + 1) * ld + i] -= s.x * yi + s.y * yr + d.x * di + d.y * dr;
 }
 
-// Complex dots h[k][f] = <V_k,f, W_f> = sum conj(v) w, for k < nk; one block
-// per (f, k), fixed-order block reduction.
-__global__ void __launch_bounds__(256) k_cgs_dots(const double *__restrict__ Vb, size_t vstride,
-                                                  const double *__restrict__ W, int N, size_t ld,
-                                                  int F, const int *__restrict__ active,
-                                                  double2 *__restrict__ h)
-{
-    __shared__ double sh[32];
-    const int f = blockIdx.x, k = blockIdx.y;
-    if (!active[f]) return;
-    const double *vr = Vb + (size_t)k * vstride + (size_t)(2 * f) * ld;
-    const double *vi = vr + ld;
-    const double *wr = W + (size_t)(2 * f) * ld, *wi = wr + ld;
-    double sr = 0.0, si = 0.0;
-    for (int i = threadIdx.x; i < N; i += blockDim.x) {
-        sr += vr[i] * wr[i] + vi[i] * wi[i];
-        si += vr[i] * wi[i] - vi[i] * wr[i];
-    }
-    double a = block_sum(sr, sh);
-    double b = block_sum(si, sh);
-    if (threadIdx.x == 0) h[(size_t)k * F + f] = make_double2(a, b);
-}
-
 // One pass over the basis: block (row chunk, f) stages its chunk of W_f in
-// shared memory, each warp forms the chunk's dots with V_k,f for k = warp,
-// warp + 8, ...; k_cgs_dots_reduce adds the chunks in order.
+// shared memory, each warp forms the chunk's dots <V_k,f, W_f> = sum conj(v) w
+// for k = warp, warp + 8, ... in double-FP32; k_cgs_dots_reduce adds the
+// chunks in order (FP64).
 constexpr int kDotRows = 1024;
 
-__global__ void __launch_bounds__(256) k_cgs_dots_chunk(const double *__restrict__ Vb, size_t vstride,
-                                                        const double *__restrict__ W, int N, size_t ld,
+__global__ void __launch_bounds__(256) k_cgs_dots_chunk(const float2 *__restrict__ Vb, size_t vstride,
+                                                        const float2 *__restrict__ W, int N, size_t ld,
                                                         int F, int nk, const int *__restrict__ active,
-                                                        double2 *__restrict__ part)
+                                                        double2 *__restrict__ part,
+                                                        unsigned long long *__restrict__ bytes)
 {
-    __shared__ double swr[kDotRows], swi[kDotRows];
+    __shared__ __align__(16) float2 swr[kDotRows], swi[kDotRows];
     const int chunk = blockIdx.x, f = blockIdx.y;
     if (!active[f]) return;
     const int r0 = chunk * kDotRows, nr = min(kDotRows, N - r0);
-    const double *wr = W + (size_t)(2 * f) * ld + r0, *wi = wr + ld;
+    if (bytes && threadIdx.x == 0) atomicAdd(bytes, (unsigned long long)nr * 16u * (nk + 1));
+    const float2 *wr = W + (size_t)(2 * f) * ld + r0, *wi = wr + ld;
     for (int t = threadIdx.x; t < nr; t += blockDim.x) {
         swr[t] = wr[t];
         swi[t] = wi[t];
     }
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int np = nr & ~1;
     for (int k = warp; k < nk; k += (int)(blockDim.x >> 5)) {
-        const double *vr = Vb + (size_t)k * vstride + (size_t)(2 * f) * ld + r0, *vi = vr + ld;
-        double sr = 0.0, si = 0.0;
-        // pairs of rows per lane (16-byte loads: r0 and ld are multiples of
-        // 32, so every pair is aligned), two pairs in flight per step
-        const int np = nr & ~1;
-        int t = 2 * lane;
-        for (; t + 64 < np; t += 128) {
-            const double2 a0 = *(const double2 *)(vr + t), b0 = *(const double2 *)(vi + t);
-            const double2 a1 = *(const double2 *)(vr + t + 64), b1 = *(const double2 *)(vi + t + 64);
-            sr += a0.x * swr[t] + b0.x * swi[t] + a0.y * swr[t + 1] + b0.y * swi[t + 1];
-            si += a0.x * swi[t] - b0.x * swr[t] + a0.y * swi[t + 1] - b0.y * swr[t + 1];
-            sr += a1.x * swr[t + 64] + b1.x * swi[t + 64] + a1.y * swr[t + 65] + b1.y * swi[t + 65];
-            si += a1.x * swi[t + 64] - b1.x * swr[t + 64] + a1.y * swi[t + 65] - b1.y * swr[t + 65];
-        }
-        for (; t < np; t += 64) {
-            const double2 a0 = *(const double2 *)(vr + t), b0 = *(const double2 *)(vi + t);
-            sr += a0.x * swr[t] + b0.x * swi[t] + a0.y * swr[t + 1] + b0.y * swi[t + 1];
-            si += a0.x * swi[t] - b0.x * swr[t] + a0.y * swi[t + 1] - b0.y * swr[t + 1];
+        const float2 *vr = Vb + (size_t)k * vstride + (size_t)(2 * f) * ld + r0, *vi = vr + ld;
+        float2 sr = make_float2(0.f, 0.f), si = make_float2(0.f, 0.f);
+        // two rows per lane and step (16-byte loads: r0 and ld are even)
+        for (int t = 2 * lane; t < np; t += 64) {
+            const float4 a = *(const float4 *)(vr + t), b = *(const float4 *)(vi + t);
+            const float4 c = *(const float4 *)(swr + t), d = *(const float4 *)(swi + t);
+            const float2 a0 = make_float2(a.x, a.y), a1 = make_float2(a.z, a.w);
+            const float2 b0 = make_float2(b.x, b.y), b1 = make_float2(b.z, b.w);
+            const float2 c0 = make_float2(c.x, c.y), c1 = make_float2(c.z, c.w);
+            const float2 d0 = make_float2(d.x, d.y), d1 = make_float2(d.z, d.w);
+            df_mac(sr, a0, c0);
+            df_mac(sr, b0, d0);
+            df_mac(si, a0, d0);
+            df_mac(si, df_neg(b0), c0);
+            df_mac(sr, a1, c1);
+            df_mac(sr, b1, d1);
+            df_mac(si, a1, d1);
+            df_mac(si, df_neg(b1), c1);
         }
         if (lane == 0 && np < nr) {
-            const double a = vr[np], b = vi[np], c = swr[np], d = swi[np];
-            sr += a * c + b * d;
-            si += a * d - b * c;
+            const float2 a0 = vr[np], b0 = vi[np], c0 = swr[np], d0 = swi[np];
+            df_mac(sr, a0, c0);
+            df_mac(sr, b0, d0);
+            df_mac(si, a0, d0);
+            df_mac(si, df_neg(b0), c0);
         }
-        sr = warp_sum(sr);
-        si = warp_sum(si);
-        if (lane == 0) part[((size_t)chunk * nk + k) * F + f] = make_double2(sr, si);
+        sr = df_warp_sum(sr);
+        si = df_warp_sum(si);
+        if (lane == 0) part[((size_t)chunk * nk + k) * F + f] = make_double2(df_to(sr), df_to(si));
     }
 }
 
@@ -450,31 +434,73 @@ __global__ void k_cgs_dots_reduce(const double2 *__restrict__ part, int nchunk, 
     h[t] = make_double2(sr, si);
 }
 
-// W_f -= sum_k h[k][f] V_k,f  (and hacc += h)
-__global__ void k_cgs_update(const double *__restrict__ Vb, size_t vstride, double *__restrict__ W,
-                             int N, size_t ld, int F, int nk, const int *__restrict__ active,
-                             const double2 *__restrict__ h, double2 *__restrict__ hacc)
+// W_f -= sum_k h[k][f] V_k,f in double-FP32 (and hacc += h).  Two rows per
+// thread; -h as double-FP32 pairs staged in shared memory per block.
+__global__ void __launch_bounds__(256) k_cgs_update(const float2 *__restrict__ Vb, size_t vstride,
+                                                    float2 *__restrict__ W, int N, size_t ld, int F,
+                                                    int nk, const int *__restrict__ active,
+                                                    const double2 *__restrict__ h,
+                                                    double2 *__restrict__ hacc,
+                                                    unsigned long long *__restrict__ bytes)
 {
-    // two consecutive rows per thread (16-byte loads; ld is a multiple of 32
-    // and the padding rows up to ld are allocated)
-    const int i = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    __shared__ float2 cr[kInnerMax + 1], ci[kInnerMax + 1], cin[kInnerMax + 1];
     const int f = blockIdx.y;
-    if (i >= N || !active[f]) return;
-    double2 wr = *(const double2 *)(W + (size_t)(2 * f) * ld + i);
-    double2 wi = *(const double2 *)(W + (size_t)(2 * f + 1) * ld + i);
-#pragma unroll 4
-    for (int k = 0; k < nk; k++) {
-        const double2 c = h[(size_t)k * F + f];
-        const double2 vr = *(const double2 *)(Vb + (size_t)k * vstride + (size_t)(2 * f) * ld + i);
-        const double2 vi = *(const double2 *)(Vb + (size_t)k * vstride + (size_t)(2 * f + 1) * ld + i);
-        wr.x -= c.x * vr.x - c.y * vi.x;
-        wi.x -= c.x * vi.x + c.y * vr.x;
-        wr.y -= c.x * vr.y - c.y * vi.y;
-        wi.y -= c.x * vi.y + c.y * vr.y;
+    if (!active[f]) return;
+    if (bytes && threadIdx.x == 0) {
+        const int rows = min(2 * (int)blockDim.x, N - 2 * (int)(blockIdx.x * blockDim.x));
+        if (rows > 0) atomicAdd(bytes, (unsigned long long)rows * 16u * (nk + 2));
     }
-    *(double2 *)(W + (size_t)(2 * f) * ld + i) = wr;
-    *(double2 *)(W + (size_t)(2 * f + 1) * ld + i) = wi;
-    if (hacc && i == 0)
+    for (int k = threadIdx.x; k < nk; k += blockDim.x) {
+        const double2 c = h[(size_t)k * F + f];
+        cr[k] = df_from(-c.x);
+        ci[k] = df_from(c.y);
+        cin[k] = df_from(-c.y);
+    }
+    __syncthreads();
+    const int i = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    if (i < N) {
+        float2 *wrp = W + (size_t)(2 * f) * ld + i, *wip = wrp + ld;
+        const float2 *vr = Vb + (size_t)(2 * f) * ld + i, *vi = vr + ld;
+        if (i + 1 < N) {
+            const float4 a = *(const float4 *)wrp, b = *(const float4 *)wip;
+            float2 wr0 = make_float2(a.x, a.y), wr1 = make_float2(a.z, a.w);
+            float2 wi0 = make_float2(b.x, b.y), wi1 = make_float2(b.z, b.w);
+#pragma unroll 2
+            for (int k = 0; k < nk; k++) {
+                const float4 p = *(const float4 *)(vr + (size_t)k * vstride);
+                const float4 q = *(const float4 *)(vi + (size_t)k * vstride);
+                const float2 p0 = make_float2(p.x, p.y), p1 = make_float2(p.z, p.w);
+                const float2 q0 = make_float2(q.x, q.y), q1 = make_float2(q.z, q.w);
+                const float2 a_r = cr[k], a_i = ci[k], a_in = cin[k];
+                df_mac(wr0, a_r, p0);   // wr -= hr vr - hi vi
+                df_mac(wr0, a_i, q0);
+                df_mac(wi0, a_r, q0);   // wi -= hr vi + hi vr
+                df_mac(wi0, a_in, p0);
+                df_mac(wr1, a_r, p1);
+                df_mac(wr1, a_i, q1);
+                df_mac(wi1, a_r, q1);
+                df_mac(wi1, a_in, p1);
+            }
+            wr0 = df_norm(wr0);
+            wr1 = df_norm(wr1);
+            wi0 = df_norm(wi0);
+            wi1 = df_norm(wi1);
+            *(float4 *)wrp = make_float4(wr0.x, wr0.y, wr1.x, wr1.y);
+            *(float4 *)wip = make_float4(wi0.x, wi0.y, wi1.x, wi1.y);
+        } else {
+            float2 wr0 = *wrp, wi0 = *wip;
+            for (int k = 0; k < nk; k++) {
+                const float2 p0 = vr[(size_t)k * vstride], q0 = vi[(size_t)k * vstride];
+                df_mac(wr0, cr[k], p0);
+                df_mac(wr0, ci[k], q0);
+                df_mac(wi0, cr[k], q0);
+                df_mac(wi0, cin[k], p0);
+            }
+            *wrp = df_norm(wr0);
+            *wip = df_norm(wi0);
+        }
+    }
+    if (hacc && blockIdx.x == 0 && threadIdx.x == 0)
         for (int k = 0; k < nk; k++) {
             double2 a = hacc[(size_t)k * F + f], c = h[(size_t)k * F + f];
             hacc[(size_t)k * F + f] = make_double2(a.x + c.x, a.y + c.y);
@@ -490,7 +516,7 @@ __global__ void k_dgks(const int *__restrict__ active, const double *__restrict_
     act2[f] = active[f] && n1[f] < 0.7071067811865476 * n0[f];
 }
 
-// nrm[f] = |W_f| (one block per system)
+// nrm[f] = |R_f| for FP64 vectors (one block per system)
 __global__ void __launch_bounds__(256) k_norms(const double *__restrict__ W, int N, size_t ld, int F,
                                                double *__restrict__ nrm)
 {
@@ -503,36 +529,114 @@ __global__ void __launch_bounds__(256) k_norms(const double *__restrict__ W, int
     if (threadIdx.x == 0) nrm[f] = sqrt(t);
 }
 
-// V_f = W_f * scale[f]
-__global__ void k_scale_into(const double *__restrict__ W, double *__restrict__ V, int N, size_t ld,
-                             int F, const double *__restrict__ scale, const int *__restrict__ active)
+// nrm[f] = |W_f| for double-FP32 vectors: the sum of squares accumulated in
+// double-FP32 per thread, warps and then the block's 8 warps added in a
+// fixed order (one block per system).
+__global__ void __launch_bounds__(256) k_norms_df(const float2 *__restrict__ W, int N, size_t ld, int F,
+                                                  double *__restrict__ nrm)
+{
+    __shared__ float2 sh[8];
+    const int f = blockIdx.x;
+    const float2 *wr = W + (size_t)(2 * f) * ld, *wi = wr + ld;
+    float2 s = make_float2(0.f, 0.f);
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        const float2 a = wr[i], b = wi[i];
+        df_mac(s, a, a);
+        df_mac(s, b, b);
+    }
+    s = df_warp_sum(s);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += df_to(sh[w]);
+        nrm[f] = sqrt(t);
+    }
+}
+
+// The GEMM operand of a Krylov vector: the tf32 pair of hi + lo.
+__device__ __forceinline__ void tf32_pair(float2 v, float &th, float &tl)
+{
+    uint32_t u;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(u) : "f"(v.x));
+    th = __uint_as_float(u);
+    tl = __fadd_rn(__fsub_rn(v.x, th), v.y);
+}
+
+// V_f = R_f * scale[f] (R in FP64) as double-FP32, and its tf32 pair for the
+// next tensor-core product (Bh, Bl: same layout, FP32).
+__global__ void k_scale_from64(const double *__restrict__ R, float2 *__restrict__ V,
+                               float *__restrict__ Bh, float *__restrict__ Bl, int N, size_t ld,
+                               int F, const double *__restrict__ scale,
+                               const int *__restrict__ active)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int f = blockIdx.y;
     if (i >= N) return;
     const double s = active[f] ? scale[f] : 0.0;
-    V[(size_t)(2 * f) * ld + i] = W[(size_t)(2 * f) * ld + i] * s;
-    V[(size_t)(2 * f + 1) * ld + i] = W[(size_t)(2 * f + 1) * ld + i] * s;
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+        const size_t o = (size_t)(2 * f + c) * ld + i;
+        const float2 v = df_from(R[o] * s);
+        float th, tl;
+        tf32_pair(v, th, tl);
+        V[o] = v;
+        Bh[o] = th;
+        Bl[o] = tl;
+    }
 }
 
-// X_f += sum_k y[k][f] V_k,f for k < m[f]
-__global__ void k_update_solution(double *__restrict__ X, const double *__restrict__ Vb,
+// V_f = W_f * scale[f] (double-FP32), and its tf32 pair.
+__global__ void k_scale_df(const float2 *__restrict__ W, float2 *__restrict__ V,
+                           float *__restrict__ Bh, float *__restrict__ Bl, int N, size_t ld, int F,
+                           const double *__restrict__ scale, const int *__restrict__ active)
+{
+    __shared__ float2 s;
+    const int f = blockIdx.y;
+    if (threadIdx.x == 0) s = df_from(active[f] ? scale[f] : 0.0);
+    __syncthreads();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+        const size_t o = (size_t)(2 * f + c) * ld + i;
+        const float2 v = df_mul(W[o], s);
+        float th, tl;
+        tf32_pair(v, th, tl);
+        V[o] = v;
+        Bh[o] = th;
+        Bl[o] = tl;
+    }
+}
+
+// D_f = sum_k y[k][f] V_k,f for k < m[f] (double-FP32 sum, FP64 result)
+__global__ void k_update_solution(double *__restrict__ D, const float2 *__restrict__ Vb,
                                   size_t vstride, int N, size_t ld, int F,
                                   const double2 *__restrict__ y, const int *__restrict__ m)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ float2 yr[kInnerMax], yi[kInnerMax], yin[kInnerMax];
     const int f = blockIdx.y;
-    if (i >= N) return;
-    double xr = X[(size_t)(2 * f) * ld + i], xi = X[(size_t)(2 * f + 1) * ld + i];
-    for (int k = 0; k < m[f]; k++) {
+    const int mf = m[f];
+    for (int k = threadIdx.x; k < mf; k += blockDim.x) {
         const double2 c = y[(size_t)k * F + f];
-        const double vr = Vb[(size_t)k * vstride + (size_t)(2 * f) * ld + i];
-        const double vi = Vb[(size_t)k * vstride + (size_t)(2 * f + 1) * ld + i];
-        xr += c.x * vr - c.y * vi;
-        xi += c.x * vi + c.y * vr;
+        yr[k] = df_from(c.x);
+        yi[k] = df_from(c.y);
+        yin[k] = df_from(-c.y);
     }
-    X[(size_t)(2 * f) * ld + i] = xr;
-    X[(size_t)(2 * f + 1) * ld + i] = xi;
+    __syncthreads();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    float2 xr = make_float2(0.f, 0.f), xi = make_float2(0.f, 0.f);
+    for (int k = 0; k < mf; k++) {
+        const float2 vr = Vb[(size_t)k * vstride + (size_t)(2 * f) * ld + i];
+        const float2 vi = Vb[(size_t)k * vstride + (size_t)(2 * f + 1) * ld + i];
+        df_mac(xr, yr[k], vr);
+        df_mac(xr, yin[k], vi);
+        df_mac(xi, yr[k], vi);
+        df_mac(xi, yi[k], vr);
+    }
+    D[(size_t)(2 * f) * ld + i] = df_to(xr);
+    D[(size_t)(2 * f + 1) * ld + i] = df_to(xi);
 }
 
 // ------------------------------------------------------- batched field
@@ -909,15 +1013,18 @@ __global__ void k_mst_batched_totals(const double *__restrict__ Fce, int npel, i
 
 struct Session::Mixed {
     int F = 0, S = 1;
-    DevBuf<double> Vb;      // (kInnerMax + 1) blocks of N x 2F (FP64)
+    DevBuf<float2> Vb;      // (kInnerMax + 1) blocks of N x 2F (double-FP32)
+    DevBuf<float2> W;       // the new Krylov vector (double-FP32)
+    DevBuf<float2> cs32, cd32;  // FP32 copies of the coefficients
     DevBuf<float> Vh, Vl;   // tf32 pair of the current Krylov block
     DevBuf<float> Yp;       // split-K partial products, S blocks
     DevBuf<int> err;        // set by the tensor-core kernel when a wait gives up
-    DevBuf<double> W, Xs, R, Y64, D;
+    DevBuf<double> Xs, R, Y64, D;
     DevBuf<double2> cs, cd, bt, h, hacc, ycoef, dpart;
     DevBuf<double> nrm, nrm0, scale, betad, itold, gc;
     DevBuf<double2> gH, gsn, gg;  // Givens state per system
     DevBuf<int> active, act0, act2, mcount;
+    DevBuf<unsigned long long> cgsb;  // bytes the Gram-Schmidt kernels moved (timing on)
     // batched field
     DevBuf<double> cf, part, sing, Enode, Fce, tot;
     // FP32 far-field pass: element centroids / offsets, split points, weights
@@ -935,24 +1042,31 @@ int Session::make_k32()
     return kOk;
 }
 
-// w_f = cs_f o (sum of the split partials of K v)_f + cd_f o v_f
+// w_f = cs_f o (sum of the split partials of K v)_f + cd_f o v_f, in FP32
+// (the product itself is FP32-accurate): the partials are added with
+// TwoSum compensation, the coefficients are FP32 copies.  W is written as
+// double-FP32 with a zero low part.
 __global__ void k_apply_epilogue_splits(const float *__restrict__ P, int S, size_t split_stride,
-                                        const double *__restrict__ V, const double2 *__restrict__ cs,
-                                        const double2 *__restrict__ cd, double *__restrict__ W, int N,
+                                        const float2 *__restrict__ V, const float2 *__restrict__ cs,
+                                        const float2 *__restrict__ cd, float2 *__restrict__ W, int N,
                                         size_t ld, int F)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int f = blockIdx.y;
     if (i >= N || f >= F) return;
-    double yr = 0.0, yi = 0.0;
+    const float *pr = P + (size_t)(2 * f) * ld + i, *pi = pr + ld;
+    float2 yr = make_float2(0.f, 0.f), yi = make_float2(0.f, 0.f);
     for (int s = 0; s < S; s++) {
-        yr += (double)P[(size_t)s * split_stride + (size_t)(2 * f) * ld + i];
-        yi += (double)P[(size_t)s * split_stride + (size_t)(2 * f + 1) * ld + i];
+        const float2 a = df_two_sum(yr.x, pr[(size_t)s * split_stride]);
+        const float2 b = df_two_sum(yi.x, pi[(size_t)s * split_stride]);
+        yr = make_float2(a.x, yr.y + a.y);
+        yi = make_float2(b.x, yi.y + b.y);
     }
-    const double vr = V[(size_t)(2 * f) * ld + i], vi = V[(size_t)(2 * f + 1) * ld + i];
-    const double2 s = cs[(size_t)f * N + i], d = cd[(size_t)f * N + i];
-    W[(size_t)(2 * f) * ld + i] = s.x * yr - s.y * yi + d.x * vr - d.y * vi;
-    W[(size_t)(2 * f + 1) * ld + i] = s.x * yi + s.y * yr + d.x * vi + d.y * vr;
+    const float ar = yr.x + yr.y, ai = yi.x + yi.y;
+    const float vr = V[(size_t)(2 * f) * ld + i].x, vi = V[(size_t)(2 * f + 1) * ld + i].x;
+    const float2 s = cs[(size_t)f * N + i], d = cd[(size_t)f * N + i];
+    W[(size_t)(2 * f) * ld + i] = make_float2(s.x * ar - s.y * ai + d.x * vr - d.y * vi, 0.f);
+    W[(size_t)(2 * f + 1) * ld + i] = make_float2(s.x * ai + s.y * ar + d.x * vi + d.y * vr, 0.f);
 }
 
 template <typename TA, typename TB, typename TC>
@@ -996,6 +1110,16 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
     }
     DSC_TRY(w.cs.upload(hcs, st));
     DSC_TRY(w.cd.upload(hcd, st));
+    {
+        std::vector<float2> c32((size_t)F * N), d32((size_t)F * N);
+        for (size_t t = 0; t < c32.size(); t++) {
+            c32[t] = make_float2((float)hcs[t].x, (float)hcs[t].y);
+            d32[t] = make_float2((float)hcd[t].x, (float)hcd[t].y);
+        }
+        DSC_TRY(w.cs32.upload(c32, st));
+        DSC_TRY(w.cd32.upload(d32, st));
+        DSC_CUDA(cudaStreamSynchronize(st));  // the host vectors go out of scope
+    }
     DSC_TRY(w.bt.upload(hbt, st));
     // x = 0, r = bt
     DSC_CUDA(cudaMemsetAsync(w.Xs.p, 0, blk * sizeof(double), st));
@@ -1043,46 +1167,55 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
         DSC_TRY(w.scale.upload(sc, st));
         DSC_TRY(w.betad.upload(beta, st));
         DSC_TRY(w.itold.upload(itol, st));
-        DSC_LAUNCH(k_scale_into<<<vg, 256, 0, st>>>(w.R.p, w.Vb.p, N, ld, F, w.scale.p, w.active.p));
+        DSC_LAUNCH(k_scale_from64<<<vg, 256, 0, st>>>(w.R.p, w.Vb.p, w.Vh.p, w.Vl.p, N, ld, F, w.scale.p,
+                                                      w.active.p));
         GivensState gst{w.gH.p, w.gc.p, w.gsn.p, w.gg.p};
         const int gb = (F + 63) / 64;
         DSC_LAUNCH(k_givens_init<<<gb, 64, 0, st>>>(gst, w.betad.p, F, w.mcount.p));
         std::vector<int> hact(F);
         for (int j = 0; j < kInnerMax; j++) {
-            const double *vj = w.Vb.p + (size_t)j * blk;
-            double *vn = w.Vb.p + (size_t)(j + 1) * blk;
+            const float2 *vj = w.Vb.p + (size_t)j * blk;
+            float2 *vn = w.Vb.p + (size_t)(j + 1) * blk;
             {
+                // the tf32 pair of v_j was written with v_j
                 TimerScope ts(tm, kTGemmK, st);
-                DSC_TRY(split_vec(vj, w.Vh.p, w.Vl.p, blk, st));
                 DSC_TRY(tc_gemm_3xtf32(s.Kt32.p, nullptr, ld, w.Vh.p, w.Vl.p, ld, N, 2 * F, N, w.Yp.p, ld,
                                        w.S, w.err.p, st));
+                tm->add_work(kTGemmK, 6.0 * N * N * 2 * F);  // three tf32 products
             }
-            TimerScope ts(tm, kTKrylov, st);
-            DSC_LAUNCH(k_apply_epilogue_splits<<<vg, 256, 0, st>>>(w.Yp.p, w.S, ld * 2 * (size_t)F, vj, w.cs.p,
-                                                                   w.cd.p, w.W.p, N, ld, F));
-            DSC_CUDA(cudaMemsetAsync(w.hacc.p, 0, (size_t)(j + 1) * F * sizeof(double2), st));
+            {
+                TimerScope ts(tm, kTKrylov, st);
+                DSC_LAUNCH(k_apply_epilogue_splits<<<vg, 256, 0, st>>>(w.Yp.p, w.S, ld * 2 * (size_t)F, vj,
+                                                                       w.cs32.p, w.cd32.p, w.W.p, N, ld, F));
+                DSC_CUDA(cudaMemsetAsync(w.hacc.p, 0, (size_t)(j + 1) * F * sizeof(double2), st));
+                DSC_LAUNCH(k_norms_df<<<F, 256, 0, st>>>(w.W.p, N, ld, F, w.nrm0.p));
+            }
             // classical Gram-Schmidt; the second pass only for the systems
             // whose vector lost more than 1 - 1/sqrt(2) of its norm in the
             // first (the DGKS criterion), decided on the device
-            DSC_LAUNCH(k_norms<<<F, 256, 0, st>>>(w.W.p, N, ld, F, w.nrm0.p));
+            unsigned long long *cgsb = tm->on ? w.cgsb.p : nullptr;
             for (int pass = 0; pass < 2; pass++) {
+                TimerScope tc(tm, kTCgs, st);
                 const int *mask = pass == 0 ? w.active.p : w.act2.p;
                 const int nchunk = (N + kDotRows - 1) / kDotRows;
                 if (pass == 1) {
-                    DSC_LAUNCH(k_norms<<<F, 256, 0, st>>>(w.W.p, N, ld, F, w.nrm.p));
+                    DSC_LAUNCH(k_norms_df<<<F, 256, 0, st>>>(w.W.p, N, ld, F, w.nrm.p));
                     DSC_LAUNCH(k_dgks<<<gb, 64, 0, st>>>(w.active.p, w.nrm0.p, w.nrm.p, F, w.act2.p));
                 }
                 DSC_LAUNCH(k_cgs_dots_chunk<<<dim3(nchunk, F), 256, 0, st>>>(w.Vb.p, blk, w.W.p, N, ld, F, j + 1,
-                                                                            mask, w.dpart.p));
+                                                                            mask, w.dpart.p, cgsb));
                 DSC_LAUNCH(k_cgs_dots_reduce<<<((j + 1) * F + 255) / 256, 256, 0, st>>>(w.dpart.p, nchunk, j + 1, F,
                                                                                        mask, w.h.p));
                 const dim3 vg2(((N + 1) / 2 + 255) / 256, F);
                 DSC_LAUNCH(k_cgs_update<<<vg2, 256, 0, st>>>(w.Vb.p, blk, w.W.p, N, ld, F, j + 1, mask, w.h.p,
-                                                 w.hacc.p));
+                                                             w.hacc.p, cgsb));
             }
-            DSC_LAUNCH(k_norms<<<F, 256, 0, st>>>(w.W.p, N, ld, F, w.nrm.p));
-            DSC_LAUNCH(k_givens_step<<<gb, 64, 0, st>>>(gst, w.hacc.p, w.nrm.p, j, F, w.betad.p, w.itold.p,
-                                                        w.active.p, w.scale.p, w.mcount.p));
+            {
+                TimerScope ts(tm, kTKrylov, st);
+                DSC_LAUNCH(k_norms_df<<<F, 256, 0, st>>>(w.W.p, N, ld, F, w.nrm.p));
+                DSC_LAUNCH(k_givens_step<<<gb, 64, 0, st>>>(gst, w.hacc.p, w.nrm.p, j, F, w.betad.p, w.itold.p,
+                                                            w.active.p, w.scale.p, w.mcount.p));
+            }
             DSC_CUDA(cudaGetLastError());
             if ((j + 1) % 4 == 0 || j + 1 == kInnerMax) {
                 // poll the converged systems every few steps only
@@ -1092,8 +1225,11 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
                 for (int f = 0; f < F; f++) still += hact[f];
                 if (still == 0) break;
             }
-            if (j + 1 < kInnerMax)
-                DSC_LAUNCH(k_scale_into<<<vg, 256, 0, st>>>(w.W.p, vn, N, ld, F, w.scale.p, w.active.p));
+            if (j + 1 < kInnerMax) {
+                TimerScope ts(tm, kTKrylov, st);
+                DSC_LAUNCH(k_scale_df<<<vg, 256, 0, st>>>(w.W.p, vn, w.Vh.p, w.Vl.p, N, ld, F, w.scale.p,
+                                                          w.active.p));
+            }
         }
         // triangular solves on the device, then x += V y below
         DSC_LAUNCH(k_backsolve<<<gb, 64, 0, st>>>(gst, w.mcount.p, w.act0.p, F, w.ycoef.p));
@@ -1102,7 +1238,6 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
         for (int f = 0; f < F; f++)
             if (act[f]) total_it[f] += mf[f];
         // correction d = V y, then x += d
-        DSC_CUDA(cudaMemsetAsync(w.D.p, 0, blk * sizeof(double), st));
         DSC_LAUNCH(k_update_solution<<<vg, 256, 0, st>>>(w.D.p, w.Vb.p, blk, N, ld, F, w.ycoef.p, w.mcount.p));
         DSC_LAUNCH(k_axpy_blocks<<<vg, 256, 0, st>>>(w.Xs.p, w.D.p, N, ld, F));
         if (outer == 0) {
@@ -1110,6 +1245,7 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
             TimerScope ts(tm, kTResidual, st);
             dim3 g((N + 63) / 64, (2 * F + 63) / 64);
             DSC_LAUNCH(k_gemm_df32<<<g, 256, 0, st>>>(s.K64.p, ld, w.Xs.p, ld, w.Y64.p, ld, N, 2 * F, N));
+            tm->add_work(kTResidual, (double)N * N * 2 * F);  // FP64-accurate multiply-adds
             DSC_LAUNCH(k_residual<<<vg, 256, 0, st>>>(w.Y64.p, w.Xs.p, w.cs.p, w.cd.p, w.bt.p, w.R.p, N, ld, F));
         } else {
             // later residuals are updated, r -= M d: d is small, so the
@@ -1118,6 +1254,7 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
             DSC_TRY(split_vec(w.D.p, w.Vh.p, w.Vl.p, blk, st));
             DSC_TRY(tc_gemm_3xtf32(s.Kt32.p, nullptr, ld, w.Vh.p, w.Vl.p, ld, N, 2 * F, N, w.Yp.p, ld, w.S,
                                    w.err.p, st));
+            tm->add_work(kTGemmK, 6.0 * N * N * 2 * F);
             DSC_LAUNCH(k_residual_update<<<vg, 256, 0, st>>>(w.Yp.p, w.S, ld * 2 * (size_t)F, w.D.p, w.cs.p,
                                                              w.cd.p, w.R.p, N, ld, F));
         }
@@ -1148,6 +1285,7 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
         DSC_TRY(w.Fce.alloc((size_t)F * std::max(fp.npel, 1) * 3));
         {
             TimerScope ts(tm, kTField, st);
+            tm->add_work(kTField, (double)P * E * F);  // (particle node, element) pairs x systems
             dim3 cg((E * kTriPts + 255) / 256, F);
             if (s.nen == 6) DSC_LAUNCH(k_charge_batched<6><<<cg, 256, 0, st>>>(s.dev.elems.p, E, s.dev.qp.p, w.Xs.p, ld, F, w.cf.p));
             else DSC_LAUNCH(k_charge_batched<3><<<cg, 256, 0, st>>>(s.dev.elems.p, E, s.dev.qp.p, w.Xs.p, ld, F, w.cf.p));
@@ -1219,6 +1357,19 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
     return kOk;
 }
 
+int Session::collect_timing(double *ms, int *count, double *work)
+{
+    DSC_TRY(timer.collect(ms, count, work));
+    if (mx && mx->cgsb.p) {
+        unsigned long long b = 0;
+        DSC_CUDA(cudaMemcpyAsync(&b, mx->cgsb.p, sizeof b, cudaMemcpyDeviceToHost, st));
+        DSC_CUDA(cudaMemsetAsync(mx->cgsb.p, 0, sizeof b, st));
+        DSC_CUDA(cudaStreamSynchronize(st));
+        work[kTCgs] += (double)b;
+    }
+    return kOk;
+}
+
 int Session::solve_mixed(unsigned nfreq, const double *freqs, double tol, unsigned max_iters,
                          double *sigma_host, double *forces_host, unsigned *iters)
 {
@@ -1258,8 +1409,11 @@ int Session::solve_mixed(unsigned nfreq, const double *freqs, double tol, unsign
         DSC_TRY(w.gH.alloc((size_t)Fmax * (kInnerMax + 1) * kInnerMax));
         DSC_TRY(w.mcount.alloc(Fmax));
         DSC_TRY(w.tot.alloc((size_t)Fmax * 9));
+        DSC_TRY(w.cgsb.alloc(1));
+        DSC_CUDA(cudaMemsetAsync(w.cgsb.p, 0, sizeof(unsigned long long), st));
         // the padding rows of the blocks are never read but keep them finite
-        DSC_CUDA(cudaMemsetAsync(w.Vb.p, 0, blk * (kInnerMax + 1) * sizeof(double), st));
+        DSC_CUDA(cudaMemsetAsync(w.Vb.p, 0, blk * (kInnerMax + 1) * sizeof(float2), st));
+        DSC_CUDA(cudaMemsetAsync(w.W.p, 0, blk * sizeof(float2), st));
         w.F = Fmax;
     }
     for (unsigned f0 = 0; f0 < nfreq; f0 += kMaxBatch) {

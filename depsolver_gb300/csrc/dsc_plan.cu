@@ -313,11 +313,13 @@ void Timer::end(cudaStream_t st)
     open_id = -1;
 }
 
-int Timer::collect(double *ms, int *count)
+int Timer::collect(double *ms, int *count, double *wk)
 {
     for (int k = 0; k < kTCount; k++) {
         ms[k] = 0.0;
         count[k] = 0;
+        wk[k] = work[k];
+        work[k] = 0.0;
     }
     for (auto &r : recs) {
         DSC_CUDA(cudaEventSynchronize(r.b));

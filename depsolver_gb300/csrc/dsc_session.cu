@@ -109,6 +109,7 @@ struct KFormOp : RealOp {
             TimerScope ts(tm, kTGemvK, st);
             dim3 g((N + 255) / 256, S);
             DSC_LAUNCH(k_gemv_K2<double><<<g, 256, 0, st>>>(K, ld, N, x, x + N, cols, part));
+            if (tm) tm->add_work(kTGemvK, 8.0 * N * N);  // bytes of K read
         }
         DSC_LAUNCH(k_kform_epilogue<<<(N + 255) / 256, 256, 0, st>>>(part, S, N, ca, cb, cd, x, y));
         DSC_CUDA(cudaGetLastError());
@@ -287,14 +288,15 @@ extern "C" int dsc_session_set_timing(dsc_session *s, int on)
     return kOk;
 }
 
-extern "C" int dsc_session_timing(dsc_session *s, double *ms, int *count, int n)
+extern "C" int dsc_session_timing(dsc_session *s, double *ms, int *count, double *work, int n)
 {
-    double t[kTCount];
+    double t[kTCount], wk[kTCount];
     int c[kTCount];
-    DSC_TRY(s->s.timer.collect(t, c));
+    DSC_TRY(s->s.collect_timing(t, c, wk));
     for (int k = 0; k < n && k < kTCount; k++) {
-        ms[k] = t[k];
-        count[k] = c[k];
+        if (ms) ms[k] = t[k];
+        if (count) count[k] = c[k];
+        if (work) work[k] = wk[k];
     }
     return kOk;
 }

@@ -46,6 +46,8 @@ struct Session {
                 std::vector<double> &d) const;
     int solve_fp64(double f, double tol, unsigned max_iters, double *sigma_dev, double *d_tot,
                    unsigned *iters);
+    // timer sums, scope counts and algorithmic work per class; resets
+    int collect_timing(double *ms, int *count, double *work);
     int solve_mixed(unsigned nfreq, const double *freqs, double tol, unsigned max_iters,
                     double *sigma_host, double *forces_host, unsigned *iters);
 };

@@ -181,15 +181,24 @@ void dsc_session_destroy(dsc_session *s);
 int dsc_session_assemble(dsc_session *s);
 int dsc_session_solve(dsc_session *s, int mode, unsigned nfreq, const double *freqs, double tol,
                       unsigned max_iters, double *sigma, double *forces, unsigned *iters);
-/* CUDA-event timing of kernel classes (off by default): ms[k] and launch
- * counts since the last call, k = 0 assembly regular pairs, 1 assembly
- * fix-up, 2 assembly singular pairs, 3 FP64 K GEMV, 4 K GEMM (mixed),
- * 5 field, 6 Maxwell stress, 7 FP64 residual GEMM, 8 Krylov updates. */
+/* CUDA-event timing of kernel classes (off by default).  Since the last
+ * call: ms[k] the summed time of class k, count[k] its timed scopes and
+ * work[k] its algorithmic work (any of the three may be NULL; n entries):
+ *   k = 0 assembly regular pairs   work: (row, element) pairs
+ *       1 assembly fix-up                0
+ *       2 assembly singular pairs        0
+ *       3 FP64 K GEMV                    bytes of K read
+ *       4 K GEMM (mixed, tensor cores)   flops of the three tf32 products
+ *       5 field                          (particle node, element) pairs x systems
+ *       6 Maxwell stress                 0
+ *       7 FP64-accurate residual GEMM    multiply-adds
+ *       8 other Krylov kernels           0
+ *       9 Gram-Schmidt passes            bytes the kernels read and wrote */
 int dsc_session_set_timing(dsc_session *s, int on);
 /* The CUDA stream (cudaStream_t) all of the session's work runs on, so a
  * caller can record its own events around a solve. */
 void *dsc_session_stream(dsc_session *s);
-int dsc_session_timing(dsc_session *s, double *ms, int *count, int n);
+int dsc_session_timing(dsc_session *s, double *ms, int *count, double *work, int n);
 
 /* Tensor-core product of host FP64 matrices, the kernel behind the mixed
  * sweep's matrix products (no counterpart call in the reference, whose

@@ -66,4 +66,16 @@ def test_session_timing_counts_kernels(gpu):
     s.solve([1e6], mode=api.MODE_FP64, tol=1e-6)
     t = s.timing()
     assert t["asm_regular"][1] >= 1 and t["gemv_K64"][1] >= 5 and t["field"][1] == 1
-    assert all(ms >= 0 for ms, _ in t.values())
+    assert all(ms >= 0 for ms, _, _ in t.values())
+    # algorithmic work: every (row, element) pair once; K read once per product
+    assert t["asm_regular"][2] == sc.N * sc.E
+    assert t["gemv_K64"][2] == 8.0 * sc.N * sc.N * t["gemv_K64"][1]
+    F = 3
+    s.solve(np.logspace(4, 7, F), mode=api.MODE_MIXED, tol=1e-10)
+    t = s.timing()
+    assert t["gemm_K"][1] >= 5 and t["gram_schmidt"][1] >= 5
+    assert t["gemm_K"][2] == 12.0 * sc.N * sc.N * F * t["gemm_K"][1]
+    # each Gram-Schmidt pass reads at least one basis vector of every
+    # active system (16 bytes per row and system)
+    assert t["gram_schmidt"][2] >= 16.0 * sc.N * t["gram_schmidt"][1]
+    assert t["asm_regular"][1] == 0 and t["residual_fp64"][2] == sc.N * sc.N * 2 * F
