@@ -290,7 +290,7 @@ def run_ours(args, rank, world):
     ev0.record(stream)
     for _ in range(args.steps):
         s.assemble()
-        s.solve(FREQS, mode=api.MODE_MIXED, tol=TOL)
+        _, its, _ = s.solve(FREQS, mode=api.MODE_MIXED, tol=TOL)
     ev1.record(stream)
     torch.cuda.synchronize()
     launches = int(L.dsc_kernel_launches() - l0)
@@ -343,6 +343,8 @@ def run_ours(args, rank, world):
         "fp64_path": {"value": 1.0 / fp64_s, "unit": UNIT, "ms_per_solve": fp64_s * 1e3,
                       "gmres_iters": int(itf[0])},
         "speedup_vs_fp64_path": value / world / (1.0 / fp64_s),
+        "inner_iterations": {"mean": float(np.mean(its)), "max": int(np.max(its)),
+                             "products_per_step": timing["gemm_K"][1] // max(1, args.steps)},
         "accuracy": {"force_err_vs_fp64": ferr, "sigma_rel_err_vs_fp64": serr,
                      "force_err_def": "max over 3 frequencies of |Fcm_mixed - Fcm_fp64| / sum|Fce|"},
         "kernels_ms": {k: {"ms": v[0], "scopes": v[1], "share": v[0] / total_ms if total_ms else 0}

@@ -93,4 +93,18 @@ __device__ __forceinline__ float2 df_warp_sum(float2 v)
     return v;
 }
 
+// Block-wide sum (blockDim.x a multiple of 32, at most 32 warps): warps by
+// shuffles, then thread 0 adds the warps in order in FP64.  The result is
+// valid in thread 0; sh holds one float2 per warp.  Every thread must call.
+__device__ __forceinline__ double df_block_sum(float2 v, float2 *sh)
+{
+    v = df_warp_sum(v);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += df_to(sh[w]);
+    return t;
+}
+
 }  // namespace dsc

@@ -35,7 +35,11 @@ typedef std::complex<double> cplx;
 constexpr int kMaxBatch = 64;   // frequencies per batch
 constexpr int kInnerMax = 80;   // Krylov dimension of one inner solve
 constexpr int kOuterMax = 6;    // refinement steps
-constexpr double kInnerTol = 1e-6;
+// Floor of the inner tolerance: near the accuracy of the FP32 products.
+// Measured on the 12k-node scene (64 frequencies to 1e-10): 1e-6 took 110
+// products per sweep (the slowest systems needed a third refinement step),
+// 3e-7 took 89, 1e-7 took 93.
+constexpr double kInnerTol = 3e-7;
 
 // ------------------------------------------------------------ GEMM (SIMT)
 // C (M x Nc) = A (M x Kd) * B (Kd x Nc), all column-major.  64 x 64 tile,
@@ -441,9 +445,10 @@ __global__ void __launch_bounds__(256) k_cgs_update(const float2 *__restrict__ V
                                                     int nk, const int *__restrict__ active,
                                                     const double2 *__restrict__ h,
                                                     double2 *__restrict__ hacc,
+                                                    double *__restrict__ npart,
                                                     unsigned long long *__restrict__ bytes)
 {
-    __shared__ float2 cr[kInnerMax + 1], ci[kInnerMax + 1], cin[kInnerMax + 1];
+    __shared__ float2 cr[kInnerMax + 1], ci[kInnerMax + 1], cin[kInnerMax + 1], sh[8];
     const int f = blockIdx.y;
     if (!active[f]) return;
     if (bytes && threadIdx.x == 0) {
@@ -458,6 +463,7 @@ __global__ void __launch_bounds__(256) k_cgs_update(const float2 *__restrict__ V
     }
     __syncthreads();
     const int i = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    float2 n2 = make_float2(0.f, 0.f);
     if (i < N) {
         float2 *wrp = W + (size_t)(2 * f) * ld + i, *wip = wrp + ld;
         const float2 *vr = Vb + (size_t)(2 * f) * ld + i, *vi = vr + ld;
@@ -487,6 +493,10 @@ __global__ void __launch_bounds__(256) k_cgs_update(const float2 *__restrict__ V
             wi1 = df_norm(wi1);
             *(float4 *)wrp = make_float4(wr0.x, wr0.y, wr1.x, wr1.y);
             *(float4 *)wip = make_float4(wi0.x, wi0.y, wi1.x, wi1.y);
+            df_mac(n2, wr0, wr0);
+            df_mac(n2, wi0, wi0);
+            df_mac(n2, wr1, wr1);
+            df_mac(n2, wi1, wi1);
         } else {
             float2 wr0 = *wrp, wi0 = *wip;
             for (int k = 0; k < nk; k++) {
@@ -496,10 +506,16 @@ __global__ void __launch_bounds__(256) k_cgs_update(const float2 *__restrict__ V
                 df_mac(wi0, cr[k], q0);
                 df_mac(wi0, cin[k], p0);
             }
-            *wrp = df_norm(wr0);
-            *wip = df_norm(wi0);
+            wr0 = df_norm(wr0);
+            wi0 = df_norm(wi0);
+            *wrp = wr0;
+            *wip = wi0;
+            df_mac(n2, wr0, wr0);
+            df_mac(n2, wi0, wi0);
         }
     }
+    const double t = df_block_sum(n2, sh);
+    if (threadIdx.x == 0) npart[(size_t)f * gridDim.x + blockIdx.x] = t;
     if (hacc && blockIdx.x == 0 && threadIdx.x == 0)
         for (int k = 0; k < nk; k++) {
             double2 a = hacc[(size_t)k * F + f], c = h[(size_t)k * F + f];
@@ -507,13 +523,25 @@ __global__ void __launch_bounds__(256) k_cgs_update(const float2 *__restrict__ V
         }
 }
 
-// act2[f]: system f needs the second Gram-Schmidt pass
-__global__ void k_dgks(const int *__restrict__ active, const double *__restrict__ n0,
-                       const double *__restrict__ n1, int F, int *__restrict__ act2)
+// nrm[f] = sqrt(sum of the nb block partials of |w_f|^2), in block order,
+// for the systems in mask.  With n0 (not null): also act2[f], whether the
+// system needs the second Gram-Schmidt pass, by the DGKS test (its vector
+// lost more than 1 - 1/sqrt(2) of its norm n0[f] in the first pass).
+__global__ void k_norm_finish(const double *__restrict__ npart, int nb, int F,
+                              const int *__restrict__ mask, double *__restrict__ nrm,
+                              const double *__restrict__ n0, int *__restrict__ act2)
 {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= F) return;
-    act2[f] = active[f] && n1[f] < 0.7071067811865476 * n0[f];
+    if (!mask[f]) {
+        if (n0) act2[f] = 0;
+        return;
+    }
+    double t = 0.0;
+    for (int b = 0; b < nb; b++) t += npart[(size_t)f * nb + b];
+    const double n = sqrt(t);
+    nrm[f] = n;
+    if (n0) act2[f] = n < 0.7071067811865476 * n0[f];
 }
 
 // nrm[f] = |R_f| for FP64 vectors (one block per system)
@@ -529,31 +557,6 @@ __global__ void __launch_bounds__(256) k_norms(const double *__restrict__ W, int
     if (threadIdx.x == 0) nrm[f] = sqrt(t);
 }
 
-// nrm[f] = |W_f| for double-FP32 vectors: the sum of squares accumulated in
-// double-FP32 per thread, warps and then the block's 8 warps added in a
-// fixed order (one block per system).
-__global__ void __launch_bounds__(256) k_norms_df(const float2 *__restrict__ W, int N, size_t ld, int F,
-                                                  double *__restrict__ nrm)
-{
-    __shared__ float2 sh[8];
-    const int f = blockIdx.x;
-    const float2 *wr = W + (size_t)(2 * f) * ld, *wi = wr + ld;
-    float2 s = make_float2(0.f, 0.f);
-    for (int i = threadIdx.x; i < N; i += blockDim.x) {
-        const float2 a = wr[i], b = wi[i];
-        df_mac(s, a, a);
-        df_mac(s, b, b);
-    }
-    s = df_warp_sum(s);
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += df_to(sh[w]);
-        nrm[f] = sqrt(t);
-    }
-}
-
 // The GEMM operand of a Krylov vector: the tf32 pair of hi + lo.
 __device__ __forceinline__ void tf32_pair(float2 v, float &th, float &tl)
 {
@@ -561,6 +564,8 @@ __device__ __forceinline__ void tf32_pair(float2 v, float &th, float &tl)
     asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(u) : "f"(v.x));
     th = __uint_as_float(u);
     tl = __fadd_rn(__fsub_rn(v.x, th), v.y);
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(u) : "f"(tl));  // the tensor core would truncate it
+    tl = __uint_as_float(u);
 }
 
 // V_f = R_f * scale[f] (R in FP64) as double-FP32, and its tf32 pair for the
@@ -1025,6 +1030,7 @@ struct Session::Mixed {
     DevBuf<double2> gH, gsn, gg;  // Givens state per system
     DevBuf<int> active, act0, act2, mcount;
     DevBuf<unsigned long long> cgsb;  // bytes the Gram-Schmidt kernels moved (timing on)
+    DevBuf<double> npart;   // per-block partials of |w|^2
     // batched field
     DevBuf<double> cf, part, sing, Enode, Fce, tot;
     // FP32 far-field pass: element centroids / offsets, split points, weights
@@ -1037,23 +1043,18 @@ int Session::make_k32()
     if (k32_ready) return kOk;
     DSC_TRY(assemble64());
     DSC_TRY(Kt32.alloc(ld * N));
-    DSC_TRY(split_transpose_K(K64.p, ld, N, Kt32.p, nullptr, ld, st));
+    DSC_TRY(split_transpose_K(K64.p, ld, N, Kt32.p, nullptr, ld, st, true));
     k32_ready = true;
     return kOk;
 }
 
-// w_f = cs_f o (sum of the split partials of K v)_f + cd_f o v_f, in FP32
-// (the product itself is FP32-accurate): the partials are added with
-// TwoSum compensation, the coefficients are FP32 copies.  W is written as
-// double-FP32 with a zero low part.
-__global__ void k_apply_epilogue_splits(const float *__restrict__ P, int S, size_t split_stride,
-                                        const float2 *__restrict__ V, const float2 *__restrict__ cs,
-                                        const float2 *__restrict__ cd, float2 *__restrict__ W, int N,
-                                        size_t ld, int F)
+// One row of the epilogue: writes and returns (Re w, Im w).
+__device__ __forceinline__ float2 epilogue_row_impl(const float *__restrict__ P, int S, size_t split_stride,
+                                                    const float2 *__restrict__ V,
+                                                    const float2 *__restrict__ cs,
+                                                    const float2 *__restrict__ cd,
+                                                    float2 *__restrict__ W, int N, size_t ld, int f, int i)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int f = blockIdx.y;
-    if (i >= N || f >= F) return;
     const float *pr = P + (size_t)(2 * f) * ld + i, *pi = pr + ld;
     float2 yr = make_float2(0.f, 0.f), yi = make_float2(0.f, 0.f);
     for (int s = 0; s < S; s++) {
@@ -1065,9 +1066,36 @@ __global__ void k_apply_epilogue_splits(const float *__restrict__ P, int S, size
     const float ar = yr.x + yr.y, ai = yi.x + yi.y;
     const float vr = V[(size_t)(2 * f) * ld + i].x, vi = V[(size_t)(2 * f + 1) * ld + i].x;
     const float2 s = cs[(size_t)f * N + i], d = cd[(size_t)f * N + i];
-    W[(size_t)(2 * f) * ld + i] = make_float2(s.x * ar - s.y * ai + d.x * vr - d.y * vi, 0.f);
-    W[(size_t)(2 * f + 1) * ld + i] = make_float2(s.x * ai + s.y * ar + d.x * vi + d.y * vr, 0.f);
+    const float wr = s.x * ar - s.y * ai + d.x * vr - d.y * vi;
+    const float wi = s.x * ai + s.y * ar + d.x * vi + d.y * vr;
+    W[(size_t)(2 * f) * ld + i] = make_float2(wr, 0.f);
+    W[(size_t)(2 * f + 1) * ld + i] = make_float2(wi, 0.f);
+    return make_float2(wr, wi);
 }
+
+// w_f = cs_f o (sum of the split partials of K v)_f + cd_f o v_f, in FP32
+// (the product itself is FP32-accurate): the partials are added with
+// TwoSum compensation, the coefficients are FP32 copies.  W is written as
+// double-FP32 with a zero low part; npart[f][block] = the block's share of
+// |w_f|^2 (k_norm_finish adds them).
+__global__ void __launch_bounds__(256) k_apply_epilogue_splits(
+    const float *__restrict__ P, int S, size_t split_stride, const float2 *__restrict__ V,
+    const float2 *__restrict__ cs, const float2 *__restrict__ cd, float2 *__restrict__ W, int N,
+    size_t ld, int F, double *__restrict__ npart)
+{
+    __shared__ float2 sh[8];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int f = blockIdx.y;
+    float2 n2 = make_float2(0.f, 0.f);
+    if (i < N) {
+        const float2 wv = epilogue_row_impl(P, S, split_stride, V, cs, cd, W, N, ld, f, i);
+        df_mac(n2, make_float2(wv.x, 0.f), make_float2(wv.x, 0.f));
+        df_mac(n2, make_float2(wv.y, 0.f), make_float2(wv.y, 0.f));
+    }
+    const double t = df_block_sum(n2, sh);
+    if (threadIdx.x == 0) npart[(size_t)f * gridDim.x + blockIdx.x] = t;
+}
+
 
 template <typename TA, typename TB, typename TC>
 static int gemm(const TA *A, size_t lda, const TB *B, size_t ldb, TC *C, size_t ldc, int M, int Nc,
@@ -1180,39 +1208,46 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
                 // the tf32 pair of v_j was written with v_j
                 TimerScope ts(tm, kTGemmK, st);
                 DSC_TRY(tc_gemm_3xtf32(s.Kt32.p, nullptr, ld, w.Vh.p, w.Vl.p, ld, N, 2 * F, N, w.Yp.p, ld,
-                                       w.S, w.err.p, st));
+                                       w.S, w.err.p, st, true));
                 tm->add_work(kTGemmK, 6.0 * N * N * 2 * F);  // three tf32 products
             }
             {
                 TimerScope ts(tm, kTKrylov, st);
                 DSC_LAUNCH(k_apply_epilogue_splits<<<vg, 256, 0, st>>>(w.Yp.p, w.S, ld * 2 * (size_t)F, vj,
-                                                                       w.cs32.p, w.cd32.p, w.W.p, N, ld, F));
+                                                                       w.cs32.p, w.cd32.p, w.W.p, N, ld, F,
+                                                                       w.npart.p));
                 DSC_CUDA(cudaMemsetAsync(w.hacc.p, 0, (size_t)(j + 1) * F * sizeof(double2), st));
-                DSC_LAUNCH(k_norms_df<<<F, 256, 0, st>>>(w.W.p, N, ld, F, w.nrm0.p));
+                DSC_LAUNCH(k_norm_finish<<<gb, 64, 0, st>>>(w.npart.p, (int)vg.x, F, w.active.p, w.nrm0.p, nullptr,
+                                                            nullptr));
             }
             // classical Gram-Schmidt; the second pass only for the systems
             // whose vector lost more than 1 - 1/sqrt(2) of its norm in the
-            // first (the DGKS criterion), decided on the device
+            // first (the DGKS criterion), decided on the device.  The norms
+            // come from block partials written by the epilogue and update
+            // kernels.
             unsigned long long *cgsb = tm->on ? w.cgsb.p : nullptr;
+            const dim3 vg2(((N + 1) / 2 + 255) / 256, F);
             for (int pass = 0; pass < 2; pass++) {
                 TimerScope tc(tm, kTCgs, st);
                 const int *mask = pass == 0 ? w.active.p : w.act2.p;
                 const int nchunk = (N + kDotRows - 1) / kDotRows;
-                if (pass == 1) {
-                    DSC_LAUNCH(k_norms_df<<<F, 256, 0, st>>>(w.W.p, N, ld, F, w.nrm.p));
-                    DSC_LAUNCH(k_dgks<<<gb, 64, 0, st>>>(w.active.p, w.nrm0.p, w.nrm.p, F, w.act2.p));
-                }
                 DSC_LAUNCH(k_cgs_dots_chunk<<<dim3(nchunk, F), 256, 0, st>>>(w.Vb.p, blk, w.W.p, N, ld, F, j + 1,
                                                                             mask, w.dpart.p, cgsb));
                 DSC_LAUNCH(k_cgs_dots_reduce<<<((j + 1) * F + 255) / 256, 256, 0, st>>>(w.dpart.p, nchunk, j + 1, F,
                                                                                        mask, w.h.p));
-                const dim3 vg2(((N + 1) / 2 + 255) / 256, F);
                 DSC_LAUNCH(k_cgs_update<<<vg2, 256, 0, st>>>(w.Vb.p, blk, w.W.p, N, ld, F, j + 1, mask, w.h.p,
-                                                             w.hacc.p, cgsb));
+                                                             w.hacc.p, w.npart.p, cgsb));
+                // pass 0: |w| of every active system and the DGKS decision;
+                // pass 1: |w| of the systems that took the second pass
+                if (pass == 0)
+                    DSC_LAUNCH(k_norm_finish<<<gb, 64, 0, st>>>(w.npart.p, (int)vg2.x, F, w.active.p, w.nrm.p,
+                                                                w.nrm0.p, w.act2.p));
+                else
+                    DSC_LAUNCH(k_norm_finish<<<gb, 64, 0, st>>>(w.npart.p, (int)vg2.x, F, w.act2.p, w.nrm.p,
+                                                                nullptr, nullptr));
             }
             {
                 TimerScope ts(tm, kTKrylov, st);
-                DSC_LAUNCH(k_norms_df<<<F, 256, 0, st>>>(w.W.p, N, ld, F, w.nrm.p));
                 DSC_LAUNCH(k_givens_step<<<gb, 64, 0, st>>>(gst, w.hacc.p, w.nrm.p, j, F, w.betad.p, w.itold.p,
                                                             w.active.p, w.scale.p, w.mcount.p));
             }
@@ -1253,7 +1288,7 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
             TimerScope ts(tm, kTGemmK, st);
             DSC_TRY(split_vec(w.D.p, w.Vh.p, w.Vl.p, blk, st));
             DSC_TRY(tc_gemm_3xtf32(s.Kt32.p, nullptr, ld, w.Vh.p, w.Vl.p, ld, N, 2 * F, N, w.Yp.p, ld, w.S,
-                                   w.err.p, st));
+                                   w.err.p, st, true));
             tm->add_work(kTGemmK, 6.0 * N * N * 2 * F);
             DSC_LAUNCH(k_residual_update<<<vg, 256, 0, st>>>(w.Yp.p, w.S, ld * 2 * (size_t)F, w.D.p, w.cs.p,
                                                              w.cd.p, w.R.p, N, ld, F));
@@ -1410,6 +1445,7 @@ int Session::solve_mixed(unsigned nfreq, const double *freqs, double tol, unsign
         DSC_TRY(w.mcount.alloc(Fmax));
         DSC_TRY(w.tot.alloc((size_t)Fmax * 9));
         DSC_TRY(w.cgsb.alloc(1));
+        DSC_TRY(w.npart.alloc((size_t)Fmax * ((N + 255) / 256)));
         DSC_CUDA(cudaMemsetAsync(w.cgsb.p, 0, sizeof(unsigned long long), st));
         // the padding rows of the blocks are never read but keep them finite
         DSC_CUDA(cudaMemsetAsync(w.Vb.p, 0, blk * (kInnerMax + 1) * sizeof(float2), st));

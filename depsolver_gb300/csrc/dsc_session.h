@@ -29,8 +29,9 @@ struct Session {
     // plain FP64 path workspace
     DevBuf<double> ca, cb, cd, gemv_part;
 
-    // mixed path: K as row-major FP32 (split into tf32 pairs inside the
-    // tensor-core products), and the batched-solver workspace
+    // mixed path: K as row-major FP32 in the biased tf32 encoding (split
+    // into tf32 pairs inside the tensor-core products), and the
+    // batched-solver workspace
     bool k32_ready = false;
     DevBuf<float> Kt32;
     struct Mixed;

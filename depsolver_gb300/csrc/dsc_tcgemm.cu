@@ -149,6 +149,13 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *b)
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(b)) : "memory");
 }
 
+// The tf32 value the tensor core reads from an FP32 word: the top 19 bits
+// (the low 13 mantissa bits are ignored).
+__device__ __forceinline__ float tf32_trunc(float v)
+{
+    return __uint_as_float(__float_as_uint(v) & 0xFFFFE000u);
+}
+
 __device__ __forceinline__ float tf32_rna(float v)
 {
     uint32_t h;
@@ -156,17 +163,62 @@ __device__ __forceinline__ float tf32_rna(float v)
     return __uint_as_float(h);
 }
 
-// SPLIT_A = false: A arrives as a tf32 pair (tmAh, tmAl).
-// SPLIT_A = true: A arrives as plain FP32 through tmAh into the hi slot and
-// warps 2 and 3 split it in shared memory (hi rounded to tf32 in place, the
-// remainder into the lo slot) before the MMA issuer may read the stage.
-template <bool SPLIT_A>
+// lo of the split a = trunc(a) + lo, itself rounded to tf32 so that the
+// tensor core's truncation of it loses nothing more
+__device__ __forceinline__ float tf32_lo(float v)
+{
+    return tf32_rna(v - tf32_trunc(v));
+}
+
+// Half a tf32 unit in the last place of t (t's sign; 0 for tiny t).
+__device__ __forceinline__ float tf32_half_ulp(float t)
+{
+    const uint32_t u = __float_as_uint(t);
+    const uint32_t e = u & 0x7F800000u;
+    return e > (11u << 23) ? __uint_as_float((u & 0x80000000u) | (e - (11u << 23))) : 0.0f;
+}
+
+// Biased encoding of an FP32 value a for the tensor core: s = a + half-ulp
+// of h = rna_tf32(a), with a's sign, so that the truncation the tensor core
+// applies to s gives h (the round-to-nearest hi) and the low part can be
+// recovered as s - trunc(s) - half-ulp, |lo| <= half a tf32 ulp.
+__device__ __forceinline__ float tf32_bias_encode(float a)
+{
+    return __fadd_rn(a, tf32_half_ulp(tf32_rna(a)));
+}
+
+// trunc(s) + half-ulp is s's top 19 bits with mantissa bit 12 set (for
+// normal s), so the low part is one exact subtraction.
+__device__ __forceinline__ float tf32_lo_biased(float s)
+{
+    const float mid = __uint_as_float((__float_as_uint(s) & 0xFFFFE000u) | 0x00001000u);
+    return tf32_rna(__fsub_rn(s, mid));
+}
+
+// AMODE 0: A arrives as a tf32 pair (tmAh, tmAl).
+// AMODE 1: A arrives as plain FP32 through tmAh into the hi slot; the tensor
+// core reads it as its truncated tf32 value, and warps 2 and 3 write the
+// remainder a - trunc(a), rounded to tf32, into the lo slot before the
+// products with lo may read the stage.
+// AMODE 2: as 1, with A in the biased encoding (tf32_bias_encode): the
+// truncation gives the round-to-nearest hi, so |lo| is half as large and the
+// dropped lo*lo product is at 2^-22 instead of 2^-21.
+// COMB (BN a multiple of 32, at most 128): Ah*Bh and Ah*Bl are one MMA of
+// N = 2 BN against the adjacent Bh and Bl tiles, into accumulator columns
+// [0, BN) and [BN, 2 BN); Al*Bh goes to [2 BN, 3 BN); the epilogue adds the
+// three.  This reads Ah once instead of twice, and keeps the small products
+// out of the main accumulator: the tensor core's FP32 accumulation
+// truncates (sums of positive products come out low), so every MMA added
+// into an accumulator costs up to one of its units in the last place.
+template <int AMODE>
 __global__ void __launch_bounds__(128, 1)
     k_tc_gemm_3xtf32(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
                      const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl,
                      int M, int Nc, int BN, int nkb_total, int kb_per_split, float *__restrict__ Y,
                      size_t ldy, size_t split_stride, int tmem_cols, int *err)
 {
+    constexpr bool SPLIT_A = AMODE != 0;
+    const bool comb = BN <= 128 && BN % 32 == 0;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const uint32_t a_bytes = kTcBM * 128, b_bytes = (uint32_t)BN * 128;
@@ -225,44 +277,61 @@ __global__ void __launch_bounds__(128, 1)
         }
     } else if (warp == 1 && lane == 0 && nkb > 0) {
         // ---- MMA issuer
-        const uint32_t idesc = idesc_tf32(BN, kTcBM);
+        const uint32_t idesc = idesc_tf32(BN, kTcBM), idesc2 = idesc_tf32(2 * BN, kTcBM);
         for (int i = 0; i < nkb; i++) {
             const int s = i % kTcStages;
-            if (!mbar_wait(SPLIT_A ? &splitb[s] : &full[s], (i / kTcStages) & 1, err, 2)) break;
+            if (!mbar_wait(&full[s], (i / kTcStages) & 1, err, 2)) break;
             tc_fence_after();
             uint8_t *st = smem + s * stage_bytes;
             const uint64_t dah = sw128_desc(st), dal = sw128_desc(st + a_bytes);
             const uint64_t dbh = sw128_desc(st + 2 * a_bytes), dbl = sw128_desc(st + 2 * a_bytes + b_bytes);
+            // products with Ah: the stage as it landed
 #pragma unroll
             for (int kk = 0; kk < kTcBK / 8; kk++) {
                 const uint64_t off = (uint64_t)(kk * 32) >> 4;  // 8 tf32 = 32 bytes
-                mma_tf32(tmem, dal + off, dbh + off, idesc, (i | kk) != 0);
-                mma_tf32(tmem, dah + off, dbl + off, idesc, 1);
-                mma_tf32(tmem, dah + off, dbh + off, idesc, 1);
+                if (comb) {
+                    mma_tf32(tmem, dah + off, dbh + off, idesc2, (i | kk) != 0);
+                } else {
+                    mma_tf32(tmem, dah + off, dbh + off, idesc, (i | kk) != 0);
+                    mma_tf32(tmem, dah + off, dbl + off, idesc, 1);
+                }
+            }
+            // products with Al: after the split
+            if (SPLIT_A) {
+                if (!mbar_wait(&splitb[s], (i / kTcStages) & 1, err, 2)) break;
+                tc_fence_after();
+            }
+#pragma unroll
+            for (int kk = 0; kk < kTcBK / 8; kk++) {
+                const uint64_t off = (uint64_t)(kk * 32) >> 4;
+                if (comb) mma_tf32(tmem + 2 * BN, dal + off, dbh + off, idesc, (i | kk) != 0);
+                else mma_tf32(tmem, dal + off, dbh + off, idesc, 1);
             }
             mma_commit(&empty[s]);
         }
         mma_commit(accum);
     } else if (SPLIT_A && warp >= 2 && nkb > 0) {
-        // ---- splitters: FP32 A tile -> tf32 hi (in place) + lo
+        // ---- splitters: lo = rna_tf32(a - trunc_tf32(a)) of the FP32 A tile
         const int tid = threadIdx.x - 64;
         for (int i = 0; i < nkb; i++) {
             const int s = i % kTcStages;
             if (!mbar_wait(&full[s], (i / kTcStages) & 1, err, 4)) break;
-            float4 *hi = (float4 *)(smem + s * stage_bytes);
+            const float4 *hi = (const float4 *)(smem + s * stage_bytes);
             float4 *lo = (float4 *)(smem + s * stage_bytes + a_bytes);
             for (int t = tid; t < (int)(a_bytes / 16); t += 64) {
                 const float4 v = hi[t];
-                float4 h, l;
-                h.x = tf32_rna(v.x);
-                h.y = tf32_rna(v.y);
-                h.z = tf32_rna(v.z);
-                h.w = tf32_rna(v.w);
-                l.x = v.x - h.x;
-                l.y = v.y - h.y;
-                l.z = v.z - h.z;
-                l.w = v.w - h.w;
-                hi[t] = h;
+                float4 l;
+                if (AMODE == 2) {
+                    l.x = tf32_lo_biased(v.x);
+                    l.y = tf32_lo_biased(v.y);
+                    l.z = tf32_lo_biased(v.z);
+                    l.w = tf32_lo_biased(v.w);
+                } else {
+                    l.x = tf32_lo(v.x);
+                    l.y = tf32_lo(v.y);
+                    l.z = tf32_lo(v.z);
+                    l.w = tf32_lo(v.w);
+                }
                 lo[t] = l;
             }
             // generic-proxy writes must be visible to the tensor core's reads
@@ -284,6 +353,14 @@ __global__ void __launch_bounds__(128, 1)
         uint32_t r[32];
         if (have) {
             tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, r);
+            if (comb) {
+                uint32_t r2[32], r3[32];
+                tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(BN + c0), r2);
+                tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(2 * BN + c0), r3);
+#pragma unroll
+                for (int j = 0; j < 32; j++)
+                    r[j] = __float_as_uint(__uint_as_float(r[j]) + (__uint_as_float(r2[j]) + __uint_as_float(r3[j])));
+            }
         } else {
 #pragma unroll
             for (int j = 0; j < 32; j++) r[j] = 0u;
@@ -348,14 +425,16 @@ static int make_map(CUtensorMap *map, const float *base, int rows, int k, size_t
 
 int tc_gemm_3xtf32(const float *Ah, const float *Al, size_t lda, const float *Bh, const float *Bl,
                    size_t ldb, int M, int Nc, int Kd, float *Y, size_t ldy, int splits, int *d_err,
-                   cudaStream_t st)
+                   cudaStream_t st, bool a_biased)
 {
     if (Nc < 1 || Nc > 256 || M < 1 || Kd < 1 || ldy < (size_t)M) {
         set_error("tc_gemm_3xtf32: unsupported shape M %d Nc %d Kd %d", M, Nc, Kd);
         return kErrArg;
     }
     const int BN = (Nc + 15) / 16 * 16;
-    const int tmem_cols = BN <= 32 ? 32 : BN <= 64 ? 64 : BN <= 128 ? 128 : 256;
+    const int acc_cols = (BN <= 128 && BN % 32 == 0) ? 3 * BN : BN;  // see COMB in the kernel
+    int tmem_cols = 32;
+    while (tmem_cols < acc_cols) tmem_cols *= 2;
     const bool split_a = Al == nullptr;  // plain FP32 A, split in shared memory
     CUtensorMap ah, al, bh, bl;
     DSC_TRY(make_map(&ah, Ah, M, Kd, lda, kTcBM));
@@ -369,17 +448,15 @@ int tc_gemm_3xtf32(const float *Ah, const float *Al, size_t lda, const float *Bh
     splits = (nkb + kps - 1) / kps;  // every split has at least one k-block
     const size_t smem = 1024 + (size_t)kTcStages * (2 * kTcBM * 128 + 2 * BN * 128) + 256;
     dim3 grid((M + kTcBM - 1) / kTcBM, splits);
-    if (split_a) {
-        DSC_CUDA(cudaFuncSetAttribute(k_tc_gemm_3xtf32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem));
-        DSC_LAUNCH(k_tc_gemm_3xtf32<true><<<grid, 128, smem, st>>>(ah, al, bh, bl, M, Nc, BN, nkb, kps, Y, ldy,
-                                                                  ldy * (size_t)Nc, tmem_cols, d_err));
-    } else {
-        DSC_CUDA(cudaFuncSetAttribute(k_tc_gemm_3xtf32<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem));
-        DSC_LAUNCH(k_tc_gemm_3xtf32<false><<<grid, 128, smem, st>>>(ah, al, bh, bl, M, Nc, BN, nkb, kps, Y, ldy,
-                                                                   ldy * (size_t)Nc, tmem_cols, d_err));
-    }
+    auto launch = [&](auto kern) -> int {
+        DSC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        DSC_LAUNCH(kern<<<grid, 128, smem, st>>>(ah, al, bh, bl, M, Nc, BN, nkb, kps, Y, ldy,
+                                                 ldy * (size_t)Nc, tmem_cols, d_err));
+        return kOk;
+    };
+    if (!split_a) DSC_TRY(launch(k_tc_gemm_3xtf32<0>));
+    else if (a_biased) DSC_TRY(launch(k_tc_gemm_3xtf32<2>));
+    else DSC_TRY(launch(k_tc_gemm_3xtf32<1>));
     DSC_CUDA(cudaGetLastError());
     return kOk;
 }
@@ -398,20 +475,19 @@ int tc_gemm_splits_for(int M, int Kd)
 }
 
 // ---------------------------------------------------------- operand split
-// tf32 pair of a value: hi = round-to-nearest tf32, lo = value - hi.
+// tf32 pair of a value: hi = round-to-nearest tf32, lo = value - hi, also
+// rounded to tf32 (the tensor core would truncate it).
 __device__ __forceinline__ void tf32_split(double v, float &hi, float &lo)
 {
-    float f = (float)v;
-    uint32_t h;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(f));
-    hi = __uint_as_float(h);
-    lo = (float)(v - (double)hi);
+    hi = tf32_rna((float)v);
+    lo = tf32_rna((float)(v - (double)hi));
 }
 
 // Column-major FP64 K (entry (i, c) at c * ld + i) to row-major tf32 pairs
 // (entry (i, c) at i * ldt + c): a 32 x 32 shared tile per block.
 __global__ void k_split_transpose(const double *__restrict__ K, size_t ld, int N,
-                                  float *__restrict__ Th, float *__restrict__ Tl, size_t ldt)
+                                  float *__restrict__ Th, float *__restrict__ Tl, size_t ldt,
+                                  bool biased)
 {
     __shared__ double t[32][33];
     const int i0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
@@ -424,7 +500,8 @@ __global__ void k_split_transpose(const double *__restrict__ K, size_t ld, int N
         int i = i0 + k, c = c0 + threadIdx.x;
         if (i < N && c < N) {
             if (!Tl) {
-                Th[(size_t)i * ldt + c] = (float)t[threadIdx.x][k];  // plain FP32
+                const float v = (float)t[threadIdx.x][k];  // plain FP32, or biased
+                Th[(size_t)i * ldt + c] = biased ? tf32_bias_encode(v) : v;
                 continue;
             }
             float h, l;
@@ -449,10 +526,10 @@ __global__ void k_split_vec(const double *__restrict__ x, float *__restrict__ h,
 }
 
 int split_transpose_K(const double *K, size_t ld, int N, float *Th, float *Tl, size_t ldt,
-                      cudaStream_t st)
+                      cudaStream_t st, bool biased)
 {
     dim3 g((N + 31) / 32, (N + 31) / 32), b(32, 8);
-    DSC_LAUNCH(k_split_transpose<<<g, b, 0, st>>>(K, ld, N, Th, Tl, ldt));
+    DSC_LAUNCH(k_split_transpose<<<g, b, 0, st>>>(K, ld, N, Th, Tl, ldt, biased));
     DSC_CUDA(cudaGetLastError());
     return kOk;
 }
@@ -464,11 +541,12 @@ int split_vec(const double *x, float *h, float *l, size_t n, cudaStream_t st)
     return kOk;
 }
 
-__global__ void k_to_f32_plain(const double *__restrict__ x, float *__restrict__ y, size_t n)
+__global__ void k_to_f32_plain(const double *__restrict__ x, float *__restrict__ y, size_t n,
+                               bool biased)
 {
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n;
          t += (size_t)gridDim.x * blockDim.x)
-        y[t] = (float)x[t];
+        y[t] = biased ? tf32_bias_encode((float)x[t]) : (float)x[t];
 }
 
 // Y (M x Nc, row-major FP64) = sum over splits of the partial tiles.
@@ -573,7 +651,8 @@ extern "C" int dsc_tc_gemm(int M, int Nc, int Kd, const double *A, const double 
     DSC_TRY(Al.alloc((size_t)M * lda));
     DSC_TRY(Bh.alloc((size_t)Nc * lda));
     DSC_TRY(Bl.alloc((size_t)Nc * lda));
-    if (a_in_smem) DSC_LAUNCH(k_to_f32_plain<<<4 * 152, 256, 0, st>>>(dA.p, Ah.p, (size_t)M * lda));
+    if (a_in_smem)
+        DSC_LAUNCH(k_to_f32_plain<<<4 * 152, 256, 0, st>>>(dA.p, Ah.p, (size_t)M * lda, a_in_smem == 2));
     else DSC_TRY(split_vec(dA.p, Ah.p, Al.p, (size_t)M * lda, st));
     DSC_TRY(split_vec(dB.p, Bh.p, Bl.p, (size_t)Nc * lda, st));
     if (splits <= 0) splits = tc_gemm_splits_for(M, Kd);
@@ -584,7 +663,7 @@ extern "C" int dsc_tc_gemm(int M, int Nc, int Kd, const double *A, const double 
     DSC_CUDA(cudaMemset(err.p, 0, sizeof(int)));
     DSC_CUDA(cudaMemset(P.p, 0, (size_t)S * Nc * M * sizeof(float)));
     DSC_TRY(tc_gemm_3xtf32(Ah.p, a_in_smem ? nullptr : Al.p, lda, Bh.p, Bl.p, lda, M, Nc, Kd, P.p,
-                           (size_t)M, S, err.p, st));
+                           (size_t)M, S, err.p, st, a_in_smem == 2));
     DSC_TRY(dY.alloc((size_t)M * Nc));
     dim3 g((M + 255) / 256, Nc);
     DSC_LAUNCH(k_sum_splits<<<g, 256, 0, st>>>(P.p, S, (size_t)M * Nc, (size_t)M, M, Nc, dY.p));

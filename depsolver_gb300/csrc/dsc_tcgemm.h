@@ -12,15 +12,18 @@ namespace dsc {
 // A: M x Kd, B: Nc x Kd, both K-major FP32 holding tf32 pairs, row strides
 // lda / ldb (multiples of 4 elements, 16-byte aligned bases).  Nc <= 256.
 // *d_err (device, zero on entry) is set when a wait inside the kernel gives
-// up.  The caller adds the splits.
+// up.  The caller adds the splits.  Al = null: A is plain FP32 (split in
+// shared memory), or with a_biased in the encoding split_transpose_K(...,
+// biased = true) writes.
 int tc_gemm_3xtf32(const float *Ah, const float *Al, size_t lda, const float *Bh, const float *Bl,
                    size_t ldb, int M, int Nc, int Kd, float *Y, size_t ldy, int splits, int *d_err,
-                   cudaStream_t st);
+                   cudaStream_t st, bool a_biased = false);
 int tc_gemm_splits_for(int M, int Kd);
 
-// Column-major FP64 N x N matrix (stride ld) to row-major tf32 pairs.
+// Column-major FP64 N x N matrix (stride ld) to row-major tf32 pairs, or
+// (Tl = null) to row-major FP32, plain or in the biased tf32 encoding.
 int split_transpose_K(const double *K, size_t ld, int N, float *Th, float *Tl, size_t ldt,
-                      cudaStream_t st);
+                      cudaStream_t st, bool biased = false);
 // FP64 array to tf32 pairs, elementwise.
 int split_vec(const double *x, float *h, float *l, size_t n, cudaStream_t st);
 // Row-major FP64 rows x k (row stride ld) to tf32 pairs (row stride ldh).

@@ -21,7 +21,7 @@ def _run(L, A, B, splits, a_in_smem=1):
     return Y
 
 
-@pytest.mark.parametrize("a_in_smem", [0, 1])
+@pytest.mark.parametrize("a_in_smem", [0, 1, 2])
 @pytest.mark.parametrize("M,Nc,Kd,splits", [
     (128, 16, 32, 1),      # one tile, one k-block
     (300, 40, 1000, 1),    # ragged everything, one split
