@@ -239,7 +239,9 @@ def run_ours(args, rank, world):
     dev = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev)
     L = _native.lib()
-    sc = scenes.cfg1()
+    # the 12k-node scene of the metric; --scene mid (level-3 sphere between
+    # 25 x 25-cell plates, N = 7764) only for profiler captures of one step
+    sc = scenes.cfg1() if args.scene == "cfg1" else scenes.sphere_between_plates(3, 25, name="mid")
     N, E = sc.N, sc.E
     s = api.Session(sc)
     stream = torch.cuda.ExternalStream(s.stream_handle())
@@ -397,9 +399,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--scene", choices=["cfg1", "mid"], default="cfg1",
+                    help="mid: a smaller scene for ncu captures (with --only-step)")
     ap.add_argument("--only-step", action="store_true",
                     help="run one warm-up and one step and nothing else (profiling)")
     args = ap.parse_args()
+    if args.scene != "cfg1" and not args.only_step:
+        ap.error("--scene mid is for profiler captures: use it with --only-step")
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     if world > 1 and args.impl == "ours":

@@ -97,11 +97,13 @@ __global__ void __launch_bounds__(256) k_gemm_cm(const TA *__restrict__ A, size_
     }
 }
 
-// C (M x Nc, FP64) = A (M x Kd) * B (Kd x Nc), all FP64 column-major, to
-// about FP64 accuracy on the FP32 pipes: each operand is split into an FP32
-// pair (hi, lo); the product hi*hi is made exact with an FMA (p + e), the
-// running sum is an unevaluated pair (s, c) kept exact by TwoSum, and the
-// cross terms hi*lo + lo*hi go into c.  64 x 64 tile, 4 x 4 outputs per
+// C (M x Nc, FP64) = A (M x Kd) * B (Kd x Nc), column-major, to about FP64
+// accuracy on the FP32 pipes: each operand is an FP32 pair (hi, lo); the
+// product hi*hi is made exact with an FMA (p + e), the running sum is an
+// unevaluated pair (s, c) kept exact by TwoSum, and the cross terms
+// hi*lo + lo*hi go into c.  A is FP64 and split while it is staged (its
+// conversions run on the FP64 pipe, once per element: a tile spans 128
+// columns); B comes pre-split (Bh, Bl).  64 x 128 tile, 4 x 8 outputs per
 // thread, k-steps of 16.
 __device__ __forceinline__ void df32_acc(float &s, float &c, float ah, float al, float bh, float bl)
 {
@@ -117,61 +119,79 @@ __device__ __forceinline__ void df32_acc(float &s, float &c, float ah, float al,
 }
 
 __global__ void __launch_bounds__(256) k_gemm_df32(const double *__restrict__ A, size_t lda,
-                                                   const double *__restrict__ B, size_t ldb,
+                                                   const float *__restrict__ Bh,
+                                                   const float *__restrict__ Bl, size_t ldb,
                                                    double *__restrict__ C, size_t ldc, int M, int Nc,
                                                    int Kd)
 {
     __shared__ float Ah[16][64 + 1], Al[16][64 + 1];
-    __shared__ float Bh[16][64 + 1], Bl[16][64 + 1];
-    const int m0 = blockIdx.x * 64, n0 = blockIdx.y * 64;
+    __shared__ float Bsh[16][128 + 1], Bsl[16][128 + 1];
+    const int m0 = blockIdx.x * 64, n0 = blockIdx.y * 128;
     const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-    float s[4][4], c[4][4];
+    float s[4][8], c[4][8];
 #pragma unroll
     for (int u = 0; u < 4; u++)
 #pragma unroll
-        for (int v = 0; v < 4; v++) s[u][v] = c[u][v] = 0.0f;
+        for (int v = 0; v < 8; v++) s[u][v] = c[u][v] = 0.0f;
     for (int k0 = 0; k0 < Kd; k0 += 16) {
         for (int t = threadIdx.x; t < 16 * 64; t += 256) {
-            int kk = t / 64, mm = t % 64;
-            int m = m0 + mm, k = k0 + kk;
-            double a = (m < M && k < Kd) ? A[(size_t)k * lda + m] : 0.0;
-            float h = (float)a;
+            const int kk = t / 64, mm = t % 64;
+            const int m = m0 + mm, k = k0 + kk;
+            const double a = (m < M && k < Kd) ? A[(size_t)k * lda + m] : 0.0;
+            const float h = (float)a;
             Ah[kk][mm] = h;
             Al[kk][mm] = (float)(a - (double)h);
-            int nn = t / 16, kb = t % 16;
-            int n = n0 + nn, k2 = k0 + kb;
-            double b = (n < Nc && k2 < Kd) ? B[(size_t)n * ldb + k2] : 0.0;
-            float g = (float)b;
-            Bh[kb][nn] = g;
-            Bl[kb][nn] = (float)(b - (double)g);
+        }
+        for (int t = threadIdx.x; t < 16 * 128; t += 256) {
+            const int nn = t / 16, kb = t % 16;
+            const int n = n0 + nn, k = k0 + kb;
+            const bool in = n < Nc && k < Kd;
+            Bsh[kb][nn] = in ? Bh[(size_t)n * ldb + k] : 0.0f;
+            Bsl[kb][nn] = in ? Bl[(size_t)n * ldb + k] : 0.0f;
         }
         __syncthreads();
-#pragma unroll 4
+#pragma unroll 2
         for (int kk = 0; kk < 16; kk++) {
-            float ah[4], al[4], bh[4], bl[4];
+            float ah[4], al[4], bh[8], bl[8];
 #pragma unroll
             for (int u = 0; u < 4; u++) {
                 ah[u] = Ah[kk][ty + 16 * u];
                 al[u] = Al[kk][ty + 16 * u];
-                bh[u] = Bh[kk][tx + 16 * u];
-                bl[u] = Bl[kk][tx + 16 * u];
+            }
+#pragma unroll
+            for (int v = 0; v < 8; v++) {
+                bh[v] = Bsh[kk][tx + 16 * v];
+                bl[v] = Bsl[kk][tx + 16 * v];
             }
 #pragma unroll
             for (int u = 0; u < 4; u++)
 #pragma unroll
-                for (int v = 0; v < 4; v++) df32_acc(s[u][v], c[u][v], ah[u], al[u], bh[v], bl[v]);
+                for (int v = 0; v < 8; v++) df32_acc(s[u][v], c[u][v], ah[u], al[u], bh[v], bl[v]);
         }
         __syncthreads();
     }
 #pragma unroll
     for (int u = 0; u < 4; u++) {
-        int m = m0 + ty + 16 * u;
+        const int m = m0 + ty + 16 * u;
         if (m >= M) continue;
 #pragma unroll
-        for (int v = 0; v < 4; v++) {
-            int n = n0 + tx + 16 * v;
+        for (int v = 0; v < 8; v++) {
+            const int n = n0 + tx + 16 * v;
             if (n < Nc) C[(size_t)n * ldc + m] = (double)s[u][v] + (double)c[u][v];
         }
+    }
+}
+
+// FP64 array to FP32 pairs (hi = rounded value, lo = the rest, rounded).
+__global__ void k_split_f32_pair(const double *__restrict__ x, float *__restrict__ h,
+                                 float *__restrict__ l, size_t n)
+{
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n;
+         t += (size_t)gridDim.x * blockDim.x) {
+        const double v = x[t];
+        const float a = (float)v;
+        h[t] = a;
+        l[t] = (float)(v - (double)a);
     }
 }
 
@@ -1021,6 +1041,8 @@ struct Session::Mixed {
     DevBuf<float2> Vb;      // (kInnerMax + 1) blocks of N x 2F (double-FP32)
     DevBuf<float2> W;       // the new Krylov vector (double-FP32)
     DevBuf<float2> cs32, cd32;  // FP32 copies of the coefficients
+    DevBuf<double> Ak, Bk;      // interface coefficients of the batch (F x nIf)
+    DevBuf<float> Xh, Xl;       // FP32 pair of the solution (FP64-accurate residual)
     DevBuf<float> Vh, Vl;   // tf32 pair of the current Krylov block
     DevBuf<float> Yp;       // split-K partial products, S blocks
     DevBuf<int> err;        // set by the tensor-core kernel when a wait gives up
@@ -1097,6 +1119,42 @@ __global__ void __launch_bounds__(256) k_apply_epilogue_splits(
 }
 
 
+// Per system f and row i, from the interface coefficients of the batch
+// (Ak, Bk: F x nIf; src/assembly_el.c:223-239): s = a - i b (1 on conductor
+// rows), d = -1/(2 eps0) on interface rows (0 otherwise), the complex Jacobi
+// scale p = 1 / (s K_ii + d), and cs = p s, cd = p d, bt = p (boundary value)
+// in FP64 and FP32; R (the first residual, x = 0) = bt.
+__global__ void k_prepare_systems(const int *__restrict__ iface_row, const double *__restrict__ Kdiag,
+                                  const double *__restrict__ bre, const double *__restrict__ bim,
+                                  const double *__restrict__ Ak, const double *__restrict__ Bk, int nIf,
+                                  int N, size_t ld, int F, double2 *__restrict__ cs,
+                                  double2 *__restrict__ cd, double2 *__restrict__ bt,
+                                  float2 *__restrict__ cs32, float2 *__restrict__ cd32,
+                                  double *__restrict__ R)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int f = blockIdx.y;
+    if (i >= N) return;
+    const int k = iface_row[i];
+    const double a = k < 0 ? 1.0 : Ak[(size_t)f * nIf + k];
+    const double b = k < 0 ? 0.0 : -Bk[(size_t)f * nIf + k];  // s = a + i b
+    const double d = k < 0 ? 0.0 : -0.5 / kEps0;
+    const double gr = a * Kdiag[i] + d, gi = b * Kdiag[i];      // s K_ii + d
+    const double q = 1.0 / (gr * gr + gi * gi);
+    const double pr = gr * q, pi = -gi * q;                      // p = 1 / (s K_ii + d)
+    const double2 c1 = make_double2(pr * a - pi * b, pr * b + pi * a);
+    const double2 c2 = make_double2(pr * d, pi * d);
+    const double2 r = make_double2(pr * bre[i] - pi * bim[i], pr * bim[i] + pi * bre[i]);
+    const size_t o = (size_t)f * N + i;
+    cs[o] = c1;
+    cd[o] = c2;
+    bt[o] = r;
+    cs32[o] = make_float2((float)c1.x, (float)c1.y);
+    cd32[o] = make_float2((float)c2.x, (float)c2.y);
+    R[(size_t)(2 * f) * ld + i] = r.x;
+    R[(size_t)(2 * f + 1) * ld + i] = r.y;
+}
+
 template <typename TA, typename TB, typename TC>
 static int gemm(const TA *A, size_t lda, const TB *B, size_t ldb, TC *C, size_t ldc, int M, int Nc,
                 int Kd, cudaStream_t st)
@@ -1117,50 +1175,25 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
     const size_t blk = ld * 2 * (size_t)F;  // one N x 2F block
     cudaStream_t st = s.st;
     Timer *tm = &s.timer;
-    // coefficients, complex Jacobi, scaled right-hand sides
-    std::vector<double2> hcs((size_t)F * N), hcd((size_t)F * N), hbt((size_t)F * N);
-    std::vector<double> bnorm(F, 0.0);
-    for (int f = 0; f < F; f++) {
-        std::vector<double> a, b, d;
-        s.coeffs(freqs[f], a, b, d);
-        for (int i = 0; i < N; i++) {
-            cplx sv(a[i], -b[i]);
-            cplx diag = sv * s.Kdiag_host[i] + d[i];
-            cplx p = 1.0 / diag;
-            cplx c1 = p * sv, c2 = p * d[i];
-            cplx rhs = p * cplx(s.mbc[3 * (size_t)i], s.mbc[3 * (size_t)(i + N)]);
-            hcs[(size_t)f * N + i] = make_double2(c1.real(), c1.imag());
-            hcd[(size_t)f * N + i] = make_double2(c2.real(), c2.imag());
-            hbt[(size_t)f * N + i] = make_double2(rhs.real(), rhs.imag());
-            bnorm[f] += std::norm(rhs);
-        }
-        bnorm[f] = sqrt(bnorm[f]);
-    }
-    DSC_TRY(w.cs.upload(hcs, st));
-    DSC_TRY(w.cd.upload(hcd, st));
+    // coefficients, complex Jacobi, scaled right-hand sides: on the device,
+    // from the interface coefficients of each frequency
+    const int nIfc = std::max(1, (int)s.nIf);
     {
-        std::vector<float2> c32((size_t)F * N), d32((size_t)F * N);
-        for (size_t t = 0; t < c32.size(); t++) {
-            c32[t] = make_float2((float)hcs[t].x, (float)hcs[t].y);
-            d32[t] = make_float2((float)hcd[t].x, (float)hcd[t].y);
-        }
-        DSC_TRY(w.cs32.upload(c32, st));
-        DSC_TRY(w.cd32.upload(d32, st));
-        DSC_CUDA(cudaStreamSynchronize(st));  // the host vectors go out of scope
-    }
-    DSC_TRY(w.bt.upload(hbt, st));
-    // x = 0, r = bt
-    DSC_CUDA(cudaMemsetAsync(w.Xs.p, 0, blk * sizeof(double), st));
-    {
-        std::vector<double> r(blk, 0.0);
+        std::vector<double> Ak((size_t)F * nIfc, 0.0), Bk((size_t)F * nIfc, 0.0);
         for (int f = 0; f < F; f++)
-            for (int i = 0; i < N; i++) {
-                r[(size_t)(2 * f) * ld + i] = hbt[(size_t)f * N + i].x;
-                r[(size_t)(2 * f + 1) * ld + i] = hbt[(size_t)f * N + i].y;
-            }
-        DSC_CUDA(cudaMemcpyAsync(w.R.p, r.data(), blk * sizeof(double), cudaMemcpyHostToDevice, st));
-        DSC_CUDA(cudaStreamSynchronize(st));
+            if (s.nIf)
+                interface_coeffs(s.nIf, s.ifaces.data(), s.mat.data(), freqs[f], &Ak[(size_t)f * nIfc],
+                                 &Bk[(size_t)f * nIfc]);
+        DSC_TRY(w.Ak.upload(Ak, st));
+        DSC_TRY(w.Bk.upload(Bk, st));
+        DSC_LAUNCH(k_prepare_systems<<<dim3((N + 255) / 256, F), 256, 0, st>>>(
+            s.rows.p, s.Kdiag.p, s.bre.p, s.bim.p, w.Ak.p, w.Bk.p, nIfc, N, ld, F, w.cs.p, w.cd.p,
+            w.bt.p, w.cs32.p, w.cd32.p, w.R.p));
+        DSC_CUDA(cudaStreamSynchronize(st));  // Ak, Bk go out of scope
     }
+    // x = 0; |b_f| is the first residual norm
+    DSC_CUDA(cudaMemsetAsync(w.Xs.p, 0, blk * sizeof(double), st));
+    std::vector<double> bnorm(F, 0.0);
     const dim3 vg((N + 255) / 256, F);
     std::vector<int> done(F, 0), total_it(F, 0);
     std::vector<double> rn(F);
@@ -1169,6 +1202,7 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
         DSC_LAUNCH(k_norms<<<F, 256, 0, st>>>(w.R.p, N, ld, F, w.nrm.p));
         DSC_CUDA(cudaMemcpyAsync(rn.data(), w.nrm.p, F * sizeof(double), cudaMemcpyDeviceToHost, st));
         DSC_CUDA(cudaStreamSynchronize(st));
+        if (outer == 0) bnorm = rn;
         int nact = 0;
         for (int f = 0; f < F; f++) {
             done[f] = rn[f] <= tol * bnorm[f];
@@ -1278,8 +1312,10 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
         if (outer == 0) {
             // the first residual in FP64: r = bt - M x
             TimerScope ts(tm, kTResidual, st);
-            dim3 g((N + 63) / 64, (2 * F + 63) / 64);
-            DSC_LAUNCH(k_gemm_df32<<<g, 256, 0, st>>>(s.K64.p, ld, w.Xs.p, ld, w.Y64.p, ld, N, 2 * F, N));
+            DSC_LAUNCH(k_split_f32_pair<<<4 * 152, 256, 0, st>>>(w.Xs.p, w.Xh.p, w.Xl.p, blk));
+            dim3 g((N + 63) / 64, (2 * F + 127) / 128);
+            DSC_LAUNCH(k_gemm_df32<<<g, 256, 0, st>>>(s.K64.p, ld, w.Xh.p, w.Xl.p, ld, w.Y64.p, ld, N, 2 * F,
+                                                      N));
             tm->add_work(kTResidual, (double)N * N * 2 * F);  // FP64-accurate multiply-adds
             DSC_LAUNCH(k_residual<<<vg, 256, 0, st>>>(w.Y64.p, w.Xs.p, w.cs.p, w.cd.p, w.bt.p, w.R.p, N, ld, F));
         } else {
@@ -1422,6 +1458,13 @@ int Session::solve_mixed(unsigned nfreq, const double *freqs, double tol, unsign
         DSC_TRY(w.err.alloc(1));
         DSC_CUDA(cudaMemsetAsync(w.err.p, 0, sizeof(int), st));
         DSC_TRY(w.W.alloc(blk));
+        DSC_TRY(w.Xh.alloc(blk));
+        DSC_TRY(w.Xl.alloc(blk));
+        DSC_TRY(w.cs.alloc((size_t)Fmax * N));
+        DSC_TRY(w.cd.alloc((size_t)Fmax * N));
+        DSC_TRY(w.bt.alloc((size_t)Fmax * N));
+        DSC_TRY(w.cs32.alloc((size_t)Fmax * N));
+        DSC_TRY(w.cd32.alloc((size_t)Fmax * N));
         DSC_TRY(w.Xs.alloc(blk));
         DSC_TRY(w.R.alloc(blk));
         DSC_TRY(w.Y64.alloc(blk));

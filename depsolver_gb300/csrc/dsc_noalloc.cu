@@ -75,8 +75,8 @@ extern "C" int dsc_tc_gemm_noalloc(int M, int Nc, int Kd, const float *A, size_t
                                    void *stream)
 {
     // shapes first: these checks touch no device
-    if (M < 1 || Kd < 1 || Nc < 1 || Nc > 256) {
-        set_error("dsc_tc_gemm_noalloc: unsupported shape M %d Nc %d Kd %d (M, Kd >= 1, 1 <= Nc <= 256)",
+    if (M < 1 || Kd < 1 || Nc < 1 || Nc > 160) {
+        set_error("dsc_tc_gemm_noalloc: unsupported shape M %d Nc %d Kd %d (M, Kd >= 1, 1 <= Nc <= 160)",
                   M, Nc, Kd);
         return kErrArg;
     }

@@ -151,6 +151,18 @@ int Session::create(int nen_, unsigned N_, unsigned E_, const double *nodes, con
             iface_of_row[i] = (int)k;
         }
     eps_medium = mat[1] * kEps0;
+    {
+        // per-row data of the systems: interface of the row, boundary value
+        std::vector<double> re(N), im(N);
+        for (int i = 0; i < N; i++) {
+            re[i] = mbc[3 * (size_t)i];
+            im[i] = mbc[3 * (size_t)(i + N)];
+        }
+        DSC_TRY(rows.upload(iface_of_row, st));
+        DSC_TRY(bre.upload(re, st));
+        DSC_TRY(bim.upload(im, st));
+        DSC_CUDA(cudaStreamSynchronize(st));
+    }
     DSC_TRY(dev.upload(plan, st));
     DSC_TRY(force.build(plan, bctype.data(), st));
     ld = ((size_t)N + 31) / 32 * 32;

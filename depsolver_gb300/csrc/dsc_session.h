@@ -19,6 +19,8 @@ struct Session {
     std::vector<unsigned> bctype, ifaces;
     std::vector<double> mbc, mat;
     std::vector<int> iface_of_row;
+    DevBuf<int> rows;          // iface_of_row on the device (-1: conductor row)
+    DevBuf<double> bre, bim;   // boundary value of each row, Re and Im
     double eps_medium = 0.0;
     size_t ld = 0;
 

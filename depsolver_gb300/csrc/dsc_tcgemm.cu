@@ -5,14 +5,17 @@
 //   with the three products Ah Bh + Ah Bl + Al Bh: about FP32 accuracy.
 //
 // A and B are K-major FP32 (row m of A and row n of B hold consecutive k).
-// One CTA computes a 128-row tile of one split: warp 0 lane 0 streams
-// 128-byte-wide k-blocks of Ah, Al, Bh, Bl into a 3-stage shared-memory ring
-// with TMA (128B swizzle), warp 1 lane 0 issues tcgen05.mma (kind::tf32,
-// M = 128, N = BN, K = 8) into an FP32 accumulator in tensor memory and
-// releases each stage with tcgen05.commit, and all four warps read the
-// accumulator back (tcgen05.ld, one TMEM lane per row) and store the
-// partial tile.  Every wait on an mbarrier gives up after ~2 s of clock,
-// sets *err and lets the CTA drain and free its tensor memory.
+// Persistent kernel: one CTA per SM walks the units (128-row tile, split of
+// k) u = blockIdx.x, + gridDim.x, ...  Warp 0 lane 0 streams 128-byte-wide
+// k-blocks of A and Bh, Bl into a 3-stage shared-memory ring with TMA (128B
+// swizzle) without pausing between units; warps 2-3 split A in shared
+// memory; warp 1 lane 0 issues tcgen05.mma (kind::tf32, M = 128, K = 8)
+// into one of two FP32 accumulator buffers in tensor memory and releases
+// each stage with tcgen05.commit; warps 4-7 read the finished buffer back
+// (tcgen05.ld, one TMEM lane per row) and store the partial tile while the
+// next unit accumulates in the other buffer.  Every wait on an mbarrier
+// gives up after ~2 s of clock, sets *err and lets the CTA drain and free
+// its tensor memory.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -24,6 +27,9 @@ namespace dsc {
 constexpr int kTcBM = 128;
 constexpr int kTcBK = 32;          // fp32 elements per k-block = one 128-byte swizzle row
 constexpr int kTcStages = 3;
+// 3 stages of 2 x 16 KB (A) + 2 x BN x 128 B (B) fit the 227 KB of shared
+// memory a CTA may use for BN <= 160
+constexpr int kTcMaxNc = 160;
 constexpr long long kTcSpin = 4000000000LL;  // clock cycles before a wait gives up
 
 __device__ __forceinline__ uint32_t su32(const void *p)
@@ -205,18 +211,21 @@ __device__ __forceinline__ float tf32_lo_biased(float s)
 // dropped lo*lo product is at 2^-22 instead of 2^-21.
 // COMB (BN a multiple of 32, at most 128): Ah*Bh and Ah*Bl are one MMA of
 // N = 2 BN against the adjacent Bh and Bl tiles, into accumulator columns
-// [0, BN) and [BN, 2 BN); Al*Bh goes to [2 BN, 3 BN); the epilogue adds the
-// three.  This reads Ah once instead of twice, and keeps the small products
-// out of the main accumulator: the tensor core's FP32 accumulation
+// [0, BN) and [BN, 2 BN); Al*Bh adds into [BN, 2 BN) too; the epilogue adds
+// the two.  This reads Ah once instead of twice, and keeps the small
+// products out of the main accumulator: the tensor core's FP32 accumulation
 // truncates (sums of positive products come out low), so every MMA added
 // into an accumulator costs up to one of its units in the last place.
 template <int AMODE>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(256, 1)
     k_tc_gemm_3xtf32(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
                      const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl,
-                     int M, int Nc, int BN, int nkb_total, int kb_per_split, float *__restrict__ Y,
-                     size_t ldy, size_t split_stride, int tmem_cols, int *err)
+                     int M, int Nc, int BN, int nkb_total, int kb_per_split, int nsplit,
+                     float *__restrict__ Y, size_t ldy, size_t split_stride, int tmem_cols,
+                     uint32_t acc_stride, int *err)
 {
+    // acc_stride: TMEM columns of one accumulator buffer, a power of two of
+    // at least the columns it holds (so each buffer's MMAs start aligned)
     constexpr bool SPLIT_A = AMODE != 0;
     const bool comb = BN <= 128 && BN % 32 == 0;
     extern __shared__ uint8_t smem_raw[];
@@ -226,12 +235,13 @@ __global__ void __launch_bounds__(128, 1)
     uint64_t *full = (uint64_t *)(smem + kTcStages * stage_bytes);
     uint64_t *empty = full + kTcStages;
     uint64_t *splitb = empty + kTcStages;
-    uint64_t *accum = splitb + kTcStages;
-    uint32_t *tmem_slot = (uint32_t *)(accum + 1);
+    uint64_t *acc_full = splitb + kTcStages;  // [2]
+    uint64_t *acc_empty = acc_full + 2;       // [2]
+    uint64_t *done = acc_empty + 2;
+    uint32_t *tmem_slot = (uint32_t *)(done + 1);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m0 = blockIdx.x * kTcBM, split = blockIdx.y;
-    const int kb0 = split * kb_per_split;
-    const int nkb = max(0, min(nkb_total, kb0 + kb_per_split) - kb0);
+    const int tiles = (M + kTcBM - 1) / kTcBM;
+    const int units = tiles * nsplit;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < kTcStages; s++) {
@@ -239,7 +249,11 @@ __global__ void __launch_bounds__(128, 1)
             mbar_init(&empty[s], 1);
             mbar_init(&splitb[s], 64);  // the 64 threads of warps 2 and 3
         }
-        mbar_init(accum, 1);
+        for (int b = 0; b < 2; b++) {
+            mbar_init(&acc_full[b], 1);
+            mbar_init(&acc_empty[b], 4);  // one lane of each epilogue warp
+        }
+        mbar_init(done, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -253,128 +267,183 @@ __global__ void __launch_bounds__(128, 1)
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
-    if (warp == 0 && lane == 0 && nkb > 0) {
-        // ---- producer
-        int issued = 0;
-        for (int i = 0; i < nkb; i++) {
-            const int s = i % kTcStages;
-            if (i >= kTcStages && !mbar_wait(&empty[s], ((i / kTcStages) - 1) & 1, err, 1)) break;
-            uint8_t *st = smem + s * stage_bytes;
-            mbar_expect_tx(&full[s], SPLIT_A ? stage_bytes - a_bytes : stage_bytes);
-            const int kx = (kb0 + i) * kTcBK;
-            tma_load_2d(st, &tmAh, &full[s], kx, m0);
-            if (!SPLIT_A) tma_load_2d(st + a_bytes, &tmAl, &full[s], kx, m0);
-            tma_load_2d(st + 2 * a_bytes, &tmBh, &full[s], kx, 0);
-            tma_load_2d(st + 2 * a_bytes + b_bytes, &tmBl, &full[s], kx, 0);
-            issued = i + 1;
-        }
-        // drain: the last loads of every stage have landed before the CTA
-        // may exit (immediate in the normal path, bounded otherwise)
-        for (int i = max(0, issued - kTcStages); i < issued; i++) {
-            const long long t0 = clock64();
-            while (!mbar_try(&full[i % kTcStages], (i / kTcStages) & 1) && clock64() - t0 < kTcSpin) {
-            }
-        }
-    } else if (warp == 1 && lane == 0 && nkb > 0) {
-        // ---- MMA issuer
-        const uint32_t idesc = idesc_tf32(BN, kTcBM), idesc2 = idesc_tf32(2 * BN, kTcBM);
-        for (int i = 0; i < nkb; i++) {
-            const int s = i % kTcStages;
-            if (!mbar_wait(&full[s], (i / kTcStages) & 1, err, 2)) break;
-            tc_fence_after();
-            uint8_t *st = smem + s * stage_bytes;
-            const uint64_t dah = sw128_desc(st), dal = sw128_desc(st + a_bytes);
-            const uint64_t dbh = sw128_desc(st + 2 * a_bytes), dbl = sw128_desc(st + 2 * a_bytes + b_bytes);
-            // products with Ah: the stage as it landed
-#pragma unroll
-            for (int kk = 0; kk < kTcBK / 8; kk++) {
-                const uint64_t off = (uint64_t)(kk * 32) >> 4;  // 8 tf32 = 32 bytes
-                if (comb) {
-                    mma_tf32(tmem, dah + off, dbh + off, idesc2, (i | kk) != 0);
-                } else {
-                    mma_tf32(tmem, dah + off, dbh + off, idesc, (i | kk) != 0);
-                    mma_tf32(tmem, dah + off, dbl + off, idesc, 1);
+    // Every role walks the same sequence: units u = blockIdx.x, + gridDim.x,
+    // ... (unit = row tile + tiles * split), and within a unit its k-blocks;
+    // g counts k-blocks over all units (stage g % kTcStages, use g / kTcStages).
+    if (warp == 0) {
+        if (lane == 0) {
+            // ---- producer
+            uint32_t g = 0;
+            bool ok = true;
+            for (int u = blockIdx.x; ok && u < units; u += gridDim.x) {
+                const int m0 = (u % tiles) * kTcBM, kb0 = (u / tiles) * kb_per_split;
+                const int nkb = min(nkb_total, kb0 + kb_per_split) - kb0;
+                for (int i = 0; i < nkb; i++, g++) {
+                    const uint32_t s = g % kTcStages, n = g / kTcStages;
+                    if (n > 0 && !mbar_wait(&empty[s], (n - 1) & 1, err, 1)) {
+                        ok = false;
+                        break;
+                    }
+                    uint8_t *st = smem + s * stage_bytes;
+                    mbar_expect_tx(&full[s], SPLIT_A ? stage_bytes - a_bytes : stage_bytes);
+                    const int kx = (kb0 + i) * kTcBK;
+                    tma_load_2d(st, &tmAh, &full[s], kx, m0);
+                    if (!SPLIT_A) tma_load_2d(st + a_bytes, &tmAl, &full[s], kx, m0);
+                    tma_load_2d(st + 2 * a_bytes, &tmBh, &full[s], kx, 0);
+                    tma_load_2d(st + 2 * a_bytes + b_bytes, &tmBl, &full[s], kx, 0);
                 }
             }
-            // products with Al: after the split
-            if (SPLIT_A) {
-                if (!mbar_wait(&splitb[s], (i / kTcStages) & 1, err, 2)) break;
+            // drain: the last loads of every stage have landed before the CTA
+            // may exit (immediate in the normal path, bounded otherwise)
+            for (uint32_t h = g > (uint32_t)kTcStages ? g - kTcStages : 0; h < g; h++) {
+                const long long t0 = clock64();
+                while (!mbar_try(&full[h % kTcStages], (h / kTcStages) & 1) && clock64() - t0 < kTcSpin) {
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            // ---- MMA issuer
+            const uint32_t idesc = idesc_tf32(BN, kTcBM), idesc2 = idesc_tf32(2 * BN, kTcBM);
+            uint32_t g = 0;
+            bool ok = true;
+            int j = 0;
+            for (int u = blockIdx.x; ok && u < units; u += gridDim.x, j++) {
+                const int kb0 = (u / tiles) * kb_per_split;
+                const int nkb = min(nkb_total, kb0 + kb_per_split) - kb0;
+                const uint32_t buf = j & 1, q = j >> 1;
+                if (q > 0 && !mbar_wait(&acc_empty[buf], (q - 1) & 1, err, 5)) break;
                 tc_fence_after();
-            }
+                const uint32_t acc = tmem + buf * acc_stride;
+                for (int i = 0; i < nkb; i++, g++) {
+                    const uint32_t s = g % kTcStages, n = g / kTcStages;
+                    if (!mbar_wait(&full[s], n & 1, err, 2)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    uint8_t *st = smem + s * stage_bytes;
+                    const uint64_t dah = sw128_desc(st), dal = sw128_desc(st + a_bytes);
+                    const uint64_t dbh = sw128_desc(st + 2 * a_bytes);
+                    const uint64_t dbl = sw128_desc(st + 2 * a_bytes + b_bytes);
+                    // products with Ah: the stage as it landed
 #pragma unroll
-            for (int kk = 0; kk < kTcBK / 8; kk++) {
-                const uint64_t off = (uint64_t)(kk * 32) >> 4;
-                if (comb) mma_tf32(tmem + 2 * BN, dal + off, dbh + off, idesc, (i | kk) != 0);
-                else mma_tf32(tmem, dal + off, dbh + off, idesc, 1);
-            }
-            mma_commit(&empty[s]);
-        }
-        mma_commit(accum);
-    } else if (SPLIT_A && warp >= 2 && nkb > 0) {
-        // ---- splitters: lo = rna_tf32(a - trunc_tf32(a)) of the FP32 A tile
-        const int tid = threadIdx.x - 64;
-        for (int i = 0; i < nkb; i++) {
-            const int s = i % kTcStages;
-            if (!mbar_wait(&full[s], (i / kTcStages) & 1, err, 4)) break;
-            const float4 *hi = (const float4 *)(smem + s * stage_bytes);
-            float4 *lo = (float4 *)(smem + s * stage_bytes + a_bytes);
-            for (int t = tid; t < (int)(a_bytes / 16); t += 64) {
-                const float4 v = hi[t];
-                float4 l;
-                if (AMODE == 2) {
-                    l.x = tf32_lo_biased(v.x);
-                    l.y = tf32_lo_biased(v.y);
-                    l.z = tf32_lo_biased(v.z);
-                    l.w = tf32_lo_biased(v.w);
-                } else {
-                    l.x = tf32_lo(v.x);
-                    l.y = tf32_lo(v.y);
-                    l.z = tf32_lo(v.z);
-                    l.w = tf32_lo(v.w);
+                    for (int kk = 0; kk < kTcBK / 8; kk++) {
+                        const uint64_t off = (uint64_t)(kk * 32) >> 4;  // 8 tf32 = 32 bytes
+                        if (comb) {
+                            mma_tf32(acc, dah + off, dbh + off, idesc2, (i | kk) != 0);
+                        } else {
+                            mma_tf32(acc, dah + off, dbh + off, idesc, (i | kk) != 0);
+                            mma_tf32(acc, dah + off, dbl + off, idesc, 1);
+                        }
+                    }
+                    // products with Al: after the split
+                    if (SPLIT_A) {
+                        if (!mbar_wait(&splitb[s], n & 1, err, 2)) {
+                            ok = false;
+                            break;
+                        }
+                        tc_fence_after();
+                    }
+#pragma unroll
+                    for (int kk = 0; kk < kTcBK / 8; kk++) {
+                        const uint64_t off = (uint64_t)(kk * 32) >> 4;
+                        mma_tf32(comb ? acc + BN : acc, dal + off, dbh + off, idesc, 1);
+                    }
+                    mma_commit(&empty[s]);
                 }
-                lo[t] = l;
+                if (ok) mma_commit(&acc_full[buf]);
             }
-            // generic-proxy writes must be visible to the tensor core's reads
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            mbar_arrive(&splitb[s]);
+            mma_commit(done);  // arrives when every MMA issued above has completed
+        }
+    } else if (warp < 4) {
+        if (SPLIT_A) {
+            // ---- splitters (warps 2 and 3): the lo slot of each stage
+            const int tid = threadIdx.x - 64;
+            uint32_t g = 0;
+            bool ok = true;
+            for (int u = blockIdx.x; ok && u < units; u += gridDim.x) {
+                const int kb0 = (u / tiles) * kb_per_split;
+                const int nkb = min(nkb_total, kb0 + kb_per_split) - kb0;
+                for (int i = 0; i < nkb; i++, g++) {
+                    const uint32_t s = g % kTcStages, n = g / kTcStages;
+                    if (!mbar_wait(&full[s], n & 1, err, 4)) {
+                        ok = false;
+                        break;
+                    }
+                    const float4 *hi = (const float4 *)(smem + s * stage_bytes);
+                    float4 *lo = (float4 *)(smem + s * stage_bytes + a_bytes);
+                    for (int t = tid; t < (int)(a_bytes / 16); t += 64) {
+                        const float4 v = hi[t];
+                        float4 l;
+                        if (AMODE == 2) {
+                            l.x = tf32_lo_biased(v.x);
+                            l.y = tf32_lo_biased(v.y);
+                            l.z = tf32_lo_biased(v.z);
+                            l.w = tf32_lo_biased(v.w);
+                        } else {
+                            l.x = tf32_lo(v.x);
+                            l.y = tf32_lo(v.y);
+                            l.z = tf32_lo(v.z);
+                            l.w = tf32_lo(v.w);
+                        }
+                        lo[t] = l;
+                    }
+                    // generic-proxy writes must be visible to the tensor core's reads
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    mbar_arrive(&splitb[s]);
+                }
+            }
+        }
+    } else {
+        // ---- epilogue (warps 4..7: TMEM lanes 32 (warp % 4) .. + 31 = rows)
+        const int ew = warp & 3;
+        int j = 0;
+        for (int u = blockIdx.x; u < units; u += gridDim.x, j++) {
+            const int m0 = (u % tiles) * kTcBM, split = u / tiles;
+            const uint32_t buf = j & 1, q = j >> 1;
+            bool have = mbar_wait(&acc_full[buf], q & 1, err, 3);
+            // tcgen05.ld is warp-collective: the whole warp reads or none of it
+            if (!__all_sync(0xffffffffu, have)) break;
+            tc_fence_after();
+            const uint32_t acc = tmem + ((uint32_t)(ew * 32) << 16) + buf * acc_stride;
+            const int m = m0 + ew * 32 + lane;
+            float *Ys = Y + (size_t)split * split_stride;
+            for (int c0 = 0; c0 < BN; c0 += 32) {
+                uint32_t r[32];
+                tmem_ld32(acc + (uint32_t)c0, r);
+                if (comb) {
+                    uint32_t r2[32];
+                    tmem_ld32(acc + (uint32_t)(BN + c0), r2);
+#pragma unroll
+                    for (int t = 0; t < 32; t++) r[t] = __float_as_uint(__uint_as_float(r[t]) + __uint_as_float(r2[t]));
+                }
+                if (m < M) {
+#pragma unroll
+                    for (int t = 0; t < 32; t++) {
+                        const int n = c0 + t;
+                        if (n < Nc) Ys[(size_t)n * ldy + m] = __uint_as_float(r[t]);
+                    }
+                }
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acc_empty[buf]);
         }
     }
     __syncwarp();
-
-    // ---- epilogue: TMEM lanes 32w .. 32w + 31 = rows of this warp
-    bool have = nkb > 0;
-    if (have) have = mbar_wait(accum, 0, err, 3);
-    // tcgen05.ld is warp-collective: the whole warp reads or none of it
-    have = __all_sync(0xffffffffu, have);
-    tc_fence_after();
-    const int m = m0 + warp * 32 + lane;
-    float *Ys = Y + (size_t)split * split_stride;
-    for (int c0 = 0; c0 < BN; c0 += 32) {
-        uint32_t r[32];
-        if (have) {
-            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, r);
-            if (comb) {
-                uint32_t r2[32], r3[32];
-                tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(BN + c0), r2);
-                tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(2 * BN + c0), r3);
-#pragma unroll
-                for (int j = 0; j < 32; j++)
-                    r[j] = __float_as_uint(__uint_as_float(r[j]) + (__uint_as_float(r2[j]) + __uint_as_float(r3[j])));
-            }
-        } else {
-#pragma unroll
-            for (int j = 0; j < 32; j++) r[j] = 0u;
-        }
-        if (m < M) {
-#pragma unroll
-            for (int j = 0; j < 32; j++) {
-                const int n = c0 + j;
-                if (n < Nc) Ys[(size_t)n * ldy + m] = __uint_as_float(r[j]);
+    if (warp == 0) {
+        // every MMA has completed before the accumulator memory is freed
+        if (lane == 0) {
+            const long long t0 = clock64();
+            while (!mbar_try(done, 0) && clock64() - t0 < kTcSpin) {
             }
         }
+        __syncwarp();
     }
     tc_fence_before();
     __syncthreads();
+    tc_fence_after();
     if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tmem_cols)
                      : "memory");
@@ -427,14 +496,16 @@ int tc_gemm_3xtf32(const float *Ah, const float *Al, size_t lda, const float *Bh
                    size_t ldb, int M, int Nc, int Kd, float *Y, size_t ldy, int splits, int *d_err,
                    cudaStream_t st, bool a_biased)
 {
-    if (Nc < 1 || Nc > 256 || M < 1 || Kd < 1 || ldy < (size_t)M) {
-        set_error("tc_gemm_3xtf32: unsupported shape M %d Nc %d Kd %d", M, Nc, Kd);
+    if (Nc < 1 || Nc > kTcMaxNc || M < 1 || Kd < 1 || ldy < (size_t)M) {
+        set_error("tc_gemm_3xtf32: unsupported shape M %d Nc %d Kd %d (Nc <= %d)", M, Nc, Kd, kTcMaxNc);
         return kErrArg;
     }
     const int BN = (Nc + 15) / 16 * 16;
-    const int acc_cols = (BN <= 128 && BN % 32 == 0) ? 3 * BN : BN;  // see COMB in the kernel
-    int tmem_cols = 32;
-    while (tmem_cols < acc_cols) tmem_cols *= 2;
+    // two accumulator buffers of 2 BN (COMB) or BN columns, each rounded up
+    // to a power of two
+    uint32_t acc_stride = 32;
+    while (acc_stride < (uint32_t)((BN <= 128 && BN % 32 == 0) ? 2 * BN : BN)) acc_stride *= 2;
+    const int tmem_cols = 2 * (int)acc_stride;
     const bool split_a = Al == nullptr;  // plain FP32 A, split in shared memory
     CUtensorMap ah, al, bh, bl;
     DSC_TRY(make_map(&ah, Ah, M, Kd, lda, kTcBM));
@@ -447,11 +518,19 @@ int tc_gemm_3xtf32(const float *Ah, const float *Al, size_t lda, const float *Bh
     const int kps = (nkb + splits - 1) / splits;
     splits = (nkb + kps - 1) / kps;  // every split has at least one k-block
     const size_t smem = 1024 + (size_t)kTcStages * (2 * kTcBM * 128 + 2 * BN * 128) + 256;
-    dim3 grid((M + kTcBM - 1) / kTcBM, splits);
+    // persistent: one CTA per SM walks the (row tile, split) units
+    static int nsm = 0;
+    if (!nsm) {
+        int dev = 0;
+        DSC_CUDA(cudaGetDevice(&dev));
+        DSC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    }
+    const int units = (M + kTcBM - 1) / kTcBM * splits;
+    const dim3 grid(std::min(units, nsm));
     auto launch = [&](auto kern) -> int {
         DSC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        DSC_LAUNCH(kern<<<grid, 128, smem, st>>>(ah, al, bh, bl, M, Nc, BN, nkb, kps, Y, ldy,
-                                                 ldy * (size_t)Nc, tmem_cols, d_err));
+        DSC_LAUNCH(kern<<<grid, 256, smem, st>>>(ah, al, bh, bl, M, Nc, BN, nkb, kps, splits, Y, ldy,
+                                                 ldy * (size_t)Nc, tmem_cols, acc_stride, d_err));
         return kOk;
     };
     if (!split_a) DSC_TRY(launch(k_tc_gemm_3xtf32<0>));
@@ -630,8 +709,8 @@ extern "C" int dsc_tc_gemm(int M, int Nc, int Kd, const double *A, const double 
         set_error("no CUDA device available");
         return kErrCuda;
     }
-    if (M < 1 || Kd < 1 || Nc < 1 || Nc > 256) {
-        set_error("dsc_tc_gemm: unsupported shape");
+    if (M < 1 || Kd < 1 || Nc < 1 || Nc > kTcMaxNc) {
+        set_error("dsc_tc_gemm: unsupported shape (1 <= Nc <= %d)", kTcMaxNc);
         return kErrArg;
     }
     cudaStream_t st = 0;

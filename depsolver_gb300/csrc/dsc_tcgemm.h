@@ -10,7 +10,7 @@ namespace dsc {
 // per split) = partial sums over split s's share of k of
 //   (Ah + Al)[m][k] * (Bh + Bl)[n][k]  with the three products hh + hl + lh.
 // A: M x Kd, B: Nc x Kd, both K-major FP32 holding tf32 pairs, row strides
-// lda / ldb (multiples of 4 elements, 16-byte aligned bases).  Nc <= 256.
+// lda / ldb (multiples of 4 elements, 16-byte aligned bases).  Nc <= 160.
 // *d_err (device, zero on entry) is set when a wait inside the kernel gives
 // up.  The caller adds the splits.  Al = null: A is plain FP32 (split in
 // shared memory), or with a_biased in the encoding split_transpose_K(...,

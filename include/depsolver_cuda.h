@@ -206,7 +206,7 @@ int dsc_session_timing(dsc_session *s, double *ms, int *count, double *work, int
  * Y (M x Nc) = A (M x Kd) * B^T (B is Nc x Kd), all row-major; each operand
  * is split into a TF32 pair and three products hi*hi + hi*lo + lo*hi are
  * accumulated in FP32 per split of k and in FP64 across splits (about FP32
- * accuracy).  Nc <= 256; splits <= 0 picks the split count.  a_in_smem = 0
+ * accuracy).  Nc <= 160; splits <= 0 picks the split count.  a_in_smem = 0
  * stores A as the tf32 pair; 1 stores A as plain FP32 and splits it inside
  * the kernel (half the reads of A); 2 does the same on A stored in a biased
  * encoding whose truncation to tf32 is the rounded hi (the mixed sweep's

@@ -92,7 +92,7 @@ def test_noalloc_rejects_host_pointers(gpu):
 def test_noalloc_rejects_oversize_before_device_work(native):
     """Shapes whose scratch exceeds the static array fail with DSC_ERR_ARG
     and a message giving both sizes, with or without a GPU."""
-    M, Nc, Kd = 40000, 256, 4       # one partial tile alone: 40000 * 256 * 4 B > 32 MiB
+    M, Nc, Kd = 60000, 160, 4       # one partial tile alone: 60000 * 160 * 4 B > 32 MiB
     A = np.zeros((M, Kd), dtype=np.float32)
     B = np.zeros((Nc, Kd))
     Y = np.zeros((M, Nc))
