@@ -59,7 +59,9 @@ def lib() -> C.CDLL:
         L.dsc_session_destroy.restype = None
         L.dsc_session_destroy.argtypes = [C.c_void_p]
         L.dsc_session_assemble.restype = C.c_int
-        L.dsc_session_assemble.argtypes = [C.c_void_p]
+        L.dsc_session_assemble.argtypes = [C.c_void_p, C.c_int]
+        L.dsc_session_geometric_matrix.restype = C.c_int
+        L.dsc_session_geometric_matrix.argtypes = [C.c_void_p, C.c_int, _dp, C.c_size_t]
         L.dsc_session_solve.restype = C.c_int
         L.dsc_session_solve.argtypes = [C.c_void_p, C.c_int, C.c_uint, _dp, C.c_double, C.c_uint,
                                         C.c_void_p, C.c_void_p, C.c_void_p]

@@ -138,8 +138,18 @@ class Session:
         except Exception:
             pass
 
-    def assemble(self):
-        _native.check(self._L.dsc_session_assemble(self._h))
+    def assemble(self, mode: int = MODE_FP64):
+        """Assemble K now: MODE_FP64 in FP64, MODE_MIXED with the regular
+        pairs in double-FP32 (and the tensor cores' FP32 copy)."""
+        _native.check(self._L.dsc_session_assemble(self._h, mode))
+
+    def geometric_matrix(self, mode: int = MODE_FP64) -> np.ndarray:
+        """K (N x N, row i = collocation node, column c = node) as assembled
+        for `mode`."""
+        N = self.scene.N
+        Kt = np.empty((N, N))
+        _native.check(self._L.dsc_session_geometric_matrix(self._h, mode, Kt, N))
+        return Kt.T
 
     def stream_handle(self) -> int:
         """cudaStream_t of the session (for torch.cuda.ExternalStream)."""

@@ -16,6 +16,7 @@
 // Singular pairs -- k_asm_singular: one warp per row, the row's elements in
 // element order, quadrature points split over the lanes (dsc_singular.cuh).
 #include "dsc_common.cuh"
+#include "dsc_df32.cuh"
 #include "dsc_internal.h"
 #include "dsc_singular.cuh"
 
@@ -57,6 +58,34 @@ constexpr Shape7 make_shape(int nen)
 
 __constant__ Shape7 c_shape3 = make_shape(3);
 __constant__ Shape7 c_shape6 = make_shape(6);
+
+// The same values as double-FP32 pairs (hi = value rounded to FP32, lo = the
+// rest).
+struct Shape7df {
+    float hi[kTriPts][6], lo[kTriPts][6];
+};
+
+constexpr Shape7df make_shape_df(int nen)
+{
+    Shape7df d{};
+    const Shape7 s = make_shape(nen);
+    for (int q = 0; q < kTriPts; q++)
+        for (int k = 0; k < 6; k++) {
+            d.hi[q][k] = (float)s.v[q][k];
+            d.lo[q][k] = (float)(s.v[q][k] - (double)d.hi[q][k]);
+        }
+    return d;
+}
+
+__constant__ Shape7df c_shape3_df = make_shape_df(3);
+__constant__ Shape7df c_shape6_df = make_shape_df(6);
+
+template <int NEN>
+__device__ __forceinline__ float2 shape_q_df(int q, int k)
+{
+    return NEN == 3 ? make_float2(c_shape3_df.hi[q][k], c_shape3_df.lo[q][k])
+                    : make_float2(c_shape6_df.hi[q][k], c_shape6_df.lo[q][k]);
+}
 
 template <int NEN>
 __device__ __forceinline__ double shape_q(int q, int k)
@@ -189,6 +218,110 @@ __global__ void __launch_bounds__(128) k_asm_regular_f64(AsmArgs a, double *__re
     }
 }
 
+// ---- the same regular pairs in double-FP32 on the FP32 pipes
+// (about 2^-46 per operation instead of FP64's 2^-53; GB300 issues FP64 at
+// 1/64 of the FP32 rate, and k_asm_regular_f64 runs at that FP64 roof).
+
+// Quadrature points of every element as double-FP32: x, y, z, w_q J_q.
+__global__ void k_qp_to_df(const double *__restrict__ qp, size_t n, float2 *__restrict__ out)
+{
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n;
+         t += (size_t)gridDim.x * blockDim.x)
+        out[t] = df_from(qp[t]);
+}
+
+template <int NEN, int MODE>
+__device__ __forceinline__ void pair_regular_df(const float2 *__restrict__ q7, float2 xi, float2 yi,
+                                                float2 zi, float2 nx, float2 ny, float2 nz, bool isH,
+                                                float2 *acc)
+{
+#pragma unroll
+    for (int q = 0; q < kTriPts; q++) {
+        const float2 *Q = q7 + q * 4;
+        const float2 dx = df_sub(xi, Q[0]), dy = df_sub(yi, Q[1]), dz = df_sub(zi, Q[2]);
+        const float2 r2 = df_add(df_add(df_sqr(dx), df_sqr(dy)), df_sqr(dz));
+        const float2 inv = df_rsqrt(r2);
+        float2 w;
+        if (MODE == 0) {
+            w = df_mul(Q[3], inv);
+        } else {
+            const float2 dot = df_add(df_add(df_mul(dx, nx), df_mul(dy, ny)), df_mul(dz, nz));
+            const float2 h = df_mul(df_mul(Q[3], df_mul(df_sqr(inv), inv)), dot);
+            w = (MODE == 1 || isH) ? h : df_mul(Q[3], inv);
+        }
+#pragma unroll
+        for (int k = 0; k < NEN; k++) df_mac(acc[k], w, shape_q_df<NEN>(q, k));
+    }
+}
+
+// As k_asm_regular_f64 (same tiles, footprints and partial slots), with the
+// pair integrals in double-FP32; K and the partial slots stay FP64.
+template <int NEN>
+__global__ void __launch_bounds__(128) k_asm_regular_df32(AsmArgs a, const float2 *__restrict__ qpd,
+                                                          double *__restrict__ K, double *__restrict__ P)
+{
+    constexpr int R = kRowTile, EG = kGroup;
+    extern __shared__ double smem[];
+    float2 *s_qp = (float2 *)smem;                          // EG * 28
+    float2 *s_V = s_qp + EG * kTriPts * 4;                  // EG * NEN * R
+    int *s_nodes = (int *)(s_V + EG * NEN * R);             // EG * NEN
+    const int g = blockIdx.y;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+
+    for (int t = threadIdx.x; t < EG * kTriPts * 4; t += blockDim.x) {
+        const int e = a.grp_elem[g * EG + t / (kTriPts * 4)];
+        s_qp[t] = e >= 0 ? qpd[(size_t)e * kTriPts * 4 + t % (kTriPts * 4)] : make_float2(0.f, 0.f);
+    }
+    for (int t = threadIdx.x; t < EG * NEN; t += blockDim.x) {
+        const int e = a.grp_elem[g * EG + t / NEN];
+        s_nodes[t] = e >= 0 ? a.elems[(size_t)e * NEN + t % NEN] : -1;
+    }
+    __syncthreads();
+
+    const int i = a.row_lo + blockIdx.x * R + lane;
+    const bool valid = i < a.row_hi;
+    const int ii = valid ? i : a.row_lo;
+    const float2 xi = df_from(a.X[ii]), yi = df_from(a.Y[ii]), zi = df_from(a.Z[ii]);
+    const float2 nx = df_from(a.normals[3 * (size_t)ii]), ny = df_from(a.normals[3 * (size_t)ii + 1]),
+                 nz = df_from(a.normals[3 * (size_t)ii + 2]);
+    const int kind = valid ? a.row_kind[ii] : 0;
+    const float2 fac = df_from(a.row_fac[ii]);
+    const bool allG = __all_sync(0xffffffffu, kind == 0);
+    const bool allH = __all_sync(0xffffffffu, kind == 1);
+
+    for (int el = w; el < EG; el += 4) {
+        float2 acc[NEN];
+#pragma unroll
+        for (int k = 0; k < NEN; k++) acc[k] = make_float2(0.f, 0.f);
+        const int *en = s_nodes + el * NEN;
+        bool drop = en[0] < 0;
+#pragma unroll
+        for (int k = 0; k < NEN; k++) drop |= en[k] == i;
+        if (en[0] >= 0) {
+            const float2 *q7 = s_qp + el * kTriPts * 4;
+            if (allG) pair_regular_df<NEN, 0>(q7, xi, yi, zi, nx, ny, nz, false, acc);
+            else if (allH) pair_regular_df<NEN, 1>(q7, xi, yi, zi, nx, ny, nz, true, acc);
+            else pair_regular_df<NEN, 2>(q7, xi, yi, zi, nx, ny, nz, kind == 1, acc);
+        }
+#pragma unroll
+        for (int k = 0; k < NEN; k++)
+            s_V[(el * NEN + k) * R + lane] = drop ? make_float2(0.f, 0.f) : df_mul(fac, df_norm(acc[k]));
+    }
+    __syncthreads();
+
+    const int f0 = a.fp_ptr[g], f1 = a.fp_ptr[g + 1];
+    for (int j = f0 + w; j < f1; j += 4) {
+        const int s0 = a.fp_sl_ptr[j], s1 = a.fp_sl_ptr[j + 1];
+        float2 sum = make_float2(0.f, 0.f);
+        for (int m = s0; m < s1; m++) sum = df_add(sum, s_V[a.fp_sl[m] * R + lane]);
+        const int dest = a.fp_dest[j];
+        if (valid) {
+            if (dest >= 0) K[(size_t)dest * a.ld + i] = df_to(sum);
+            else P[(size_t)(-dest - 1) * a.ldp + (i - a.row_lo)] = df_to(sum);
+        }
+    }
+}
+
 // K column of every node shared by several groups = sum of its slots in
 // group order; nodes in no element get a zero column.
 template <typename T>
@@ -260,11 +393,17 @@ static size_t regular_smem(int nen)
 }
 
 template <int NEN>
-static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStream_t st, Timer *tm)
+static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStream_t st, Timer *tm,
+                              bool df32)
 {
     DSC_LAUNCH(k_elem_qp<NEN><<<(m.E * kTriPts + 255) / 256, 256, 0, st>>>(m.x.p, m.y.p, m.z.p, m.elems.p, m.E,
                                                                   m.qp.p));
     DSC_CUDA(cudaGetLastError());
+    DevBuf<float2> qpd;
+    if (df32) {
+        DSC_TRY(qpd.alloc((size_t)m.E * kTriPts * 4));
+        DSC_LAUNCH(k_qp_to_df<<<4 * 152, 256, 0, st>>>(m.qp.p, (size_t)m.E * kTriPts * 4, qpd.p));
+    }
     // Partial-sum buffer: n_slots columns of a row chunk, at most ~1 GiB.
     const size_t budget = (size_t)1 << 30;
     int rc = m.N;
@@ -278,6 +417,8 @@ static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStr
     const size_t smem = regular_smem(NEN);
     DSC_CUDA(cudaFuncSetAttribute(k_asm_regular_f64<NEN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)smem));
+    DSC_CUDA(cudaFuncSetAttribute(k_asm_regular_df32<NEN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem));
     AsmArgs a{m.x.p, m.y.p, m.z.p, m.normals.p, m.row_fac.p, m.qp.p, m.row_kind.p, m.elems.p,
               m.grp_elem.p, m.fp_ptr.p, m.fp_dest.p, m.fp_sl_ptr.p, m.fp_sl.p, m.N, 0, 0, ld,
               (size_t)rc};
@@ -288,7 +429,8 @@ static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStr
         dim3 grid((hi - lo + kRowTile - 1) / kRowTile, m.G);
         {
             TimerScope ts(tm, kTAsmRegular, st);
-            DSC_LAUNCH(k_asm_regular_f64<NEN><<<grid, 128, smem, st>>>(a, K, P.p));
+            if (df32) DSC_LAUNCH(k_asm_regular_df32<NEN><<<grid, 128, smem, st>>>(a, qpd.p, K, P.p));
+            else DSC_LAUNCH(k_asm_regular_f64<NEN><<<grid, 128, smem, st>>>(a, K, P.p));
             if (tm) tm->add_work(kTAsmRegular, (double)(hi - lo) * m.E);  // (row, element) pairs
         }
         DSC_CUDA(cudaGetLastError());
@@ -311,9 +453,10 @@ static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStr
     return kOk;
 }
 
-int assemble_K_fp64(const DeviceMesh &m, double *K, size_t ld, cudaStream_t st, Timer *tm)
+int assemble_K_fp64(const DeviceMesh &m, double *K, size_t ld, cudaStream_t st, Timer *tm, bool df32)
 {
-    return m.nen == 6 ? assemble_fp64_impl<6>(m, K, ld, st, tm) : assemble_fp64_impl<3>(m, K, ld, st, tm);
+    return m.nen == 6 ? assemble_fp64_impl<6>(m, K, ld, st, tm, df32)
+                      : assemble_fp64_impl<3>(m, K, ld, st, tm, df32);
 }
 
 }  // namespace dsc

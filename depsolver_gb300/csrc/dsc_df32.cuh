@@ -68,6 +68,32 @@ __device__ __forceinline__ float2 df_add(float2 a, float2 b)
 
 __device__ __forceinline__ float2 df_neg(float2 a) { return make_float2(-a.x, -a.y); }
 
+__device__ __forceinline__ float2 df_sub(float2 a, float2 b) { return df_add(a, df_neg(b)); }
+
+// a * a, renormalised
+__device__ __forceinline__ float2 df_sqr(float2 a)
+{
+    const float p = __fmul_rn(a.x, a.x);
+    float e = __fmaf_rn(a.x, a.x, -p);
+    e = __fmaf_rn(2.0f * a.x, a.y, e);
+    return df_fast_two_sum(p, e);
+}
+
+// 1 / sqrt(a) for a > 0: an FP32 seed and two Newton steps
+// y <- y + y (1 - a y^2) / 2 with a y^2 in double-FP32 (each step squares
+// the relative error; the seed's ~2^-22 ends below 2^-46).
+__device__ __forceinline__ float2 df_rsqrt(float2 a)
+{
+    float2 y = make_float2(rsqrtf(a.x), 0.0f);
+#pragma unroll
+    for (int it = 0; it < 2; it++) {
+        const float2 t = df_mul(a, df_sqr(y));
+        const float u = __fsub_rn(__fsub_rn(1.0f, t.x), t.y);  // 1 - t.x is exact
+        y = df_add(y, df_mul(y, make_float2(0.5f * u, 0.0f)));
+    }
+    return y;
+}
+
 // FP64 <-> double-FP32 (these conversions run on the FP64 pipe: use them
 // per block or per system, not per element, in the streaming kernels)
 __device__ __forceinline__ float2 df_from(double v)

@@ -194,7 +194,10 @@ struct DeviceMesh {
 // geometric integral of row i against node c: C * int G N_c for conductor
 // rows, int H N_c (normal derivative, sign as the reference) for interface
 // rows.  The frequency enters only through per-row coefficients.
-int assemble_K_fp64(const DeviceMesh &m, double *K, size_t ld, cudaStream_t st, Timer *tm = nullptr);
-int assemble_K_fp32(const DeviceMesh &m, float *K, size_t ld, cudaStream_t st, Timer *tm = nullptr);
+// df32: the regular pairs in double-FP32 on the FP32 pipes (about 2^-46
+// per operation; the mixed-precision path), else in FP64 (the reference's
+// arithmetic).  Singular pairs are FP64 either way; K is FP64.
+int assemble_K_fp64(const DeviceMesh &m, double *K, size_t ld, cudaStream_t st, Timer *tm = nullptr,
+                    bool df32 = false);
 
 }  // namespace dsc

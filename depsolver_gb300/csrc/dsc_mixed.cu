@@ -103,8 +103,8 @@ __global__ void __launch_bounds__(256) k_gemm_cm(const TA *__restrict__ A, size_
 // unevaluated pair (s, c) kept exact by TwoSum, and the cross terms
 // hi*lo + lo*hi go into c.  A is FP64 and split while it is staged (its
 // conversions run on the FP64 pipe, once per element: a tile spans 128
-// columns); B comes pre-split (Bh, Bl).  64 x 128 tile, 4 x 8 outputs per
-// thread, k-steps of 16.
+// columns); B comes pre-split (Bh, Bl).  64 x 128 tile, 512 threads with
+// 4 x 4 outputs each, k-steps of 16.
 __device__ __forceinline__ void df32_acc(float &s, float &c, float ah, float al, float bh, float bl)
 {
     // the _rn intrinsics keep the compiler from fusing these operations,
@@ -118,7 +118,7 @@ __device__ __forceinline__ void df32_acc(float &s, float &c, float ah, float al,
     c += err + e + fmaf(ah, bl, al * bh);
 }
 
-__global__ void __launch_bounds__(256) k_gemm_df32(const double *__restrict__ A, size_t lda,
+__global__ void __launch_bounds__(512) k_gemm_df32(const double *__restrict__ A, size_t lda,
                                                    const float *__restrict__ Bh,
                                                    const float *__restrict__ Bl, size_t ldb,
                                                    double *__restrict__ C, size_t ldc, int M, int Nc,
@@ -127,14 +127,14 @@ __global__ void __launch_bounds__(256) k_gemm_df32(const double *__restrict__ A,
     __shared__ float Ah[16][64 + 1], Al[16][64 + 1];
     __shared__ float Bsh[16][128 + 1], Bsl[16][128 + 1];
     const int m0 = blockIdx.x * 64, n0 = blockIdx.y * 128;
-    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-    float s[4][8], c[4][8];
+    const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;
+    float s[4][4], c[4][4];
 #pragma unroll
     for (int u = 0; u < 4; u++)
 #pragma unroll
-        for (int v = 0; v < 8; v++) s[u][v] = c[u][v] = 0.0f;
+        for (int v = 0; v < 4; v++) s[u][v] = c[u][v] = 0.0f;
     for (int k0 = 0; k0 < Kd; k0 += 16) {
-        for (int t = threadIdx.x; t < 16 * 64; t += 256) {
+        for (int t = threadIdx.x; t < 16 * 64; t += 512) {
             const int kk = t / 64, mm = t % 64;
             const int m = m0 + mm, k = k0 + kk;
             const double a = (m < M && k < Kd) ? A[(size_t)k * lda + m] : 0.0;
@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(256) k_gemm_df32(const double *__restrict__ A,
             Ah[kk][mm] = h;
             Al[kk][mm] = (float)(a - (double)h);
         }
-        for (int t = threadIdx.x; t < 16 * 128; t += 256) {
+        for (int t = threadIdx.x; t < 16 * 128; t += 512) {
             const int nn = t / 16, kb = t % 16;
             const int n = n0 + nn, k = k0 + kb;
             const bool in = n < Nc && k < Kd;
@@ -152,21 +152,21 @@ __global__ void __launch_bounds__(256) k_gemm_df32(const double *__restrict__ A,
         __syncthreads();
 #pragma unroll 2
         for (int kk = 0; kk < 16; kk++) {
-            float ah[4], al[4], bh[8], bl[8];
+            float ah[4], al[4], bh[4], bl[4];
 #pragma unroll
             for (int u = 0; u < 4; u++) {
                 ah[u] = Ah[kk][ty + 16 * u];
                 al[u] = Al[kk][ty + 16 * u];
             }
 #pragma unroll
-            for (int v = 0; v < 8; v++) {
-                bh[v] = Bsh[kk][tx + 16 * v];
-                bl[v] = Bsl[kk][tx + 16 * v];
+            for (int v = 0; v < 4; v++) {
+                bh[v] = Bsh[kk][tx + 32 * v];
+                bl[v] = Bsl[kk][tx + 32 * v];
             }
 #pragma unroll
             for (int u = 0; u < 4; u++)
 #pragma unroll
-                for (int v = 0; v < 8; v++) df32_acc(s[u][v], c[u][v], ah[u], al[u], bh[v], bl[v]);
+                for (int v = 0; v < 4; v++) df32_acc(s[u][v], c[u][v], ah[u], al[u], bh[v], bl[v]);
         }
         __syncthreads();
     }
@@ -175,8 +175,8 @@ __global__ void __launch_bounds__(256) k_gemm_df32(const double *__restrict__ A,
         const int m = m0 + ty + 16 * u;
         if (m >= M) continue;
 #pragma unroll
-        for (int v = 0; v < 8; v++) {
-            const int n = n0 + tx + 16 * v;
+        for (int v = 0; v < 4; v++) {
+            const int n = n0 + tx + 32 * v;
             if (n < Nc) C[(size_t)n * ldc + m] = (double)s[u][v] + (double)c[u][v];
         }
     }
@@ -688,67 +688,6 @@ __global__ void k_charge_batched(const int *__restrict__ elems, int E, const dou
 constexpr int kBF = 16;   // frequencies per thread in the batched field
 constexpr int kBChunk = 32;
 
-// part[chunk][f][p][3]: regular contributions of one element chunk.
-template <int NEN>
-__global__ void __launch_bounds__(128) k_field_batched(const double *__restrict__ px,
-                                                       const double *__restrict__ py,
-                                                       const double *__restrict__ pz,
-                                                       const int4 *__restrict__ coinc, int P,
-                                                       const int *__restrict__ elems, int E,
-                                                       const double *__restrict__ qp,
-                                                       const double *__restrict__ cf, int F,
-                                                       double *__restrict__ part)
-{
-    __shared__ double s_q[kBChunk * kTriPts * 4];
-    __shared__ double s_c[kBF][kBChunk * kTriPts];
-    __shared__ int s_en[kBChunk * NEN];
-    const int chunk = blockIdx.y, fg = blockIdx.z;
-    const int e0 = chunk * kBChunk, ne = min(kBChunk, E - e0);
-    const int f0 = fg * kBF, nf = min(kBF, F - f0);
-    for (int t = threadIdx.x; t < ne * kTriPts * 4; t += blockDim.x)
-        s_q[t] = qp[(size_t)e0 * kTriPts * 4 + t];
-    for (int t = threadIdx.x; t < kBF * ne * kTriPts; t += blockDim.x) {
-        int ff = t / (ne * kTriPts), r = t % (ne * kTriPts);
-        s_c[ff][r] = ff < nf ? cf[(size_t)(f0 + ff) * E * kTriPts + (size_t)e0 * kTriPts + r] : 0.0;
-    }
-    for (int t = threadIdx.x; t < ne * NEN; t += blockDim.x) s_en[t] = elems[(size_t)e0 * NEN + t];
-    __syncthreads();
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= P) return;
-    const double x = px[p], y = py[p], z = pz[p];
-    const int4 c = coinc[p];
-    double acc[kBF][3];
-#pragma unroll
-    for (int ff = 0; ff < kBF; ff++) acc[ff][0] = acc[ff][1] = acc[ff][2] = 0.0;
-    for (int e = 0; e < ne; e++) {
-        bool sing = false;
-#pragma unroll
-        for (int k = 0; k < NEN; k++) {
-            int v = s_en[e * NEN + k];
-            sing |= (v == c.x) | (v == c.y) | (v == c.z) | (v == c.w);
-        }
-        if (sing && c.x >= 0) continue;
-#pragma unroll
-        for (int q = 0; q < kTriPts; q++) {
-            const double *Q = s_q + (e * kTriPts + q) * 4;
-            double dx = x - Q[0], dy = y - Q[1], dz = z - Q[2];
-            double inv = rsqrt(dx * dx + dy * dy + dz * dz);
-            double i3 = inv * inv * inv;
-            double gx = dx * i3, gy = dy * i3, gz = dz * i3;
-#pragma unroll
-            for (int ff = 0; ff < kBF; ff++) {
-                double cq = s_c[ff][e * kTriPts + q];
-                acc[ff][0] += cq * gx;
-                acc[ff][1] += cq * gy;
-                acc[ff][2] += cq * gz;
-            }
-        }
-    }
-    for (int ff = 0; ff < nf; ff++)
-        for (int d = 0; d < 3; d++)
-            part[(((size_t)chunk * F + f0 + ff) * P + p) * 3 + d] = acc[ff][d];
-}
-
 // ---- FP32 far field with FP64 near field
 // Per element: centroid as an FP32 (hi, lo) pair, squared near radius, and
 // the 7 quadrature points relative to the centroid.  A (point, element)
@@ -805,90 +744,101 @@ __global__ void k_to_f32(const double *__restrict__ x, float *__restrict__ y, si
         y[t] = (float)x[t];
 }
 
-// part[chunk][f][p][3]: as k_field_batched, far pairs in FP32 (rsqrt with a
-// Newton step, coordinates as centroid-relative offsets), near pairs in FP64.
+// part[group][f][p][3] (FP32): regular contributions of one group of
+// kBLoop x kBChunk elements to the field at point p for system f.  Far
+// pairs in FP32 (rsqrt with a Newton step, coordinates as centroid-relative
+// offsets); near pairs take the point-to-quadrature-point geometry in FP64
+// (the difference of close points) and the products in FP32.
+constexpr int kBLoop = 8;   // element chunks per block
 template <int NEN>
 __global__ void __launch_bounds__(128) k_field_batched_mixed(
     const float *__restrict__ phl, const int4 *__restrict__ coinc, int P, const int *__restrict__ elems,
     int E, const float *__restrict__ ecent, const float *__restrict__ qoff, const float *__restrict__ cf32,
-    const double *__restrict__ qp, const double *__restrict__ cf, int F, double *__restrict__ part)
+    const double *__restrict__ qp, int F, float *__restrict__ part)
 {
     __shared__ float s_cent[kBChunk * 8];
     __shared__ float s_off[kBChunk * kTriPts * 3];
     __shared__ float s_c[kBF][kBChunk * kTriPts];
     __shared__ int s_en[kBChunk * NEN];
-    const int chunk = blockIdx.y, fg = blockIdx.z;
-    const int e0 = chunk * kBChunk, ne = min(kBChunk, E - e0);
+    const int group = blockIdx.y, fg = blockIdx.z;
     const int f0 = fg * kBF, nf = min(kBF, F - f0);
-    for (int t = threadIdx.x; t < ne * 8; t += blockDim.x) s_cent[t] = ecent[(size_t)e0 * 8 + t];
-    for (int t = threadIdx.x; t < ne * kTriPts * 3; t += blockDim.x)
-        s_off[t] = qoff[(size_t)e0 * kTriPts * 3 + t];
-    for (int t = threadIdx.x; t < kBF * ne * kTriPts; t += blockDim.x) {
-        int ff = t / (ne * kTriPts), r = t % (ne * kTriPts);
-        s_c[ff][r] = ff < nf ? cf32[(size_t)(f0 + ff) * E * kTriPts + (size_t)e0 * kTriPts + r] : 0.0f;
-    }
-    for (int t = threadIdx.x; t < ne * NEN; t += blockDim.x) s_en[t] = elems[(size_t)e0 * NEN + t];
-    __syncthreads();
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= P) return;
-    const float ph[3] = {phl[(size_t)p * 6], phl[(size_t)p * 6 + 1], phl[(size_t)p * 6 + 2]};
-    const float pl[3] = {phl[(size_t)p * 6 + 3], phl[(size_t)p * 6 + 4], phl[(size_t)p * 6 + 5]};
-    const int4 c = coinc[p];
+    const bool valid = p < P;
+    const int pp = valid ? p : 0;
+    const float ph[3] = {phl[(size_t)pp * 6], phl[(size_t)pp * 6 + 1], phl[(size_t)pp * 6 + 2]};
+    const float pl[3] = {phl[(size_t)pp * 6 + 3], phl[(size_t)pp * 6 + 4], phl[(size_t)pp * 6 + 5]};
+    const double p64[3] = {(double)ph[0] + (double)pl[0], (double)ph[1] + (double)pl[1],
+                           (double)ph[2] + (double)pl[2]};
+    const int4 c = coinc[pp];
     float acc[kBF][3];
 #pragma unroll
     for (int ff = 0; ff < kBF; ff++) acc[ff][0] = acc[ff][1] = acc[ff][2] = 0.0f;
-    for (int e = 0; e < ne; e++) {
-        bool sing = false;
-#pragma unroll
-        for (int k = 0; k < NEN; k++) {
-            int v = s_en[e * NEN + k];
-            sing |= (v == c.x) | (v == c.y) | (v == c.z) | (v == c.w);
+    for (int cl = 0; cl < kBLoop; cl++) {
+        const int e0 = (group * kBLoop + cl) * kBChunk;
+        if (e0 >= E) break;  // uniform over the block
+        const int ne = min(kBChunk, E - e0);
+        __syncthreads();  // the previous chunk is no longer read
+        for (int t = threadIdx.x; t < ne * 8; t += blockDim.x) s_cent[t] = ecent[(size_t)e0 * 8 + t];
+        for (int t = threadIdx.x; t < ne * kTriPts * 3; t += blockDim.x)
+            s_off[t] = qoff[(size_t)e0 * kTriPts * 3 + t];
+        for (int t = threadIdx.x; t < kBF * ne * kTriPts; t += blockDim.x) {
+            const int ff = t / (ne * kTriPts), r = t % (ne * kTriPts);
+            s_c[ff][r] = ff < nf ? cf32[(size_t)(f0 + ff) * E * kTriPts + (size_t)e0 * kTriPts + r] : 0.0f;
         }
-        if (sing && c.x >= 0) continue;
-        const float *ce = s_cent + e * 8;
-        const float d0x = (ph[0] - ce[0]) + (pl[0] - ce[3]);
-        const float d0y = (ph[1] - ce[1]) + (pl[1] - ce[4]);
-        const float d0z = (ph[2] - ce[2]) + (pl[2] - ce[5]);
-        if (d0x * d0x + d0y * d0y + d0z * d0z < ce[6]) {
-            // near pair: FP64
-            const double p64[3] = {(double)ph[0] + (double)pl[0], (double)ph[1] + (double)pl[1],
-                                   (double)ph[2] + (double)pl[2]};
-            for (int q = 0; q < kTriPts; q++) {
-                const double *Q = qp + ((size_t)(e0 + e) * kTriPts + q) * 4;
-                double dx = p64[0] - Q[0], dy = p64[1] - Q[1], dz = p64[2] - Q[2];
-                double inv = rsqrt(dx * dx + dy * dy + dz * dz);
-                double i3 = inv * inv * inv;
-                double gx = dx * i3, gy = dy * i3, gz = dz * i3;
-                for (int ff = 0; ff < nf; ff++) {
-                    double cq = cf[(size_t)(f0 + ff) * E * kTriPts + (size_t)(e0 + e) * kTriPts + q];
-                    acc[ff][0] += (float)(cq * gx);
-                    acc[ff][1] += (float)(cq * gy);
-                    acc[ff][2] += (float)(cq * gz);
-                }
+        for (int t = threadIdx.x; t < ne * NEN; t += blockDim.x) s_en[t] = elems[(size_t)e0 * NEN + t];
+        __syncthreads();
+        if (!valid) continue;
+        for (int e = 0; e < ne; e++) {
+            bool sing = false;
+#pragma unroll
+            for (int k = 0; k < NEN; k++) {
+                const int v = s_en[e * NEN + k];
+                sing |= (v == c.x) | (v == c.y) | (v == c.z) | (v == c.w);
             }
-            continue;
-        }
-        const float *O = s_off + e * kTriPts * 3;
+            if (sing && c.x >= 0) continue;
+            const float *ce = s_cent + e * 8;
+            const float d0x = (ph[0] - ce[0]) + (pl[0] - ce[3]);
+            const float d0y = (ph[1] - ce[1]) + (pl[1] - ce[4]);
+            const float d0z = (ph[2] - ce[2]) + (pl[2] - ce[5]);
+            const bool near = d0x * d0x + d0y * d0y + d0z * d0z < ce[6];
+            const float *O = s_off + e * kTriPts * 3;
 #pragma unroll
-        for (int q = 0; q < kTriPts; q++) {
-            const float dx = d0x - O[q * 3], dy = d0y - O[q * 3 + 1], dz = d0z - O[q * 3 + 2];
-            const float r2 = dx * dx + dy * dy + dz * dz;
-            float inv = rsqrtf(r2);
-            inv = inv * (1.5f - 0.5f * r2 * inv * inv);
-            const float i3 = inv * inv * inv;
-            const float gx = dx * i3, gy = dy * i3, gz = dz * i3;
+            for (int q = 0; q < kTriPts; q++) {
+                float gx, gy, gz;
+                if (near) {
+                    const double *Q = qp + ((size_t)(e0 + e) * kTriPts + q) * 4;
+                    const double dx = p64[0] - Q[0], dy = p64[1] - Q[1], dz = p64[2] - Q[2];
+                    const double inv = rsqrt(dx * dx + dy * dy + dz * dz);
+                    const double i3 = inv * inv * inv;
+                    gx = (float)(dx * i3);
+                    gy = (float)(dy * i3);
+                    gz = (float)(dz * i3);
+                } else {
+                    const float dx = d0x - O[q * 3], dy = d0y - O[q * 3 + 1], dz = d0z - O[q * 3 + 2];
+                    const float r2 = dx * dx + dy * dy + dz * dz;
+                    float inv = rsqrtf(r2);
+                    inv = inv * (1.5f - 0.5f * r2 * inv * inv);
+                    const float i3 = inv * inv * inv;
+                    gx = dx * i3;
+                    gy = dy * i3;
+                    gz = dz * i3;
+                }
 #pragma unroll
-            for (int ff = 0; ff < kBF; ff++) {
-                const float cq = s_c[ff][e * kTriPts + q];
-                acc[ff][0] += cq * gx;
-                acc[ff][1] += cq * gy;
-                acc[ff][2] += cq * gz;
+                for (int ff = 0; ff < kBF; ff++) {
+                    const float cq = s_c[ff][e * kTriPts + q];
+                    acc[ff][0] += cq * gx;
+                    acc[ff][1] += cq * gy;
+                    acc[ff][2] += cq * gz;
+                }
             }
         }
     }
-    for (int ff = 0; ff < nf; ff++)
-        for (int d = 0; d < 3; d++)
-            part[(((size_t)chunk * F + f0 + ff) * P + p) * 3 + d] = (double)acc[ff][d];
+    if (!valid) return;
+#pragma unroll
+    for (int ff = 0; ff < kBF; ff++)  // unrolled: acc stays in registers
+        if (ff < nf)
+#pragma unroll
+            for (int d = 0; d < 3; d++) part[(((size_t)group * F + f0 + ff) * P + p) * 3 + d] = acc[ff][d];
 }
 
 // Singular elements of each point, FP64 subdivision once per (point,
@@ -947,7 +897,7 @@ __global__ void __launch_bounds__(128) k_field_batched_singular(
 }
 
 // Enode[f][node][3] = A * sum_chunks part + sing, scattered to node ids.
-__global__ void k_field_batched_reduce(const double *__restrict__ part, int nchunk, int F, int P,
+__global__ void k_field_batched_reduce(const float *__restrict__ part, int nchunk, int F, int P,
                                        const double *__restrict__ sing, const int *__restrict__ ids,
                                        int N, double *__restrict__ Enode)
 {
@@ -956,7 +906,7 @@ __global__ void k_field_batched_reduce(const double *__restrict__ part, int nchu
     const int d = (int)(t % 3), p = (int)((t / 3) % P), f = (int)(t / (3 * (size_t)P));
     const double A = 0.5 / kEps0 / kPi2;
     double s = 0.0;
-    for (int c = 0; c < nchunk; c++) s += part[(size_t)c * F * P * 3 + t];
+    for (int c = 0; c < nchunk; c++) s += (double)part[(size_t)c * F * P * 3 + t];
     Enode[((size_t)f * N + ids[p]) * 3 + d] = A * s + sing[t];
 }
 
@@ -1054,7 +1004,8 @@ struct Session::Mixed {
     DevBuf<unsigned long long> cgsb;  // bytes the Gram-Schmidt kernels moved (timing on)
     DevBuf<double> npart;   // per-block partials of |w|^2
     // batched field
-    DevBuf<double> cf, part, sing, Enode, Fce, tot;
+    DevBuf<double> cf, sing, Enode, Fce, tot;
+    DevBuf<float> part;  // field partials per element group (FP32)
     // FP32 far-field pass: element centroids / offsets, split points, weights
     bool far_ready = false;
     DevBuf<float> ecent, qoff, phl, cf32;
@@ -1062,8 +1013,8 @@ struct Session::Mixed {
 
 int Session::make_k32()
 {
-    if (k32_ready) return kOk;
-    DSC_TRY(assemble64());
+    if (k32_ready && k64_ready) return kOk;
+    DSC_TRY(assemble64(false));
     DSC_TRY(Kt32.alloc(ld * N));
     DSC_TRY(split_transpose_K(K64.p, ld, N, Kt32.p, nullptr, ld, st, true));
     k32_ready = true;
@@ -1314,7 +1265,7 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
             TimerScope ts(tm, kTResidual, st);
             DSC_LAUNCH(k_split_f32_pair<<<4 * 152, 256, 0, st>>>(w.Xs.p, w.Xh.p, w.Xl.p, blk));
             dim3 g((N + 63) / 64, (2 * F + 127) / 128);
-            DSC_LAUNCH(k_gemm_df32<<<g, 256, 0, st>>>(s.K64.p, ld, w.Xh.p, w.Xl.p, ld, w.Y64.p, ld, N, 2 * F,
+            DSC_LAUNCH(k_gemm_df32<<<g, 512, 0, st>>>(s.K64.p, ld, w.Xh.p, w.Xl.p, ld, w.Y64.p, ld, N, 2 * F,
                                                       N));
             tm->add_work(kTResidual, (double)N * N * 2 * F);  // FP64-accurate multiply-adds
             DSC_LAUNCH(k_residual<<<vg, 256, 0, st>>>(w.Y64.p, w.Xs.p, w.cs.p, w.cd.p, w.bt.p, w.R.p, N, ld, F));
@@ -1348,7 +1299,7 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
     ForcePlan &fp = s.force;
     if (fp.P > 0) {
         const int E = s.E, P = fp.P;
-        const int nchunk = (E + kBChunk - 1) / kBChunk;
+        const int nchunk = (E + kBChunk * kBLoop - 1) / (kBChunk * kBLoop);  // element groups
         DSC_TRY(w.cf.alloc((size_t)F * E * kTriPts));
         DSC_TRY(w.part.alloc((size_t)nchunk * F * P * 3));
         DSC_TRY(w.sing.alloc((size_t)F * P * 3));
@@ -1376,11 +1327,11 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
             if (s.nen == 6)
                 DSC_LAUNCH(k_field_batched_mixed<6><<<fg, 128, 0, st>>>(w.phl.p, fp.ps.coinc.p, P, s.dev.elems.p, E,
                                                                         w.ecent.p, w.qoff.p, w.cf32.p,
-                                                                        s.dev.qp.p, w.cf.p, F, w.part.p));
+                                                                        s.dev.qp.p, F, w.part.p));
             else
                 DSC_LAUNCH(k_field_batched_mixed<3><<<fg, 128, 0, st>>>(w.phl.p, fp.ps.coinc.p, P, s.dev.elems.p, E,
                                                                         w.ecent.p, w.qoff.p, w.cf32.p,
-                                                                        s.dev.qp.p, w.cf.p, F, w.part.p));
+                                                                        s.dev.qp.p, F, w.part.p));
             const int sb = (P * 32 + 127) / 128;
             if (s.nen == 6)
                 DSC_LAUNCH(k_field_batched_singular<6><<<sb, 128, 0, st>>>(

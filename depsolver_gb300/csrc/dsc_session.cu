@@ -177,11 +177,15 @@ Session::~Session()
     if (st) cudaStreamDestroy(st);
 }
 
-int Session::assemble64()
+int Session::assemble64(bool need_fp64)
 {
-    if (k64_ready) return kOk;
+    // a K assembled in FP64 serves both modes; one assembled in
+    // double-FP32 serves the mixed mode only
+    if (k64_ready && (!need_fp64 || !k64_df32)) return kOk;
+    k32_ready = false;  // the FP32 copy follows K
     DSC_TRY(K64.alloc(ld * N));
-    DSC_TRY(assemble_K_fp64(dev, K64.p, ld, st, &timer));
+    DSC_TRY(assemble_K_fp64(dev, K64.p, ld, st, &timer, !need_fp64));
+    k64_df32 = !need_fp64;
     DSC_TRY(Kdiag.alloc(N));
     DSC_LAUNCH(k_diag<<<(N + 255) / 256, 256, 0, st>>>(K64.p, ld, N, Kdiag.p));
     DSC_CUDA(cudaGetLastError());
@@ -219,7 +223,7 @@ void Session::coeffs(double f, std::vector<double> &a, std::vector<double> &b,
 int Session::solve_fp64(double f, double tol, unsigned max_iters, double *sigma_dev,
                         double *d_tot, unsigned *iters)
 {
-    DSC_TRY(assemble64());
+    DSC_TRY(assemble64(true));
     std::vector<double> a, b, d;
     coeffs(f, a, b, d);
     std::vector<double> B(2 * (size_t)N);
@@ -313,12 +317,31 @@ extern "C" int dsc_session_timing(dsc_session *s, double *ms, int *count, double
     return kOk;
 }
 
-extern "C" int dsc_session_assemble(dsc_session *s)
+extern "C" int dsc_session_assemble(dsc_session *s, int mode)
 {
+    if (mode != DSC_MODE_FP64 && mode != DSC_MODE_MIXED) {
+        set_error("dsc_session_assemble: unknown mode %d", mode);
+        return kErrArg;
+    }
     // always re-assemble: the caller asks for the work to be done now
     s->s.k64_ready = false;
     s->s.k32_ready = false;
-    return s->s.assemble64();
+    DSC_TRY(s->s.assemble64(mode == DSC_MODE_FP64));
+    return mode == DSC_MODE_MIXED ? s->s.make_k32() : kOk;
+}
+
+extern "C" int dsc_session_geometric_matrix(dsc_session *s, int mode, double *K, size_t ldk)
+{
+    Session &S = s->s;
+    if ((mode != DSC_MODE_FP64 && mode != DSC_MODE_MIXED) || !K || ldk < (size_t)S.N) {
+        set_error("dsc_session_geometric_matrix: bad arguments");
+        return kErrArg;
+    }
+    DSC_TRY(S.assemble64(mode == DSC_MODE_FP64));
+    DSC_CUDA(cudaMemcpy2DAsync(K, ldk * sizeof(double), S.K64.p, S.ld * sizeof(double),
+                               (size_t)S.N * sizeof(double), S.N, cudaMemcpyDeviceToHost, S.st));
+    DSC_CUDA(cudaStreamSynchronize(S.st));
+    return kOk;
 }
 
 extern "C" int dsc_session_solve(dsc_session *sess, int mode, unsigned nfreq, const double *freqs,

@@ -26,6 +26,7 @@ struct Session {
 
     // FP64 geometric matrix and its diagonal
     bool k64_ready = false;
+    bool k64_df32 = false;  // K64's regular pairs were integrated in double-FP32
     DevBuf<double> K64, Kdiag;
     std::vector<double> Kdiag_host;
     // plain FP64 path workspace
@@ -43,7 +44,9 @@ struct Session {
                const unsigned *bctype, const double *mbc, unsigned nIf, const unsigned *ifaces,
                unsigned nMat, const double *mat);
     ~Session();
-    int assemble64();
+    // K64 (and Kdiag) if not there yet; need_fp64: the regular pairs in FP64
+    // (else double-FP32 is enough and is what a new assembly uses)
+    int assemble64(bool need_fp64);
     int make_k32();
     void coeffs(double f, std::vector<double> &a, std::vector<double> &b,
                 std::vector<double> &d) const;

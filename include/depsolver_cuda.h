@@ -176,9 +176,18 @@ int dsc_session_create(int nen, unsigned N, unsigned E, const double *nodes, con
                        const unsigned *ifaces, unsigned nMat, const double *mat,
                        dsc_session **out);
 void dsc_session_destroy(dsc_session *s);
-/* Assembles the FP64 geometric matrix now, again if it already exists
- * (otherwise it is assembled on the first solve and then reused). */
-int dsc_session_assemble(dsc_session *s);
+/* Assembles the geometric matrix now, again if it already exists
+ * (otherwise the first solve assembles it and later solves reuse it).
+ * mode DSC_MODE_FP64: regular pairs in FP64, the reference's arithmetic;
+ * DSC_MODE_MIXED: regular pairs in double-FP32 on the FP32 pipes (about
+ * 2^-46 per operation, entries within ~1e-13 of FP64) and the FP32 copy for
+ * the tensor cores.  Singular pairs are FP64 in both.  An FP64 solve on a
+ * matrix assembled for the mixed mode assembles it again in FP64. */
+int dsc_session_assemble(dsc_session *s, int mode);
+/* The geometric matrix K (N x N) as assembled for `mode` (assembling it if
+ * needed): K[c * ldk + i] = entry (row i, node c), i.e. C * int G N_c for
+ * conductor rows and int H N_c for interface rows (src/assembly_el.c). */
+int dsc_session_geometric_matrix(dsc_session *s, int mode, double *K, size_t ldk);
 int dsc_session_solve(dsc_session *s, int mode, unsigned nfreq, const double *freqs, double tol,
                       unsigned max_iters, double *sigma, double *forces, unsigned *iters);
 /* CUDA-event timing of kernel classes (off by default).  Since the last

@@ -37,8 +37,10 @@ def test_mixed_matches_fp64_across_frequencies(gpu, port, nen):
     sc = scenes.small(nen=nen, sphere_level=2, plate_cells=4)
     freqs = np.logspace(3, 8, 6)
     s = api.Session(sc)
-    f64, it64, s64 = s.solve(freqs, mode=api.MODE_FP64, tol=1e-12, want_sigma=True)
+    # the mixed solve first: it assembles K with double-FP32 regular pairs;
+    # the FP64 solve then assembles it again in FP64
     fmx, itmx, smx = s.solve(freqs, mode=api.MODE_MIXED, tol=1e-11, want_sigma=True)
+    f64, it64, s64 = s.solve(freqs, mode=api.MODE_FP64, tol=1e-12, want_sigma=True)
     for k in range(len(freqs)):
         assert relerr(smx[k], s64[k]) < 1e-9, k
         scale = f64[k, 6:9].sum()
@@ -79,3 +81,22 @@ def test_session_timing_counts_kernels(gpu):
     # active system (16 bytes per row and system)
     assert t["gram_schmidt"][2] >= 16.0 * sc.N * t["gram_schmidt"][1]
     assert t["asm_regular"][1] == 0 and t["residual_fp64"][2] == sc.N * sc.N * 2 * F
+
+
+@pytest.mark.parametrize("nen", [6, 3])
+def test_double_fp32_assembly_matches_fp64(gpu, port, nen):
+    """K with the regular pairs in double-FP32 (the mixed mode's assembly)
+    against the FP64 assembly and the C restatement of the reference."""
+    sc = scenes.small(nen=nen)
+    s = api.Session(sc)
+    s.assemble(api.MODE_MIXED)
+    Kd = s.geometric_matrix(api.MODE_MIXED)
+    K64 = s.geometric_matrix(api.MODE_FP64)      # assembles again in FP64
+    scale = np.abs(K64).max()
+    assert np.abs(Kd - K64).max() <= 1e-13 * scale
+    assert not np.array_equal(Kd, K64)            # it is a different computation
+    # the FP64 K against the checker's compact matrix (conductor rows: C int G)
+    A, _ = port.assemble(sc)
+    N = sc.N
+    cond = sc.bctype[:N] != 6
+    assert relerr(K64[cond], A[cond][:, :N]) < 1e-12
