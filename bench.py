@@ -86,7 +86,11 @@ def roofline(timing, N, E):
 # DRAM bytes per timed scope of a class, from one ncu capture of the same
 # workload (dram__bytes_read.sum + dram__bytes_write.sum); None where not
 # captured.  The summaries behind these numbers are under profiles/.
-TRAFFIC = {}
+TRAFFIC = {
+    # k_tc_gemm_3xtf32 at N = 17684, Nc = 128: 1284.7 MB read + 98.3 MB
+    # written (profiles/tc_gemm_3xtf32_mid.md)
+    "gemm_K": 1382973696,
+}
 
 
 # ------------------------------------------------------------------ clocks
@@ -247,10 +251,16 @@ def run_ours(args, rank, world):
     s = api.Session(sc)
     stream = torch.cuda.ExternalStream(s.stream_handle())
     if args.only_step:
-        # one warm-up and one timed step only (for profiler launch lists)
+        # one warm-up and one timed step only (for profiler launch lists);
+        # --step-mode fp64: the plain FP64 path's step (FP64 assembly, the
+        # reference's GMRES at 1 MHz, force) instead
         for _ in range(2):
-            s.assemble(api.MODE_MIXED)
-            s.solve(FREQS, mode=api.MODE_MIXED, tol=TOL)
+            if args.step_mode == "fp64":
+                s.assemble(api.MODE_FP64)
+                s.solve([1e6], mode=api.MODE_FP64, tol=TOL)
+            else:
+                s.assemble(api.MODE_MIXED)
+                s.solve(FREQS, mode=api.MODE_MIXED, tol=TOL)
         torch.cuda.synchronize()
         print(json.dumps({"only_step": True, "launches": int(L.dsc_kernel_launches())}))
         return
@@ -402,6 +412,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--scene", choices=["cfg1", "mid"], default="cfg1",
                     help="mid: a smaller scene for ncu captures (with --only-step)")
+    ap.add_argument("--step-mode", choices=["mixed", "fp64"], default="mixed",
+                    help="with --only-step: profile the mixed sweep or the plain FP64 path")
     ap.add_argument("--only-step", action="store_true",
                     help="run one warm-up and one step and nothing else (profiling)")
     args = ap.parse_args()

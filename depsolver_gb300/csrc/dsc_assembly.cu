@@ -394,12 +394,14 @@ static size_t regular_smem(int nen)
 
 template <int NEN>
 static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStream_t st, Timer *tm,
-                              bool df32)
+                              bool df32, AsmWorkspace *ws)
 {
+    AsmWorkspace local;
+    AsmWorkspace &w = ws ? *ws : local;
     DSC_LAUNCH(k_elem_qp<NEN><<<(m.E * kTriPts + 255) / 256, 256, 0, st>>>(m.x.p, m.y.p, m.z.p, m.elems.p, m.E,
                                                                   m.qp.p));
     DSC_CUDA(cudaGetLastError());
-    DevBuf<float2> qpd;
+    DevBuf<float2> &qpd = w.qpd;
     if (df32) {
         DSC_TRY(qpd.alloc((size_t)m.E * kTriPts * 4));
         DSC_LAUNCH(k_qp_to_df<<<4 * 152, 256, 0, st>>>(m.qp.p, (size_t)m.E * kTriPts * 4, qpd.p));
@@ -412,7 +414,7 @@ static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStr
         size_t fit = budget / per_row;
         if (fit < (size_t)rc) rc = (int)std::max<size_t>(kRowTile, fit / kRowTile * kRowTile);
     }
-    DevBuf<double> P;
+    DevBuf<double> &P = w.P;
     DSC_TRY(P.alloc((size_t)std::max(m.n_slots, 1) * rc));
     const size_t smem = regular_smem(NEN);
     DSC_CUDA(cudaFuncSetAttribute(k_asm_regular_f64<NEN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -448,15 +450,17 @@ static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStr
             m.ne_elem.p, m.ne_pos.p, lo, hi, K, ld));
         DSC_CUDA(cudaGetLastError());
     }
-    // P is released at scope exit: wait for the kernels that read it.
-    DSC_CUDA(cudaStreamSynchronize(st));
+    // a local workspace is released at scope exit: wait for the kernels
+    // that read it
+    if (!ws) DSC_CUDA(cudaStreamSynchronize(st));
     return kOk;
 }
 
-int assemble_K_fp64(const DeviceMesh &m, double *K, size_t ld, cudaStream_t st, Timer *tm, bool df32)
+int assemble_K_fp64(const DeviceMesh &m, double *K, size_t ld, cudaStream_t st, Timer *tm, bool df32,
+                    AsmWorkspace *ws)
 {
-    return m.nen == 6 ? assemble_fp64_impl<6>(m, K, ld, st, tm, df32)
-                      : assemble_fp64_impl<3>(m, K, ld, st, tm, df32);
+    return m.nen == 6 ? assemble_fp64_impl<6>(m, K, ld, st, tm, df32, ws)
+                      : assemble_fp64_impl<3>(m, K, ld, st, tm, df32, ws);
 }
 
 }  // namespace dsc

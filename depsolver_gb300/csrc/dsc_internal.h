@@ -194,10 +194,19 @@ struct DeviceMesh {
 // geometric integral of row i against node c: C * int G N_c for conductor
 // rows, int H N_c (normal derivative, sign as the reference) for interface
 // rows.  The frequency enters only through per-row coefficients.
+// Device workspace of an assembly (partial slots, double-FP32 quadrature
+// points); a caller that assembles repeatedly keeps one to avoid
+// allocating every time.
+struct AsmWorkspace {
+    DevBuf<double> P;
+    DevBuf<float2> qpd;
+};
+
 // df32: the regular pairs in double-FP32 on the FP32 pipes (about 2^-46
 // per operation; the mixed-precision path), else in FP64 (the reference's
-// arithmetic).  Singular pairs are FP64 either way; K is FP64.
+// arithmetic).  Singular pairs are FP64 either way; K is FP64.  ws (may be
+// null: a local one, freed before returning) holds the scratch.
 int assemble_K_fp64(const DeviceMesh &m, double *K, size_t ld, cudaStream_t st, Timer *tm = nullptr,
-                    bool df32 = false);
+                    bool df32 = false, AsmWorkspace *ws = nullptr);
 
 }  // namespace dsc

@@ -184,7 +184,7 @@ int Session::assemble64(bool need_fp64)
     if (k64_ready && (!need_fp64 || !k64_df32)) return kOk;
     k32_ready = false;  // the FP32 copy follows K
     DSC_TRY(K64.alloc(ld * N));
-    DSC_TRY(assemble_K_fp64(dev, K64.p, ld, st, &timer, !need_fp64));
+    DSC_TRY(assemble_K_fp64(dev, K64.p, ld, st, &timer, !need_fp64, &asm_ws));
     k64_df32 = !need_fp64;
     DSC_TRY(Kdiag.alloc(N));
     DSC_LAUNCH(k_diag<<<(N + 255) / 256, 256, 0, st>>>(K64.p, ld, N, Kdiag.p));

@@ -27,6 +27,7 @@ struct Session {
     // FP64 geometric matrix and its diagonal
     bool k64_ready = false;
     bool k64_df32 = false;  // K64's regular pairs were integrated in double-FP32
+    AsmWorkspace asm_ws;    // kept between assemblies
     DevBuf<double> K64, Kdiag;
     std::vector<double> Kdiag_host;
     // plain FP64 path workspace
