@@ -8,10 +8,10 @@
 // Persistent kernel: one CTA per SM walks the units (128-row tile, split of
 // k) u = blockIdx.x, + gridDim.x, ...  Warp 0 lane 0 streams 128-byte-wide
 // k-blocks of A and Bh, Bl into a 3-stage shared-memory ring with TMA (128B
-// swizzle) without pausing between units; warps 2-3 split A in shared
+// swizzle) without pausing between units; warps 2-5 split A in shared
 // memory; warp 1 lane 0 issues tcgen05.mma (kind::tf32, M = 128, K = 8)
 // into one of two FP32 accumulator buffers in tensor memory and releases
-// each stage with tcgen05.commit; warps 4-7 read the finished buffer back
+// each stage with tcgen05.commit; warps 6-9 read the finished buffer back
 // (tcgen05.ld, one TMEM lane per row) and store the partial tile while the
 // next unit accumulates in the other buffer.  Every wait on an mbarrier
 // gives up after ~2 s of clock, sets *err and lets the CTA drain and free
@@ -203,7 +203,7 @@ __device__ __forceinline__ float tf32_lo_biased(float s)
 
 // AMODE 0: A arrives as a tf32 pair (tmAh, tmAl).
 // AMODE 1: A arrives as plain FP32 through tmAh into the hi slot; the tensor
-// core reads it as its truncated tf32 value, and warps 2 and 3 write the
+// core reads it as its truncated tf32 value, and warps 2..5 write the
 // remainder a - trunc(a), rounded to tf32, into the lo slot before the
 // products with lo may read the stage.
 // AMODE 2: as 1, with A in the biased encoding (tf32_bias_encode): the
@@ -217,7 +217,7 @@ __device__ __forceinline__ float tf32_lo_biased(float s)
 // truncates (sums of positive products come out low), so every MMA added
 // into an accumulator costs up to one of its units in the last place.
 template <int AMODE>
-__global__ void __launch_bounds__(256, 1)
+__global__ void __launch_bounds__(320, 1)
     k_tc_gemm_3xtf32(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
                      const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl,
                      int M, int Nc, int BN, int nkb_total, int kb_per_split, int nsplit,
@@ -247,7 +247,7 @@ __global__ void __launch_bounds__(256, 1)
         for (int s = 0; s < kTcStages; s++) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
-            mbar_init(&splitb[s], 64);  // the 64 threads of warps 2 and 3
+            mbar_init(&splitb[s], 128);  // the 128 threads of warps 2..5
         }
         for (int b = 0; b < 2; b++) {
             mbar_init(&acc_full[b], 1);
@@ -356,9 +356,9 @@ __global__ void __launch_bounds__(256, 1)
             }
             mma_commit(done);  // arrives when every MMA issued above has completed
         }
-    } else if (warp < 4) {
+    } else if (warp < 6) {
         if (SPLIT_A) {
-            // ---- splitters (warps 2 and 3): the lo slot of each stage
+            // ---- splitters (warps 2..5): the lo slot of each stage
             const int tid = threadIdx.x - 64;
             uint32_t g = 0;
             bool ok = true;
@@ -373,7 +373,7 @@ __global__ void __launch_bounds__(256, 1)
                     }
                     const float4 *hi = (const float4 *)(smem + s * stage_bytes);
                     float4 *lo = (float4 *)(smem + s * stage_bytes + a_bytes);
-                    for (int t = tid; t < (int)(a_bytes / 16); t += 64) {
+                    for (int t = tid; t < (int)(a_bytes / 16); t += 128) {
                         const float4 v = hi[t];
                         float4 l;
                         if (AMODE == 2) {
@@ -396,7 +396,7 @@ __global__ void __launch_bounds__(256, 1)
             }
         }
     } else {
-        // ---- epilogue (warps 4..7: TMEM lanes 32 (warp % 4) .. + 31 = rows)
+        // ---- epilogue (warps 6..9: TMEM lanes 32 (warp % 4) .. + 31 = rows)
         const int ew = warp & 3;
         int j = 0;
         for (int u = blockIdx.x; u < units; u += gridDim.x, j++) {
@@ -529,7 +529,7 @@ int tc_gemm_3xtf32(const float *Ah, const float *Al, size_t lda, const float *Bh
     const dim3 grid(std::min(units, nsm));
     auto launch = [&](auto kern) -> int {
         DSC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        DSC_LAUNCH(kern<<<grid, 256, smem, st>>>(ah, al, bh, bl, M, Nc, BN, nkb, kps, splits, Y, ldy,
+        DSC_LAUNCH(kern<<<grid, 320, smem, st>>>(ah, al, bh, bl, M, Nc, BN, nkb, kps, splits, Y, ldy,
                                                  ldy * (size_t)Nc, tmem_cols, acc_stride, d_err));
         return kOk;
     };
