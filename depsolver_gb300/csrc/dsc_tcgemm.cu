@@ -6,8 +6,8 @@
 //
 // A and B are K-major FP32 (row m of A and row n of B hold consecutive k).
 // Persistent kernel: one CTA per SM walks the units (128-row tile, split of
-// k) u = blockIdx.x, + gridDim.x, ...  Warp 0 lane 0 streams 128-byte-wide
-// k-blocks of A and Bh, Bl into a 3-stage shared-memory ring with TMA (128B
+// k) u = blockIdx.x, + gridDim.x, ...  Warp 0 lane 0 streams k-blocks (one
+// swizzle row) of A and Bh, Bl into a 3-stage shared-memory ring with TMA (128B
 // swizzle) without pausing between units; warps 2-5 split A in shared
 // memory; warp 1 lane 0 issues tcgen05.mma (kind::tf32, M = 128, K = 8)
 // into one of two FP32 accumulator buffers in tensor memory and releases
@@ -25,8 +25,18 @@
 namespace dsc {
 
 constexpr int kTcBM = 128;
-constexpr int kTcBK = 32;          // fp32 elements per k-block = one 128-byte swizzle row
+// A k-block is one swizzle row of kTcRowBytes bytes (128: 32 FP32 values).
+// Measured at the 12k-node scene: 128-byte rows in 3 stages 32.5 ms per
+// sweep's products, 64-byte rows in 6 stages 47.1 ms (twice the barrier
+// hand-offs per byte).
+constexpr int kTcRowBytes = 128;
+constexpr int kTcBK = kTcRowBytes / 4;  // fp32 elements per k-block
 constexpr int kTcStages = 3;
+// warps: 0 TMA producer, 1 MMA issuer, 2 .. 2 + kTcSplitWarps - 1 split A,
+// the last 4 read the accumulators back
+constexpr int kTcSplitWarps = 4;
+constexpr int kTcSplitters = 32 * kTcSplitWarps;
+constexpr int kTcThreads = 32 * (2 + kTcSplitWarps + 4);
 // 3 stages of 2 x 16 KB (A) + 2 x BN x 128 B (B) fit the 227 KB of shared
 // memory a CTA may use for BN <= 160
 constexpr int kTcMaxNc = 160;
@@ -86,16 +96,17 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, u
         : "memory");
 }
 
-// Shared-memory matrix descriptor of a K-major tile in the 128B-swizzled
-// canonical layout: rows of 128 bytes, 8-row groups 1024 bytes apart.
-__device__ __forceinline__ uint64_t sw128_desc(const void *tile)
+// Shared-memory matrix descriptor of a K-major tile in the swizzled
+// canonical layout: rows of kTcRowBytes bytes (the swizzle width), 8-row
+// groups 8 rows apart.
+__device__ __forceinline__ uint64_t sw_desc(const void *tile)
 {
     const uint64_t a = su32(tile);
-    uint64_t d = (a >> 4) & 0x3FFFull;        // start address
-    d |= (uint64_t)1 << 16;                   // leading byte offset (unused when swizzled)
-    d |= (uint64_t)(1024 >> 4) << 32;         // stride byte offset: 8 rows x 128 B
-    d |= (uint64_t)1 << 46;                   // descriptor version
-    d |= (uint64_t)2 << 61;                   // 128-byte swizzle
+    uint64_t d = (a >> 4) & 0x3FFFull;                    // start address
+    d |= (uint64_t)1 << 16;                               // leading byte offset (unused when swizzled)
+    d |= (uint64_t)((8 * kTcRowBytes) >> 4) << 32;        // stride byte offset: 8 rows
+    d |= (uint64_t)1 << 46;                               // descriptor version
+    d |= (uint64_t)(kTcRowBytes == 128 ? 2 : 4) << 61;    // 128- or 64-byte swizzle
     return d;
 }
 
@@ -203,7 +214,7 @@ __device__ __forceinline__ float tf32_lo_biased(float s)
 
 // AMODE 0: A arrives as a tf32 pair (tmAh, tmAl).
 // AMODE 1: A arrives as plain FP32 through tmAh into the hi slot; the tensor
-// core reads it as its truncated tf32 value, and warps 2..5 write the
+// core reads it as its truncated tf32 value, and the splitter warps write the
 // remainder a - trunc(a), rounded to tf32, into the lo slot before the
 // products with lo may read the stage.
 // AMODE 2: as 1, with A in the biased encoding (tf32_bias_encode): the
@@ -217,7 +228,7 @@ __device__ __forceinline__ float tf32_lo_biased(float s)
 // truncates (sums of positive products come out low), so every MMA added
 // into an accumulator costs up to one of its units in the last place.
 template <int AMODE>
-__global__ void __launch_bounds__(320, 1)
+__global__ void __launch_bounds__(kTcThreads, 1)
     k_tc_gemm_3xtf32(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
                      const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl,
                      int M, int Nc, int BN, int nkb_total, int kb_per_split, int nsplit,
@@ -230,7 +241,7 @@ __global__ void __launch_bounds__(320, 1)
     const bool comb = BN <= 128 && BN % 32 == 0;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    const uint32_t a_bytes = kTcBM * 128, b_bytes = (uint32_t)BN * 128;
+    const uint32_t a_bytes = kTcBM * kTcRowBytes, b_bytes = (uint32_t)BN * kTcRowBytes;
     const uint32_t stage_bytes = 2 * a_bytes + 2 * b_bytes;
     uint64_t *full = (uint64_t *)(smem + kTcStages * stage_bytes);
     uint64_t *empty = full + kTcStages;
@@ -247,7 +258,7 @@ __global__ void __launch_bounds__(320, 1)
         for (int s = 0; s < kTcStages; s++) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
-            mbar_init(&splitb[s], 128);  // the 128 threads of warps 2..5
+            mbar_init(&splitb[s], kTcSplitters);  // the threads of warps 2 .. 2 + kTcSplitWarps - 1
         }
         for (int b = 0; b < 2; b++) {
             mbar_init(&acc_full[b], 1);
@@ -323,9 +334,9 @@ __global__ void __launch_bounds__(320, 1)
                     }
                     tc_fence_after();
                     uint8_t *st = smem + s * stage_bytes;
-                    const uint64_t dah = sw128_desc(st), dal = sw128_desc(st + a_bytes);
-                    const uint64_t dbh = sw128_desc(st + 2 * a_bytes);
-                    const uint64_t dbl = sw128_desc(st + 2 * a_bytes + b_bytes);
+                    const uint64_t dah = sw_desc(st), dal = sw_desc(st + a_bytes);
+                    const uint64_t dbh = sw_desc(st + 2 * a_bytes);
+                    const uint64_t dbl = sw_desc(st + 2 * a_bytes + b_bytes);
                     // products with Ah: the stage as it landed
 #pragma unroll
                     for (int kk = 0; kk < kTcBK / 8; kk++) {
@@ -356,9 +367,9 @@ __global__ void __launch_bounds__(320, 1)
             }
             mma_commit(done);  // arrives when every MMA issued above has completed
         }
-    } else if (warp < 6) {
+    } else if (warp < 2 + kTcSplitWarps) {
         if (SPLIT_A) {
-            // ---- splitters (warps 2..5): the lo slot of each stage
+            // ---- splitters: the lo slot of each stage
             const int tid = threadIdx.x - 64;
             uint32_t g = 0;
             bool ok = true;
@@ -373,7 +384,7 @@ __global__ void __launch_bounds__(320, 1)
                     }
                     const float4 *hi = (const float4 *)(smem + s * stage_bytes);
                     float4 *lo = (float4 *)(smem + s * stage_bytes + a_bytes);
-                    for (int t = tid; t < (int)(a_bytes / 16); t += 128) {
+                    for (int t = tid; t < (int)(a_bytes / 16); t += kTcSplitters) {
                         const float4 v = hi[t];
                         float4 l;
                         if (AMODE == 2) {
@@ -396,7 +407,7 @@ __global__ void __launch_bounds__(320, 1)
             }
         }
     } else {
-        // ---- epilogue (warps 6..9: TMEM lanes 32 (warp % 4) .. + 31 = rows)
+        // ---- epilogue (the last 4 warps: TMEM lanes 32 (warp % 4) .. + 31 = rows)
         const int ew = warp & 3;
         int j = 0;
         for (int u = blockIdx.x; u < units; u += gridDim.x, j++) {
@@ -466,7 +477,7 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
 }
 
 // 2-D FP32 tensor: rows x k (k contiguous, row stride ld elements), boxes
-// of 32 k x box_rows rows, 128-byte swizzle, zero fill outside.
+// of kTcBK k x box_rows rows, kTcRowBytes-byte swizzle, zero fill outside.
 static int make_map(CUtensorMap *map, const float *base, int rows, int k, size_t ld, int box_rows)
 {
     auto fn = encode_fn();
@@ -483,7 +494,8 @@ static int make_map(CUtensorMap *map, const float *base, int rows, int k, size_t
     cuuint32_t box[2] = {(cuuint32_t)kTcBK, (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)base, dims, strides, box, estr,
-                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    kTcRowBytes == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
         set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
@@ -517,7 +529,7 @@ int tc_gemm_3xtf32(const float *Ah, const float *Al, size_t lda, const float *Bh
     splits = std::max(1, std::min(splits, nkb));
     const int kps = (nkb + splits - 1) / splits;
     splits = (nkb + kps - 1) / kps;  // every split has at least one k-block
-    const size_t smem = 1024 + (size_t)kTcStages * (2 * kTcBM * 128 + 2 * BN * 128) + 256;
+    const size_t smem = 1024 + (size_t)kTcStages * (2 * kTcBM + 2 * BN) * kTcRowBytes + 256;
     // persistent: one CTA per SM walks the (row tile, split) units
     static int nsm = 0;
     if (!nsm) {
@@ -529,7 +541,7 @@ int tc_gemm_3xtf32(const float *Ah, const float *Al, size_t lda, const float *Bh
     const dim3 grid(std::min(units, nsm));
     auto launch = [&](auto kern) -> int {
         DSC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        DSC_LAUNCH(kern<<<grid, 320, smem, st>>>(ah, al, bh, bl, M, Nc, BN, nkb, kps, splits, Y, ldy,
+        DSC_LAUNCH(kern<<<grid, kTcThreads, smem, st>>>(ah, al, bh, bl, M, Nc, BN, nkb, kps, splits, Y, ldy,
                                                  ldy * (size_t)Nc, tmem_cols, acc_stride, d_err));
         return kOk;
     };
