@@ -397,8 +397,12 @@ __global__ void __launch_bounds__(256) k_cgs_dots_chunk(const float2 *__restrict
                                                         unsigned long long *__restrict__ bytes)
 {
     __shared__ __align__(16) float2 swr[kDotRows], swi[kDotRows];
-    const int chunk = blockIdx.x, f = blockIdx.y;
-    if (!active[f]) return;
+    // items (row chunk, system f), grid-stride so that one resident wave of
+    // blocks covers them all
+    const int nchunk = (N + kDotRows - 1) / kDotRows;
+    for (int item = blockIdx.x; item < nchunk * F; item += gridDim.x) {
+    const int chunk = item % nchunk, f = item / nchunk;
+    if (!active[f]) continue;  // uniform over the block
     const int r0 = chunk * kDotRows, nr = min(kDotRows, N - r0);
     if (bytes && threadIdx.x == 0) atomicAdd(bytes, (unsigned long long)nr * 16u * (nk + 1));
     const float2 *wr = W + (size_t)(2 * f) * ld + r0, *wi = wr + ld;
@@ -440,6 +444,8 @@ __global__ void __launch_bounds__(256) k_cgs_dots_chunk(const float2 *__restrict
         si = df_warp_sum(si);
         if (lane == 0) part[((size_t)chunk * nk + k) * F + f] = make_double2(df_to(sr), df_to(si));
     }
+    __syncthreads();  // swr, swi are rewritten by the next item
+    }
 }
 
 __global__ void k_cgs_dots_reduce(const double2 *__restrict__ part, int nchunk, int nk, int F,
@@ -469,78 +475,84 @@ __global__ void __launch_bounds__(256) k_cgs_update(const float2 *__restrict__ V
                                                     unsigned long long *__restrict__ bytes)
 {
     __shared__ float2 cr[kInnerMax + 1], ci[kInnerMax + 1], cin[kInnerMax + 1], sh[8];
-    const int f = blockIdx.y;
-    if (!active[f]) return;
-    if (bytes && threadIdx.x == 0) {
-        const int rows = min(2 * (int)blockDim.x, N - 2 * (int)(blockIdx.x * blockDim.x));
-        if (rows > 0) atomicAdd(bytes, (unsigned long long)rows * 16u * (nk + 2));
-    }
-    for (int k = threadIdx.x; k < nk; k += blockDim.x) {
-        const double2 c = h[(size_t)k * F + f];
-        cr[k] = df_from(-c.x);
-        ci[k] = df_from(c.y);
-        cin[k] = df_from(-c.y);
-    }
-    __syncthreads();
-    const int i = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
-    float2 n2 = make_float2(0.f, 0.f);
-    if (i < N) {
-        float2 *wrp = W + (size_t)(2 * f) * ld + i, *wip = wrp + ld;
-        const float2 *vr = Vb + (size_t)(2 * f) * ld + i, *vi = vr + ld;
-        if (i + 1 < N) {
-            const float4 a = *(const float4 *)wrp, b = *(const float4 *)wip;
-            float2 wr0 = make_float2(a.x, a.y), wr1 = make_float2(a.z, a.w);
-            float2 wi0 = make_float2(b.x, b.y), wi1 = make_float2(b.z, b.w);
+    // items (row block rb of 2 blockDim.x rows, system f), grid-stride so
+    // that one resident wave of blocks covers them all
+    const int nrb = (N + 2 * (int)blockDim.x - 1) / (2 * (int)blockDim.x);
+    for (int item = blockIdx.x; item < nrb * F; item += gridDim.x) {
+        const int rb = item % nrb, f = item / nrb;
+        if (!active[f]) continue;  // uniform over the block
+        if (bytes && threadIdx.x == 0) {
+            const int rows = min(2 * (int)blockDim.x, N - 2 * rb * (int)blockDim.x);
+            atomicAdd(bytes, (unsigned long long)rows * 16u * (nk + 2));
+        }
+        for (int k = threadIdx.x; k < nk; k += blockDim.x) {
+            const double2 c = h[(size_t)k * F + f];
+            cr[k] = df_from(-c.x);
+            ci[k] = df_from(c.y);
+            cin[k] = df_from(-c.y);
+        }
+        __syncthreads();
+        const int i = 2 * (rb * (int)blockDim.x + (int)threadIdx.x);
+        float2 n2 = make_float2(0.f, 0.f);
+        if (i < N) {
+            float2 *wrp = W + (size_t)(2 * f) * ld + i, *wip = wrp + ld;
+            const float2 *vr = Vb + (size_t)(2 * f) * ld + i, *vi = vr + ld;
+            if (i + 1 < N) {
+                const float4 a = *(const float4 *)wrp, b = *(const float4 *)wip;
+                float2 wr0 = make_float2(a.x, a.y), wr1 = make_float2(a.z, a.w);
+                float2 wi0 = make_float2(b.x, b.y), wi1 = make_float2(b.z, b.w);
 #pragma unroll 2
-            for (int k = 0; k < nk; k++) {
-                const float4 p = *(const float4 *)(vr + (size_t)k * vstride);
-                const float4 q = *(const float4 *)(vi + (size_t)k * vstride);
-                const float2 p0 = make_float2(p.x, p.y), p1 = make_float2(p.z, p.w);
-                const float2 q0 = make_float2(q.x, q.y), q1 = make_float2(q.z, q.w);
-                const float2 a_r = cr[k], a_i = ci[k], a_in = cin[k];
-                df_mac(wr0, a_r, p0);   // wr -= hr vr - hi vi
-                df_mac(wr0, a_i, q0);
-                df_mac(wi0, a_r, q0);   // wi -= hr vi + hi vr
-                df_mac(wi0, a_in, p0);
-                df_mac(wr1, a_r, p1);
-                df_mac(wr1, a_i, q1);
-                df_mac(wi1, a_r, q1);
-                df_mac(wi1, a_in, p1);
+                for (int k = 0; k < nk; k++) {
+                    const float4 p = *(const float4 *)(vr + (size_t)k * vstride);
+                    const float4 q = *(const float4 *)(vi + (size_t)k * vstride);
+                    const float2 p0 = make_float2(p.x, p.y), p1 = make_float2(p.z, p.w);
+                    const float2 q0 = make_float2(q.x, q.y), q1 = make_float2(q.z, q.w);
+                    const float2 a_r = cr[k], a_i = ci[k], a_in = cin[k];
+                    df_mac(wr0, a_r, p0);   // wr -= hr vr - hi vi
+                    df_mac(wr0, a_i, q0);
+                    df_mac(wi0, a_r, q0);   // wi -= hr vi + hi vr
+                    df_mac(wi0, a_in, p0);
+                    df_mac(wr1, a_r, p1);
+                    df_mac(wr1, a_i, q1);
+                    df_mac(wi1, a_r, q1);
+                    df_mac(wi1, a_in, p1);
+                }
+                wr0 = df_norm(wr0);
+                wr1 = df_norm(wr1);
+                wi0 = df_norm(wi0);
+                wi1 = df_norm(wi1);
+                *(float4 *)wrp = make_float4(wr0.x, wr0.y, wr1.x, wr1.y);
+                *(float4 *)wip = make_float4(wi0.x, wi0.y, wi1.x, wi1.y);
+                df_mac(n2, wr0, wr0);
+                df_mac(n2, wi0, wi0);
+                df_mac(n2, wr1, wr1);
+                df_mac(n2, wi1, wi1);
+            } else {
+                float2 wr0 = *wrp, wi0 = *wip;
+                for (int k = 0; k < nk; k++) {
+                    const float2 p0 = vr[(size_t)k * vstride], q0 = vi[(size_t)k * vstride];
+                    df_mac(wr0, cr[k], p0);
+                    df_mac(wr0, ci[k], q0);
+                    df_mac(wi0, cr[k], q0);
+                    df_mac(wi0, cin[k], p0);
+                }
+                wr0 = df_norm(wr0);
+                wi0 = df_norm(wi0);
+                *wrp = wr0;
+                *wip = wi0;
+                df_mac(n2, wr0, wr0);
+                df_mac(n2, wi0, wi0);
             }
-            wr0 = df_norm(wr0);
-            wr1 = df_norm(wr1);
-            wi0 = df_norm(wi0);
-            wi1 = df_norm(wi1);
-            *(float4 *)wrp = make_float4(wr0.x, wr0.y, wr1.x, wr1.y);
-            *(float4 *)wip = make_float4(wi0.x, wi0.y, wi1.x, wi1.y);
-            df_mac(n2, wr0, wr0);
-            df_mac(n2, wi0, wi0);
-            df_mac(n2, wr1, wr1);
-            df_mac(n2, wi1, wi1);
-        } else {
-            float2 wr0 = *wrp, wi0 = *wip;
-            for (int k = 0; k < nk; k++) {
-                const float2 p0 = vr[(size_t)k * vstride], q0 = vi[(size_t)k * vstride];
-                df_mac(wr0, cr[k], p0);
-                df_mac(wr0, ci[k], q0);
-                df_mac(wi0, cr[k], q0);
-                df_mac(wi0, cin[k], p0);
-            }
-            wr0 = df_norm(wr0);
-            wi0 = df_norm(wi0);
-            *wrp = wr0;
-            *wip = wi0;
-            df_mac(n2, wr0, wr0);
-            df_mac(n2, wi0, wi0);
         }
+        const double t = df_block_sum(n2, sh);
+        if (threadIdx.x == 0) npart[(size_t)f * nrb + rb] = t;
+        if (hacc && rb == 0 && threadIdx.x == 0)
+            for (int k = 0; k < nk; k++) {
+                double2 a = hacc[(size_t)k * F + f], c = h[(size_t)k * F + f];
+                hacc[(size_t)k * F + f] = make_double2(a.x + c.x, a.y + c.y);
+            }
+        __syncthreads();  // cr, ci, cin and sh are rewritten by the next item
     }
-    const double t = df_block_sum(n2, sh);
-    if (threadIdx.x == 0) npart[(size_t)f * gridDim.x + blockIdx.x] = t;
-    if (hacc && blockIdx.x == 0 && threadIdx.x == 0)
-        for (int k = 0; k < nk; k++) {
-            double2 a = hacc[(size_t)k * F + f], c = h[(size_t)k * F + f];
-            hacc[(size_t)k * F + f] = make_double2(a.x + c.x, a.y + c.y);
-        }
 }
 
 // nrm[f] = sqrt(sum of the nb block partials of |w_f|^2), in block order,
@@ -1003,6 +1015,7 @@ struct Session::Mixed {
     DevBuf<int> active, act0, act2, mcount;
     DevBuf<unsigned long long> cgsb;  // bytes the Gram-Schmidt kernels moved (timing on)
     DevBuf<double> npart;   // per-block partials of |w|^2
+    int dots_grid = 0, upd_grid = 0;  // one resident wave of the Gram-Schmidt kernels
     // batched field
     DevBuf<double> cf, sing, Enode, Fce, tot;
     DevBuf<float> part;  // field partials per element group (FP32)
@@ -1216,12 +1229,13 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
                 TimerScope tc(tm, kTCgs, st);
                 const int *mask = pass == 0 ? w.active.p : w.act2.p;
                 const int nchunk = (N + kDotRows - 1) / kDotRows;
-                DSC_LAUNCH(k_cgs_dots_chunk<<<dim3(nchunk, F), 256, 0, st>>>(w.Vb.p, blk, w.W.p, N, ld, F, j + 1,
+                DSC_LAUNCH(k_cgs_dots_chunk<<<std::min(nchunk * F, w.dots_grid), 256, 0, st>>>(w.Vb.p, blk, w.W.p, N,
+                                                                                               ld, F, j + 1,
                                                                             mask, w.dpart.p, cgsb));
                 DSC_LAUNCH(k_cgs_dots_reduce<<<((j + 1) * F + 255) / 256, 256, 0, st>>>(w.dpart.p, nchunk, j + 1, F,
                                                                                        mask, w.h.p));
-                DSC_LAUNCH(k_cgs_update<<<vg2, 256, 0, st>>>(w.Vb.p, blk, w.W.p, N, ld, F, j + 1, mask, w.h.p,
-                                                             w.hacc.p, w.npart.p, cgsb));
+                DSC_LAUNCH(k_cgs_update<<<std::min((int)(vg2.x * vg2.y), w.upd_grid), 256, 0, st>>>(
+                    w.Vb.p, blk, w.W.p, N, ld, F, j + 1, mask, w.h.p, w.hacc.p, w.npart.p, cgsb));
                 // pass 0: |w| of every active system and the DGKS decision;
                 // pass 1: |w| of the systems that took the second pass
                 if (pass == 0)
@@ -1439,6 +1453,15 @@ int Session::solve_mixed(unsigned nfreq, const double *freqs, double tol, unsign
         DSC_TRY(w.mcount.alloc(Fmax));
         DSC_TRY(w.tot.alloc((size_t)Fmax * 9));
         DSC_TRY(w.cgsb.alloc(1));
+        {
+            int dev = 0, nsm = 0, o1 = 0, o2 = 0;
+            DSC_CUDA(cudaGetDevice(&dev));
+            DSC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+            DSC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o1, k_cgs_dots_chunk, 256, 0));
+            DSC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o2, k_cgs_update, 256, 0));
+            w.dots_grid = nsm * std::max(1, o1);
+            w.upd_grid = nsm * std::max(1, o2);
+        }
         DSC_TRY(w.npart.alloc((size_t)Fmax * ((N + 255) / 256)));
         DSC_CUDA(cudaMemsetAsync(w.cgsb.p, 0, sizeof(unsigned long long), st));
         // the padding rows of the blocks are never read but keep them finite
