@@ -49,30 +49,65 @@ void note_launch();
     } while (0)
 
 // ---------------------------------------------------------------- buffers
+// Stream-ordered allocation.  While an AllocStreamScope is active on a
+// thread (a session's calls set one with the session's stream), DevBuf
+// takes memory with cudaMallocAsync on that stream from the device's
+// default pool, which keeps freed memory for the next allocation (a new
+// session reuses the previous one's blocks instead of mapping new memory),
+// and gives it back with cudaFreeAsync on the same stream.  Outside a scope
+// it uses cudaMalloc / cudaFree.
+cudaStream_t &alloc_stream();
+int alloc_pool_setup();  // once per device: the default pool keeps freed memory
+
+struct AllocStreamScope {
+    cudaStream_t prev;
+    explicit AllocStreamScope(cudaStream_t s) : prev(alloc_stream()) { alloc_stream() = s; }
+    ~AllocStreamScope() { alloc_stream() = prev; }
+    AllocStreamScope(const AllocStreamScope &) = delete;
+    AllocStreamScope &operator=(const AllocStreamScope &) = delete;
+};
+
 template <typename T>
 struct DevBuf {
     T *p = nullptr;
     size_t n = 0;
+    cudaStream_t s = nullptr;  // the stream of a stream-ordered allocation
+    bool async = false;
     DevBuf() = default;
     DevBuf(const DevBuf &) = delete;
     DevBuf &operator=(const DevBuf &) = delete;
     ~DevBuf() { release(); }
     void release()
     {
-        if (p) cudaFree(p);
+        if (p) {
+            if (async) cudaFreeAsync(p, s);
+            else cudaFree(p);
+        }
         p = nullptr;
         n = 0;
+        async = false;
     }
     int alloc(size_t count)
     {
         if (count <= n && p) return kOk;
         release();
         if (count == 0) count = 1;
-        if (cudaMalloc(&p, count * sizeof(T)) != cudaSuccess) {
+        const cudaStream_t as = alloc_stream();
+        cudaError_t e;
+        if (as) {
+            DSC_TRY(alloc_pool_setup());
+            e = cudaMallocAsync((void **)&p, count * sizeof(T), as);
+        } else {
+            e = cudaMalloc(&p, count * sizeof(T));
+        }
+        if (e != cudaSuccess) {
             cudaGetLastError();
-            set_error("cudaMalloc of %zu bytes failed", count * sizeof(T));
+            p = nullptr;
+            set_error("device allocation of %zu bytes failed", count * sizeof(T));
             return kErrMemory;
         }
+        async = as != nullptr;
+        s = as;
         n = count;
         return kOk;
     }

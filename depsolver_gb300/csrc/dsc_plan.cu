@@ -286,6 +286,26 @@ std::vector<int> plan_coords_find(const HostPlan &p, double x, double y, double 
     return out;
 }
 
+cudaStream_t &alloc_stream()
+{
+    static thread_local cudaStream_t s = nullptr;
+    return s;
+}
+
+int alloc_pool_setup()
+{
+    static bool done[64] = {};
+    int dev = 0;
+    DSC_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64 || done[dev]) return kOk;
+    cudaMemPool_t pool;
+    DSC_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
+    uint64_t keep = ~(uint64_t)0;
+    DSC_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    done[dev] = true;
+    return kOk;
+}
+
 cudaEvent_t Timer::take()
 {
     if (!pool.empty()) {

@@ -128,6 +128,7 @@ int Session::create(int nen_, unsigned N_, unsigned E_, const double *nodes, con
     E = (int)E_;
     nIf = nIf_;
     DSC_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    AllocStreamScope as(st);
     std::vector<int> e0((size_t)E * nen);
     for (size_t t = 0; t < e0.size(); t++) e0[t] = (int)elems[t] - 1;
     DSC_TRY(build_plan(nen, N, E, nodes, e0.data(), bctype_, plan));
@@ -173,8 +174,7 @@ void destroy_mixed(Session::Mixed *m);
 
 Session::~Session()
 {
-    if (mx) destroy_mixed(mx);
-    if (st) cudaStreamDestroy(st);
+    if (mx) destroy_mixed(mx);  // the stream itself goes last (StreamGuard)
 }
 
 int Session::assemble64(bool need_fp64)
@@ -319,6 +319,7 @@ extern "C" int dsc_session_timing(dsc_session *s, double *ms, int *count, double
 
 extern "C" int dsc_session_assemble(dsc_session *s, int mode)
 {
+    AllocStreamScope as(s->s.st);
     if (mode != DSC_MODE_FP64 && mode != DSC_MODE_MIXED) {
         set_error("dsc_session_assemble: unknown mode %d", mode);
         return kErrArg;
@@ -332,6 +333,7 @@ extern "C" int dsc_session_assemble(dsc_session *s, int mode)
 
 extern "C" int dsc_session_geometric_matrix(dsc_session *s, int mode, double *K, size_t ldk)
 {
+    AllocStreamScope as(s->s.st);
     Session &S = s->s;
     if ((mode != DSC_MODE_FP64 && mode != DSC_MODE_MIXED) || !K || ldk < (size_t)S.N) {
         set_error("dsc_session_geometric_matrix: bad arguments");
@@ -349,6 +351,7 @@ extern "C" int dsc_session_solve(dsc_session *sess, int mode, unsigned nfreq, co
                                  unsigned *iters)
 {
     Session &s = sess->s;
+    AllocStreamScope as(s.st);
     if (mode != DSC_MODE_FP64 && mode != DSC_MODE_MIXED) {
         set_error("dsc_session_solve: unknown mode %d", mode);
         return kErrArg;

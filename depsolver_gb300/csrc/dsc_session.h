@@ -8,10 +8,26 @@
 
 namespace dsc {
 
+// Destroys the session's stream after every other member (members go in
+// reverse order of declaration): buffers of stream-ordered allocations are
+// freed on the stream first, then the stream is drained and destroyed.
+struct StreamGuard {
+    cudaStream_t *st;
+    explicit StreamGuard(cudaStream_t *s) : st(s) {}
+    ~StreamGuard()
+    {
+        if (*st) {
+            cudaStreamSynchronize(*st);
+            cudaStreamDestroy(*st);
+        }
+    }
+};
+
 struct Session {
     int nen = 6, N = 0, E = 0;
     unsigned nIf = 0;
     cudaStream_t st = nullptr;
+    StreamGuard st_guard{&st};  // declared before every device buffer
     HostPlan plan;
     DeviceMesh dev;
     ForcePlan force;

@@ -175,6 +175,9 @@ int dsc_session_create(int nen, unsigned N, unsigned E, const double *nodes, con
                        const unsigned *bctype, const double *mbc, unsigned nIf,
                        const unsigned *ifaces, unsigned nMat, const double *mat,
                        dsc_session **out);
+/* A session's device memory comes from the device's default memory pool in
+ * stream order; on destroy it goes back to the pool, which keeps it for the
+ * next session of the process instead of returning it to the device. */
 void dsc_session_destroy(dsc_session *s);
 /* Assembles the geometric matrix now, again if it already exists
  * (otherwise the first solve assembles it and later solves reuse it).
