@@ -97,35 +97,34 @@ __global__ void __launch_bounds__(256) k_gemm_cm(const TA *__restrict__ A, size_
     }
 }
 
-// C (M x Nc, FP64) = A (M x Kd) * B (Kd x Nc), column-major, to about FP64
-// accuracy on the FP32 pipes: each operand is an FP32 pair (hi, lo); the
-// product hi*hi is made exact with an FMA (p + e), the running sum is an
-// unevaluated pair (s, c) kept exact by TwoSum, and the cross terms
-// hi*lo + lo*hi go into c.  A is FP64 and split while it is staged (its
-// conversions run on the FP64 pipe, once per element: a tile spans 128
-// columns); B comes pre-split (Bh, Bl).  64 x 128 tile, 512 threads with
-// 4 x 4 outputs each, k-steps of 16.
-__device__ __forceinline__ void df32_acc(float &s, float &c, float ah, float al, float bh, float bl)
+// C (M x Nc, FP64) = fl32(A) (M x Kd) * B (Kd x Nc), column-major: A is FP64
+// and rounded to FP32 as it is staged (one conversion per element on the
+// FP64 pipe: a tile spans 128 columns), B is FP32; every product is exact
+// (p = a*b and e = fma(a, b, -p)) and the running sum is an unevaluated pair
+// (s, c) kept exact by TwoSum: about 2^-46 of the sum of |a b|.  The parts
+// of A and of the true B below FP32 are small (2^-24 relative) and go to
+// the tensor cores (the first residual of the mixed sweep).  64 x 128 tile,
+// 512 threads with 4 x 4 outputs each, k-steps of 16.
+__device__ __forceinline__ void exact_acc(float &s, float &c, float a, float b)
 {
     // the _rn intrinsics keep the compiler from fusing these operations,
     // which would break the exactness of the product and of TwoSum
-    const float p = __fmul_rn(ah, bh);
-    const float e = fmaf(ah, bh, -p);
+    const float p = __fmul_rn(a, b);
+    const float e = __fmaf_rn(a, b, -p);
     const float t = __fadd_rn(s, p);
     const float bp = __fsub_rn(t, s);
     const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
     s = t;
-    c += err + e + fmaf(ah, bl, al * bh);
+    c += err + e;
 }
 
-__global__ void __launch_bounds__(512) k_gemm_df32(const double *__restrict__ A, size_t lda,
-                                                   const float *__restrict__ Bh,
-                                                   const float *__restrict__ Bl, size_t ldb,
-                                                   double *__restrict__ C, size_t ldc, int M, int Nc,
-                                                   int Kd)
+__global__ void __launch_bounds__(512, 1) k_gemm_exact32(const double *__restrict__ A, size_t lda,
+                                                      const float *__restrict__ B, size_t ldb,
+                                                      double *__restrict__ C, size_t ldc, int M, int Nc,
+                                                      int Kd)
 {
-    __shared__ float Ah[16][64 + 1], Al[16][64 + 1];
-    __shared__ float Bsh[16][128 + 1], Bsl[16][128 + 1];
+    __shared__ float As[16][64 + 1];
+    __shared__ float Bs[16][128 + 1];
     const int m0 = blockIdx.x * 64, n0 = blockIdx.y * 128;
     const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;
     float s[4][4], c[4][4];
@@ -137,36 +136,25 @@ __global__ void __launch_bounds__(512) k_gemm_df32(const double *__restrict__ A,
         for (int t = threadIdx.x; t < 16 * 64; t += 512) {
             const int kk = t / 64, mm = t % 64;
             const int m = m0 + mm, k = k0 + kk;
-            const double a = (m < M && k < Kd) ? A[(size_t)k * lda + m] : 0.0;
-            const float h = (float)a;
-            Ah[kk][mm] = h;
-            Al[kk][mm] = (float)(a - (double)h);
+            As[kk][mm] = (m < M && k < Kd) ? (float)A[(size_t)k * lda + m] : 0.0f;
         }
         for (int t = threadIdx.x; t < 16 * 128; t += 512) {
             const int nn = t / 16, kb = t % 16;
             const int n = n0 + nn, k = k0 + kb;
-            const bool in = n < Nc && k < Kd;
-            Bsh[kb][nn] = in ? Bh[(size_t)n * ldb + k] : 0.0f;
-            Bsl[kb][nn] = in ? Bl[(size_t)n * ldb + k] : 0.0f;
+            Bs[kb][nn] = (n < Nc && k < Kd) ? B[(size_t)n * ldb + k] : 0.0f;
         }
         __syncthreads();
 #pragma unroll 2
         for (int kk = 0; kk < 16; kk++) {
-            float ah[4], al[4], bh[4], bl[4];
+            float a[4], b[4];
 #pragma unroll
-            for (int u = 0; u < 4; u++) {
-                ah[u] = Ah[kk][ty + 16 * u];
-                al[u] = Al[kk][ty + 16 * u];
-            }
+            for (int u = 0; u < 4; u++) a[u] = As[kk][ty + 16 * u];
 #pragma unroll
-            for (int v = 0; v < 4; v++) {
-                bh[v] = Bsh[kk][tx + 32 * v];
-                bl[v] = Bsl[kk][tx + 32 * v];
-            }
+            for (int v = 0; v < 4; v++) b[v] = Bs[kk][tx + 32 * v];
 #pragma unroll
             for (int u = 0; u < 4; u++)
 #pragma unroll
-                for (int v = 0; v < 4; v++) df32_acc(s[u][v], c[u][v], ah[u], al[u], bh[v], bl[v]);
+                for (int v = 0; v < 4; v++) exact_acc(s[u][v], c[u][v], a[u], b[v]);
         }
         __syncthreads();
     }
@@ -1029,7 +1017,8 @@ int Session::make_k32()
     if (k32_ready && k64_ready) return kOk;
     DSC_TRY(assemble64(false));
     DSC_TRY(Kt32.alloc(ld * N));
-    DSC_TRY(split_transpose_K(K64.p, ld, N, Kt32.p, nullptr, ld, st, true));
+    DSC_TRY(dKt32.alloc(ld * N));
+    DSC_TRY(split_transpose_K(K64.p, ld, N, Kt32.p, dKt32.p, ld, st, kTransposeBiasedRem));
     k32_ready = true;
     return kOk;
 }
@@ -1277,11 +1266,22 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
         if (outer == 0) {
             // the first residual in FP64: r = bt - M x
             TimerScope ts(tm, kTResidual, st);
+            // K x = fl32(K) xh (exact products, on the FP32 pipes)
+            //     + fl32(K) xl + (K - fl32(K)) xh (both ~2^-24 of K x: the
+            //       tensor cores' FP32-level accuracy suffices)
+            // with x = xh + xl, xh = fl32(x)
             DSC_LAUNCH(k_split_f32_pair<<<4 * 152, 256, 0, st>>>(w.Xs.p, w.Xh.p, w.Xl.p, blk));
             dim3 g((N + 63) / 64, (2 * F + 127) / 128);
-            DSC_LAUNCH(k_gemm_df32<<<g, 512, 0, st>>>(s.K64.p, ld, w.Xh.p, w.Xl.p, ld, w.Y64.p, ld, N, 2 * F,
-                                                      N));
+            DSC_LAUNCH(k_gemm_exact32<<<g, 512, 0, st>>>(s.K64.p, ld, w.Xh.p, ld, w.Y64.p, ld, N, 2 * F, N));
             tm->add_work(kTResidual, (double)N * N * 2 * F);  // FP64-accurate multiply-adds
+            DSC_TRY(f32_to_tf32_pair(w.Xl.p, w.Vh.p, w.Vl.p, blk, st));
+            DSC_TRY(tc_gemm_3xtf32(s.Kt32.p, nullptr, ld, w.Vh.p, w.Vl.p, ld, N, 2 * F, N, w.Yp.p, ld, w.S,
+                                   w.err.p, st, true));
+            DSC_TRY(add_splits(w.Yp.p, w.S, ld * 2 * (size_t)F, ld, N, 2 * F, w.Y64.p, ld, st));
+            DSC_TRY(f32_to_tf32_pair(w.Xh.p, w.Vh.p, w.Vl.p, blk, st));
+            DSC_TRY(tc_gemm_3xtf32(s.dKt32.p, nullptr, ld, w.Vh.p, w.Vl.p, ld, N, 2 * F, N, w.Yp.p, ld, w.S,
+                                   w.err.p, st, true));
+            DSC_TRY(add_splits(w.Yp.p, w.S, ld * 2 * (size_t)F, ld, N, 2 * F, w.Y64.p, ld, st));
             DSC_LAUNCH(k_residual<<<vg, 256, 0, st>>>(w.Y64.p, w.Xs.p, w.cs.p, w.cd.p, w.bt.p, w.R.p, N, ld, F));
         } else {
             // later residuals are updated, r -= M d: d is small, so the

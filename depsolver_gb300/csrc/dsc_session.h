@@ -54,6 +54,7 @@ struct Session {
     // batched-solver workspace
     bool k32_ready = false;
     DevBuf<float> Kt32;
+    DevBuf<float> dKt32;  // K - fl32(K), row-major, biased tf32 encoding
     struct Mixed;
     Mixed *mx = nullptr;
 

@@ -578,7 +578,7 @@ __device__ __forceinline__ void tf32_split(double v, float &hi, float &lo)
 // (entry (i, c) at i * ldt + c): a 32 x 32 shared tile per block.
 __global__ void k_split_transpose(const double *__restrict__ K, size_t ld, int N,
                                   float *__restrict__ Th, float *__restrict__ Tl, size_t ldt,
-                                  bool biased)
+                                  int mode)
 {
     __shared__ double t[32][33];
     const int i0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
@@ -590,15 +590,18 @@ __global__ void k_split_transpose(const double *__restrict__ K, size_t ld, int N
     for (int k = threadIdx.y; k < 32; k += blockDim.y) {
         int i = i0 + k, c = c0 + threadIdx.x;
         if (i < N && c < N) {
-            if (!Tl) {
-                const float v = (float)t[threadIdx.x][k];  // plain FP32, or biased
-                Th[(size_t)i * ldt + c] = biased ? tf32_bias_encode(v) : v;
+            const double a = t[threadIdx.x][k];
+            if (mode == kTransposePair) {
+                float h, l;
+                tf32_split(a, h, l);
+                Th[(size_t)i * ldt + c] = h;
+                Tl[(size_t)i * ldt + c] = l;
                 continue;
             }
-            float h, l;
-            tf32_split(t[threadIdx.x][k], h, l);
-            Th[(size_t)i * ldt + c] = h;
-            Tl[(size_t)i * ldt + c] = l;
+            const float v = (float)a;
+            Th[(size_t)i * ldt + c] = mode == kTransposePlain ? v : tf32_bias_encode(v);
+            if (mode == kTransposeBiasedRem)  // the part of a below FP32, biased too
+                Tl[(size_t)i * ldt + c] = tf32_bias_encode((float)(a - (double)v));
         }
     }
 }
@@ -617,10 +620,10 @@ __global__ void k_split_vec(const double *__restrict__ x, float *__restrict__ h,
 }
 
 int split_transpose_K(const double *K, size_t ld, int N, float *Th, float *Tl, size_t ldt,
-                      cudaStream_t st, bool biased)
+                      cudaStream_t st, int mode)
 {
     dim3 g((N + 31) / 32, (N + 31) / 32), b(32, 8);
-    DSC_LAUNCH(k_split_transpose<<<g, b, 0, st>>>(K, ld, N, Th, Tl, ldt, biased));
+    DSC_LAUNCH(k_split_transpose<<<g, b, 0, st>>>(K, ld, N, Th, Tl, ldt, mode));
     DSC_CUDA(cudaGetLastError());
     return kOk;
 }
@@ -704,6 +707,46 @@ int tc_gemm_splits_used(int Kd, int splits)
     splits = std::max(1, std::min(splits, nkb));
     const int kps = (nkb + splits - 1) / splits;
     return (nkb + kps - 1) / kps;
+}
+
+// FP32 array to tf32 pairs (hi = rna(x), lo = rna(x - hi)), elementwise.
+__global__ void k_f32_to_tf32_pair(const float *__restrict__ x, float *__restrict__ h,
+                                   float *__restrict__ l, size_t n)
+{
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n;
+         t += (size_t)gridDim.x * blockDim.x) {
+        const float a = x[t], hi = tf32_rna(a);
+        h[t] = hi;
+        l[t] = tf32_rna(a - hi);
+    }
+}
+
+int f32_to_tf32_pair(const float *x, float *h, float *l, size_t n, cudaStream_t st)
+{
+    DSC_LAUNCH(k_f32_to_tf32_pair<<<4 * 152, 256, 0, st>>>(x, h, l, n));
+    DSC_CUDA(cudaGetLastError());
+    return kOk;
+}
+
+// Y[n * ldy + m] (FP64, column n) += the S partial tiles, in split order.
+__global__ void k_add_splits(const float *__restrict__ P, int S, size_t split_stride, size_t ldp,
+                             int M, double *__restrict__ Y, size_t ldy)
+{
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = blockIdx.y;
+    if (m >= M) return;
+    double s = 0.0;
+    for (int k = 0; k < S; k++) s += (double)P[(size_t)k * split_stride + (size_t)n * ldp + m];
+    Y[(size_t)n * ldy + m] += s;
+}
+
+int add_splits(const float *P, int S, size_t split_stride, size_t ldp, int M, int Nc, double *Y,
+               size_t ldy, cudaStream_t st)
+{
+    dim3 g((M + 255) / 256, Nc);
+    DSC_LAUNCH(k_add_splits<<<g, 256, 0, st>>>(P, S, split_stride, ldp, M, Y, ldy));
+    DSC_CUDA(cudaGetLastError());
+    return kOk;
 }
 
 }  // namespace dsc

@@ -20,10 +20,19 @@ int tc_gemm_3xtf32(const float *Ah, const float *Al, size_t lda, const float *Bh
                    cudaStream_t st, bool a_biased = false);
 int tc_gemm_splits_for(int M, int Kd);
 
-// Column-major FP64 N x N matrix (stride ld) to row-major tf32 pairs, or
-// (Tl = null) to row-major FP32, plain or in the biased tf32 encoding.
+// Column-major FP64 N x N matrix (stride ld) to row-major FP32: the tf32
+// pair of each entry (Th, Tl), the entry rounded to FP32 (Th; plain or in
+// the biased tf32 encoding), or the biased FP32 entry (Th) and the biased
+// FP32 rounding of the rest (Tl: a - (double)(float)a).
+enum { kTransposePair = 0, kTransposePlain = 1, kTransposeBiased = 2, kTransposeBiasedRem = 3 };
 int split_transpose_K(const double *K, size_t ld, int N, float *Th, float *Tl, size_t ldt,
-                      cudaStream_t st, bool biased = false);
+                      cudaStream_t st, int mode);
+// FP32 array to tf32 pairs, elementwise.
+int f32_to_tf32_pair(const float *x, float *h, float *l, size_t n, cudaStream_t st);
+// Y[n * ldy + m] += the S partial tiles of tc_gemm_3xtf32 (tile s, column n,
+// row m at s * split_stride + n * ldp + m), in split order.
+int add_splits(const float *P, int S, size_t split_stride, size_t ldp, int M, int Nc, double *Y,
+               size_t ldy, cudaStream_t st);
 // FP64 array to tf32 pairs, elementwise.
 int split_vec(const double *x, float *h, float *l, size_t n, cudaStream_t st);
 // Row-major FP64 rows x k (row stride ld) to tf32 pairs (row stride ldh).
