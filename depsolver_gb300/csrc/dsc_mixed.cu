@@ -696,7 +696,7 @@ constexpr int kBChunk = 32;
 constexpr float kNearFactor = 4.0f;
 
 __global__ void k_prepare_far(const double *__restrict__ qp, int E, float *__restrict__ ecent,
-                              float *__restrict__ qoff)
+                              float *__restrict__ qoff, float2 *__restrict__ qdf)
 {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
@@ -710,6 +710,7 @@ __global__ void k_prepare_far(const double *__restrict__ qp, int E, float *__res
         for (int d = 0; d < 3; d++) {
             double o = qp[((size_t)e * kTriPts + q) * 4 + d] - c[d];
             qoff[((size_t)e * kTriPts + q) * 3 + d] = (float)o;
+            qdf[((size_t)e * kTriPts + q) * 3 + d] = df_from(qp[((size_t)e * kTriPts + q) * 4 + d]);
             s += o * o;
         }
         r2 = fmax(r2, s);
@@ -754,11 +755,11 @@ template <int NEN>
 __global__ void __launch_bounds__(128) k_field_batched_mixed(
     const float *__restrict__ phl, const int4 *__restrict__ coinc, int P, const int *__restrict__ elems,
     int E, const float *__restrict__ ecent, const float *__restrict__ qoff, const float *__restrict__ cf32,
-    const double *__restrict__ qp, int F, float *__restrict__ part)
+    const float2 *__restrict__ qdf, int F, float *__restrict__ part)
 {
     __shared__ float s_cent[kBChunk * 8];
     __shared__ float s_off[kBChunk * kTriPts * 3];
-    __shared__ float s_c[kBF][kBChunk * kTriPts];
+    __shared__ __align__(16) float s_c[kBChunk * kTriPts][kBF];  // charge of (e, q) for the group's systems
     __shared__ int s_en[kBChunk * NEN];
     const int group = blockIdx.y, fg = blockIdx.z;
     const int f0 = fg * kBF, nf = min(kBF, F - f0);
@@ -767,8 +768,7 @@ __global__ void __launch_bounds__(128) k_field_batched_mixed(
     const int pp = valid ? p : 0;
     const float ph[3] = {phl[(size_t)pp * 6], phl[(size_t)pp * 6 + 1], phl[(size_t)pp * 6 + 2]};
     const float pl[3] = {phl[(size_t)pp * 6 + 3], phl[(size_t)pp * 6 + 4], phl[(size_t)pp * 6 + 5]};
-    const double p64[3] = {(double)ph[0] + (double)pl[0], (double)ph[1] + (double)pl[1],
-                           (double)ph[2] + (double)pl[2]};
+    const float2 pdf[3] = {make_float2(ph[0], pl[0]), make_float2(ph[1], pl[1]), make_float2(ph[2], pl[2])};
     const int4 c = coinc[pp];
     float acc[kBF][3];
 #pragma unroll
@@ -783,7 +783,7 @@ __global__ void __launch_bounds__(128) k_field_batched_mixed(
             s_off[t] = qoff[(size_t)e0 * kTriPts * 3 + t];
         for (int t = threadIdx.x; t < kBF * ne * kTriPts; t += blockDim.x) {
             const int ff = t / (ne * kTriPts), r = t % (ne * kTriPts);
-            s_c[ff][r] = ff < nf ? cf32[(size_t)(f0 + ff) * E * kTriPts + (size_t)e0 * kTriPts + r] : 0.0f;
+            s_c[r][ff] = ff < nf ? cf32[(size_t)(f0 + ff) * E * kTriPts + (size_t)e0 * kTriPts + r] : 0.0f;
         }
         for (int t = threadIdx.x; t < ne * NEN; t += blockDim.x) s_en[t] = elems[(size_t)e0 * NEN + t];
         __syncthreads();
@@ -806,13 +806,15 @@ __global__ void __launch_bounds__(128) k_field_batched_mixed(
             for (int q = 0; q < kTriPts; q++) {
                 float gx, gy, gz;
                 if (near) {
-                    const double *Q = qp + ((size_t)(e0 + e) * kTriPts + q) * 4;
-                    const double dx = p64[0] - Q[0], dy = p64[1] - Q[1], dz = p64[2] - Q[2];
-                    const double inv = rsqrt(dx * dx + dy * dy + dz * dz);
-                    const double i3 = inv * inv * inv;
-                    gx = (float)(dx * i3);
-                    gy = (float)(dy * i3);
-                    gz = (float)(dz * i3);
+                    // the difference of close points in double-FP32
+                    const float2 *Q = qdf + ((size_t)(e0 + e) * kTriPts + q) * 3;
+                    const float2 dx = df_sub(pdf[0], Q[0]), dy = df_sub(pdf[1], Q[1]), dz = df_sub(pdf[2], Q[2]);
+                    const float2 r2 = df_add(df_add(df_sqr(dx), df_sqr(dy)), df_sqr(dz));
+                    const float2 inv = df_rsqrt(r2);
+                    const float2 i3 = df_mul(df_sqr(inv), inv);
+                    gx = df_mul(dx, i3).x;
+                    gy = df_mul(dy, i3).x;
+                    gz = df_mul(dz, i3).x;
                 } else {
                     const float dx = d0x - O[q * 3], dy = d0y - O[q * 3 + 1], dz = d0z - O[q * 3 + 2];
                     const float r2 = dx * dx + dy * dy + dz * dz;
@@ -823,12 +825,22 @@ __global__ void __launch_bounds__(128) k_field_batched_mixed(
                     gy = dy * i3;
                     gz = dz * i3;
                 }
+                const float4 *cq4 = (const float4 *)s_c[e * kTriPts + q];
 #pragma unroll
-                for (int ff = 0; ff < kBF; ff++) {
-                    const float cq = s_c[ff][e * kTriPts + q];
-                    acc[ff][0] += cq * gx;
-                    acc[ff][1] += cq * gy;
-                    acc[ff][2] += cq * gz;
+                for (int f4 = 0; f4 < kBF / 4; f4++) {
+                    const float4 cq = cq4[f4];
+                    acc[4 * f4][0] += cq.x * gx;
+                    acc[4 * f4][1] += cq.x * gy;
+                    acc[4 * f4][2] += cq.x * gz;
+                    acc[4 * f4 + 1][0] += cq.y * gx;
+                    acc[4 * f4 + 1][1] += cq.y * gy;
+                    acc[4 * f4 + 1][2] += cq.y * gz;
+                    acc[4 * f4 + 2][0] += cq.z * gx;
+                    acc[4 * f4 + 2][1] += cq.z * gy;
+                    acc[4 * f4 + 2][2] += cq.z * gz;
+                    acc[4 * f4 + 3][0] += cq.w * gx;
+                    acc[4 * f4 + 3][1] += cq.w * gy;
+                    acc[4 * f4 + 3][2] += cq.w * gz;
                 }
             }
         }
@@ -1010,6 +1022,7 @@ struct Session::Mixed {
     // FP32 far-field pass: element centroids / offsets, split points, weights
     bool far_ready = false;
     DevBuf<float> ecent, qoff, phl, cf32;
+    DevBuf<float2> qdf;  // quadrature points in double-FP32 (near pairs)
 };
 
 int Session::make_k32()
@@ -1331,7 +1344,9 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
                 DSC_TRY(w.ecent.alloc((size_t)E * 8));
                 DSC_TRY(w.qoff.alloc((size_t)E * kTriPts * 3));
                 DSC_TRY(w.phl.alloc((size_t)P * 6));
-                DSC_LAUNCH(k_prepare_far<<<(E + 127) / 128, 128, 0, st>>>(s.dev.qp.p, E, w.ecent.p, w.qoff.p));
+                DSC_TRY(w.qdf.alloc((size_t)E * kTriPts * 3));
+                DSC_LAUNCH(k_prepare_far<<<(E + 127) / 128, 128, 0, st>>>(s.dev.qp.p, E, w.ecent.p, w.qoff.p,
+                                                                          w.qdf.p));
                 DSC_LAUNCH(k_points_split<<<(P + 127) / 128, 128, 0, st>>>(fp.ps.px.p, fp.ps.py.p, fp.ps.pz.p,
                                                                            P, w.phl.p));
                 w.far_ready = true;
@@ -1341,11 +1356,11 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
             if (s.nen == 6)
                 DSC_LAUNCH(k_field_batched_mixed<6><<<fg, 128, 0, st>>>(w.phl.p, fp.ps.coinc.p, P, s.dev.elems.p, E,
                                                                         w.ecent.p, w.qoff.p, w.cf32.p,
-                                                                        s.dev.qp.p, F, w.part.p));
+                                                                        w.qdf.p, F, w.part.p));
             else
                 DSC_LAUNCH(k_field_batched_mixed<3><<<fg, 128, 0, st>>>(w.phl.p, fp.ps.coinc.p, P, s.dev.elems.p, E,
                                                                         w.ecent.p, w.qoff.p, w.cf32.p,
-                                                                        s.dev.qp.p, F, w.part.p));
+                                                                        w.qdf.p, F, w.part.p));
             const int sb = (P * 32 + 127) / 128;
             if (s.nen == 6)
                 DSC_LAUNCH(k_field_batched_singular<6><<<sb, 128, 0, st>>>(
