@@ -234,6 +234,24 @@ def cpu_baseline(sc, nthreads: int, sample_div: int = 8, full_first: bool = True
 
 
 # ------------------------------------------------------------------ ours
+def max_over_ranks(ms: float, world: int, device: str) -> float:
+    """The slowest rank's time (every rank gets it): replicas share no data,
+    so the job ends when the last replica does."""
+    if world <= 1:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    torch.distributed.barrier()
+    return float(t.item())
+
+
+def replica_throughput(ms: float, world: int, steps: int) -> float:
+    """Whole-job systems per second: every replica solves `steps` sweeps of
+    NFREQ systems in the slowest rank's `ms`."""
+    return world * steps * NFREQ / (ms / 1e3)
+
+
 def run_ours(args, rank, world):
     import torch
 
@@ -308,15 +326,10 @@ def run_ours(args, rank, world):
     torch.cuda.synchronize()
     launches = int(L.dsc_kernel_launches() - l0)
     clk = clocks.stop()
-    ms = ev0.elapsed_time(ev1)
-    tms = torch.tensor([ms], device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(tms, op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.barrier()
-    ms = float(tms.item())
+    ms = max_over_ranks(ev0.elapsed_time(ev1), world, "cuda")
     timing = s.timing()
     total_ms = sum(v[0] for v in timing.values())
-    value = world * args.steps * NFREQ / (ms / 1e3)
+    value = replica_throughput(ms, world, args.steps)
 
     # e2e through the C ABI from host arrays: dsc_sweep (session created,
     # mesh uploaded, assembled, solved, nodal solution and forces read back)
