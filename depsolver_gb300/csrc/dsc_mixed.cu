@@ -15,7 +15,6 @@
 #include <string.h>
 
 #include <algorithm>
-#include <complex>
 #include <vector>
 
 #include "../../include/depsolver_cuda.h"
@@ -30,8 +29,6 @@
 
 namespace dsc {
 
-typedef std::complex<double> cplx;
-
 constexpr int kMaxBatch = 64;   // frequencies per batch
 constexpr int kInnerMax = 80;   // Krylov dimension of one inner solve
 constexpr int kOuterMax = 6;    // refinement steps
@@ -40,62 +37,6 @@ constexpr int kOuterMax = 6;    // refinement steps
 // products per sweep (the slowest systems needed a third refinement step),
 // 3e-7 took 89, 1e-7 took 93.
 constexpr double kInnerTol = 3e-7;
-
-// ------------------------------------------------------------ GEMM (SIMT)
-// C (M x Nc) = A (M x Kd) * B (Kd x Nc), all column-major.  64 x 64 tile,
-// 256 threads with 4 x 4 outputs each, k-steps of 16.  TA = element of A,
-// TC = accumulation and C type.
-template <typename TA, typename TB, typename TC>
-__global__ void __launch_bounds__(256) k_gemm_cm(const TA *__restrict__ A, size_t lda,
-                                                 const TB *__restrict__ B, size_t ldb,
-                                                 TC *__restrict__ C, size_t ldc, int M, int Nc,
-                                                 int Kd)
-{
-    __shared__ TC As[16][64 + 1];
-    __shared__ TC Bs[16][64 + 1];
-    const int m0 = blockIdx.x * 64, n0 = blockIdx.y * 64;
-    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-    TC acc[4][4];
-#pragma unroll
-    for (int u = 0; u < 4; u++)
-#pragma unroll
-        for (int v = 0; v < 4; v++) acc[u][v] = 0;
-    for (int k0 = 0; k0 < Kd; k0 += 16) {
-        for (int t = threadIdx.x; t < 16 * 64; t += 256) {
-            int kk = t / 64, mm = t % 64;
-            int m = m0 + mm, k = k0 + kk;
-            As[kk][mm] = (m < M && k < Kd) ? (TC)A[(size_t)k * lda + m] : (TC)0;
-            int nn = t / 16, kb = t % 16;
-            int n = n0 + nn, k2 = k0 + kb;
-            Bs[kb][nn] = (n < Nc && k2 < Kd) ? (TC)B[(size_t)n * ldb + k2] : (TC)0;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int kk = 0; kk < 16; kk++) {
-            TC a[4], b[4];
-#pragma unroll
-            for (int u = 0; u < 4; u++) {
-                a[u] = As[kk][ty + 16 * u];
-                b[u] = Bs[kk][tx + 16 * u];
-            }
-#pragma unroll
-            for (int u = 0; u < 4; u++)
-#pragma unroll
-                for (int v = 0; v < 4; v++) acc[u][v] += a[u] * b[v];
-        }
-        __syncthreads();
-    }
-#pragma unroll
-    for (int u = 0; u < 4; u++) {
-        int m = m0 + ty + 16 * u;
-        if (m >= M) continue;
-#pragma unroll
-        for (int v = 0; v < 4; v++) {
-            int n = n0 + tx + 16 * v;
-            if (n < Nc) C[(size_t)n * ldc + m] = acc[u][v];
-        }
-    }
-}
 
 // C (M x Nc, FP64) = fl32(A) (M x Kd) * B (Kd x Nc), column-major: A is FP64
 // and rounded to FP32 as it is staged (one conversion per element on the
@@ -181,38 +122,6 @@ __global__ void k_split_f32_pair(const double *__restrict__ x, float *__restrict
         h[t] = a;
         l[t] = (float)(v - (double)a);
     }
-}
-
-__global__ void k_to_float(const double *__restrict__ x, float *__restrict__ y, size_t n)
-{
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n;
-         t += (size_t)gridDim.x * blockDim.x)
-        y[t] = (float)x[t];
-}
-
-// K32 = (float) K64, leading dimension kept.
-__global__ void k_k_to_float(const double *__restrict__ K, float *__restrict__ K32, size_t n)
-{
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n;
-         t += (size_t)gridDim.x * blockDim.x)
-        K32[t] = (float)K[t];
-}
-
-// Vectors of the batch: column 2f = Re, 2f + 1 = Im of system f, stride ld.
-// w_f = cs_f o Y_f + cd_f o v_f (complex), Y from the K product.
-template <typename TY>
-__global__ void k_apply_epilogue(const TY *__restrict__ Y, const double *__restrict__ V,
-                                 const double2 *__restrict__ cs, const double2 *__restrict__ cd,
-                                 double *__restrict__ W, int N, size_t ld, int F)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int f = blockIdx.y;
-    if (i >= N || f >= F) return;
-    const double yr = (double)Y[(size_t)(2 * f) * ld + i], yi = (double)Y[(size_t)(2 * f + 1) * ld + i];
-    const double vr = V[(size_t)(2 * f) * ld + i], vi = V[(size_t)(2 * f + 1) * ld + i];
-    const double2 s = cs[(size_t)f * N + i], d = cd[(size_t)f * N + i];
-    W[(size_t)(2 * f) * ld + i] = s.x * yr - s.y * yi + d.x * vr - d.y * vi;
-    W[(size_t)(2 * f + 1) * ld + i] = s.x * yi + s.y * yr + d.x * vi + d.y * vr;
 }
 
 // r_f = bt_f - (cs_f o Y_f + cd_f o x_f)
@@ -1119,16 +1028,6 @@ __global__ void k_prepare_systems(const int *__restrict__ iface_row, const doubl
     cd32[o] = make_float2((float)c2.x, (float)c2.y);
     R[(size_t)(2 * f) * ld + i] = r.x;
     R[(size_t)(2 * f + 1) * ld + i] = r.y;
-}
-
-template <typename TA, typename TB, typename TC>
-static int gemm(const TA *A, size_t lda, const TB *B, size_t ldb, TC *C, size_t ldc, int M, int Nc,
-                int Kd, cudaStream_t st)
-{
-    dim3 g((M + 63) / 64, (Nc + 63) / 64);
-    DSC_LAUNCH(k_gemm_cm<TA, TB, TC><<<g, 256, 0, st>>>(A, lda, B, ldb, C, ldc, M, Nc, Kd));
-    DSC_CUDA(cudaGetLastError());
-    return kOk;
 }
 
 // One batch of F <= kMaxBatch frequencies.
