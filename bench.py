@@ -49,10 +49,10 @@ def peaks():
 # ------------------------------------------------------------------ roofline
 # Per kernel class: the bound, the unit, the scale from the library's work
 # count to that unit, the peak and where the peak comes from.  The tensor-core
-# product runs tf32, which issues at half the bf16 rate on this GPU; FP64 and
-# FP32-pipe classes are listed against nominal pipe rates, marked as such.
-FP64_NOMINAL_TFLOPS = 1.25   # GB300 FP64, nominal (not in the measured peaks)
-ASM_FLOPS_PER_PAIR = 7 * 27  # 7 quadrature points x ~27 FP64 flops
+# product runs tf32, which issues at half the bf16 rate on this GPU.  The
+# mixed mode's regular-pair assembly runs double-FP32 on the FP32 pipes: it
+# is reported as (row, element) pairs per second with no single-number peak
+# (its FP32-pipe utilisation is in profiles/asm_regular_mid.md).
 
 
 def roofline(timing, N, E):
@@ -67,8 +67,8 @@ def roofline(timing, N, E):
                    f"{src} bf16_tflops / 2 (tf32 rate), of measured"),
         "gram_schmidt": ("hbm", "GB/s", 1e-9, hbm, f"{src} hbm_gbs, of measured"),
         "gemv_K64": ("hbm", "GB/s", 1e-9, hbm, f"{src} hbm_gbs, of measured"),
-        "asm_regular": ("fp64", "TFLOP/s", ASM_FLOPS_PER_PAIR * 1e-12, FP64_NOMINAL_TFLOPS,
-                        "nominal FP64 rate (not measured)"),
+        "asm_regular": ("fp32-pipe", "Gpairs/s", 1e-9, None,
+                        "no single-number peak: double-FP32 on the FP32 pipes"),
     }
     out = {}
     for k, (bound, unit, scale, peak, psrc) in models.items():
@@ -76,7 +76,8 @@ def roofline(timing, N, E):
         if cnt and ms > 0 and wk > 0:
             ach = wk * scale / (ms / 1e3)
             out[k] = {"kernel": k, "bound": bound, "achieved": ach, "peak": peak, "unit": unit,
-                      "frac": ach / peak, "traffic": TRAFFIC.get(k), "peak_source": psrc,
+                      "frac": ach / peak if peak else None, "traffic": TRAFFIC.get(k),
+                      "peak_source": psrc,
                       "ms": ms, "scopes": cnt}
     main = [k for k in out if out[k]["bound"] in ("hbm", "tensor")]
     dom = max(main, key=lambda k: out[k]["ms"]) if main else None

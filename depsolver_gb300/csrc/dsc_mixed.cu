@@ -281,196 +281,199 @@ __global__ void k_residual_update(const float *__restrict__ P, int S, size_t spl
     R[(size_t)(2 * f + 1) * ld + i] -= s.x * yi + s.y * yr + d.x * di + d.y * dr;
 }
 
-// One pass over the basis: block (row chunk, f) stages its chunk of W_f in
-// shared memory, each warp forms the chunk's dots <V_k,f, W_f> = sum conj(v) w
-// for k = warp, warp + 8, ... in double-FP32; k_cgs_dots_reduce adds the
-// chunks in order (FP64).
-constexpr int kDotRows = 1024;
+// Gram-Schmidt over the basis in two launches per pass, both without block
+// barriers: every warp works alone on units taken in a grid-stride loop
+// over the warps of one resident wave.
+//
+// Dots: unit (row chunk of kDotRows rows, system f, vector k); the warp
+// forms the chunk's <V_k,f, W_f> = sum conj(v) w in double-FP32 (two rows
+// per lane and step, kDotBatch steps' loads issued together) and lane 0
+// writes the double-FP32 pair; k_cgs_dots_reduce adds the chunks in order
+// (FP64).  k runs fastest over the units, so the warps of a block share
+// their W chunk through the caches.
+constexpr int kDotRows = 512;
+constexpr int kDotBatch = 4;
+static_assert(kDotRows % (64 * kDotBatch) == 0, "a chunk is whole batches of 64-row steps");
 
-__global__ void __launch_bounds__(256) k_cgs_dots_chunk(const float2 *__restrict__ Vb, size_t vstride,
-                                                        const float2 *__restrict__ W, int N, size_t ld,
-                                                        int F, int nk, const int *__restrict__ active,
-                                                        double2 *__restrict__ part,
-                                                        unsigned long long *__restrict__ bytes)
+__global__ void __launch_bounds__(256) k_cgs_dots(const float2 *__restrict__ Vb, size_t vstride,
+                                                  const float2 *__restrict__ W, int N, size_t ld, int F,
+                                                  int nk, const int *__restrict__ active,
+                                                  float4 *__restrict__ part,
+                                                  unsigned long long *__restrict__ bytes)
 {
-    __shared__ __align__(16) float2 swr[kDotRows], swi[kDotRows];
-    // items (row chunk, system f), grid-stride so that one resident wave of
-    // blocks covers them all
+    const int lane = threadIdx.x & 31;
+    const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int nw = (int)((gridDim.x * blockDim.x) >> 5);
     const int nchunk = (N + kDotRows - 1) / kDotRows;
-    for (int item = blockIdx.x; item < nchunk * F; item += gridDim.x) {
-    const int chunk = item % nchunk, f = item / nchunk;
-    if (!active[f]) continue;  // uniform over the block
-    const int r0 = chunk * kDotRows, nr = min(kDotRows, N - r0);
-    if (bytes && threadIdx.x == 0) atomicAdd(bytes, (unsigned long long)nr * 16u * (nk + 1));
-    const float2 *wr = W + (size_t)(2 * f) * ld + r0, *wi = wr + ld;
-    for (int t = threadIdx.x; t < nr; t += blockDim.x) {
-        swr[t] = wr[t];
-        swi[t] = wi[t];
-    }
-    __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int np = nr & ~1;
-    for (int k = warp; k < nk; k += (int)(blockDim.x >> 5)) {
+    const int units = nchunk * F * nk;
+    for (int un = gw; un < units; un += nw) {
+        const int k = un % nk, cf = un / nk, chunk = cf % nchunk, f = cf / nchunk;
+        if (!active[f]) continue;  // uniform over the warp
+        const int r0 = chunk * kDotRows, nr = min(kDotRows, N - r0);
+        // rows up to the even count np2 <= ld exist in V and W (ld is a
+        // multiple of 32); the padding row N of both holds zero
+        const int np2 = (nr + 1) & ~1;
+        if (bytes && lane == 0) atomicAdd(bytes, (unsigned long long)nr * 16u * (k == 0 ? 2 : 1));
         const float2 *vr = Vb + (size_t)k * vstride + (size_t)(2 * f) * ld + r0, *vi = vr + ld;
+        const float2 *wr = W + (size_t)(2 * f) * ld + r0, *wi = wr + ld;
         float2 sr = make_float2(0.f, 0.f), si = make_float2(0.f, 0.f);
         // two rows per lane and step (16-byte loads: r0 and ld are even)
-        for (int t = 2 * lane; t < np; t += 64) {
-            const float4 a = *(const float4 *)(vr + t), b = *(const float4 *)(vi + t);
-            const float4 c = *(const float4 *)(swr + t), d = *(const float4 *)(swi + t);
-            const float2 a0 = make_float2(a.x, a.y), a1 = make_float2(a.z, a.w);
-            const float2 b0 = make_float2(b.x, b.y), b1 = make_float2(b.z, b.w);
-            const float2 c0 = make_float2(c.x, c.y), c1 = make_float2(c.z, c.w);
-            const float2 d0 = make_float2(d.x, d.y), d1 = make_float2(d.z, d.w);
-            df_mac(sr, a0, c0);
-            df_mac(sr, b0, d0);
-            df_mac(si, a0, d0);
-            df_mac(si, df_neg(b0), c0);
-            df_mac(sr, a1, c1);
-            df_mac(sr, b1, d1);
-            df_mac(si, a1, d1);
-            df_mac(si, df_neg(b1), c1);
-        }
-        if (lane == 0 && np < nr) {
-            const float2 a0 = vr[np], b0 = vi[np], c0 = swr[np], d0 = swi[np];
-            df_mac(sr, a0, c0);
-            df_mac(sr, b0, d0);
-            df_mac(si, a0, d0);
-            df_mac(si, df_neg(b0), c0);
+        for (int t0 = 2 * lane; t0 < np2; t0 += 64 * kDotBatch) {
+            float4 a[kDotBatch], b[kDotBatch], c[kDotBatch], d[kDotBatch];
+#pragma unroll
+            for (int u = 0; u < kDotBatch; u++) {
+                const int t = t0 + 64 * u < np2 ? t0 + 64 * u : 0;  // past the chunk: row 0, unused
+                a[u] = __ldcs((const float4 *)(vr + t));
+                b[u] = __ldcs((const float4 *)(vi + t));
+                c[u] = __ldg((const float4 *)(wr + t));
+                d[u] = __ldg((const float4 *)(wi + t));
+            }
+#pragma unroll
+            for (int u = 0; u < kDotBatch; u++) {
+                if (t0 + 64 * u >= np2) break;
+                const float2 a0 = make_float2(a[u].x, a[u].y), a1 = make_float2(a[u].z, a[u].w);
+                const float2 b0 = make_float2(b[u].x, b[u].y), b1 = make_float2(b[u].z, b[u].w);
+                const float2 c0 = make_float2(c[u].x, c[u].y), c1 = make_float2(c[u].z, c[u].w);
+                const float2 d0 = make_float2(d[u].x, d[u].y), d1 = make_float2(d[u].z, d[u].w);
+                df_mac(sr, a0, c0);
+                df_mac(sr, b0, d0);
+                df_mac(si, a0, d0);
+                df_mac(si, df_neg(b0), c0);
+                df_mac(sr, a1, c1);
+                df_mac(sr, b1, d1);
+                df_mac(si, a1, d1);
+                df_mac(si, df_neg(b1), c1);
+            }
         }
         sr = df_warp_sum(sr);
         si = df_warp_sum(si);
-        if (lane == 0) part[((size_t)chunk * nk + k) * F + f] = make_double2(df_to(sr), df_to(si));
-    }
-    __syncthreads();  // swr, swi are rewritten by the next item
+        if (lane == 0) part[((size_t)chunk * nk + k) * F + f] = make_float4(sr.x, sr.y, si.x, si.y);
     }
 }
 
-__global__ void k_cgs_dots_reduce(const double2 *__restrict__ part, int nchunk, int nk, int F,
-                                  const int *__restrict__ active, double2 *__restrict__ h)
+// h[k][f] = the sum of the chunk partials, hacc[k][f] += h[k][f] (the
+// Hessenberg column sums the passes' coefficients), hdf[k][f] = the
+// update's coefficients (-Re h, Im h) in double-FP32.  One warp per (k, f):
+// lane-strided double-FP32 sums over the chunks, then a fixed shuffle tree
+// (FP32 pipes; FP64 only for the warp's final h).
+__global__ void k_cgs_dots_reduce(const float4 *__restrict__ part, int nchunk, int nk, int F,
+                                  const int *__restrict__ active, double2 *__restrict__ h,
+                                  double2 *__restrict__ hacc, float4 *__restrict__ hdf)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nk * F) return;
+    const int t = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (t >= nk * F) return;  // uniform over the warp
     const int f = t % F;
     if (!active[f]) return;
-    double sr = 0.0, si = 0.0;
-    for (int c = 0; c < nchunk; c++) {
-        const double2 v = part[(size_t)c * nk * F + t];
-        sr += v.x;
-        si += v.y;
+    float2 sr = make_float2(0.f, 0.f), si = make_float2(0.f, 0.f);
+    for (int c = lane; c < nchunk; c += 32) {
+        const float4 v = part[(size_t)c * nk * F + t];  // double-FP32 (re, im) of chunk c
+        sr = df_add(sr, make_float2(v.x, v.y));
+        si = df_add(si, make_float2(v.z, v.w));
     }
-    h[t] = make_double2(sr, si);
+    sr = df_norm(df_warp_sum(sr));
+    si = df_norm(df_warp_sum(si));
+    if (lane == 0) {
+        const double hr = df_to(sr), hi = df_to(si);
+        h[t] = make_double2(hr, hi);
+        const double2 a = hacc[t];
+        hacc[t] = make_double2(a.x + hr, a.y + hi);
+        hdf[t] = make_float4(-sr.x, -sr.y, si.x, si.y);
+    }
 }
 
-// W_f -= sum_k h[k][f] V_k,f in double-FP32 (and hacc += h).  Two rows per
-// thread; -h as double-FP32 pairs staged in shared memory per block.
+// Update: unit (block of 64 rows, system f); each lane takes two rows and
+// W_f -= sum_k h[k][f] V_k,f in double-FP32 with the coefficients of
+// k_cgs_dots_reduce, then lane 0 writes the unit's share of |w_f|^2 to
+// npart[f][unit] (nb = ceil(N / 64) per system).
+constexpr int kUpdRows = 64;
+
 __global__ void __launch_bounds__(256) k_cgs_update(const float2 *__restrict__ Vb, size_t vstride,
                                                     float2 *__restrict__ W, int N, size_t ld, int F,
                                                     int nk, const int *__restrict__ active,
-                                                    const double2 *__restrict__ h,
-                                                    double2 *__restrict__ hacc,
+                                                    const float4 *__restrict__ hdf,
                                                     double *__restrict__ npart,
                                                     unsigned long long *__restrict__ bytes)
 {
-    __shared__ float2 cr[kInnerMax + 1], ci[kInnerMax + 1], cin[kInnerMax + 1], sh[8];
-    // items (row block rb of 2 blockDim.x rows, system f), grid-stride so
-    // that one resident wave of blocks covers them all
-    const int nrb = (N + 2 * (int)blockDim.x - 1) / (2 * (int)blockDim.x);
-    for (int item = blockIdx.x; item < nrb * F; item += gridDim.x) {
-        const int rb = item % nrb, f = item / nrb;
-        if (!active[f]) continue;  // uniform over the block
-        if (bytes && threadIdx.x == 0) {
-            const int rows = min(2 * (int)blockDim.x, N - 2 * rb * (int)blockDim.x);
-            atomicAdd(bytes, (unsigned long long)rows * 16u * (nk + 2));
-        }
-        for (int k = threadIdx.x; k < nk; k += blockDim.x) {
-            const double2 c = h[(size_t)k * F + f];
-            cr[k] = df_from(-c.x);
-            ci[k] = df_from(c.y);
-            cin[k] = df_from(-c.y);
-        }
-        __syncthreads();
-        const int i = 2 * (rb * (int)blockDim.x + (int)threadIdx.x);
+    const int lane = threadIdx.x & 31;
+    const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int nw = (int)((gridDim.x * blockDim.x) >> 5);
+    const int nrb = (N + kUpdRows - 1) / kUpdRows;
+    for (int un = gw; un < nrb * F; un += nw) {
+        const int rb = un % nrb, f = un / nrb;
+        if (!active[f]) continue;  // uniform over the warp
+        if (bytes && lane == 0)
+            atomicAdd(bytes, (unsigned long long)min(kUpdRows, N - rb * kUpdRows) * 16u * (nk + 2));
+        // rows i and i + 1 (row N, when i + 1 == N, is a padding row: it is
+        // read, updated and not stored)
+        const int i = rb * kUpdRows + 2 * lane;
         float2 n2 = make_float2(0.f, 0.f);
         if (i < N) {
             float2 *wrp = W + (size_t)(2 * f) * ld + i, *wip = wrp + ld;
             const float2 *vr = Vb + (size_t)(2 * f) * ld + i, *vi = vr + ld;
+            const float4 a = *(const float4 *)wrp, b = *(const float4 *)wip;
+            float2 wr0 = make_float2(a.x, a.y), wr1 = make_float2(a.z, a.w);
+            float2 wi0 = make_float2(b.x, b.y), wi1 = make_float2(b.z, b.w);
+#pragma unroll 4
+            for (int k = 0; k < nk; k++) {
+                const float4 p = __ldcs((const float4 *)(vr + (size_t)k * vstride));
+                const float4 q = __ldcs((const float4 *)(vi + (size_t)k * vstride));
+                const float4 c = __ldg(hdf + (size_t)k * F + f);
+                const float2 p0 = make_float2(p.x, p.y), p1 = make_float2(p.z, p.w);
+                const float2 q0 = make_float2(q.x, q.y), q1 = make_float2(q.z, q.w);
+                const float2 a_r = make_float2(c.x, c.y), a_i = make_float2(c.z, c.w), a_in = df_neg(a_i);
+                df_mac(wr0, a_r, p0);   // wr -= hr vr - hi vi
+                df_mac(wr0, a_i, q0);
+                df_mac(wi0, a_r, q0);   // wi -= hr vi + hi vr
+                df_mac(wi0, a_in, p0);
+                df_mac(wr1, a_r, p1);
+                df_mac(wr1, a_i, q1);
+                df_mac(wi1, a_r, q1);
+                df_mac(wi1, a_in, p1);
+            }
+            wr0 = df_norm(wr0);
+            wi0 = df_norm(wi0);
+            df_mac(n2, wr0, wr0);
+            df_mac(n2, wi0, wi0);
             if (i + 1 < N) {
-                const float4 a = *(const float4 *)wrp, b = *(const float4 *)wip;
-                float2 wr0 = make_float2(a.x, a.y), wr1 = make_float2(a.z, a.w);
-                float2 wi0 = make_float2(b.x, b.y), wi1 = make_float2(b.z, b.w);
-#pragma unroll 2
-                for (int k = 0; k < nk; k++) {
-                    const float4 p = *(const float4 *)(vr + (size_t)k * vstride);
-                    const float4 q = *(const float4 *)(vi + (size_t)k * vstride);
-                    const float2 p0 = make_float2(p.x, p.y), p1 = make_float2(p.z, p.w);
-                    const float2 q0 = make_float2(q.x, q.y), q1 = make_float2(q.z, q.w);
-                    const float2 a_r = cr[k], a_i = ci[k], a_in = cin[k];
-                    df_mac(wr0, a_r, p0);   // wr -= hr vr - hi vi
-                    df_mac(wr0, a_i, q0);
-                    df_mac(wi0, a_r, q0);   // wi -= hr vi + hi vr
-                    df_mac(wi0, a_in, p0);
-                    df_mac(wr1, a_r, p1);
-                    df_mac(wr1, a_i, q1);
-                    df_mac(wi1, a_r, q1);
-                    df_mac(wi1, a_in, p1);
-                }
-                wr0 = df_norm(wr0);
                 wr1 = df_norm(wr1);
-                wi0 = df_norm(wi0);
                 wi1 = df_norm(wi1);
                 *(float4 *)wrp = make_float4(wr0.x, wr0.y, wr1.x, wr1.y);
                 *(float4 *)wip = make_float4(wi0.x, wi0.y, wi1.x, wi1.y);
-                df_mac(n2, wr0, wr0);
-                df_mac(n2, wi0, wi0);
                 df_mac(n2, wr1, wr1);
                 df_mac(n2, wi1, wi1);
             } else {
-                float2 wr0 = *wrp, wi0 = *wip;
-                for (int k = 0; k < nk; k++) {
-                    const float2 p0 = vr[(size_t)k * vstride], q0 = vi[(size_t)k * vstride];
-                    df_mac(wr0, cr[k], p0);
-                    df_mac(wr0, ci[k], q0);
-                    df_mac(wi0, cr[k], q0);
-                    df_mac(wi0, cin[k], p0);
-                }
-                wr0 = df_norm(wr0);
-                wi0 = df_norm(wi0);
                 *wrp = wr0;
                 *wip = wi0;
-                df_mac(n2, wr0, wr0);
-                df_mac(n2, wi0, wi0);
             }
         }
-        const double t = df_block_sum(n2, sh);
-        if (threadIdx.x == 0) npart[(size_t)f * nrb + rb] = t;
-        if (hacc && rb == 0 && threadIdx.x == 0)
-            for (int k = 0; k < nk; k++) {
-                double2 a = hacc[(size_t)k * F + f], c = h[(size_t)k * F + f];
-                hacc[(size_t)k * F + f] = make_double2(a.x + c.x, a.y + c.y);
-            }
-        __syncthreads();  // cr, ci, cin and sh are rewritten by the next item
+        n2 = df_warp_sum(n2);
+        if (lane == 0) npart[(size_t)f * nrb + rb] = df_to(n2);
     }
 }
 
-// nrm[f] = sqrt(sum of the nb block partials of |w_f|^2), in block order,
-// for the systems in mask.  With n0 (not null): also act2[f], whether the
-// system needs the second Gram-Schmidt pass, by the DGKS test (its vector
-// lost more than 1 - 1/sqrt(2) of its norm n0[f] in the first pass).
+// nrm[f] = sqrt(sum of the nb block partials of |w_f|^2) for the systems
+// in mask, one warp per system (lane-strided sums, then a fixed shuffle
+// tree).  With n0 (not null): also act2[f], whether the system needs the
+// second Gram-Schmidt pass, by the DGKS test (its vector lost more than
+// 1 - 1/sqrt(2) of its norm n0[f] in the first pass).
 __global__ void k_norm_finish(const double *__restrict__ npart, int nb, int F,
                               const int *__restrict__ mask, double *__restrict__ nrm,
                               const double *__restrict__ n0, int *__restrict__ act2)
 {
-    const int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= F) return;
+    const int f = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (f >= F) return;  // uniform over the warp
     if (!mask[f]) {
-        if (n0) act2[f] = 0;
+        if (n0 && lane == 0) act2[f] = 0;
         return;
     }
     double t = 0.0;
-    for (int b = 0; b < nb; b++) t += npart[(size_t)f * nb + b];
-    const double n = sqrt(t);
-    nrm[f] = n;
-    if (n0) act2[f] = n < 0.7071067811865476 * n0[f];
+    for (int b = lane; b < nb; b += 32) t += npart[(size_t)f * nb + b];
+    t = warp_sum(t);
+    if (lane == 0) {
+        const double n = sqrt(t);
+        nrm[f] = n;
+        if (n0) act2[f] = n < 0.7071067811865476 * n0[f];
+    }
 }
 
 // nrm[f] = |R_f| for FP64 vectors (one block per system)
@@ -486,21 +489,20 @@ __global__ void __launch_bounds__(256) k_norms(const double *__restrict__ W, int
     if (threadIdx.x == 0) nrm[f] = sqrt(t);
 }
 
-// The GEMM operand of a Krylov vector: the tf32 pair of hi + lo.
-__device__ __forceinline__ void tf32_pair(float2 v, float &th, float &tl)
+// The GEMM operand of a Krylov vector v = hi + lo (|v| <= 1: a unit
+// vector): the fp16 pair of 2^14 v (the product's column factor is 2^-14).
+constexpr float kVScale = 16384.0f;
+__device__ __forceinline__ void f16_pair(float2 v, __half &h, __half &l)
 {
-    uint32_t u;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(u) : "f"(v.x));
-    th = __uint_as_float(u);
-    tl = __fadd_rn(__fsub_rn(v.x, th), v.y);
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(u) : "f"(tl));  // the tensor core would truncate it
-    tl = __uint_as_float(u);
+    const float x = v.x * kVScale;  // exact
+    h = __float2half_rn(x);
+    l = __float2half_rn(__fadd_rn(__fsub_rn(x, __half2float(h)), v.y * kVScale));
 }
 
-// V_f = R_f * scale[f] (R in FP64) as double-FP32, and its tf32 pair for the
-// next tensor-core product (Bh, Bl: same layout, FP32).
+// V_f = R_f * scale[f] (R in FP64) as double-FP32, and its fp16 pair for the
+// next tensor-core product (Bh, Bl: same layout).
 __global__ void k_scale_from64(const double *__restrict__ R, float2 *__restrict__ V,
-                               float *__restrict__ Bh, float *__restrict__ Bl, int N, size_t ld,
+                               __half *__restrict__ Bh, __half *__restrict__ Bl, int N, size_t ld,
                                int F, const double *__restrict__ scale,
                                const int *__restrict__ active)
 {
@@ -512,17 +514,17 @@ __global__ void k_scale_from64(const double *__restrict__ R, float2 *__restrict_
     for (int c = 0; c < 2; c++) {
         const size_t o = (size_t)(2 * f + c) * ld + i;
         const float2 v = df_from(R[o] * s);
-        float th, tl;
-        tf32_pair(v, th, tl);
+        __half th, tl;
+        f16_pair(v, th, tl);
         V[o] = v;
         Bh[o] = th;
         Bl[o] = tl;
     }
 }
 
-// V_f = W_f * scale[f] (double-FP32), and its tf32 pair.
+// V_f = W_f * scale[f] (double-FP32), and its fp16 pair.
 __global__ void k_scale_df(const float2 *__restrict__ W, float2 *__restrict__ V,
-                           float *__restrict__ Bh, float *__restrict__ Bl, int N, size_t ld, int F,
+                           __half *__restrict__ Bh, __half *__restrict__ Bl, int N, size_t ld, int F,
                            const double *__restrict__ scale, const int *__restrict__ active)
 {
     __shared__ float2 s;
@@ -535,8 +537,8 @@ __global__ void k_scale_df(const float2 *__restrict__ W, float2 *__restrict__ V,
     for (int c = 0; c < 2; c++) {
         const size_t o = (size_t)(2 * f + c) * ld + i;
         const float2 v = df_mul(W[o], s);
-        float th, tl;
-        tf32_pair(v, th, tl);
+        __half th, tl;
+        f16_pair(v, th, tl);
         V[o] = v;
         Bh[o] = th;
         Bl[o] = tl;
@@ -914,11 +916,15 @@ struct Session::Mixed {
     DevBuf<float2> cs32, cd32;  // FP32 copies of the coefficients
     DevBuf<double> Ak, Bk;      // interface coefficients of the batch (F x nIf)
     DevBuf<float> Xh, Xl;       // FP32 pair of the solution (FP64-accurate residual)
-    DevBuf<float> Vh, Vl;   // tf32 pair of the current Krylov block
+    DevBuf<__half> Vh, Vl;  // scaled fp16 pair of the current GEMM operand block
+    DevBuf<float> cscK;     // column factors of the Krylov blocks' pairs (2^-14)
+    DevBuf<float> cscX;     // column factors of the other operands' pairs
     DevBuf<float> Yp;       // split-K partial products, S blocks
     DevBuf<int> err;        // set by the tensor-core kernel when a wait gives up
     DevBuf<double> Xs, R, Y64, D;
-    DevBuf<double2> cs, cd, bt, h, hacc, ycoef, dpart;
+    DevBuf<double2> cs, cd, bt, h, hacc, ycoef;
+    DevBuf<float4> dpart;   // Gram-Schmidt dot partials per row chunk (double-FP32 re, im)
+    DevBuf<float4> hdf;     // the update's coefficients (-Re h, Im h) in double-FP32
     DevBuf<double> nrm, nrm0, scale, betad, itold, gc;
     DevBuf<double2> gH, gsn, gg;  // Givens state per system
     DevBuf<int> active, act0, act2, mcount;
@@ -934,14 +940,22 @@ struct Session::Mixed {
     DevBuf<float2> qdf;  // quadrature points in double-FP32 (near pairs)
 };
 
-int Session::make_k32()
+int Session::make_k16()
 {
-    if (k32_ready && k64_ready) return kOk;
+    if (k16_ready && k64_ready) return kOk;
     DSC_TRY(assemble64(false));
-    DSC_TRY(Kt32.alloc(ld * N));
-    DSC_TRY(dKt32.alloc(ld * N));
-    DSC_TRY(split_transpose_K(K64.p, ld, N, Kt32.p, dKt32.p, ld, st, kTransposeBiasedRem));
-    k32_ready = true;
+    TimerScope ts(&timer, kTConvertK, st);
+    DSC_TRY(Kh16.alloc(ld * N));
+    DSC_TRY(Kl16.alloc(ld * N));
+    DSC_TRY(dKh16.alloc(ld * N));
+    DSC_TRY(dKl16.alloc(ld * N));
+    DSC_TRY(rowE.alloc(N));
+    DSC_TRY(rsK.alloc(N));
+    DSC_TRY(rsdK.alloc(N));
+    DSC_TRY(k16_row_scales(K64.p, ld, N, rowE.p, rsK.p, rsdK.p, st));
+    DSC_TRY(split_transpose_K16(K64.p, ld, N, rowE.p, Kh16.p, Kl16.p, dKh16.p, dKl16.p, ld, st));
+    timer.add_work(kTConvertK, 16.0 * N * N);  // bytes: K read (8), four fp16 copies written (8)
+    k16_ready = true;
     return kOk;
 }
 
@@ -954,11 +968,23 @@ __device__ __forceinline__ float2 epilogue_row_impl(const float *__restrict__ P,
 {
     const float *pr = P + (size_t)(2 * f) * ld + i, *pi = pr + ld;
     float2 yr = make_float2(0.f, 0.f), yi = make_float2(0.f, 0.f);
-    for (int s = 0; s < S; s++) {
-        const float2 a = df_two_sum(yr.x, pr[(size_t)s * split_stride]);
-        const float2 b = df_two_sum(yi.x, pi[(size_t)s * split_stride]);
-        yr = make_float2(a.x, yr.y + a.y);
-        yi = make_float2(b.x, yi.y + b.y);
+    // the partials' loads four splits at a time, ahead of the additions
+    for (int s0 = 0; s0 < S; s0 += 4) {
+        float u[4], v[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const size_t o = (size_t)min(s0 + q, S - 1) * split_stride;
+            u[q] = pr[o];
+            v[q] = pi[o];
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            if (s0 + q >= S) break;
+            const float2 a = df_two_sum(yr.x, u[q]);
+            const float2 b = df_two_sum(yi.x, v[q]);
+            yr = make_float2(a.x, yr.y + a.y);
+            yi = make_float2(b.x, yi.y + b.y);
+        }
     }
     const float ar = yr.x + yr.y, ai = yi.x + yi.y;
     const float vr = V[(size_t)(2 * f) * ld + i].x, vi = V[(size_t)(2 * f + 1) * ld + i].x;
@@ -1106,8 +1132,8 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
             {
                 // the tf32 pair of v_j was written with v_j
                 TimerScope ts(tm, kTGemmK, st);
-                DSC_TRY(tc_gemm_3xtf32(s.Kt32.p, nullptr, ld, w.Vh.p, w.Vl.p, ld, N, 2 * F, N, w.Yp.p, ld,
-                                       w.S, w.err.p, st, true));
+                DSC_TRY(tc_gemm_3xf16(s.Kh16.p, s.Kl16.p, ld, w.Vh.p, w.Vl.p, ld, N, 2 * F, N, w.Yp.p, ld,
+                                      w.S, w.err.p, st, s.rsK.p, w.cscK.p));
                 tm->add_work(kTGemmK, 6.0 * N * N * 2 * F);  // three tf32 products
             }
             {
@@ -1116,8 +1142,8 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
                                                                        w.cs32.p, w.cd32.p, w.W.p, N, ld, F,
                                                                        w.npart.p));
                 DSC_CUDA(cudaMemsetAsync(w.hacc.p, 0, (size_t)(j + 1) * F * sizeof(double2), st));
-                DSC_LAUNCH(k_norm_finish<<<gb, 64, 0, st>>>(w.npart.p, (int)vg.x, F, w.active.p, w.nrm0.p, nullptr,
-                                                            nullptr));
+                DSC_LAUNCH(k_norm_finish<<<(F * 32 + 255) / 256, 256, 0, st>>>(w.npart.p, (int)vg.x, F, w.active.p,
+                                                                                w.nrm0.p, nullptr, nullptr));
             }
             // classical Gram-Schmidt; the second pass only for the systems
             // whose vector lost more than 1 - 1/sqrt(2) of its norm in the
@@ -1125,26 +1151,27 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
             // come from block partials written by the epilogue and update
             // kernels.
             unsigned long long *cgsb = tm->on ? w.cgsb.p : nullptr;
-            const dim3 vg2(((N + 1) / 2 + 255) / 256, F);
+            const int nrb = (N + kUpdRows - 1) / kUpdRows, wb = (F * 32 + 255) / 256;
             for (int pass = 0; pass < 2; pass++) {
                 TimerScope tc(tm, kTCgs, st);
                 const int *mask = pass == 0 ? w.active.p : w.act2.p;
                 const int nchunk = (N + kDotRows - 1) / kDotRows;
-                DSC_LAUNCH(k_cgs_dots_chunk<<<std::min(nchunk * F, w.dots_grid), 256, 0, st>>>(w.Vb.p, blk, w.W.p, N,
-                                                                                               ld, F, j + 1,
-                                                                            mask, w.dpart.p, cgsb));
-                DSC_LAUNCH(k_cgs_dots_reduce<<<((j + 1) * F + 255) / 256, 256, 0, st>>>(w.dpart.p, nchunk, j + 1, F,
-                                                                                       mask, w.h.p));
-                DSC_LAUNCH(k_cgs_update<<<std::min((int)(vg2.x * vg2.y), w.upd_grid), 256, 0, st>>>(
-                    w.Vb.p, blk, w.W.p, N, ld, F, j + 1, mask, w.h.p, w.hacc.p, w.npart.p, cgsb));
+                const int dunits = nchunk * F * (j + 1), uunits = nrb * F;
+                DSC_LAUNCH(k_cgs_dots<<<std::min((dunits + 7) / 8, w.dots_grid), 256, 0, st>>>(
+                    w.Vb.p, blk, w.W.p, N, ld, F, j + 1, mask, w.dpart.p, cgsb));
+                DSC_LAUNCH(k_cgs_dots_reduce<<<((j + 1) * F + 7) / 8, 256, 0, st>>>(w.dpart.p, nchunk, j + 1, F,
+                                                                                   mask, w.h.p, w.hacc.p,
+                                                                                   w.hdf.p));
+                DSC_LAUNCH(k_cgs_update<<<std::min((uunits + 7) / 8, w.upd_grid), 256, 0, st>>>(
+                    w.Vb.p, blk, w.W.p, N, ld, F, j + 1, mask, w.hdf.p, w.npart.p, cgsb));
                 // pass 0: |w| of every active system and the DGKS decision;
                 // pass 1: |w| of the systems that took the second pass
                 if (pass == 0)
-                    DSC_LAUNCH(k_norm_finish<<<gb, 64, 0, st>>>(w.npart.p, (int)vg2.x, F, w.active.p, w.nrm.p,
-                                                                w.nrm0.p, w.act2.p));
+                    DSC_LAUNCH(k_norm_finish<<<wb, 256, 0, st>>>(w.npart.p, nrb, F, w.active.p, w.nrm.p,
+                                                                 w.nrm0.p, w.act2.p));
                 else
-                    DSC_LAUNCH(k_norm_finish<<<gb, 64, 0, st>>>(w.npart.p, (int)vg2.x, F, w.act2.p, w.nrm.p,
-                                                                nullptr, nullptr));
+                    DSC_LAUNCH(k_norm_finish<<<wb, 256, 0, st>>>(w.npart.p, nrb, F, w.act2.p, w.nrm.p,
+                                                                 nullptr, nullptr));
             }
             {
                 TimerScope ts(tm, kTKrylov, st);
@@ -1186,22 +1213,22 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
             dim3 g((N + 63) / 64, (2 * F + 127) / 128);
             DSC_LAUNCH(k_gemm_exact32<<<g, 512, 0, st>>>(s.K64.p, ld, w.Xh.p, ld, w.Y64.p, ld, N, 2 * F, N));
             tm->add_work(kTResidual, (double)N * N * 2 * F);  // FP64-accurate multiply-adds
-            DSC_TRY(f32_to_tf32_pair(w.Xl.p, w.Vh.p, w.Vl.p, blk, st));
-            DSC_TRY(tc_gemm_3xtf32(s.Kt32.p, nullptr, ld, w.Vh.p, w.Vl.p, ld, N, 2 * F, N, w.Yp.p, ld, w.S,
-                                   w.err.p, st, true));
+            DSC_TRY(split_cols_f16(w.Xl.p, ld, N, 2 * F, w.Vh.p, w.Vl.p, ld, w.cscX.p, st));
+            DSC_TRY(tc_gemm_3xf16(s.Kh16.p, s.Kl16.p, ld, w.Vh.p, w.Vl.p, ld, N, 2 * F, N, w.Yp.p, ld, w.S,
+                                  w.err.p, st, s.rsK.p, w.cscX.p));
             DSC_TRY(add_splits(w.Yp.p, w.S, ld * 2 * (size_t)F, ld, N, 2 * F, w.Y64.p, ld, st));
-            DSC_TRY(f32_to_tf32_pair(w.Xh.p, w.Vh.p, w.Vl.p, blk, st));
-            DSC_TRY(tc_gemm_3xtf32(s.dKt32.p, nullptr, ld, w.Vh.p, w.Vl.p, ld, N, 2 * F, N, w.Yp.p, ld, w.S,
-                                   w.err.p, st, true));
+            DSC_TRY(split_cols_f16(w.Xh.p, ld, N, 2 * F, w.Vh.p, w.Vl.p, ld, w.cscX.p, st));
+            DSC_TRY(tc_gemm_3xf16(s.dKh16.p, s.dKl16.p, ld, w.Vh.p, w.Vl.p, ld, N, 2 * F, N, w.Yp.p, ld, w.S,
+                                  w.err.p, st, s.rsdK.p, w.cscX.p));
             DSC_TRY(add_splits(w.Yp.p, w.S, ld * 2 * (size_t)F, ld, N, 2 * F, w.Y64.p, ld, st));
             DSC_LAUNCH(k_residual<<<vg, 256, 0, st>>>(w.Y64.p, w.Xs.p, w.cs.p, w.cd.p, w.bt.p, w.R.p, N, ld, F));
         } else {
             // later residuals are updated, r -= M d: d is small, so the
             // tensor-core product's error is relative to |r|, not to |b|
             TimerScope ts(tm, kTGemmK, st);
-            DSC_TRY(split_vec(w.D.p, w.Vh.p, w.Vl.p, blk, st));
-            DSC_TRY(tc_gemm_3xtf32(s.Kt32.p, nullptr, ld, w.Vh.p, w.Vl.p, ld, N, 2 * F, N, w.Yp.p, ld, w.S,
-                                   w.err.p, st, true));
+            DSC_TRY(split_cols_f16(w.D.p, ld, N, 2 * F, w.Vh.p, w.Vl.p, ld, w.cscX.p, st));
+            DSC_TRY(tc_gemm_3xf16(s.Kh16.p, s.Kl16.p, ld, w.Vh.p, w.Vl.p, ld, N, 2 * F, N, w.Yp.p, ld, w.S,
+                                  w.err.p, st, s.rsK.p, w.cscX.p));
             tm->add_work(kTGemmK, 6.0 * N * N * 2 * F);
             DSC_LAUNCH(k_residual_update<<<vg, 256, 0, st>>>(w.Yp.p, w.S, ld * 2 * (size_t)F, w.D.p, w.cs.p,
                                                              w.cd.p, w.R.p, N, ld, F));
@@ -1294,14 +1321,11 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
         memset(tot_host, 0, (size_t)F * 9 * sizeof(double));
     }
     if (sigma_host) {
-        // the solution with Re / Im halves, as the reference's vB
-        for (int f = 0; f < F; f++) {
-            double *o = sigma_host + (size_t)f * 2 * N;
-            DSC_CUDA(cudaMemcpyAsync(o, w.Xs.p + (size_t)(2 * f) * ld, N * sizeof(double),
-                                     cudaMemcpyDeviceToHost, st));
-            DSC_CUDA(cudaMemcpyAsync(o + N, w.Xs.p + (size_t)(2 * f + 1) * ld, N * sizeof(double),
-                                     cudaMemcpyDeviceToHost, st));
-        }
+        // the solution with Re / Im halves, as the reference's vB: column c
+        // of Xs (2f = Re, 2f + 1 = Im of frequency f) is row c of the
+        // caller's F x 2N array, so one strided copy moves them all
+        DSC_CUDA(cudaMemcpy2DAsync(sigma_host, (size_t)N * sizeof(double), w.Xs.p, ld * sizeof(double),
+                                   (size_t)N * sizeof(double), (size_t)2 * F, cudaMemcpyDeviceToHost, st));
     }
     DSC_CUDA(cudaStreamSynchronize(st));
     return kOk;
@@ -1323,16 +1347,22 @@ int Session::collect_timing(double *ms, int *count, double *work)
 int Session::solve_mixed(unsigned nfreq, const double *freqs, double tol, unsigned max_iters,
                          double *sigma_host, double *forces_host, unsigned *iters)
 {
-    DSC_TRY(make_k32());
+    DSC_TRY(make_k16());
     if (!mx) mx = new Mixed();
     Mixed &w = *mx;
     const int Fmax = (int)std::min<unsigned>(nfreq, kMaxBatch);
     if (w.F < Fmax) {
         const size_t blk = ld * 2 * (size_t)Fmax;
         DSC_TRY(w.Vb.alloc(blk * (kInnerMax + 1)));
-        w.S = tc_gemm_splits_for(N, N);
+        w.S = tc_gemm_f16_splits_for(N, N);
         DSC_TRY(w.Vh.alloc(blk));
         DSC_TRY(w.Vl.alloc(blk));
+        DSC_TRY(w.cscK.alloc(2 * (size_t)Fmax));
+        DSC_TRY(w.cscX.alloc(2 * (size_t)Fmax));
+        {
+            std::vector<float> c(2 * (size_t)Fmax, 1.0f / kVScale);
+            DSC_TRY(w.cscK.upload(c, st));
+        }
         DSC_TRY(w.Yp.alloc(blk * w.S));
         DSC_TRY(w.err.alloc(1));
         DSC_CUDA(cudaMemsetAsync(w.err.p, 0, sizeof(int), st));
@@ -1351,6 +1381,7 @@ int Session::solve_mixed(unsigned nfreq, const double *freqs, double tol, unsign
         DSC_TRY(w.h.alloc((size_t)(kInnerMax + 1) * Fmax));
         DSC_TRY(w.dpart.alloc((size_t)((N + kDotRows - 1) / kDotRows) * (kInnerMax + 1) * Fmax));
         DSC_TRY(w.hacc.alloc((size_t)(kInnerMax + 1) * Fmax));
+        DSC_TRY(w.hdf.alloc((size_t)(kInnerMax + 1) * Fmax));
         DSC_TRY(w.ycoef.alloc((size_t)kInnerMax * Fmax));
         DSC_TRY(w.nrm.alloc(Fmax));
         DSC_TRY(w.scale.alloc(Fmax));
@@ -1371,12 +1402,12 @@ int Session::solve_mixed(unsigned nfreq, const double *freqs, double tol, unsign
             int dev = 0, nsm = 0, o1 = 0, o2 = 0;
             DSC_CUDA(cudaGetDevice(&dev));
             DSC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-            DSC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o1, k_cgs_dots_chunk, 256, 0));
+            DSC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o1, k_cgs_dots, 256, 0));
             DSC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o2, k_cgs_update, 256, 0));
             w.dots_grid = nsm * std::max(1, o1);
             w.upd_grid = nsm * std::max(1, o2);
         }
-        DSC_TRY(w.npart.alloc((size_t)Fmax * ((N + 255) / 256)));
+        DSC_TRY(w.npart.alloc((size_t)Fmax * ((N + kUpdRows - 1) / kUpdRows)));
         DSC_CUDA(cudaMemsetAsync(w.cgsb.p, 0, sizeof(unsigned long long), st));
         // the padding rows of the blocks are never read but keep them finite
         DSC_CUDA(cudaMemsetAsync(w.Vb.p, 0, blk * (kInnerMax + 1) * sizeof(float2), st));

@@ -182,7 +182,7 @@ int Session::assemble64(bool need_fp64)
     // a K assembled in FP64 serves both modes; one assembled in
     // double-FP32 serves the mixed mode only
     if (k64_ready && (!need_fp64 || !k64_df32)) return kOk;
-    k32_ready = false;  // the FP32 copy follows K
+    k16_ready = false;  // the fp16 copies follow K
     DSC_TRY(K64.alloc(ld * N));
     DSC_TRY(assemble_K_fp64(dev, K64.p, ld, st, &timer, !need_fp64, &asm_ws));
     k64_df32 = !need_fp64;
@@ -326,9 +326,9 @@ extern "C" int dsc_session_assemble(dsc_session *s, int mode)
     }
     // always re-assemble: the caller asks for the work to be done now
     s->s.k64_ready = false;
-    s->s.k32_ready = false;
+    s->s.k16_ready = false;
     DSC_TRY(s->s.assemble64(mode == DSC_MODE_FP64));
-    return mode == DSC_MODE_MIXED ? s->s.make_k32() : kOk;
+    return mode == DSC_MODE_MIXED ? s->s.make_k16() : kOk;
 }
 
 extern "C" int dsc_session_geometric_matrix(dsc_session *s, int mode, double *K, size_t ldk)

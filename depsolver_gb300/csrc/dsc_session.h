@@ -1,6 +1,8 @@
 // dsc_session.h -- device-resident scene of libdepsolver_cuda (not exported).
 #pragma once
 
+#include <cuda_fp16.h>
+
 #include <vector>
 
 #include "dsc_field.h"
@@ -49,12 +51,14 @@ struct Session {
     // plain FP64 path workspace
     DevBuf<double> ca, cb, cd, gemv_part;
 
-    // mixed path: K as row-major FP32 in the biased tf32 encoding (split
-    // into tf32 pairs inside the tensor-core products), and the
-    // batched-solver workspace
-    bool k32_ready = false;
-    DevBuf<float> Kt32;
-    DevBuf<float> dKt32;  // K - fl32(K), row-major, biased tf32 encoding
+    // mixed path: K as row-major scaled fp16 pairs (2^s_i fl32(K) per row i)
+    // for the tensor-core products, the same of K - fl32(K) (scaled by
+    // 2^(s_i + 24)) for the first FP64-accurate residual, the epilogue's row
+    // factors, and the batched-solver workspace
+    bool k16_ready = false;
+    DevBuf<__half> Kh16, Kl16, dKh16, dKl16;
+    DevBuf<int> rowE;           // biased FP64 exponent of each row's largest entry
+    DevBuf<float> rsK, rsdK;    // 2^-s_i, 2^-(s_i + 24)
     struct Mixed;
     Mixed *mx = nullptr;
 
@@ -65,7 +69,7 @@ struct Session {
     // K64 (and Kdiag) if not there yet; need_fp64: the regular pairs in FP64
     // (else double-FP32 is enough and is what a new assembly uses)
     int assemble64(bool need_fp64);
-    int make_k32();
+    int make_k16();
     void coeffs(double f, std::vector<double> &a, std::vector<double> &b,
                 std::vector<double> &d) const;
     int solve_fp64(double f, double tol, unsigned max_iters, double *sigma_dev, double *d_tot,

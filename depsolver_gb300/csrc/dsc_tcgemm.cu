@@ -1,23 +1,33 @@
-// dsc_tcgemm.cu -- split-K 3xTF32 GEMM on the 5th-generation tensor cores.
+// dsc_tcgemm.cu -- split-K three-product GEMM on the 5th-generation tensor
+// cores, in tf32 or in fp16.
 //
 //   Y[s] (Nc x M, per split s) = sum over the k-range of split s of
-//       A (M x Kd) * B^T,   A = Ah + Al,  B = Bh + Bl (tf32 pairs)
+//       A (M x Kd) * B^T,   A = Ah + Al,  B = Bh + Bl
 //   with the three products Ah Bh + Ah Bl + Al Bh: about FP32 accuracy.
 //
-// A and B are K-major FP32 (row m of A and row n of B hold consecutive k).
+// tf32 (3xTF32): A and B are K-major FP32 tf32 pairs, or A plain FP32 split
+// in shared memory.  fp16 (3xFP16): A and B are K-major fp16 pairs of
+// operands scaled by powers of two (per row of A, per column of B) so that
+// each row's / column's largest entry lies in [2^14, 2^15); the epilogue
+// multiplies the scales back out (exact).  Both halves of a pair carry 11
+// significant bits, as tf32 does, and kind::f16 issues at twice the
+// kind::tf32 rate.
+//
 // Persistent kernel: one CTA per SM walks the units (128-row tile, split of
 // k) u = blockIdx.x, + gridDim.x, ...  Warp 0 lane 0 streams k-blocks (one
-// swizzle row) of A and Bh, Bl into a 3-stage shared-memory ring with TMA (128B
-// swizzle) without pausing between units; warps 2-5 split A in shared
-// memory; warp 1 lane 0 issues tcgen05.mma (kind::tf32, M = 128, K = 8)
-// into one of two FP32 accumulator buffers in tensor memory and releases
-// each stage with tcgen05.commit; warps 6-9 read the finished buffer back
-// (tcgen05.ld, one TMEM lane per row) and store the partial tile while the
-// next unit accumulates in the other buffer.  Every wait on an mbarrier
-// gives up after ~2 s of clock, sets *err and lets the CTA drain and free
-// its tensor memory.
+// 128-byte swizzle row: 32 tf32 or 64 fp16 values) of A and Bh, Bl into a
+// 3-stage shared-memory ring with TMA (128B swizzle) without pausing between
+// units; warps 2-5 split a plain FP32 A in shared memory; warp 1 lane 0
+// issues tcgen05.mma (M = 128, 32 bytes of k per instruction: K = 8 tf32 or
+// K = 16 fp16) into one of two FP32 accumulator buffers in tensor memory and
+// releases each stage with tcgen05.commit; warps 6-9 read the finished
+// buffer back (tcgen05.ld, one TMEM lane per row) and store the partial tile
+// while the next unit accumulates in the other buffer.  Every wait on an
+// mbarrier gives up after ~2 s of clock, sets *err and lets the CTA drain
+// and free its tensor memory.
 #include <cuda.h>
 #include <cudaTypedefs.h>
+#include <cuda_fp16.h>
 
 #include "dsc_internal.h"
 #include "dsc_tcgemm.h"
@@ -25,12 +35,14 @@
 namespace dsc {
 
 constexpr int kTcBM = 128;
-// A k-block is one swizzle row of kTcRowBytes bytes (128: 32 FP32 values).
+// A k-block is one swizzle row of kTcRowBytes bytes (128: 32 FP32 or 64
+// fp16 values).
 // Measured at the 12k-node scene: 128-byte rows in 3 stages 32.5 ms per
 // sweep's products, 64-byte rows in 6 stages 47.1 ms (twice the barrier
 // hand-offs per byte).
 constexpr int kTcRowBytes = 128;
-constexpr int kTcBK = kTcRowBytes / 4;  // fp32 elements per k-block
+constexpr int kTcBK = kTcRowBytes / 4;    // fp32 elements per k-block
+constexpr int kTcBK16 = kTcRowBytes / 2;  // fp16 elements per k-block
 constexpr int kTcStages = 3;
 // warps: 0 TMA producer, 1 MMA issuer, 2 .. 2 + kTcSplitWarps - 1 split A,
 // the last 4 read the accumulators back
@@ -117,6 +129,13 @@ __host__ __device__ constexpr uint32_t idesc_tf32(int n, int m)
            ((uint32_t)(m >> 4) << 24);
 }
 
+// The same for kind::f16 with A and B both fp16 (type code 0).
+__host__ __device__ constexpr uint32_t idesc_f16(int n, int m)
+{
+    return (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(n >> 3) << 17) |
+           ((uint32_t)(m >> 4) << 24);
+}
+
 __device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc,
                                          uint32_t acc)
 {
@@ -126,6 +145,24 @@ __device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, uin
         "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
         "l"(a), "l"(b), "r"(idesc), "r"(acc)
         : "memory");
+}
+
+__device__ __forceinline__ void mma_f16(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc,
+                                        uint32_t acc)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+template <bool F16>
+__device__ __forceinline__ void mma_op(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
+{
+    if (F16) mma_f16(d, a, b, idesc, acc);
+    else mma_tf32(d, a, b, idesc, acc);
 }
 
 __device__ __forceinline__ void mma_commit(uint64_t *bar)
@@ -220,6 +257,8 @@ __device__ __forceinline__ float tf32_lo_biased(float s)
 // AMODE 2: as 1, with A in the biased encoding (tf32_bias_encode): the
 // truncation gives the round-to-nearest hi, so |lo| is half as large and the
 // dropped lo*lo product is at 2^-22 instead of 2^-21.
+// AMODE 3: A and B arrive as scaled fp16 pairs (kind::f16); the epilogue
+// multiplies row m by rsc[m] and column n by csc[n] (null: 1).
 // COMB (BN a multiple of 32, at most 128): Ah*Bh and Ah*Bl are one MMA of
 // N = 2 BN against the adjacent Bh and Bl tiles, into accumulator columns
 // [0, BN) and [BN, 2 BN); Al*Bh adds into [BN, 2 BN) too; the epilogue adds
@@ -229,15 +268,18 @@ __device__ __forceinline__ float tf32_lo_biased(float s)
 // into an accumulator costs up to one of its units in the last place.
 template <int AMODE>
 __global__ void __launch_bounds__(kTcThreads, 1)
-    k_tc_gemm_3xtf32(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
-                     const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl,
-                     int M, int Nc, int BN, int nkb_total, int kb_per_split, int nsplit,
-                     float *__restrict__ Y, size_t ldy, size_t split_stride, int tmem_cols,
-                     uint32_t acc_stride, int *err)
+    k_tc_gemm3(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
+               const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl,
+               int M, int Nc, int BN, int nkb_total, int kb_per_split, int nsplit,
+               float *__restrict__ Y, size_t ldy, size_t split_stride, int tmem_cols,
+               uint32_t acc_stride, const float *__restrict__ rsc, const float *__restrict__ csc,
+               int *err)
 {
     // acc_stride: TMEM columns of one accumulator buffer, a power of two of
     // at least the columns it holds (so each buffer's MMAs start aligned)
-    constexpr bool SPLIT_A = AMODE != 0;
+    constexpr bool SPLIT_A = AMODE == 1 || AMODE == 2;
+    constexpr bool F16 = AMODE == 3;
+    constexpr int BK = F16 ? kTcBK16 : kTcBK;  // elements per k-block
     const bool comb = BN <= 128 && BN % 32 == 0;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -297,7 +339,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     }
                     uint8_t *st = smem + s * stage_bytes;
                     mbar_expect_tx(&full[s], SPLIT_A ? stage_bytes - a_bytes : stage_bytes);
-                    const int kx = (kb0 + i) * kTcBK;
+                    const int kx = (kb0 + i) * BK;
                     tma_load_2d(st, &tmAh, &full[s], kx, m0);
                     if (!SPLIT_A) tma_load_2d(st + a_bytes, &tmAl, &full[s], kx, m0);
                     tma_load_2d(st + 2 * a_bytes, &tmBh, &full[s], kx, 0);
@@ -315,7 +357,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     } else if (warp == 1) {
         if (lane == 0) {
             // ---- MMA issuer
-            const uint32_t idesc = idesc_tf32(BN, kTcBM), idesc2 = idesc_tf32(2 * BN, kTcBM);
+            const uint32_t idesc = F16 ? idesc_f16(BN, kTcBM) : idesc_tf32(BN, kTcBM);
+            const uint32_t idesc2 = F16 ? idesc_f16(2 * BN, kTcBM) : idesc_tf32(2 * BN, kTcBM);
             uint32_t g = 0;
             bool ok = true;
             int j = 0;
@@ -339,13 +382,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     const uint64_t dbl = sw_desc(st + 2 * a_bytes + b_bytes);
                     // products with Ah: the stage as it landed
 #pragma unroll
-                    for (int kk = 0; kk < kTcBK / 8; kk++) {
-                        const uint64_t off = (uint64_t)(kk * 32) >> 4;  // 8 tf32 = 32 bytes
+                    for (int kk = 0; kk < kTcRowBytes / 32; kk++) {
+                        // 32 bytes of k per MMA: 8 tf32 or 16 fp16
+                        const uint64_t off = (uint64_t)(kk * 32) >> 4;
                         if (comb) {
-                            mma_tf32(acc, dah + off, dbh + off, idesc2, (i | kk) != 0);
+                            mma_op<F16>(acc, dah + off, dbh + off, idesc2, (i | kk) != 0);
                         } else {
-                            mma_tf32(acc, dah + off, dbh + off, idesc, (i | kk) != 0);
-                            mma_tf32(acc, dah + off, dbl + off, idesc, 1);
+                            mma_op<F16>(acc, dah + off, dbh + off, idesc, (i | kk) != 0);
+                            mma_op<F16>(acc, dah + off, dbl + off, idesc, 1);
                         }
                     }
                     // products with Al: after the split
@@ -357,9 +401,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                         tc_fence_after();
                     }
 #pragma unroll
-                    for (int kk = 0; kk < kTcBK / 8; kk++) {
+                    for (int kk = 0; kk < kTcRowBytes / 32; kk++) {
                         const uint64_t off = (uint64_t)(kk * 32) >> 4;
-                        mma_tf32(comb ? acc + BN : acc, dal + off, dbh + off, idesc, 1);
+                        mma_op<F16>(comb ? acc + BN : acc, dal + off, dbh + off, idesc, 1);
                     }
                     mma_commit(&empty[s]);
                 }
@@ -419,6 +463,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             tc_fence_after();
             const uint32_t acc = tmem + ((uint32_t)(ew * 32) << 16) + buf * acc_stride;
             const int m = m0 + ew * 32 + lane;
+            const float rs = (rsc && m < M) ? rsc[m] : 1.0f;
             float *Ys = Y + (size_t)split * split_stride;
             for (int c0 = 0; c0 < BN; c0 += 32) {
                 uint32_t r[32];
@@ -433,7 +478,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
                     for (int t = 0; t < 32; t++) {
                         const int n = c0 + t;
-                        if (n < Nc) Ys[(size_t)n * ldy + m] = __uint_as_float(r[t]);
+                        if (n < Nc) {
+                            // powers of two: the scaling is exact
+                            const float cn = csc ? csc[n] : 1.0f;
+                            Ys[(size_t)n * ldy + m] = __uint_as_float(r[t]) * rs * cn;
+                        }
                     }
                 }
             }
@@ -476,24 +525,27 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
     return fn;
 }
 
-// 2-D FP32 tensor: rows x k (k contiguous, row stride ld elements), boxes
-// of kTcBK k x box_rows rows, kTcRowBytes-byte swizzle, zero fill outside.
-static int make_map(CUtensorMap *map, const float *base, int rows, int k, size_t ld, int box_rows)
+// 2-D tensor of FP32 (esize 4) or fp16 (esize 2) values: rows x k (k
+// contiguous, row stride ld elements), boxes of one swizzle row of k x
+// box_rows rows, kTcRowBytes-byte swizzle, zero fill outside.
+static int make_map(CUtensorMap *map, const void *base, int esize, int rows, int k, size_t ld,
+                    int box_rows)
 {
     auto fn = encode_fn();
     if (!fn) {
         set_error("cuTensorMapEncodeTiled is not available");
         return kErrCuda;
     }
-    if (((uintptr_t)base & 15) || ((ld * sizeof(float)) & 15)) {
+    if (((uintptr_t)base & 15) || ((ld * esize) & 15)) {
         set_error("TMA operand not 16-byte aligned");
         return kErrArg;
     }
     cuuint64_t dims[2] = {(cuuint64_t)k, (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)(ld * sizeof(float))};
-    cuuint32_t box[2] = {(cuuint32_t)kTcBK, (cuuint32_t)box_rows};
+    cuuint64_t strides[1] = {(cuuint64_t)(ld * esize)};
+    cuuint32_t box[2] = {(cuuint32_t)(kTcRowBytes / esize), (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
-    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)base, dims, strides, box, estr,
+    CUresult r = fn(map, esize == 2 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+                    (void *)base, dims, strides, box, estr,
                     CU_TENSOR_MAP_INTERLEAVE_NONE,
                     kTcRowBytes == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -504,31 +556,39 @@ static int make_map(CUtensorMap *map, const float *base, int rows, int k, size_t
     return kOk;
 }
 
-int tc_gemm_3xtf32(const float *Ah, const float *Al, size_t lda, const float *Bh, const float *Bl,
-                   size_t ldb, int M, int Nc, int Kd, float *Y, size_t ldy, int splits, int *d_err,
-                   cudaStream_t st, bool a_biased)
+// Split counts: at least one k-block per split, normalised so that every
+// split has one (callers size their partial-tile buffers by this count).
+static int splits_norm(int nkb, int splits)
 {
-    if (Nc < 1 || Nc > kTcMaxNc || M < 1 || Kd < 1 || ldy < (size_t)M) {
-        set_error("tc_gemm_3xtf32: unsupported shape M %d Nc %d Kd %d (Nc <= %d)", M, Nc, Kd, kTcMaxNc);
-        return kErrArg;
-    }
+    splits = std::max(1, std::min(splits, nkb));
+    const int kps = (nkb + splits - 1) / splits;
+    return (nkb + kps - 1) / kps;
+}
+
+// about eleven waves of one CTA per SM, at least four k-blocks per split
+static int splits_for_bk(int M, int Kd, int bk)
+{
+    const int tiles = (M + kTcBM - 1) / kTcBM;
+    const int nkb = (Kd + bk - 1) / bk;
+    int s = std::max(1, (11 * 152) / std::max(1, tiles));
+    s = std::max(1, std::min(s, nkb / 4));
+    return splits_norm(nkb, s);
+}
+
+// Launch of the persistent kernel on encoded maps (bk: elements per k-block).
+static int tc_launch(int amode, const CUtensorMap &ah, const CUtensorMap &al, const CUtensorMap &bh,
+                     const CUtensorMap &bl, int M, int Nc, int Kd, int bk, float *Y, size_t ldy, int splits,
+                     int *d_err, cudaStream_t st, const float *rsc, const float *csc)
+{
     const int BN = (Nc + 15) / 16 * 16;
     // two accumulator buffers of 2 BN (COMB) or BN columns, each rounded up
     // to a power of two
     uint32_t acc_stride = 32;
     while (acc_stride < (uint32_t)((BN <= 128 && BN % 32 == 0) ? 2 * BN : BN)) acc_stride *= 2;
     const int tmem_cols = 2 * (int)acc_stride;
-    const bool split_a = Al == nullptr;  // plain FP32 A, split in shared memory
-    CUtensorMap ah, al, bh, bl;
-    DSC_TRY(make_map(&ah, Ah, M, Kd, lda, kTcBM));
-    if (split_a) al = ah;
-    else DSC_TRY(make_map(&al, Al, M, Kd, lda, kTcBM));
-    DSC_TRY(make_map(&bh, Bh, Nc, Kd, ldb, BN));
-    DSC_TRY(make_map(&bl, Bl, Nc, Kd, ldb, BN));
-    const int nkb = (Kd + kTcBK - 1) / kTcBK;
-    splits = std::max(1, std::min(splits, nkb));
+    const int nkb = (Kd + bk - 1) / bk;
+    splits = splits_norm(nkb, splits);
     const int kps = (nkb + splits - 1) / splits;
-    splits = (nkb + kps - 1) / kps;  // every split has at least one k-block
     const size_t smem = 1024 + (size_t)kTcStages * (2 * kTcBM + 2 * BN) * kTcRowBytes + 256;
     // persistent: one CTA per SM walks the (row tile, split) units
     static int nsm = 0;
@@ -542,28 +602,59 @@ int tc_gemm_3xtf32(const float *Ah, const float *Al, size_t lda, const float *Bh
     auto launch = [&](auto kern) -> int {
         DSC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         DSC_LAUNCH(kern<<<grid, kTcThreads, smem, st>>>(ah, al, bh, bl, M, Nc, BN, nkb, kps, splits, Y, ldy,
-                                                 ldy * (size_t)Nc, tmem_cols, acc_stride, d_err));
+                                                 ldy * (size_t)Nc, tmem_cols, acc_stride, rsc, csc, d_err));
         return kOk;
     };
-    if (!split_a) DSC_TRY(launch(k_tc_gemm_3xtf32<0>));
-    else if (a_biased) DSC_TRY(launch(k_tc_gemm_3xtf32<2>));
-    else DSC_TRY(launch(k_tc_gemm_3xtf32<1>));
+    switch (amode) {
+    case 0: DSC_TRY(launch(k_tc_gemm3<0>)); break;
+    case 1: DSC_TRY(launch(k_tc_gemm3<1>)); break;
+    case 2: DSC_TRY(launch(k_tc_gemm3<2>)); break;
+    default: DSC_TRY(launch(k_tc_gemm3<3>)); break;
+    }
     DSC_CUDA(cudaGetLastError());
     return kOk;
 }
 
-int tc_gemm_splits_for(int M, int Kd)
+int tc_gemm_3xtf32(const float *Ah, const float *Al, size_t lda, const float *Bh, const float *Bl,
+                   size_t ldb, int M, int Nc, int Kd, float *Y, size_t ldy, int splits, int *d_err,
+                   cudaStream_t st, bool a_biased)
 {
-    const int tiles = (M + kTcBM - 1) / kTcBM;
-    const int nkb = (Kd + kTcBK - 1) / kTcBK;
-    // about eleven waves of one CTA per SM, at least four k-blocks per split;
-    // normalised exactly as tc_gemm_3xtf32 does, so callers can size buffers
-    int s = std::max(1, (11 * 152) / std::max(1, tiles));
-    s = std::max(1, std::min(s, nkb / 4));
-    s = std::min(s, nkb);
-    const int kps = (nkb + s - 1) / s;
-    return (nkb + kps - 1) / kps;
+    if (Nc < 1 || Nc > kTcMaxNc || M < 1 || Kd < 1 || ldy < (size_t)M) {
+        set_error("tc_gemm_3xtf32: unsupported shape M %d Nc %d Kd %d (Nc <= %d)", M, Nc, Kd, kTcMaxNc);
+        return kErrArg;
+    }
+    const int BN = (Nc + 15) / 16 * 16;
+    const bool split_a = Al == nullptr;  // plain FP32 A, split in shared memory
+    CUtensorMap ah, al, bh, bl;
+    DSC_TRY(make_map(&ah, Ah, 4, M, Kd, lda, kTcBM));
+    if (split_a) al = ah;
+    else DSC_TRY(make_map(&al, Al, 4, M, Kd, lda, kTcBM));
+    DSC_TRY(make_map(&bh, Bh, 4, Nc, Kd, ldb, BN));
+    DSC_TRY(make_map(&bl, Bl, 4, Nc, Kd, ldb, BN));
+    const int amode = !split_a ? 0 : a_biased ? 2 : 1;
+    return tc_launch(amode, ah, al, bh, bl, M, Nc, Kd, kTcBK, Y, ldy, splits, d_err, st, nullptr, nullptr);
 }
+
+int tc_gemm_3xf16(const __half *Ah, const __half *Al, size_t lda, const __half *Bh, const __half *Bl,
+                  size_t ldb, int M, int Nc, int Kd, float *Y, size_t ldy, int splits, int *d_err,
+                  cudaStream_t st, const float *rsc, const float *csc)
+{
+    if (Nc < 1 || Nc > kTcMaxNc || M < 1 || Kd < 1 || ldy < (size_t)M || !Al) {
+        set_error("tc_gemm_3xf16: unsupported shape M %d Nc %d Kd %d (Nc <= %d)", M, Nc, Kd, kTcMaxNc);
+        return kErrArg;
+    }
+    const int BN = (Nc + 15) / 16 * 16;
+    CUtensorMap ah, al, bh, bl;
+    DSC_TRY(make_map(&ah, Ah, 2, M, Kd, lda, kTcBM));
+    DSC_TRY(make_map(&al, Al, 2, M, Kd, lda, kTcBM));
+    DSC_TRY(make_map(&bh, Bh, 2, Nc, Kd, ldb, BN));
+    DSC_TRY(make_map(&bl, Bl, 2, Nc, Kd, ldb, BN));
+    return tc_launch(3, ah, al, bh, bl, M, Nc, Kd, kTcBK16, Y, ldy, splits, d_err, st, rsc, csc);
+}
+
+int tc_gemm_splits_for(int M, int Kd) { return splits_for_bk(M, Kd, kTcBK); }
+
+int tc_gemm_f16_splits_for(int M, int Kd) { return splits_for_bk(M, Kd, kTcBK16); }
 
 // ---------------------------------------------------------- operand split
 // tf32 pair of a value: hi = round-to-nearest tf32, lo = value - hi, also
@@ -604,6 +695,153 @@ __global__ void k_split_transpose(const double *__restrict__ K, size_t ld, int N
                 Tl[(size_t)i * ldt + c] = tf32_bias_encode((float)(a - (double)v));
         }
     }
+}
+
+// ------------------------------------------------ fp16 operand preparation
+
+// 2^k as FP32, exact, for -126 <= k <= 127.
+__device__ __forceinline__ float pow2f(int k) { return __int_as_float((127 + k) << 23); }
+
+// Shift s with 2^s * max in [2^14, 2^15) from the biased exponent E of the
+// largest magnitude (FP64: bias 1023, FP32: bias 127; E = 0: all zero, no
+// shift), clamped so that 2^s and 2^(s + 24) stay normal FP32 values.
+__device__ __forceinline__ int scale_shift(int E, int bias)
+{
+    return E == 0 ? 0 : max(-100, min(100, 14 - (E - bias)));
+}
+
+// rowE[i] = max over the row's entries of the biased FP64 exponent of
+// column-major K (entry (i, c) at c * ld + i); rowE zero on entry.  Block
+// (row block, column chunk); the exponent comes from the high word of each
+// double (integer work only).
+__global__ void k_row_exponent(const double *__restrict__ K, size_t ld, int N, int cols, int *rowE)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const int c0 = blockIdx.y * cols, c1 = min(N, c0 + cols);
+    int e = 0;
+#pragma unroll 8
+    for (int c = c0; c < c1; c++) e = max(e, (__double2hiint(K[(size_t)c * ld + i]) >> 20) & 0x7FF);
+    atomicMax(&rowE[i], e);
+}
+
+// The epilogue's row factors: rsK[i] = 2^-s_i for K's fp16 pair, rsdK[i] =
+// 2^-(s_i + 24) for that of K - fl32(K).
+__global__ void k_row_scales(const int *__restrict__ rowE, int N, float *__restrict__ rsK,
+                             float *__restrict__ rsdK)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const int sh = scale_shift(rowE[i], 1023);
+    rsK[i] = pow2f(-sh);
+    if (rsdK) rsdK[i] = pow2f(-sh - 24);
+}
+
+// Column-major FP64 K to row-major fp16 pairs (entry (i, c) at i * ldt + c)
+// of 2^s_i fl32(K) (Th, Tl) and, with Dh not null, of 2^(s_i + 24) (K -
+// fl32(K)) (Dh, Dl): hi = rn_fp16(x), lo = rn_fp16(x - hi).  |K - fl32(K)|
+// <= 2^-24 |K| entrywise, so both scaled matrices stay below 2^15 (fp16's
+// largest finite value is 65504).  A
+// 32 x 32 shared tile per block.
+__global__ void k_split_transpose_f16(const double *__restrict__ K, size_t ld, int N,
+                                      const int *__restrict__ rowE, __half *__restrict__ Th,
+                                      __half *__restrict__ Tl, __half *__restrict__ Dh,
+                                      __half *__restrict__ Dl, size_t ldt)
+{
+    __shared__ double t[32][33];
+    const int i0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        int c = c0 + k, i = i0 + threadIdx.x;
+        t[k][threadIdx.x] = (c < N && i < N) ? K[(size_t)c * ld + i] : 0.0;
+    }
+    __syncthreads();
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        int i = i0 + k, c = c0 + threadIdx.x;
+        if (i < N && c < N) {
+            const double a = t[threadIdx.x][k];
+            const int sh = scale_shift(rowE[i], 1023);
+            const float v = (float)a;
+            const float x = v * pow2f(sh);
+            const __half h = __float2half_rn(x);
+            Th[(size_t)i * ldt + c] = h;
+            Tl[(size_t)i * ldt + c] = __float2half_rn(x - __half2float(h));
+            if (Dh) {
+                const float y = (float)(a - (double)v) * pow2f(sh + 24);
+                const __half dh = __float2half_rn(y);
+                Dh[(size_t)i * ldt + c] = dh;
+                Dl[(size_t)i * ldt + c] = __float2half_rn(y - __half2float(dh));
+            }
+        }
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ float to_f32(T v) { return (float)v; }
+
+// Columns of x (column n: N entries at n * ldx) to fp16 pairs of
+// 2^t_n x (rows of h / l: n * ldh), t_n from the column's largest FP32
+// exponent; csc[n] = 2^-t_n.  One block per column.
+template <typename T>
+__global__ void __launch_bounds__(256) k_split_cols_f16(const T *__restrict__ x, size_t ldx, int N,
+                                                        __half *__restrict__ h, __half *__restrict__ l,
+                                                        size_t ldh, float *__restrict__ csc)
+{
+    __shared__ int emax;
+    if (threadIdx.x == 0) emax = 0;
+    __syncthreads();
+    const T *col = x + (size_t)blockIdx.x * ldx;
+    int e = 0;
+    for (int i = threadIdx.x; i < N; i += blockDim.x)
+        e = max(e, (__float_as_int(to_f32(col[i])) >> 23) & 0xFF);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(&emax, e);
+    __syncthreads();
+    const int sh = scale_shift(emax, 127);
+    const float f = pow2f(sh);
+    __half *hc = h + (size_t)blockIdx.x * ldh, *lc = l + (size_t)blockIdx.x * ldh;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        const float v = to_f32(col[i]) * f;
+        const __half a = __float2half_rn(v);
+        hc[i] = a;
+        lc[i] = __float2half_rn(v - __half2float(a));
+    }
+    if (threadIdx.x == 0) csc[blockIdx.x] = pow2f(-sh);
+}
+
+int k16_row_scales(const double *K, size_t ld, int N, int *rowE, float *rsK, float *rsdK, cudaStream_t st)
+{
+    DSC_CUDA(cudaMemsetAsync(rowE, 0, (size_t)N * sizeof(int), st));
+    const int chunks = 64, cols = (N + chunks - 1) / chunks;
+    DSC_LAUNCH(k_row_exponent<<<dim3((N + 255) / 256, (N + cols - 1) / cols), 256, 0, st>>>(K, ld, N, cols, rowE));
+    DSC_LAUNCH(k_row_scales<<<(N + 255) / 256, 256, 0, st>>>(rowE, N, rsK, rsdK));
+    DSC_CUDA(cudaGetLastError());
+    return kOk;
+}
+
+int split_transpose_K16(const double *K, size_t ld, int N, const int *rowE, __half *Th, __half *Tl,
+                        __half *Dh, __half *Dl, size_t ldt, cudaStream_t st)
+{
+    dim3 g((N + 31) / 32, (N + 31) / 32), b(32, 8);
+    DSC_LAUNCH(k_split_transpose_f16<<<g, b, 0, st>>>(K, ld, N, rowE, Th, Tl, Dh, Dl, ldt));
+    DSC_CUDA(cudaGetLastError());
+    return kOk;
+}
+
+int split_cols_f16(const double *x, size_t ldx, int N, int ncol, __half *h, __half *l, size_t ldh,
+                   float *csc, cudaStream_t st)
+{
+    DSC_LAUNCH(k_split_cols_f16<double><<<ncol, 256, 0, st>>>(x, ldx, N, h, l, ldh, csc));
+    DSC_CUDA(cudaGetLastError());
+    return kOk;
+}
+
+int split_cols_f16(const float *x, size_t ldx, int N, int ncol, __half *h, __half *l, size_t ldh,
+                   float *csc, cudaStream_t st)
+{
+    DSC_LAUNCH(k_split_cols_f16<float><<<ncol, 256, 0, st>>>(x, ldx, N, h, l, ldh, csc));
+    DSC_CUDA(cudaGetLastError());
+    return kOk;
 }
 
 // FP64 vectors (any layout) to tf32 pairs, elementwise.
@@ -701,13 +939,7 @@ int sum_splits(const float *P, int S, size_t split_stride, size_t ldp, int M, in
     return kOk;
 }
 
-int tc_gemm_splits_used(int Kd, int splits)
-{
-    const int nkb = (Kd + kTcBK - 1) / kTcBK;
-    splits = std::max(1, std::min(splits, nkb));
-    const int kps = (nkb + splits - 1) / splits;
-    return (nkb + kps - 1) / kps;
-}
+int tc_gemm_splits_used(int Kd, int splits) { return splits_norm((Kd + kTcBK - 1) / kTcBK, splits); }
 
 // FP32 array to tf32 pairs (hi = rna(x), lo = rna(x - hi)), elementwise.
 __global__ void k_f32_to_tf32_pair(const float *__restrict__ x, float *__restrict__ h,
@@ -754,7 +986,10 @@ int add_splits(const float *P, int S, size_t split_stride, size_t ldp, int M, in
 using namespace dsc;
 
 // Host-array entry point of the tensor-core product (row-major FP64 in and
-// out): Y (M x Nc) = A (M x Kd) * B^T (B: Nc x Kd) with 3xTF32 products.
+// out): Y (M x Nc) = A (M x Kd) * B^T (B: Nc x Kd) with 3xTF32 products
+// (a_in_smem 0: A as a tf32 pair, 1: plain FP32 A split in shared memory,
+// 2: the same in the biased encoding) or 3xFP16 products on per-row scaled
+// fp16 pairs (a_in_smem 3).
 extern "C" int dsc_tc_gemm(int M, int Nc, int Kd, const double *A, const double *B, double *Y,
                            int splits, int a_in_smem)
 {
@@ -766,6 +1001,10 @@ extern "C" int dsc_tc_gemm(int M, int Nc, int Kd, const double *A, const double 
     }
     if (M < 1 || Kd < 1 || Nc < 1 || Nc > kTcMaxNc) {
         set_error("dsc_tc_gemm: unsupported shape (1 <= Nc <= %d)", kTcMaxNc);
+        return kErrArg;
+    }
+    if (a_in_smem < 0 || a_in_smem > 3) {
+        set_error("dsc_tc_gemm: unknown operand mode %d (0 .. 3)", a_in_smem);
         return kErrArg;
     }
     cudaStream_t st = 0;
@@ -781,6 +1020,36 @@ extern "C" int dsc_tc_gemm(int M, int Nc, int Kd, const double *A, const double 
                           cudaMemcpyHostToDevice));
     DSC_CUDA(cudaMemcpy2D(dB.p, lda * sizeof(double), B, Kd * sizeof(double), Kd * sizeof(double), Nc,
                           cudaMemcpyHostToDevice));
+    if (a_in_smem == 3) {
+        // 3xFP16: rows of A and of B to scaled fp16 pairs (row factors of A
+        // and of B as the epilogue's row and column factors)
+        DevBuf<__half> h16[4];
+        DevBuf<float> ra, cb;
+        for (auto &b16 : h16) DSC_TRY(b16.alloc((size_t)std::max(M, Nc) * lda));
+        DSC_TRY(ra.alloc(M));
+        DSC_TRY(cb.alloc(Nc));
+        DSC_TRY(split_cols_f16(dA.p, lda, Kd, M, h16[0].p, h16[1].p, lda, ra.p, st));
+        DSC_TRY(split_cols_f16(dB.p, lda, Kd, Nc, h16[2].p, h16[3].p, lda, cb.p, st));
+        if (splits <= 0) splits = tc_gemm_f16_splits_for(M, Kd);
+        const int S = splits_norm((Kd + kTcBK16 - 1) / kTcBK16, splits);
+        DSC_TRY(P.alloc((size_t)S * Nc * M));
+        DSC_TRY(err.alloc(1));
+        DSC_CUDA(cudaMemset(err.p, 0, sizeof(int)));
+        DSC_TRY(tc_gemm_3xf16(h16[0].p, h16[1].p, lda, h16[2].p, h16[3].p, lda, M, Nc, Kd, P.p, (size_t)M, S,
+                              err.p, st, ra.p, cb.p));
+        DSC_TRY(dY.alloc((size_t)M * Nc));
+        dim3 g((M + 255) / 256, Nc);
+        DSC_LAUNCH(k_sum_splits<<<g, 256, 0, st>>>(P.p, S, (size_t)M * Nc, (size_t)M, M, Nc, dY.p));
+        DSC_CUDA(cudaGetLastError());
+        int herr = 0;
+        DSC_CUDA(cudaMemcpy(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost));
+        if (herr) {
+            set_error("tensor-core GEMM: a pipeline wait gave up (code %d)", herr);
+            return kErrCuda;
+        }
+        DSC_CUDA(cudaMemcpy(Y, dY.p, (size_t)M * Nc * sizeof(double), cudaMemcpyDeviceToHost));
+        return kOk;
+    }
     DSC_TRY(Ah.alloc((size_t)M * lda));
     DSC_TRY(Al.alloc((size_t)M * lda));
     DSC_TRY(Bh.alloc((size_t)Nc * lda));

@@ -1,6 +1,7 @@
 // dsc_tcgemm.h -- tensor-core GEMM of libdepsolver_cuda (not exported).
 #pragma once
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stddef.h>
 
@@ -19,6 +20,31 @@ int tc_gemm_3xtf32(const float *Ah, const float *Al, size_t lda, const float *Bh
                    size_t ldb, int M, int Nc, int Kd, float *Y, size_t ldy, int splits, int *d_err,
                    cudaStream_t st, bool a_biased = false);
 int tc_gemm_splits_for(int M, int Kd);
+
+// The same three products in fp16 (kind::f16, twice the tf32 rate) on
+// scaled fp16 pairs: A = 2^s_m (Ah + Al) per row, B = 2^t_n (Bh + Bl) per
+// column, each row's / column's largest entry in [2^14, 2^15).  Y is the
+// unscaled product: the epilogue multiplies row m by rsc[m] = 2^-s_m and
+// column n by csc[n] = 2^-t_n (either null: 1).  Row strides lda / ldb in
+// elements (multiples of 8, 16-byte aligned bases).
+int tc_gemm_3xf16(const __half *Ah, const __half *Al, size_t lda, const __half *Bh, const __half *Bl,
+                  size_t ldb, int M, int Nc, int Kd, float *Y, size_t ldy, int splits, int *d_err,
+                  cudaStream_t st, const float *rsc, const float *csc);
+int tc_gemm_f16_splits_for(int M, int Kd);
+// Row scales of column-major FP64 K (stride ld): rowE (N ints, scratch) the
+// biased exponent of each row's largest entry, rsK = 2^-s_i, rsdK (may be
+// null) = 2^-(s_i + 24).
+int k16_row_scales(const double *K, size_t ld, int N, int *rowE, float *rsK, float *rsdK, cudaStream_t st);
+// K to the row-major scaled fp16 pairs of fl32(K) (Th, Tl) and, with Dh
+// not null, of K - fl32(K) (Dh, Dl), after k16_row_scales.
+int split_transpose_K16(const double *K, size_t ld, int N, const int *rowE, __half *Th, __half *Tl,
+                        __half *Dh, __half *Dl, size_t ldt, cudaStream_t st);
+// Columns (N entries each, stride ldx) to scaled fp16 pairs (stride ldh),
+// csc[n] = the column's 2^-t_n.
+int split_cols_f16(const double *x, size_t ldx, int N, int ncol, __half *h, __half *l, size_t ldh,
+                   float *csc, cudaStream_t st);
+int split_cols_f16(const float *x, size_t ldx, int N, int ncol, __half *h, __half *l, size_t ldh,
+                   float *csc, cudaStream_t st);
 
 // Column-major FP64 N x N matrix (stride ld) to row-major FP32: the tf32
 // pair of each entry (Th, Tl), the entry rounded to FP32 (Th; plain or in

@@ -200,12 +200,13 @@ int dsc_session_solve(dsc_session *s, int mode, unsigned nfreq, const double *fr
  *       1 assembly fix-up                0
  *       2 assembly singular pairs        0
  *       3 FP64 K GEMV                    bytes of K read
- *       4 K GEMM (mixed, tensor cores)   flops of the three tf32 products
+ *       4 K GEMM (mixed, tensor cores)   flops of the three fp16 products
  *       5 field                          (particle node, element) pairs x systems
  *       6 Maxwell stress                 0
  *       7 FP64-accurate residual GEMM    multiply-adds
  *       8 other Krylov kernels           0
- *       9 Gram-Schmidt passes            bytes the kernels read and wrote */
+ *       9 Gram-Schmidt passes            bytes the kernels read and wrote
+ *      10 K to its fp16 pairs (mixed)    bytes read and written */
 int dsc_session_set_timing(dsc_session *s, int on);
 /* The CUDA stream (cudaStream_t) all of the session's work runs on, so a
  * caller can record its own events around a solve. */
@@ -216,13 +217,15 @@ int dsc_session_timing(dsc_session *s, double *ms, int *count, double *work, int
  * sweep's matrix products (no counterpart call in the reference, whose
  * GMRES product is the scalar loop of src/gmres_el.c:323-337):
  * Y (M x Nc) = A (M x Kd) * B^T (B is Nc x Kd), all row-major; each operand
- * is split into a TF32 pair and three products hi*hi + hi*lo + lo*hi are
- * accumulated in FP32 per split of k and in FP64 across splits (about FP32
- * accuracy).  Nc <= 160; splits <= 0 picks the split count.  a_in_smem = 0
- * stores A as the tf32 pair; 1 stores A as plain FP32 and splits it inside
- * the kernel (half the reads of A); 2 does the same on A stored in a biased
- * encoding whose truncation to tf32 is the rounded hi (the mixed sweep's
- * mode, about twice as accurate as 1). */
+ * is split into a pair of 11-bit halves and three products hi*hi + hi*lo +
+ * lo*hi are accumulated in FP32 per split of k and in FP64 across splits
+ * (about FP32 accuracy).  Nc <= 160; splits <= 0 picks the split count.
+ * a_in_smem = 0 stores A as the tf32 pair; 1 stores A as plain FP32 and
+ * splits it inside the kernel (half the reads of A); 2 does the same on A
+ * stored in a biased encoding whose truncation to tf32 is the rounded hi;
+ * 3 (the mixed sweep's mode) scales each row of A and of B by a power of two
+ * and splits it into an fp16 pair, products on the fp16 tensor path (twice
+ * the tf32 rate), the scales multiplied back out in the epilogue. */
 int dsc_tc_gemm(int M, int Nc, int Kd, const double *A, const double *B, double *Y, int splits,
                 int a_in_smem);
 

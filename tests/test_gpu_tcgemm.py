@@ -1,8 +1,9 @@
-"""The tcgen05 3xTF32 split-K GEMM against an FP64 product (NumPy).
+"""The tcgen05 split-K GEMM (3xTF32, and 3xFP16 on scaled fp16 pairs)
+against an FP64 product (NumPy).
 
 Bar: |Y - A B^T| <= 2e-6 * (|A| |B|^T) elementwise -- the FP32-level
 accuracy the mixed inner solver relies on -- for ragged shapes (rows not a
-multiple of 128, k not a multiple of 32, columns not a multiple of 16).
+multiple of 128, k not a multiple of 32 / 64, columns not a multiple of 16).
 """
 import numpy as np
 import pytest
@@ -21,7 +22,7 @@ def _run(L, A, B, splits, a_in_smem=1):
     return Y
 
 
-@pytest.mark.parametrize("a_in_smem", [0, 1, 2])
+@pytest.mark.parametrize("a_in_smem", [0, 1, 2, 3])
 @pytest.mark.parametrize("M,Nc,Kd,splits", [
     (128, 16, 32, 1),      # one tile, one k-block
     (300, 40, 1000, 1),    # ragged everything, one split
@@ -47,3 +48,21 @@ def test_tc_gemm_beats_plain_tf32(gpu):
     Y = _run(gpu, A, B, 2)
     rel = np.abs(Y - A @ B.T).max() / np.abs(A @ B.T).max()
     assert rel < 1e-5
+
+
+def test_tc_gemm_f16_scales_rows_and_columns(gpu):
+    """3xFP16: rows of A and of B spread over 2^-40 .. 2^40 (far outside
+    fp16's range; the products stay inside FP32's, where the partial tiles
+    live) keep the FP32-level bound: each row's power-of-two scale is
+    multiplied back out exactly."""
+    rng = np.random.default_rng(11)
+    M, Nc, Kd = 400, 96, 700
+    A = rng.standard_normal((M, Kd)) * np.exp2(rng.integers(-40, 40, (M, 1)))
+    A[:, ::7] *= 1e-9   # small entries next to large ones in the same row
+    B = rng.standard_normal((Nc, Kd)) * np.exp2(rng.integers(-40, 40, (Nc, 1)))
+    B[3] = 0.0           # an all-zero operand row
+    Y = _run(gpu, A, B, 0, 3)
+    ref = A @ B.T
+    bound = np.abs(A) @ np.abs(B).T
+    assert np.all(np.abs(Y - ref) <= 2e-6 * bound + 1e-300), float(np.nanmax(np.abs(Y - ref) / bound))
+    assert np.all(Y[:, 3] == 0.0)
