@@ -38,14 +38,17 @@ constexpr int kOuterMax = 6;    // refinement steps
 // 3e-7 took 89, 1e-7 took 93.
 constexpr double kInnerTol = 3e-7;
 
-// C (M x Nc, FP64) = fl32(A) (M x Kd) * B (Kd x Nc), column-major: A is FP64
-// and rounded to FP32 as it is staged (one conversion per element on the
-// FP64 pipe: a tile spans 128 columns), B is FP32; every product is exact
-// (p = a*b and e = fma(a, b, -p)) and the running sum is an unevaluated pair
-// (s, c) kept exact by TwoSum: about 2^-46 of the sum of |a b|.  The parts
-// of A and of the true B below FP32 are small (2^-24 relative) and go to
-// the tensor cores (the first residual of the mixed sweep).  64 x 128 tile,
-// 512 threads with 4 x 4 outputs each, k-steps of 16.
+// P[z] (M x Nc, FP64) = the part over k-split z of fl32(A) (M x Kd) * B
+// (Kd x Nc), column-major: A is FP64 and rounded to FP32 as it is staged
+// (one conversion per element on the FP64 pipe), B is FP32; every product
+// is exact (p = a*b and e = fma(a, b, -p)) and the running sum is an
+// unevaluated pair (s, c) kept exact by TwoSum: about 2^-46 of the sum of
+// |a b|.  The parts of A and of the true B below FP32 are small (2^-24
+// relative) and go to the tensor cores (the first residual of the mixed
+// sweep).  64 x 128 tile, 512 threads with 4 x 4 outputs each, k-steps of
+// 16 through two shared-memory buffers (the next step's tile is fetched into
+// registers while the current one is used); grid (row tiles, column tiles,
+// k-splits), the splits added in order by k_sum_exact_splits.
 __device__ __forceinline__ void exact_acc(float &s, float &c, float a, float b)
 {
     // the _rn intrinsics keep the compiler from fusing these operations,
@@ -59,46 +62,77 @@ __device__ __forceinline__ void exact_acc(float &s, float &c, float a, float b)
     c += err + e;
 }
 
+constexpr int kExBK = 16;
+constexpr int kExSplits = 8;
+
 __global__ void __launch_bounds__(512, 1) k_gemm_exact32(const double *__restrict__ A, size_t lda,
                                                       const float *__restrict__ B, size_t ldb,
-                                                      double *__restrict__ C, size_t ldc, int M, int Nc,
-                                                      int Kd)
+                                                      double *__restrict__ P, size_t ldp, size_t split_stride,
+                                                      int M, int Nc, int Kd, int kchunk)
 {
-    __shared__ float As[16][64 + 1];
-    __shared__ float Bs[16][128 + 1];
+    __shared__ float As[2][kExBK][64];
+    __shared__ float Bs[2][kExBK][128 + 1];
     const int m0 = blockIdx.x * 64, n0 = blockIdx.y * 128;
+    const int k_beg = blockIdx.z * kchunk, k_end = min(Kd, k_beg + kchunk);
     const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;
     float s[4][4], c[4][4];
 #pragma unroll
     for (int u = 0; u < 4; u++)
 #pragma unroll
         for (int v = 0; v < 4; v++) s[u][v] = c[u][v] = 0.0f;
-    for (int k0 = 0; k0 < Kd; k0 += 16) {
-        for (int t = threadIdx.x; t < 16 * 64; t += 512) {
-            const int kk = t / 64, mm = t % 64;
+    // staging: A element (kk = t / 64, mm = t % 64) for t = tid, tid + 512;
+    // B element (nn = t / 16, kb = t % 16) for t = tid + 512 q, q < 4
+    float ra[2], rb[4];
+    auto fetch = [&](int k0) {
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            const int t = threadIdx.x + 512 * q, kk = t / 64, mm = t % 64;
             const int m = m0 + mm, k = k0 + kk;
-            As[kk][mm] = (m < M && k < Kd) ? (float)A[(size_t)k * lda + m] : 0.0f;
+            ra[q] = (m < M && k < k_end) ? (float)A[(size_t)k * lda + m] : 0.0f;
         }
-        for (int t = threadIdx.x; t < 16 * 128; t += 512) {
-            const int nn = t / 16, kb = t % 16;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int t = threadIdx.x + 512 * q, nn = t / 16, kb = t % 16;
             const int n = n0 + nn, k = k0 + kb;
-            Bs[kb][nn] = (n < Nc && k < Kd) ? B[(size_t)n * ldb + k] : 0.0f;
+            rb[q] = (n < Nc && k < k_end) ? B[(size_t)n * ldb + k] : 0.0f;
         }
-        __syncthreads();
+    };
+    auto stash = [&](int buf) {
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            const int t = threadIdx.x + 512 * q;
+            As[buf][t / 64][t % 64] = ra[q];
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int t = threadIdx.x + 512 * q;
+            Bs[buf][t % 16][t / 16] = rb[q];
+        }
+    };
+    fetch(k_beg);
+    stash(0);
+    __syncthreads();
+    int buf = 0;
+    for (int k0 = k_beg; k0 < k_end; k0 += kExBK) {
+        const bool more = k0 + kExBK < k_end;
+        if (more) fetch(k0 + kExBK);
 #pragma unroll 2
-        for (int kk = 0; kk < 16; kk++) {
+        for (int kk = 0; kk < kExBK; kk++) {
             float a[4], b[4];
 #pragma unroll
-            for (int u = 0; u < 4; u++) a[u] = As[kk][ty + 16 * u];
+            for (int u = 0; u < 4; u++) a[u] = As[buf][kk][ty + 16 * u];
 #pragma unroll
-            for (int v = 0; v < 4; v++) b[v] = Bs[kk][tx + 32 * v];
+            for (int v = 0; v < 4; v++) b[v] = Bs[buf][kk][tx + 32 * v];
 #pragma unroll
             for (int u = 0; u < 4; u++)
 #pragma unroll
                 for (int v = 0; v < 4; v++) exact_acc(s[u][v], c[u][v], a[u], b[v]);
         }
+        if (more) stash(buf ^ 1);
         __syncthreads();
+        buf ^= 1;
     }
+    double *Pz = P + (size_t)blockIdx.z * split_stride;
 #pragma unroll
     for (int u = 0; u < 4; u++) {
         const int m = m0 + ty + 16 * u;
@@ -106,9 +140,21 @@ __global__ void __launch_bounds__(512, 1) k_gemm_exact32(const double *__restric
 #pragma unroll
         for (int v = 0; v < 4; v++) {
             const int n = n0 + tx + 32 * v;
-            if (n < Nc) C[(size_t)n * ldc + m] = (double)s[u][v] + (double)c[u][v];
+            if (n < Nc) Pz[(size_t)n * ldp + m] = (double)s[u][v] + (double)c[u][v];
         }
     }
+}
+
+// C[n * ldc + m] = sum over the S splits of P, in split order (FP64).
+__global__ void k_sum_exact_splits(const double *__restrict__ P, int S, size_t split_stride, size_t ldp,
+                                   int M, double *__restrict__ C, size_t ldc)
+{
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = blockIdx.y;
+    if (m >= M) return;
+    double t = 0.0;
+    for (int z = 0; z < S; z++) t += P[(size_t)z * split_stride + (size_t)n * ldp + m];
+    C[(size_t)n * ldc + m] = t;
 }
 
 // FP64 array to FP32 pairs (hi = rounded value, lo = the rest, rounded).
@@ -922,6 +968,7 @@ struct Session::Mixed {
     DevBuf<float> Yp;       // split-K partial products, S blocks
     DevBuf<int> err;        // set by the tensor-core kernel when a wait gives up
     DevBuf<double> Xs, R, Y64, D;
+    DevBuf<double> Pex;     // k-split partials of the first residual's exact product
     DevBuf<double2> cs, cd, bt, h, hacc, ycoef;
     DevBuf<float4> dpart;   // Gram-Schmidt dot partials per row chunk (double-FP32 re, im)
     DevBuf<float4> hdf;     // the update's coefficients (-Re h, Im h) in double-FP32
@@ -1210,8 +1257,14 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
             //       tensor cores' FP32-level accuracy suffices)
             // with x = xh + xl, xh = fl32(x)
             DSC_LAUNCH(k_split_f32_pair<<<4 * 152, 256, 0, st>>>(w.Xs.p, w.Xh.p, w.Xl.p, blk));
-            dim3 g((N + 63) / 64, (2 * F + 127) / 128);
-            DSC_LAUNCH(k_gemm_exact32<<<g, 512, 0, st>>>(s.K64.p, ld, w.Xh.p, ld, w.Y64.p, ld, N, 2 * F, N));
+            const int kchunk = ((N + kExSplits - 1) / kExSplits + kExBK - 1) / kExBK * kExBK;
+            const int nz = (N + kchunk - 1) / kchunk;
+            DSC_TRY(w.Pex.alloc(blk * nz));
+            dim3 g((N + 63) / 64, (2 * F + 127) / 128, nz);
+            DSC_LAUNCH(k_gemm_exact32<<<g, 512, 0, st>>>(s.K64.p, ld, w.Xh.p, ld, w.Pex.p, ld, blk, N, 2 * F, N,
+                                                         kchunk));
+            DSC_LAUNCH(k_sum_exact_splits<<<dim3((N + 255) / 256, 2 * F), 256, 0, st>>>(w.Pex.p, nz, blk, ld, N,
+                                                                                       w.Y64.p, ld));
             tm->add_work(kTResidual, (double)N * N * 2 * F);  // FP64-accurate multiply-adds
             DSC_TRY(split_cols_f16(w.Xl.p, ld, N, 2 * F, w.Vh.p, w.Vl.p, ld, w.cscX.p, st));
             DSC_TRY(tc_gemm_3xf16(s.Kh16.p, s.Kl16.p, ld, w.Vh.p, w.Vl.p, ld, N, 2 * F, N, w.Yp.p, ld, w.S,
@@ -1323,7 +1376,11 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
     if (sigma_host) {
         // the solution with Re / Im halves, as the reference's vB: column c
         // of Xs (2f = Re, 2f + 1 = Im of frequency f) is row c of the
-        // caller's F x 2N array, so one strided copy moves them all
+        // caller's F x 2N array, so one strided copy moves them all.  The
+        // caller's pages are written once on the host first, while the
+        // field kernels run: a device-to-host copy into pages never touched
+        // (fresh pageable memory) runs several times slower.
+        memset(sigma_host, 0, (size_t)F * 2 * N * sizeof(double));
         DSC_CUDA(cudaMemcpy2DAsync(sigma_host, (size_t)N * sizeof(double), w.Xs.p, ld * sizeof(double),
                                    (size_t)N * sizeof(double), (size_t)2 * F, cudaMemcpyDeviceToHost, st));
     }
