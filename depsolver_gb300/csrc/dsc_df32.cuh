@@ -104,6 +104,23 @@ __device__ __forceinline__ float2 df_from(double v)
 
 __device__ __forceinline__ double df_to(float2 a) { return (double)a.x + (double)a.y; }
 
+// a = hi + lo with hi = (float)a (round to nearest; one FP64-pipe
+// conversion) and lo = a - hi (exact in FP64, at most 2^-24 |a|) rounded to
+// FP32, without further FP64 operations: the difference of the two
+// significands, in units of a's last place, fits in 29 bits and equals the
+// low word of a minus hi's low three significand bits shifted to a's
+// weights (two's complement, also when rounding carried into the next
+// binade).  lo is 0 for |a| below 2^-74.
+__device__ __forceinline__ void f64_split_rn(double a, float &hi, float &lo)
+{
+    hi = (float)a;
+    const unsigned hw = (unsigned)__double2hiint(a), lw = (unsigned)__double2loint(a);
+    const int E = (int)((hw >> 20) & 0x7FFu);                          // biased FP64 exponent
+    const int d = (int)(lw - ((__float_as_uint(hi) & 7u) << 29));    // a - hi in units of 2^(E - 1075)
+    const float m = (float)(((int)hw < 0) ? -d : d);                   // with a's sign
+    lo = E >= 949 ? m * __int_as_float((E - 1075 + 127) << 23) : 0.0f;
+}
+
 // Warp-wide sum of accumulators (fixed shuffle order).
 __device__ __forceinline__ float2 df_warp_sum(float2 v)
 {

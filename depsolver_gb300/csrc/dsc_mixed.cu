@@ -40,7 +40,7 @@ constexpr double kInnerTol = 3e-7;
 
 // P[z] (M x Nc, FP64) = the part over k-split z of fl32(A) (M x Kd) * B
 // (Kd x Nc), column-major: A is FP64 and rounded to FP32 as it is staged
-// (one conversion per element on the FP64 pipe), B is FP32; every product
+// (one conversion per element), B is FP32; every product
 // is exact (p = a*b and e = fma(a, b, -p)) and the running sum is an
 // unevaluated pair (s, c) kept exact by TwoSum: about 2^-46 of the sum of
 // |a b|.  The parts of A and of the true B below FP32 are small (2^-24
@@ -1006,66 +1006,75 @@ int Session::make_k16()
     return kOk;
 }
 
-// One row of the epilogue: writes and returns (Re w, Im w).
-__device__ __forceinline__ float2 epilogue_row_impl(const float *__restrict__ P, int S, size_t split_stride,
-                                                    const float2 *__restrict__ V,
-                                                    const float2 *__restrict__ cs,
-                                                    const float2 *__restrict__ cd,
-                                                    float2 *__restrict__ W, int N, size_t ld, int f, int i)
-{
-    const float *pr = P + (size_t)(2 * f) * ld + i, *pi = pr + ld;
-    float2 yr = make_float2(0.f, 0.f), yi = make_float2(0.f, 0.f);
-    // the partials' loads four splits at a time, ahead of the additions
-    for (int s0 = 0; s0 < S; s0 += 4) {
-        float u[4], v[4];
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            const size_t o = (size_t)min(s0 + q, S - 1) * split_stride;
-            u[q] = pr[o];
-            v[q] = pi[o];
-        }
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            if (s0 + q >= S) break;
-            const float2 a = df_two_sum(yr.x, u[q]);
-            const float2 b = df_two_sum(yi.x, v[q]);
-            yr = make_float2(a.x, yr.y + a.y);
-            yi = make_float2(b.x, yi.y + b.y);
-        }
-    }
-    const float ar = yr.x + yr.y, ai = yi.x + yi.y;
-    const float vr = V[(size_t)(2 * f) * ld + i].x, vi = V[(size_t)(2 * f + 1) * ld + i].x;
-    const float2 s = cs[(size_t)f * N + i], d = cd[(size_t)f * N + i];
-    const float wr = s.x * ar - s.y * ai + d.x * vr - d.y * vi;
-    const float wi = s.x * ai + s.y * ar + d.x * vi + d.y * vr;
-    W[(size_t)(2 * f) * ld + i] = make_float2(wr, 0.f);
-    W[(size_t)(2 * f + 1) * ld + i] = make_float2(wi, 0.f);
-    return make_float2(wr, wi);
-}
-
 // w_f = cs_f o (sum of the split partials of K v)_f + cd_f o v_f, in FP32
 // (the product itself is FP32-accurate): the partials are added with
-// TwoSum compensation, the coefficients are FP32 copies.  W is written as
-// double-FP32 with a zero low part; npart[f][block] = the block's share of
-// |w_f|^2 (k_norm_finish adds them).
+// TwoSum compensation, the coefficients are FP32 copies.  Two rows per
+// thread (8-byte loads of the partials, all splits' loads issued four at a
+// time ahead of the additions).  W is written as double-FP32 with a zero
+// low part; npart[f][block] = the block's share of |w_f|^2 (k_norm_finish
+// adds them).  Row N (a padding row, when N is odd) is neither stored nor
+// counted.
 __global__ void __launch_bounds__(256) k_apply_epilogue_splits(
     const float *__restrict__ P, int S, size_t split_stride, const float2 *__restrict__ V,
     const float2 *__restrict__ cs, const float2 *__restrict__ cd, float2 *__restrict__ W, int N,
     size_t ld, int F, double *__restrict__ npart)
 {
     __shared__ float2 sh[8];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     const int f = blockIdx.y;
     float2 n2 = make_float2(0.f, 0.f);
     if (i < N) {
-        const float2 wv = epilogue_row_impl(P, S, split_stride, V, cs, cd, W, N, ld, f, i);
-        df_mac(n2, make_float2(wv.x, 0.f), make_float2(wv.x, 0.f));
-        df_mac(n2, make_float2(wv.y, 0.f), make_float2(wv.y, 0.f));
+        const float *pr = P + (size_t)(2 * f) * ld + i, *pi = pr + ld;
+        float2 yr0 = make_float2(0.f, 0.f), yr1 = yr0, yi0 = yr0, yi1 = yr0;
+        for (int s0 = 0; s0 < S; s0 += 4) {
+            float2 u[4], v[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const size_t o = (size_t)min(s0 + q, S - 1) * split_stride;
+                u[q] = *(const float2 *)(pr + o);
+                v[q] = *(const float2 *)(pi + o);
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                if (s0 + q >= S) break;
+                float2 a = df_two_sum(yr0.x, u[q].x);
+                yr0 = make_float2(a.x, yr0.y + a.y);
+                a = df_two_sum(yr1.x, u[q].y);
+                yr1 = make_float2(a.x, yr1.y + a.y);
+                a = df_two_sum(yi0.x, v[q].x);
+                yi0 = make_float2(a.x, yi0.y + a.y);
+                a = df_two_sum(yi1.x, v[q].y);
+                yi1 = make_float2(a.x, yi1.y + a.y);
+            }
+        }
+        const float4 vr = *(const float4 *)(V + (size_t)(2 * f) * ld + i);
+        const float4 vi = *(const float4 *)(V + (size_t)(2 * f + 1) * ld + i);
+        const bool two = i + 1 < N;
+        const float2 s0 = cs[(size_t)f * N + i], d0 = cd[(size_t)f * N + i];
+        const float2 s1 = two ? cs[(size_t)f * N + i + 1] : make_float2(0.f, 0.f);
+        const float2 d1 = two ? cd[(size_t)f * N + i + 1] : make_float2(0.f, 0.f);
+        const float ar0 = yr0.x + yr0.y, ai0 = yi0.x + yi0.y;
+        const float ar1 = yr1.x + yr1.y, ai1 = yi1.x + yi1.y;
+        const float wr0 = s0.x * ar0 - s0.y * ai0 + d0.x * vr.x - d0.y * vi.x;
+        const float wi0 = s0.x * ai0 + s0.y * ar0 + d0.x * vi.x + d0.y * vr.x;
+        const float wr1 = s1.x * ar1 - s1.y * ai1 + d1.x * vr.z - d1.y * vi.z;
+        const float wi1 = s1.x * ai1 + s1.y * ar1 + d1.x * vi.z + d1.y * vr.z;
+        float2 *wr = W + (size_t)(2 * f) * ld + i, *wi = wr + ld;
+        df_mac(n2, make_float2(wr0, 0.f), make_float2(wr0, 0.f));
+        df_mac(n2, make_float2(wi0, 0.f), make_float2(wi0, 0.f));
+        if (two) {
+            *(float4 *)wr = make_float4(wr0, 0.f, wr1, 0.f);
+            *(float4 *)wi = make_float4(wi0, 0.f, wi1, 0.f);
+            df_mac(n2, make_float2(wr1, 0.f), make_float2(wr1, 0.f));
+            df_mac(n2, make_float2(wi1, 0.f), make_float2(wi1, 0.f));
+        } else {
+            *wr = make_float2(wr0, 0.f);
+            *wi = make_float2(wi0, 0.f);
+        }
     }
     const double t = df_block_sum(n2, sh);
     if (threadIdx.x == 0) npart[(size_t)f * gridDim.x + blockIdx.x] = t;
 }
-
 
 // Per system f and row i, from the interface coefficients of the batch
 // (Ak, Bk: F x nIf; src/assembly_el.c:223-239): s = a - i b (1 on conductor
@@ -1185,11 +1194,12 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
             }
             {
                 TimerScope ts(tm, kTKrylov, st);
-                DSC_LAUNCH(k_apply_epilogue_splits<<<vg, 256, 0, st>>>(w.Yp.p, w.S, ld * 2 * (size_t)F, vj,
+                const dim3 eg((N + 511) / 512, F);  // two rows per thread
+                DSC_LAUNCH(k_apply_epilogue_splits<<<eg, 256, 0, st>>>(w.Yp.p, w.S, ld * 2 * (size_t)F, vj,
                                                                        w.cs32.p, w.cd32.p, w.W.p, N, ld, F,
                                                                        w.npart.p));
                 DSC_CUDA(cudaMemsetAsync(w.hacc.p, 0, (size_t)(j + 1) * F * sizeof(double2), st));
-                DSC_LAUNCH(k_norm_finish<<<(F * 32 + 255) / 256, 256, 0, st>>>(w.npart.p, (int)vg.x, F, w.active.p,
+                DSC_LAUNCH(k_norm_finish<<<(F * 32 + 255) / 256, 256, 0, st>>>(w.npart.p, (int)eg.x, F, w.active.p,
                                                                                 w.nrm0.p, nullptr, nullptr));
             }
             // classical Gram-Schmidt; the second pass only for the systems

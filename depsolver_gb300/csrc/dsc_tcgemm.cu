@@ -29,6 +29,8 @@
 #include <cudaTypedefs.h>
 #include <cuda_fp16.h>
 
+#include "dsc_async.cuh"
+#include "dsc_df32.cuh"
 #include "dsc_internal.h"
 #include "dsc_tcgemm.h"
 
@@ -52,51 +54,7 @@ constexpr int kTcThreads = 32 * (2 + kTcSplitWarps + 4);
 // 3 stages of 2 x 16 KB (A) + 2 x BN x 128 B (B) fit the 227 KB of shared
 // memory a CTA may use for BN <= 160
 constexpr int kTcMaxNc = 160;
-constexpr long long kTcSpin = 4000000000LL;  // clock cycles before a wait gives up
-
-__device__ __forceinline__ uint32_t su32(const void *p)
-{
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *b, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(b)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *b, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(b)), "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try(uint64_t *b, uint32_t parity)
-{
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(su32(b)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// Bounded wait for the phase of parity `parity`; false (and *err = code)
-// after kTcSpin cycles or when another thread has already failed.
-__device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, int *err, int code)
-{
-    const long long t0 = clock64();
-    while (!mbar_try(b, parity)) {
-        if (*(volatile int *)err) return false;
-        if (clock64() - t0 > kTcSpin) {
-            atomicCAS(err, 0, code);
-            return false;
-        }
-    }
-    return true;
-}
+constexpr long long kTcSpin = kSpin;  // clock cycles before a wait gives up
 
 __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar, int x,
                                             int y)
@@ -196,11 +154,6 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t *r)
           "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
         : "r"(taddr));
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive(uint64_t *b)
-{
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(b)) : "memory");
 }
 
 // The tf32 value the tensor core reads from an FP32 word: the top 19 bits
@@ -739,9 +692,10 @@ __global__ void k_row_scales(const int *__restrict__ rowE, int N, float *__restr
 
 // Column-major FP64 K to row-major fp16 pairs (entry (i, c) at i * ldt + c)
 // of 2^s_i fl32(K) (Th, Tl) and, with Dh not null, of 2^(s_i + 24) (K -
-// fl32(K)) (Dh, Dl): hi = rn_fp16(x), lo = rn_fp16(x - hi).  |K - fl32(K)|
-// <= 2^-24 |K| entrywise, so both scaled matrices stay below 2^15 (fp16's
-// largest finite value is 65504).  A
+// fl32(K)) (Dh, Dl) (f64_split_rn): hi = rn_fp16(x), lo = rn_fp16(x - hi).
+// |K - fl32(K)| <= 2^-24 |K| entrywise and each row's largest entry scales
+// below 2^15, so both scaled matrices stay below 2^15 (fp16's largest
+// finite value is 65504).  A
 // 32 x 32 shared tile per block.
 __global__ void k_split_transpose_f16(const double *__restrict__ K, size_t ld, int N,
                                       const int *__restrict__ rowE, __half *__restrict__ Th,
@@ -760,13 +714,14 @@ __global__ void k_split_transpose_f16(const double *__restrict__ K, size_t ld, i
         if (i < N && c < N) {
             const double a = t[threadIdx.x][k];
             const int sh = scale_shift(rowE[i], 1023);
-            const float v = (float)a;
+            float v, r;
+            f64_split_rn(a, v, r);  // a = v + r, v = fl32(a) (one FP64-pipe conversion)
             const float x = v * pow2f(sh);
             const __half h = __float2half_rn(x);
             Th[(size_t)i * ldt + c] = h;
             Tl[(size_t)i * ldt + c] = __float2half_rn(x - __half2float(h));
             if (Dh) {
-                const float y = (float)(a - (double)v) * pow2f(sh + 24);
+                const float y = r * pow2f(sh + 24);
                 const __half dh = __float2half_rn(y);
                 Dh[(size_t)i * ldt + c] = dh;
                 Dl[(size_t)i * ldt + c] = __float2half_rn(y - __half2float(dh));
