@@ -48,11 +48,20 @@ def peaks():
 
 # ------------------------------------------------------------------ roofline
 # Per kernel class: the bound, the unit, the scale from the library's work
-# count to that unit, the peak and where the peak comes from.  The tensor-core
-# product runs tf32, which issues at half the bf16 rate on this GPU.  The
-# mixed mode's regular-pair assembly runs double-FP32 on the FP32 pipes: it
-# is reported as (row, element) pairs per second with no single-number peak
-# (its FP32-pipe utilisation is in profiles/asm_regular_mid.md).
+# count to that unit, the peak and where the peak comes from.  The
+# tensor-core product (3xFP16, kind::f16 at the bf16 rate) is HBM-bound: its
+# work counter (flops of the three products) converts to the algorithmic
+# bytes of a product -- the fp16 pair of K (4 N^2), the operand pairs and the
+# FP32 result (8 F N each) -- and its tensor-pipe fraction is reported
+# beside.  The mixed mode's regular-pair assembly runs double-FP32 on the
+# FP32 pipes: it is reported as (row, element) pairs per second with no
+# single-number peak (its FP32-pipe utilisation is in
+# profiles/asm_regular_mid.md).
+
+
+def gemm_bytes_per_flop(N, F=None):
+    F = F or NFREQ
+    return (4.0 * N * N + 16.0 * F * N) / (12.0 * F * N * N)
 
 
 def roofline(timing, N, E):
@@ -63,8 +72,8 @@ def roofline(timing, N, E):
     if not hbm:
         hbm, bf16 = 6800.0, 1900.0
     models = {
-        "gemm_K": ("tensor", "TFLOP/s", 1e-12, bf16 / 2,
-                   f"{src} bf16_tflops / 2 (tf32 rate), of measured"),
+        "gemm_K": ("hbm", "GB/s", gemm_bytes_per_flop(N) * 1e-9, hbm,
+                   f"{src} hbm_gbs, of measured"),
         "gram_schmidt": ("hbm", "GB/s", 1e-9, hbm, f"{src} hbm_gbs, of measured"),
         "gemv_K64": ("hbm", "GB/s", 1e-9, hbm, f"{src} hbm_gbs, of measured"),
         "asm_regular": ("fp32-pipe", "Gpairs/s", 1e-9, None,
@@ -79,6 +88,11 @@ def roofline(timing, N, E):
                       "frac": ach / peak if peak else None, "traffic": TRAFFIC.get(k),
                       "peak_source": psrc,
                       "ms": ms, "scopes": cnt}
+            if k == "gemm_K":
+                tf = wk * 1e-12 / (ms / 1e3)
+                out[k]["tensor"] = {"achieved_tflops": tf, "peak_tflops": bf16,
+                                    "frac": tf / bf16 if bf16 else None,
+                                    "peak_source": f"{src} bf16_tflops (fp16 issues at the same rate)"}
     main = [k for k in out if out[k]["bound"] in ("hbm", "tensor")]
     dom = max(main, key=lambda k: out[k]["ms"]) if main else None
     return (out[dom] if dom else None), out
@@ -88,9 +102,9 @@ def roofline(timing, N, E):
 # workload (dram__bytes_read.sum + dram__bytes_write.sum); None where not
 # captured.  The summaries behind these numbers are under profiles/.
 TRAFFIC = {
-    # k_tc_gemm_3xtf32 at N = 17684, Nc = 128: 1284.7 MB read + 98.3 MB
-    # written (profiles/tc_gemm_3xtf32_mid.md)
-    "gemm_K": 1382973696,
+    # k_tc_gemm3<3> at N = 17684, Nc = 128: 1.28 GB read + 93.4 MB written
+    # (profiles/tc_gemm3_f16_cfg1.md)
+    "gemm_K": 1373360000,
 }
 
 
