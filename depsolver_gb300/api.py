@@ -108,7 +108,8 @@ def force_mst(sc: Scene, vB: np.ndarray, eps: float | None = None):
 MODE_FP64 = 1
 MODE_MIXED = 2
 TIMER_NAMES = ("asm_regular", "asm_fixup", "asm_singular", "gemv_K64", "gemm_K", "field", "mst",
-               "residual_fp64", "krylov", "gram_schmidt", "convert_K")
+               "residual_fp64", "krylov", "gram_schmidt", "convert_K", "precond_build",
+               "precond_apply")
 
 
 class Session:

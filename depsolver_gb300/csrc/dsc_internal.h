@@ -125,7 +125,7 @@ struct DevBuf {
 // the caller; off by default so that the plain entry points pay nothing).
 enum TimerId {
     kTAsmRegular = 0, kTAsmFixup, kTAsmSingular, kTGemvK, kTGemmK, kTField, kTMst, kTResidual,
-    kTKrylov, kTCgs, kTConvertK, kTCount
+    kTKrylov, kTCgs, kTConvertK, kTPreBuild, kTPreApply, kTCount
 };
 
 struct Timer {

@@ -965,6 +965,7 @@ struct Session::Mixed {
     DevBuf<__half> Vh, Vl;  // scaled fp16 pair of the current GEMM operand block
     DevBuf<float> cscK;     // column factors of the Krylov blocks' pairs (2^-14)
     DevBuf<float> cscX;     // column factors of the other operands' pairs
+    DevBuf<float> Z;        // P^-1 v of the current Krylov block (FP32)
     DevBuf<float> Yp;       // split-K partial products, S blocks
     DevBuf<int> err;        // set by the tensor-core kernel when a wait gives up
     DevBuf<double> Xs, R, Y64, D;
@@ -991,17 +992,20 @@ int Session::make_k16()
 {
     if (k16_ready && k64_ready) return kOk;
     DSC_TRY(assemble64(false));
-    TimerScope ts(&timer, kTConvertK, st);
-    DSC_TRY(Kh16.alloc(ld * N));
-    DSC_TRY(Kl16.alloc(ld * N));
-    DSC_TRY(dKh16.alloc(ld * N));
-    DSC_TRY(dKl16.alloc(ld * N));
-    DSC_TRY(rowE.alloc(N));
-    DSC_TRY(rsK.alloc(N));
-    DSC_TRY(rsdK.alloc(N));
-    DSC_TRY(k16_row_scales(K64.p, ld, N, rowE.p, rsK.p, rsdK.p, st));
-    DSC_TRY(split_transpose_K16(K64.p, ld, N, rowE.p, Kh16.p, Kl16.p, dKh16.p, dKl16.p, ld, st));
-    timer.add_work(kTConvertK, 16.0 * N * N);  // bytes: K read (8), four fp16 copies written (8)
+    {
+        TimerScope ts(&timer, kTConvertK, st);
+        DSC_TRY(Kh16.alloc(ld * N));
+        DSC_TRY(Kl16.alloc(ld * N));
+        DSC_TRY(dKh16.alloc(ld * N));
+        DSC_TRY(dKl16.alloc(ld * N));
+        DSC_TRY(rowE.alloc(N));
+        DSC_TRY(rsK.alloc(N));
+        DSC_TRY(rsdK.alloc(N));
+        DSC_TRY(k16_row_scales(K64.p, ld, N, rowE.p, rsK.p, rsdK.p, st));
+        DSC_TRY(split_transpose_K16(K64.p, ld, N, rowE.p, Kh16.p, Kl16.p, dKh16.p, dKl16.p, ld, st));
+        timer.add_work(kTConvertK, 16.0 * N * N);  // bytes: K read (8), four fp16 copies written (8)
+    }
+    DSC_TRY(precond_build(*this));
     k16_ready = true;
     return kOk;
 }
@@ -1122,6 +1126,8 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
     const size_t blk = ld * 2 * (size_t)F;  // one N x 2F block
     cudaStream_t st = s.st;
     Timer *tm = &s.timer;
+    const bool pre = s.pre && s.pre->nb > 0 && s.pre->ready;
+    if (pre) DSC_TRY(precond_reserve(s, F));
     // coefficients, complex Jacobi, scaled right-hand sides: on the device,
     // from the interface coefficients of each frequency
     const int nIfc = std::max(1, (int)s.nIf);
@@ -1185,11 +1191,19 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
         for (int j = 0; j < kInnerMax; j++) {
             const float2 *vj = w.Vb.p + (size_t)j * blk;
             float2 *vn = w.Vb.p + (size_t)(j + 1) * blk;
+            const float *csc = w.cscK.p;
+            if (pre) {
+                // right preconditioning: the product is K z with z = P^-1 v_j
+                DSC_TRY(precond_apply_v(s, vj, F, w.Z.p, w.cscK.p, w.err.p));
+                TimerScope ts(tm, kTPreApply, st);
+                DSC_TRY(split_cols_f16(w.Z.p, ld, N, 2 * F, w.Vh.p, w.Vl.p, ld, w.cscX.p, st));
+                csc = w.cscX.p;
+            }
             {
-                // the tf32 pair of v_j was written with v_j
+                // without preconditioning the fp16 pair of v_j was written with v_j
                 TimerScope ts(tm, kTGemmK, st);
                 DSC_TRY(tc_gemm_3xf16(s.Kh16.p, s.Kl16.p, ld, w.Vh.p, w.Vl.p, ld, N, 2 * F, N, w.Yp.p, ld,
-                                      w.S, w.err.p, st, s.rsK.p, w.cscK.p));
+                                      w.S, w.err.p, st, s.rsK.p, csc));
                 tm->add_work(kTGemmK, 6.0 * N * N * 2 * F);  // three tf32 products
             }
             {
@@ -1256,8 +1270,9 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
         DSC_CUDA(cudaStreamSynchronize(st));
         for (int f = 0; f < F; f++)
             if (act[f]) total_it[f] += mf[f];
-        // correction d = V y, then x += d
+        // correction d = P^-1 V y, then x += d
         DSC_LAUNCH(k_update_solution<<<vg, 256, 0, st>>>(w.D.p, w.Vb.p, blk, N, ld, F, w.ycoef.p, w.mcount.p));
+        if (pre) DSC_TRY(precond_apply_d(s, w.D.p, F, w.err.p));
         DSC_LAUNCH(k_axpy_blocks<<<vg, 256, 0, st>>>(w.Xs.p, w.D.p, N, ld, F));
         if (outer == 0) {
             // the first residual in FP64: r = bt - M x
@@ -1426,6 +1441,7 @@ int Session::solve_mixed(unsigned nfreq, const double *freqs, double tol, unsign
         DSC_TRY(w.Vl.alloc(blk));
         DSC_TRY(w.cscK.alloc(2 * (size_t)Fmax));
         DSC_TRY(w.cscX.alloc(2 * (size_t)Fmax));
+        DSC_TRY(w.Z.alloc(blk));
         {
             std::vector<float> c(2 * (size_t)Fmax, 1.0f / kVScale);
             DSC_TRY(w.cscK.upload(c, st));

@@ -1,0 +1,65 @@
+// dsc_precond.h -- conductor-block right preconditioner of the mixed sweep
+// (not exported).
+//
+// Conductor rows (boundary type 1: a fixed potential) carry the first-kind
+// single-layer equations of the electrodes; their part of every system's
+// matrix is the same at every frequency (s = 1, d = 0) and, after the
+// Jacobi scaling, is the real block D_E^-1 K_EE.  That block is what makes
+// GMRES slow (its condition number grows with the mesh), while the
+// interface rows form a second-kind equation.  The preconditioner is
+// P^-1 = blockdiag(X_1, ..., X_m, I): X_b the inverse of the scaled block
+// of one connected electrode (Gauss-Jordan in FP32 on the device, once per
+// assembly of K), I on the interface rows.  It is applied on the right:
+// GMRES runs on M P^-1 and the correction is P^-1 (V y), so the solution
+// stays that of M; the inverse only needs to be good enough to cluster the
+// spectrum (an fp16-accurate one already does).
+#pragma once
+
+#include <cuda_fp16.h>
+
+#include <vector>
+
+#include "dsc_internal.h"
+
+namespace dsc {
+
+struct Session;
+
+struct Precond {
+    int nb = 0;                       // blocks (connected electrodes)
+    std::vector<int> n, ldx, nbk;     // rows, padded size (multiple of 128), 128-blocks
+    std::vector<size_t> xoff;         // block b's ldx^2 matrix in X, Xh, Xl
+    std::vector<size_t> noff;         // block b's rows in `nodes`, `rs`
+    std::vector<size_t> toff;         // block b's 128 x ldx temporaries in tR, tC
+    std::vector<int> S;               // split count of block b's product
+    std::vector<size_t> yoff;         // block b's partial tiles in Y
+    std::vector<size_t> boff;         // block b's operand pairs in Bh, Bl, G
+    int F = 0;                        // systems the apply workspace is sized for
+    DevBuf<int> nodes;                // rows of each block, ascending
+    DevBuf<int> rblk, rpos;           // per row: its block (-1: none) and position
+    DevBuf<float> X;                  // scaled blocks, inverted in place
+    DevBuf<__half> Xh, Xl;            // the inverses as row-scaled fp16 pairs
+    DevBuf<float> rs;                 // their row factors
+    DevBuf<float> tP, tR, tC;         // Gauss-Jordan temporaries
+    DevBuf<__half> Bh, Bl;            // gathered operands (2F x ldx per block)
+    DevBuf<double> G;                 // gathered corrections (FP64)
+    DevBuf<float> csc;                // column factors of gathered corrections
+    DevBuf<float> Y;                  // split partials of the block products
+    DevBuf<long long> yinfo;          // per block: Y offset, split stride, S (device copy)
+    bool ready = false;               // the inverses match the current K
+};
+
+// Blocks from the mesh and the conductor rows (once per session; no blocks
+// when the scene has no conductor rows).
+int precond_plan(Session &s);
+// The inverses for the current K64 (after each assembly).
+int precond_build(Session &s);
+// Workspace of the apply calls for F systems.
+int precond_reserve(Session &s, int F);
+// Z (FP32, column c at c * ld, rows < N) = P^-1 v for the 2F columns of the
+// double-FP32 block V (Re, Im of each system; |v| <= 1: unit vectors).
+int precond_apply_v(Session &s, const float2 *V, int F, float *Z, const float *cscK, int *d_err);
+// D (FP64, 2F columns) = P^-1 D in place.
+int precond_apply_d(Session &s, double *D, int F, int *d_err);
+
+}  // namespace dsc

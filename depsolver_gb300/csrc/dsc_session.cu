@@ -167,14 +167,19 @@ int Session::create(int nen_, unsigned N_, unsigned E_, const double *nodes, con
     DSC_TRY(dev.upload(plan, st));
     DSC_TRY(force.build(plan, bctype.data(), st));
     ld = ((size_t)N + 31) / 32 * 32;
+    pre = new Precond();
+    DSC_TRY(precond_plan(*this));
     return kOk;
 }
 
 void destroy_mixed(Session::Mixed *m);
+void destroy_precond(Precond *p);
 
 Session::~Session()
 {
-    if (mx) destroy_mixed(mx);  // the stream itself goes last (StreamGuard)
+    // the stream itself goes last (StreamGuard)
+    if (mx) destroy_mixed(mx);
+    if (pre) destroy_precond(pre);
 }
 
 int Session::assemble64(bool need_fp64)
@@ -182,7 +187,8 @@ int Session::assemble64(bool need_fp64)
     // a K assembled in FP64 serves both modes; one assembled in
     // double-FP32 serves the mixed mode only
     if (k64_ready && (!need_fp64 || !k64_df32)) return kOk;
-    k16_ready = false;  // the fp16 copies follow K
+    k16_ready = false;  // the fp16 copies and the preconditioner follow K
+    if (pre) pre->ready = false;
     DSC_TRY(K64.alloc(ld * N));
     DSC_TRY(assemble_K_fp64(dev, K64.p, ld, st, &timer, !need_fp64, &asm_ws));
     k64_df32 = !need_fp64;

@@ -7,6 +7,7 @@
 
 #include "dsc_field.h"
 #include "dsc_internal.h"
+#include "dsc_precond.h"
 
 namespace dsc {
 
@@ -61,6 +62,8 @@ struct Session {
     DevBuf<float> rsK, rsdK;    // 2^-s_i, 2^-(s_i + 24)
     struct Mixed;
     Mixed *mx = nullptr;
+    // conductor-block right preconditioner of the mixed sweep
+    Precond *pre = nullptr;
 
     int create(int nen, unsigned N, unsigned E, const double *nodes, const unsigned *elems,
                const unsigned *bctype, const double *mbc, unsigned nIf, const unsigned *ifaces,

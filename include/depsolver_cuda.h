@@ -206,7 +206,9 @@ int dsc_session_solve(dsc_session *s, int mode, unsigned nfreq, const double *fr
  *       7 FP64-accurate residual GEMM    multiply-adds
  *       8 other Krylov kernels           0
  *       9 Gram-Schmidt passes            bytes the kernels read and wrote
- *      10 K to its fp16 pairs (mixed)    bytes read and written */
+ *      10 K to its fp16 pairs (mixed)    bytes read and written
+ *      11 conductor-block inverses       flops of the Gauss-Jordan updates
+ *      12 conductor-block products       flops of the three fp16 products */
 int dsc_session_set_timing(dsc_session *s, int on);
 /* The CUDA stream (cudaStream_t) all of the session's work runs on, so a
  * caller can record its own events around a solve. */
