@@ -102,197 +102,231 @@ int precond_plan(Session &s)
 }
 
 // ----------------------------------------------------------- Gauss-Jordan
+//
+// Blocked Gauss-Jordan without pivoting on the padded, Jacobi-scaled block
+// (column-major FP32, ldx a multiple of 128; the padding is the identity).
+// Step k: P = inverse of the diagonal block (one CTA in shared memory);
+// R_J = P X_kJ becomes row block k (X_kk = P); every other tile takes
+// X_IJ -= X_Ik R_J and X_Ik = -X_Ik P -- the update runs on the tensor
+// cores (3xFP16 on scaled fp16 pairs of the old column block and of R^T,
+// tc_gj_update_f16), everything else on the FP32 pipes.
 
 struct GJArgs {
     float *X[kPreMaxBlocks];
     float *tP[kPreMaxBlocks];
-    float *tR[kPreMaxBlocks];
-    float *tC[kPreMaxBlocks];
+    __half *Ah[kPreMaxBlocks], *Al[kPreMaxBlocks];  // ldx x 128: old column block, rows scaled
+    __half *Bh[kPreMaxBlocks], *Bl[kPreMaxBlocks];  // ldx x 128: R^T (P^T in tile k), rows scaled
+    float *ra[kPreMaxBlocks], *rb[kPreMaxBlocks];   // their row factors
     int ldx[kPreMaxBlocks];
     int nbk[kPreMaxBlocks];
 };
 
-// X[a][c] (row-major, ldx) = K(E[a], E[c]) / K(E[a], E[a]) for a, c < n (K
-// column-major FP64, rounded to FP32), the identity on the padding; 32 x 32
-// tiles through shared memory.
+// X[c * ldx + a] = K(E[a], E[c]) / K(E[a], E[a]) for a, c < n (K
+// column-major FP64, rounded to FP32), the identity on the padding.
 __global__ void k_pre_init(const double *__restrict__ K, size_t ld, const double *__restrict__ Kdiag,
                            const int *__restrict__ nodes, int n, float *__restrict__ X, int ldx)
 {
-    __shared__ float t[32][33];
-    const int a0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
-    {
-        const int a = a0 + threadIdx.x;
-        const float rd = a < n ? 1.0f / (float)Kdiag[nodes[a]] : 0.0f;
-        for (int y = threadIdx.y; y < 32; y += blockDim.y) {
-            const int c = c0 + y;
-            float v;
-            if (a < n && c < n) v = (float)K[(size_t)nodes[c] * ld + nodes[a]] * rd;
-            else v = (a == c) ? 1.0f : 0.0f;
-            t[y][threadIdx.x] = v;  // t[c - c0][a - a0]
-        }
-    }
-    __syncthreads();
-    for (int y = threadIdx.y; y < 32; y += blockDim.y) {
-        const int a = a0 + y, c = c0 + threadIdx.x;
-        X[(size_t)a * ldx + c] = t[threadIdx.x][y];
-    }
+    const int a = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
+    if (a >= ldx) return;
+    float v;
+    if (a < n && c < n) v = (float)K[(size_t)nodes[c] * ld + nodes[a]] * (1.0f / (float)Kdiag[nodes[a]]);
+    else v = (a == c) ? 1.0f : 0.0f;
+    X[(size_t)c * ldx + a] = v;
 }
 
-// tP = inverse of the 128 x 128 diagonal block k of each matrix
-// (Gauss-Jordan without pivoting in shared memory, one CTA per matrix).
-__global__ void __launch_bounds__(1024) k_gj_pivot(GJArgs g, int nb, int k)
+// tP = inverse of the 128 x 128 diagonal block k of each matrix, row-major
+// (Gauss-Jordan without pivoting, one CTA of 256 threads per matrix).  The
+// block lives in registers: thread (tr, tc) = (t / 16, t % 16) owns rows
+// 8 tr .. 8 tr + 7 and columns 8 tc .. 8 tc + 7.  Per pivot j: the owners of
+// column j publish it and replace it by the unit vector e_j; the owners of
+// row j scale it by 1 / a_jj and publish it (a_jj becomes the reciprocal);
+// then every thread takes a_rc -= a_rj a_jc (with a_jj's row left alone) on
+// its 64 entries without branches.  Shared rows and columns alternate
+// between two buffers by the parity of j: two barriers a pivot.
+__global__ void __launch_bounds__(256) k_gj_pivot(GJArgs g, int nb, int k)
 {
     const int b = blockIdx.x;
     if (b >= nb || k >= g.nbk[b]) return;
     const float *X = g.X[b];
     const int ldx = g.ldx[b];
-    extern __shared__ float sm[];
-    float *a = sm;                // 128 x 129
-    float *col = sm + kPB * 129;  // 128
-    for (int t = threadIdx.x; t < kPB * kPB; t += blockDim.x) {
-        const int r = t >> 7, c = t & 127;
-        a[r * 129 + c] = X[(size_t)(k * kPB + r) * ldx + k * kPB + c];
+    __shared__ __align__(16) float col[2][kPB], row[2][kPB];
+    const int tr = threadIdx.x >> 4, tc = threadIdx.x & 15;
+    float a[8][8];
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+        const float *src = X + (size_t)(k * kPB + 8 * tc + c) * ldx + k * kPB + 8 * tr;
+        const float4 lo = *(const float4 *)src, hi = *(const float4 *)(src + 4);
+        a[0][c] = lo.x; a[1][c] = lo.y; a[2][c] = lo.z; a[3][c] = lo.w;
+        a[4][c] = hi.x; a[5][c] = hi.y; a[6][c] = hi.z; a[7][c] = hi.w;
     }
-    __syncthreads();
     for (int j = 0; j < kPB; j++) {
-        if (threadIdx.x < kPB) col[threadIdx.x] = a[threadIdx.x * 129 + j];
-        __syncthreads();
-        const float piv = 1.0f / col[j];
-        if (threadIdx.x < kPB) {
-            const int c = threadIdx.x;
-            a[j * 129 + c] = (c == j) ? piv : a[j * 129 + c] * piv;
+        const int p = j & 1, jb = j >> 3, jo = j & 7;
+        if (tc == jb) {
+#pragma unroll
+            for (int c = 0; c < 8; c++) {
+                if (c != jo) continue;
+#pragma unroll
+                for (int i = 0; i < 8; i++) {
+                    col[p][8 * tr + i] = a[i][c];
+                    a[i][c] = (8 * tr + i == j) ? 1.0f : 0.0f;
+                }
+            }
         }
         __syncthreads();
-        for (int t = threadIdx.x; t < kPB * kPB; t += blockDim.x) {
-            const int r = t >> 7, c = t & 127;
-            if (r == j) continue;
-            const float f = col[r];
-            a[r * 129 + c] = (c == j) ? -f * piv : a[r * 129 + c] - f * a[j * 129 + c];
+        if (tr == jb) {
+            const float piv = __frcp_rn(col[p][j]);
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                if (i != jo) continue;
+#pragma unroll
+                for (int c = 0; c < 8; c++) {
+                    a[i][c] *= piv;
+                    row[p][8 * tc + c] = a[i][c];
+                }
+            }
         }
         __syncthreads();
+        const float4 f0 = *(const float4 *)&col[p][8 * tr], f1 = *(const float4 *)&col[p][8 * tr + 4];
+        const float4 r0 = *(const float4 *)&row[p][8 * tc], r1 = *(const float4 *)&row[p][8 * tc + 4];
+        float f[8] = {f0.x, f0.y, f0.z, f0.w, f1.x, f1.y, f1.z, f1.w};
+        const float rv[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            if (8 * tr + i == j) f[i] = 0.0f;
+#pragma unroll
+            for (int c = 0; c < 8; c++) a[i][c] = fmaf(-f[i], rv[c], a[i][c]);
+        }
     }
     float *P = g.tP[b];
-    for (int t = threadIdx.x; t < kPB * kPB; t += blockDim.x) P[t] = a[(t >> 7) * 129 + (t & 127)];
-}
-
-// acc (8 x 8 per thread: rows 8 ty + u, columns 8 tx + v of a 128 x 128
-// tile; 256 threads) = A (128 x 128, row-major, lda) * B (128 x 128,
-// row-major, ldb), k in chunks of 32 through shared memory.
-__device__ __forceinline__ void tile_gemm128(const float *__restrict__ A, int lda, const float *__restrict__ B,
-                                             int ldb, float (*As)[129], float (*Bs)[128], float acc[8][8])
-{
-    const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
 #pragma unroll
-    for (int u = 0; u < 8; u++)
-#pragma unroll
-        for (int v = 0; v < 8; v++) acc[u][v] = 0.0f;
-    for (int k0 = 0; k0 < kPB; k0 += 32) {
-        // A chunk: 128 rows x 32 k, stored transposed As[kk][row]
-#pragma unroll
-        for (int q = 0; q < 16; q++) {
-            const int t = tid + 256 * q, kk = t & 31, row = t >> 5;
-            As[kk][row] = A[(size_t)row * lda + k0 + kk];
-        }
-        // B chunk: 32 k x 128 columns
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            const int t = tid + 256 * q, kk = t >> 5, c4 = t & 31;
-            *(float4 *)&Bs[kk][4 * c4] = *(const float4 *)(B + (size_t)(k0 + kk) * ldb + 4 * c4);
-        }
-        __syncthreads();
-#pragma unroll 4
-        for (int kk = 0; kk < 32; kk++) {
-            float a[8], bv[8];
-#pragma unroll
-            for (int u = 0; u < 8; u++) a[u] = As[kk][8 * ty + u];
-            const float4 b0 = *(const float4 *)&Bs[kk][8 * tx], b1 = *(const float4 *)&Bs[kk][8 * tx + 4];
-            bv[0] = b0.x; bv[1] = b0.y; bv[2] = b0.z; bv[3] = b0.w;
-            bv[4] = b1.x; bv[5] = b1.y; bv[6] = b1.z; bv[7] = b1.w;
-#pragma unroll
-            for (int u = 0; u < 8; u++)
-#pragma unroll
-                for (int v = 0; v < 8; v++) acc[u][v] = fmaf(a[u], bv[v], acc[u][v]);
-        }
-        __syncthreads();
+    for (int i = 0; i < 8; i++) {
+        float *o = P + (size_t)(8 * tr + i) * kPB + 8 * tc;
+        *(float4 *)o = make_float4(a[i][0], a[i][1], a[i][2], a[i][3]);
+        *(float4 *)(o + 4) = make_float4(a[i][4], a[i][5], a[i][6], a[i][7]);
     }
 }
 
-constexpr size_t kTileSmem = sizeof(float) * (32 * 129 + 32 * 128);
+// Shift of a row whose largest magnitude has FP32 biased exponent e (see
+// scale_shift in the tensor-core product: largest entry to [2^14, 2^15)).
+__device__ __forceinline__ int pre_shift(int e) { return e == 0 ? 0 : max(-100, min(100, 14 - (e - 127))); }
 
-// Step k, per matrix: tR[:, J] = tP * X[row block k][column block J] (J != k)
-// for blockIdx.y = 0, tC[row block J][:] = X[row block J][column block k]
-// for blockIdx.y = 1.
+__device__ __forceinline__ float pre_pow2(int k) { return __int_as_float((127 + k) << 23); }
+
+// One 128-value row v[0..127] (in shared memory, stride 1) to a scaled fp16
+// pair at h, l and its factor; a warp per row.
+__device__ __forceinline__ void pre_row_pair(const float *v, __half *h, __half *l, float *factor)
+{
+    const int lane = threadIdx.x & 31;
+    int e = 0;
+#pragma unroll
+    for (int q = 0; q < 4; q++) e = max(e, (__float_as_int(v[lane + 32 * q]) >> 23) & 0xFF);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
+    const int sh = pre_shift(e);
+    const float f = pre_pow2(sh);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const float x = v[lane + 32 * q] * f;
+        const __half a = __float2half_rn(x);
+        h[lane + 32 * q] = a;
+        l[lane + 32 * q] = __float2half_rn(x - __half2float(a));
+    }
+    if (lane == 0) *factor = pre_pow2(-sh);
+}
+
+// Step k, per matrix: blockIdx.y = 0, tile J: R_J = P X_kJ (P itself for
+// J = k) written into row block k of X and, transposed, as the update's B
+// rows; blockIdx.y = 1, tile I != k: the old column block's rows as the
+// update's A rows (zero rows for I = k).  256 threads; the 128 x 128 tile in
+// shared memory ([row][col + 1]).
 __global__ void __launch_bounds__(256) k_gj_row(GJArgs g, int nb, int k)
 {
     const int b = blockIdx.z, J = blockIdx.x;
     if (b >= nb || k >= g.nbk[b] || J >= g.nbk[b]) return;
-    const float *X = g.X[b];
-    const int ldx = g.ldx[b];
-    if (blockIdx.y == 1) {
-        float *C = g.tC[b] + (size_t)J * kPB * kPB;
-        for (int t = threadIdx.x; t < kPB * kPB / 4; t += blockDim.x) {
-            const int r = t >> 5, c4 = t & 31;
-            *(float4 *)(C + (size_t)r * kPB + 4 * c4) =
-                *(const float4 *)(X + (size_t)(J * kPB + r) * ldx + k * kPB + 4 * c4);
-        }
-        return;
-    }
-    if (J == k) return;
-    extern __shared__ float sm[];
-    float(*As)[129] = (float(*)[129])sm;
-    float(*Bs)[128] = (float(*)[128])(sm + 32 * 129);
-    float acc[8][8];
-    tile_gemm128(g.tP[b], kPB, X + (size_t)k * kPB * ldx + J * kPB, ldx, As, Bs, acc);
-    const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
-    float *R = g.tR[b] + J * kPB;
-#pragma unroll
-    for (int u = 0; u < 8; u++) {
-        float *o = R + (size_t)(8 * ty + u) * ldx + 8 * tx;
-        *(float4 *)o = make_float4(acc[u][0], acc[u][1], acc[u][2], acc[u][3]);
-        *(float4 *)(o + 4) = make_float4(acc[u][4], acc[u][5], acc[u][6], acc[u][7]);
-    }
-}
-
-// Step k, per matrix and tile (I, J): row block k takes tR (and tP on the
-// diagonal); other rows X_IJ -= tC_I tR_J, and X_Ik = -tC_I tP.
-__global__ void __launch_bounds__(256) k_gj_update(GJArgs g, int nb, int k)
-{
-    const int b = blockIdx.z, I = blockIdx.y, J = blockIdx.x;
-    if (b >= nb || k >= g.nbk[b] || I >= g.nbk[b] || J >= g.nbk[b]) return;
     float *X = g.X[b];
     const int ldx = g.ldx[b];
-    float *T = X + (size_t)I * kPB * ldx + J * kPB;
-    if (I == k) {
-        const float *src = J == k ? g.tP[b] : g.tR[b] + J * kPB;
-        const int lds = J == k ? kPB : ldx;
-        for (int t = threadIdx.x; t < kPB * kPB / 4; t += blockDim.x) {
-            const int r = t >> 5, c4 = t & 31;
-            *(float4 *)(T + (size_t)r * ldx + 4 * c4) = *(const float4 *)(src + (size_t)r * lds + 4 * c4);
+    extern __shared__ float sm[];
+    float(*T)[129] = (float(*)[129])sm;  // T[r][c]
+    const int warp = threadIdx.x >> 5;
+    if (blockIdx.y == 1) {
+        // A rows: row i of tile J of column block k, A[i][kk] = X(J*128 + i, k*128 + kk)
+        __half *Ah = g.Ah[b] + (size_t)J * kPB * kPB, *Al = g.Al[b] + (size_t)J * kPB * kPB;
+        if (J == k) {
+            for (int t = threadIdx.x; t < kPB * kPB; t += blockDim.x) {
+                Ah[t] = __float2half_rn(0.0f);
+                Al[t] = __float2half_rn(0.0f);
+            }
+            if (threadIdx.x < kPB) g.ra[b][J * kPB + threadIdx.x] = 1.0f;
+            return;
         }
+        for (int t = threadIdx.x; t < kPB * kPB; t += blockDim.x) {
+            const int kk = t >> 7, i = t & 127;
+            T[i][kk] = X[(size_t)(k * kPB + kk) * ldx + J * kPB + i];
+        }
+        __syncthreads();
+        for (int i = warp; i < kPB; i += 8)
+            pre_row_pair(&T[i][0], Ah + (size_t)i * kPB, Al + (size_t)i * kPB, &g.ra[b][J * kPB + i]);
         return;
     }
-    extern __shared__ float sm[];
-    float(*As)[129] = (float(*)[129])sm;
-    float(*Bs)[128] = (float(*)[128])(sm + 32 * 129);
-    float acc[8][8];
-    const bool diag = J == k;
-    tile_gemm128(g.tC[b] + (size_t)I * kPB * kPB, kPB, diag ? g.tP[b] : g.tR[b] + J * kPB, diag ? kPB : ldx, As,
-                 Bs, acc);
-    const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
-#pragma unroll
-    for (int u = 0; u < 8; u++) {
-        float *o = T + (size_t)(8 * ty + u) * ldx + 8 * tx;
-        float4 p = *(const float4 *)o, q = *(const float4 *)(o + 4);
-        if (diag) {
-            p = make_float4(-acc[u][0], -acc[u][1], -acc[u][2], -acc[u][3]);
-            q = make_float4(-acc[u][4], -acc[u][5], -acc[u][6], -acc[u][7]);
-        } else {
-            p.x -= acc[u][0]; p.y -= acc[u][1]; p.z -= acc[u][2]; p.w -= acc[u][3];
-            q.x -= acc[u][4]; q.y -= acc[u][5]; q.z -= acc[u][6]; q.w -= acc[u][7];
+    // R_J[kk][j] = sum_q P[kk][q] X(k*128 + q, J*128 + j); T[j][kk] = R_J[kk][j]
+    const float *P = g.tP[b];
+    if (J == k) {
+        for (int t = threadIdx.x; t < kPB * kPB; t += blockDim.x) {
+            const int kk = t >> 7, j = t & 127;
+            T[j][kk] = P[t];
         }
-        *(float4 *)o = p;
-        *(float4 *)(o + 4) = q;
+    } else {
+        float(*Pt)[128] = (float(*)[128])(sm + kPB * 129);       // Pt[q][kk] = P[kk][q]
+        float(*Xs)[129] = (float(*)[129])(sm + kPB * 129 + kPB * 128);  // Xs[j][q] = X(k*128 + q, J*128 + j)
+        for (int t = threadIdx.x; t < kPB * kPB; t += blockDim.x) {
+            const int r = t >> 7, c = t & 127;
+            Pt[c][r] = P[t];
+            Xs[r][c] = X[(size_t)(J * kPB + r) * ldx + k * kPB + c];
+        }
+        __syncthreads();
+        // thread (ty, tx): kk = 8 ty + u, j = tx + 16 v (u, v < 8)
+        const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
+        float acc[8][8];
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+#pragma unroll
+            for (int v = 0; v < 8; v++) acc[u][v] = 0.0f;
+#pragma unroll 4
+        for (int q = 0; q < kPB; q++) {
+            const float4 p0 = *(const float4 *)&Pt[q][8 * ty], p1 = *(const float4 *)&Pt[q][8 * ty + 4];
+            const float pa[8] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w};
+            float xb[8];
+#pragma unroll
+            for (int v = 0; v < 8; v++) xb[v] = Xs[tx + 16 * v][q];
+#pragma unroll
+            for (int u = 0; u < 8; u++)
+#pragma unroll
+                for (int v = 0; v < 8; v++) acc[u][v] = fmaf(pa[u], xb[v], acc[u][v]);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+#pragma unroll
+            for (int v = 0; v < 8; v++) T[tx + 16 * v][8 * ty + u] = acc[u][v];
     }
+    __syncthreads();
+    // row block k of X takes R_J (P for J = k): X(k*128 + kk, J*128 + j)
+    for (int t = threadIdx.x; t < kPB * kPB; t += blockDim.x) {
+        const int j = t >> 7, kk = t & 127;
+        X[(size_t)(J * kPB + j) * ldx + k * kPB + kk] = T[j][kk];
+    }
+    __half *Bh = g.Bh[b] + (size_t)J * kPB * kPB, *Bl = g.Bl[b] + (size_t)J * kPB * kPB;
+    for (int jj = warp; jj < kPB; jj += 8)
+        pre_row_pair(&T[jj][0], Bh + (size_t)jj * kPB, Bl + (size_t)jj * kPB, &g.rb[b][J * kPB + jj]);
+}
+
+// Xt[r * ldx + c] = X[c * ldx + r] (32 x 32 tiles).
+__global__ void k_pre_transpose(const float *__restrict__ X, int ldx, float *__restrict__ Xt)
+{
+    __shared__ float t[32][33];
+    const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+    for (int y = threadIdx.y; y < 32; y += blockDim.y) t[y][threadIdx.x] = X[(size_t)(c0 + y) * ldx + r0 + threadIdx.x];
+    __syncthreads();
+    for (int y = threadIdx.y; y < 32; y += blockDim.y) Xt[(size_t)(r0 + y) * ldx + c0 + threadIdx.x] = t[threadIdx.x][y];
 }
 
 int precond_build(Session &s)
@@ -304,23 +338,28 @@ int precond_build(Session &s)
     const size_t xtot = pc.xoff.back() + (size_t)pc.ldx.back() * pc.ldx.back();
     const size_t ttot = pc.toff.back() + (size_t)kPB * pc.ldx.back();
     DSC_TRY(pc.X.alloc(xtot));
+    DSC_TRY(pc.Xt.alloc(xtot));
     DSC_TRY(pc.Xh.alloc(xtot));
     DSC_TRY(pc.Xl.alloc(xtot));
     DSC_TRY(pc.rs.alloc(pc.noff.back() + pc.n.back()));
     DSC_TRY(pc.tP.alloc((size_t)kPreMaxBlocks * kPB * kPB));
-    DSC_TRY(pc.tR.alloc(ttot));
-    DSC_TRY(pc.tC.alloc(ttot));
+    DSC_TRY(pc.gAh.alloc(ttot));
+    DSC_TRY(pc.gAl.alloc(ttot));
+    DSC_TRY(pc.gBh.alloc(ttot));
+    DSC_TRY(pc.gBl.alloc(ttot));
+    DSC_TRY(pc.gra.alloc(ttot / kPB));
+    DSC_TRY(pc.grb.alloc(ttot / kPB));
+    DSC_TRY(pc.err.alloc(1));
+    DSC_CUDA(cudaMemsetAsync(pc.err.p, 0, sizeof(int), st));
     double flops = 0.0;
     for (int b = 0; b < pc.nb; b++) {
-        const dim3 g(pc.ldx[b] / 32, pc.ldx[b] / 32);
-        DSC_LAUNCH(k_pre_init<<<g, dim3(32, 8), 0, st>>>(s.K64.p, s.ld, s.Kdiag.p, pc.nodes.p + pc.noff[b], pc.n[b],
-                                                         pc.X.p + pc.xoff[b], pc.ldx[b]));
+        const dim3 g((pc.ldx[b] + 255) / 256, pc.ldx[b]);
+        DSC_LAUNCH(k_pre_init<<<g, 256, 0, st>>>(s.K64.p, s.ld, s.Kdiag.p, pc.nodes.p + pc.noff[b], pc.n[b],
+                                                 pc.X.p + pc.xoff[b], pc.ldx[b]));
         flops += 2.0 * pc.ldx[b] * (double)pc.ldx[b] * pc.ldx[b];
     }
-    const size_t psmem = sizeof(float) * (kPB * 129 + kPB);
-    DSC_CUDA(cudaFuncSetAttribute(k_gj_pivot, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
-    DSC_CUDA(cudaFuncSetAttribute(k_gj_row, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem));
-    DSC_CUDA(cudaFuncSetAttribute(k_gj_update, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem));
+    const size_t rsmem = sizeof(float) * (2 * kPB * 129 + kPB * 128);
+    DSC_CUDA(cudaFuncSetAttribute(k_gj_row, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem));
     for (int b0 = 0; b0 < pc.nb; b0 += kPreMaxBlocks) {
         const int nb = std::min(kPreMaxBlocks, pc.nb - b0);
         GJArgs ga{};
@@ -329,25 +368,46 @@ int precond_build(Session &s)
             const int b = b0 + q;
             ga.X[q] = pc.X.p + pc.xoff[b];
             ga.tP[q] = pc.tP.p + (size_t)q * kPB * kPB;
-            ga.tR[q] = pc.tR.p + pc.toff[b];
-            ga.tC[q] = pc.tC.p + pc.toff[b];
+            ga.Ah[q] = pc.gAh.p + pc.toff[b];
+            ga.Al[q] = pc.gAl.p + pc.toff[b];
+            ga.Bh[q] = pc.gBh.p + pc.toff[b];
+            ga.Bl[q] = pc.gBl.p + pc.toff[b];
+            ga.ra[q] = pc.gra.p + pc.toff[b] / kPB;
+            ga.rb[q] = pc.grb.p + pc.toff[b] / kPB;
             ga.ldx[q] = pc.ldx[b];
             ga.nbk[q] = pc.nbk[b];
             nbk_max = std::max(nbk_max, pc.nbk[b]);
         }
+        std::vector<TcGjPlan> plans(nb);
+        for (int q = 0; q < nb; q++)
+            DSC_TRY(tc_gj_plan(plans[q], ga.Ah[q], ga.Al[q], kPB, ga.Bh[q], ga.Bl[q], kPB, ga.ldx[q], ga.ldx[q],
+                               ga.X[q], (size_t)ga.ldx[q], pc.err.p, ga.ra[q], ga.rb[q]));
         for (int k = 0; k < nbk_max; k++) {
-            DSC_LAUNCH(k_gj_pivot<<<nb, 1024, psmem, st>>>(ga, nb, k));
-            DSC_LAUNCH(k_gj_row<<<dim3(nbk_max, 2, nb), 256, kTileSmem, st>>>(ga, nb, k));
-            DSC_LAUNCH(k_gj_update<<<dim3(nbk_max, nbk_max, nb), 256, kTileSmem, st>>>(ga, nb, k));
+            DSC_LAUNCH(k_gj_pivot<<<nb, 256, 0, st>>>(ga, nb, k));
+            DSC_LAUNCH(k_gj_row<<<dim3(nbk_max, 2, nb), 256, rsmem, st>>>(ga, nb, k));
+            for (int q = 0; q < nb; q++)
+                if (k < ga.nbk[q]) DSC_TRY(tc_gj_run(plans[q], k, st));
         }
     }
-    // the inverses as row-scaled fp16 pairs (rows of X are the K-major rows
-    // of the product's A operand; their factors are the epilogue's)
-    for (int b = 0; b < pc.nb; b++)
-        DSC_TRY(split_cols_f16(pc.X.p + pc.xoff[b], (size_t)pc.ldx[b], pc.n[b], pc.n[b], pc.Xh.p + pc.xoff[b],
-                               pc.Xl.p + pc.xoff[b], (size_t)pc.ldx[b], pc.rs.p + pc.noff[b], st));
+    // the inverses as row-scaled fp16 pairs for the products (X is
+    // column-major: its transpose's rows are X's columns; the products take
+    // X^T's rows as their A rows, so the transposed copy goes first)
+    for (int b = 0; b < pc.nb; b++) {
+        const int ldx = pc.ldx[b];
+        DSC_LAUNCH(k_pre_transpose<<<dim3(ldx / 32, ldx / 32), dim3(32, 8), 0, st>>>(pc.X.p + pc.xoff[b], ldx,
+                                                                                     pc.Xt.p + pc.xoff[b]));
+        DSC_TRY(split_cols_f16(pc.Xt.p + pc.xoff[b], (size_t)ldx, pc.n[b], pc.n[b], pc.Xh.p + pc.xoff[b],
+                               pc.Xl.p + pc.xoff[b], (size_t)ldx, pc.rs.p + pc.noff[b], st));
+    }
     s.timer.add_work(kTPreBuild, flops);
     DSC_CUDA(cudaGetLastError());
+    int herr = 0;
+    DSC_CUDA(cudaMemcpyAsync(&herr, pc.err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    DSC_CUDA(cudaStreamSynchronize(st));
+    if (herr) {
+        set_error("conductor-block inverse: a pipeline wait of the tensor-core update gave up (code %d)", herr);
+        return kErrCuda;
+    }
     pc.ready = true;
     return kOk;
 }

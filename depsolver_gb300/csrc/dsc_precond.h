@@ -30,17 +30,21 @@ struct Precond {
     std::vector<int> n, ldx, nbk;     // rows, padded size (multiple of 128), 128-blocks
     std::vector<size_t> xoff;         // block b's ldx^2 matrix in X, Xh, Xl
     std::vector<size_t> noff;         // block b's rows in `nodes`, `rs`
-    std::vector<size_t> toff;         // block b's 128 x ldx temporaries in tR, tC
+    std::vector<size_t> toff;         // block b's ldx x 128 Gauss-Jordan operands
     std::vector<int> S;               // split count of block b's product
     std::vector<size_t> yoff;         // block b's partial tiles in Y
     std::vector<size_t> boff;         // block b's operand pairs in Bh, Bl, G
     int F = 0;                        // systems the apply workspace is sized for
     DevBuf<int> nodes;                // rows of each block, ascending
     DevBuf<int> rblk, rpos;           // per row: its block (-1: none) and position
-    DevBuf<float> X;                  // scaled blocks, inverted in place
+    DevBuf<float> X;                  // scaled blocks (column-major), inverted in place
+    DevBuf<float> Xt;                 // the inverses transposed (row-major)
     DevBuf<__half> Xh, Xl;            // the inverses as row-scaled fp16 pairs
     DevBuf<float> rs;                 // their row factors
-    DevBuf<float> tP, tR, tC;         // Gauss-Jordan temporaries
+    DevBuf<float> tP;                 // Gauss-Jordan pivot-block inverses
+    DevBuf<__half> gAh, gAl, gBh, gBl;  // Gauss-Jordan update operands (fp16 pairs)
+    DevBuf<float> gra, grb;           // their row factors
+    DevBuf<int> err;                  // set when a wait of the update kernel gives up
     DevBuf<__half> Bh, Bl;            // gathered operands (2F x ldx per block)
     DevBuf<double> G;                 // gathered corrections (FP64)
     DevBuf<float> csc;                // column factors of gathered corrections

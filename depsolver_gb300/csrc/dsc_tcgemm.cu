@@ -219,15 +219,19 @@ __device__ __forceinline__ float tf32_lo_biased(float s)
 // products out of the main accumulator: the tensor core's FP32 accumulation
 // truncates (sums of positive products come out low), so every MMA added
 // into an accumulator costs up to one of its units in the last place.
-template <int AMODE>
+template <int AMODE, bool GJ = false>
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_tc_gemm3(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
                const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl,
-               int M, int Nc, int BN, int nkb_total, int kb_per_split, int nsplit,
+               int M, int Nc, int BN, int ntn, int nkb_total, int kb_per_split, int nsplit,
                float *__restrict__ Y, size_t ldy, size_t split_stride, int tmem_cols,
                uint32_t acc_stride, const float *__restrict__ rsc, const float *__restrict__ csc,
-               int *err)
+               int gj_k, int *err)
 {
+    // ntn: column tiles of BN columns (1 unless the product is the
+    // Gauss-Jordan update); GJ selects that update's epilogue with gj_k:
+    // Y[column][row] -= the product (Y = -the product in column tile gj_k),
+    // row tile gj_k left alone.
     // acc_stride: TMEM columns of one accumulator buffer, a power of two of
     // at least the columns it holds (so each buffer's MMAs start aligned)
     constexpr bool SPLIT_A = AMODE == 1 || AMODE == 2;
@@ -247,7 +251,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     uint32_t *tmem_slot = (uint32_t *)(done + 1);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int tiles = (M + kTcBM - 1) / kTcBM;
-    const int units = tiles * nsplit;
+    const int units = tiles * ntn * nsplit;  // unit u: row tile u % tiles, then column tile, then split
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < kTcStages; s++) {
@@ -282,7 +286,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             uint32_t g = 0;
             bool ok = true;
             for (int u = blockIdx.x; ok && u < units; u += gridDim.x) {
-                const int m0 = (u % tiles) * kTcBM, kb0 = (u / tiles) * kb_per_split;
+                const int m0 = (u % tiles) * kTcBM, n0 = ((u / tiles) % ntn) * BN;
+                const int kb0 = (u / tiles / ntn) * kb_per_split;
                 const int nkb = min(nkb_total, kb0 + kb_per_split) - kb0;
                 for (int i = 0; i < nkb; i++, g++) {
                     const uint32_t s = g % kTcStages, n = g / kTcStages;
@@ -295,8 +300,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     const int kx = (kb0 + i) * BK;
                     tma_load_2d(st, &tmAh, &full[s], kx, m0);
                     if (!SPLIT_A) tma_load_2d(st + a_bytes, &tmAl, &full[s], kx, m0);
-                    tma_load_2d(st + 2 * a_bytes, &tmBh, &full[s], kx, 0);
-                    tma_load_2d(st + 2 * a_bytes + b_bytes, &tmBl, &full[s], kx, 0);
+                    tma_load_2d(st + 2 * a_bytes, &tmBh, &full[s], kx, n0);
+                    tma_load_2d(st + 2 * a_bytes + b_bytes, &tmBl, &full[s], kx, n0);
                 }
             }
             // drain: the last loads of every stage have landed before the CTA
@@ -316,7 +321,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             bool ok = true;
             int j = 0;
             for (int u = blockIdx.x; ok && u < units; u += gridDim.x, j++) {
-                const int kb0 = (u / tiles) * kb_per_split;
+                const int kb0 = (u / tiles / ntn) * kb_per_split;
                 const int nkb = min(nkb_total, kb0 + kb_per_split) - kb0;
                 const uint32_t buf = j & 1, q = j >> 1;
                 if (q > 0 && !mbar_wait(&acc_empty[buf], (q - 1) & 1, err, 5)) break;
@@ -371,7 +376,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             uint32_t g = 0;
             bool ok = true;
             for (int u = blockIdx.x; ok && u < units; u += gridDim.x) {
-                const int kb0 = (u / tiles) * kb_per_split;
+                const int kb0 = (u / tiles / ntn) * kb_per_split;
                 const int nkb = min(nkb_total, kb0 + kb_per_split) - kb0;
                 for (int i = 0; i < nkb; i++, g++) {
                     const uint32_t s = g % kTcStages, n = g / kTcStages;
@@ -408,7 +413,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         const int ew = warp & 3;
         int j = 0;
         for (int u = blockIdx.x; u < units; u += gridDim.x, j++) {
-            const int m0 = (u % tiles) * kTcBM, split = u / tiles;
+            const int tm = u % tiles, tn = (u / tiles) % ntn, split = u / tiles / ntn;
+            const int m0 = tm * kTcBM, n0 = tn * BN;
             const uint32_t buf = j & 1, q = j >> 1;
             bool have = mbar_wait(&acc_full[buf], q & 1, err, 3);
             // tcgen05.ld is warp-collective: the whole warp reads or none of it
@@ -427,14 +433,34 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
                     for (int t = 0; t < 32; t++) r[t] = __float_as_uint(__uint_as_float(r[t]) + __uint_as_float(r2[t]));
                 }
-                if (m < M) {
+                if (m < M && !GJ) {
 #pragma unroll
                     for (int t = 0; t < 32; t++) {
-                        const int n = c0 + t;
+                        const int n = n0 + c0 + t;
                         if (n < Nc) {
                             // powers of two: the scaling is exact
                             const float cn = csc ? csc[n] : 1.0f;
                             Ys[(size_t)n * ldy + m] = __uint_as_float(r[t]) * rs * cn;
+                        }
+                    }
+                } else if (m < M && tm != gj_k) {
+                    // 16 old values at a time first (independent loads in
+                    // flight together), then their stores
+#pragma unroll
+                    for (int h = 0; h < 32; h += 16) {
+                        float old[16];
+#pragma unroll
+                        for (int t = 0; t < 16; t++) {
+                            const int n = n0 + c0 + h + t;
+                            old[t] = (n < Nc && tn != gj_k) ? Ys[(size_t)n * ldy + m] : 0.0f;
+                        }
+#pragma unroll
+                        for (int t = 0; t < 16; t++) {
+                            const int n = n0 + c0 + h + t;
+                            if (n < Nc) {
+                                const float cn = csc ? csc[n] : 1.0f;
+                                Ys[(size_t)n * ldy + m] = old[t] - __uint_as_float(r[h + t]) * rs * cn;
+                            }
                         }
                     }
                 }
@@ -531,9 +557,11 @@ static int splits_for_bk(int M, int Kd, int bk)
 // Launch of the persistent kernel on encoded maps (bk: elements per k-block).
 static int tc_launch(int amode, const CUtensorMap &ah, const CUtensorMap &al, const CUtensorMap &bh,
                      const CUtensorMap &bl, int M, int Nc, int Kd, int bk, float *Y, size_t ldy, int splits,
-                     int *d_err, cudaStream_t st, const float *rsc, const float *csc)
+                     int *d_err, cudaStream_t st, const float *rsc, const float *csc, int gj_k = -1)
 {
-    const int BN = (Nc + 15) / 16 * 16;
+    // one column tile of all Nc columns, or tiles of 128 (the Gauss-Jordan update)
+    const int BN = gj_k >= 0 ? 128 : (Nc + 15) / 16 * 16;
+    const int ntn = (Nc + BN - 1) / BN;
     // two accumulator buffers of 2 BN (COMB) or BN columns, each rounded up
     // to a power of two
     uint32_t acc_stride = 32;
@@ -550,19 +578,29 @@ static int tc_launch(int amode, const CUtensorMap &ah, const CUtensorMap &al, co
         DSC_CUDA(cudaGetDevice(&dev));
         DSC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     }
-    const int units = (M + kTcBM - 1) / kTcBM * splits;
+    const int units = (M + kTcBM - 1) / kTcBM * ntn * splits;
     const dim3 grid(std::min(units, nsm));
-    auto launch = [&](auto kern) -> int {
-        DSC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        DSC_LAUNCH(kern<<<grid, kTcThreads, smem, st>>>(ah, al, bh, bl, M, Nc, BN, nkb, kps, splits, Y, ldy,
-                                                 ldy * (size_t)Nc, tmem_cols, acc_stride, rsc, csc, d_err));
+    // the shared-memory limit of each instantiation is raised to the largest
+    // request seen on the device (once per size, not per launch)
+    constexpr int kDevs = 16;
+    static int smem_set[kDevs][5] = {};
+    int dev = 0;
+    DSC_CUDA(cudaGetDevice(&dev));
+    auto launch = [&](auto kern, int slot) -> int {
+        if (dev >= kDevs || smem_set[dev][slot] < (int)smem) {
+            DSC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            if (dev < kDevs) smem_set[dev][slot] = (int)smem;
+        }
+        DSC_LAUNCH(kern<<<grid, kTcThreads, smem, st>>>(ah, al, bh, bl, M, Nc, BN, ntn, nkb, kps, splits, Y, ldy,
+                                                 ldy * (size_t)Nc, tmem_cols, acc_stride, rsc, csc, gj_k, d_err));
         return kOk;
     };
-    switch (amode) {
-    case 0: DSC_TRY(launch(k_tc_gemm3<0>)); break;
-    case 1: DSC_TRY(launch(k_tc_gemm3<1>)); break;
-    case 2: DSC_TRY(launch(k_tc_gemm3<2>)); break;
-    default: DSC_TRY(launch(k_tc_gemm3<3>)); break;
+    if (gj_k >= 0) DSC_TRY(launch(k_tc_gemm3<3, true>, 4));
+    else switch (amode) {
+    case 0: DSC_TRY(launch(k_tc_gemm3<0>, 0)); break;
+    case 1: DSC_TRY(launch(k_tc_gemm3<1>, 1)); break;
+    case 2: DSC_TRY(launch(k_tc_gemm3<2>, 2)); break;
+    default: DSC_TRY(launch(k_tc_gemm3<3>, 3)); break;
     }
     DSC_CUDA(cudaGetLastError());
     return kOk;
@@ -603,6 +641,45 @@ int tc_gemm_3xf16(const __half *Ah, const __half *Al, size_t lda, const __half *
     DSC_TRY(make_map(&bh, Bh, 2, Nc, Kd, ldb, BN));
     DSC_TRY(make_map(&bl, Bl, 2, Nc, Kd, ldb, BN));
     return tc_launch(3, ah, al, bh, bl, M, Nc, Kd, kTcBK16, Y, ldy, splits, d_err, st, rsc, csc);
+}
+
+struct TcGjPlan::Maps {
+    CUtensorMap ah, al, bh, bl;
+};
+
+TcGjPlan::~TcGjPlan() { delete maps; }
+
+int tc_gj_plan(TcGjPlan &p, const __half *Ah, const __half *Al, size_t lda, const __half *Bh,
+               const __half *Bl, size_t ldb, int M, int Nc, float *C, size_t ldc, int *d_err,
+               const float *rsc, const float *csc)
+{
+    if (M < 1 || Nc < 1 || ldc < (size_t)M) {
+        set_error("tc_gj_plan: unsupported shape M %d Nc %d", M, Nc);
+        return kErrArg;
+    }
+    if (!p.maps) p.maps = new TcGjPlan::Maps();
+    DSC_TRY(make_map(&p.maps->ah, Ah, 2, M, 128, lda, kTcBM));
+    DSC_TRY(make_map(&p.maps->al, Al, 2, M, 128, lda, kTcBM));
+    DSC_TRY(make_map(&p.maps->bh, Bh, 2, Nc, 128, ldb, 128));
+    DSC_TRY(make_map(&p.maps->bl, Bl, 2, Nc, 128, ldb, 128));
+    p.M = M;
+    p.Nc = Nc;
+    p.C = C;
+    p.ldc = ldc;
+    p.err = d_err;
+    p.rsc = rsc;
+    p.csc = csc;
+    return kOk;
+}
+
+int tc_gj_run(const TcGjPlan &p, int k, cudaStream_t st)
+{
+    if (!p.maps || k < 0) {
+        set_error("tc_gj_run: no plan or negative step");
+        return kErrArg;
+    }
+    return tc_launch(3, p.maps->ah, p.maps->al, p.maps->bh, p.maps->bl, p.M, p.Nc, 128, kTcBK16, p.C, p.ldc, 1,
+                     p.err, st, p.rsc, p.csc, k);
 }
 
 int tc_gemm_splits_for(int M, int Kd) { return splits_for_bk(M, Kd, kTcBK); }

@@ -31,6 +31,28 @@ int tc_gemm_3xf16(const __half *Ah, const __half *Al, size_t lda, const __half *
                   size_t ldb, int M, int Nc, int Kd, float *Y, size_t ldy, int splits, int *d_err,
                   cudaStream_t st, const float *rsc, const float *csc);
 int tc_gemm_f16_splits_for(int M, int Kd);
+// The Gauss-Jordan update of step k on the same kernel (3xFP16, K = 128):
+// for every 128 x 128 tile (I, J) of C (column-major, M x Nc, stride ldc)
+// with I != k: C_IJ -= A_I B_J^T (C_Ik = -A_I B_k^T); A (M x 128) and B
+// (Nc x 128) K-major scaled fp16 pairs with row factors rsc, csc.  The
+// operands' tensor maps are encoded once (tc_gj_plan) for all steps.
+struct TcGjPlan {
+    struct Maps;
+    Maps *maps = nullptr;
+    int M = 0, Nc = 0;
+    float *C = nullptr;
+    size_t ldc = 0;
+    int *err = nullptr;
+    const float *rsc = nullptr, *csc = nullptr;
+    TcGjPlan() = default;
+    TcGjPlan(const TcGjPlan &) = delete;
+    TcGjPlan &operator=(const TcGjPlan &) = delete;
+    ~TcGjPlan();
+};
+int tc_gj_plan(TcGjPlan &p, const __half *Ah, const __half *Al, size_t lda, const __half *Bh,
+               const __half *Bl, size_t ldb, int M, int Nc, float *C, size_t ldc, int *d_err,
+               const float *rsc, const float *csc);
+int tc_gj_run(const TcGjPlan &p, int k, cudaStream_t st);
 // Row scales of column-major FP64 K (stride ld): rowE (N ints, scratch) the
 // biased exponent of each row's largest entry, rsK = 2^-s_i, rsdK (may be
 // null) = 2^-(s_i + 24).
