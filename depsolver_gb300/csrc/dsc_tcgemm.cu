@@ -261,7 +261,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
         for (int b = 0; b < 2; b++) {
             mbar_init(&acc_full[b], 1);
-            mbar_init(&acc_empty[b], 4);  // one lane of each epilogue warp
+            // one lane of each epilogue warp (the Gauss-Jordan update's
+            // read-modify-write epilogue also runs on the splitter warps)
+            mbar_init(&acc_empty[b], GJ ? 4 + kTcSplitWarps : 4);
         }
         mbar_init(done, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -369,7 +371,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             }
             mma_commit(done);  // arrives when every MMA issued above has completed
         }
-    } else if (warp < 2 + kTcSplitWarps) {
+    } else if (warp < 2 + kTcSplitWarps && !GJ) {
         if (SPLIT_A) {
             // ---- splitters: the lo slot of each stage
             const int tid = threadIdx.x - 64;
@@ -409,8 +411,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             }
         }
     } else {
-        // ---- epilogue (the last 4 warps: TMEM lanes 32 (warp % 4) .. + 31 = rows)
+        // ---- epilogue (the last 4 warps: TMEM lanes 32 (warp % 4) .. + 31 =
+        // rows; for the Gauss-Jordan update warps 2 .. 9, two per lane
+        // group, each on half of the tile's columns)
+        static_assert(kTcSplitWarps == 4, "the Gauss-Jordan epilogue pairs the splitter and epilogue warps");
         const int ew = warp & 3;
+        const int cbeg = GJ && warp >= 2 + kTcSplitWarps ? BN / 2 : 0;
+        const int cend = GJ && warp < 2 + kTcSplitWarps ? BN / 2 : BN;
         int j = 0;
         for (int u = blockIdx.x; u < units; u += gridDim.x, j++) {
             const int tm = u % tiles, tn = (u / tiles) % ntn, split = u / tiles / ntn;
@@ -424,7 +431,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             const int m = m0 + ew * 32 + lane;
             const float rs = (rsc && m < M) ? rsc[m] : 1.0f;
             float *Ys = Y + (size_t)split * split_stride;
-            for (int c0 = 0; c0 < BN; c0 += 32) {
+            for (int c0 = cbeg; c0 < cend; c0 += 32) {
                 uint32_t r[32];
                 tmem_ld32(acc + (uint32_t)c0, r);
                 if (comb) {
