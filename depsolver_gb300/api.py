@@ -159,6 +159,17 @@ class Session:
     def set_timing(self, on: bool):
         _native.check(self._L.dsc_session_set_timing(self._h, int(on)))
 
+    def set_preconditioner(self, on: bool):
+        """Mixed mode: the conductor-block right preconditioner (default on)."""
+        _native.check(self._L.dsc_session_set_preconditioner(self._h, int(on)))
+
+    def preconditioner_blocks(self):
+        """Row counts of the preconditioner's blocks (one per electrode)."""
+        n = self._L.dsc_session_preconditioner_blocks(self._h, None, 0)
+        rows = np.zeros(max(n, 1), dtype=np.int32)
+        self._L.dsc_session_preconditioner_blocks(self._h, rows.ctypes.data, n)
+        return rows[:n].tolist()
+
     def timing(self):
         """{class: (ms, timed scopes, algorithmic work)} since the last call
         (work units per class in dsc_session_timing's header comment)."""

@@ -1005,7 +1005,7 @@ int Session::make_k16()
         DSC_TRY(split_transpose_K16(K64.p, ld, N, rowE.p, Kh16.p, Kl16.p, dKh16.p, dKl16.p, ld, st));
         timer.add_work(kTConvertK, 16.0 * N * N);  // bytes: K read (8), four fp16 copies written (8)
     }
-    DSC_TRY(precond_build(*this));
+    if (pre_on) DSC_TRY(precond_build(*this));
     k16_ready = true;
     return kOk;
 }
@@ -1126,7 +1126,8 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
     const size_t blk = ld * 2 * (size_t)F;  // one N x 2F block
     cudaStream_t st = s.st;
     Timer *tm = &s.timer;
-    const bool pre = s.pre && s.pre->nb > 0 && s.pre->ready;
+    if (s.pre_on) DSC_TRY(precond_build(s));  // no-op when built for this K
+    const bool pre = s.pre_on && s.pre && s.pre->nb > 0 && s.pre->ready;
     if (pre) DSC_TRY(precond_reserve(s, F));
     // coefficients, complex Jacobi, scaled right-hand sides: on the device,
     // from the interface coefficients of each frequency

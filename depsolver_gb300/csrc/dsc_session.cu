@@ -310,6 +310,20 @@ extern "C" int dsc_session_set_timing(dsc_session *s, int on)
     return kOk;
 }
 
+extern "C" int dsc_session_set_preconditioner(dsc_session *s, int on)
+{
+    s->s.pre_on = on != 0;
+    return kOk;
+}
+
+extern "C" int dsc_session_preconditioner_blocks(dsc_session *s, int *rows, int n)
+{
+    const Precond *p = s->s.pre;
+    const int nb = p ? p->nb : 0;
+    for (int b = 0; b < nb && b < n && rows; b++) rows[b] = p->n[b];
+    return nb;
+}
+
 extern "C" int dsc_session_timing(dsc_session *s, double *ms, int *count, double *work, int n)
 {
     double t[kTCount], wk[kTCount];

@@ -62,8 +62,10 @@ struct Session {
     DevBuf<float> rsK, rsdK;    // 2^-s_i, 2^-(s_i + 24)
     struct Mixed;
     Mixed *mx = nullptr;
-    // conductor-block right preconditioner of the mixed sweep
+    // conductor-block right preconditioner of the mixed sweep (pre_on: used
+    // by mixed solves)
     Precond *pre = nullptr;
+    bool pre_on = true;
 
     int create(int nen, unsigned N, unsigned E, const double *nodes, const unsigned *elems,
                const unsigned *bctype, const double *mbc, unsigned nIf, const unsigned *ifaces,

@@ -210,6 +210,16 @@ int dsc_session_solve(dsc_session *s, int mode, unsigned nfreq, const double *fr
  *      11 conductor-block inverses       flops of the Gauss-Jordan updates
  *      12 conductor-block products       flops of the three fp16 products */
 int dsc_session_set_timing(dsc_session *s, int on);
+/* The mixed mode's right preconditioner (on by default): the rows of each
+ * connected electrode (boundary type 1, a fixed potential) form a
+ * frequency-independent first-kind block whose inverse (Gauss-Jordan on
+ * the device after each assembly of K) is applied on the right, so GMRES
+ * converges in a few iterations while the solution stays that of the
+ * unpreconditioned system.  on = 0 solves with the complex Jacobi scaling
+ * alone.  dsc_session_preconditioner_blocks returns the number of blocks
+ * and writes up to n of their row counts to rows (may be NULL). */
+int dsc_session_set_preconditioner(dsc_session *s, int on);
+int dsc_session_preconditioner_blocks(dsc_session *s, int *rows, int n);
 /* The CUDA stream (cudaStream_t) all of the session's work runs on, so a
  * caller can record its own events around a solve. */
 void *dsc_session_stream(dsc_session *s);
