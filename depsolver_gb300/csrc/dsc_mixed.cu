@@ -965,7 +965,6 @@ struct Session::Mixed {
     DevBuf<__half> Vh, Vl;  // scaled fp16 pair of the current GEMM operand block
     DevBuf<float> cscK;     // column factors of the Krylov blocks' pairs (2^-14)
     DevBuf<float> cscX;     // column factors of the other operands' pairs
-    DevBuf<float> Z;        // P^-1 v of the current Krylov block (FP32)
     DevBuf<float> Yp;       // split-K partial products, S blocks
     DevBuf<int> err;        // set by the tensor-core kernel when a wait gives up
     DevBuf<double> Xs, R, Y64, D;
@@ -1193,13 +1192,8 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
             const float2 *vj = w.Vb.p + (size_t)j * blk;
             float2 *vn = w.Vb.p + (size_t)(j + 1) * blk;
             const float *csc = w.cscK.p;
-            if (pre) {
-                // right preconditioning: the product is K z with z = P^-1 v_j
-                DSC_TRY(precond_apply_v(s, vj, F, w.Z.p, w.cscK.p, w.err.p));
-                TimerScope ts(tm, kTPreApply, st);
-                DSC_TRY(split_cols_f16(w.Z.p, ld, N, 2 * F, w.Vh.p, w.Vl.p, ld, w.cscX.p, st));
-                csc = w.cscX.p;
-            }
+            if (pre)  // right preconditioning: the product is K z with z = P^-1 v_j
+                DSC_TRY(precond_apply_v(s, vj, F, w.Vh.p, w.Vl.p, w.cscK.p, w.err.p, &csc));
             {
                 // without preconditioning the fp16 pair of v_j was written with v_j
                 TimerScope ts(tm, kTGemmK, st);
@@ -1442,7 +1436,6 @@ int Session::solve_mixed(unsigned nfreq, const double *freqs, double tol, unsign
         DSC_TRY(w.Vl.alloc(blk));
         DSC_TRY(w.cscK.alloc(2 * (size_t)Fmax));
         DSC_TRY(w.cscX.alloc(2 * (size_t)Fmax));
-        DSC_TRY(w.Z.alloc(blk));
         {
             std::vector<float> c(2 * (size_t)Fmax, 1.0f / kVScale);
             DSC_TRY(w.cscK.upload(c, st));

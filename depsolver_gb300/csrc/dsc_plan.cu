@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <atomic>
 #include <numeric>
+#include <thread>
 
 #include "dsc_common.cuh"
 #include "dsc_field.h"
@@ -122,113 +123,10 @@ int set_rows(HostPlan &p, const unsigned *bctype)
     return kOk;
 }
 
-int build_plan(int nen, int N, int E, const double *nodes, const int *el,
-               const unsigned *bctype, HostPlan &p)
+// node -> elements containing it (element order, first position in the
+// element) and the nodes sorted by (x, y, z).
+static void plan_adjacency_and_coords(HostPlan &p, int nen, int N, int E, const int *el)
 {
-    if ((nen != 3 && nen != 6) || N <= 0 || E <= 0) {
-        set_error("bad mesh sizes (nen %d, N %d, E %d)", nen, N, E);
-        return kErrArg;
-    }
-    for (size_t t = 0; t < (size_t)E * nen; t++)
-        if (el[t] < 0 || el[t] >= N) {
-            set_error("element %zu references node %d outside 1..%d", t / nen, el[t] + 1, N);
-            return kErrArg;
-        }
-    p.nen = nen;
-    p.N = N;
-    p.E = E;
-    p.nodes.assign(nodes, nodes + (size_t)N * 3);
-    p.elems.assign(el, el + (size_t)E * nen);
-    p.row_kind.assign(N, 1);
-    p.row_fac.assign(N, -1.0);
-    if (bctype) DSC_TRY(set_rows(p, bctype));
-    p.normals.resize((size_t)N * 3);
-    node_normals(nen, N, E, nodes, el, p.normals.data());
-
-    // Morton order of element centroids.
-    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-    for (int i = 0; i < N; i++)
-        for (int d = 0; d < 3; d++) {
-            lo[d] = std::min(lo[d], nodes[3 * (size_t)i + d]);
-            hi[d] = std::max(hi[d], nodes[3 * (size_t)i + d]);
-        }
-    std::vector<uint64_t> code(E);
-    for (int e = 0; e < E; e++) {
-        uint64_t c = 0;
-        for (int d = 0; d < 3; d++) {
-            double s = 0.0;
-            for (int k = 0; k < nen; k++) s += nodes[3 * (size_t)el[(size_t)e * nen + k] + d];
-            s /= nen;
-            double span = hi[d] - lo[d];
-            double f = span > 0 ? (s - lo[d]) / span : 0.0;
-            uint64_t q = (uint64_t)std::min(2097151.0, std::max(0.0, f * 2097151.0));
-            c |= spread3(q) << d;
-        }
-        code[e] = c;
-    }
-    std::vector<int> order(E);
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return code[a] < code[b]; });
-
-    p.G = (E + kGroup - 1) / kGroup;
-    p.grp_elem.assign((size_t)p.G * kGroup, -1);
-    for (int t = 0; t < E; t++) p.grp_elem[t] = order[t];
-
-    // Footprints: (node, slot) pairs of each group sorted by node.
-    std::vector<std::vector<std::pair<int, int>>> fps(p.G);
-    std::vector<int> ngroups(N, 0), lastg(N, -1);
-    for (int g = 0; g < p.G; g++) {
-        auto &f = fps[g];
-        for (int j = 0; j < kGroup; j++) {
-            int e = p.grp_elem[(size_t)g * kGroup + j];
-            if (e < 0) continue;
-            for (int k = 0; k < nen; k++) f.push_back({el[(size_t)e * nen + k], j * nen + k});
-        }
-        std::sort(f.begin(), f.end());
-        for (size_t t = 0; t < f.size(); t++) {
-            int v = f[t].first;
-            if (lastg[v] != g) {
-                lastg[v] = g;
-                ngroups[v]++;
-            }
-        }
-    }
-    std::vector<std::vector<int>> node_slots(N);
-    p.fp_ptr.assign(1, 0);
-    p.fp_dest.clear();
-    p.fp_sl_ptr.assign(1, 0);
-    p.fp_sl.clear();
-    p.n_slots = 0;
-    p.max_fp = 0;
-    for (int g = 0; g < p.G; g++) {
-        auto &f = fps[g];
-        int nfp = 0;
-        for (size_t t = 0; t < f.size();) {
-            int v = f[t].first;
-            size_t u = t;
-            while (u < f.size() && f[u].first == v) p.fp_sl.push_back((uint16_t)f[u++].second);
-            if (ngroups[v] == 1) p.fp_dest.push_back(v);
-            else {
-                node_slots[v].push_back(p.n_slots);
-                p.fp_dest.push_back(-(p.n_slots + 1));
-                p.n_slots++;
-            }
-            p.fp_sl_ptr.push_back((int)p.fp_sl.size());
-            nfp++;
-            t = u;
-        }
-        p.max_fp = std::max(p.max_fp, nfp);
-        p.fp_ptr.push_back((int)p.fp_dest.size());
-    }
-    p.fix_ptr.assign(1, 0);
-    p.fix_slot.clear();
-    p.fix_col.clear();
-    for (int v = 0; v < N; v++) {
-        if (ngroups[v] == 1) continue;
-        p.fix_col.push_back(v);
-        for (int s : node_slots[v]) p.fix_slot.push_back(s);
-        p.fix_ptr.push_back((int)p.fix_slot.size());
-    }
     // node -> elements containing it, element order, first position
     std::vector<int> cnt(N + 1, 0);
     for (int e = 0; e < E; e++)
@@ -263,6 +161,132 @@ int build_plan(int nen, int N, int E, const double *nodes, const int *el,
         if (u[1] != v[1]) return u[1] < v[1];
         return u[2] < v[2];
     });
+}
+
+int build_plan(int nen, int N, int E, const double *nodes, const int *el,
+               const unsigned *bctype, HostPlan &p)
+{
+    if ((nen != 3 && nen != 6) || N <= 0 || E <= 0) {
+        set_error("bad mesh sizes (nen %d, N %d, E %d)", nen, N, E);
+        return kErrArg;
+    }
+    for (size_t t = 0; t < (size_t)E * nen; t++)
+        if (el[t] < 0 || el[t] >= N) {
+            set_error("element %zu references node %d outside 1..%d", t / nen, el[t] + 1, N);
+            return kErrArg;
+        }
+    p.nen = nen;
+    p.N = N;
+    p.E = E;
+    p.nodes.assign(nodes, nodes + (size_t)N * 3);
+    p.elems.assign(el, el + (size_t)E * nen);
+    p.row_kind.assign(N, 1);
+    p.row_fac.assign(N, -1.0);
+    if (bctype) DSC_TRY(set_rows(p, bctype));
+    // node normals, node -> element adjacency and the coordinate order
+    // are independent of the groups below: two host threads build them
+    // meanwhile
+    p.normals.resize((size_t)N * 3);
+    std::thread t_normals([&] { node_normals(nen, N, E, nodes, el, p.normals.data()); });
+    std::thread t_side([&] { plan_adjacency_and_coords(p, nen, N, E, el); });
+
+    // Morton order of element centroids.
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int i = 0; i < N; i++)
+        for (int d = 0; d < 3; d++) {
+            lo[d] = std::min(lo[d], nodes[3 * (size_t)i + d]);
+            hi[d] = std::max(hi[d], nodes[3 * (size_t)i + d]);
+        }
+    std::vector<uint64_t> code(E);
+    for (int e = 0; e < E; e++) {
+        uint64_t c = 0;
+        for (int d = 0; d < 3; d++) {
+            double s = 0.0;
+            for (int k = 0; k < nen; k++) s += nodes[3 * (size_t)el[(size_t)e * nen + k] + d];
+            s /= nen;
+            double span = hi[d] - lo[d];
+            double f = span > 0 ? (s - lo[d]) / span : 0.0;
+            uint64_t q = (uint64_t)std::min(2097151.0, std::max(0.0, f * 2097151.0));
+            c |= spread3(q) << d;
+        }
+        code[e] = c;
+    }
+    std::vector<int> order(E);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return code[a] < code[b]; });
+
+    p.G = (E + kGroup - 1) / kGroup;
+    p.grp_elem.assign((size_t)p.G * kGroup, -1);
+    for (int t = 0; t < E; t++) p.grp_elem[t] = order[t];
+
+    // Footprints: (node, slot) pairs of each group sorted by node, in one
+    // flat array (group g at [g * kGroup * nen, ...)).
+    const size_t per = (size_t)kGroup * nen;
+    std::vector<std::pair<int, int>> fpa((size_t)p.G * per);
+    std::vector<int> fpn(p.G, 0);
+    std::vector<int> ngroups(N, 0), lastg(N, -1);
+    for (int g = 0; g < p.G; g++) {
+        std::pair<int, int> *f = fpa.data() + (size_t)g * per;
+        int n = 0;
+        for (int j = 0; j < kGroup; j++) {
+            int e = p.grp_elem[(size_t)g * kGroup + j];
+            if (e < 0) continue;
+            for (int k = 0; k < nen; k++) f[n++] = {el[(size_t)e * nen + k], j * nen + k};
+        }
+        std::sort(f, f + n);
+        fpn[g] = n;
+        for (int t = 0; t < n; t++) {
+            int v = f[t].first;
+            if (lastg[v] != g) {
+                lastg[v] = g;
+                ngroups[v]++;
+            }
+        }
+    }
+    // a node in more than one footprint gets one partial slot per group
+    // (numbered in group order); fix_* list them per node in node order
+    p.fix_ptr.assign(1, 0);
+    p.fix_col.clear();
+    std::vector<int> fix_at(N, -1);
+    for (int v = 0; v < N; v++) {
+        if (ngroups[v] == 1) continue;
+        fix_at[v] = p.fix_ptr.back();
+        p.fix_col.push_back(v);
+        p.fix_ptr.push_back(p.fix_ptr.back() + ngroups[v]);
+    }
+    p.fix_slot.assign(p.fix_ptr.back(), 0);
+    p.fp_ptr.assign(1, 0);
+    p.fp_dest.clear();
+    p.fp_dest.reserve((size_t)E * nen);
+    p.fp_sl_ptr.assign(1, 0);
+    p.fp_sl_ptr.reserve((size_t)E * nen + 1);
+    p.fp_sl.clear();
+    p.fp_sl.reserve((size_t)E * nen);
+    p.n_slots = 0;
+    p.max_fp = 0;
+    for (int g = 0; g < p.G; g++) {
+        const std::pair<int, int> *f = fpa.data() + (size_t)g * per;
+        const int n = fpn[g];
+        int nfp = 0;
+        for (int t = 0; t < n;) {
+            int v = f[t].first;
+            int u = t;
+            while (u < n && f[u].first == v) p.fp_sl.push_back((uint16_t)f[u++].second);
+            if (ngroups[v] == 1) p.fp_dest.push_back(v);
+            else {
+                p.fix_slot[fix_at[v]++] = p.n_slots;
+                p.fp_dest.push_back(-(p.n_slots + 1));
+                p.n_slots++;
+            }
+            p.fp_sl_ptr.push_back((int)p.fp_sl.size());
+            nfp++;
+            t = u;
+        }
+        p.max_fp = std::max(p.max_fp, nfp);
+        p.fp_ptr.push_back((int)p.fp_dest.size());
+    }
+    t_normals.join();
+    t_side.join();
     return kOk;
 }
 

@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <numeric>
 
+#include "dsc_common.cuh"
 #include "dsc_df32.cuh"
 #include "dsc_precond.h"
 #include "dsc_session.h"
@@ -319,6 +320,19 @@ __global__ void __launch_bounds__(256) k_gj_row(GJArgs g, int nb, int k)
         pre_row_pair(&T[jj][0], Bh + (size_t)jj * kPB, Bl + (size_t)jj * kPB, &g.rb[b][J * kPB + jj]);
 }
 
+// *bound = max(*bound, largest row sum of |Xt| over the first n rows and
+// columns) as FP32 bits (non-negative floats order as their bits); one warp
+// per row.
+__global__ void k_pre_rowsum_max(const float *__restrict__ Xt, int ldx, int n, unsigned *bound)
+{
+    const int r = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (r >= n) return;
+    float t = 0.0f;
+    for (int c = lane; c < n; c += 32) t += fabsf(Xt[(size_t)r * ldx + c]);
+    t = warp_sum(t);
+    if (lane == 0) atomicMax(bound, __float_as_uint(t * 1.001f));  // margin for the rounding of the sum
+}
+
 // Xt[r * ldx + c] = X[c * ldx + r] (32 x 32 tiles).
 __global__ void k_pre_transpose(const float *__restrict__ X, int ldx, float *__restrict__ Xt)
 {
@@ -391,13 +405,21 @@ int precond_build(Session &s)
     }
     // the inverses as row-scaled fp16 pairs for the products (X is
     // column-major: its transpose's rows are X's columns; the products take
-    // X^T's rows as their A rows, so the transposed copy goes first)
+    // X^T's rows as their A rows, so the transposed copy goes first), and
+    // the bound on |P^-1 v| for unit vectors v
+    DSC_TRY(pc.zbound.alloc(1));
+    {
+        const unsigned one = 0x3F800000u;  // 1.0f: the interface rows keep v
+        DSC_CUDA(cudaMemcpyAsync(pc.zbound.p, &one, sizeof(unsigned), cudaMemcpyHostToDevice, st));
+    }
     for (int b = 0; b < pc.nb; b++) {
         const int ldx = pc.ldx[b];
         DSC_LAUNCH(k_pre_transpose<<<dim3(ldx / 32, ldx / 32), dim3(32, 8), 0, st>>>(pc.X.p + pc.xoff[b], ldx,
                                                                                      pc.Xt.p + pc.xoff[b]));
         DSC_TRY(split_cols_f16(pc.Xt.p + pc.xoff[b], (size_t)ldx, pc.n[b], pc.n[b], pc.Xh.p + pc.xoff[b],
                                pc.Xl.p + pc.xoff[b], (size_t)ldx, pc.rs.p + pc.noff[b], st));
+        DSC_LAUNCH(k_pre_rowsum_max<<<(pc.n[b] * 32 + 255) / 256, 256, 0, st>>>(pc.Xt.p + pc.xoff[b], ldx,
+                                                                                pc.n[b], pc.zbound.p));
     }
     s.timer.add_work(kTPreBuild, flops);
     DSC_CUDA(cudaGetLastError());
@@ -441,6 +463,7 @@ int precond_reserve(Session &s, int F)
     DSC_TRY(pc.Bl.alloc(bo));
     DSC_TRY(pc.G.alloc(bo));
     DSC_TRY(pc.csc.alloc((size_t)2 * F * pc.nb));
+    DSC_TRY(pc.cz.alloc((size_t)2 * F));
     DSC_TRY(pc.yinfo.upload(info, s.st));
     DSC_CUDA(cudaStreamSynchronize(s.st));
     pc.F = F;
@@ -461,13 +484,19 @@ __global__ void k_pre_gather_v(const float2 *__restrict__ V, size_t ld, const in
     Bl[(size_t)c * ldb + r] = __float2half_rn(__fadd_rn(__fsub_rn(x, __half2float(h)), v.y * kPreVScale));
 }
 
-// Z[c][i] = P^-1 v: the block products' partial tiles summed in split order
-// on preconditioned rows, v (hi + lo, rounded) elsewhere.
+// z = P^-1 v for column c: the block products' partial tiles summed in
+// split order on preconditioned rows, v (hi + lo, rounded) elsewhere;
+// written as the fp16 pair of 2^t z (Zh, Zl) for the product with K, t
+// fixed by zbound (the FP32 bits of a bound on |z|: max(1, the largest row
+// sum of |X_b|)); cz[c] = 2^-t.
 __global__ void k_pre_combine(const float2 *__restrict__ V, size_t ld, int N, const int *__restrict__ rblk,
                               const int *__restrict__ rpos, const float *__restrict__ Y,
-                              const long long *__restrict__ yinfo, float *__restrict__ Z)
+                              const long long *__restrict__ yinfo, const unsigned *__restrict__ zbound,
+                              __half *__restrict__ Zh, __half *__restrict__ Zl, float *__restrict__ cz)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
+    const int sh = max(-100, min(100, 14 - ((int)(*zbound >> 23) - 127)));
+    if (i == 0) cz[c] = pre_pow2(-sh);
     if (i >= N) return;
     const int b = rblk[i];
     float z;
@@ -484,8 +513,12 @@ __global__ void k_pre_combine(const float2 *__restrict__ V, size_t ld, int N, co
         }
         z = acc.x + acc.y;
     }
-    Z[(size_t)c * ld + i] = z;
+    const float x = z * pre_pow2(sh);
+    const __half h = __float2half_rn(x);
+    Zh[(size_t)c * ld + i] = h;
+    Zl[(size_t)c * ld + i] = __float2half_rn(x - __half2float(h));
 }
+
 
 // G[c * ldg + r] = D[c][E[r]] for the rows of one block.
 __global__ void k_pre_gather_d(const double *__restrict__ D, size_t ld, const int *__restrict__ nodes, int n,
@@ -507,7 +540,8 @@ __global__ void k_pre_scatter_d(double *__restrict__ D, size_t ld, const int *__
     D[(size_t)c * ld + nodes[r]] = t;
 }
 
-int precond_apply_v(Session &s, const float2 *V, int F, float *Z, const float *cscK, int *d_err)
+int precond_apply_v(Session &s, const float2 *V, int F, __half *Zh, __half *Zl, const float *cscK, int *d_err,
+                    const float **cz)
 {
     Precond &pc = *s.pre;
     cudaStream_t st = s.st;
@@ -522,9 +556,10 @@ int precond_apply_v(Session &s, const float2 *V, int F, float *Z, const float *c
                               pc.rs.p + pc.noff[b], cscK));
         s.timer.add_work(kTPreApply, 6.0 * n * (double)n * F2);
     }
-    DSC_LAUNCH(k_pre_combine<<<dim3((s.N + 255) / 256, F2), 256, 0, st>>>(V, s.ld, s.N, pc.rblk.p, pc.rpos.p,
-                                                                         pc.Y.p, pc.yinfo.p, Z));
+    DSC_LAUNCH(k_pre_combine<<<dim3((s.N + 255) / 256, F2), 256, 0, st>>>(
+        V, s.ld, s.N, pc.rblk.p, pc.rpos.p, pc.Y.p, pc.yinfo.p, pc.zbound.p, Zh, Zl, pc.cz.p));
     DSC_CUDA(cudaGetLastError());
+    *cz = pc.cz.p;
     return kOk;
 }
 

@@ -50,6 +50,8 @@ struct Precond {
     DevBuf<float> csc;                // column factors of gathered corrections
     DevBuf<float> Y;                  // split partials of the block products
     DevBuf<long long> yinfo;          // per block: Y offset, split stride, S (device copy)
+    DevBuf<unsigned> zbound;          // FP32 bits of a bound on |P^-1 v| for |v| <= 1
+    DevBuf<float> cz;                 // the K product's column factors of z's pair
     bool ready = false;               // the inverses match the current K
 };
 
@@ -60,9 +62,12 @@ int precond_plan(Session &s);
 int precond_build(Session &s);
 // Workspace of the apply calls for F systems.
 int precond_reserve(Session &s, int F);
-// Z (FP32, column c at c * ld, rows < N) = P^-1 v for the 2F columns of the
-// double-FP32 block V (Re, Im of each system; |v| <= 1: unit vectors).
-int precond_apply_v(Session &s, const float2 *V, int F, float *Z, const float *cscK, int *d_err);
+// z = P^-1 v for the 2F columns of the double-FP32 block V (Re, Im of each
+// system; |v| <= 1: unit vectors), written as the fp16 pair (Zh, Zl; column
+// c at c * ld, rows < N) of z scaled by a fixed power of two; *cz receives
+// the product's column factors.
+int precond_apply_v(Session &s, const float2 *V, int F, __half *Zh, __half *Zl, const float *cscK, int *d_err,
+                    const float **cz);
 // D (FP64, 2F columns) = P^-1 D in place.
 int precond_apply_d(Session &s, double *D, int F, int *d_err);
 
