@@ -642,7 +642,7 @@ __global__ void k_charge_batched(const int *__restrict__ elems, int E, const dou
     cf[(size_t)f * E * kTriPts + t] = qp[(size_t)t * 4 + 3] * s;
 }
 
-constexpr int kBF = 16;   // frequencies per thread in the batched field
+constexpr int kBF = 32;   // frequencies per thread in the batched field
 constexpr int kBChunk = 32;
 
 // ---- FP32 far field with FP64 near field
@@ -716,7 +716,9 @@ __global__ void __launch_bounds__(128) k_field_batched_mixed(
 {
     __shared__ float s_cent[kBChunk * 8];
     __shared__ float s_off[kBChunk * kTriPts * 3];
-    __shared__ __align__(16) float s_c[kBChunk * kTriPts][kBF];  // charge of (e, q) for the group's systems
+    // charge of (e, q) for the group's systems; rows padded by 4 floats so
+    // that the staging stores of consecutive (e, q) spread over the banks
+    __shared__ __align__(16) float s_c[kBChunk * kTriPts][kBF + 4];
     __shared__ int s_en[kBChunk * NEN];
     const int group = blockIdx.y, fg = blockIdx.z;
     const int f0 = fg * kBF, nf = min(kBF, F - f0);
@@ -746,18 +748,22 @@ __global__ void __launch_bounds__(128) k_field_batched_mixed(
         __syncthreads();
         if (!valid) continue;
         for (int e = 0; e < ne; e++) {
-            bool sing = false;
-#pragma unroll
-            for (int k = 0; k < NEN; k++) {
-                const int v = s_en[e * NEN + k];
-                sing |= (v == c.x) | (v == c.y) | (v == c.z) | (v == c.w);
-            }
-            if (sing && c.x >= 0) continue;
             const float *ce = s_cent + e * 8;
             const float d0x = (ph[0] - ce[0]) + (pl[0] - ce[3]);
             const float d0y = (ph[1] - ce[1]) + (pl[1] - ce[4]);
             const float d0z = (ph[2] - ce[2]) + (pl[2] - ce[5]);
             const bool near = d0x * d0x + d0y * d0y + d0z * d0z < ce[6];
+            if (near) {
+                // singular elements (the point is one of their nodes) lie
+                // within the near radius; the singular pass takes them
+                bool sing = false;
+#pragma unroll
+                for (int k = 0; k < NEN; k++) {
+                    const int v = s_en[e * NEN + k];
+                    sing |= (v == c.x) | (v == c.y) | (v == c.z) | (v == c.w);
+                }
+                if (sing && c.x >= 0) continue;
+            }
             const float *O = s_off + e * kTriPts * 3;
 #pragma unroll
             for (int q = 0; q < kTriPts; q++) {
