@@ -79,18 +79,17 @@ __device__ __forceinline__ float2 df_sqr(float2 a)
     return df_fast_two_sum(p, e);
 }
 
-// 1 / sqrt(a) for a > 0: an FP32 seed and two Newton steps
-// y <- y + y (1 - a y^2) / 2 with a y^2 in double-FP32 (each step squares
-// the relative error; the seed's ~2^-22 ends below 2^-46).
+// 1 / sqrt(a) for a > 0: an FP32 seed refined by one FP32 Newton step
+// (relative error about 2^-23), then one Newton step y <- y + y (1 - a
+// y^2) / 2 with a y^2 in double-FP32 (which squares it: about 2^-45).
 __device__ __forceinline__ float2 df_rsqrt(float2 a)
 {
-    float2 y = make_float2(rsqrtf(a.x), 0.0f);
-#pragma unroll
-    for (int it = 0; it < 2; it++) {
-        const float2 t = df_mul(a, df_sqr(y));
-        const float u = __fsub_rn(__fsub_rn(1.0f, t.x), t.y);  // 1 - t.x is exact
-        y = df_add(y, df_mul(y, make_float2(0.5f * u, 0.0f)));
-    }
+    float y0 = rsqrtf(a.x);
+    y0 = y0 * (1.5f - 0.5f * a.x * y0 * y0);
+    float2 y = make_float2(y0, 0.0f);
+    const float2 t = df_mul(a, df_sqr(y));
+    const float u = __fsub_rn(__fsub_rn(1.0f, t.x), t.y);  // 1 - t.x is exact
+    y = df_add(y, df_mul(y, make_float2(0.5f * u, 0.0f)));
     return y;
 }
 
