@@ -38,138 +38,6 @@ constexpr int kOuterMax = 6;    // refinement steps
 // 3e-7 took 89, 1e-7 took 93.
 constexpr double kInnerTol = 3e-7;
 
-// P[z] (M x Nc, FP64) = the part over k-split z of fl32(A) (M x Kd) * B
-// (Kd x Nc), column-major: A is FP64 and rounded to FP32 as it is staged
-// (one conversion per element), B is FP32; every product
-// is exact (p = a*b and e = fma(a, b, -p)) and the running sum is an
-// unevaluated pair (s, c) kept exact by TwoSum: about 2^-46 of the sum of
-// |a b|.  The parts of A and of the true B below FP32 are small (2^-24
-// relative) and go to the tensor cores (the first residual of the mixed
-// sweep).  64 x 128 tile, 512 threads with 4 x 4 outputs each, k-steps of
-// 16 through two shared-memory buffers (the next step's tile is fetched into
-// registers while the current one is used); grid (row tiles, column tiles,
-// k-splits), the splits added in order by k_sum_exact_splits.
-__device__ __forceinline__ void exact_acc(float &s, float &c, float a, float b)
-{
-    // the _rn intrinsics keep the compiler from fusing these operations,
-    // which would break the exactness of the product and of TwoSum
-    const float p = __fmul_rn(a, b);
-    const float e = __fmaf_rn(a, b, -p);
-    const float t = __fadd_rn(s, p);
-    const float bp = __fsub_rn(t, s);
-    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
-    s = t;
-    c += err + e;
-}
-
-constexpr int kExBK = 16;
-constexpr int kExSplits = 8;
-
-__global__ void __launch_bounds__(512, 1) k_gemm_exact32(const double *__restrict__ A, size_t lda,
-                                                      const float *__restrict__ B, size_t ldb,
-                                                      double *__restrict__ P, size_t ldp, size_t split_stride,
-                                                      int M, int Nc, int Kd, int kchunk)
-{
-    __shared__ float As[2][kExBK][64];
-    __shared__ float Bs[2][kExBK][128 + 1];
-    const int m0 = blockIdx.x * 64, n0 = blockIdx.y * 128;
-    const int k_beg = blockIdx.z * kchunk, k_end = min(Kd, k_beg + kchunk);
-    const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;
-    float s[4][4], c[4][4];
-#pragma unroll
-    for (int u = 0; u < 4; u++)
-#pragma unroll
-        for (int v = 0; v < 4; v++) s[u][v] = c[u][v] = 0.0f;
-    // staging: A element (kk = t / 64, mm = t % 64) for t = tid, tid + 512;
-    // B element (nn = t / 16, kb = t % 16) for t = tid + 512 q, q < 4
-    float ra[2], rb[4];
-    auto fetch = [&](int k0) {
-#pragma unroll
-        for (int q = 0; q < 2; q++) {
-            const int t = threadIdx.x + 512 * q, kk = t / 64, mm = t % 64;
-            const int m = m0 + mm, k = k0 + kk;
-            ra[q] = (m < M && k < k_end) ? (float)A[(size_t)k * lda + m] : 0.0f;
-        }
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            const int t = threadIdx.x + 512 * q, nn = t / 16, kb = t % 16;
-            const int n = n0 + nn, k = k0 + kb;
-            rb[q] = (n < Nc && k < k_end) ? B[(size_t)n * ldb + k] : 0.0f;
-        }
-    };
-    auto stash = [&](int buf) {
-#pragma unroll
-        for (int q = 0; q < 2; q++) {
-            const int t = threadIdx.x + 512 * q;
-            As[buf][t / 64][t % 64] = ra[q];
-        }
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            const int t = threadIdx.x + 512 * q;
-            Bs[buf][t % 16][t / 16] = rb[q];
-        }
-    };
-    fetch(k_beg);
-    stash(0);
-    __syncthreads();
-    int buf = 0;
-    for (int k0 = k_beg; k0 < k_end; k0 += kExBK) {
-        const bool more = k0 + kExBK < k_end;
-        if (more) fetch(k0 + kExBK);
-#pragma unroll 2
-        for (int kk = 0; kk < kExBK; kk++) {
-            float a[4], b[4];
-#pragma unroll
-            for (int u = 0; u < 4; u++) a[u] = As[buf][kk][ty + 16 * u];
-#pragma unroll
-            for (int v = 0; v < 4; v++) b[v] = Bs[buf][kk][tx + 32 * v];
-#pragma unroll
-            for (int u = 0; u < 4; u++)
-#pragma unroll
-                for (int v = 0; v < 4; v++) exact_acc(s[u][v], c[u][v], a[u], b[v]);
-        }
-        if (more) stash(buf ^ 1);
-        __syncthreads();
-        buf ^= 1;
-    }
-    double *Pz = P + (size_t)blockIdx.z * split_stride;
-#pragma unroll
-    for (int u = 0; u < 4; u++) {
-        const int m = m0 + ty + 16 * u;
-        if (m >= M) continue;
-#pragma unroll
-        for (int v = 0; v < 4; v++) {
-            const int n = n0 + tx + 32 * v;
-            if (n < Nc) Pz[(size_t)n * ldp + m] = (double)s[u][v] + (double)c[u][v];
-        }
-    }
-}
-
-// C[n * ldc + m] = sum over the S splits of P, in split order (FP64).
-__global__ void k_sum_exact_splits(const double *__restrict__ P, int S, size_t split_stride, size_t ldp,
-                                   int M, double *__restrict__ C, size_t ldc)
-{
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    const int n = blockIdx.y;
-    if (m >= M) return;
-    double t = 0.0;
-    for (int z = 0; z < S; z++) t += P[(size_t)z * split_stride + (size_t)n * ldp + m];
-    C[(size_t)n * ldc + m] = t;
-}
-
-// FP64 array to FP32 pairs (hi = rounded value, lo = the rest, rounded).
-__global__ void k_split_f32_pair(const double *__restrict__ x, float *__restrict__ h,
-                                 float *__restrict__ l, size_t n)
-{
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n;
-         t += (size_t)gridDim.x * blockDim.x) {
-        const double v = x[t];
-        const float a = (float)v;
-        h[t] = a;
-        l[t] = (float)(v - (double)a);
-    }
-}
-
 // r_f = bt_f - (cs_f o Y_f + cd_f o x_f)
 __global__ void k_residual(const double *__restrict__ Y, const double *__restrict__ X,
                            const double2 *__restrict__ cs, const double2 *__restrict__ cd,
@@ -967,14 +835,18 @@ struct Session::Mixed {
     DevBuf<float2> W;       // the new Krylov vector (double-FP32)
     DevBuf<float2> cs32, cd32;  // FP32 copies of the coefficients
     DevBuf<double> Ak, Bk;      // interface coefficients of the batch (F x nIf)
-    DevBuf<float> Xh, Xl;       // FP32 pair of the solution (FP64-accurate residual)
+    // the first residual's digit product: x's digits (fp16 rows j * 2F + c),
+    // the rest of x (FP64), its columns' exponents, the digit partial tiles
+    DevBuf<__half> Xd;
+    DevBuf<double> Xrem;
+    DevBuf<int> colE;
+    DevBuf<float> Pd;
     DevBuf<__half> Vh, Vl;  // scaled fp16 pair of the current GEMM operand block
     DevBuf<float> cscK;     // column factors of the Krylov blocks' pairs (2^-14)
     DevBuf<float> cscX;     // column factors of the other operands' pairs
     DevBuf<float> Yp;       // split-K partial products, S blocks
     DevBuf<int> err;        // set by the tensor-core kernel when a wait gives up
     DevBuf<double> Xs, R, Y64, D;
-    DevBuf<double> Pex;     // k-split partials of the first residual's exact product
     DevBuf<double2> cs, cd, bt, h, hacc, ycoef;
     DevBuf<float4> dpart;   // Gram-Schmidt dot partials per row chunk (double-FP32 re, im)
     DevBuf<float4> hdf;     // the update's coefficients (-Re h, Im h) in double-FP32
@@ -1001,14 +873,13 @@ int Session::make_k16()
         TimerScope ts(&timer, kTConvertK, st);
         DSC_TRY(Kh16.alloc(ld * N));
         DSC_TRY(Kl16.alloc(ld * N));
-        DSC_TRY(dKh16.alloc(ld * N));
-        DSC_TRY(dKl16.alloc(ld * N));
+        DSC_TRY(Kdig.alloc(kKDigits * ld * N));
         DSC_TRY(rowE.alloc(N));
         DSC_TRY(rsK.alloc(N));
-        DSC_TRY(rsdK.alloc(N));
-        DSC_TRY(k16_row_scales(K64.p, ld, N, rowE.p, rsK.p, rsdK.p, st));
-        DSC_TRY(split_transpose_K16(K64.p, ld, N, rowE.p, Kh16.p, Kl16.p, dKh16.p, dKl16.p, ld, st));
-        timer.add_work(kTConvertK, 16.0 * N * N);  // bytes: K read (8), four fp16 copies written (8)
+        DSC_TRY(k16_row_scales(K64.p, ld, N, rowE.p, rsK.p, st));
+        DSC_TRY(split_transpose_K16(K64.p, ld, N, rowE.p, Kh16.p, Kl16.p, Kdig.p, ld * N, ld, st));
+        // bytes: K read (8), the fp16 pair and the digits written (2 each)
+        timer.add_work(kTConvertK, (8.0 + 2.0 * (2 + kKDigits)) * N * N);
     }
     if (pre_on) DSC_TRY(precond_build(*this));
     k16_ready = true;
@@ -1276,30 +1147,27 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
         if (pre) DSC_TRY(precond_apply_d(s, w.D.p, F, w.err.p));
         DSC_LAUNCH(k_axpy_blocks<<<vg, 256, 0, st>>>(w.Xs.p, w.D.p, N, ld, F));
         if (outer == 0) {
-            // the first residual in FP64: r = bt - M x
+            // the first residual in FP64: r = bt - M x, with K x from
+            //   K's row digits times x's column digits (fixed point, the
+            //     21 digit products whose weight is within 2^-48 of the
+            //     largest), exact integer sums on the tensor cores
+            // + K times the rest of x (below 2^-23 of its column's largest
+            //     entry: the fp16-pair product's FP32-level accuracy suffices)
             TimerScope ts(tm, kTResidual, st);
-            // K x = fl32(K) xh (exact products, on the FP32 pipes)
-            //     + fl32(K) xl + (K - fl32(K)) xh (both ~2^-24 of K x: the
-            //       tensor cores' FP32-level accuracy suffices)
-            // with x = xh + xl, xh = fl32(x)
-            DSC_LAUNCH(k_split_f32_pair<<<4 * 152, 256, 0, st>>>(w.Xs.p, w.Xh.p, w.Xl.p, blk));
-            const int kchunk = ((N + kExSplits - 1) / kExSplits + kExBK - 1) / kExBK * kExBK;
-            const int nz = (N + kchunk - 1) / kchunk;
-            DSC_TRY(w.Pex.alloc(blk * nz));
-            dim3 g((N + 63) / 64, (2 * F + 127) / 128, nz);
-            DSC_LAUNCH(k_gemm_exact32<<<g, 512, 0, st>>>(s.K64.p, ld, w.Xh.p, ld, w.Pex.p, ld, blk, N, 2 * F, N,
-                                                         kchunk));
-            DSC_LAUNCH(k_sum_exact_splits<<<dim3((N + 255) / 256, 2 * F), 256, 0, st>>>(w.Pex.p, nz, blk, ld, N,
-                                                                                       w.Y64.p, ld));
-            tm->add_work(kTResidual, (double)N * N * 2 * F);  // FP64-accurate multiply-adds
-            DSC_TRY(split_cols_f16(w.Xl.p, ld, N, 2 * F, w.Vh.p, w.Vl.p, ld, w.cscX.p, st));
-            DSC_TRY(tc_gemm_3xf16(s.Kh16.p, s.Kl16.p, ld, w.Vh.p, w.Vl.p, ld, N, 2 * F, N, w.Yp.p, ld, w.S,
+            const int ncol = 2 * F, Sd = tc_digit_splits(N);
+            DSC_TRY(x_digits(w.Xs.p, ld, N, ncol, w.Xd.p, ld, w.Xrem.p, ld, w.colE.p, st));
+            for (int i = 0; i < kKDigits; i++) {
+                const int nj = x_digits_for(i);
+                DSC_TRY(tc_gemm_digits(s.Kdig.p + (size_t)i * ld * N, ld, w.Xd.p, ld, N, nj * ncol, N, w.Pd.p, ld,
+                                       w.err.p, st));
+                DSC_TRY(digit_accumulate(w.Pd.p, Sd, ld, ncol, nj, i, N, w.Y64.p, ld, i == 0, st));
+                tm->add_work(kTResidual, (double)N * N * nj * ncol);  // digit multiply-adds
+            }
+            DSC_TRY(digit_finish(s.rowE.p, w.colE.p, N, ncol, w.Y64.p, ld, st));
+            DSC_TRY(split_cols_f16(w.Xrem.p, ld, N, ncol, w.Vh.p, w.Vl.p, ld, w.cscX.p, st));
+            DSC_TRY(tc_gemm_3xf16(s.Kh16.p, s.Kl16.p, ld, w.Vh.p, w.Vl.p, ld, N, ncol, N, w.Yp.p, ld, w.S,
                                   w.err.p, st, s.rsK.p, w.cscX.p));
-            DSC_TRY(add_splits(w.Yp.p, w.S, ld * 2 * (size_t)F, ld, N, 2 * F, w.Y64.p, ld, st));
-            DSC_TRY(split_cols_f16(w.Xh.p, ld, N, 2 * F, w.Vh.p, w.Vl.p, ld, w.cscX.p, st));
-            DSC_TRY(tc_gemm_3xf16(s.dKh16.p, s.dKl16.p, ld, w.Vh.p, w.Vl.p, ld, N, 2 * F, N, w.Yp.p, ld, w.S,
-                                  w.err.p, st, s.rsdK.p, w.cscX.p));
-            DSC_TRY(add_splits(w.Yp.p, w.S, ld * 2 * (size_t)F, ld, N, 2 * F, w.Y64.p, ld, st));
+            DSC_TRY(add_splits(w.Yp.p, w.S, ld * (size_t)ncol, ld, N, ncol, w.Y64.p, ld, st));
             DSC_LAUNCH(k_residual<<<vg, 256, 0, st>>>(w.Y64.p, w.Xs.p, w.cs.p, w.cd.p, w.bt.p, w.R.p, N, ld, F));
         } else {
             // later residuals are updated, r -= M d: d is small, so the
@@ -1450,8 +1318,10 @@ int Session::solve_mixed(unsigned nfreq, const double *freqs, double tol, unsign
         DSC_TRY(w.err.alloc(1));
         DSC_CUDA(cudaMemsetAsync(w.err.p, 0, sizeof(int), st));
         DSC_TRY(w.W.alloc(blk));
-        DSC_TRY(w.Xh.alloc(blk));
-        DSC_TRY(w.Xl.alloc(blk));
+        DSC_TRY(w.Xd.alloc(kXDigits * blk));
+        DSC_TRY(w.Xrem.alloc(blk));
+        DSC_TRY(w.colE.alloc(2 * (size_t)Fmax));
+        DSC_TRY(w.Pd.alloc((size_t)tc_digit_splits(N) * kXDigits * blk));
         DSC_TRY(w.cs.alloc((size_t)Fmax * N));
         DSC_TRY(w.cd.alloc((size_t)Fmax * N));
         DSC_TRY(w.bt.alloc((size_t)Fmax * N));

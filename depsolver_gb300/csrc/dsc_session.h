@@ -53,13 +53,13 @@ struct Session {
     DevBuf<double> ca, cb, cd, gemv_part;
 
     // mixed path: K as row-major scaled fp16 pairs (2^s_i fl32(K) per row i)
-    // for the tensor-core products, the same of K - fl32(K) (scaled by
-    // 2^(s_i + 24)) for the first FP64-accurate residual, the epilogue's row
-    // factors, and the batched-solver workspace
+    // for the tensor-core products, K's fixed-point row digits (kKDigits
+    // fp16 matrices) for the first FP64-accurate residual, the epilogue's
+    // row factors, and the batched-solver workspace
     bool k16_ready = false;
-    DevBuf<__half> Kh16, Kl16, dKh16, dKl16;
+    DevBuf<__half> Kh16, Kl16, Kdig;
     DevBuf<int> rowE;           // biased FP64 exponent of each row's largest entry
-    DevBuf<float> rsK, rsdK;    // 2^-s_i, 2^-(s_i + 24)
+    DevBuf<float> rsK;          // 2^-s_i
     struct Mixed;
     Mixed *mx = nullptr;
     // conductor-block right preconditioner of the mixed sweep (pre_on: used

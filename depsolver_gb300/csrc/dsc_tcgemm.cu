@@ -55,6 +55,10 @@ constexpr int kTcThreads = 32 * (2 + kTcSplitWarps + 4);
 // memory a CTA may use for BN <= 160
 constexpr int kTcMaxNc = 160;
 constexpr long long kTcSpin = kSpin;  // clock cycles before a wait gives up
+// digit products: at most 64 k-blocks (4096 k) per split, and up to 384
+// columns (3 stages of a 16 KB A tile and a 48 KB B tile)
+constexpr int kTcDigitKBlocks = 64;
+constexpr int kTcMaxDigitCols = 384;
 
 __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar, int x,
                                             int y)
@@ -212,6 +216,11 @@ __device__ __forceinline__ float tf32_lo_biased(float s)
 // dropped lo*lo product is at 2^-22 instead of 2^-21.
 // AMODE 3: A and B arrive as scaled fp16 pairs (kind::f16); the epilogue
 // multiplies row m by rsc[m] and column n by csc[n] (null: 1).
+// AMODE 4 (digits): one product A B^T of single fp16 operands (no pairs),
+// BN up to 384 columns (two MMAs of BN / 2 when BN > 256; one accumulator
+// buffer when two do not fit the 512 TMEM columns).  With small-integer
+// operands and short enough splits every partial sum is an integer below
+// 2^24, which the FP32 accumulator holds exactly whatever its rounding.
 // COMB (BN a multiple of 32, at most 128): Ah*Bh and Ah*Bl are one MMA of
 // N = 2 BN against the adjacent Bh and Bl tiles, into accumulator columns
 // [0, BN) and [BN, 2 BN); Al*Bh adds into [BN, 2 BN) too; the epilogue adds
@@ -235,13 +244,18 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     // acc_stride: TMEM columns of one accumulator buffer, a power of two of
     // at least the columns it holds (so each buffer's MMAs start aligned)
     constexpr bool SPLIT_A = AMODE == 1 || AMODE == 2;
-    constexpr bool F16 = AMODE == 3;
+    constexpr bool DIG = AMODE == 4;
+    constexpr bool F16 = AMODE == 3 || DIG;
     constexpr int BK = F16 ? kTcBK16 : kTcBK;  // elements per k-block
-    const bool comb = BN <= 128 && BN % 32 == 0;
+    const bool comb = !DIG && BN <= 128 && BN % 32 == 0;
+    // B rows per TMA box and per MMA (a box and an MMA take at most 256)
+    const int bsub = BN > 256 ? BN / 2 : BN;
+    // accumulator buffers: two unless they do not fit the allocation
+    const int nbuf = 2 * (int)acc_stride <= tmem_cols ? 2 : 1;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const uint32_t a_bytes = kTcBM * kTcRowBytes, b_bytes = (uint32_t)BN * kTcRowBytes;
-    const uint32_t stage_bytes = 2 * a_bytes + 2 * b_bytes;
+    const uint32_t stage_bytes = DIG ? a_bytes + b_bytes : 2 * a_bytes + 2 * b_bytes;
     uint64_t *full = (uint64_t *)(smem + kTcStages * stage_bytes);
     uint64_t *empty = full + kTcStages;
     uint64_t *splitb = empty + kTcStages;
@@ -301,6 +315,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     mbar_expect_tx(&full[s], SPLIT_A ? stage_bytes - a_bytes : stage_bytes);
                     const int kx = (kb0 + i) * BK;
                     tma_load_2d(st, &tmAh, &full[s], kx, m0);
+                    if (DIG) {
+                        for (int r = 0; r < BN; r += bsub)
+                            tma_load_2d(st + a_bytes + (uint32_t)r * kTcRowBytes, &tmBh, &full[s], kx, n0 + r);
+                        continue;
+                    }
                     if (!SPLIT_A) tma_load_2d(st + a_bytes, &tmAl, &full[s], kx, m0);
                     tma_load_2d(st + 2 * a_bytes, &tmBh, &full[s], kx, n0);
                     tma_load_2d(st + 2 * a_bytes + b_bytes, &tmBl, &full[s], kx, n0);
@@ -317,7 +336,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     } else if (warp == 1) {
         if (lane == 0) {
             // ---- MMA issuer
-            const uint32_t idesc = F16 ? idesc_f16(BN, kTcBM) : idesc_tf32(BN, kTcBM);
+            const uint32_t idesc = F16 ? idesc_f16(DIG ? bsub : BN, kTcBM) : idesc_tf32(BN, kTcBM);
             const uint32_t idesc2 = F16 ? idesc_f16(2 * BN, kTcBM) : idesc_tf32(2 * BN, kTcBM);
             uint32_t g = 0;
             bool ok = true;
@@ -325,7 +344,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             for (int u = blockIdx.x; ok && u < units; u += gridDim.x, j++) {
                 const int kb0 = (u / tiles / ntn) * kb_per_split;
                 const int nkb = min(nkb_total, kb0 + kb_per_split) - kb0;
-                const uint32_t buf = j & 1, q = j >> 1;
+                const uint32_t buf = j % nbuf, q = j / nbuf;
                 if (q > 0 && !mbar_wait(&acc_empty[buf], (q - 1) & 1, err, 5)) break;
                 tc_fence_after();
                 const uint32_t acc = tmem + buf * acc_stride;
@@ -337,6 +356,19 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     }
                     tc_fence_after();
                     uint8_t *st = smem + s * stage_bytes;
+                    if (DIG) {
+                        const uint64_t da = sw_desc(st);
+#pragma unroll
+                        for (int kk = 0; kk < kTcRowBytes / 32; kk++) {
+                            const uint64_t off = (uint64_t)(kk * 32) >> 4;
+                            for (int r = 0; r < BN; r += bsub)
+                                mma_op<true>(acc + (uint32_t)r, da + off,
+                                             sw_desc(st + a_bytes + (uint32_t)r * kTcRowBytes) + off, idesc,
+                                             (i | kk) != 0);
+                        }
+                        mma_commit(&empty[s]);
+                        continue;
+                    }
                     const uint64_t dah = sw_desc(st), dal = sw_desc(st + a_bytes);
                     const uint64_t dbh = sw_desc(st + 2 * a_bytes);
                     const uint64_t dbl = sw_desc(st + 2 * a_bytes + b_bytes);
@@ -422,7 +454,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         for (int u = blockIdx.x; u < units; u += gridDim.x, j++) {
             const int tm = u % tiles, tn = (u / tiles) % ntn, split = u / tiles / ntn;
             const int m0 = tm * kTcBM, n0 = tn * BN;
-            const uint32_t buf = j & 1, q = j >> 1;
+            const uint32_t buf = j % nbuf, q = j / nbuf;
             bool have = mbar_wait(&acc_full[buf], q & 1, err, 3);
             // tcgen05.ld is warp-collective: the whole warp reads or none of it
             if (!__all_sync(0xffffffffu, have)) break;
@@ -566,18 +598,21 @@ static int tc_launch(int amode, const CUtensorMap &ah, const CUtensorMap &al, co
                      const CUtensorMap &bl, int M, int Nc, int Kd, int bk, float *Y, size_t ldy, int splits,
                      int *d_err, cudaStream_t st, const float *rsc, const float *csc, int gj_k = -1)
 {
-    // one column tile of all Nc columns, or tiles of 128 (the Gauss-Jordan update)
-    const int BN = gj_k >= 0 ? 128 : (Nc + 15) / 16 * 16;
+    // one column tile of all Nc columns, or tiles of 128 (the Gauss-Jordan
+    // update); above 256 columns (digits) a multiple of 32 (two halves)
+    int BN = gj_k >= 0 ? 128 : (Nc + 15) / 16 * 16;
+    if (BN > 256) BN = (Nc + 31) / 32 * 32;
     const int ntn = (Nc + BN - 1) / BN;
     // two accumulator buffers of 2 BN (COMB) or BN columns, each rounded up
-    // to a power of two
+    // to a power of two; one when two would pass the 512 TMEM columns
+    const bool comb = amode != 4 && BN <= 128 && BN % 32 == 0;
     uint32_t acc_stride = 32;
-    while (acc_stride < (uint32_t)((BN <= 128 && BN % 32 == 0) ? 2 * BN : BN)) acc_stride *= 2;
-    const int tmem_cols = 2 * (int)acc_stride;
+    while (acc_stride < (uint32_t)(comb ? 2 * BN : BN)) acc_stride *= 2;
+    const int tmem_cols = std::min(2 * (int)acc_stride, 512);
     const int nkb = (Kd + bk - 1) / bk;
     splits = splits_norm(nkb, splits);
     const int kps = (nkb + splits - 1) / splits;
-    const size_t smem = 1024 + (size_t)kTcStages * (2 * kTcBM + 2 * BN) * kTcRowBytes + 256;
+    const size_t smem = 1024 + (size_t)kTcStages * (amode == 4 ? kTcBM + BN : 2 * kTcBM + 2 * BN) * kTcRowBytes + 256;
     // persistent: one CTA per SM walks the (row tile, split) units
     static int nsm = 0;
     if (!nsm) {
@@ -590,7 +625,7 @@ static int tc_launch(int amode, const CUtensorMap &ah, const CUtensorMap &al, co
     // the shared-memory limit of each instantiation is raised to the largest
     // request seen on the device (once per size, not per launch)
     constexpr int kDevs = 16;
-    static int smem_set[kDevs][5] = {};
+    static int smem_set[kDevs][6] = {};
     int dev = 0;
     DSC_CUDA(cudaGetDevice(&dev));
     auto launch = [&](auto kern, int slot) -> int {
@@ -607,6 +642,7 @@ static int tc_launch(int amode, const CUtensorMap &ah, const CUtensorMap &al, co
     case 0: DSC_TRY(launch(k_tc_gemm3<0>, 0)); break;
     case 1: DSC_TRY(launch(k_tc_gemm3<1>, 1)); break;
     case 2: DSC_TRY(launch(k_tc_gemm3<2>, 2)); break;
+    case 4: DSC_TRY(launch(k_tc_gemm3<4>, 5)); break;
     default: DSC_TRY(launch(k_tc_gemm3<3>, 3)); break;
     }
     DSC_CUDA(cudaGetLastError());
@@ -648,6 +684,27 @@ int tc_gemm_3xf16(const __half *Ah, const __half *Al, size_t lda, const __half *
     DSC_TRY(make_map(&bh, Bh, 2, Nc, Kd, ldb, BN));
     DSC_TRY(make_map(&bl, Bl, 2, Nc, Kd, ldb, BN));
     return tc_launch(3, ah, al, bh, bl, M, Nc, Kd, kTcBK16, Y, ldy, splits, d_err, st, rsc, csc);
+}
+
+int tc_gemm_digits(const __half *A, size_t lda, const __half *B, size_t ldb, int M, int Nc, int Kd, float *Y,
+                   size_t ldy, int *d_err, cudaStream_t st)
+{
+    if (Nc < 1 || Nc > kTcMaxDigitCols || M < 1 || Kd < 1 || ldy < (size_t)M) {
+        set_error("tc_gemm_digits: unsupported shape M %d Nc %d Kd %d (Nc <= %d)", M, Nc, Kd, kTcMaxDigitCols);
+        return kErrArg;
+    }
+    int BN = (Nc + 15) / 16 * 16;
+    if (BN > 256) BN = (Nc + 31) / 32 * 32;
+    CUtensorMap a, b;
+    DSC_TRY(make_map(&a, A, 2, M, Kd, lda, kTcBM));
+    DSC_TRY(make_map(&b, B, 2, Nc, Kd, ldb, BN > 256 ? BN / 2 : BN));
+    return tc_launch(4, a, a, b, b, M, Nc, Kd, kTcBK16, Y, ldy, tc_digit_splits(Kd), d_err, st, nullptr, nullptr);
+}
+
+int tc_digit_splits(int Kd)
+{
+    const int nkb = (Kd + kTcBK16 - 1) / kTcBK16;
+    return splits_norm(nkb, (nkb + kTcDigitKBlocks - 1) / kTcDigitKBlocks);
 }
 
 struct TcGjPlan::Maps {
@@ -762,29 +819,70 @@ __global__ void k_row_exponent(const double *__restrict__ K, size_t ld, int N, i
     atomicMax(&rowE[i], e);
 }
 
-// The epilogue's row factors: rsK[i] = 2^-s_i for K's fp16 pair, rsdK[i] =
-// 2^-(s_i + 24) for that of K - fl32(K).
-__global__ void k_row_scales(const int *__restrict__ rowE, int N, float *__restrict__ rsK,
-                             float *__restrict__ rsdK)
+// The epilogue's row factors: rsK[i] = 2^-s_i for K's fp16 pair.
+__global__ void k_row_scales(const int *__restrict__ rowE, int N, float *__restrict__ rsK)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
-    const int sh = scale_shift(rowE[i], 1023);
-    rsK[i] = pow2f(-sh);
-    if (rsdK) rsdK[i] = pow2f(-sh - 24);
+    rsK[i] = pow2f(-scale_shift(rowE[i], 1023));
+}
+
+// ---------------------------------------------------------------- digits
+// Fixed-point digits for exact products on the tensor cores.  A value a
+// with |a| < 2^(E - 1022) (E: the biased FP64 exponent of the largest
+// magnitude in its row or column) is rounded to the integer V = round(a *
+// 2^(B - E + 1022)), |V| <= 2^B, and V is written in balanced digits of b
+// bits, q_0 2^(b (n - 1)) + ... + q_(n-1), |q| <= 2^(b - 1) (bn = B + 1).
+// The work is integer only: the 53-bit significand shifted right by the
+// exponent difference, rounded half up in magnitude; the digits of |V|,
+// negated for a < 0.  An fp16 holds the small integers exactly: the value
+// 1536 + q has the bits 0x6600 + q (1536 <= 1536 + q < 2048, one binade of
+// integer steps), and the subtraction of 1536 is exact.
+
+// |V| for a's significand M (53 bits): V = M 2^(E - 1075 + B - (Erow -
+// 1022)), a right shift by sh = Erow - E + off with off = 53 - B; 0 for
+// zeros, subnormals and shifts of 54 or more
+__device__ __forceinline__ unsigned long long digit_magnitude(double a, int Erow, int off)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(a);
+    const int E = (int)((b >> 52) & 0x7FF);
+    const int sh = Erow - E + off;
+    if (E == 0 || sh >= 54) return 0;
+    const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    return (m + (1ull << (sh - 1))) >> sh;
+}
+
+__device__ __forceinline__ __half digit_f16(int q)
+{
+    return __hsub(__ushort_as_half((unsigned short)(0x6600 + q)), __ushort_as_half((unsigned short)0x6600));
+}
+
+// The kKDigits base-2^kKDigitBits digits of a K entry (row exponent Erow):
+// B = 47, |q| <= 32.
+__device__ __forceinline__ void k_digits(double a, int Erow, __half *q)
+{
+    unsigned long long u = digit_magnitude(a, Erow, 53 - (kKDigits * kKDigitBits - 1));
+    const bool neg = __double_as_longlong(a) < 0;
+    const unsigned half = 1u << (kKDigitBits - 1), mask = (1u << kKDigitBits) - 1;
+#pragma unroll
+    for (int d = kKDigits - 1; d > 0; d--) {
+        const int t = (int)((unsigned)(u + half) & mask) - (int)half;
+        u = (u + half) >> kKDigitBits;
+        q[d] = digit_f16(neg ? -t : t);
+    }
+    q[0] = digit_f16(neg ? -(int)u : (int)u);
 }
 
 // Column-major FP64 K to row-major fp16 pairs (entry (i, c) at i * ldt + c)
-// of 2^s_i fl32(K) (Th, Tl) and, with Dh not null, of 2^(s_i + 24) (K -
-// fl32(K)) (Dh, Dl) (f64_split_rn): hi = rn_fp16(x), lo = rn_fp16(x - hi).
-// |K - fl32(K)| <= 2^-24 |K| entrywise and each row's largest entry scales
-// below 2^15, so both scaled matrices stay below 2^15 (fp16's largest
-// finite value is 65504).  A
-// 32 x 32 shared tile per block.
+// of 2^s_i fl32(K) (Th, Tl; hi = rn_fp16(x), lo = rn_fp16(x - hi)) and,
+// with Dg not null, to the kKDigits digit matrices of K (digit d at Dg + d *
+// dstride, same layout).  Each row's largest entry scales below 2^15, so
+// the pair stays below fp16's largest finite value (65504).  A 32 x 32
+// shared tile per block.
 __global__ void k_split_transpose_f16(const double *__restrict__ K, size_t ld, int N,
                                       const int *__restrict__ rowE, __half *__restrict__ Th,
-                                      __half *__restrict__ Tl, __half *__restrict__ Dh,
-                                      __half *__restrict__ Dl, size_t ldt)
+                                      __half *__restrict__ Tl, __half *__restrict__ Dg, size_t dstride,
+                                      size_t ldt)
 {
     __shared__ double t[32][33];
     const int i0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
@@ -797,18 +895,16 @@ __global__ void k_split_transpose_f16(const double *__restrict__ K, size_t ld, i
         int i = i0 + k, c = c0 + threadIdx.x;
         if (i < N && c < N) {
             const double a = t[threadIdx.x][k];
-            const int sh = scale_shift(rowE[i], 1023);
-            float v, r;
-            f64_split_rn(a, v, r);  // a = v + r, v = fl32(a) (one FP64-pipe conversion)
-            const float x = v * pow2f(sh);
+            const int Er = rowE[i];
+            const float x = (float)a * pow2f(scale_shift(Er, 1023));
             const __half h = __float2half_rn(x);
             Th[(size_t)i * ldt + c] = h;
             Tl[(size_t)i * ldt + c] = __float2half_rn(x - __half2float(h));
-            if (Dh) {
-                const float y = r * pow2f(sh + 24);
-                const __half dh = __float2half_rn(y);
-                Dh[(size_t)i * ldt + c] = dh;
-                Dl[(size_t)i * ldt + c] = __float2half_rn(y - __half2float(dh));
+            if (Dg) {
+                __half q[kKDigits];
+                k_digits(a, Er, q);
+#pragma unroll
+                for (int d = 0; d < kKDigits; d++) Dg[d * dstride + (size_t)i * ldt + c] = q[d];
             }
         }
     }
@@ -848,21 +944,123 @@ __global__ void __launch_bounds__(256) k_split_cols_f16(const T *__restrict__ x,
     if (threadIdx.x == 0) csc[blockIdx.x] = pow2f(-sh);
 }
 
-int k16_row_scales(const double *K, size_t ld, int N, int *rowE, float *rsK, float *rsdK, cudaStream_t st)
+int k16_row_scales(const double *K, size_t ld, int N, int *rowE, float *rsK, cudaStream_t st)
 {
     DSC_CUDA(cudaMemsetAsync(rowE, 0, (size_t)N * sizeof(int), st));
     const int chunks = 64, cols = (N + chunks - 1) / chunks;
     DSC_LAUNCH(k_row_exponent<<<dim3((N + 255) / 256, (N + cols - 1) / cols), 256, 0, st>>>(K, ld, N, cols, rowE));
-    DSC_LAUNCH(k_row_scales<<<(N + 255) / 256, 256, 0, st>>>(rowE, N, rsK, rsdK));
+    DSC_LAUNCH(k_row_scales<<<(N + 255) / 256, 256, 0, st>>>(rowE, N, rsK));
     DSC_CUDA(cudaGetLastError());
     return kOk;
 }
 
 int split_transpose_K16(const double *K, size_t ld, int N, const int *rowE, __half *Th, __half *Tl,
-                        __half *Dh, __half *Dl, size_t ldt, cudaStream_t st)
+                        __half *Dg, size_t dstride, size_t ldt, cudaStream_t st)
 {
     dim3 g((N + 31) / 32, (N + 31) / 32), b(32, 8);
-    DSC_LAUNCH(k_split_transpose_f16<<<g, b, 0, st>>>(K, ld, N, rowE, Th, Tl, Dh, Dl, ldt));
+    DSC_LAUNCH(k_split_transpose_f16<<<g, b, 0, st>>>(K, ld, N, rowE, Th, Tl, Dg, dstride, ldt));
+    DSC_CUDA(cudaGetLastError());
+    return kOk;
+}
+
+// Columns of X (column c: N entries at c * ldx) to kXDigits digits of
+// kXDigitBits bits each (B = 23, |q| <= 128), written as fp16 rows j * ncol
+// + c of Xd (stride ldd), colE[c] = the column's largest biased exponent,
+// and the remainder X - (the digits' value) (FP64, exact) at Xr.  One block
+// per column.
+__global__ void __launch_bounds__(256) k_x_digits(const double *__restrict__ X, size_t ldx, int N, int ncol,
+                                                  __half *__restrict__ Xd, size_t ldd, double *__restrict__ Xr,
+                                                  size_t ldr, int *__restrict__ colE)
+{
+    __shared__ int emax;
+    if (threadIdx.x == 0) emax = 0;
+    __syncthreads();
+    const int c = blockIdx.x;
+    const double *col = X + (size_t)c * ldx;
+    int e = 0;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) e = max(e, (__double2hiint(col[i]) >> 20) & 0x7FF);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(&emax, e);
+    __syncthreads();
+    const int Ec = emax;
+    constexpr int B = kXDigits * kXDigitBits - 1;
+    const unsigned half = 1u << (kXDigitBits - 1), mask = (1u << kXDigitBits) - 1;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        const double a = col[i];
+        // V = round(a 2^(B - Ec + 1022)): shift Ec - E + 1075 - 1022 - B
+        const unsigned long long u0 = digit_magnitude(a, Ec, 53 - B);
+        const bool neg = __double_as_longlong(a) < 0;
+        unsigned long long u = u0;
+#pragma unroll
+        for (int d = kXDigits - 1; d > 0; d--) {
+            const int t = (int)((unsigned)(u + half) & mask) - (int)half;
+            u = (u + half) >> kXDigitBits;
+            Xd[((size_t)d * ncol + c) * ldd + i] = digit_f16(neg ? -t : t);
+        }
+        Xd[(size_t)c * ldd + i] = digit_f16(neg ? -(int)u : (int)u);
+        const double v = ldexp(neg ? -(double)u0 : (double)u0, Ec - 1022 - B);
+        Xr[(size_t)c * ldr + i] = a - v;
+    }
+    if (threadIdx.x == 0) colE[c] = Ec;
+}
+
+int x_digits(const double *X, size_t ldx, int N, int ncol, __half *Xd, size_t ldd, double *Xr, size_t ldr,
+             int *colE, cudaStream_t st)
+{
+    DSC_LAUNCH(k_x_digits<<<ncol, 256, 0, st>>>(X, ldx, N, ncol, Xd, ldd, Xr, ldr, colE));
+    DSC_CUDA(cudaGetLastError());
+    return kOk;
+}
+
+// Y[c * ldy + m] (+)= 2^(kKDigitBits (kKDigits - 1 - i)) * sum over x digits
+// j < nj of 2^(kXDigitBits (kXDigits - 1 - j)) * (the S partial tiles of the
+// product of K digit i with x digit j; column j * ncol + c of the tiles).
+// The tiles hold integers below 2^24: they are summed as integers (exact),
+// then added in FP64.
+__global__ void k_digit_accumulate(const float *__restrict__ P, int S, size_t ldp, int ncol, int nj, int i,
+                                   int N, double *__restrict__ Y, size_t ldy, int first)
+{
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = blockIdx.y;
+    if (m >= N) return;
+    const size_t split_stride = ldp * (size_t)(nj * ncol);
+    long long t = 0;
+    for (int j = 0; j < nj; j++) {
+        int s = 0;
+        for (int k = 0; k < S; k++) s += __float2int_rn(P[k * split_stride + (size_t)(j * ncol + c) * ldp + m]);
+        t += (long long)s * (1ll << (kXDigitBits * (kXDigits - 1 - j)));
+    }
+    const double v = ldexp((double)t, kKDigitBits * (kKDigits - 1 - i));
+    double *y = Y + (size_t)c * ldy + m;
+    *y = first ? v : *y + v;
+}
+
+int digit_accumulate(const float *P, int S, size_t ldp, int ncol, int nj, int i, int N, double *Y, size_t ldy,
+                     bool first, cudaStream_t st)
+{
+    dim3 g((N + 255) / 256, ncol);
+    DSC_LAUNCH(k_digit_accumulate<<<g, 256, 0, st>>>(P, S, ldp, ncol, nj, i, N, Y, ldy, first ? 1 : 0));
+    DSC_CUDA(cudaGetLastError());
+    return kOk;
+}
+
+// Y[c * ldy + m] *= the units of K's row m and x's column c:
+// 2^(rowE[m] - 1022 - 47) * 2^(colE[c] - 1022 - 23)
+__global__ void k_digit_finish(const int *__restrict__ rowE, const int *__restrict__ colE, int N,
+                               double *__restrict__ Y, size_t ldy)
+{
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = blockIdx.y;
+    if (m >= N) return;
+    double *y = Y + (size_t)c * ldy + m;
+    *y = ldexp(*y, rowE[m] + colE[c] - 2044 - (kKDigits * kKDigitBits - 1) - (kXDigits * kXDigitBits - 1));
+}
+
+int digit_finish(const int *rowE, const int *colE, int N, int ncol, double *Y, size_t ldy, cudaStream_t st)
+{
+    dim3 g((N + 255) / 256, ncol);
+    DSC_LAUNCH(k_digit_finish<<<g, 256, 0, st>>>(rowE, colE, N, Y, ldy));
     DSC_CUDA(cudaGetLastError());
     return kOk;
 }
@@ -1024,11 +1222,21 @@ int add_splits(const float *P, int S, size_t split_stride, size_t ldp, int M, in
 
 using namespace dsc;
 
+namespace dsc {
+__global__ void k_f64_to_f16(const double *__restrict__ x, __half *__restrict__ y, size_t n)
+{
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+        y[t] = __float2half_rn((float)x[t]);  // exact for integers below 2048 in magnitude
+}
+}  // namespace dsc
+
 // Host-array entry point of the tensor-core product (row-major FP64 in and
 // out): Y (M x Nc) = A (M x Kd) * B^T (B: Nc x Kd) with 3xTF32 products
 // (a_in_smem 0: A as a tf32 pair, 1: plain FP32 A split in shared memory,
-// 2: the same in the biased encoding) or 3xFP16 products on per-row scaled
-// fp16 pairs (a_in_smem 3).
+// 2: the same in the biased encoding), 3xFP16 products on per-row scaled
+// fp16 pairs (a_in_smem 3), or the digit product of A and B rounded to
+// fp16 (a_in_smem 4: exact for integer entries |A| <= 32, |B| <= 128;
+// Nc <= 384; `splits` ignored).
 extern "C" int dsc_tc_gemm(int M, int Nc, int Kd, const double *A, const double *B, double *Y,
                            int splits, int a_in_smem)
 {
@@ -1038,12 +1246,12 @@ extern "C" int dsc_tc_gemm(int M, int Nc, int Kd, const double *A, const double 
         set_error("no CUDA device available");
         return kErrCuda;
     }
-    if (M < 1 || Kd < 1 || Nc < 1 || Nc > kTcMaxNc) {
-        set_error("dsc_tc_gemm: unsupported shape (1 <= Nc <= %d)", kTcMaxNc);
+    if (M < 1 || Kd < 1 || Nc < 1 || Nc > (a_in_smem == 4 ? kTcMaxDigitCols : kTcMaxNc)) {
+        set_error("dsc_tc_gemm: unsupported shape (1 <= Nc <= %d)", a_in_smem == 4 ? kTcMaxDigitCols : kTcMaxNc);
         return kErrArg;
     }
-    if (a_in_smem < 0 || a_in_smem > 3) {
-        set_error("dsc_tc_gemm: unknown operand mode %d (0 .. 3)", a_in_smem);
+    if (a_in_smem < 0 || a_in_smem > 4) {
+        set_error("dsc_tc_gemm: unknown operand mode %d (0 .. 4)", a_in_smem);
         return kErrArg;
     }
     cudaStream_t st = 0;
@@ -1059,6 +1267,30 @@ extern "C" int dsc_tc_gemm(int M, int Nc, int Kd, const double *A, const double 
                           cudaMemcpyHostToDevice));
     DSC_CUDA(cudaMemcpy2D(dB.p, lda * sizeof(double), B, Kd * sizeof(double), Kd * sizeof(double), Nc,
                           cudaMemcpyHostToDevice));
+    if (a_in_smem == 4) {
+        DevBuf<__half> a16, b16;
+        DSC_TRY(a16.alloc((size_t)M * lda));
+        DSC_TRY(b16.alloc((size_t)Nc * lda));
+        DSC_LAUNCH(k_f64_to_f16<<<4 * 152, 256, 0, st>>>(dA.p, a16.p, (size_t)M * lda));
+        DSC_LAUNCH(k_f64_to_f16<<<4 * 152, 256, 0, st>>>(dB.p, b16.p, (size_t)Nc * lda));
+        const int S = tc_digit_splits(Kd);
+        DSC_TRY(P.alloc((size_t)S * Nc * M));
+        DSC_TRY(err.alloc(1));
+        DSC_CUDA(cudaMemset(err.p, 0, sizeof(int)));
+        DSC_TRY(tc_gemm_digits(a16.p, lda, b16.p, lda, M, Nc, Kd, P.p, (size_t)M, err.p, st));
+        DSC_TRY(dY.alloc((size_t)M * Nc));
+        dim3 g((M + 255) / 256, Nc);
+        DSC_LAUNCH(k_sum_splits<<<g, 256, 0, st>>>(P.p, S, (size_t)M * Nc, (size_t)M, M, Nc, dY.p));
+        DSC_CUDA(cudaGetLastError());
+        int herr = 0;
+        DSC_CUDA(cudaMemcpy(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost));
+        if (herr) {
+            set_error("tensor-core GEMM: a pipeline wait gave up (code %d)", herr);
+            return kErrCuda;
+        }
+        DSC_CUDA(cudaMemcpy(Y, dY.p, (size_t)M * Nc * sizeof(double), cudaMemcpyDeviceToHost));
+        return kOk;
+    }
     if (a_in_smem == 3) {
         // 3xFP16: rows of A and of B to scaled fp16 pairs (row factors of A
         // and of B as the epilogue's row and column factors)

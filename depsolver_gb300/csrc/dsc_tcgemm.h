@@ -7,6 +7,21 @@
 
 namespace dsc {
 
+// Fixed-point digits of the FP64-accurate product K x (the mixed sweep's
+// first residual): K as kKDigits balanced digits of kKDigitBits bits per
+// row (|q| <= 32), x as kXDigits digits of kXDigitBits bits per column
+// (|q| <= 128): every digit product is at most 2^12 and a 4096-long sum of
+// them at most 2^24.
+constexpr int kKDigits = 8, kKDigitBits = 6;
+constexpr int kXDigits = 3, kXDigitBits = 8;
+// The x digits taken with K digit i: those whose weight is within 2^-48 of
+// the largest, kKDigitBits i + kXDigitBits j <= 48.
+constexpr int x_digits_for(int i)
+{
+    return (48 - kKDigitBits * i) / kXDigitBits + 1 < kXDigits ? (48 - kKDigitBits * i) / kXDigitBits + 1
+                                                               : kXDigits;
+}
+
 // Y[s][n][m] (split s, column n, row m; stride ldy per column and ldy * Nc
 // per split) = partial sums over split s's share of k of
 //   (Ah + Al)[m][k] * (Bh + Bl)[n][k]  with the three products hh + hl + lh.
@@ -31,6 +46,16 @@ int tc_gemm_3xf16(const __half *Ah, const __half *Al, size_t lda, const __half *
                   size_t ldb, int M, int Nc, int Kd, float *Y, size_t ldy, int splits, int *d_err,
                   cudaStream_t st, const float *rsc, const float *csc);
 int tc_gemm_f16_splits_for(int M, int Kd);
+// One fp16 product per split, for integer-valued operands ("digits"):
+// Y[s][n][m] = sum over split s's k-range of A[m][k] * B[n][k], each split
+// at most 4096 k long, so that with |A| <= 32 and |B| <= 128 (or any pair
+// whose product stays within 2^12) every partial sum is an integer of at
+// most 2^24 and exact in the FP32 accumulator.  Nc <= 384; row strides in
+// elements (multiples of 8, 16-byte aligned bases).  tc_digit_splits(Kd)
+// is the split count, S, the partial tiles Y holds (stride ldy * Nc).
+int tc_gemm_digits(const __half *A, size_t lda, const __half *B, size_t ldb, int M, int Nc, int Kd, float *Y,
+                   size_t ldy, int *d_err, cudaStream_t st);
+int tc_digit_splits(int Kd);
 // The Gauss-Jordan update of step k on the same kernel (3xFP16, K = 128):
 // for every 128 x 128 tile (I, J) of C (column-major, M x Nc, stride ldc)
 // with I != k: C_IJ -= A_I B_J^T (C_Ik = -A_I B_k^T); A (M x 128) and B
@@ -53,14 +78,28 @@ int tc_gj_plan(TcGjPlan &p, const __half *Ah, const __half *Al, size_t lda, cons
                const __half *Bl, size_t ldb, int M, int Nc, float *C, size_t ldc, int *d_err,
                const float *rsc, const float *csc);
 int tc_gj_run(const TcGjPlan &p, int k, cudaStream_t st);
-// Row scales of column-major FP64 K (stride ld): rowE (N ints, scratch) the
-// biased exponent of each row's largest entry, rsK = 2^-s_i, rsdK (may be
-// null) = 2^-(s_i + 24).
-int k16_row_scales(const double *K, size_t ld, int N, int *rowE, float *rsK, float *rsdK, cudaStream_t st);
-// K to the row-major scaled fp16 pairs of fl32(K) (Th, Tl) and, with Dh
-// not null, of K - fl32(K) (Dh, Dl), after k16_row_scales.
+// Row scales of column-major FP64 K (stride ld): rowE (N ints) the biased
+// exponent of each row's largest entry, rsK = 2^-s_i.
+int k16_row_scales(const double *K, size_t ld, int N, int *rowE, float *rsK, cudaStream_t st);
+// K to the row-major scaled fp16 pair of fl32(K) (Th, Tl) and, with Dg not
+// null, to K's kKDigits row digits (digit d at Dg + d * dstride: fp16
+// integers, K[i][c] ~ 2^(rowE[i] - 1069) sum_d q_d 2^(kKDigitBits
+// (kKDigits - 1 - d))), after k16_row_scales.
 int split_transpose_K16(const double *K, size_t ld, int N, const int *rowE, __half *Th, __half *Tl,
-                        __half *Dh, __half *Dl, size_t ldt, cudaStream_t st);
+                        __half *Dg, size_t dstride, size_t ldt, cudaStream_t st);
+// Columns of X (ncol, N entries each, stride ldx) to their kXDigits digits
+// (digit j of column c: fp16 row j * ncol + c of Xd, stride ldd;
+// X[c][i] = 2^(colE[c] - 1045) sum_j q_j 2^(kXDigitBits (kXDigits - 1 - j))
+// + Xr[c][i], the remainder exact in FP64, stride ldr).
+int x_digits(const double *X, size_t ldx, int N, int ncol, __half *Xd, size_t ldd, double *Xr, size_t ldr,
+             int *colE, cudaStream_t st);
+// Y (FP64, column c at c * ldy; first: =, else +=) gets the product of K
+// digit i with the first nj x digits from tc_gemm_digits' S partial tiles
+// P (column j * ncol + c at stride ldp), weighted by the digits' places.
+int digit_accumulate(const float *P, int S, size_t ldp, int ncol, int nj, int i, int N, double *Y, size_t ldy,
+                     bool first, cudaStream_t st);
+// Y *= the units of K's rows and x's columns: Y = K x (digit parts).
+int digit_finish(const int *rowE, const int *colE, int N, int ncol, double *Y, size_t ldy, cudaStream_t st);
 // Columns (N entries each, stride ldx) to scaled fp16 pairs (stride ldh),
 // csc[n] = the column's 2^-t_n.
 int split_cols_f16(const double *x, size_t ldx, int N, int ncol, __half *h, __half *l, size_t ldh,

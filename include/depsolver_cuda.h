@@ -203,10 +203,10 @@ int dsc_session_solve(dsc_session *s, int mode, unsigned nfreq, const double *fr
  *       4 K GEMM (mixed, tensor cores)   flops of the three fp16 products
  *       5 field                          (particle node, element) pairs x systems
  *       6 Maxwell stress                 0
- *       7 FP64-accurate residual GEMM    multiply-adds
+ *       7 FP64-accurate residual         digit multiply-adds (tensor cores)
  *       8 other Krylov kernels           0
  *       9 Gram-Schmidt passes            bytes the kernels read and wrote
- *      10 K to its fp16 pairs (mixed)    bytes read and written
+ *      10 K to its fp16 pair and digits  bytes read and written
  *      11 conductor-block inverses       flops of the Gauss-Jordan updates
  *      12 conductor-block products       flops of the three fp16 products */
 int dsc_session_set_timing(dsc_session *s, int on);
@@ -237,7 +237,10 @@ int dsc_session_timing(dsc_session *s, double *ms, int *count, double *work, int
  * stored in a biased encoding whose truncation to tf32 is the rounded hi;
  * 3 (the mixed sweep's mode) scales each row of A and of B by a power of two
  * and splits it into an fp16 pair, products on the fp16 tensor path (twice
- * the tf32 rate), the scales multiplied back out in the epilogue. */
+ * the tf32 rate), the scales multiplied back out in the epilogue; 4 is the
+ * digit product of the mixed sweep's first residual: A and B rounded to
+ * fp16 and one product per split of at most 4096 k, exact for integer
+ * entries |A| <= 32 and |B| <= 128 (Nc <= 384, splits ignored). */
 int dsc_tc_gemm(int M, int Nc, int Kd, const double *A, const double *B, double *Y, int splits,
                 int a_in_smem);
 

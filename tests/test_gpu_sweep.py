@@ -80,7 +80,9 @@ def test_session_timing_counts_kernels(gpu):
     # each Gram-Schmidt pass reads at least one basis vector of every
     # active system (16 bytes per row and system)
     assert t["gram_schmidt"][2] >= 16.0 * sc.N * t["gram_schmidt"][1]
-    assert t["asm_regular"][1] == 0 and t["residual_fp64"][2] == sc.N * sc.N * 2 * F
+    # the first residual's digit products: 8 digits of K against 3, 3, 3,
+    # 3, 3, 3, 2, 1 digits of the 2F solution columns
+    assert t["asm_regular"][1] == 0 and t["residual_fp64"][2] == sc.N * sc.N * 2 * F * 21
 
 
 @pytest.mark.parametrize("nen", [6, 3])

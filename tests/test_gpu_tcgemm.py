@@ -66,3 +66,26 @@ def test_tc_gemm_f16_scales_rows_and_columns(gpu):
     bound = np.abs(A) @ np.abs(B).T
     assert np.all(np.abs(Y - ref) <= 2e-6 * bound + 1e-300), float(np.nanmax(np.abs(Y - ref) / bound))
     assert np.all(Y[:, 3] == 0.0)
+
+
+@pytest.mark.parametrize("M,Nc,Kd", [
+    (300, 384, 10000),  # three splits of at most 4096, two MMAs of 192 columns
+    (257, 256, 4096),   # one full split
+    (128, 16, 77),      # ragged k
+    (1000, 200, 9000),
+])
+def test_tc_gemm_digits_exact(gpu, M, Nc, Kd):
+    """The digit product (mode 4) is exact: integer operands |A| <= 32,
+    |B| <= 128 give integer partial sums of at most 2^24 per split, which
+    the FP32 accumulator must hold without rounding whatever its order."""
+    rng = np.random.default_rng(M * Nc + Kd)
+    A = rng.integers(-32, 33, (M, Kd))
+    B = rng.integers(-128, 129, (Nc, Kd))
+    # rows at the bound: every product +4096 (the partial sums reach 2^24)
+    A[0] = 32
+    B[0] = 128
+    A[1] = -32
+    B[1] = np.where(np.arange(Kd) % 2 == 0, 128, -127)  # alternating, no cancellation to zero
+    Y = _run(gpu, A.astype(float), B.astype(float), 0, 4)
+    ref = A.astype(np.int64) @ B.astype(np.int64).T
+    assert np.array_equal(Y, ref.astype(float)), float(np.abs(Y - ref).max())
