@@ -107,6 +107,9 @@ def force_mst(sc: Scene, vB: np.ndarray, eps: float | None = None):
 
 MODE_FP64 = 1
 MODE_MIXED = 2
+# arithmetic of the mixed mode's regular pairs (Session.set_mixed_assembly)
+ASM_DF32 = 1
+ASM_FP32 = 2
 TIMER_NAMES = ("asm_regular", "asm_fixup", "asm_singular", "gemv_K64", "gemm_K", "field", "mst",
                "residual_fp64", "krylov", "gram_schmidt", "convert_K", "precond_build",
                "precond_apply")
@@ -158,6 +161,11 @@ class Session:
 
     def set_timing(self, on: bool):
         _native.check(self._L.dsc_session_set_timing(self._h, int(on)))
+
+    def set_mixed_assembly(self, prec: int):
+        """Mixed mode's regular pairs: ASM_FP32 (default; ~1e-7 per entry)
+        or ASM_DF32 (double-FP32, within ~1e-13 of FP64)."""
+        _native.check(self._L.dsc_session_set_mixed_assembly(self._h, int(prec)))
 
     def set_preconditioner(self, on: bool):
         """Mixed mode: the conductor-block right preconditioner (default on)."""

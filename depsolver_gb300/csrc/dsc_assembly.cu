@@ -322,6 +322,156 @@ __global__ void __launch_bounds__(128) k_asm_regular_df32(AsmArgs a, const float
     }
 }
 
+// ---- the regular pairs in FP32 (the mixed mode's far-field assembly):
+// each element's quadrature points as FP32 offsets from its centroid, the
+// row point's offset from the centroid from double-FP32 coordinates, so the
+// differences x - y carry FP32's relative accuracy whatever the distance
+// from the origin; about 1e-7 of each entry.  The centroid-relative form is
+// also what makes near pairs safe (no cancellation of large coordinates).
+
+// Per element: centroid (double-FP32 x, y, z) and per point (offset x, y,
+// z, w_q J_q) in FP32.
+__global__ void k_qp_local(const double *__restrict__ qp, int E, float2 *__restrict__ cen,
+                           float4 *__restrict__ qloc)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    const double *q = qp + (size_t)e * kTriPts * 4;
+    double c[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int t = 0; t < kTriPts; t++)
+#pragma unroll
+        for (int d = 0; d < 3; d++) c[d] += q[4 * t + d];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const float2 cd = df_from(c[d] / kTriPts);
+        cen[(size_t)e * 3 + d] = cd;
+        c[d] = (double)cd.x + (double)cd.y;  // the centroid as the kernel sees it
+    }
+#pragma unroll
+    for (int t = 0; t < kTriPts; t++)
+        qloc[(size_t)e * kTriPts + t] = make_float4((float)(q[4 * t] - c[0]), (float)(q[4 * t + 1] - c[1]),
+                                                    (float)(q[4 * t + 2] - c[2]), (float)q[4 * t + 3]);
+}
+
+// FP32 to FP64 by integer operations (a register move, no FP64-pipe work):
+// sign, exponent rebiased by 1023 - 127, significand shifted into place.
+// Subnormal FP32 values (below 1.2e-38) become zero.
+__device__ __forceinline__ double f32_widen(float v)
+{
+    const unsigned u = __float_as_uint(v);
+    const unsigned e = (u >> 23) & 0xFFu;
+    if (e == 0) return __hiloint2double((int)(u & 0x80000000u), 0);
+    const unsigned e64 = e == 0xFFu ? 0x7FFu : e + 896u;
+    return __hiloint2double((int)((u & 0x80000000u) | (e64 << 20) | ((u >> 3) & 0xFFFFFu)), (int)(u << 29));
+}
+
+template <int NEN>
+__device__ __forceinline__ float shape_q_f(int q, int k)
+{
+    return NEN == 3 ? c_shape3_df.hi[q][k] : c_shape6_df.hi[q][k];
+}
+
+template <int NEN, int MODE>
+__device__ __forceinline__ void pair_regular_f32(const float4 *__restrict__ q7, float dx0, float dy0, float dz0,
+                                                 float nx, float ny, float nz, bool isH, float *acc)
+{
+#pragma unroll
+    for (int q = 0; q < kTriPts; q++) {
+        const float4 Q = q7[q];
+        const float dx = dx0 - Q.x, dy = dy0 - Q.y, dz = dz0 - Q.z;
+        const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        const float inv = rsqrtf(r2);
+        float w;
+        if (MODE == 0) {
+            w = Q.w * inv;
+        } else {
+            const float h = Q.w * (inv * inv * inv) * fmaf(dz, nz, fmaf(dy, ny, dx * nx));
+            w = (MODE == 1 || isH) ? h : Q.w * inv;
+        }
+#pragma unroll
+        for (int k = 0; k < NEN; k++) acc[k] = fmaf(w, shape_q_f<NEN>(q, k), acc[k]);
+    }
+}
+
+// As k_asm_regular_df32 (same tiles, footprints and partial slots), with the
+// pair integrals, the row factor and the footprint sums in FP32.
+template <int NEN>
+__global__ void __launch_bounds__(128) k_asm_regular_f32(AsmArgs a, const float2 *__restrict__ cen,
+                                                         const float4 *__restrict__ qloc, double *__restrict__ K,
+                                                         double *__restrict__ P)
+{
+    constexpr int R = kRowTile, EG = kGroup;
+    __shared__ float4 s_q[EG * kTriPts];
+    __shared__ float2 s_c[EG * 3];
+    __shared__ float s_V[EG * NEN * R];
+    __shared__ int s_nodes[EG * NEN];
+    const int g = blockIdx.y;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+
+    for (int t = threadIdx.x; t < EG * kTriPts; t += blockDim.x) {
+        const int e = a.grp_elem[g * EG + t / kTriPts];
+        s_q[t] = e >= 0 ? qloc[(size_t)e * kTriPts + t % kTriPts] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    for (int t = threadIdx.x; t < EG * 3; t += blockDim.x) {
+        const int e = a.grp_elem[g * EG + t / 3];
+        s_c[t] = e >= 0 ? cen[(size_t)e * 3 + t % 3] : make_float2(0.f, 0.f);
+    }
+    for (int t = threadIdx.x; t < EG * NEN; t += blockDim.x) {
+        const int e = a.grp_elem[g * EG + t / NEN];
+        s_nodes[t] = e >= 0 ? a.elems[(size_t)e * NEN + t % NEN] : -1;
+    }
+    __syncthreads();
+
+    const int i = a.row_lo + blockIdx.x * R + lane;
+    const bool valid = i < a.row_hi;
+    const int ii = valid ? i : a.row_lo;
+    const float2 xi = df_from(a.X[ii]), yi = df_from(a.Y[ii]), zi = df_from(a.Z[ii]);
+    const float nx = (float)a.normals[3 * (size_t)ii], ny = (float)a.normals[3 * (size_t)ii + 1],
+                nz = (float)a.normals[3 * (size_t)ii + 2];
+    const int kind = valid ? a.row_kind[ii] : 0;
+    const float fac = (float)a.row_fac[ii];
+    const bool allG = __all_sync(0xffffffffu, kind == 0);
+    const bool allH = __all_sync(0xffffffffu, kind == 1);
+
+    for (int el = w; el < EG; el += 4) {
+        float acc[NEN];
+#pragma unroll
+        for (int k = 0; k < NEN; k++) acc[k] = 0.f;
+        const int *en = s_nodes + el * NEN;
+        bool drop = en[0] < 0;
+#pragma unroll
+        for (int k = 0; k < NEN; k++) drop |= en[k] == i;
+        if (en[0] >= 0) {
+            // the row point relative to the centroid: both parts of each
+            // double-FP32 coordinate, the high parts' difference first
+            const float2 *c = s_c + el * 3;
+            const float dx = (xi.x - c[0].x) + (xi.y - c[0].y);
+            const float dy = (yi.x - c[1].x) + (yi.y - c[1].y);
+            const float dz = (zi.x - c[2].x) + (zi.y - c[2].y);
+            const float4 *q7 = s_q + el * kTriPts;
+            if (allG) pair_regular_f32<NEN, 0>(q7, dx, dy, dz, nx, ny, nz, false, acc);
+            else if (allH) pair_regular_f32<NEN, 1>(q7, dx, dy, dz, nx, ny, nz, true, acc);
+            else pair_regular_f32<NEN, 2>(q7, dx, dy, dz, nx, ny, nz, kind == 1, acc);
+        }
+#pragma unroll
+        for (int k = 0; k < NEN; k++) s_V[(el * NEN + k) * R + lane] = drop ? 0.f : fac * acc[k];
+    }
+    __syncthreads();
+
+    const int f0 = a.fp_ptr[g], f1 = a.fp_ptr[g + 1];
+    for (int j = f0 + w; j < f1; j += 4) {
+        const int s0 = a.fp_sl_ptr[j], s1 = a.fp_sl_ptr[j + 1];
+        float sum = 0.f;
+        for (int m = s0; m < s1; m++) sum += s_V[a.fp_sl[m] * R + lane];
+        const int dest = a.fp_dest[j];
+        if (valid) {
+            if (dest >= 0) K[(size_t)dest * a.ld + i] = f32_widen(sum);
+            else P[(size_t)(-dest - 1) * a.ldp + (i - a.row_lo)] = f32_widen(sum);
+        }
+    }
+}
+
 // K column of every node shared by several groups = sum of its slots in
 // group order; nodes in no element get a zero column.
 template <typename T>
@@ -394,10 +544,11 @@ static size_t regular_smem(int nen)
 
 template <int NEN>
 static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStream_t st, Timer *tm,
-                              bool df32, AsmWorkspace *ws)
+                              int prec, AsmWorkspace *ws)
 {
     AsmWorkspace local;
     AsmWorkspace &w = ws ? *ws : local;
+    const bool df32 = prec == kAsmDf32, f32 = prec == kAsmF32;
     DSC_LAUNCH(k_elem_qp<NEN><<<(m.E * kTriPts + 255) / 256, 256, 0, st>>>(m.x.p, m.y.p, m.z.p, m.elems.p, m.E,
                                                                   m.qp.p));
     DSC_CUDA(cudaGetLastError());
@@ -405,6 +556,11 @@ static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStr
     if (df32) {
         DSC_TRY(qpd.alloc((size_t)m.E * kTriPts * 4));
         DSC_LAUNCH(k_qp_to_df<<<4 * 152, 256, 0, st>>>(m.qp.p, (size_t)m.E * kTriPts * 4, qpd.p));
+    }
+    if (f32) {
+        DSC_TRY(w.cen.alloc((size_t)m.E * 3));
+        DSC_TRY(w.qloc.alloc((size_t)m.E * kTriPts));
+        DSC_LAUNCH(k_qp_local<<<(m.E + 127) / 128, 128, 0, st>>>(m.qp.p, m.E, w.cen.p, w.qloc.p));
     }
     // Partial-sum buffer: n_slots columns of a row chunk, at most ~1 GiB.
     const size_t budget = (size_t)1 << 30;
@@ -431,7 +587,8 @@ static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStr
         dim3 grid((hi - lo + kRowTile - 1) / kRowTile, m.G);
         {
             TimerScope ts(tm, kTAsmRegular, st);
-            if (df32) DSC_LAUNCH(k_asm_regular_df32<NEN><<<grid, 128, smem, st>>>(a, qpd.p, K, P.p));
+            if (f32) DSC_LAUNCH(k_asm_regular_f32<NEN><<<grid, 128, 0, st>>>(a, w.cen.p, w.qloc.p, K, P.p));
+            else if (df32) DSC_LAUNCH(k_asm_regular_df32<NEN><<<grid, 128, smem, st>>>(a, qpd.p, K, P.p));
             else DSC_LAUNCH(k_asm_regular_f64<NEN><<<grid, 128, smem, st>>>(a, K, P.p));
             if (tm) tm->add_work(kTAsmRegular, (double)(hi - lo) * m.E);  // (row, element) pairs
         }
@@ -456,11 +613,11 @@ static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStr
     return kOk;
 }
 
-int assemble_K_fp64(const DeviceMesh &m, double *K, size_t ld, cudaStream_t st, Timer *tm, bool df32,
+int assemble_K_fp64(const DeviceMesh &m, double *K, size_t ld, cudaStream_t st, Timer *tm, int prec,
                     AsmWorkspace *ws)
 {
-    return m.nen == 6 ? assemble_fp64_impl<6>(m, K, ld, st, tm, df32, ws)
-                      : assemble_fp64_impl<3>(m, K, ld, st, tm, df32, ws);
+    return m.nen == 6 ? assemble_fp64_impl<6>(m, K, ld, st, tm, prec, ws)
+                      : assemble_fp64_impl<3>(m, K, ld, st, tm, prec, ws);
 }
 
 }  // namespace dsc

@@ -230,18 +230,24 @@ struct DeviceMesh {
 // rows, int H N_c (normal derivative, sign as the reference) for interface
 // rows.  The frequency enters only through per-row coefficients.
 // Device workspace of an assembly (partial slots, double-FP32 quadrature
-// points); a caller that assembles repeatedly keeps one to avoid
-// allocating every time.
+// points, FP32 centroid-relative points); a caller that assembles
+// repeatedly keeps one to avoid allocating every time.
 struct AsmWorkspace {
     DevBuf<double> P;
     DevBuf<float2> qpd;
+    DevBuf<float2> cen;
+    DevBuf<float4> qloc;
 };
 
-// df32: the regular pairs in double-FP32 on the FP32 pipes (about 2^-46
-// per operation; the mixed-precision path), else in FP64 (the reference's
-// arithmetic).  Singular pairs are FP64 either way; K is FP64.  ws (may be
-// null: a local one, freed before returning) holds the scratch.
+// Arithmetic of the regular pairs, most accurate first: FP64 (the
+// reference's), double-FP32 on the FP32 pipes (about 2^-46 per operation),
+// FP32 (about 1e-7 per entry: the mixed mode's far-field assembly).
+enum { kAsmF64 = 0, kAsmDf32 = 1, kAsmF32 = 2 };
+
+// prec: one of the above for the regular pairs.  Singular pairs are FP64
+// whatever prec is; K is FP64.  ws (may be null: a local one, freed before
+// returning) holds the scratch.
 int assemble_K_fp64(const DeviceMesh &m, double *K, size_t ld, cudaStream_t st, Timer *tm = nullptr,
-                    bool df32 = false, AsmWorkspace *ws = nullptr);
+                    int prec = kAsmF64, AsmWorkspace *ws = nullptr);
 
 }  // namespace dsc

@@ -186,12 +186,13 @@ int Session::assemble64(bool need_fp64)
 {
     // a K assembled in FP64 serves both modes; one assembled in
     // double-FP32 serves the mixed mode only
-    if (k64_ready && (!need_fp64 || !k64_df32)) return kOk;
+    const int want = need_fp64 ? kAsmF64 : mixed_asm;
+    if (k64_ready && k64_prec <= want) return kOk;
     k16_ready = false;  // the fp16 copies and the preconditioner follow K
     if (pre) pre->ready = false;
     DSC_TRY(K64.alloc(ld * N));
-    DSC_TRY(assemble_K_fp64(dev, K64.p, ld, st, &timer, !need_fp64, &asm_ws));
-    k64_df32 = !need_fp64;
+    DSC_TRY(assemble_K_fp64(dev, K64.p, ld, st, &timer, want, &asm_ws));
+    k64_prec = want;
     DSC_TRY(Kdiag.alloc(N));
     DSC_LAUNCH(k_diag<<<(N + 255) / 256, 256, 0, st>>>(K64.p, ld, N, Kdiag.p));
     DSC_CUDA(cudaGetLastError());
@@ -313,6 +314,16 @@ extern "C" int dsc_session_set_timing(dsc_session *s, int on)
 extern "C" int dsc_session_set_preconditioner(dsc_session *s, int on)
 {
     s->s.pre_on = on != 0;
+    return kOk;
+}
+
+extern "C" int dsc_session_set_mixed_assembly(dsc_session *s, int prec)
+{
+    if (prec != DSC_ASM_FP32 && prec != DSC_ASM_DF32) {
+        set_error("dsc_session_set_mixed_assembly: unknown arithmetic %d", prec);
+        return kErrArg;
+    }
+    s->s.mixed_asm = prec == DSC_ASM_FP32 ? kAsmF32 : kAsmDf32;
     return kOk;
 }
 

@@ -45,7 +45,8 @@ struct Session {
 
     // FP64 geometric matrix and its diagonal
     bool k64_ready = false;
-    bool k64_df32 = false;  // K64's regular pairs were integrated in double-FP32
+    int k64_prec = kAsmF64;   // arithmetic K64's regular pairs were integrated in
+    int mixed_asm = kAsmF32;  // the mixed mode's choice (kAsmF32 or kAsmDf32)
     AsmWorkspace asm_ws;    // kept between assemblies
     DevBuf<double> K64, Kdiag;
     std::vector<double> Kdiag_host;
@@ -72,7 +73,7 @@ struct Session {
                unsigned nMat, const double *mat);
     ~Session();
     // K64 (and Kdiag) if not there yet; need_fp64: the regular pairs in FP64
-    // (else double-FP32 is enough and is what a new assembly uses)
+    // (else in mixed_asm's arithmetic; a more accurate K64 is kept)
     int assemble64(bool need_fp64);
     int make_k16();
     void coeffs(double f, std::vector<double> &a, std::vector<double> &b,

@@ -182,11 +182,23 @@ void dsc_session_destroy(dsc_session *s);
 /* Assembles the geometric matrix now, again if it already exists
  * (otherwise the first solve assembles it and later solves reuse it).
  * mode DSC_MODE_FP64: regular pairs in FP64, the reference's arithmetic;
- * DSC_MODE_MIXED: regular pairs in double-FP32 on the FP32 pipes (about
- * 2^-46 per operation, entries within ~1e-13 of FP64) and the FP32 copy for
- * the tensor cores.  Singular pairs are FP64 in both.  An FP64 solve on a
- * matrix assembled for the mixed mode assembles it again in FP64. */
+ * DSC_MODE_MIXED: regular pairs in the arithmetic dsc_session_set_mixed_
+ * assembly chose, and the fp16 copies for the tensor cores.  Singular pairs
+ * are FP64 in both.  An FP64 solve on a matrix assembled for the mixed mode
+ * assembles it again in FP64; a mixed solve keeps a more accurate matrix. */
 int dsc_session_assemble(dsc_session *s, int mode);
+/* Arithmetic of the mixed mode's regular (non-singular) pairs:
+ *   DSC_ASM_FP32 (default) -- FP32, with each element's quadrature points
+ *     as offsets from its centroid (about 1e-7 of each entry: the far-field
+ *     assembly in FP32; the solution follows that matrix to ~1e-7, the
+ *     Maxwell-stress force to ~1e-9 of the sum of |Fce| on the 12k-node
+ *     scene);
+ *   DSC_ASM_DF32 -- double-FP32 on the FP32 pipes (about 2^-46 per
+ *     operation, entries within ~1e-13 of FP64; the mixed solution then
+ *     matches the FP64 one to ~1e-10). */
+#define DSC_ASM_FP32 2
+#define DSC_ASM_DF32 1
+int dsc_session_set_mixed_assembly(dsc_session *s, int prec);
 /* The geometric matrix K (N x N) as assembled for `mode` (assembling it if
  * needed): K[c * ldk + i] = entry (row i, node c), i.e. C * int G N_c for
  * conductor rows and int H N_c for interface rows (src/assembly_el.c). */

@@ -2,8 +2,10 @@
 
 The plain FP64 path must reproduce the reference's GMRES (through the
 strict compact path and the checker); the mixed path must reach the FP64
-solution: nodal solution within 1e-9 relative and Maxwell-stress force within
-1e-6 of the force scale (sum over particle elements of |Fce|).
+solution: Maxwell-stress force within 1e-6 of the force scale (sum over
+particle elements of |Fce|), and the nodal solution within 1e-9 relative
+when the matrix's regular pairs are assembled in double-FP32, within 1e-5
+(the FP32 entries' ~1e-7 times the conditioning) when they are FP32.
 """
 import numpy as np
 import pytest
@@ -32,24 +34,26 @@ def test_fp64_session_matches_reference_gmres(gpu, port, nen):
     assert np.allclose(forces[0, 6:9], np.abs(Fce[pel]).sum(0), rtol=1e-9)
 
 
+@pytest.mark.parametrize("asm,sig_tol", [(api.ASM_DF32, 1e-9), (api.ASM_FP32, 1e-5)])
 @pytest.mark.parametrize("nen", [6, 3])
-def test_mixed_matches_fp64_across_frequencies(gpu, port, nen):
+def test_mixed_matches_fp64_across_frequencies(gpu, port, nen, asm, sig_tol):
     sc = scenes.small(nen=nen, sphere_level=2, plate_cells=4)
     freqs = np.logspace(3, 8, 6)
     s = api.Session(sc)
-    # the mixed solve first: it assembles K with double-FP32 regular pairs;
-    # the FP64 solve then assembles it again in FP64
+    s.set_mixed_assembly(asm)
+    # the mixed solve first: it assembles K with double-FP32 or FP32 regular
+    # pairs; the FP64 solve then assembles it again in FP64
     fmx, itmx, smx = s.solve(freqs, mode=api.MODE_MIXED, tol=1e-11, want_sigma=True)
     f64, it64, s64 = s.solve(freqs, mode=api.MODE_FP64, tol=1e-12, want_sigma=True)
     for k in range(len(freqs)):
-        assert relerr(smx[k], s64[k]) < 1e-9, k
+        assert relerr(smx[k], s64[k]) < sig_tol, k
         scale = f64[k, 6:9].sum()
         assert np.abs(fmx[k, :3] - f64[k, :3]).max() <= FORCE_TOL * scale, k
     # the reference's own solution at one frequency, by the checker
     scf = sc.with_freq(freqs[2])
     Ap, Bp = port.assemble(scf)
     xp, _, st = port.gmres(Ap, Bp, tol=1e-12)
-    assert st == 0 and relerr(smx[2], xp) < 1e-9
+    assert st == 0 and relerr(smx[2], xp) < sig_tol
 
 
 def test_sweep_equals_session(gpu):
@@ -91,6 +95,7 @@ def test_double_fp32_assembly_matches_fp64(gpu, port, nen):
     against the FP64 assembly and the C restatement of the reference."""
     sc = scenes.small(nen=nen)
     s = api.Session(sc)
+    s.set_mixed_assembly(api.ASM_DF32)
     s.assemble(api.MODE_MIXED)
     Kd = s.geometric_matrix(api.MODE_MIXED)
     K64 = s.geometric_matrix(api.MODE_FP64)      # assembles again in FP64
@@ -104,6 +109,23 @@ def test_double_fp32_assembly_matches_fp64(gpu, port, nen):
     assert relerr(K64[cond], A[cond][:, :N]) < 1e-12
 
 
+@pytest.mark.parametrize("nen", [6, 3])
+def test_fp32_assembly_matches_fp64(gpu, nen):
+    """K with the regular pairs in FP32 (centroid-relative offsets): every
+    entry within a few FP32 units of its row's scale of the FP64 one."""
+    sc = scenes.small(nen=nen)
+    s = api.Session(sc)
+    s.set_mixed_assembly(api.ASM_FP32)
+    s.assemble(api.MODE_MIXED)
+    Kf = s.geometric_matrix(api.MODE_MIXED)
+    K64 = s.geometric_matrix(api.MODE_FP64)
+    rowmax = np.abs(K64).max(axis=1)               # row i = collocation node
+    err = np.abs(Kf - K64).max(axis=1) / rowmax
+    assert err.max() <= 2e-6, float(err.max())
+    assert np.linalg.norm(Kf - K64) <= 1e-6 * np.linalg.norm(K64)
+    assert not np.array_equal(Kf, K64)
+
+
 def test_conductor_preconditioner_cuts_iterations_not_accuracy(gpu):
     """The conductor-block right preconditioner (one block per plate) leaves
     the solution that of the unpreconditioned system -- both runs within
@@ -111,6 +133,7 @@ def test_conductor_preconditioner_cuts_iterations_not_accuracy(gpu):
     sc = scenes.small(nen=6, sphere_level=2, plate_cells=6)
     freqs = np.logspace(3, 8, 4)
     s = api.Session(sc)
+    s.set_mixed_assembly(api.ASM_DF32)
     ntop = int((sc.bctype[: sc.N] == 1).sum())
     assert s.preconditioner_blocks() == [ntop // 2, ntop // 2]
     f_on, it_on, s_on = s.solve(freqs, mode=api.MODE_MIXED, tol=1e-11, want_sigma=True)
