@@ -489,6 +489,11 @@ __global__ void k_asm_fixup(const int *__restrict__ fix_ptr, const int *__restri
 }
 
 // Singular pairs: warp per row, adds into K (FP64 sums, stored as T).
+// Rows with row_grad[i] set (row_grad may be null) also store the gradient
+// integral of each of their singular elements (warp_singular_H's FLAG 1
+// sums, 3 NEN per tuple t of ne_ptr's numbering) at Wg + t * 3 NEN: the
+// field's singular part at that node, taken from the same points as the
+// row's H integral.
 template <int NEN, typename T>
 __global__ void __launch_bounds__(128) k_asm_singular(const double *__restrict__ X,
                                                       const double *__restrict__ Y,
@@ -500,11 +505,14 @@ __global__ void __launch_bounds__(128) k_asm_singular(const double *__restrict__
                                                       const int *__restrict__ ne_ptr,
                                                       const int *__restrict__ ne_elem,
                                                       const int *__restrict__ ne_pos, int row_lo,
-                                                      int row_hi, T *__restrict__ K, size_t ld)
+                                                      int row_hi, T *__restrict__ K, size_t ld,
+                                                      const int *__restrict__ row_grad,
+                                                      double *__restrict__ Wg)
 {
     const int i = row_lo + (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (i >= row_hi) return;
+    const bool grad = row_grad && row_grad[i];
     const double xe[3] = {X[i], Y[i], Z[i]};
     const double n[3] = {normals[3 * (size_t)i], normals[3 * (size_t)i + 1],
                          normals[3 * (size_t)i + 2]};
@@ -523,14 +531,26 @@ __global__ void __launch_bounds__(128) k_asm_singular(const double *__restrict__
             Xe[k][1] = Y[v];
             Xe[k][2] = Z[v];
         }
-        if (kind == 0) warp_singular_G<NEN>(s, Xe, xe, out);
-        else warp_singular_H<NEN, 0>(s, Xe, xe, n, out);
+        double g[4 * NEN];  // FLAG 2: out's values, then the gradient
+        if (kind == 0) {
+            warp_singular_G<NEN>(s, Xe, xe, out);
+            if (grad) warp_singular_H<NEN, 1>(s, Xe, xe, n, g + NEN);
+        } else if (grad) {
+            warp_singular_H<NEN, 2>(s, Xe, xe, n, g);
+#pragma unroll
+            for (int k = 0; k < NEN; k++) out[k] = g[k];
+        } else {
+            warp_singular_H<NEN, 0>(s, Xe, xe, n, out);
+        }
         if (lane == 0) {
 #pragma unroll
             for (int k = 0; k < NEN; k++) {
                 size_t o = (size_t)elems[(size_t)e * NEN + k] * ld + i;
                 K[o] = (T)((double)K[o] + fac * out[k]);
             }
+            if (grad)
+#pragma unroll
+                for (int j = 0; j < 3 * NEN; j++) Wg[(size_t)t * 3 * NEN + j] = g[NEN + j];
         }
         __syncwarp();
     }
@@ -544,7 +564,7 @@ static size_t regular_smem(int nen)
 
 template <int NEN>
 static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStream_t st, Timer *tm,
-                              int prec, AsmWorkspace *ws)
+                              int prec, AsmWorkspace *ws, const int *row_grad, double *Wg)
 {
     AsmWorkspace local;
     AsmWorkspace &w = ws ? *ws : local;
@@ -604,7 +624,7 @@ static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStr
         TimerScope ts(tm, kTAsmSingular, st);
         DSC_LAUNCH(k_asm_singular<NEN, double><<<(warps * 32 + 127) / 128, 128, 0, st>>>(
             m.x.p, m.y.p, m.z.p, m.normals.p, m.row_kind.p, m.row_fac.p, m.elems.p, m.ne_ptr.p,
-            m.ne_elem.p, m.ne_pos.p, lo, hi, K, ld));
+            m.ne_elem.p, m.ne_pos.p, lo, hi, K, ld, Wg ? row_grad : nullptr, Wg));
         DSC_CUDA(cudaGetLastError());
     }
     // a local workspace is released at scope exit: wait for the kernels
@@ -614,10 +634,10 @@ static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStr
 }
 
 int assemble_K_fp64(const DeviceMesh &m, double *K, size_t ld, cudaStream_t st, Timer *tm, int prec,
-                    AsmWorkspace *ws)
+                    AsmWorkspace *ws, const int *row_grad, double *Wg)
 {
-    return m.nen == 6 ? assemble_fp64_impl<6>(m, K, ld, st, tm, prec, ws)
-                      : assemble_fp64_impl<3>(m, K, ld, st, tm, prec, ws);
+    return m.nen == 6 ? assemble_fp64_impl<6>(m, K, ld, st, tm, prec, ws, row_grad, Wg)
+                      : assemble_fp64_impl<3>(m, K, ld, st, tm, prec, ws, row_grad, Wg);
 }
 
 }  // namespace dsc

@@ -405,6 +405,8 @@ int PointSet::build(const HostPlan &plan, int P, const double *pts)
     DSC_TRY(pz.upload(zs, st));
     DSC_TRY(coinc.upload(co, st));
     DSC_TRY(sp_ptr.upload(ptr, st));
+    sp_ptr_h = ptr;
+    sp_h = tup;
     if (tup.empty()) tup.push_back(make_int4(0, 0, 0, 0));
     DSC_TRY(sp.upload(tup, st));
     DSC_CUDA(cudaStreamSynchronize(st));
@@ -521,6 +523,26 @@ int ForcePlan::build(const HostPlan &plan, const unsigned *bctype, cudaStream_t 
     npel = (int)pel_host.size();
     if (P == 0) return kOk;
     DSC_TRY(ps.build(plan, P, pts.data()));
+    {
+        // tuple (e, s, v) of the field = tuple (row v, element e, position
+        // s - 1) of the assembly's singular pass, which takes it at v's
+        // coordinates, the point's
+        std::vector<int> tm(std::max<size_t>(ps.sp_h.size(), 1), 0), rg(plan.N, 0);
+        for (size_t t = 0; t < ps.sp_h.size(); t++) {
+            const int4 u = ps.sp_h[t];
+            int found = -1;
+            for (int a = plan.ne_ptr[u.z]; a < plan.ne_ptr[u.z + 1]; a++)
+                if (plan.ne_elem[a] == u.x && plan.ne_pos[a] == u.y - 1) found = a;
+            if (found < 0) {
+                set_error("field tuple of element %d has no singular pair in the assembly", u.x);
+                return kErrArg;
+            }
+            tm[t] = found;
+            rg[u.z] = 1;
+        }
+        DSC_TRY(tmap.upload(tm, st));
+        DSC_TRY(row_grad.upload(rg, st));
+    }
     DSC_TRY(ids.upload(idv, st));
     DSC_TRY(pel.upload(pel_host.empty() ? std::vector<int>{0} : pel_host, st));
     DSC_TRY(Ept.alloc((size_t)P * 6));

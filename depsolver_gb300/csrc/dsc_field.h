@@ -18,6 +18,8 @@ struct PointSet {
     DevBuf<int4> coinc;
     DevBuf<int> sp_ptr;
     DevBuf<int4> sp;
+    std::vector<int> sp_ptr_h;  // host copies of the singular tuples
+    std::vector<int4> sp_h;
     // workspace of eval_points (charge-weighted points, chunk partials,
     // singular parts), kept between calls
     DevBuf<double> cq, part, sing;
@@ -36,6 +38,10 @@ struct ForcePlan {
     int P = 0, npel = 0;
     PointSet ps;
     DevBuf<int> ids, pel;
+    // the field's singular tuples (ps.sp) as tuples of the assembly's
+    // singular pass (node, element: the plan's ne_ptr numbering), whose
+    // gradient integrals it leaves for the rows flagged in row_grad
+    DevBuf<int> tmap, row_grad;
     std::vector<int> pel_host;
     DevBuf<double> Ept, Enode, Fce, Xce;
     int build(const HostPlan &plan, const unsigned *bctype, cudaStream_t st);

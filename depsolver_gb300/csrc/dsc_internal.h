@@ -212,6 +212,7 @@ void interface_coeffs(unsigned nIf, const unsigned *ifaces, const double *mat, d
 // Device copy of a plan plus the element quadrature data.
 struct DeviceMesh {
     int nen = 6, N = 0, E = 0, G = 0, n_slots = 0, n_fix = 0;
+    int ne_total = 0;              // (node, element containing it) tuples
     DevBuf<double> x, y, z;        // node coordinates (SoA)
     DevBuf<int> elems;             // E x nen
     DevBuf<int> row_kind;
@@ -246,8 +247,12 @@ enum { kAsmF64 = 0, kAsmDf32 = 1, kAsmF32 = 2 };
 
 // prec: one of the above for the regular pairs.  Singular pairs are FP64
 // whatever prec is; K is FP64.  ws (may be null: a local one, freed before
-// returning) holds the scratch.
+// returning) holds the scratch.  With Wg not null, the rows flagged in
+// row_grad (N flags) also leave the gradient integrals of their singular
+// elements there: 3 nen doubles per (node, element) tuple of the plan's
+// ne_ptr numbering.
 int assemble_K_fp64(const DeviceMesh &m, double *K, size_t ld, cudaStream_t st, Timer *tm = nullptr,
-                    int prec = kAsmF64, AsmWorkspace *ws = nullptr);
+                    int prec = kAsmF64, AsmWorkspace *ws = nullptr, const int *row_grad = nullptr,
+                    double *Wg = nullptr);
 
 }  // namespace dsc

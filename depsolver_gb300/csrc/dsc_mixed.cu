@@ -684,39 +684,30 @@ __global__ void __launch_bounds__(128) k_field_batched_mixed(
             for (int d = 0; d < 3; d++) part[(((size_t)group * F + f0 + ff) * P + p) * 3 + d] = acc[ff][d];
 }
 
-// Singular elements of each point, FP64 subdivision once per (point,
-// element), applied to every frequency; lanes = frequencies afterwards.
+// The singular part of the field at each point for every system: the
+// gradient integrals of its singular elements (left by the assembly's
+// singular pass: Wg + tmap[t] * 3 NEN for the point's tuple t) applied to
+// the solution's charges, plus the jump term of the point's own node.  Warp
+// per point, lanes = systems f = lane, lane + 32.
 template <int NEN>
-__global__ void __launch_bounds__(128) k_field_batched_singular(
-    const double *__restrict__ px, const double *__restrict__ py, const double *__restrict__ pz,
-    int P, const int *__restrict__ elems, const double *__restrict__ X, const double *__restrict__ Y,
-    const double *__restrict__ Z, const double *__restrict__ normals, const int *__restrict__ sp_ptr,
-    const int4 *__restrict__ sp, const double *__restrict__ Xs, size_t ld, int F,
-    double *__restrict__ sing)
+__global__ void __launch_bounds__(128) k_field_singular_apply(
+    int P, const int *__restrict__ elems, const double *__restrict__ normals, const int *__restrict__ sp_ptr,
+    const int4 *__restrict__ sp, const int *__restrict__ tmap, const double *__restrict__ Wg,
+    const double *__restrict__ Xs, size_t ld, int F, double *__restrict__ sing)
 {
     const int p = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (p >= P) return;
-    const double xe[3] = {px[p], py[p], pz[p]};
     const double A = 0.5 / kEps0 / kPi2, B = 0.5 / kEps0;
-    double acc[2][3] = {{0, 0, 0}, {0, 0, 0}};  // lanes own f = lane, lane + 32
+    double acc[2][3] = {{0, 0, 0}, {0, 0, 0}};
     for (int t = sp_ptr[p]; t < sp_ptr[p + 1]; t++) {
         const int4 tu = sp[t];
-        const int e = tu.x, s = tu.y;
-        double Xe[NEN][3];
         int nodes[NEN];
 #pragma unroll
-        for (int k = 0; k < NEN; k++) {
-            int v = elems[(size_t)e * NEN + k];
-            nodes[k] = v;
-            Xe[k][0] = X[v];
-            Xe[k][1] = Y[v];
-            Xe[k][2] = Z[v];
-        }
+        for (int k = 0; k < NEN; k++) nodes[k] = elems[(size_t)tu.x * NEN + k];
         const double n[3] = {normals[3 * (size_t)tu.z], normals[3 * (size_t)tu.z + 1],
                              normals[3 * (size_t)tu.z + 2]};
-        double sub[3 * NEN];
-        warp_singular_H<NEN, 1>(s, Xe, xe, n, sub);
+        const double *w = Wg + (size_t)tmap[t] * 3 * NEN;
         for (int r = 0; r < 2; r++) {
             const int f = lane + 32 * r;
             if (f >= F) continue;
@@ -725,7 +716,7 @@ __global__ void __launch_bounds__(128) k_field_batched_singular(
             for (int k = 0; k < NEN; k++) {
                 const double sr = xr[nodes[k]];
 #pragma unroll
-                for (int c = 0; c < 3; c++) acc[r][c] += A * sub[3 * k + c] * sr;
+                for (int c = 0; c < 3; c++) acc[r][c] += A * w[3 * k + c] * sr;
             }
             const double s0 = xr[nodes[0]];
 #pragma unroll
@@ -1236,13 +1227,13 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
                                                                         w.qdf.p, F, w.part.p));
             const int sb = (P * 32 + 127) / 128;
             if (s.nen == 6)
-                DSC_LAUNCH(k_field_batched_singular<6><<<sb, 128, 0, st>>>(
-                    fp.ps.px.p, fp.ps.py.p, fp.ps.pz.p, P, s.dev.elems.p, s.dev.x.p, s.dev.y.p, s.dev.z.p,
-                    s.dev.normals.p, fp.ps.sp_ptr.p, fp.ps.sp.p, w.Xs.p, ld, F, w.sing.p));
+                DSC_LAUNCH(k_field_singular_apply<6><<<sb, 128, 0, st>>>(P, s.dev.elems.p, s.dev.normals.p,
+                                                                         fp.ps.sp_ptr.p, fp.ps.sp.p, fp.tmap.p,
+                                                                         s.Wsing.p, w.Xs.p, ld, F, w.sing.p));
             else
-                DSC_LAUNCH(k_field_batched_singular<3><<<sb, 128, 0, st>>>(
-                    fp.ps.px.p, fp.ps.py.p, fp.ps.pz.p, P, s.dev.elems.p, s.dev.x.p, s.dev.y.p, s.dev.z.p,
-                    s.dev.normals.p, fp.ps.sp_ptr.p, fp.ps.sp.p, w.Xs.p, ld, F, w.sing.p));
+                DSC_LAUNCH(k_field_singular_apply<3><<<sb, 128, 0, st>>>(P, s.dev.elems.p, s.dev.normals.p,
+                                                                         fp.ps.sp_ptr.p, fp.ps.sp.p, fp.tmap.p,
+                                                                         s.Wsing.p, w.Xs.p, ld, F, w.sing.p));
             DSC_CUDA(cudaMemsetAsync(w.Enode.p, 0, (size_t)F * N * 3 * sizeof(double), st));
             const size_t nt = (size_t)F * P * 3;
             DSC_LAUNCH(k_field_batched_reduce<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(

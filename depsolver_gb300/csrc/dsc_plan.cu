@@ -424,6 +424,7 @@ int DeviceMesh::upload(const HostPlan &p, cudaStream_t st)
     DSC_TRY(fix_slot.upload(p.fix_slot.empty() ? std::vector<int>{0} : p.fix_slot, st));
     DSC_TRY(fix_col.upload(p.fix_col.empty() ? std::vector<int>{0} : p.fix_col, st));
     DSC_TRY(ne_ptr.upload(p.ne_ptr, st));
+    ne_total = (int)p.ne_elem.size();
     DSC_TRY(ne_elem.upload(p.ne_elem, st));
     DSC_TRY(ne_pos.upload(p.ne_pos, st));
     DSC_TRY(qp.alloc((size_t)E * kTriPts * 4));

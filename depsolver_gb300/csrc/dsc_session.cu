@@ -191,7 +191,12 @@ int Session::assemble64(bool need_fp64)
     k16_ready = false;  // the fp16 copies and the preconditioner follow K
     if (pre) pre->ready = false;
     DSC_TRY(K64.alloc(ld * N));
-    DSC_TRY(assemble_K_fp64(dev, K64.p, ld, st, &timer, want, &asm_ws));
+    double *Wg = nullptr;
+    if (force.P > 0) {
+        DSC_TRY(Wsing.alloc((size_t)std::max(dev.ne_total, 1) * 3 * nen));
+        Wg = Wsing.p;
+    }
+    DSC_TRY(assemble_K_fp64(dev, K64.p, ld, st, &timer, want, &asm_ws, force.row_grad.p, Wg));
     k64_prec = want;
     DSC_TRY(Kdiag.alloc(N));
     DSC_LAUNCH(k_diag<<<(N + 255) / 256, 256, 0, st>>>(K64.p, ld, N, Kdiag.p));

@@ -48,6 +48,9 @@ struct Session {
     int k64_prec = kAsmF64;   // arithmetic K64's regular pairs were integrated in
     int mixed_asm = kAsmF32;  // the mixed mode's choice (kAsmF32 or kAsmDf32)
     AsmWorkspace asm_ws;    // kept between assemblies
+    // the gradient integrals of the force points' singular elements, left
+    // by each assembly (3 nen per singular tuple; see assemble_K_fp64)
+    DevBuf<double> Wsing;
     DevBuf<double> K64, Kdiag;
     std::vector<double> Kdiag_host;
     // plain FP64 path workspace

@@ -87,17 +87,20 @@ __device__ __forceinline__ int singular_perm(int s, int p)
 }
 
 // Warp-cooperative strongly singular H (FLAG = 0: normal derivative with
-// the node normal n, out[k]; FLAG = 1: gradient, out[3k + c]) by 8-level
-// subdivision x 3 sub-triangles x 7 points towards local (0,0) of the
-// rotated element (src/kernelIntegrals.c:472-593 tria3, :611-805 tria6).
-// For tria6 mid-side nodes each point is split into two mapped points with
-// weight 1/2; the FLAG = 1 z-component of the second one uses its
-// y-distance, as in the reference (:762).
+// the node normal n, out[k]; FLAG = 1: gradient, out[3k + c]; FLAG = 2:
+// both from the same points, out[k] and out[NEN + 3k + c], each summed as
+// FLAG 0 and FLAG 1 sum it) by 8-level subdivision x 3 sub-triangles x 7
+// points towards local (0,0) of the rotated element
+// (src/kernelIntegrals.c:472-593 tria3, :611-805 tria6).  For tria6
+// mid-side nodes each point is split into two mapped points with weight
+// 1/2; the gradient's z-component of the second one uses its y-distance,
+// as in the reference (:762).
 template <int NEN, int FLAG>
 __device__ void warp_singular_H(int s, const double (*X0)[3], const double *xe, const double *n,
                                 double *out)
 {
-    constexpr int NOUT = FLAG ? 3 * NEN : NEN;
+    constexpr int NOUT = FLAG == 2 ? 4 * NEN : FLAG ? 3 * NEN : NEN;
+    constexpr int G0 = FLAG == 2 ? NEN : 0;  // first gradient accumulator
     const int lane = threadIdx.x & 31;
     double X[NEN][3];
 #pragma unroll
@@ -136,16 +139,17 @@ __device__ void warp_singular_H(int s, const double (*X0)[3], const double *xe, 
                 double dr = sqrt(dx * dx + dy * dy + dz * dz);
                 A = J * JL * W / (dr * dr * dr);
             }
-            if (FLAG == 0) {
-                A *= dx * n[0] + dy * n[1] + dz * n[2];
+            if (FLAG != 1) {
+                const double An = A * (dx * n[0] + dy * n[1] + dz * n[2]);
 #pragma unroll
-                for (int k = 0; k < NEN; k++) acc[k] -= A * N1[k];
-            } else {
+                for (int k = 0; k < NEN; k++) acc[k] -= An * N1[k];
+            }
+            if (FLAG != 0) {
 #pragma unroll
                 for (int k = 0; k < NEN; k++) {
-                    acc[3 * k + 0] += A * dx * N1[k];
-                    acc[3 * k + 1] += A * dy * N1[k];
-                    acc[3 * k + 2] += A * dz * N1[k];
+                    acc[G0 + 3 * k + 0] += A * dx * N1[k];
+                    acc[G0 + 3 * k + 1] += A * dy * N1[k];
+                    acc[G0 + 3 * k + 2] += A * dz * N1[k];
                 }
             }
         } else {
@@ -166,17 +170,18 @@ __device__ void warp_singular_H(int s, const double (*X0)[3], const double *xe, 
             double dr2 = sqrt(dx2 * dx2 + dy2 * dy2 + dz2 * dz2);
             double A1 = 0.5 * J * JL1 * W / (dr1 * dr1 * dr1);
             double A2 = 0.5 * J * JL2 * W / (dr2 * dr2 * dr2);
-            if (FLAG == 0) {
-                A1 *= dx1 * n[0] + dy1 * n[1] + dz1 * n[2];
-                A2 *= dx2 * n[0] + dy2 * n[1] + dz2 * n[2];
+            if (FLAG != 1) {
+                const double An1 = A1 * (dx1 * n[0] + dy1 * n[1] + dz1 * n[2]);
+                const double An2 = A2 * (dx2 * n[0] + dy2 * n[1] + dz2 * n[2]);
 #pragma unroll
-                for (int k = 0; k < NEN; k++) acc[k] -= A1 * N1[k] + A2 * N2[k];
-            } else {
+                for (int k = 0; k < NEN; k++) acc[k] -= An1 * N1[k] + An2 * N2[k];
+            }
+            if (FLAG != 0) {
 #pragma unroll
                 for (int k = 0; k < NEN; k++) {
-                    acc[3 * k + 0] += A1 * dx1 * N1[k] + A2 * dx2 * N2[k];
-                    acc[3 * k + 1] += A1 * dy1 * N1[k] + A2 * dy2 * N2[k];
-                    acc[3 * k + 2] += A1 * dz1 * N1[k] + A2 * dy2 * N2[k];
+                    acc[G0 + 3 * k + 0] += A1 * dx1 * N1[k] + A2 * dx2 * N2[k];
+                    acc[G0 + 3 * k + 1] += A1 * dy1 * N1[k] + A2 * dy2 * N2[k];
+                    acc[G0 + 3 * k + 2] += A1 * dz1 * N1[k] + A2 * dy2 * N2[k];
                 }
             }
         }
@@ -188,11 +193,11 @@ __device__ void warp_singular_H(int s, const double (*X0)[3], const double *xe, 
 #pragma unroll
     for (int p = 0; p < NEN; p++) {
         int o = singular_perm<NEN>(s, p);
-        if (FLAG == 0) out[o] = red[p];
-        else {
-            out[3 * o + 0] = red[3 * p + 0];
-            out[3 * o + 1] = red[3 * p + 1];
-            out[3 * o + 2] = red[3 * p + 2];
+        if (FLAG != 1) out[o] = red[p];
+        if (FLAG != 0) {
+            out[G0 + 3 * o + 0] = red[G0 + 3 * p + 0];
+            out[G0 + 3 * o + 1] = red[G0 + 3 * p + 1];
+            out[G0 + 3 * o + 2] = red[G0 + 3 * p + 2];
         }
     }
 }
