@@ -395,11 +395,12 @@ __device__ __forceinline__ void pair_regular_f32(const float4 *__restrict__ q7, 
 }
 
 // As k_asm_regular_df32 (same tiles, footprints and partial slots), with the
-// pair integrals, the row factor and the footprint sums in FP32.
+// pair integrals, the row factor and the footprint sums in FP32; K's
+// entries widened to FP64, the partial slots kept in FP32 (k_asm_fixup_f32).
 template <int NEN>
 __global__ void __launch_bounds__(128) k_asm_regular_f32(AsmArgs a, const float2 *__restrict__ cen,
                                                          const float4 *__restrict__ qloc, double *__restrict__ K,
-                                                         double *__restrict__ P)
+                                                         float *__restrict__ P)
 {
     constexpr int R = kRowTile, EG = kGroup;
     __shared__ float4 s_q[EG * kTriPts];
@@ -467,8 +468,22 @@ __global__ void __launch_bounds__(128) k_asm_regular_f32(AsmArgs a, const float2
         const int dest = a.fp_dest[j];
         if (valid) {
             if (dest >= 0) K[(size_t)dest * a.ld + i] = f32_widen(sum);
-            else P[(size_t)(-dest - 1) * a.ldp + (i - a.row_lo)] = f32_widen(sum);
+            else P[(size_t)(-dest - 1) * a.ldp + (i - a.row_lo)] = sum;
         }
+    }
+}
+
+// k_asm_fixup for FP32 partial slots: the sum in FP32, K in FP64.
+__global__ void k_asm_fixup_f32(const int *__restrict__ fix_ptr, const int *__restrict__ fix_slot,
+                                const int *__restrict__ fix_col, int n_fix, const float *__restrict__ P,
+                                size_t ldp, double *__restrict__ K, size_t ld, int row_lo, int nrows)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrows) return;
+    for (int b = blockIdx.y; b < n_fix; b += gridDim.y) {
+        float sum = 0.f;
+        for (int t = fix_ptr[b]; t < fix_ptr[b + 1]; t++) sum += P[(size_t)fix_slot[t] * ldp + r];
+        K[(size_t)fix_col[b] * ld + row_lo + r] = f32_widen(sum);
     }
 }
 
@@ -591,7 +606,8 @@ static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStr
         if (fit < (size_t)rc) rc = (int)std::max<size_t>(kRowTile, fit / kRowTile * kRowTile);
     }
     DevBuf<double> &P = w.P;
-    DSC_TRY(P.alloc((size_t)std::max(m.n_slots, 1) * rc));
+    if (f32) DSC_TRY(w.P32.alloc((size_t)std::max(m.n_slots, 1) * rc));
+    else DSC_TRY(P.alloc((size_t)std::max(m.n_slots, 1) * rc));
     const size_t smem = regular_smem(NEN);
     DSC_CUDA(cudaFuncSetAttribute(k_asm_regular_f64<NEN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)smem));
@@ -607,7 +623,7 @@ static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStr
         dim3 grid((hi - lo + kRowTile - 1) / kRowTile, m.G);
         {
             TimerScope ts(tm, kTAsmRegular, st);
-            if (f32) DSC_LAUNCH(k_asm_regular_f32<NEN><<<grid, 128, 0, st>>>(a, w.cen.p, w.qloc.p, K, P.p));
+            if (f32) DSC_LAUNCH(k_asm_regular_f32<NEN><<<grid, 128, 0, st>>>(a, w.cen.p, w.qloc.p, K, w.P32.p));
             else if (df32) DSC_LAUNCH(k_asm_regular_df32<NEN><<<grid, 128, smem, st>>>(a, qpd.p, K, P.p));
             else DSC_LAUNCH(k_asm_regular_f64<NEN><<<grid, 128, smem, st>>>(a, K, P.p));
             if (tm) tm->add_work(kTAsmRegular, (double)(hi - lo) * m.E);  // (row, element) pairs
@@ -616,8 +632,12 @@ static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStr
         if (m.n_fix > 0) {
             dim3 fg((hi - lo + 255) / 256, std::min(m.n_fix, 65535));
             TimerScope ts(tm, kTAsmFixup, st);
-            DSC_LAUNCH(k_asm_fixup<double><<<fg, 256, 0, st>>>(m.fix_ptr.p, m.fix_slot.p, m.fix_col.p, m.n_fix,
-                                                    P.p, (size_t)rc, K, ld, lo, hi - lo));
+            if (f32)
+                DSC_LAUNCH(k_asm_fixup_f32<<<fg, 256, 0, st>>>(m.fix_ptr.p, m.fix_slot.p, m.fix_col.p, m.n_fix,
+                                                               w.P32.p, (size_t)rc, K, ld, lo, hi - lo));
+            else
+                DSC_LAUNCH(k_asm_fixup<double><<<fg, 256, 0, st>>>(m.fix_ptr.p, m.fix_slot.p, m.fix_col.p,
+                                                                   m.n_fix, P.p, (size_t)rc, K, ld, lo, hi - lo));
             DSC_CUDA(cudaGetLastError());
         }
         int warps = hi - lo;

@@ -510,12 +510,45 @@ int force_mst(const DeviceMesh &m, const HostPlan &plan, const unsigned *bctype,
 int ForcePlan::build(const HostPlan &plan, const unsigned *bctype, cudaStream_t st)
 {
     std::vector<int> idv;
-    std::vector<double> pts;
     for (int i = 0; i < plan.N; i++)
-        if (bctype[i] == 6) {
-            idv.push_back(i);
-            for (int d = 0; d < 3; d++) pts.push_back(plan.nodes[3 * (size_t)i + d]);
+        if (bctype[i] == 6) idv.push_back(i);
+    {
+        // points in Morton order of their coordinates (10 bits per axis
+        // over the points' bounding box): a warp of consecutive points is
+        // one patch of the surface, whose near elements it shares
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+        for (int i : idv)
+            for (int d = 0; d < 3; d++) {
+                lo[d] = std::min(lo[d], plan.nodes[3 * (size_t)i + d]);
+                hi[d] = std::max(hi[d], plan.nodes[3 * (size_t)i + d]);
+            }
+        auto spread = [](unsigned v) {  // 10 bits to every third of 30
+            v &= 0x3FFu;
+            v = (v | (v << 16)) & 0x030000FFu;
+            v = (v | (v << 8)) & 0x0300F00Fu;
+            v = (v | (v << 4)) & 0x030C30C3u;
+            v = (v | (v << 2)) & 0x09249249u;
+            return v;
+        };
+        std::vector<std::pair<unsigned, int>> key;
+        key.reserve(idv.size());
+        for (int i : idv) {
+            unsigned c = 0;
+            for (int d = 0; d < 3; d++) {
+                const double w = hi[d] > lo[d] ? (plan.nodes[3 * (size_t)i + d] - lo[d]) / (hi[d] - lo[d]) : 0.0;
+                c |= spread((unsigned)std::min(1023.0, w * 1024.0)) << d;
+            }
+            key.push_back({c, i});
         }
+        std::stable_sort(key.begin(), key.end(),
+                         [](const std::pair<unsigned, int> &a, const std::pair<unsigned, int> &b) {
+                             return a.first < b.first;
+                         });
+        for (size_t t = 0; t < key.size(); t++) idv[t] = key[t].second;
+    }
+    std::vector<double> pts;
+    for (int i : idv)
+        for (int d = 0; d < 3; d++) pts.push_back(plan.nodes[3 * (size_t)i + d]);
     pel_host.clear();
     for (int e = 0; e < plan.E; e++)
         if (bctype[plan.elems[(size_t)e * plan.nen]] == 6) pel_host.push_back(e);

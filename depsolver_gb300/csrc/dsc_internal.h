@@ -235,6 +235,7 @@ struct DeviceMesh {
 // repeatedly keeps one to avoid allocating every time.
 struct AsmWorkspace {
     DevBuf<double> P;
+    DevBuf<float> P32;  // the FP32 assembly's partial slots
     DevBuf<float2> qpd;
     DevBuf<float2> cen;
     DevBuf<float4> qloc;

@@ -584,6 +584,7 @@ __global__ void __launch_bounds__(128) k_field_batched_mixed(
 {
     __shared__ float s_cent[kBChunk * 8];
     __shared__ float s_off[kBChunk * kTriPts * 3];
+    __shared__ float2 s_qdf[kBChunk * kTriPts * 3];  // the points in double-FP32 (near pairs)
     // charge of (e, q) for the group's systems; rows padded by 4 floats so
     // that the staging stores of consecutive (e, q) spread over the banks
     __shared__ __align__(16) float s_c[kBChunk * kTriPts][kBF + 4];
@@ -606,8 +607,10 @@ __global__ void __launch_bounds__(128) k_field_batched_mixed(
         const int ne = min(kBChunk, E - e0);
         __syncthreads();  // the previous chunk is no longer read
         for (int t = threadIdx.x; t < ne * 8; t += blockDim.x) s_cent[t] = ecent[(size_t)e0 * 8 + t];
-        for (int t = threadIdx.x; t < ne * kTriPts * 3; t += blockDim.x)
+        for (int t = threadIdx.x; t < ne * kTriPts * 3; t += blockDim.x) {
             s_off[t] = qoff[(size_t)e0 * kTriPts * 3 + t];
+            s_qdf[t] = qdf[(size_t)e0 * kTriPts * 3 + t];
+        }
         for (int t = threadIdx.x; t < kBF * ne * kTriPts; t += blockDim.x) {
             const int ff = t / (ne * kTriPts), r = t % (ne * kTriPts);
             s_c[r][ff] = ff < nf ? cf32[(size_t)(f0 + ff) * E * kTriPts + (size_t)e0 * kTriPts + r] : 0.0f;
@@ -638,7 +641,7 @@ __global__ void __launch_bounds__(128) k_field_batched_mixed(
                 float gx, gy, gz;
                 if (near) {
                     // the difference of close points in double-FP32
-                    const float2 *Q = qdf + ((size_t)(e0 + e) * kTriPts + q) * 3;
+                    const float2 *Q = s_qdf + (e * kTriPts + q) * 3;
                     const float2 dx = df_sub(pdf[0], Q[0]), dy = df_sub(pdf[1], Q[1]), dz = df_sub(pdf[2], Q[2]);
                     const float2 r2 = df_add(df_add(df_sqr(dx), df_sqr(dy)), df_sqr(dz));
                     const float2 inv = df_rsqrt(r2);

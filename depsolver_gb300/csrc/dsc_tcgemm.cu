@@ -857,55 +857,76 @@ __device__ __forceinline__ __half digit_f16(int q)
     return __hsub(__ushort_as_half((unsigned short)(0x6600 + q)), __ushort_as_half((unsigned short)0x6600));
 }
 
-// The kKDigits base-2^kKDigitBits digits of a K entry (row exponent Erow):
-// B = 47, |q| <= 32.
-__device__ __forceinline__ void k_digits(double a, int Erow, __half *q)
+// The kKDigits = 8 base-64 digits of a K entry (row exponent Erow): B =
+// 47, |q| <= 32.  Adding 32 to every 6-bit field of the signed V (the
+// constant 0x820820820820) makes each field minus 32 a balanced digit, so
+// the digits are plain bit fields of w = V + that constant (w >= 0; the top
+// field, bits 42 and up, reaches 64 for V = 2^47).  The fp16 of q is 0x65E0
+// + (q + 32) minus 1536, exact.
+static_assert(kKDigits == 8 && kKDigitBits == 6, "k_digit_fields extracts 8 fields of 6 bits");
+__device__ __forceinline__ __half2 digit_pair_f16(unsigned fa, unsigned fb)
 {
-    unsigned long long u = digit_magnitude(a, Erow, 53 - (kKDigits * kKDigitBits - 1));
-    const bool neg = __double_as_longlong(a) < 0;
-    const unsigned half = 1u << (kKDigitBits - 1), mask = (1u << kKDigitBits) - 1;
-#pragma unroll
-    for (int d = kKDigits - 1; d > 0; d--) {
-        const int t = (int)((unsigned)(u + half) & mask) - (int)half;
-        u = (u + half) >> kKDigitBits;
-        q[d] = digit_f16(neg ? -t : t);
-    }
-    q[0] = digit_f16(neg ? -(int)u : (int)u);
+    const __half2 h = __halves2half2(__ushort_as_half((unsigned short)(0x65E0u + fa)),
+                                     __ushort_as_half((unsigned short)(0x65E0u + fb)));
+    return __hsub2(h, __halves2half2(__ushort_as_half((unsigned short)0x6600u),
+                                     __ushort_as_half((unsigned short)0x6600u)));
+}
+
+// f[d] = digit d + 32, most significant first
+__device__ __forceinline__ void k_digit_fields(double a, int Erow, unsigned *f)
+{
+    const unsigned long long u = digit_magnitude(a, Erow, 53 - (kKDigits * kKDigitBits - 1));
+    const long long V = __double_as_longlong(a) < 0 ? -(long long)u : (long long)u;
+    const unsigned long long w = (unsigned long long)(V + 0x820820820820ll);
+    const unsigned lo = (unsigned)w, hi = (unsigned)(w >> 32);
+    f[7] = lo & 63u;
+    f[6] = (lo >> 6) & 63u;
+    f[5] = (lo >> 12) & 63u;
+    f[4] = (lo >> 18) & 63u;
+    f[3] = (lo >> 24) & 63u;
+    f[2] = __funnelshift_r(lo, hi, 30) & 63u;
+    f[1] = (hi >> 4) & 63u;
+    f[0] = hi >> 10;
 }
 
 // Column-major FP64 K to row-major fp16 pairs (entry (i, c) at i * ldt + c)
 // of 2^s_i fl32(K) (Th, Tl; hi = rn_fp16(x), lo = rn_fp16(x - hi)) and,
 // with Dg not null, to the kKDigits digit matrices of K (digit d at Dg + d *
 // dstride, same layout).  Each row's largest entry scales below 2^15, so
-// the pair stays below fp16's largest finite value (65504).  A 32 x 32
-// shared tile per block.
+// the pair stays below fp16's largest finite value (65504).  Block: 32 rows
+// x 64 columns through a shared tile; each thread writes two adjacent
+// columns of a row (4-byte stores; ldt is even, and the column after N - 1
+// is the row's padding, written with zeros).
 __global__ void k_split_transpose_f16(const double *__restrict__ K, size_t ld, int N,
                                       const int *__restrict__ rowE, __half *__restrict__ Th,
                                       __half *__restrict__ Tl, __half *__restrict__ Dg, size_t dstride,
                                       size_t ldt)
 {
-    __shared__ double t[32][33];
-    const int i0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
-    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
-        int c = c0 + k, i = i0 + threadIdx.x;
+    __shared__ double t[64][33];
+    const int i0 = blockIdx.x * 32, c0 = blockIdx.y * 64;
+    for (int k = threadIdx.y; k < 64; k += blockDim.y) {
+        const int c = c0 + k, i = i0 + threadIdx.x;
         t[k][threadIdx.x] = (c < N && i < N) ? K[(size_t)c * ld + i] : 0.0;
     }
     __syncthreads();
+    const int c = c0 + 2 * threadIdx.x;
     for (int k = threadIdx.y; k < 32; k += blockDim.y) {
-        int i = i0 + k, c = c0 + threadIdx.x;
-        if (i < N && c < N) {
-            const double a = t[threadIdx.x][k];
-            const int Er = rowE[i];
-            const float x = (float)a * pow2f(scale_shift(Er, 1023));
-            const __half h = __float2half_rn(x);
-            Th[(size_t)i * ldt + c] = h;
-            Tl[(size_t)i * ldt + c] = __float2half_rn(x - __half2float(h));
-            if (Dg) {
-                __half q[kKDigits];
-                k_digits(a, Er, q);
+        const int i = i0 + k;
+        if (i >= N || c >= N) continue;
+        const double a0 = t[2 * threadIdx.x][k], a1 = t[2 * threadIdx.x + 1][k];
+        const int Er = rowE[i];
+        const float sc = pow2f(scale_shift(Er, 1023));
+        const float x0 = (float)a0 * sc, x1 = (float)a1 * sc;
+        const __half2 h = __floats2half2_rn(x0, x1);
+        const size_t o = (size_t)i * ldt + c;
+        *(__half2 *)(Th + o) = h;
+        *(__half2 *)(Tl + o) = __floats2half2_rn(x0 - __low2float(h), x1 - __high2float(h));
+        if (Dg) {
+            unsigned f0[kKDigits], f1[kKDigits];
+            k_digit_fields(a0, Er, f0);
+            k_digit_fields(a1, Er, f1);
 #pragma unroll
-                for (int d = 0; d < kKDigits; d++) Dg[d * dstride + (size_t)i * ldt + c] = q[d];
-            }
+            for (int d = 0; d < kKDigits; d++) *(__half2 *)(Dg + d * dstride + o) = digit_pair_f16(f0[d], f1[d]);
         }
     }
 }
@@ -957,7 +978,11 @@ int k16_row_scales(const double *K, size_t ld, int N, int *rowE, float *rsK, cud
 int split_transpose_K16(const double *K, size_t ld, int N, const int *rowE, __half *Th, __half *Tl,
                         __half *Dg, size_t dstride, size_t ldt, cudaStream_t st)
 {
-    dim3 g((N + 31) / 32, (N + 31) / 32), b(32, 8);
+    if (ldt % 2 || ldt < (size_t)N + (N & 1) || (Dg && dstride % 2)) {
+        set_error("split_transpose_K16: strides must be even and the row stride cover N rounded up to even");
+        return kErrArg;
+    }
+    dim3 g((N + 31) / 32, (N + 63) / 64), b(32, 8);
     DSC_LAUNCH(k_split_transpose_f16<<<g, b, 0, st>>>(K, ld, N, rowE, Th, Tl, Dg, dstride, ldt));
     DSC_CUDA(cudaGetLastError());
     return kOk;
