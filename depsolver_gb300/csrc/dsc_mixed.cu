@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "../../include/depsolver_cuda.h"
+#include "dsc_async.cuh"
 #include "dsc_blas.cuh"
 #include "dsc_common.cuh"
 #include "dsc_df32.cuh"
@@ -490,28 +491,36 @@ __global__ void k_update_solution(double *__restrict__ D, const float2 *__restri
 }
 
 // ------------------------------------------------------- batched field
-// Charge weights of Re(sigma_f) at every quadrature point:
-// cf[f][e*7+q] = w_q J_q sum_k N_k(q) Re sigma_f(node k).
-template <int NEN>
-__global__ void k_charge_batched(const int *__restrict__ elems, int E, const double *__restrict__ qp,
-                                 const double *__restrict__ X, size_t ld, int F,
-                                 double *__restrict__ cf)
-{
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const int f = blockIdx.y;
-    if (t >= E * kTriPts) return;
-    const int e = t / kTriPts, q = t % kTriPts;
-    double N6[NEN];
-    shape<NEN>(c_tri7[q][0], c_tri7[q][1], N6);
-    const double *xr = X + (size_t)(2 * f) * ld;
-    double s = 0.0;
-#pragma unroll
-    for (int k = 0; k < NEN; k++) s += N6[k] * xr[elems[(size_t)e * NEN + k]];
-    cf[(size_t)f * E * kTriPts + t] = qp[(size_t)t * 4 + 3] * s;
-}
-
 constexpr int kBF = 32;   // frequencies per thread in the batched field
 constexpr int kBChunk = 32;
+
+// Charge weights of Re(sigma_f) at every quadrature point, in FP32 for the
+// field pass, grouped by kBF systems with the systems innermost:
+// cT[(g * E7p + e*7+q) * kBF + ff] = w_q J_q sum_k N_k(q) Re sigma_f(node k)
+// (FP64 sum, rounded), f = g kBF + ff; zero for f >= F and for the rows
+// e*7+q >= 7E up to E7p (E rounded up to whole chunks of kBChunk).  Block
+// (kBF, 8): a warp writes one row's kBF systems.
+template <int NEN>
+__global__ void k_charge_batched(const int *__restrict__ elems, int E, const double *__restrict__ qp,
+                                 const double *__restrict__ X, size_t ld, int F, int E7p, float *__restrict__ cT)
+{
+    const int ff = threadIdx.x;
+    const int t = blockIdx.x * blockDim.y + threadIdx.y;
+    const int g = blockIdx.y, f = g * kBF + ff;
+    if (t >= E7p) return;
+    float v = 0.0f;
+    if (t < E * kTriPts && f < F) {
+        const int e = t / kTriPts, q = t % kTriPts;
+        double N6[NEN];
+        shape<NEN>(c_tri7[q][0], c_tri7[q][1], N6);
+        const double *xr = X + (size_t)(2 * f) * ld;
+        double sum = 0.0;
+#pragma unroll
+        for (int k = 0; k < NEN; k++) sum += N6[k] * xr[elems[(size_t)e * NEN + k]];
+        v = (float)(qp[(size_t)t * 4 + 3] * sum);
+    }
+    cT[((size_t)g * E7p + t) * kBF + ff] = v;
+}
 
 // ---- FP32 far field with FP64 near field
 // Per element: centroid as an FP32 (hi, lo) pair, squared near radius, and
@@ -563,32 +572,32 @@ __global__ void k_points_split(const double *__restrict__ px, const double *__re
     }
 }
 
-__global__ void k_to_f32(const double *__restrict__ x, float *__restrict__ y, size_t n)
-{
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n;
-         t += (size_t)gridDim.x * blockDim.x)
-        y[t] = (float)x[t];
-}
-
 // part[group][f][p][3] (FP32): regular contributions of one group of
 // kBLoop x kBChunk elements to the field at point p for system f.  Far
 // pairs in FP32 (rsqrt with a Newton step, coordinates as centroid-relative
-// offsets); near pairs take the point-to-quadrature-point geometry in FP64
-// (the difference of close points) and the products in FP32.
+// offsets); near pairs take the point-to-quadrature-point geometry in
+// double-FP32 and the products in FP32.  Each chunk's element data (charges
+// of the block's kBF systems, centroids, offsets, points, nodes: contiguous
+// slices of arrays padded to whole chunks) arrives in shared memory by bulk
+// copies on one mbarrier; a wait that gives up sets *err (code 8) and ends
+// the block.
 constexpr int kBLoop = 8;   // element chunks per block
 template <int NEN>
 __global__ void __launch_bounds__(128) k_field_batched_mixed(
-    const float *__restrict__ phl, const int4 *__restrict__ coinc, int P, const int *__restrict__ elems,
-    int E, const float *__restrict__ ecent, const float *__restrict__ qoff, const float *__restrict__ cf32,
-    const float2 *__restrict__ qdf, int F, float *__restrict__ part)
+    const float *__restrict__ phl, const int4 *__restrict__ coinc, int P, const int *__restrict__ en_pad,
+    int E, int E7p, const float *__restrict__ ecent, const float *__restrict__ qoff,
+    const float *__restrict__ cT, const float2 *__restrict__ qdf, int F, float *__restrict__ part, int *err)
 {
-    __shared__ float s_cent[kBChunk * 8];
-    __shared__ float s_off[kBChunk * kTriPts * 3];
-    __shared__ float2 s_qdf[kBChunk * kTriPts * 3];  // the points in double-FP32 (near pairs)
-    // charge of (e, q) for the group's systems; rows padded by 4 floats so
-    // that the staging stores of consecutive (e, q) spread over the banks
-    __shared__ __align__(16) float s_c[kBChunk * kTriPts][kBF + 4];
-    __shared__ int s_en[kBChunk * NEN];
+    __shared__ __align__(16) float s_c[kBChunk * kTriPts][kBF];
+    __shared__ __align__(16) float s_cent[kBChunk * 8];
+    __shared__ __align__(16) float s_off[kBChunk * kTriPts * 3];
+    __shared__ __align__(16) float2 s_qdf[kBChunk * kTriPts * 3];  // the points in double-FP32 (near pairs)
+    __shared__ __align__(16) int s_en[kBChunk * NEN];
+    __shared__ __align__(8) uint64_t bar;
+    constexpr uint32_t kBytes = sizeof(s_c) + sizeof(s_cent) + sizeof(s_off) + sizeof(s_qdf) + sizeof(s_en);
+    static_assert(sizeof(s_c) % 16 == 0 && sizeof(s_cent) % 16 == 0 && sizeof(s_off) % 16 == 0 &&
+                      sizeof(s_qdf) % 16 == 0 && sizeof(s_en) % 16 == 0,
+                  "bulk copies move multiples of 16 bytes");
     const int group = blockIdx.y, fg = blockIdx.z;
     const int f0 = fg * kBF, nf = min(kBF, F - f0);
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -598,25 +607,33 @@ __global__ void __launch_bounds__(128) k_field_batched_mixed(
     const float pl[3] = {phl[(size_t)pp * 6 + 3], phl[(size_t)pp * 6 + 4], phl[(size_t)pp * 6 + 5]};
     const float2 pdf[3] = {make_float2(ph[0], pl[0]), make_float2(ph[1], pl[1]), make_float2(ph[2], pl[2])};
     const int4 c = coinc[pp];
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
     float acc[kBF][3];
 #pragma unroll
     for (int ff = 0; ff < kBF; ff++) acc[ff][0] = acc[ff][1] = acc[ff][2] = 0.0f;
+    uint32_t phase = 0;
     for (int cl = 0; cl < kBLoop; cl++) {
         const int e0 = (group * kBLoop + cl) * kBChunk;
         if (e0 >= E) break;  // uniform over the block
         const int ne = min(kBChunk, E - e0);
-        __syncthreads();  // the previous chunk is no longer read
-        for (int t = threadIdx.x; t < ne * 8; t += blockDim.x) s_cent[t] = ecent[(size_t)e0 * 8 + t];
-        for (int t = threadIdx.x; t < ne * kTriPts * 3; t += blockDim.x) {
-            s_off[t] = qoff[(size_t)e0 * kTriPts * 3 + t];
-            s_qdf[t] = qdf[(size_t)e0 * kTriPts * 3 + t];
+        __syncthreads();  // the previous chunk is no longer read (and the barrier is initialised)
+        if (threadIdx.x == 0) {
+            mbar_expect_tx(&bar, kBytes);
+            bulk_g2s(s_c, cT + ((size_t)fg * E7p + (size_t)e0 * kTriPts) * kBF, sizeof(s_c), &bar);
+            bulk_g2s(s_cent, ecent + (size_t)e0 * 8, sizeof(s_cent), &bar);
+            bulk_g2s(s_off, qoff + (size_t)e0 * kTriPts * 3, sizeof(s_off), &bar);
+            bulk_g2s(s_qdf, qdf + (size_t)e0 * kTriPts * 3, sizeof(s_qdf), &bar);
+            bulk_g2s(s_en, en_pad + (size_t)e0 * NEN, sizeof(s_en), &bar);
         }
-        for (int t = threadIdx.x; t < kBF * ne * kTriPts; t += blockDim.x) {
-            const int ff = t / (ne * kTriPts), r = t % (ne * kTriPts);
-            s_c[r][ff] = ff < nf ? cf32[(size_t)(f0 + ff) * E * kTriPts + (size_t)e0 * kTriPts + r] : 0.0f;
+        const bool ok = mbar_wait(&bar, phase & 1, err, 8);
+        if (!__syncthreads_and(ok)) {
+            if (threadIdx.x == 0) mbar_drain(&bar, phase & 1);  // no copy outlives the block
+            return;
         }
-        for (int t = threadIdx.x; t < ne * NEN; t += blockDim.x) s_en[t] = elems[(size_t)e0 * NEN + t];
-        __syncthreads();
+        phase++;
         if (!valid) continue;
         for (int e = 0; e < ne; e++) {
             const float *ce = s_cent + e * 8;
@@ -659,7 +676,7 @@ __global__ void __launch_bounds__(128) k_field_batched_mixed(
                     gy = dy * i3;
                     gz = dz * i3;
                 }
-                const float4 *cq4 = (const float4 *)s_c[e * kTriPts + q];
+                const float4 *cq4 = (const float4 *)s_c[e * kTriPts + q];  // broadcast reads
 #pragma unroll
                 for (int f4 = 0; f4 < kBF / 4; f4++) {
                     const float4 cq = cq4[f4];
@@ -851,11 +868,12 @@ struct Session::Mixed {
     DevBuf<double> npart;   // per-block partials of |w|^2
     int dots_grid = 0, upd_grid = 0;  // one resident wave of the Gram-Schmidt kernels
     // batched field
-    DevBuf<double> cf, sing, Enode, Fce, tot;
+    DevBuf<double> sing, Enode, Fce, tot;
     DevBuf<float> part;  // field partials per element group (FP32)
     // FP32 far-field pass: element centroids / offsets, split points, weights
     bool far_ready = false;
-    DevBuf<float> ecent, qoff, phl, cf32;
+    DevBuf<float> ecent, qoff, phl, cf32;  // cf32: the charges, kBF systems innermost
+    DevBuf<int> en_pad;                    // element nodes, padded to whole chunks (-1)
     DevBuf<float2> qdf;  // quadrature points in double-FP32 (near pairs)
 };
 
@@ -1194,7 +1212,6 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
     if (fp.P > 0) {
         const int E = s.E, P = fp.P;
         const int nchunk = (E + kBChunk * kBLoop - 1) / (kBChunk * kBLoop);  // element groups
-        DSC_TRY(w.cf.alloc((size_t)F * E * kTriPts));
         DSC_TRY(w.part.alloc((size_t)nchunk * F * P * 3));
         DSC_TRY(w.sing.alloc((size_t)F * P * 3));
         DSC_TRY(w.Enode.alloc((size_t)F * N * 3));
@@ -1202,32 +1219,45 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
         {
             TimerScope ts(tm, kTField, st);
             tm->add_work(kTField, (double)P * E * F);  // (particle node, element) pairs x systems
-            dim3 cg((E * kTriPts + 255) / 256, F);
-            if (s.nen == 6) DSC_LAUNCH(k_charge_batched<6><<<cg, 256, 0, st>>>(s.dev.elems.p, E, s.dev.qp.p, w.Xs.p, ld, F, w.cf.p));
-            else DSC_LAUNCH(k_charge_batched<3><<<cg, 256, 0, st>>>(s.dev.elems.p, E, s.dev.qp.p, w.Xs.p, ld, F, w.cf.p));
+            // element arrays padded to whole chunks for the field pass's bulk copies
+            const int Epad = (E + kBChunk - 1) / kBChunk * kBChunk, E7p = Epad * kTriPts;
+            const int ngrp = (F + kBF - 1) / kBF;
+            DSC_TRY(w.cf32.alloc((size_t)ngrp * E7p * kBF));
+            dim3 cg((E7p + 7) / 8, ngrp), cb(kBF, 8);
+            if (s.nen == 6)
+                DSC_LAUNCH(k_charge_batched<6><<<cg, cb, 0, st>>>(s.dev.elems.p, E, s.dev.qp.p, w.Xs.p, ld, F, E7p,
+                                                                  w.cf32.p));
+            else
+                DSC_LAUNCH(k_charge_batched<3><<<cg, cb, 0, st>>>(s.dev.elems.p, E, s.dev.qp.p, w.Xs.p, ld, F, E7p,
+                                                                  w.cf32.p));
             dim3 fg((P + 127) / 128, nchunk, (F + kBF - 1) / kBF);
             if (!w.far_ready) {
                 // geometry of the far-field pass (the session's mesh is fixed)
-                DSC_TRY(w.ecent.alloc((size_t)E * 8));
-                DSC_TRY(w.qoff.alloc((size_t)E * kTriPts * 3));
+                DSC_TRY(w.ecent.alloc((size_t)Epad * 8));
+                DSC_TRY(w.qoff.alloc((size_t)Epad * kTriPts * 3));
                 DSC_TRY(w.phl.alloc((size_t)P * 6));
-                DSC_TRY(w.qdf.alloc((size_t)E * kTriPts * 3));
+                DSC_TRY(w.qdf.alloc((size_t)Epad * kTriPts * 3));
+                DSC_TRY(w.en_pad.alloc((size_t)Epad * s.nen));
+                DSC_CUDA(cudaMemsetAsync(w.ecent.p, 0, (size_t)Epad * 8 * sizeof(float), st));
+                DSC_CUDA(cudaMemsetAsync(w.qoff.p, 0, (size_t)Epad * kTriPts * 3 * sizeof(float), st));
+                DSC_CUDA(cudaMemsetAsync(w.qdf.p, 0, (size_t)Epad * kTriPts * 3 * sizeof(float2), st));
+                DSC_CUDA(cudaMemsetAsync(w.en_pad.p, 0xFF, (size_t)Epad * s.nen * sizeof(int), st));
+                DSC_CUDA(cudaMemcpyAsync(w.en_pad.p, s.dev.elems.p, (size_t)E * s.nen * sizeof(int),
+                                         cudaMemcpyDeviceToDevice, st));
                 DSC_LAUNCH(k_prepare_far<<<(E + 127) / 128, 128, 0, st>>>(s.dev.qp.p, E, w.ecent.p, w.qoff.p,
                                                                           w.qdf.p));
                 DSC_LAUNCH(k_points_split<<<(P + 127) / 128, 128, 0, st>>>(fp.ps.px.p, fp.ps.py.p, fp.ps.pz.p,
                                                                            P, w.phl.p));
                 w.far_ready = true;
             }
-            DSC_TRY(w.cf32.alloc((size_t)F * E * kTriPts));
-            DSC_LAUNCH(k_to_f32<<<4 * 152, 256, 0, st>>>(w.cf.p, w.cf32.p, (size_t)F * E * kTriPts));
             if (s.nen == 6)
-                DSC_LAUNCH(k_field_batched_mixed<6><<<fg, 128, 0, st>>>(w.phl.p, fp.ps.coinc.p, P, s.dev.elems.p, E,
-                                                                        w.ecent.p, w.qoff.p, w.cf32.p,
-                                                                        w.qdf.p, F, w.part.p));
+                DSC_LAUNCH(k_field_batched_mixed<6><<<fg, 128, 0, st>>>(w.phl.p, fp.ps.coinc.p, P, w.en_pad.p, E,
+                                                                        E7p, w.ecent.p, w.qoff.p, w.cf32.p,
+                                                                        w.qdf.p, F, w.part.p, w.err.p));
             else
-                DSC_LAUNCH(k_field_batched_mixed<3><<<fg, 128, 0, st>>>(w.phl.p, fp.ps.coinc.p, P, s.dev.elems.p, E,
-                                                                        w.ecent.p, w.qoff.p, w.cf32.p,
-                                                                        w.qdf.p, F, w.part.p));
+                DSC_LAUNCH(k_field_batched_mixed<3><<<fg, 128, 0, st>>>(w.phl.p, fp.ps.coinc.p, P, w.en_pad.p, E,
+                                                                        E7p, w.ecent.p, w.qoff.p, w.cf32.p,
+                                                                        w.qdf.p, F, w.part.p, w.err.p));
             const int sb = (P * 32 + 127) / 128;
             if (s.nen == 6)
                 DSC_LAUNCH(k_field_singular_apply<6><<<sb, 128, 0, st>>>(P, s.dev.elems.p, s.dev.normals.p,
@@ -1272,7 +1302,13 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
         DSC_CUDA(cudaMemcpy2DAsync(sigma_host, (size_t)N * sizeof(double), w.Xs.p, ld * sizeof(double),
                                    (size_t)N * sizeof(double), (size_t)2 * F, cudaMemcpyDeviceToHost, st));
     }
+    int herr = 0;  // the field pass's staging waits
+    DSC_CUDA(cudaMemcpyAsync(&herr, w.err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     DSC_CUDA(cudaStreamSynchronize(st));
+    if (herr) {
+        set_error("batched field: a shared-memory staging wait gave up (code %d)", herr);
+        return kErrCuda;
+    }
     return kOk;
 }
 
