@@ -353,7 +353,7 @@ __global__ void k_mst_totals(const double *__restrict__ Fce, int npel, const dou
 
 // ------------------------------------------------------------------ host
 
-int PointSet::build(const HostPlan &plan, int P, const double *pts)
+int PointSet::build(const HostPlan &plan, int P, const double *pts, const int *node_ids)
 {
     this->P = P;
     std::vector<double> xs(P), ys(P), zs(P);
@@ -361,15 +361,43 @@ int PointSet::build(const HostPlan &plan, int P, const double *pts)
     std::vector<int> ptr(1, 0);
     std::vector<int4> tup;
     const int nen = plan.nen;
+    // points that are mesh nodes: each node's group of nodes with identical
+    // coordinates (a run of the coordinate order), found in one pass
+    std::vector<int> grp_lo, grp_hi;
+    if (node_ids) {
+        grp_lo.resize(plan.N);
+        grp_hi.resize(plan.N);
+        for (int a = 0; a < plan.N;) {
+            const double *u = &plan.nodes[3 * (size_t)plan.coord_order[a]];
+            int b = a + 1;
+            while (b < plan.N) {
+                const double *w = &plan.nodes[3 * (size_t)plan.coord_order[b]];
+                if (w[0] != u[0] || w[1] != u[1] || w[2] != u[2]) break;
+                b++;
+            }
+            for (int t = a; t < b; t++) {
+                grp_lo[plan.coord_order[t]] = a;
+                grp_hi[plan.coord_order[t]] = b;
+            }
+            a = b;
+        }
+    }
+    std::vector<int> found, cand;
     // exact-coordinate lookup of mesh nodes
     for (int p = 0; p < P; p++) {
         xs[p] = pts[3 * p];
         ys[p] = pts[3 * p + 1];
         zs[p] = pts[3 * p + 2];
-        auto it = plan_coords_find(plan, xs[p], ys[p], zs[p]);
+        if (node_ids) {
+            const int v = node_ids[p];
+            found.assign(plan.coord_order.begin() + grp_lo[v], plan.coord_order.begin() + grp_hi[v]);
+            std::sort(found.begin(), found.end());
+        } else {
+            found = plan_coords_find(plan, xs[p], ys[p], zs[p]);
+        }
         int nco = 0;
         int ids[4] = {-1, -1, -1, -1};
-        for (int v : it) {
+        for (int v : found) {
             if (nco == 4) {
                 set_error("more than 4 mesh nodes share the coordinates of point %d", p);
                 return kErrArg;
@@ -380,7 +408,7 @@ int PointSet::build(const HostPlan &plan, int P, const double *pts)
         // singular elements of this point, element order, first matching
         // position within the element (src/field.c:164-173)
         if (nco > 0) {
-            std::vector<int> cand;
+            cand.clear();
             for (int u = 0; u < nco; u++)
                 for (int t = plan.ne_ptr[ids[u]]; t < plan.ne_ptr[ids[u] + 1]; t++)
                     cand.push_back(plan.ne_elem[t]);
@@ -555,7 +583,7 @@ int ForcePlan::build(const HostPlan &plan, const unsigned *bctype, cudaStream_t 
     P = (int)idv.size();
     npel = (int)pel_host.size();
     if (P == 0) return kOk;
-    DSC_TRY(ps.build(plan, P, pts.data()));
+    DSC_TRY(ps.build(plan, P, pts.data(), idv.data()));
     {
         // tuple (e, s, v) of the field = tuple (row v, element e, position
         // s - 1) of the assembly's singular pass, which takes it at v's

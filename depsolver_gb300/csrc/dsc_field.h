@@ -23,7 +23,10 @@ struct PointSet {
     // workspace of eval_points (charge-weighted points, chunk partials,
     // singular parts), kept between calls
     DevBuf<double> cq, part, sing;
-    int build(const HostPlan &plan, int P, const double *pts);
+    // node_ids (may be null): point p is mesh node node_ids[p] (its
+    // coincident nodes then come from one pass over the coordinate order
+    // instead of a search per point)
+    int build(const HostPlan &plan, int P, const double *pts, const int *node_ids = nullptr);
 };
 
 // field = 1: dout = P x 6 (Re Ex, Im Ex, Re Ey, Im Ey, Re Ez, Im Ez);

@@ -153,14 +153,22 @@ static void plan_adjacency_and_coords(HostPlan &p, int nen, int N, int E, const 
             p.ne_pos[fill[v]] = k;
             fill[v]++;
         }
-    p.coord_order.resize(N);
-    std::iota(p.coord_order.begin(), p.coord_order.end(), 0);
-    std::stable_sort(p.coord_order.begin(), p.coord_order.end(), [&](int a, int b) {
-        const double *u = &p.nodes[3 * (size_t)a], *v = &p.nodes[3 * (size_t)b];
-        if (u[0] != v[0]) return u[0] < v[0];
-        if (u[1] != v[1]) return u[1] < v[1];
-        return u[2] < v[2];
+    // (x, y, z, node) records sorted directly (no indirection through the
+    // node array); ties in the coordinates keep node order
+    struct Rec {
+        double x, y, z;
+        int i;
+    };
+    std::vector<Rec> r(N);
+    for (int i = 0; i < N; i++) r[i] = {p.nodes[3 * (size_t)i], p.nodes[3 * (size_t)i + 1], p.nodes[3 * (size_t)i + 2], i};
+    std::sort(r.begin(), r.end(), [](const Rec &a, const Rec &b) {
+        if (a.x != b.x) return a.x < b.x;
+        if (a.y != b.y) return a.y < b.y;
+        if (a.z != b.z) return a.z < b.z;
+        return a.i < b.i;
     });
+    p.coord_order.resize(N);
+    for (int t = 0; t < N; t++) p.coord_order[t] = r[t].i;
 }
 
 int build_plan(int nen, int N, int E, const double *nodes, const int *el,
@@ -211,9 +219,12 @@ int build_plan(int nen, int N, int E, const double *nodes, const int *el,
         }
         code[e] = c;
     }
+    // (code, element) pairs sorted directly; equal codes keep element order
+    std::vector<std::pair<uint64_t, int>> ce(E);
+    for (int e = 0; e < E; e++) ce[e] = {code[e], e};
+    std::sort(ce.begin(), ce.end());
     std::vector<int> order(E);
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return code[a] < code[b]; });
+    for (int t = 0; t < E; t++) order[t] = ce[t].second;
 
     p.G = (E + kGroup - 1) / kGroup;
     p.grp_elem.assign((size_t)p.G * kGroup, -1);
