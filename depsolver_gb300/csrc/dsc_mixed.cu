@@ -611,9 +611,12 @@ __global__ void __launch_bounds__(128) k_field_batched_mixed(
         mbar_init(&bar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    float acc[kBF][3];
+    // accumulators of system pairs (2j, 2j + 1) per component: one packed
+    // FP32x2 FMA (two round-to-nearest FMAs, as two FFMAs would give) per
+    // pair, half the issue slots
+    float2 acc[kBF / 2][3];
 #pragma unroll
-    for (int ff = 0; ff < kBF; ff++) acc[ff][0] = acc[ff][1] = acc[ff][2] = 0.0f;
+    for (int j = 0; j < kBF / 2; j++) acc[j][0] = acc[j][1] = acc[j][2] = make_float2(0.0f, 0.0f);
     uint32_t phase = 0;
     for (int cl = 0; cl < kBLoop; cl++) {
         const int e0 = (group * kBLoop + cl) * kBChunk;
@@ -677,21 +680,17 @@ __global__ void __launch_bounds__(128) k_field_batched_mixed(
                     gz = dz * i3;
                 }
                 const float4 *cq4 = (const float4 *)s_c[e * kTriPts + q];  // broadcast reads
+                const float2 g2x = make_float2(gx, gx), g2y = make_float2(gy, gy), g2z = make_float2(gz, gz);
 #pragma unroll
                 for (int f4 = 0; f4 < kBF / 4; f4++) {
                     const float4 cq = cq4[f4];
-                    acc[4 * f4][0] += cq.x * gx;
-                    acc[4 * f4][1] += cq.x * gy;
-                    acc[4 * f4][2] += cq.x * gz;
-                    acc[4 * f4 + 1][0] += cq.y * gx;
-                    acc[4 * f4 + 1][1] += cq.y * gy;
-                    acc[4 * f4 + 1][2] += cq.y * gz;
-                    acc[4 * f4 + 2][0] += cq.z * gx;
-                    acc[4 * f4 + 2][1] += cq.z * gy;
-                    acc[4 * f4 + 2][2] += cq.z * gz;
-                    acc[4 * f4 + 3][0] += cq.w * gx;
-                    acc[4 * f4 + 3][1] += cq.w * gy;
-                    acc[4 * f4 + 3][2] += cq.w * gz;
+                    const float2 c01 = make_float2(cq.x, cq.y), c23 = make_float2(cq.z, cq.w);
+                    acc[2 * f4][0] = __ffma2_rn(c01, g2x, acc[2 * f4][0]);
+                    acc[2 * f4][1] = __ffma2_rn(c01, g2y, acc[2 * f4][1]);
+                    acc[2 * f4][2] = __ffma2_rn(c01, g2z, acc[2 * f4][2]);
+                    acc[2 * f4 + 1][0] = __ffma2_rn(c23, g2x, acc[2 * f4 + 1][0]);
+                    acc[2 * f4 + 1][1] = __ffma2_rn(c23, g2y, acc[2 * f4 + 1][1]);
+                    acc[2 * f4 + 1][2] = __ffma2_rn(c23, g2z, acc[2 * f4 + 1][2]);
                 }
             }
         }
@@ -701,7 +700,8 @@ __global__ void __launch_bounds__(128) k_field_batched_mixed(
     for (int ff = 0; ff < kBF; ff++)  // unrolled: acc stays in registers
         if (ff < nf)
 #pragma unroll
-            for (int d = 0; d < 3; d++) part[(((size_t)group * F + f0 + ff) * P + p) * 3 + d] = acc[ff][d];
+            for (int d = 0; d < 3; d++)
+                part[(((size_t)group * F + f0 + ff) * P + p) * 3 + d] = (ff & 1) ? acc[ff / 2][d].y : acc[ff / 2][d].x;
 }
 
 // The singular part of the field at each point for every system: the
