@@ -764,35 +764,57 @@ __global__ void k_field_batched_reduce(const float *__restrict__ part, int nchun
     Enode[((size_t)f * N + ids[p]) * 3 + d] = A * s + sing[t];
 }
 
-// Maxwell stress per (particle element, frequency).
+// Frequency-independent geometry of the Maxwell-stress integrals: per
+// (particle element t, point q) the weight w_q J_q and the unit normal.
 template <int NEN>
-__global__ void k_mst_batched(const double *__restrict__ X, const double *__restrict__ Y,
-                              const double *__restrict__ Z, const int *__restrict__ elems,
-                              const int *__restrict__ pel, int npel, const double *__restrict__ Enode,
-                              int N, int F, double eps, double *__restrict__ Fce)
+__global__ void k_mst_geometry(const double *__restrict__ X, const double *__restrict__ Y,
+                               const double *__restrict__ Z, const int *__restrict__ elems,
+                               const int *__restrict__ pel, int npel, double4 *__restrict__ geo)
+{
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= npel * kTriPts) return;
+    const int t = u / kTriPts, q = u % kTriPts;
+    const int e = pel[t];
+    double Xe[NEN][3], N6[NEN], XL[3], n[3];
+#pragma unroll
+    for (int k = 0; k < NEN; k++) {
+        const int v = elems[(size_t)e * NEN + k];
+        Xe[k][0] = X[v];
+        Xe[k][1] = Y[v];
+        Xe[k][2] = Z[v];
+    }
+    const double l1 = c_tri7[q][0], l2 = c_tri7[q][1];
+    shape<NEN>(l1, l2, N6);
+    const double J = map_point<NEN>(Xe, l1, l2, N6, XL);
+    local_normal<NEN>(Xe, l1, l2, n);
+    geo[u] = make_double4(J * c_tri7[q][2], n[0], n[1], n[2]);
+}
+
+// Maxwell stress per (particle element, frequency), from the element's
+// geometry (k_mst_geometry) and the nodal field of that frequency.
+template <int NEN>
+__global__ void k_mst_batched(const int *__restrict__ elems, const int *__restrict__ pel, int npel,
+                              const double4 *__restrict__ geo, const double *__restrict__ Enode, int N, int F,
+                              double eps, double *__restrict__ Fce)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int f = blockIdx.y;
     if (t >= npel) return;
     const int e = pel[t];
     const double *En0 = Enode + (size_t)f * N * 3;
-    double Xe[NEN][3], En[NEN][3], N6[NEN], XL[3], n[3];
+    double En[NEN][3], N6[NEN];
 #pragma unroll
     for (int k = 0; k < NEN; k++) {
-        int v = elems[(size_t)e * NEN + k];
-        Xe[k][0] = X[v];
-        Xe[k][1] = Y[v];
-        Xe[k][2] = Z[v];
+        const int v = elems[(size_t)e * NEN + k];
         En[k][0] = En0[3 * (size_t)v];
         En[k][1] = En0[3 * (size_t)v + 1];
         En[k][2] = En0[3 * (size_t)v + 2];
     }
     double I0 = 0.0, I1 = 0.0, I2 = 0.0;
+#pragma unroll
     for (int q = 0; q < kTriPts; q++) {
-        double l1 = c_tri7[q][0], l2 = c_tri7[q][1];
-        shape<NEN>(l1, l2, N6);
-        double J = map_point<NEN>(Xe, l1, l2, N6, XL);
-        local_normal<NEN>(Xe, l1, l2, n);
+        shape<NEN>(c_tri7[q][0], c_tri7[q][1], N6);
+        const double4 g = geo[(size_t)t * kTriPts + q];
         double Ex = 0.0, Ey = 0.0, Ez = 0.0;
 #pragma unroll
         for (int k = 0; k < NEN; k++) {
@@ -800,12 +822,11 @@ __global__ void k_mst_batched(const double *__restrict__ X, const double *__rest
             Ey += En[k][1] * N6[k];
             Ez += En[k][2] * N6[k];
         }
-        double NE = Ex * n[0] + Ey * n[1] + Ez * n[2];
-        double Esq = Ex * Ex + Ey * Ey + Ez * Ez;
-        double A = J * c_tri7[q][2];
-        I0 += A * (Ex * NE - 0.5 * Esq * n[0]);
-        I1 += A * (Ey * NE - 0.5 * Esq * n[1]);
-        I2 += A * (Ez * NE - 0.5 * Esq * n[2]);
+        const double NE = Ex * g.y + Ey * g.z + Ez * g.w;
+        const double Esq = Ex * Ex + Ey * Ey + Ez * Ez;
+        I0 += g.x * (Ex * NE - 0.5 * Esq * g.y);
+        I1 += g.x * (Ey * NE - 0.5 * Esq * g.z);
+        I2 += g.x * (Ez * NE - 0.5 * Esq * g.w);
     }
     const double A = 0.5 * eps;
     double *o = Fce + ((size_t)f * npel + t) * 3;
@@ -814,28 +835,41 @@ __global__ void k_mst_batched(const double *__restrict__ X, const double *__rest
     o[2] = A * I2;
 }
 
-// tot[f][9]: Fcm, Xcm, sum |Fce| (one warp per frequency, fixed order)
-__global__ void k_mst_batched_totals(const double *__restrict__ Fce, int npel, int F,
-                                     const double *__restrict__ X, const double *__restrict__ Y,
-                                     const double *__restrict__ Z, const int *__restrict__ ids, int P,
-                                     double *__restrict__ tot)
+// tot[f][9]: Fcm, Xcm, sum |Fce| (one block of kTotThreads per frequency;
+// per-thread strided sums, warp sums, then the warps' sums in order: a
+// fixed order)
+constexpr int kTotThreads = 256;
+__global__ void __launch_bounds__(kTotThreads) k_mst_batched_totals(const double *__restrict__ Fce, int npel, int F,
+                                                                    const double *__restrict__ X,
+                                                                    const double *__restrict__ Y,
+                                                                    const double *__restrict__ Z,
+                                                                    const int *__restrict__ ids, int P,
+                                                                    double *__restrict__ tot)
 {
-    const int f = blockIdx.x, lane = threadIdx.x;
+    __shared__ double sh[kTotThreads / 32][9];
+    const int f = blockIdx.x, lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
     const double *Fc = Fce + (size_t)f * npel * 3;
     double s[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int t = lane; t < npel; t += 32)
+    for (int t = threadIdx.x; t < npel; t += kTotThreads)
         for (int d = 0; d < 3; d++) {
             s[d] += Fc[3 * (size_t)t + d];
             s[6 + d] += fabs(Fc[3 * (size_t)t + d]);
         }
-    for (int q = lane; q < P; q += 32) {
+    for (int q = threadIdx.x; q < P; q += kTotThreads) {
         s[3] += X[ids[q]];
         s[4] += Y[ids[q]];
         s[5] += Z[ids[q]];
     }
     for (int k = 0; k < 9; k++) s[k] = warp_sum(s[k]);
     if (lane == 0)
-        for (int k = 0; k < 9; k++) tot[(size_t)f * 9 + k] = (k >= 3 && k < 6) ? s[k] / P : s[k];
+        for (int k = 0; k < 9; k++) sh[wp][k] = s[k];
+    __syncthreads();
+    if (threadIdx.x < 9) {
+        const int k = threadIdx.x;
+        double t = 0.0;
+        for (int w = 0; w < kTotThreads / 32; w++) t += sh[w][k];
+        tot[(size_t)f * 9 + k] = (k >= 3 && k < 6) ? t / P : t;
+    }
 }
 
 // ------------------------------------------------------------ workspace
@@ -869,6 +903,7 @@ struct Session::Mixed {
     int dots_grid = 0, upd_grid = 0;  // one resident wave of the Gram-Schmidt kernels
     // batched field
     DevBuf<double> sing, Enode, Fce, tot;
+    DevBuf<double4> mst_geo;  // per (particle element, point): w J and the unit normal
     DevBuf<float> part;  // field partials per element group (FP32)
     // FP32 far-field pass: element centroids / offsets, split points, weights
     bool far_ready = false;
@@ -1274,16 +1309,23 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
         }
         TimerScope ts(tm, kTMst, st);
         if (fp.npel > 0) {
+            DSC_TRY(w.mst_geo.alloc((size_t)fp.npel * kTriPts));
+            const int gq = (fp.npel * kTriPts + 127) / 128;
             dim3 mg((fp.npel + 127) / 128, F);
-            if (s.nen == 6)
-                DSC_LAUNCH(k_mst_batched<6><<<mg, 128, 0, st>>>(s.dev.x.p, s.dev.y.p, s.dev.z.p, s.dev.elems.p, fp.pel.p,
-                                                     fp.npel, w.Enode.p, N, F, s.eps_medium, w.Fce.p));
-            else
-                DSC_LAUNCH(k_mst_batched<3><<<mg, 128, 0, st>>>(s.dev.x.p, s.dev.y.p, s.dev.z.p, s.dev.elems.p, fp.pel.p,
-                                                     fp.npel, w.Enode.p, N, F, s.eps_medium, w.Fce.p));
+            if (s.nen == 6) {
+                DSC_LAUNCH(k_mst_geometry<6><<<gq, 128, 0, st>>>(s.dev.x.p, s.dev.y.p, s.dev.z.p, s.dev.elems.p,
+                                                                 fp.pel.p, fp.npel, w.mst_geo.p));
+                DSC_LAUNCH(k_mst_batched<6><<<mg, 128, 0, st>>>(s.dev.elems.p, fp.pel.p, fp.npel, w.mst_geo.p,
+                                                                w.Enode.p, N, F, s.eps_medium, w.Fce.p));
+            } else {
+                DSC_LAUNCH(k_mst_geometry<3><<<gq, 128, 0, st>>>(s.dev.x.p, s.dev.y.p, s.dev.z.p, s.dev.elems.p,
+                                                                 fp.pel.p, fp.npel, w.mst_geo.p));
+                DSC_LAUNCH(k_mst_batched<3><<<mg, 128, 0, st>>>(s.dev.elems.p, fp.pel.p, fp.npel, w.mst_geo.p,
+                                                                w.Enode.p, N, F, s.eps_medium, w.Fce.p));
+            }
         }
-        DSC_LAUNCH(k_mst_batched_totals<<<F, 32, 0, st>>>(w.Fce.p, fp.npel, F, s.dev.x.p, s.dev.y.p, s.dev.z.p,
-                                               fp.ids.p, P, w.tot.p));
+        DSC_LAUNCH(k_mst_batched_totals<<<F, kTotThreads, 0, st>>>(w.Fce.p, fp.npel, F, s.dev.x.p, s.dev.y.p,
+                                                                   s.dev.z.p, fp.ids.p, P, w.tot.p));
         DSC_CUDA(cudaGetLastError());
         if (tot_host)
             DSC_CUDA(cudaMemcpyAsync(tot_host, w.tot.p, (size_t)F * 9 * sizeof(double),
