@@ -135,6 +135,28 @@ __global__ void k_pre_init(const double *__restrict__ K, size_t ld, const double
     X[(size_t)c * ldx + a] = v;
 }
 
+// A 128 x 128 FP32 tile at base (element (a, b) at base[a * stride + b], b
+// contiguous, 16-byte aligned rows) into shared memory through put(a, b,
+// value): 16 float4 loads per thread (256 threads) issued before the stores.
+template <typename Put>
+__device__ __forceinline__ void load_tile128(const float *__restrict__ base, size_t stride, Put put)
+{
+    float4 v[16];
+#pragma unroll
+    for (int u = 0; u < 16; u++) {
+        const int t = threadIdx.x + 256 * u, a = t >> 5, b = 4 * (t & 31);
+        v[u] = *(const float4 *)(base + (size_t)a * stride + b);
+    }
+#pragma unroll
+    for (int u = 0; u < 16; u++) {
+        const int t = threadIdx.x + 256 * u, a = t >> 5, b = 4 * (t & 31);
+        put(a, b, v[u].x);
+        put(a, b + 1, v[u].y);
+        put(a, b + 2, v[u].z);
+        put(a, b + 3, v[u].w);
+    }
+}
+
 // tP = inverse of the 128 x 128 diagonal block k of each matrix, row-major
 // (Gauss-Jordan without pivoting, one CTA of 256 threads per matrix).  The
 // block lives in registers: thread (tr, tc) = (t / 16, t % 16) owns rows
@@ -260,10 +282,7 @@ __global__ void __launch_bounds__(256) k_gj_row(GJArgs g, int nb, int k)
             if (threadIdx.x < kPB) g.ra[b][J * kPB + threadIdx.x] = 1.0f;
             return;
         }
-        for (int t = threadIdx.x; t < kPB * kPB; t += blockDim.x) {
-            const int kk = t >> 7, i = t & 127;
-            T[i][kk] = X[(size_t)(k * kPB + kk) * ldx + J * kPB + i];
-        }
+        load_tile128(X + (size_t)k * kPB * ldx + J * kPB, (size_t)ldx, [&](int kk, int i, float v) { T[i][kk] = v; });
         __syncthreads();
         for (int i = warp; i < kPB; i += 8)
             pre_row_pair(&T[i][0], Ah + (size_t)i * kPB, Al + (size_t)i * kPB, &g.ra[b][J * kPB + i]);
@@ -272,18 +291,12 @@ __global__ void __launch_bounds__(256) k_gj_row(GJArgs g, int nb, int k)
     // R_J[kk][j] = sum_q P[kk][q] X(k*128 + q, J*128 + j); T[j][kk] = R_J[kk][j]
     const float *P = g.tP[b];
     if (J == k) {
-        for (int t = threadIdx.x; t < kPB * kPB; t += blockDim.x) {
-            const int kk = t >> 7, j = t & 127;
-            T[j][kk] = P[t];
-        }
+        load_tile128(P, kPB, [&](int kk, int j, float v) { T[j][kk] = v; });
     } else {
         float(*Pt)[128] = (float(*)[128])(sm + kPB * 129);       // Pt[q][kk] = P[kk][q]
         float(*Xs)[129] = (float(*)[129])(sm + kPB * 129 + kPB * 128);  // Xs[j][q] = X(k*128 + q, J*128 + j)
-        for (int t = threadIdx.x; t < kPB * kPB; t += blockDim.x) {
-            const int r = t >> 7, c = t & 127;
-            Pt[c][r] = P[t];
-            Xs[r][c] = X[(size_t)(J * kPB + r) * ldx + k * kPB + c];
-        }
+        load_tile128(P, kPB, [&](int r, int c, float v) { Pt[c][r] = v; });
+        load_tile128(X + (size_t)J * kPB * ldx + k * kPB, (size_t)ldx, [&](int r, int c, float v) { Xs[r][c] = v; });
         __syncthreads();
         // thread (ty, tx): kk = 8 ty + u, j = tx + 16 v (u, v < 8)
         const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
