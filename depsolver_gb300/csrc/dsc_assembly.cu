@@ -407,8 +407,16 @@ __global__ void __launch_bounds__(128) k_asm_regular_f32(AsmArgs a, const float2
     __shared__ float2 s_c[EG * 3];
     __shared__ float s_V[EG * NEN * R];
     __shared__ int s_nodes[EG * NEN];
+    // the group's footprint lists (at most EG * NEN nodes and slots)
+    __shared__ int s_ptr[EG * NEN + 1], s_dest[EG * NEN];
+    __shared__ uint16_t s_sl[EG * NEN];
     const int g = blockIdx.y;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int f0 = a.fp_ptr[g], nfp = a.fp_ptr[g + 1] - f0;
+    const int sl0 = a.fp_sl_ptr[f0], nsl = a.fp_sl_ptr[f0 + nfp] - sl0;
+    for (int t = threadIdx.x; t <= nfp; t += blockDim.x) s_ptr[t] = a.fp_sl_ptr[f0 + t] - sl0;
+    for (int t = threadIdx.x; t < nfp; t += blockDim.x) s_dest[t] = a.fp_dest[f0 + t];
+    for (int t = threadIdx.x; t < nsl; t += blockDim.x) s_sl[t] = a.fp_sl[sl0 + t];
 
     for (int t = threadIdx.x; t < EG * kTriPts; t += blockDim.x) {
         const int e = a.grp_elem[g * EG + t / kTriPts];
@@ -460,12 +468,11 @@ __global__ void __launch_bounds__(128) k_asm_regular_f32(AsmArgs a, const float2
     }
     __syncthreads();
 
-    const int f0 = a.fp_ptr[g], f1 = a.fp_ptr[g + 1];
-    for (int j = f0 + w; j < f1; j += 4) {
-        const int s0 = a.fp_sl_ptr[j], s1 = a.fp_sl_ptr[j + 1];
+    for (int j = w; j < nfp; j += 4) {
+        const int s0 = s_ptr[j], s1 = s_ptr[j + 1];
         float sum = 0.f;
-        for (int m = s0; m < s1; m++) sum += s_V[a.fp_sl[m] * R + lane];
-        const int dest = a.fp_dest[j];
+        for (int m = s0; m < s1; m++) sum += s_V[s_sl[m] * R + lane];
+        const int dest = s_dest[j];
         if (valid) {
             if (dest >= 0) K[(size_t)dest * a.ld + i] = f32_widen(sum);
             else P[(size_t)(-dest - 1) * a.ldp + (i - a.row_lo)] = sum;
