@@ -18,6 +18,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <thread>
 
 #include "dsc_common.cuh"
 #include "dsc_field.h"
@@ -382,51 +383,72 @@ int PointSet::build(const HostPlan &plan, int P, const double *pts, const int *n
             a = b;
         }
     }
-    std::vector<int> found, cand;
-    // exact-coordinate lookup of mesh nodes
-    for (int p = 0; p < P; p++) {
-        xs[p] = pts[3 * p];
-        ys[p] = pts[3 * p + 1];
-        zs[p] = pts[3 * p + 2];
-        if (node_ids) {
-            const int v = node_ids[p];
-            found.assign(plan.coord_order.begin() + grp_lo[v], plan.coord_order.begin() + grp_hi[v]);
-            std::sort(found.begin(), found.end());
-        } else {
-            found = plan_coords_find(plan, xs[p], ys[p], zs[p]);
-        }
-        int nco = 0;
-        int ids[4] = {-1, -1, -1, -1};
-        for (int v : found) {
-            if (nco == 4) {
-                set_error("more than 4 mesh nodes share the coordinates of point %d", p);
-                return kErrArg;
+    // points split over host threads in contiguous ranges (tuples
+    // concatenated in point order afterwards)
+    const int nth = P >= 2048 ? std::min(8, (P + 1023) / 1024) : 1;
+    std::vector<std::vector<int4>> tups(nth);
+    std::vector<int> cnt(P, 0), bad(nth, -1);
+    auto work = [&](int th) {
+        std::vector<int> found, cand;
+        const int p0 = (int)((long long)P * th / nth), p1 = (int)((long long)P * (th + 1) / nth);
+        std::vector<int4> &tu = tups[th];
+        for (int p = p0; p < p1; p++) {
+            xs[p] = pts[3 * p];
+            ys[p] = pts[3 * p + 1];
+            zs[p] = pts[3 * p + 2];
+            // exact-coordinate lookup of mesh nodes
+            if (node_ids) {
+                const int v = node_ids[p];
+                found.assign(plan.coord_order.begin() + grp_lo[v], plan.coord_order.begin() + grp_hi[v]);
+                std::sort(found.begin(), found.end());
+            } else {
+                found = plan_coords_find(plan, xs[p], ys[p], zs[p]);
             }
-            ids[nco++] = v;
-        }
-        co[p] = make_int4(ids[0], ids[1], ids[2], ids[3]);
-        // singular elements of this point, element order, first matching
-        // position within the element (src/field.c:164-173)
-        if (nco > 0) {
-            cand.clear();
-            for (int u = 0; u < nco; u++)
-                for (int t = plan.ne_ptr[ids[u]]; t < plan.ne_ptr[ids[u] + 1]; t++)
-                    cand.push_back(plan.ne_elem[t]);
-            std::sort(cand.begin(), cand.end());
-            cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
-            for (int e : cand) {
-                for (int k = 0; k < nen; k++) {
-                    int v = plan.elems[(size_t)e * nen + k];
-                    if (plan.nodes[3 * (size_t)v] == xs[p] && plan.nodes[3 * (size_t)v + 1] == ys[p] &&
-                        plan.nodes[3 * (size_t)v + 2] == zs[p]) {
-                        tup.push_back(make_int4(e, k + 1, v, 0));
-                        break;
+            if (found.size() > 4) {
+                bad[th] = p;
+                return;
+            }
+            int ids[4] = {-1, -1, -1, -1};
+            const int nco = (int)found.size();
+            for (int u = 0; u < nco; u++) ids[u] = found[u];
+            co[p] = make_int4(ids[0], ids[1], ids[2], ids[3]);
+            // singular elements of this point, element order, first matching
+            // position within the element (src/field.c:164-173)
+            const size_t before = tu.size();
+            if (nco > 0) {
+                cand.clear();
+                for (int u = 0; u < nco; u++)
+                    for (int t = plan.ne_ptr[ids[u]]; t < plan.ne_ptr[ids[u] + 1]; t++)
+                        cand.push_back(plan.ne_elem[t]);
+                std::sort(cand.begin(), cand.end());
+                cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
+                for (int e : cand) {
+                    for (int k = 0; k < nen; k++) {
+                        int v = plan.elems[(size_t)e * nen + k];
+                        if (plan.nodes[3 * (size_t)v] == xs[p] && plan.nodes[3 * (size_t)v + 1] == ys[p] &&
+                            plan.nodes[3 * (size_t)v + 2] == zs[p]) {
+                            tu.push_back(make_int4(e, k + 1, v, 0));
+                            break;
+                        }
                     }
                 }
             }
+            cnt[p] = (int)(tu.size() - before);
         }
-        ptr.push_back((int)tup.size());
+    };
+    {
+        std::vector<std::thread> th;
+        for (int t = 1; t < nth; t++) th.emplace_back(work, t);
+        work(0);
+        for (auto &t : th) t.join();
     }
+    for (int t = 0; t < nth; t++)
+        if (bad[t] >= 0) {
+            set_error("more than 4 mesh nodes share the coordinates of point %d", bad[t]);
+            return kErrArg;
+        }
+    for (int p = 0; p < P; p++) ptr.push_back(ptr.back() + cnt[p]);
+    for (int t = 0; t < nth; t++) tup.insert(tup.end(), tups[t].begin(), tups[t].end());
     cudaStream_t st = 0;
     DSC_TRY(px.upload(xs, st));
     DSC_TRY(py.upload(ys, st));

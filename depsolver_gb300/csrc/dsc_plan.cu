@@ -236,16 +236,30 @@ int build_plan(int nen, int N, int E, const double *nodes, const int *el,
     std::vector<std::pair<int, int>> fpa((size_t)p.G * per);
     std::vector<int> fpn(p.G, 0);
     std::vector<int> ngroups(N, 0), lastg(N, -1);
+    {
+        // each group's (node, slot) pairs sorted, groups split over host threads
+        const int nt = std::max(1, std::min(8, (p.G + 31) / 32));
+        auto work = [&](int t0) {
+            for (int g = t0; g < p.G; g += nt) {
+                std::pair<int, int> *f = fpa.data() + (size_t)g * per;
+                int n = 0;
+                for (int j = 0; j < kGroup; j++) {
+                    int e = p.grp_elem[(size_t)g * kGroup + j];
+                    if (e < 0) continue;
+                    for (int k = 0; k < nen; k++) f[n++] = {el[(size_t)e * nen + k], j * nen + k};
+                }
+                std::sort(f, f + n);
+                fpn[g] = n;
+            }
+        };
+        std::vector<std::thread> th;
+        for (int t = 1; t < nt; t++) th.emplace_back(work, t);
+        work(0);
+        for (auto &t : th) t.join();
+    }
     for (int g = 0; g < p.G; g++) {
-        std::pair<int, int> *f = fpa.data() + (size_t)g * per;
-        int n = 0;
-        for (int j = 0; j < kGroup; j++) {
-            int e = p.grp_elem[(size_t)g * kGroup + j];
-            if (e < 0) continue;
-            for (int k = 0; k < nen; k++) f[n++] = {el[(size_t)e * nen + k], j * nen + k};
-        }
-        std::sort(f, f + n);
-        fpn[g] = n;
+        const std::pair<int, int> *f = fpa.data() + (size_t)g * per;
+        const int n = fpn[g];
         for (int t = 0; t < n; t++) {
             int v = f[t].first;
             if (lastg[v] != g) {
