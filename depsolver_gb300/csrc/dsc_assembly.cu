@@ -394,11 +394,37 @@ __device__ __forceinline__ void pair_regular_f32(const float4 *__restrict__ q7, 
     }
 }
 
+// Per-row data of the FP32 assembly, once per assembly (its conversions run
+// on the FP64 pipe): x, y, z as double-FP32 pairs, the normal and the row
+// factor in FP32.
+struct RowF32 {
+    float2 x, y, z;
+    float nx, ny, nz, fac;
+};
+
+__global__ void k_rows_f32(const double *__restrict__ X, const double *__restrict__ Y, const double *__restrict__ Z,
+                           const double *__restrict__ normals, const double *__restrict__ row_fac, int N,
+                           RowF32 *__restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    RowF32 r;
+    r.x = df_from(X[i]);
+    r.y = df_from(Y[i]);
+    r.z = df_from(Z[i]);
+    r.nx = (float)normals[3 * (size_t)i];
+    r.ny = (float)normals[3 * (size_t)i + 1];
+    r.nz = (float)normals[3 * (size_t)i + 2];
+    r.fac = (float)row_fac[i];
+    out[i] = r;
+}
+
 // As k_asm_regular_df32 (same tiles, footprints and partial slots), with the
 // pair integrals, the row factor and the footprint sums in FP32; K's
 // entries widened to FP64, the partial slots kept in FP32 (k_asm_fixup_f32).
 template <int NEN>
-__global__ void __launch_bounds__(128) k_asm_regular_f32(AsmArgs a, const float2 *__restrict__ cen,
+__global__ void __launch_bounds__(128) k_asm_regular_f32(AsmArgs a, const RowF32 *__restrict__ rows,
+                                                         const float2 *__restrict__ cen,
                                                          const float4 *__restrict__ qloc, double *__restrict__ K,
                                                          float *__restrict__ P)
 {
@@ -435,11 +461,11 @@ __global__ void __launch_bounds__(128) k_asm_regular_f32(AsmArgs a, const float2
     const int i = a.row_lo + blockIdx.x * R + lane;
     const bool valid = i < a.row_hi;
     const int ii = valid ? i : a.row_lo;
-    const float2 xi = df_from(a.X[ii]), yi = df_from(a.Y[ii]), zi = df_from(a.Z[ii]);
-    const float nx = (float)a.normals[3 * (size_t)ii], ny = (float)a.normals[3 * (size_t)ii + 1],
-                nz = (float)a.normals[3 * (size_t)ii + 2];
+    const RowF32 rd = rows[ii];
+    const float2 xi = rd.x, yi = rd.y, zi = rd.z;
+    const float nx = rd.nx, ny = rd.ny, nz = rd.nz;
     const int kind = valid ? a.row_kind[ii] : 0;
-    const float fac = (float)a.row_fac[ii];
+    const float fac = rd.fac;
     const bool allG = __all_sync(0xffffffffu, kind == 0);
     const bool allH = __all_sync(0xffffffffu, kind == 1);
 
@@ -602,7 +628,10 @@ static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStr
     if (f32) {
         DSC_TRY(w.cen.alloc((size_t)m.E * 3));
         DSC_TRY(w.qloc.alloc((size_t)m.E * kTriPts));
+        DSC_TRY(w.rows.alloc((size_t)m.N * sizeof(RowF32)));
         DSC_LAUNCH(k_qp_local<<<(m.E + 127) / 128, 128, 0, st>>>(m.qp.p, m.E, w.cen.p, w.qloc.p));
+        DSC_LAUNCH(k_rows_f32<<<(m.N + 127) / 128, 128, 0, st>>>(m.x.p, m.y.p, m.z.p, m.normals.p, m.row_fac.p,
+                                                                 m.N, (RowF32 *)w.rows.p));
     }
     // Partial-sum buffer: n_slots columns of a row chunk, at most ~1 GiB.
     const size_t budget = (size_t)1 << 30;
@@ -630,7 +659,9 @@ static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStr
         dim3 grid((hi - lo + kRowTile - 1) / kRowTile, m.G);
         {
             TimerScope ts(tm, kTAsmRegular, st);
-            if (f32) DSC_LAUNCH(k_asm_regular_f32<NEN><<<grid, 128, 0, st>>>(a, w.cen.p, w.qloc.p, K, w.P32.p));
+            if (f32)
+                DSC_LAUNCH(k_asm_regular_f32<NEN><<<grid, 128, 0, st>>>(a, (const RowF32 *)w.rows.p, w.cen.p, w.qloc.p,
+                                                                        K, w.P32.p));
             else if (df32) DSC_LAUNCH(k_asm_regular_df32<NEN><<<grid, 128, smem, st>>>(a, qpd.p, K, P.p));
             else DSC_LAUNCH(k_asm_regular_f64<NEN><<<grid, 128, smem, st>>>(a, K, P.p));
             if (tm) tm->add_work(kTAsmRegular, (double)(hi - lo) * m.E);  // (row, element) pairs

@@ -239,6 +239,7 @@ struct AsmWorkspace {
     DevBuf<float2> qpd;
     DevBuf<float2> cen;
     DevBuf<float4> qloc;
+    DevBuf<unsigned char> rows;  // per-row FP32 data of the FP32 assembly
 };
 
 // Arithmetic of the regular pairs, most accurate first: FP64 (the
