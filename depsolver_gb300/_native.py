@@ -78,6 +78,8 @@ def lib() -> C.CDLL:
         L.dsc_session_set_timing.restype = C.c_int
         L.dsc_session_set_timing.argtypes = [C.c_void_p, C.c_int]
         L.dsc_session_set_preconditioner.restype = C.c_int
+        L.dsc_session_set_field_tensor.restype = C.c_int
+        L.dsc_session_set_field_tensor.argtypes = [C.c_void_p, C.c_int]
         L.dsc_session_set_mixed_assembly.restype = C.c_int
         L.dsc_session_set_mixed_assembly.argtypes = [C.c_void_p, C.c_int]
         L.dsc_session_set_preconditioner.argtypes = [C.c_void_p, C.c_int]

@@ -167,6 +167,11 @@ class Session:
         or ASM_DF32 (double-FP32, within ~1e-13 of FP64)."""
         _native.check(self._L.dsc_session_set_mixed_assembly(self._h, int(prec)))
 
+    def set_field_tensor(self, on: bool):
+        """Mixed mode: the batched field's far pairs on the tensor cores
+        (default on) or on the FP32 pipes."""
+        _native.check(self._L.dsc_session_set_field_tensor(self._h, int(on)))
+
     def set_preconditioner(self, on: bool):
         """Mixed mode: the conductor-block right preconditioner (default on)."""
         _native.check(self._L.dsc_session_set_preconditioner(self._h, int(on)))

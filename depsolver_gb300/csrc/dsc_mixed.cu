@@ -23,6 +23,7 @@
 #include "dsc_common.cuh"
 #include "dsc_df32.cuh"
 #include "dsc_field.h"
+#include "dsc_field_tc.h"
 #include "dsc_internal.h"
 #include "dsc_session.h"
 #include "dsc_singular.cuh"
@@ -493,6 +494,7 @@ __global__ void k_update_solution(double *__restrict__ D, const float2 *__restri
 // ------------------------------------------------------- batched field
 constexpr int kBF = 32;   // frequencies per thread in the batched field
 constexpr int kBChunk = 32;
+constexpr int kFieldTcSplits = 16;  // at most this many q-ranges in the tensor-core far pass
 
 // Charge weights of Re(sigma_f) at every quadrature point, in FP32 for the
 // field pass, grouped by kBF systems with the systems innermost:
@@ -586,7 +588,8 @@ template <int NEN>
 __global__ void __launch_bounds__(128) k_field_batched_mixed(
     const float *__restrict__ phl, const int4 *__restrict__ coinc, int P, const int *__restrict__ en_pad,
     int E, int E7p, const float *__restrict__ ecent, const float *__restrict__ qoff,
-    const float *__restrict__ cT, const float2 *__restrict__ qdf, int F, float *__restrict__ part, int *err)
+    const float *__restrict__ cT, const float2 *__restrict__ qdf, int F, float *__restrict__ part, int *err,
+    int far_on)
 {
     __shared__ __align__(16) float s_c[kBChunk * kTriPts][kBF];
     __shared__ __align__(16) float s_cent[kBChunk * 8];
@@ -643,7 +646,10 @@ __global__ void __launch_bounds__(128) k_field_batched_mixed(
             const float d0x = (ph[0] - ce[0]) + (pl[0] - ce[3]);
             const float d0y = (ph[1] - ce[1]) + (pl[1] - ce[4]);
             const float d0z = (ph[2] - ce[2]) + (pl[2] - ce[5]);
-            const bool near = d0x * d0x + d0y * d0y + d0z * d0z < ce[6];
+            // rounded as the tensor-core far pass rounds it: the two passes
+            // split the pairs exactly
+            const bool near = __fmaf_rn(d0z, d0z, __fmaf_rn(d0y, d0y, __fmul_rn(d0x, d0x))) < ce[6];
+            if (!near && !far_on) continue;  // the far pairs go to the tensor cores
             if (near) {
                 // singular elements (the point is one of their nodes) lie
                 // within the near radius; the singular pass takes them
@@ -909,6 +915,7 @@ struct Session::Mixed {
     bool far_ready = false;
     DevBuf<float> ecent, qoff, phl, cf32;  // cf32: the charges, kBF systems innermost
     DevBuf<int> en_pad;                    // element nodes, padded to whole chunks (-1)
+    FieldTcWork ftc;                       // the tensor-core far pass
     DevBuf<float2> qdf;  // quadrature points in double-FP32 (near pairs)
 };
 
@@ -1247,7 +1254,7 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
     if (fp.P > 0) {
         const int E = s.E, P = fp.P;
         const int nchunk = (E + kBChunk * kBLoop - 1) / (kBChunk * kBLoop);  // element groups
-        DSC_TRY(w.part.alloc((size_t)nchunk * F * P * 3));
+        DSC_TRY(w.part.alloc((size_t)(nchunk + kFieldTcSplits) * F * P * 3));
         DSC_TRY(w.sing.alloc((size_t)F * P * 3));
         DSC_TRY(w.Enode.alloc((size_t)F * N * 3));
         DSC_TRY(w.Fce.alloc((size_t)F * std::max(fp.npel, 1) * 3));
@@ -1285,14 +1292,22 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
                                                                            P, w.phl.p));
                 w.far_ready = true;
             }
+            // far pairs on the tensor cores (partials after the FP32 pass's
+            // nchunk groups), the near ones on the FP32 pipes; or all on the
+            // FP32 pipes
+            int ntc = 0;
+            const bool tc = s.field_tc && F <= 64;
+            if (tc)
+                DSC_TRY(field_far_tc(w.phl.p, P, w.ecent.p, w.qoff.p, E, w.cf32.p, E7p, F, w.ftc,
+                                     w.part.p + (size_t)nchunk * F * P * 3, kFieldTcSplits, w.err.p, st, &ntc));
             if (s.nen == 6)
                 DSC_LAUNCH(k_field_batched_mixed<6><<<fg, 128, 0, st>>>(w.phl.p, fp.ps.coinc.p, P, w.en_pad.p, E,
                                                                         E7p, w.ecent.p, w.qoff.p, w.cf32.p,
-                                                                        w.qdf.p, F, w.part.p, w.err.p));
+                                                                        w.qdf.p, F, w.part.p, w.err.p, tc ? 0 : 1));
             else
                 DSC_LAUNCH(k_field_batched_mixed<3><<<fg, 128, 0, st>>>(w.phl.p, fp.ps.coinc.p, P, w.en_pad.p, E,
                                                                         E7p, w.ecent.p, w.qoff.p, w.cf32.p,
-                                                                        w.qdf.p, F, w.part.p, w.err.p));
+                                                                        w.qdf.p, F, w.part.p, w.err.p, tc ? 0 : 1));
             const int sb = (P * 32 + 127) / 128;
             if (s.nen == 6)
                 DSC_LAUNCH(k_field_singular_apply<6><<<sb, 128, 0, st>>>(P, s.dev.elems.p, s.dev.normals.p,
@@ -1305,7 +1320,7 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
             DSC_CUDA(cudaMemsetAsync(w.Enode.p, 0, (size_t)F * N * 3 * sizeof(double), st));
             const size_t nt = (size_t)F * P * 3;
             DSC_LAUNCH(k_field_batched_reduce<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(
-                w.part.p, nchunk, F, P, w.sing.p, fp.ids.p, N, w.Enode.p));
+                w.part.p, nchunk + ntc, F, P, w.sing.p, fp.ids.p, N, w.Enode.p));
         }
         TimerScope ts(tm, kTMst, st);
         if (fp.npel > 0) {

@@ -322,6 +322,12 @@ extern "C" int dsc_session_set_preconditioner(dsc_session *s, int on)
     return kOk;
 }
 
+extern "C" int dsc_session_set_field_tensor(dsc_session *s, int on)
+{
+    s->s.field_tc = on != 0;
+    return kOk;
+}
+
 extern "C" int dsc_session_set_mixed_assembly(dsc_session *s, int prec)
 {
     if (prec != DSC_ASM_FP32 && prec != DSC_ASM_DF32) {

@@ -70,6 +70,9 @@ struct Session {
     // by mixed solves)
     Precond *pre = nullptr;
     bool pre_on = true;
+    // mixed solves: the batched field's far pairs on the tensor cores (else
+    // all pairs on the FP32 pipes)
+    bool field_tc = true;
 
     int create(int nen, unsigned N, unsigned E, const double *nodes, const unsigned *elems,
                const unsigned *bctype, const double *mbc, unsigned nIf, const unsigned *ifaces,

@@ -30,6 +30,7 @@
 #include <cuda_fp16.h>
 
 #include "dsc_async.cuh"
+#include "dsc_tc.cuh"
 #include "dsc_df32.cuh"
 #include "dsc_internal.h"
 #include "dsc_tcgemm.h"
@@ -37,12 +38,9 @@
 namespace dsc {
 
 constexpr int kTcBM = 128;
-// A k-block is one swizzle row of kTcRowBytes bytes (128: 32 FP32 or 64
-// fp16 values).
-// Measured at the 12k-node scene: 128-byte rows in 3 stages 32.5 ms per
-// sweep's products, 64-byte rows in 6 stages 47.1 ms (twice the barrier
-// hand-offs per byte).
-constexpr int kTcRowBytes = 128;
+// k-blocks of kTcRowBytes (dsc_tc.cuh).  Measured at the 12k-node scene:
+// 128-byte rows in 3 stages 32.5 ms per sweep's products, 64-byte rows in
+// 6 stages 47.1 ms (twice the barrier hand-offs per byte).
 constexpr int kTcBK = kTcRowBytes / 4;    // fp32 elements per k-block
 constexpr int kTcBK16 = kTcRowBytes / 2;  // fp16 elements per k-block
 constexpr int kTcStages = 3;
@@ -59,106 +57,6 @@ constexpr long long kTcSpin = kSpin;  // clock cycles before a wait gives up
 // columns (3 stages of a 16 KB A tile and a 48 KB B tile)
 constexpr int kTcDigitKBlocks = 64;
 constexpr int kTcMaxDigitCols = 384;
-
-__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar, int x,
-                                            int y)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
-        " [%0], [%1, {%3, %4}], [%2];" ::"r"(su32(dst)),
-        "l"((uint64_t)map), "r"(su32(bar)), "r"(x), "r"(y)
-        : "memory");
-}
-
-// Shared-memory matrix descriptor of a K-major tile in the swizzled
-// canonical layout: rows of kTcRowBytes bytes (the swizzle width), 8-row
-// groups 8 rows apart.
-__device__ __forceinline__ uint64_t sw_desc(const void *tile)
-{
-    const uint64_t a = su32(tile);
-    uint64_t d = (a >> 4) & 0x3FFFull;                    // start address
-    d |= (uint64_t)1 << 16;                               // leading byte offset (unused when swizzled)
-    d |= (uint64_t)((8 * kTcRowBytes) >> 4) << 32;        // stride byte offset: 8 rows
-    d |= (uint64_t)1 << 46;                               // descriptor version
-    d |= (uint64_t)(kTcRowBytes == 128 ? 2 : 4) << 61;    // 128- or 64-byte swizzle
-    return d;
-}
-
-// Instruction descriptor: D f32, A and B tf32, both K-major, N x M shape.
-__host__ __device__ constexpr uint32_t idesc_tf32(int n, int m)
-{
-    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) |
-           ((uint32_t)(m >> 4) << 24);
-}
-
-// The same for kind::f16 with A and B both fp16 (type code 0).
-__host__ __device__ constexpr uint32_t idesc_f16(int n, int m)
-{
-    return (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(n >> 3) << 17) |
-           ((uint32_t)(m >> 4) << 24);
-}
-
-__device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc,
-                                         uint32_t acc)
-{
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
-        "l"(a), "l"(b), "r"(idesc), "r"(acc)
-        : "memory");
-}
-
-__device__ __forceinline__ void mma_f16(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc,
-                                        uint32_t acc)
-{
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
-        "l"(a), "l"(b), "r"(idesc), "r"(acc)
-        : "memory");
-}
-
-template <bool F16>
-__device__ __forceinline__ void mma_op(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
-{
-    if (F16) mma_f16(d, a, b, idesc, acc);
-    else mma_tf32(d, a, b, idesc, acc);
-}
-
-__device__ __forceinline__ void mma_commit(uint64_t *bar)
-{
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                     su32(bar))
-                 : "memory");
-}
-
-__device__ __forceinline__ void tc_fence_before()
-{
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-}
-
-__device__ __forceinline__ void tc_fence_after()
-{
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-}
-
-// 32 consecutive accumulator columns of this warp's 32 TMEM lanes.
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t *r)
-{
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
-        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-          "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
-          "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
-          "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-}
 
 // The tf32 value the tensor core reads from an FP32 word: the top 19 bits
 // (the low 13 mantissa bits are ignored).
@@ -572,6 +470,11 @@ static int make_map(CUtensorMap *map, const void *base, int esize, int rows, int
         return kErrCuda;
     }
     return kOk;
+}
+
+int tc_make_map(CUtensorMap *map, const void *base, int esize, int rows, int k, size_t ld, int box_rows)
+{
+    return make_map(map, base, esize, rows, k, ld, box_rows);
 }
 
 // Split counts: at least one k-block per split, normalised so that every

@@ -1,6 +1,7 @@
 // dsc_tcgemm.h -- tensor-core GEMM of libdepsolver_cuda (not exported).
 #pragma once
 
+#include <cuda.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stddef.h>
@@ -56,6 +57,10 @@ int tc_gemm_f16_splits_for(int M, int Kd);
 int tc_gemm_digits(const __half *A, size_t lda, const __half *B, size_t ldb, int M, int Nc, int Kd, float *Y,
                    size_t ldy, int *d_err, cudaStream_t st);
 int tc_digit_splits(int Kd);
+// Tensor map of a row-major matrix of FP32 (esize 4) or fp16 (esize 2)
+// values, rows x k (k contiguous, row stride ld elements, 16-byte aligned),
+// boxes of one 128-byte swizzle row of k by box_rows rows, zero fill.
+int tc_make_map(CUtensorMap *map, const void *base, int esize, int rows, int k, size_t ld, int box_rows);
 // The Gauss-Jordan update of step k on the same kernel (3xFP16, K = 128):
 // for every 128 x 128 tile (I, J) of C (column-major, M x Nc, stride ldc)
 // with I != k: C_IJ -= A_I B_J^T (C_Ik = -A_I B_k^T); A (M x 128) and B

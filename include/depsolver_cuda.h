@@ -199,6 +199,12 @@ int dsc_session_assemble(dsc_session *s, int mode);
 #define DSC_ASM_FP32 2
 #define DSC_ASM_DF32 1
 int dsc_session_set_mixed_assembly(dsc_session *s, int prec);
+/* Mixed mode's batched field at the force points: on (default) takes the
+ * far element-point pairs on the tensor cores (the kernel 1/r^2 generated
+ * into shared memory as fp16 pairs, 3xFP16 products read back into FP32
+ * every 64 quadrature points) and the near ones on the FP32 pipes; off
+ * takes all of them on the FP32 pipes. */
+int dsc_session_set_field_tensor(dsc_session *s, int on);
 /* The geometric matrix K (N x N) as assembled for `mode` (assembling it if
  * needed): K[c * ldk + i] = entry (row i, node c), i.e. C * int G N_c for
  * conductor rows and int H N_c for interface rows (src/assembly_el.c). */

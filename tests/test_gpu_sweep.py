@@ -148,3 +148,23 @@ def test_conductor_preconditioner_cuts_iterations_not_accuracy(gpu):
     assert it_on.max() * 2 <= it_off.min(), (it_on, it_off)
     t = s.timing()
     assert set(["precond_build", "precond_apply"]) <= set(t)
+
+
+def test_field_tensor_cores_match_fp32_pipes(gpu):
+    """The batched field's far pairs on the tensor cores (3xFP16 products of
+    the generated kernel, read back into FP32 every 64 quadrature points)
+    give the forces of the all-FP32-pipe pass to far below the metric's
+    bound, and both stay within it against the FP64 path."""
+    sc = scenes.small(nen=6, sphere_level=2, plate_cells=6)
+    freqs = np.logspace(3, 8, 8)
+    s = api.Session(sc)
+    f_tc, _, s_tc = s.solve(freqs, mode=api.MODE_MIXED, tol=1e-11, want_sigma=True)
+    s.set_field_tensor(False)
+    f_32, _, s_32 = s.solve(freqs, mode=api.MODE_MIXED, tol=1e-11, want_sigma=True)
+    f64, _, _ = s.solve(freqs, mode=api.MODE_FP64, tol=1e-12, want_sigma=True)
+    assert np.array_equal(s_tc, s_32)  # the field does not feed back into the solve
+    for k in range(len(freqs)):
+        scale = f64[k, 6:9].sum()
+        assert np.abs(f_tc[k, :3] - f_32[k, :3]).max() <= 1e-7 * scale, k
+        assert np.allclose(f_tc[k, 6:9], f_32[k, 6:9], rtol=1e-5), k
+        assert np.abs(f_tc[k, :3] - f64[k, :3]).max() <= FORCE_TOL * scale, k
