@@ -15,14 +15,17 @@
 //     centroid, which includes the singular elements) and padding get 0 --
 //     the FP32 pass takes them;
 //   * warp 0 streams the charges' fp16 pairs (64 systems x 64 q per
-//     k-block, scaled per system) with TMA;
+//     k-block, scaled per system) with TMA into one buffer (the products of
+//     a k-block finish long before the next one is generated), and each
+//     k-block's geometry (8 centroids, 64 point offsets: 1280 contiguous
+//     bytes) with bulk copies into two buffers, one k-block ahead;
 //   * warp 1 issues tcgen05.mma kind::f16, hi*hi + hi*lo + lo*hi per
 //     component, into one of two TMEM buffers (3 x 64 columns);
 //   * warps 2-9, after generating the next k-block, read the finished
 //     buffer back and add it into FP32 registers (round to nearest): the
 //     tensor core's truncating FP32 accumulation never spans more than one
 //     k-block of 64 terms.
-// Two stages of 112 KB; every mbarrier wait is bounded (codes 21-25).
+// Two stages of 96 KB for G; every mbarrier wait is bounded (codes 21-26).
 #include <cuda.h>
 #include <cuda_fp16.h>
 
@@ -44,10 +47,11 @@ constexpr int kFtGen = 8;                     // generator / reader warps
 constexpr int kFtThreads = 32 * (2 + kFtGen);
 constexpr uint32_t kFtATile = kFtM * kTcRowBytes;   // one (component, half) of G: 16 KB
 constexpr uint32_t kFtBTile = kFtN * kTcRowBytes;   // one half of the charges: 8 KB
-constexpr uint32_t kFtStage = 6 * kFtATile + 2 * kFtBTile;
+constexpr uint32_t kFtStage = 6 * kFtATile;   // the generated G of one k-block
 constexpr int kFtStages = 2;
+constexpr uint32_t kFtGeo = 8 * 32 + kFtK * 16;  // one k-block's centroids and point offsets
 constexpr uint32_t kFtAcc = 256;              // TMEM columns per accumulator buffer (192 used)
-constexpr size_t kFtSmem = 1024 + (size_t)kFtStages * kFtStage + 256;
+constexpr size_t kFtSmem = 1024 + (size_t)kFtStages * kFtStage + 2 * kFtBTile + kFtStages * kFtGeo + 256;
 
 struct FieldTcArgs {
     const float *phl;    // P x 6: point hi (3), lo (3)
@@ -72,10 +76,14 @@ __global__ void __launch_bounds__(kFtThreads, 1)
 {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint64_t *a_full = (uint64_t *)(smem + kFtStages * kFtStage);
-    uint64_t *b_full = a_full + kFtStages;
-    uint64_t *st_free = b_full + kFtStages;
-    uint64_t *acc_full = st_free + kFtStages;
+    uint8_t *btile = smem + kFtStages * kFtStage;        // charges (hi, lo), one buffer
+    uint8_t *geo = btile + 2 * kFtBTile;                 // kFtStages x kFtGeo
+    uint64_t *a_full = (uint64_t *)(geo + kFtStages * kFtGeo);
+    uint64_t *geo_full = a_full + kFtStages;
+    uint64_t *st_free = geo_full + kFtStages;
+    uint64_t *b_full = st_free + kFtStages;              // [1]
+    uint64_t *b_free = b_full + 1;                       // [1]
+    uint64_t *acc_full = b_free + 1;
     uint64_t *acc_empty = acc_full + 2;
     uint64_t *done = acc_empty + 2;
     uint32_t *tmem_slot = (uint32_t *)(done + 1);
@@ -85,9 +93,11 @@ __global__ void __launch_bounds__(kFtThreads, 1)
     if (threadIdx.x == 0) {
         for (int s = 0; s < kFtStages; s++) {
             mbar_init(&a_full[s], 32 * kFtGen);
-            mbar_init(&b_full[s], 1);
+            mbar_init(&geo_full[s], 1);
             mbar_init(&st_free[s], 1);
         }
+        mbar_init(b_full, 1);
+        mbar_init(b_free, 1);
         for (int b = 0; b < 2; b++) {
             mbar_init(&acc_full[b], 1);
             mbar_init(&acc_empty[b], kFtGen);
@@ -109,7 +119,7 @@ __global__ void __launch_bounds__(kFtThreads, 1)
     // split u / tiles) and their k-blocks; g counts k-blocks over the units
     if (warp == 0) {
         if (lane == 0) {
-            // ---- charges: TMA producer
+            // ---- geometry (bulk copies) and charges (TMA)
             uint32_t g = 0;
             bool ok = true;
             for (int u = blockIdx.x; ok && u < units; u += gridDim.x) {
@@ -120,15 +130,28 @@ __global__ void __launch_bounds__(kFtThreads, 1)
                         ok = false;
                         break;
                     }
-                    uint8_t *b = smem + s * kFtStage + 6 * kFtATile;
-                    mbar_expect_tx(&b_full[s], 2 * kFtBTile);
-                    tma_load_2d(b, &tmBh, &b_full[s], kb * kFtK, 0);
-                    tma_load_2d(b + kFtBTile, &tmBl, &b_full[s], kb * kFtK, 0);
+                    uint8_t *gs_ = geo + s * kFtGeo;
+                    mbar_expect_tx(&geo_full[s], kFtGeo);
+                    bulk_g2s(gs_, a.ecent + (size_t)kb * 8 * 8, 8 * 32, &geo_full[s]);
+                    bulk_g2s(gs_ + 8 * 32, a.q8 + (size_t)kb * kFtK, kFtK * 16, &geo_full[s]);
+                    if (g > 0 && !mbar_wait(b_free, (g - 1) & 1, a.err, 26)) {
+                        ok = false;
+                        break;
+                    }
+                    mbar_expect_tx(b_full, 2 * kFtBTile);
+                    tma_load_2d(btile, &tmBh, b_full, kb * kFtK, 0);
+                    tma_load_2d(btile + kFtBTile, &tmBl, b_full, kb * kFtK, 0);
+                }
+            }
+            // drain: the last copies have landed before the CTA may exit
+            if (g > 0) {
+                const long long t0 = clock64();
+                while (!mbar_try(b_full, (g - 1) & 1) && clock64() - t0 < kSpin) {
                 }
             }
             for (uint32_t h = g > (uint32_t)kFtStages ? g - kFtStages : 0; h < g; h++) {
                 const long long t0 = clock64();
-                while (!mbar_try(&b_full[h % kFtStages], (h / kFtStages) & 1) && clock64() - t0 < kSpin) {
+                while (!mbar_try(&geo_full[h % kFtStages], (h / kFtStages) & 1) && clock64() - t0 < kSpin) {
                 }
             }
         }
@@ -143,14 +166,14 @@ __global__ void __launch_bounds__(kFtThreads, 1)
                 for (int kb = kb0; kb < kb1; kb++, g++) {
                     const uint32_t s = g % kFtStages, n = g / kFtStages;
                     const uint32_t buf = g & 1, q = g >> 1;
-                    if (!mbar_wait(&a_full[s], n & 1, a.err, 22) || !mbar_wait(&b_full[s], n & 1, a.err, 22) ||
+                    if (!mbar_wait(&a_full[s], n & 1, a.err, 22) || !mbar_wait(b_full, g & 1, a.err, 22) ||
                         (q > 0 && !mbar_wait(&acc_empty[buf], (q - 1) & 1, a.err, 23))) {
                         ok = false;
                         break;
                     }
                     tc_fence_after();
                     uint8_t *st = smem + s * kFtStage;
-                    const uint64_t dbh = sw_desc(st + 6 * kFtATile), dbl = sw_desc(st + 6 * kFtATile + kFtBTile);
+                    const uint64_t dbh = sw_desc(btile), dbl = sw_desc(btile + kFtBTile);
 #pragma unroll
                     for (int c = 0; c < 3; c++) {
                         const uint32_t acc = tmem + buf * kFtAcc + (uint32_t)(c * kFtN);
@@ -165,6 +188,7 @@ __global__ void __launch_bounds__(kFtThreads, 1)
                         }
                     }
                     mma_commit(&st_free[s]);
+                    mma_commit(b_free);
                     mma_commit(&acc_full[buf]);
                 }
             }
@@ -208,17 +232,20 @@ __global__ void __launch_bounds__(kFtThreads, 1)
             const float pl[3] = {a.phl[(size_t)p * 6 + 3], a.phl[(size_t)p * 6 + 4], a.phl[(size_t)p * 6 + 5]};
             for (int kb = kb0; kb < kb1; kb++, g++) {
                 const uint32_t s = g % kFtStages, n = g / kFtStages;
-                if (n > 0 && !mbar_wait(&st_free[s], (n - 1) & 1, a.err, 25)) {
+                if ((n > 0 && !mbar_wait(&st_free[s], (n - 1) & 1, a.err, 25)) ||
+                    !mbar_wait(&geo_full[s], n & 1, a.err, 25)) {
                     ok = false;
                     break;
                 }
                 uint8_t *st = smem + s * kFtStage;
+                const float *gce = (const float *)(geo + s * kFtGeo);           // [8][8]
+                const float4 *gq8 = (const float4 *)(geo + s * kFtGeo + 8 * 32);  // [64]
                 // the thread's four elements: one 16-byte chunk each of row r
 #pragma unroll 1
                 for (int j = 0; j < 4; j++) {
-                    const int e = kb * 8 + 4 * h + j;
-                    const float4 c0 = __ldg((const float4 *)(a.ecent + (size_t)e * 8));
-                    const float4 c1 = __ldg((const float4 *)(a.ecent + (size_t)e * 8) + 1);
+                    const int el = 4 * h + j, e = kb * 8 + el;
+                    const float4 c0 = ((const float4 *)(gce + el * 8))[0];
+                    const float4 c1 = ((const float4 *)(gce + el * 8))[1];
                     const float d0x = (ph[0] - c0.x) + (pl[0] - c0.w);
                     const float d0y = (ph[1] - c0.y) + (pl[1] - c1.x);
                     const float d0z = (ph[2] - c0.z) + (pl[2] - c1.y);
@@ -230,32 +257,33 @@ __global__ void __launch_bounds__(kFtThreads, 1)
                     if (far) {
                         float4 o[kTriPts];
 #pragma unroll
-                        for (int k = 0; k < kTriPts; k++) o[k] = __ldg(a.q8 + (size_t)e * 8 + k);
+                        for (int k = 0; k < kTriPts; k++) o[k] = gq8[el * 8 + k];
+                        const float2 dx0 = make_float2(d0x, d0x), dy0 = make_float2(d0y, d0y),
+                                     dz0 = make_float2(d0z, d0z);
+                        const float2 g2 = make_float2(gs, gs), half2c = make_float2(-0.5f, -0.5f),
+                                     th2 = make_float2(1.5f, 1.5f);
+                        // two quadrature points (k, k + 1) per step in packed FP32x2
 #pragma unroll
                         for (int k = 0; k < 8; k += 2) {
-                            float gv[2][3];
-#pragma unroll
-                            for (int kk = 0; kk < 2; kk++) {
-                                if (k + kk < kTriPts) {
-                                    const float dx = d0x - o[k + kk].x, dy = d0y - o[k + kk].y, dz = d0z - o[k + kk].z;
-                                    const float r2 = dx * dx + dy * dy + dz * dz;
-                                    float inv = rsqrtf(r2);
-                                    inv = inv * (1.5f - 0.5f * r2 * inv * inv);
-                                    const float i3 = inv * inv * inv * gs;
-                                    gv[kk][0] = dx * i3;
-                                    gv[kk][1] = dy * i3;
-                                    gv[kk][2] = dz * i3;
-                                } else {
-                                    gv[kk][0] = gv[kk][1] = gv[kk][2] = 0.0f;
-                                }
-                            }
+                            const float4 ob = k + 1 < kTriPts ? o[k + 1] : o[k];  // slot 7: zeroed below
+                            const float2 dx = __fadd2_rn(dx0, make_float2(-o[k].x, -ob.x));
+                            const float2 dy = __fadd2_rn(dy0, make_float2(-o[k].y, -ob.y));
+                            const float2 dz = __fadd2_rn(dz0, make_float2(-o[k].z, -ob.z));
+                            const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+                            float2 inv = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+                            // one Newton step: inv (1.5 - 0.5 r2 inv^2)
+                            inv = __fmul2_rn(inv, __ffma2_rn(half2c, __fmul2_rn(__fmul2_rn(r2, inv), inv), th2));
+                            float2 i3 = __fmul2_rn(__fmul2_rn(__fmul2_rn(inv, inv), inv), g2);
+                            if (k + 1 >= kTriPts) i3.y = 0.0f;
+                            const float2 gv[3] = {__fmul2_rn(dx, i3), __fmul2_rn(dy, i3), __fmul2_rn(dz, i3)};
 #pragma unroll
                             for (int c = 0; c < 3; c++) {
-                                const __half h0 = __float2half_rn(gv[0][c]), h1 = __float2half_rn(gv[1][c]);
-                                const __half l0 = __float2half_rn(gv[0][c] - __half2float(h0));
-                                const __half l1 = __float2half_rn(gv[1][c] - __half2float(h1));
-                                w[2 * c][k / 2] = pack_half2(h0, h1);
-                                w[2 * c + 1][k / 2] = pack_half2(l0, l1);
+                                const __half2 hi = __floats2half2_rn(gv[c].x, gv[c].y);
+                                const float2 hb = __half22float2(hi);
+                                const float2 rem = __fadd2_rn(gv[c], make_float2(-hb.x, -hb.y));
+                                const __half2 lo = __floats2half2_rn(rem.x, rem.y);
+                                w[2 * c][k / 2] = *(const uint32_t *)&hi;
+                                w[2 * c + 1][k / 2] = *(const uint32_t *)&lo;
                             }
                         }
                     } else {
