@@ -668,7 +668,9 @@ static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStr
         }
         DSC_CUDA(cudaGetLastError());
         if (m.n_fix > 0) {
-            dim3 fg((hi - lo + 255) / 256, std::min(m.n_fix, 65535));
+            // each block walks many shared columns (a block per column would
+            // be hundreds of thousands of tiny blocks)
+            dim3 fg((hi - lo + 255) / 256, std::min(m.n_fix, 256));
             TimerScope ts(tm, kTAsmFixup, st);
             if (f32)
                 DSC_LAUNCH(k_asm_fixup_f32<<<fg, 256, 0, st>>>(m.fix_ptr.p, m.fix_slot.p, m.fix_col.p, m.n_fix,

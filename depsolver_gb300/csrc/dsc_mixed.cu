@@ -583,13 +583,14 @@ __global__ void k_points_split(const double *__restrict__ px, const double *__re
 // slices of arrays padded to whole chunks) arrives in shared memory by bulk
 // copies on one mbarrier; a wait that gives up sets *err (code 8) and ends
 // the block.
-constexpr int kBLoop = 8;   // element chunks per block
+constexpr int kBLoop = 8;   // element chunks per block (all pairs)
+constexpr int kBLoopNear = 32;  // the same with the far pairs on the tensor cores: fewer partials
 template <int NEN>
 __global__ void __launch_bounds__(128) k_field_batched_mixed(
     const float *__restrict__ phl, const int4 *__restrict__ coinc, int P, const int *__restrict__ en_pad,
     int E, int E7p, const float *__restrict__ ecent, const float *__restrict__ qoff,
     const float *__restrict__ cT, const float2 *__restrict__ qdf, int F, float *__restrict__ part, int *err,
-    int far_on)
+    int far_on, int nloop)
 {
     __shared__ __align__(16) float s_c[kBChunk * kTriPts][kBF];
     __shared__ __align__(16) float s_cent[kBChunk * 8];
@@ -621,8 +622,8 @@ __global__ void __launch_bounds__(128) k_field_batched_mixed(
 #pragma unroll
     for (int j = 0; j < kBF / 2; j++) acc[j][0] = acc[j][1] = acc[j][2] = make_float2(0.0f, 0.0f);
     uint32_t phase = 0;
-    for (int cl = 0; cl < kBLoop; cl++) {
-        const int e0 = (group * kBLoop + cl) * kBChunk;
+    for (int cl = 0; cl < nloop; cl++) {
+        const int e0 = (group * nloop + cl) * kBChunk;
         if (e0 >= E) break;  // uniform over the block
         const int ne = min(kBChunk, E - e0);
         __syncthreads();  // the previous chunk is no longer read (and the barrier is initialised)
@@ -1253,7 +1254,9 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
     ForcePlan &fp = s.force;
     if (fp.P > 0) {
         const int E = s.E, P = fp.P;
-        const int nchunk = (E + kBChunk * kBLoop - 1) / (kBChunk * kBLoop);  // element groups
+        const bool tc = s.field_tc && F <= 64;  // far pairs on the tensor cores
+        const int nloop = tc ? kBLoopNear : kBLoop;
+        const int nchunk = (E + kBChunk * nloop - 1) / (kBChunk * nloop);  // element groups
         DSC_TRY(w.part.alloc((size_t)(nchunk + kFieldTcSplits) * F * P * 3));
         DSC_TRY(w.sing.alloc((size_t)F * P * 3));
         DSC_TRY(w.Enode.alloc((size_t)F * N * 3));
@@ -1296,18 +1299,19 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
             // nchunk groups), the near ones on the FP32 pipes; or all on the
             // FP32 pipes
             int ntc = 0;
-            const bool tc = s.field_tc && F <= 64;
             if (tc)
                 DSC_TRY(field_far_tc(w.phl.p, P, w.ecent.p, w.qoff.p, E, w.cf32.p, E7p, F, w.ftc,
                                      w.part.p + (size_t)nchunk * F * P * 3, kFieldTcSplits, w.err.p, st, &ntc));
             if (s.nen == 6)
                 DSC_LAUNCH(k_field_batched_mixed<6><<<fg, 128, 0, st>>>(w.phl.p, fp.ps.coinc.p, P, w.en_pad.p, E,
                                                                         E7p, w.ecent.p, w.qoff.p, w.cf32.p,
-                                                                        w.qdf.p, F, w.part.p, w.err.p, tc ? 0 : 1));
+                                                                        w.qdf.p, F, w.part.p, w.err.p, tc ? 0 : 1,
+                                                                        nloop));
             else
                 DSC_LAUNCH(k_field_batched_mixed<3><<<fg, 128, 0, st>>>(w.phl.p, fp.ps.coinc.p, P, w.en_pad.p, E,
                                                                         E7p, w.ecent.p, w.qoff.p, w.cf32.p,
-                                                                        w.qdf.p, F, w.part.p, w.err.p, tc ? 0 : 1));
+                                                                        w.qdf.p, F, w.part.p, w.err.p, tc ? 0 : 1,
+                                                                        nloop));
             const int sb = (P * 32 + 127) / 128;
             if (s.nen == 6)
                 DSC_LAUNCH(k_field_singular_apply<6><<<sb, 128, 0, st>>>(P, s.dev.elems.p, s.dev.normals.p,
