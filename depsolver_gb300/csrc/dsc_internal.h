@@ -153,6 +153,42 @@ struct Timer {
     ~Timer();
 };
 
+// Work on a second stream between fork() and done(), joined back into the
+// main stream by join() -- or by the destructor, on every early return, so
+// that nothing queued on the main stream later (a free of a buffer the side
+// work uses) overtakes it.
+struct SideJoin {
+    cudaStream_t main = nullptr;
+    cudaEvent_t ev = nullptr;
+    int fork(cudaStream_t m, cudaStream_t side)
+    {
+        main = m;
+        cudaEvent_t e0;
+        DSC_CUDA(cudaEventCreateWithFlags(&e0, cudaEventDisableTiming));
+        cudaError_t r = cudaEventRecord(e0, m);
+        if (r == cudaSuccess) r = cudaStreamWaitEvent(side, e0, 0);
+        cudaEventDestroy(e0);
+        DSC_CUDA(r);
+        return kOk;
+    }
+    int done(cudaStream_t side)
+    {
+        DSC_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        DSC_CUDA(cudaEventRecord(ev, side));
+        return kOk;
+    }
+    int join()
+    {
+        if (!ev) return kOk;
+        const cudaError_t r = cudaStreamWaitEvent(main, ev, 0);
+        cudaEventDestroy(ev);
+        ev = nullptr;
+        DSC_CUDA(r);
+        return kOk;
+    }
+    ~SideJoin() { join(); }
+};
+
 struct TimerScope {
     Timer *t;
     cudaStream_t st;

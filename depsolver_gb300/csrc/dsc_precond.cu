@@ -390,7 +390,6 @@ int precond_build(Session &s)
     for (int b0 = 0; b0 < pc.nb; b0 += kPreMaxBlocks) {
         const int nb = std::min(kPreMaxBlocks, pc.nb - b0);
         GJArgs ga{};
-        int nbk_max = 0;
         for (int q = 0; q < nb; q++) {
             const int b = b0 + q;
             ga.X[q] = pc.X.p + pc.xoff[b];
@@ -403,17 +402,48 @@ int precond_build(Session &s)
             ga.rb[q] = pc.grb.p + pc.toff[b] / kPB;
             ga.ldx[q] = pc.ldx[b];
             ga.nbk[q] = pc.nbk[b];
-            nbk_max = std::max(nbk_max, pc.nbk[b]);
         }
         std::vector<TcGjPlan> plans(nb);
         for (int q = 0; q < nb; q++)
             DSC_TRY(tc_gj_plan(plans[q], ga.Ah[q], ga.Al[q], kPB, ga.Bh[q], ga.Bl[q], kPB, ga.ldx[q], ga.ldx[q],
                                ga.X[q], (size_t)ga.ldx[q], pc.err.p, ga.ra[q], ga.rb[q]));
-        for (int k = 0; k < nbk_max; k++) {
-            DSC_LAUNCH(k_gj_pivot<<<nb, 256, 0, st>>>(ga, nb, k));
-            DSC_LAUNCH(k_gj_row<<<dim3(nbk_max, 2, nb), 256, rsmem, st>>>(ga, nb, k));
-            for (int q = 0; q < nb; q++)
-                if (k < ga.nbk[q]) DSC_TRY(tc_gj_run(plans[q], k, st));
+        // two interleaved Gauss-Jordan sequences when there are two or more
+        // blocks: even blocks on st, odd ones on the side stream, so that one
+        // sequence's pivot inversion (one CTA) runs beside the other's
+        // tensor-core update
+        const int nseq = (nb >= 2 && s.side) ? 2 : 1;
+        GJArgs gsub[2] = {};
+        int nsub[2] = {0, 0}, nbk_sub[2] = {0, 0};
+        std::vector<int> which[2];
+        for (int q = 0; q < nb; q++) {
+            const int t = q % nseq, i = nsub[t]++;
+            gsub[t].X[i] = ga.X[q];
+            gsub[t].tP[i] = ga.tP[q];
+            gsub[t].Ah[i] = ga.Ah[q];
+            gsub[t].Al[i] = ga.Al[q];
+            gsub[t].Bh[i] = ga.Bh[q];
+            gsub[t].Bl[i] = ga.Bl[q];
+            gsub[t].ra[i] = ga.ra[q];
+            gsub[t].rb[i] = ga.rb[q];
+            gsub[t].ldx[i] = ga.ldx[q];
+            gsub[t].nbk[i] = ga.nbk[q];
+            nbk_sub[t] = std::max(nbk_sub[t], ga.nbk[q]);
+            which[t].push_back(q);
+        }
+        SideJoin sj;
+        if (nseq == 2) DSC_TRY(sj.fork(st, s.side));
+        for (int t = 0; t < nseq; t++) {
+            cudaStream_t ss = t ? s.side : st;
+            for (int k = 0; k < nbk_sub[t]; k++) {
+                DSC_LAUNCH(k_gj_pivot<<<nsub[t], 256, 0, ss>>>(gsub[t], nsub[t], k));
+                DSC_LAUNCH(k_gj_row<<<dim3(nbk_sub[t], 2, nsub[t]), 256, rsmem, ss>>>(gsub[t], nsub[t], k));
+                for (int q : which[t])
+                    if (k < ga.nbk[q]) DSC_TRY(tc_gj_run(plans[q], k, ss));
+            }
+        }
+        if (nseq == 2) {
+            DSC_TRY(sj.done(s.side));
+            DSC_TRY(sj.join());
         }
     }
     // the inverses as row-scaled fp16 pairs for the products (X is

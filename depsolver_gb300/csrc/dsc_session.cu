@@ -128,6 +128,7 @@ int Session::create(int nen_, unsigned N_, unsigned E_, const double *nodes, con
     E = (int)E_;
     nIf = nIf_;
     DSC_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    DSC_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
     AllocStreamScope as(st);
     std::vector<int> e0((size_t)E * nen);
     for (size_t t = 0; t < e0.size(); t++) e0[t] = (int)elems[t] - 1;

@@ -31,6 +31,10 @@ struct Session {
     unsigned nIf = 0;
     cudaStream_t st = nullptr;
     StreamGuard st_guard{&st};  // declared before every device buffer
+    // a second stream for independent work beside st (the conductor blocks'
+    // Gauss-Jordan sequences), joined back by events
+    cudaStream_t side = nullptr;
+    StreamGuard side_guard{&side};
     HostPlan plan;
     DeviceMesh dev;
     ForcePlan force;
