@@ -347,9 +347,14 @@ def run_ours(args, rank, world):
     total_ms = sum(v[0] for v in timing.values())
     value = replica_throughput(ms, world, args.steps)
 
+    s.close()  # its device memory goes back to the pool the sweeps draw from
+
     # e2e through the C ABI from host arrays: dsc_sweep (session created,
-    # mesh uploaded, assembled, solved, nodal solution and forces read back)
+    # mesh uploaded, assembled, solved, nodal solution and forces read back);
+    # one untimed call first, which grows the device memory pool to a
+    # sweep's size (later calls reuse those blocks)
     e2e_steps = max(1, min(args.steps, 3))
+    api.sweep(sc, FREQS, mode=api.MODE_MIXED, tol=TOL, want_sigma=True)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
@@ -379,7 +384,7 @@ def run_ours(args, rank, world):
                    "l2": "inputs larger than L2 (K 2.5 GB FP64 + 1.25 GB FP32)",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": NFREQ / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h)},
+                "d2h_bytes_per_step": int(d2h), "calls_timed": e2e_steps, "untimed_calls_before": 1},
         "roofline": roof,
         "cpu_baseline": cpu,
         "fp64_path": {"value": 1.0 / fp64_s, "unit": UNIT, "ms_per_solve": fp64_s * 1e3,

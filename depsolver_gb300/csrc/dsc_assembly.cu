@@ -329,8 +329,14 @@ __global__ void __launch_bounds__(128) k_asm_regular_df32(AsmArgs a, const float
 // from the origin; about 1e-7 of each entry.  The centroid-relative form is
 // also what makes near pairs safe (no cancellation of large coordinates).
 
-// Per element: centroid (double-FP32 x, y, z) and per point (offset x, y,
-// z, w_q J_q) in FP32.
+// Per element: centroid (double-FP32 x, y, z) and the points' offsets from
+// it, negated, with w_q J_q, in FP32, as four point pairs (q = 2p, 2p + 1)
+// of two float4 each: {-x_q, -x_q+1, -y_q, -y_q+1}, {-z_q, -z_q+1, w_q,
+// w_q+1}.  The eighth point is a pad of weight 0 far away (1e18: its 1 / r
+// and 1 / r^3 stay finite or zero whatever the row point).
+constexpr int kQpPairs = (kTriPts + 1) / 2;
+constexpr float kQpPad = 1e18f;
+
 __global__ void k_qp_local(const double *__restrict__ qp, int E, float2 *__restrict__ cen,
                            float4 *__restrict__ qloc)
 {
@@ -348,10 +354,21 @@ __global__ void k_qp_local(const double *__restrict__ qp, int E, float2 *__restr
         cen[(size_t)e * 3 + d] = cd;
         c[d] = (double)cd.x + (double)cd.y;  // the centroid as the kernel sees it
     }
+    float o[2 * kQpPairs][4];
 #pragma unroll
-    for (int t = 0; t < kTriPts; t++)
-        qloc[(size_t)e * kTriPts + t] = make_float4((float)(q[4 * t] - c[0]), (float)(q[4 * t + 1] - c[1]),
-                                                    (float)(q[4 * t + 2] - c[2]), (float)q[4 * t + 3]);
+    for (int t = 0; t < 2 * kQpPairs; t++) {
+        const bool pt = t < kTriPts;
+        o[t][0] = pt ? (float)(c[0] - q[4 * t]) : -kQpPad;
+        o[t][1] = pt ? (float)(c[1] - q[4 * t + 1]) : 0.f;
+        o[t][2] = pt ? (float)(c[2] - q[4 * t + 2]) : 0.f;
+        o[t][3] = pt ? (float)q[4 * t + 3] : 0.f;
+    }
+#pragma unroll
+    for (int p = 0; p < kQpPairs; p++) {
+        const float *a = o[2 * p], *b = o[2 * p + 1];
+        qloc[((size_t)e * kQpPairs + p) * 2] = make_float4(a[0], b[0], a[1], b[1]);
+        qloc[((size_t)e * kQpPairs + p) * 2 + 1] = make_float4(a[2], b[2], a[3], b[3]);
+    }
 }
 
 // FP32 to FP64 by integer operations (a register move, no FP64-pipe work):
@@ -372,26 +389,42 @@ __device__ __forceinline__ float shape_q_f(int q, int k)
     return NEN == 3 ? c_shape3_df.hi[q][k] : c_shape6_df.hi[q][k];
 }
 
+// The points in pairs on the packed FP32x2 pipe: per pair 15 instructions
+// (3 FADD2, 1 FMUL2 + 2 FFMA2 for r^2, 2 MUFU, 1 FMUL2, NEN FFMA2) where
+// two single points take 28; each shape function's two partial sums are
+// added at the end.  S holds the shape values in point pairs.
 template <int NEN, int MODE>
-__device__ __forceinline__ void pair_regular_f32(const float4 *__restrict__ q7, float dx0, float dy0, float dz0,
-                                                 float nx, float ny, float nz, bool isH, float *acc)
+__device__ __forceinline__ void pair_regular_f32(const float4 *__restrict__ q8, float dx0, float dy0, float dz0,
+                                                 float nx, float ny, float nz, bool isH,
+                                                 const float2 (&S)[kQpPairs][NEN], float *acc)
 {
+    const float2 d0x = make_float2(dx0, dx0), d0y = make_float2(dy0, dy0), d0z = make_float2(dz0, dz0);
+    float2 a2[NEN];
 #pragma unroll
-    for (int q = 0; q < kTriPts; q++) {
-        const float4 Q = q7[q];
-        const float dx = dx0 - Q.x, dy = dy0 - Q.y, dz = dz0 - Q.z;
-        const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-        const float inv = rsqrtf(r2);
-        float w;
+    for (int k = 0; k < NEN; k++) a2[k] = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int p = 0; p < kQpPairs; p++) {
+        const float4 A = q8[2 * p], B = q8[2 * p + 1];
+        const float2 dx = __fadd2_rn(d0x, make_float2(A.x, A.y));
+        const float2 dy = __fadd2_rn(d0y, make_float2(A.z, A.w));
+        const float2 dz = __fadd2_rn(d0z, make_float2(B.x, B.y));
+        const float2 wq = make_float2(B.z, B.w);
+        const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+        const float2 inv = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+        float2 w;
         if (MODE == 0) {
-            w = Q.w * inv;
+            w = __fmul2_rn(wq, inv);
         } else {
-            const float h = Q.w * (inv * inv * inv) * fmaf(dz, nz, fmaf(dy, ny, dx * nx));
-            w = (MODE == 1 || isH) ? h : Q.w * inv;
+            const float2 t = __ffma2_rn(dz, make_float2(nz, nz),
+                                        __ffma2_rn(dy, make_float2(ny, ny), __fmul2_rn(dx, make_float2(nx, nx))));
+            const float2 h = __fmul2_rn(__fmul2_rn(wq, __fmul2_rn(__fmul2_rn(inv, inv), inv)), t);
+            w = (MODE == 1 || isH) ? h : __fmul2_rn(wq, inv);
         }
 #pragma unroll
-        for (int k = 0; k < NEN; k++) acc[k] = fmaf(w, shape_q_f<NEN>(q, k), acc[k]);
+        for (int k = 0; k < NEN; k++) a2[k] = __ffma2_rn(w, S[p][k], a2[k]);
     }
+#pragma unroll
+    for (int k = 0; k < NEN; k++) acc[k] = a2[k].x + a2[k].y;
 }
 
 // Per-row data of the FP32 assembly, once per assembly (its conversions run
@@ -429,7 +462,7 @@ __global__ void __launch_bounds__(128) k_asm_regular_f32(AsmArgs a, const RowF32
                                                          float *__restrict__ P)
 {
     constexpr int R = kRowTile, EG = kGroup;
-    __shared__ float4 s_q[EG * kTriPts];
+    __shared__ float4 s_q[EG * 2 * kQpPairs];
     __shared__ float2 s_c[EG * 3];
     __shared__ float s_V[EG * NEN * R];
     __shared__ int s_nodes[EG * NEN];
@@ -444,14 +477,21 @@ __global__ void __launch_bounds__(128) k_asm_regular_f32(AsmArgs a, const RowF32
     for (int t = threadIdx.x; t < nfp; t += blockDim.x) s_dest[t] = a.fp_dest[f0 + t];
     for (int t = threadIdx.x; t < nsl; t += blockDim.x) s_sl[t] = a.fp_sl[sl0 + t];
 
-    for (int t = threadIdx.x; t < EG * kTriPts; t += blockDim.x) {
-        const int e = a.grp_elem[g * EG + t / kTriPts];
-        s_q[t] = e >= 0 ? qloc[(size_t)e * kTriPts + t % kTriPts] : make_float4(0.f, 0.f, 0.f, 0.f);
+    constexpr int Q8 = 2 * kQpPairs;
+    for (int t = threadIdx.x; t < EG * Q8; t += blockDim.x) {
+        const int e = a.grp_elem[g * EG + t / Q8];
+        s_q[t] = e >= 0 ? qloc[(size_t)e * Q8 + t % Q8] : make_float4(0.f, 0.f, 0.f, 0.f);
     }
     for (int t = threadIdx.x; t < EG * 3; t += blockDim.x) {
         const int e = a.grp_elem[g * EG + t / 3];
         s_c[t] = e >= 0 ? cen[(size_t)e * 3 + t % 3] : make_float2(0.f, 0.f);
     }
+    float2 S[kQpPairs][NEN];
+#pragma unroll
+    for (int p = 0; p < kQpPairs; p++)
+#pragma unroll
+        for (int k = 0; k < NEN; k++)
+            S[p][k] = make_float2(shape_q_f<NEN>(2 * p, k), 2 * p + 1 < kTriPts ? shape_q_f<NEN>(2 * p + 1, k) : 0.f);
     for (int t = threadIdx.x; t < EG * NEN; t += blockDim.x) {
         const int e = a.grp_elem[g * EG + t / NEN];
         s_nodes[t] = e >= 0 ? a.elems[(size_t)e * NEN + t % NEN] : -1;
@@ -484,10 +524,10 @@ __global__ void __launch_bounds__(128) k_asm_regular_f32(AsmArgs a, const RowF32
             const float dx = (xi.x - c[0].x) + (xi.y - c[0].y);
             const float dy = (yi.x - c[1].x) + (yi.y - c[1].y);
             const float dz = (zi.x - c[2].x) + (zi.y - c[2].y);
-            const float4 *q7 = s_q + el * kTriPts;
-            if (allG) pair_regular_f32<NEN, 0>(q7, dx, dy, dz, nx, ny, nz, false, acc);
-            else if (allH) pair_regular_f32<NEN, 1>(q7, dx, dy, dz, nx, ny, nz, true, acc);
-            else pair_regular_f32<NEN, 2>(q7, dx, dy, dz, nx, ny, nz, kind == 1, acc);
+            const float4 *q8 = s_q + el * Q8;
+            if (allG) pair_regular_f32<NEN, 0>(q8, dx, dy, dz, nx, ny, nz, false, S, acc);
+            else if (allH) pair_regular_f32<NEN, 1>(q8, dx, dy, dz, nx, ny, nz, true, S, acc);
+            else pair_regular_f32<NEN, 2>(q8, dx, dy, dz, nx, ny, nz, kind == 1, S, acc);
         }
 #pragma unroll
         for (int k = 0; k < NEN; k++) s_V[(el * NEN + k) * R + lane] = drop ? 0.f : fac * acc[k];
@@ -627,7 +667,7 @@ static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStr
     }
     if (f32) {
         DSC_TRY(w.cen.alloc((size_t)m.E * 3));
-        DSC_TRY(w.qloc.alloc((size_t)m.E * kTriPts));
+        DSC_TRY(w.qloc.alloc((size_t)m.E * 2 * kQpPairs));
         DSC_TRY(w.rows.alloc((size_t)m.N * sizeof(RowF32)));
         DSC_LAUNCH(k_qp_local<<<(m.E + 127) / 128, 128, 0, st>>>(m.qp.p, m.E, w.cen.p, w.qloc.p));
         DSC_LAUNCH(k_rows_f32<<<(m.N + 127) / 128, 128, 0, st>>>(m.x.p, m.y.p, m.z.p, m.normals.p, m.row_fac.p,
