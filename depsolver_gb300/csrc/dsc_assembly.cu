@@ -652,7 +652,8 @@ static size_t regular_smem(int nen)
 
 template <int NEN>
 static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStream_t st, Timer *tm,
-                              int prec, AsmWorkspace *ws, const int *row_grad, double *Wg)
+                              int prec, AsmWorkspace *ws, const int *row_grad, double *Wg,
+                              const std::function<int(const int **, double **)> *late)
 {
     AsmWorkspace local;
     AsmWorkspace &w = ws ? *ws : local;
@@ -720,6 +721,10 @@ static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStr
                                                                    m.n_fix, P.p, (size_t)rc, K, ld, lo, hi - lo));
             DSC_CUDA(cudaGetLastError());
         }
+        if (late) {
+            DSC_TRY((*late)(&row_grad, &Wg));
+            late = nullptr;
+        }
         int warps = hi - lo;
         TimerScope ts(tm, kTAsmSingular, st);
         DSC_LAUNCH(k_asm_singular<NEN, double><<<(warps * 32 + 127) / 128, 128, 0, st>>>(
@@ -734,10 +739,11 @@ static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStr
 }
 
 int assemble_K_fp64(const DeviceMesh &m, double *K, size_t ld, cudaStream_t st, Timer *tm, int prec,
-                    AsmWorkspace *ws, const int *row_grad, double *Wg)
+                    AsmWorkspace *ws, const int *row_grad, double *Wg,
+                    const std::function<int(const int **, double **)> *late)
 {
-    return m.nen == 6 ? assemble_fp64_impl<6>(m, K, ld, st, tm, prec, ws, row_grad, Wg)
-                      : assemble_fp64_impl<3>(m, K, ld, st, tm, prec, ws, row_grad, Wg);
+    return m.nen == 6 ? assemble_fp64_impl<6>(m, K, ld, st, tm, prec, ws, row_grad, Wg, late)
+                      : assemble_fp64_impl<3>(m, K, ld, st, tm, prec, ws, row_grad, Wg, late);
 }
 
 }  // namespace dsc

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -288,9 +289,12 @@ enum { kAsmF64 = 0, kAsmDf32 = 1, kAsmF32 = 2 };
 // returning) holds the scratch.  With Wg not null, the rows flagged in
 // row_grad (N flags) also leave the gradient integrals of their singular
 // elements there: 3 nen doubles per (node, element) tuple of the plan's
-// ne_ptr numbering.
+// ne_ptr numbering.  late (may be null) is called once, after the regular
+// pairs are queued and before the singular ones, to give row_grad and Wg
+// in place of the arguments (so that their producer may still be running
+// while the regular pairs are launched).
 int assemble_K_fp64(const DeviceMesh &m, double *K, size_t ld, cudaStream_t st, Timer *tm = nullptr,
                     int prec = kAsmF64, AsmWorkspace *ws = nullptr, const int *row_grad = nullptr,
-                    double *Wg = nullptr);
+                    double *Wg = nullptr, const std::function<int(const int **, double **)> *late = nullptr);
 
 }  // namespace dsc

@@ -1251,6 +1251,7 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
     }
 
     // ---- batched field at the particle nodes and Maxwell-stress force
+    DSC_TRY(s.force_wait());
     ForcePlan &fp = s.force;
     if (fp.P > 0) {
         const int E = s.E, P = fp.P;

@@ -166,7 +166,11 @@ int Session::create(int nen_, unsigned N_, unsigned E_, const double *nodes, con
         DSC_CUDA(cudaStreamSynchronize(st));
     }
     DSC_TRY(dev.upload(plan, st));
-    DSC_TRY(force.build(plan, bctype.data(), st));
+    force_job = std::thread([this] {
+        AllocStreamScope fs(side);
+        force_rc = force.build(plan, bctype.data(), side);
+        if (force_rc != (int)kOk) force_err = last_error();
+    });
     ld = ((size_t)N + 31) / 32 * 32;
     pre = new Precond();
     DSC_TRY(precond_plan(*this));
@@ -176,8 +180,17 @@ int Session::create(int nen_, unsigned N_, unsigned E_, const double *nodes, con
 void destroy_mixed(Session::Mixed *m);
 void destroy_precond(Precond *p);
 
+int Session::force_wait()
+{
+    if (force_job.joinable()) force_job.join();
+    if (force_rc != kOk) set_error("%s", force_err.c_str());
+    return force_rc;
+}
+
 Session::~Session()
 {
+    if (force_job.joinable()) force_job.join();
+    if (st) cudaStreamSynchronize(st);  // nothing on st still reads a buffer freed on side
     // the stream itself goes last (StreamGuard)
     if (mx) destroy_mixed(mx);
     if (pre) destroy_precond(pre);
@@ -192,12 +205,19 @@ int Session::assemble64(bool need_fp64)
     k16_ready = false;  // the fp16 copies and the preconditioner follow K
     if (pre) pre->ready = false;
     DSC_TRY(K64.alloc(ld * N));
-    double *Wg = nullptr;
-    if (force.P > 0) {
-        DSC_TRY(Wsing.alloc((size_t)std::max(dev.ne_total, 1) * 3 * nen));
-        Wg = Wsing.p;
-    }
-    DSC_TRY(assemble_K_fp64(dev, K64.p, ld, st, &timer, want, &asm_ws, force.row_grad.p, Wg));
+    // the force plan is joined only before the singular pairs, which store
+    // the gradients its points take
+    const std::function<int(const int **, double **)> late = [this](const int **row_grad, double **Wg) -> int {
+        DSC_TRY(force_wait());
+        *row_grad = force.row_grad.p;
+        *Wg = nullptr;
+        if (force.P > 0) {
+            DSC_TRY(Wsing.alloc((size_t)std::max(dev.ne_total, 1) * 3 * nen));
+            *Wg = Wsing.p;
+        }
+        return kOk;
+    };
+    DSC_TRY(assemble_K_fp64(dev, K64.p, ld, st, &timer, want, &asm_ws, nullptr, nullptr, &late));
     k64_prec = want;
     DSC_TRY(Kdiag.alloc(N));
     DSC_LAUNCH(k_diag<<<(N + 255) / 256, 256, 0, st>>>(K64.p, ld, N, Kdiag.p));
@@ -271,6 +291,7 @@ int Session::solve_fp64(double f, double tol, unsigned max_iters, double *sigma_
     op.part = gemv_part.p;
     op.tm = &timer;
     DSC_TRY(gmres_real_fp64(2 * N, op, sigma_dev, nullptr, tol, max_iters, nullptr, iters, st));
+    DSC_TRY(force_wait());
     DSC_TRY(force_mst_dev(dev, force, sigma_dev, eps_medium, d_tot, st, &timer));
     return kOk;
 }

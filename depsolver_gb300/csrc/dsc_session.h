@@ -3,6 +3,9 @@
 
 #include <cuda_fp16.h>
 
+#include <functional>
+#include <string>
+#include <thread>
 #include <vector>
 
 #include "dsc_field.h"
@@ -38,6 +41,14 @@ struct Session {
     HostPlan plan;
     DeviceMesh dev;
     ForcePlan force;
+    // the force plan's host part (field points, their near lists, the
+    // singular tuples they share with the assembly) is built on a thread
+    // from create() on, beside the first assembly's regular pairs, with its
+    // uploads on the side stream; force_wait() joins it (the destructor too)
+    std::thread force_job;
+    int force_rc = 0;
+    std::string force_err;
+    int force_wait();
     Timer timer;
     std::vector<unsigned> bctype, ifaces;
     std::vector<double> mbc, mat;
