@@ -40,14 +40,99 @@ __device__ __forceinline__ int duffy(int s, double u1, double u2, double *La, do
     }
 }
 
+// The element's map X(l1, l2) = sum N_k(l) X_k as its polynomial about
+// local (0, 0): X = k0 + k1 l1 + k2 l2 (+ d11 l1^2 / 2 + k12 l1 l2 +
+// d22 l2^2 / 2 for tria6), with the tangents dX/dl1 = k1 + d11 l1 + k12 l2,
+// dX/dl2 = k2 + k12 l1 + d22 l2.  X - k0 = (l1 (t1 + k1) + l2 (t2 + k2)) / 2,
+// so a point's offset from the collocation point comes from the tangents in
+// a few FMAs (the same map as shape() / tangents(), summed differently).
+template <int NEN>
+struct ElemMap {
+    double k0[3], k1[3], k2[3], d11[3], k12[3], d22[3];
+    __device__ __forceinline__ void init(const double (*X)[3])
+    {
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            if (NEN == 3) {
+                k0[d] = X[2][d];
+                k1[d] = X[0][d] - X[2][d];
+                k2[d] = X[1][d] - X[2][d];
+                d11[d] = k12[d] = d22[d] = 0.0;
+            } else {
+                k0[d] = X[4][d];
+                k1[d] = 4.0 * X[5][d] - X[0][d] - 3.0 * X[4][d];
+                k2[d] = 4.0 * X[3][d] - X[2][d] - 3.0 * X[4][d];
+                d11[d] = 4.0 * (X[0][d] + X[4][d] - 2.0 * X[5][d]);
+                k12[d] = 4.0 * (X[1][d] - X[3][d] + X[4][d] - X[5][d]);
+                d22[d] = 4.0 * (X[2][d] + X[4][d] - 2.0 * X[3][d]);
+            }
+        }
+    }
+    // dd = xe - X(l1, l2), given e0 = xe - k0; returns the Jacobian |t1 x t2|.
+    __device__ __forceinline__ double at(double l1, double l2, const double *e0, double *dd) const
+    {
+        double t1[3], t2[3];
+        const double h1 = 0.5 * l1, h2 = 0.5 * l2;
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            if (NEN == 3) {
+                t1[d] = k1[d];
+                t2[d] = k2[d];
+                dd[d] = e0[d] - fma(l1, k1[d], l2 * k2[d]);
+            } else {
+                t1[d] = fma(d11[d], l1, fma(k12[d], l2, k1[d]));
+                t2[d] = fma(k12[d], l1, fma(d22[d], l2, k2[d]));
+                dd[d] = e0[d] - fma(h1, t1[d] + k1[d], h2 * (t2[d] + k2[d]));
+            }
+        }
+        const double j1 = t1[1] * t2[2] - t2[1] * t1[2];
+        const double j2 = t2[0] * t1[2] - t1[0] * t2[2];
+        const double j3 = t1[0] * t2[1] - t2[0] * t1[1];
+        return sqrt(j1 * j1 + j2 * j2 + j3 * j3);
+    }
+};
+
+// A point of the singular quadrature: dd = xe - X(l1, l2), returns the
+// Jacobian.  FAST: from the polynomial map; else as the reference sums it
+// (nodal shape functions, N the shape values at (l1, l2)), which the FP64
+// mode keeps so that its K follows the reference's rounding.
+template <int NEN, bool FAST>
+__device__ __forceinline__ double sing_point(const ElemMap<NEN> &em, const double (*X)[3], const double *xe,
+                                             const double *e0, double l1, double l2, const double *N, double *dd)
+{
+    if (FAST) return em.at(l1, l2, e0, dd);
+    double XL[3];
+    const double J = map_point<NEN>(X, l1, l2, N, XL);
+#pragma unroll
+    for (int d = 0; d < 3; d++) dd[d] = xe[d] - XL[d];
+    return J;
+}
+
+// c / r^3 at squared distance rsq: FAST by the reciprocal square root, else
+// by the reference's division.
+template <int NEN, bool FAST>
+__device__ __forceinline__ double over_r3(double c, double rsq)
+{
+    if (FAST) {
+        const double ri = rsqrt(rsq);
+        return c * (ri * ri * ri);
+    }
+    if (NEN == 3) return c / (rsq * sqrt(rsq));
+    const double dr = sqrt(rsq);
+    return c / (dr * dr * dr);
+}
+
 // Warp-cooperative weakly singular G: out[k] (lane 0 valid after the call,
 // every lane holds the reduced value) = sum over 8 x 8 (x2) points of
 // w1 w2 J B N_k / r, B = 1/8 (one sub-triangle) or 1/16 (two).
-template <int NEN>
+template <int NEN, bool FAST = false>
 __device__ void warp_singular_G(int s, const double (*X)[3], const double *xe, double *out)
 {
     const int lane = threadIdx.x & 31;
-    double La[2], Lb[2], N[6], XL[3];
+    double La[2], Lb[2], N[6], dd[3];
+    ElemMap<NEN> em;
+    em.init(X);
+    const double e0[3] = {xe[0] - em.k0[0], xe[1] - em.k0[1], xe[2] - em.k0[2]};
     double acc[NEN];
 #pragma unroll
     for (int k = 0; k < NEN; k++) acc[k] = 0.0;
@@ -61,9 +146,10 @@ __device__ void warp_singular_G(int s, const double (*X)[3], const double *xe, d
         duffy<NEN>(s, u1, u2, La, Lb);
         const double *L = t == 0 ? La : Lb;
         shape<NEN>(L[0], L[1], N);
-        double J = map_point<NEN>(X, L[0], L[1], N, XL);
-        double dx = xe[0] - XL[0], dy = xe[1] - XL[1], dz = xe[2] - XL[2];
-        double A = w1 * w2 * J * B / sqrt(dx * dx + dy * dy + dz * dz);
+        const double J = sing_point<NEN, FAST>(em, X, xe, e0, L[0], L[1], N, dd);
+        const double dx = dd[0], dy = dd[1], dz = dd[2];
+        const double rsq = dx * dx + dy * dy + dz * dz;
+        const double A = FAST ? w1 * w2 * J * B * rsqrt(rsq) : w1 * w2 * J * B / sqrt(rsq);
 #pragma unroll
         for (int k = 0; k < NEN; k++) acc[k] += A * N[k];
     }
@@ -95,7 +181,7 @@ __device__ __forceinline__ int singular_perm(int s, int p)
 // mid-side nodes each point is split into two mapped points with weight
 // 1/2; the gradient's z-component of the second one uses its y-distance,
 // as in the reference (:762).
-template <int NEN, int FLAG>
+template <int NEN, int FLAG, bool FAST = false>
 __device__ void warp_singular_H(int s, const double (*X0)[3], const double *xe, const double *n,
                                 double *out)
 {
@@ -107,6 +193,9 @@ __device__ void warp_singular_H(int s, const double (*X0)[3], const double *xe, 
     for (int p = 0; p < NEN; p++)
 #pragma unroll
         for (int d = 0; d < 3; d++) X[p][d] = X0[singular_perm<NEN>(s, p)][d];
+    ElemMap<NEN> em;
+    em.init(X);
+    const double e0[3] = {xe[0] - em.k0[0], xe[1] - em.k0[1], xe[2] - em.k0[2]};
     double acc[NOUT];
 #pragma unroll
     for (int k = 0; k < NOUT; k++) acc[k] = 0.0;
@@ -115,7 +204,7 @@ __device__ void warp_singular_H(int s, const double (*X0)[3], const double *xe, 
     const double xs0[3][3][2] = {{{1.0, 0.0}, {0.5, 0.5}, {0.5, 0.0}},
                                  {{0.5, 0.0}, {0.5, 0.5}, {0.0, 0.5}},
                                  {{0.5, 0.5}, {0.0, 1.0}, {0.0, 0.5}}};
-    double N1[6], N2[6], XL1[3], XL2[3];
+    double N1[6], N2[6], D1[3], D2[3];
     for (int p = lane; p < kSubdiv * 3 * kTriPts; p += 32) {
         int m = p / (3 * kTriPts), i = (p / kTriPts) % 3, q = p % kTriPts;
         double scale = ldexp(1.0, -m);          // xs halves each level (exact)
@@ -129,16 +218,9 @@ __device__ void warp_singular_H(int s, const double (*X0)[3], const double *xe, 
             double l1 = x00 * M1 + x10 * M2 + x20 * M3;
             double l2 = x01 * M1 + x11 * M2 + x21 * M3;
             shape<NEN>(l1, l2, N1);
-            double JL = map_point<NEN>(X, l1, l2, N1, XL1);
-            double dx = xe[0] - XL1[0], dy = xe[1] - XL1[1], dz = xe[2] - XL1[2];
-            double A;
-            if (NEN == 3) {
-                double rsq = dx * dx + dy * dy + dz * dz;
-                A = J * JL * W / (rsq * sqrt(rsq));
-            } else {
-                double dr = sqrt(dx * dx + dy * dy + dz * dz);
-                A = J * JL * W / (dr * dr * dr);
-            }
+            const double JL = sing_point<NEN, FAST>(em, X, xe, e0, l1, l2, N1, D1);
+            const double dx = D1[0], dy = D1[1], dz = D1[2];
+            const double A = over_r3<NEN, FAST>(J * JL * W, dx * dx + dy * dy + dz * dz);
             if (FLAG != 1) {
                 const double An = A * (dx * n[0] + dy * n[1] + dz * n[2]);
 #pragma unroll
@@ -162,14 +244,12 @@ __device__ void warp_singular_H(int s, const double (*X0)[3], const double *xe, 
             double b1 = x00 * V1 + x10 * V2 + x20 * V3, b2 = x01 * V1 + x11 * V2 + x21 * V3;
             shape<NEN>(a1, a2, N1);
             shape<NEN>(b1, b2, N2);
-            double JL1 = map_point<NEN>(X, a1, a2, N1, XL1);
-            double JL2 = map_point<NEN>(X, b1, b2, N2, XL2);
-            double dx1 = xe[0] - XL1[0], dy1 = xe[1] - XL1[1], dz1 = xe[2] - XL1[2];
-            double dx2 = xe[0] - XL2[0], dy2 = xe[1] - XL2[1], dz2 = xe[2] - XL2[2];
-            double dr1 = sqrt(dx1 * dx1 + dy1 * dy1 + dz1 * dz1);
-            double dr2 = sqrt(dx2 * dx2 + dy2 * dy2 + dz2 * dz2);
-            double A1 = 0.5 * J * JL1 * W / (dr1 * dr1 * dr1);
-            double A2 = 0.5 * J * JL2 * W / (dr2 * dr2 * dr2);
+            const double JL1 = sing_point<NEN, FAST>(em, X, xe, e0, a1, a2, N1, D1);
+            const double JL2 = sing_point<NEN, FAST>(em, X, xe, e0, b1, b2, N2, D2);
+            const double dx1 = D1[0], dy1 = D1[1], dz1 = D1[2];
+            const double dx2 = D2[0], dy2 = D2[1], dz2 = D2[2];
+            const double A1 = over_r3<NEN, FAST>(0.5 * J * JL1 * W, dx1 * dx1 + dy1 * dy1 + dz1 * dz1);
+            const double A2 = over_r3<NEN, FAST>(0.5 * J * JL2 * W, dx2 * dx2 + dy2 * dy2 + dz2 * dz2);
             if (FLAG != 1) {
                 const double An1 = A1 * (dx1 * n[0] + dy1 * n[1] + dz1 * n[2]);
                 const double An2 = A2 * (dx2 * n[0] + dy2 * n[1] + dz2 * n[2]);
