@@ -21,14 +21,22 @@ constexpr int kSubdiv = 8;    // NSUBDIVISIONS
 // Published rules written to the 15 significant digits the reference
 // tabulates: Dunavant's 7-point degree-5 triangle rule (weights sum 1/2),
 // 8-point Gauss-Legendre, and 8-point Gauss-Jacobi for weight (1 + x).
-__constant__ __device__ static const double c_tri7[kTriPts][3] = {
-    {0.333333333333333, 0.333333333333333, 0.1125},
-    {0.470142064105115, 0.470142064105115, 0.066197076394253},
-    {0.0597158717897700, 0.470142064105115, 0.066197076394253},
-    {0.470142064105115, 0.0597158717897700, 0.066197076394253},
-    {0.101286507323456, 0.101286507323456, 0.062969590272414},
-    {0.797426985353088, 0.101286507323456, 0.062969590272414},
-    {0.101286507323456, 0.797426985353088, 0.062969590272414}};
+#define DSC_TRI7_ROWS                                                \
+    {0.333333333333333, 0.333333333333333, 0.1125},                  \
+        {0.470142064105115, 0.470142064105115, 0.066197076394253},   \
+        {0.0597158717897700, 0.470142064105115, 0.066197076394253},  \
+        {0.470142064105115, 0.0597158717897700, 0.066197076394253},  \
+        {0.101286507323456, 0.101286507323456, 0.062969590272414},   \
+        {0.797426985353088, 0.101286507323456, 0.062969590272414},   \
+    {                                                                \
+        0.101286507323456, 0.797426985353088, 0.062969590272414      \
+    }
+__constant__ __device__ static const double c_tri7[kTriPts][3] = {DSC_TRI7_ROWS};
+// the same rule for tables built at compile time
+struct Tri7Rule {
+    double v[kTriPts][3];
+};
+constexpr Tri7Rule kTri7{{DSC_TRI7_ROWS}};
 
 __constant__ __device__ static const double c_gl8[kLinePts][2] = {
     {-0.960289856497536, 0.101228536290370}, {-0.796666477413627, 0.222381034453376},

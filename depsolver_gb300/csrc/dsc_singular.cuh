@@ -157,6 +157,45 @@ __device__ void warp_singular_G(int s, const double (*X)[3], const double *xe, d
     for (int k = 0; k < NEN; k++) out[k] = warp_sum(acc[k]);
 }
 
+// The subdivision's points at level 0 (level m: times 2^-m, exact): for
+// sub-triangle i and point q of the 7-point rule, l[i][q] = (l1, l2); for
+// the tria6 mid-side rotations s = 2, 4, 6, ab[s / 2 - 1][i][q] = the two
+// mapped points (a1, a2, b1, b2).  The same sums as the loop below takes
+// per point, evaluated once at compile time.
+struct SubdivPts {
+    double l[3][kTriPts][2];
+    double ab[3][3][kTriPts][4];
+};
+
+constexpr SubdivPts make_subdiv_pts()
+{
+    SubdivPts t{};
+    const double xs[3][3][2] = {{{1.0, 0.0}, {0.5, 0.5}, {0.5, 0.0}},
+                                {{0.5, 0.0}, {0.5, 0.5}, {0.0, 0.5}},
+                                {{0.5, 0.5}, {0.0, 1.0}, {0.0, 0.5}}};
+    for (int i = 0; i < 3; i++)
+        for (int q = 0; q < kTriPts; q++) {
+            const double M1 = kTri7.v[q][0], M2 = kTri7.v[q][1], M3 = 1.0 - M1 - M2;
+            t.l[i][q][0] = xs[i][0][0] * M1 + xs[i][1][0] * M2 + xs[i][2][0] * M3;
+            t.l[i][q][1] = xs[i][0][1] * M1 + xs[i][1][1] * M2 + xs[i][2][1] * M3;
+            for (int r = 0; r < 3; r++) {
+                double U1 = 0.0, U2 = 0.0, V1 = 0.0, V2 = 0.0;
+                if (r == 0) { U1 = 0.5 * M3; U2 = M1 + 0.5 * M3; V1 = M1 + 0.5 * M3; V2 = M3; }
+                else if (r == 1) { U1 = M1; U2 = 0.5 * M3; V1 = M1; V2 = M2 + 0.5 * M3; }
+                else { U1 = 0.5 * M3; U2 = M1; V1 = M1 + 0.5 * M3; V2 = M2; }
+                const double U3 = 1.0 - U1 - U2, V3 = 1.0 - V1 - V2;
+                t.ab[r][i][q][0] = xs[i][0][0] * U1 + xs[i][1][0] * U2 + xs[i][2][0] * U3;
+                t.ab[r][i][q][1] = xs[i][0][1] * U1 + xs[i][1][1] * U2 + xs[i][2][1] * U3;
+                t.ab[r][i][q][2] = xs[i][0][0] * V1 + xs[i][1][0] * V2 + xs[i][2][0] * V3;
+                t.ab[r][i][q][3] = xs[i][0][1] * V1 + xs[i][1][1] * V2 + xs[i][2][1] * V3;
+            }
+        }
+    return t;
+}
+
+// in global memory: the lanes of a warp read different entries
+__device__ const SubdivPts g_subdiv = make_subdiv_pts();
+
 // Position p of the rotated element holds original node perm[p]
 // (src/kernelIntegrals.c:494-499, :636-647).
 template <int NEN>
@@ -170,6 +209,51 @@ __device__ __forceinline__ int singular_perm(int s, int p)
     if (s == 1) return (p + 2) % 6;
     if (s == 3) return (p + 4) % 6;
     return p;
+}
+
+// One point's (two mapped points') terms of warp_singular_H: FLAG != 1 the
+// normal derivative (acc[k] -= A (d . n) N_k), FLAG != 0 the gradient
+// (acc[G0 + 3 k + c] += A d_c N_k; the second mapped point's z term with its
+// y distance, as in the reference, src/kernelIntegrals.c:762).
+template <int NEN, int FLAG>
+__device__ __forceinline__ void singular_H_add(double A, double dx, double dy, double dz, const double *n,
+                                               const double *N1, double *acc)
+{
+    constexpr int G0 = FLAG == 2 ? NEN : 0;
+    if (FLAG != 1) {
+        const double An = A * (dx * n[0] + dy * n[1] + dz * n[2]);
+#pragma unroll
+        for (int k = 0; k < NEN; k++) acc[k] -= An * N1[k];
+    }
+    if (FLAG != 0) {
+#pragma unroll
+        for (int k = 0; k < NEN; k++) {
+            acc[G0 + 3 * k + 0] += A * dx * N1[k];
+            acc[G0 + 3 * k + 1] += A * dy * N1[k];
+            acc[G0 + 3 * k + 2] += A * dz * N1[k];
+        }
+    }
+}
+
+template <int NEN, int FLAG>
+__device__ __forceinline__ void singular_H_add2(double A1, const double *D1, const double *N1, double A2,
+                                                const double *D2, const double *N2, const double *n, double *acc)
+{
+    constexpr int G0 = FLAG == 2 ? NEN : 0;
+    if (FLAG != 1) {
+        const double An1 = A1 * (D1[0] * n[0] + D1[1] * n[1] + D1[2] * n[2]);
+        const double An2 = A2 * (D2[0] * n[0] + D2[1] * n[1] + D2[2] * n[2]);
+#pragma unroll
+        for (int k = 0; k < NEN; k++) acc[k] -= An1 * N1[k] + An2 * N2[k];
+    }
+    if (FLAG != 0) {
+#pragma unroll
+        for (int k = 0; k < NEN; k++) {
+            acc[G0 + 3 * k + 0] += A1 * D1[0] * N1[k] + A2 * D2[0] * N2[k];
+            acc[G0 + 3 * k + 1] += A1 * D1[1] * N1[k] + A2 * D2[1] * N2[k];
+            acc[G0 + 3 * k + 2] += A1 * D1[2] * N1[k] + A2 * D2[1] * N2[k];
+        }
+    }
 }
 
 // Warp-cooperative strongly singular H (FLAG = 0: normal derivative with
@@ -211,6 +295,29 @@ __device__ void warp_singular_H(int s, const double (*X0)[3], const double *xe, 
         double J = ldexp(1.0, -2 * (m + 1));    // 0.25^(m+1) (exact)
         double M1 = c_tri7[q][0], M2 = c_tri7[q][1];
         double M3 = 1.0 - M1 - M2, W = c_tri7[q][2];
+        if (FAST) {
+            if (!two) {
+                const double2 L = __ldg((const double2 *)g_subdiv.l[i][q]);
+                const double l1 = L.x * scale, l2 = L.y * scale;
+                shape<NEN>(l1, l2, N1);
+                const double JL = em.at(l1, l2, e0, D1);
+                const double dx = D1[0], dy = D1[1], dz = D1[2];
+                const double A = over_r3<NEN, true>(J * JL * W, dx * dx + dy * dy + dz * dz);
+                singular_H_add<NEN, FLAG>(A, dx, dy, dz, n, N1, acc);
+            } else {
+                const double2 *ab = (const double2 *)g_subdiv.ab[s / 2 - 1][i][q];
+                const double2 P1 = __ldg(ab), P2 = __ldg(ab + 1);
+                const double a1 = P1.x * scale, a2 = P1.y * scale, b1 = P2.x * scale, b2 = P2.y * scale;
+                shape<NEN>(a1, a2, N1);
+                shape<NEN>(b1, b2, N2);
+                const double JL1 = em.at(a1, a2, e0, D1);
+                const double JL2 = em.at(b1, b2, e0, D2);
+                const double A1 = over_r3<NEN, true>(0.5 * J * JL1 * W, D1[0] * D1[0] + D1[1] * D1[1] + D1[2] * D1[2]);
+                const double A2 = over_r3<NEN, true>(0.5 * J * JL2 * W, D2[0] * D2[0] + D2[1] * D2[1] + D2[2] * D2[2]);
+                singular_H_add2<NEN, FLAG>(A1, D1, N1, A2, D2, N2, n, acc);
+            }
+            continue;
+        }
         double x00 = xs0[i][0][0] * scale, x01 = xs0[i][0][1] * scale;
         double x10 = xs0[i][1][0] * scale, x11 = xs0[i][1][1] * scale;
         double x20 = xs0[i][2][0] * scale, x21 = xs0[i][2][1] * scale;
