@@ -68,8 +68,9 @@ struct ElemMap {
             }
         }
     }
-    // dd = xe - X(l1, l2), given e0 = xe - k0; returns the Jacobian |t1 x t2|.
-    __device__ __forceinline__ double at(double l1, double l2, const double *e0, double *dd) const
+    // dd = xe - X(l1, l2), given e0 = xe - k0; returns the squared Jacobian
+    // |t1 x t2|^2.
+    __device__ __forceinline__ double at_sq(double l1, double l2, const double *e0, double *dd) const
     {
         double t1[3], t2[3];
         const double h1 = 0.5 * l1, h2 = 0.5 * l2;
@@ -88,9 +89,20 @@ struct ElemMap {
         const double j1 = t1[1] * t2[2] - t2[1] * t1[2];
         const double j2 = t2[0] * t1[2] - t1[0] * t2[2];
         const double j3 = t1[0] * t2[1] - t2[0] * t1[1];
-        return sqrt(j1 * j1 + j2 * j2 + j3 * j3);
+        return j1 * j1 + j2 * j2 + j3 * j3;
+    }
+    __device__ __forceinline__ double at(double l1, double l2, const double *e0, double *dd) const
+    {
+        return sqrt(at_sq(l1, l2, e0, dd));
     }
 };
+
+// |J| / r^3 from the squared Jacobian and squared distance in one
+// reciprocal square root: |J| / r^3 = J^2 / sqrt(J^2 r^6).
+__device__ __forceinline__ double jac_over_r3(double j2, double rsq)
+{
+    return j2 * rsqrt(j2 * (rsq * rsq * rsq));
+}
 
 // A point of the singular quadrature: dd = xe - X(l1, l2), returns the
 // Jacobian.  FAST: from the polynomial map; else as the reference sums it
@@ -146,10 +158,17 @@ __device__ void warp_singular_G(int s, const double (*X)[3], const double *xe, d
         duffy<NEN>(s, u1, u2, La, Lb);
         const double *L = t == 0 ? La : Lb;
         shape<NEN>(L[0], L[1], N);
-        const double J = sing_point<NEN, FAST>(em, X, xe, e0, L[0], L[1], N, dd);
-        const double dx = dd[0], dy = dd[1], dz = dd[2];
-        const double rsq = dx * dx + dy * dy + dz * dz;
-        const double A = FAST ? w1 * w2 * J * B * rsqrt(rsq) : w1 * w2 * J * B / sqrt(rsq);
+        double A;
+        if (FAST) {
+            // |J| / r = J^2 / sqrt(J^2 r^2)
+            const double j2 = em.at_sq(L[0], L[1], e0, dd);
+            const double rsq = dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2];
+            A = w1 * w2 * B * (j2 * rsqrt(j2 * rsq));
+        } else {
+            const double J = sing_point<NEN, FAST>(em, X, xe, e0, L[0], L[1], N, dd);
+            const double dx = dd[0], dy = dd[1], dz = dd[2];
+            A = w1 * w2 * J * B / sqrt(dx * dx + dy * dy + dz * dz);
+        }
 #pragma unroll
         for (int k = 0; k < NEN; k++) acc[k] += A * N[k];
     }
@@ -300,9 +319,9 @@ __device__ void warp_singular_H(int s, const double (*X0)[3], const double *xe, 
                 const double2 L = __ldg((const double2 *)g_subdiv.l[i][q]);
                 const double l1 = L.x * scale, l2 = L.y * scale;
                 shape<NEN>(l1, l2, N1);
-                const double JL = em.at(l1, l2, e0, D1);
+                const double j2 = em.at_sq(l1, l2, e0, D1);
                 const double dx = D1[0], dy = D1[1], dz = D1[2];
-                const double A = over_r3<NEN, true>(J * JL * W, dx * dx + dy * dy + dz * dz);
+                const double A = J * W * jac_over_r3(j2, dx * dx + dy * dy + dz * dz);
                 singular_H_add<NEN, FLAG>(A, dx, dy, dz, n, N1, acc);
             } else {
                 const double2 *ab = (const double2 *)g_subdiv.ab[s / 2 - 1][i][q];
@@ -310,10 +329,11 @@ __device__ void warp_singular_H(int s, const double (*X0)[3], const double *xe, 
                 const double a1 = P1.x * scale, a2 = P1.y * scale, b1 = P2.x * scale, b2 = P2.y * scale;
                 shape<NEN>(a1, a2, N1);
                 shape<NEN>(b1, b2, N2);
-                const double JL1 = em.at(a1, a2, e0, D1);
-                const double JL2 = em.at(b1, b2, e0, D2);
-                const double A1 = over_r3<NEN, true>(0.5 * J * JL1 * W, D1[0] * D1[0] + D1[1] * D1[1] + D1[2] * D1[2]);
-                const double A2 = over_r3<NEN, true>(0.5 * J * JL2 * W, D2[0] * D2[0] + D2[1] * D2[1] + D2[2] * D2[2]);
+                const double j21 = em.at_sq(a1, a2, e0, D1);
+                const double j22 = em.at_sq(b1, b2, e0, D2);
+                const double hJW = 0.5 * J * W;
+                const double A1 = hJW * jac_over_r3(j21, D1[0] * D1[0] + D1[1] * D1[1] + D1[2] * D1[2]);
+                const double A2 = hJW * jac_over_r3(j22, D2[0] * D2[0] + D2[1] * D2[1] + D2[2] * D2[2]);
                 singular_H_add2<NEN, FLAG>(A1, D1, N1, A2, D2, N2, n, acc);
             }
             continue;
