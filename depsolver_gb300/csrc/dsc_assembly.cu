@@ -553,10 +553,33 @@ __global__ void k_asm_fixup_f32(const int *__restrict__ fix_ptr, const int *__re
 {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nrows) return;
-    for (int b = blockIdx.y; b < n_fix; b += gridDim.y) {
-        float sum = 0.f;
-        for (int t = fix_ptr[b]; t < fix_ptr[b + 1]; t++) sum += P[(size_t)fix_slot[t] * ldp + r];
-        K[(size_t)fix_col[b] * ld + row_lo + r] = f32_widen(sum);
+    // four columns at a time, their slot loads interleaved (each column's
+    // slots still summed in order): four dependent load chains in flight
+    constexpr int U = 4;
+    const int stride = gridDim.y;
+    for (int b0 = blockIdx.y; b0 < n_fix; b0 += U * stride) {
+        int lo[U], hi[U];
+        int len = 0;
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int b = b0 + u * stride;
+            lo[u] = b < n_fix ? fix_ptr[b] : 0;
+            hi[u] = b < n_fix ? fix_ptr[b + 1] : 0;
+            len = max(len, hi[u] - lo[u]);
+        }
+        float sum[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) sum[u] = 0.f;
+        for (int j = 0; j < len; j++) {
+#pragma unroll
+            for (int u = 0; u < U; u++)
+                if (lo[u] + j < hi[u]) sum[u] += P[(size_t)fix_slot[lo[u] + j] * ldp + r];
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int b = b0 + u * stride;
+            if (b < n_fix) K[(size_t)fix_col[b] * ld + row_lo + r] = f32_widen(sum[u]);
+        }
     }
 }
 
