@@ -590,14 +590,24 @@ int precond_apply_v(Session &s, const float2 *V, int F, __half *Zh, __half *Zl, 
     cudaStream_t st = s.st;
     TimerScope ts(&s.timer, kTPreApply, st);
     const int F2 = 2 * F;
+    // odd blocks on the side stream: each block's product is a small GEMM
+    // (tens of CTAs), two of them fill more of the GPU
+    SideJoin sj;
+    const bool two = pc.nb >= 2 && s.side;
+    if (two) DSC_TRY(sj.fork(st, s.side));
     for (int b = 0; b < pc.nb; b++) {
         const int n = pc.n[b], ldx = pc.ldx[b];
-        DSC_LAUNCH(k_pre_gather_v<<<dim3((n + 255) / 256, F2), 256, 0, st>>>(
+        cudaStream_t sb = two && (b & 1) ? s.side : st;
+        DSC_LAUNCH(k_pre_gather_v<<<dim3((n + 255) / 256, F2), 256, 0, sb>>>(
             V, s.ld, pc.nodes.p + pc.noff[b], n, pc.Bh.p + pc.boff[b], pc.Bl.p + pc.boff[b], ldx));
         DSC_TRY(tc_gemm_3xf16(pc.Xh.p + pc.xoff[b], pc.Xl.p + pc.xoff[b], ldx, pc.Bh.p + pc.boff[b],
-                              pc.Bl.p + pc.boff[b], ldx, n, F2, n, pc.Y.p + pc.yoff[b], ldx, pc.S[b], d_err, st,
+                              pc.Bl.p + pc.boff[b], ldx, n, F2, n, pc.Y.p + pc.yoff[b], ldx, pc.S[b], d_err, sb,
                               pc.rs.p + pc.noff[b], cscK));
         s.timer.add_work(kTPreApply, 6.0 * n * (double)n * F2);
+    }
+    if (two) {
+        DSC_TRY(sj.done(s.side));
+        DSC_TRY(sj.join());
     }
     DSC_LAUNCH(k_pre_combine<<<dim3((s.N + 255) / 256, F2), 256, 0, st>>>(
         V, s.ld, s.N, pc.rblk.p, pc.rpos.p, pc.Y.p, pc.yinfo.p, pc.zbound.p, Zh, Zl, pc.cz.p));
@@ -612,19 +622,28 @@ int precond_apply_d(Session &s, double *D, int F, int *d_err)
     cudaStream_t st = s.st;
     TimerScope ts(&s.timer, kTPreApply, st);
     const int F2 = 2 * F;
+    // blocks' rows are disjoint: odd blocks on the side stream
+    SideJoin sj;
+    const bool two = pc.nb >= 2 && s.side;
+    if (two) DSC_TRY(sj.fork(st, s.side));
     for (int b = 0; b < pc.nb; b++) {
         const int n = pc.n[b], ldx = pc.ldx[b];
         const dim3 g((n + 255) / 256, F2);
-        DSC_LAUNCH(k_pre_gather_d<<<g, 256, 0, st>>>(D, s.ld, pc.nodes.p + pc.noff[b], n, pc.G.p + pc.boff[b], ldx));
+        cudaStream_t sb = two && (b & 1) ? s.side : st;
+        DSC_LAUNCH(k_pre_gather_d<<<g, 256, 0, sb>>>(D, s.ld, pc.nodes.p + pc.noff[b], n, pc.G.p + pc.boff[b], ldx));
         float *csc = pc.csc.p + (size_t)F2 * b;
         DSC_TRY(split_cols_f16(pc.G.p + pc.boff[b], (size_t)ldx, n, F2, pc.Bh.p + pc.boff[b], pc.Bl.p + pc.boff[b],
-                               (size_t)ldx, csc, st));
+                               (size_t)ldx, csc, sb));
         DSC_TRY(tc_gemm_3xf16(pc.Xh.p + pc.xoff[b], pc.Xl.p + pc.xoff[b], ldx, pc.Bh.p + pc.boff[b],
-                              pc.Bl.p + pc.boff[b], ldx, n, F2, n, pc.Y.p + pc.yoff[b], ldx, pc.S[b], d_err, st,
+                              pc.Bl.p + pc.boff[b], ldx, n, F2, n, pc.Y.p + pc.yoff[b], ldx, pc.S[b], d_err, sb,
                               pc.rs.p + pc.noff[b], csc));
-        DSC_LAUNCH(k_pre_scatter_d<<<g, 256, 0, st>>>(D, s.ld, pc.nodes.p + pc.noff[b], n, pc.Y.p + pc.yoff[b],
+        DSC_LAUNCH(k_pre_scatter_d<<<g, 256, 0, sb>>>(D, s.ld, pc.nodes.p + pc.noff[b], n, pc.Y.p + pc.yoff[b],
                                                       pc.S[b], (size_t)ldx * F2, ldx));
         s.timer.add_work(kTPreApply, 6.0 * n * (double)n * F2);
+    }
+    if (two) {
+        DSC_TRY(sj.done(s.side));
+        DSC_TRY(sj.join());
     }
     DSC_CUDA(cudaGetLastError());
     return kOk;
