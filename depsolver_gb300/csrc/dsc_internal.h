@@ -6,6 +6,7 @@
 
 #include <functional>
 #include <string>
+#include <utility>
 #include <vector>
 
 namespace dsc {
@@ -48,6 +49,33 @@ void note_launch();
         int s_ = (call);                  \
         if (s_ != ::dsc::kOk) return s_;  \
     } while (0)
+
+// Programmatic dependent launch: the kernel may be scheduled while the
+// stream's previous kernel drains (its launch latency hidden behind that
+// kernel's tail).  The kernel must call grid_dep_wait() before it reads
+// anything the previous kernels wrote (the wait returns once they have
+// completed and their writes are visible).
+template <typename... KArgs, typename... Args>
+int launch_dependent(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args &&...args)
+{
+    note_launch();
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    DSC_CUDA(cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...));
+    return kOk;
+}
+
+#ifdef __CUDACC__
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+#endif
 
 // ---------------------------------------------------------------- buffers
 // Stream-ordered allocation.  While an AllocStreamScope is active on a

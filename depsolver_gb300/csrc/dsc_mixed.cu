@@ -217,6 +217,7 @@ __global__ void __launch_bounds__(256) k_cgs_dots(const float2 *__restrict__ Vb,
                                                   float4 *__restrict__ part,
                                                   unsigned long long *__restrict__ bytes)
 {
+    grid_dep_wait();
     const int lane = threadIdx.x & 31;
     const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int nw = (int)((gridDim.x * blockDim.x) >> 5);
@@ -276,6 +277,7 @@ __global__ void k_cgs_dots_reduce(const float4 *__restrict__ part, int nchunk, i
                                   const int *__restrict__ active, double2 *__restrict__ h,
                                   double2 *__restrict__ hacc, float4 *__restrict__ hdf)
 {
+    grid_dep_wait();
     const int t = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
     if (t >= nk * F) return;  // uniform over the warp
     const int f = t % F;
@@ -310,6 +312,7 @@ __global__ void __launch_bounds__(256) k_cgs_update(const float2 *__restrict__ V
                                                     double *__restrict__ npart,
                                                     unsigned long long *__restrict__ bytes)
 {
+    grid_dep_wait();
     const int lane = threadIdx.x & 31;
     const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int nw = (int)((gridDim.x * blockDim.x) >> 5);
@@ -376,6 +379,7 @@ __global__ void k_norm_finish(const double *__restrict__ npart, int nb, int F,
                               const int *__restrict__ mask, double *__restrict__ nrm,
                               const double *__restrict__ n0, int *__restrict__ act2)
 {
+    grid_dep_wait();
     const int f = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
     if (f >= F) return;  // uniform over the warp
     if (!mask[f]) {
@@ -1155,21 +1159,23 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
                 const int *mask = pass == 0 ? w.active.p : w.act2.p;
                 const int nchunk = (N + kDotRows - 1) / kDotRows;
                 const int dunits = nchunk * F * (j + 1), uunits = nrb * F;
-                DSC_LAUNCH(k_cgs_dots<<<std::min((dunits + 7) / 8, w.dots_grid), 256, 0, st>>>(
-                    w.Vb.p, blk, w.W.p, N, ld, F, j + 1, mask, w.dpart.p, cgsb));
-                DSC_LAUNCH(k_cgs_dots_reduce<<<((j + 1) * F + 7) / 8, 256, 0, st>>>(w.dpart.p, nchunk, j + 1, F,
-                                                                                   mask, w.h.p, w.hacc.p,
-                                                                                   w.hdf.p));
-                DSC_LAUNCH(k_cgs_update<<<std::min((uunits + 7) / 8, w.upd_grid), 256, 0, st>>>(
-                    w.Vb.p, blk, w.W.p, N, ld, F, j + 1, mask, w.hdf.p, w.npart.p, cgsb));
+                // the four kernels of a pass follow one another by
+                // programmatic dependent launch (each waits for the one
+                // before at its start)
+                DSC_TRY(launch_dependent(k_cgs_dots, dim3(std::min((dunits + 7) / 8, w.dots_grid)), dim3(256), 0, st,
+                                         w.Vb.p, blk, w.W.p, N, ld, F, j + 1, mask, w.dpart.p, cgsb));
+                DSC_TRY(launch_dependent(k_cgs_dots_reduce, dim3(((j + 1) * F + 7) / 8), dim3(256), 0, st, w.dpart.p,
+                                         nchunk, j + 1, F, mask, w.h.p, w.hacc.p, w.hdf.p));
+                DSC_TRY(launch_dependent(k_cgs_update, dim3(std::min((uunits + 7) / 8, w.upd_grid)), dim3(256), 0,
+                                         st, w.Vb.p, blk, w.W.p, N, ld, F, j + 1, mask, w.hdf.p, w.npart.p, cgsb));
                 // pass 0: |w| of every active system and the DGKS decision;
                 // pass 1: |w| of the systems that took the second pass
                 if (pass == 0)
-                    DSC_LAUNCH(k_norm_finish<<<wb, 256, 0, st>>>(w.npart.p, nrb, F, w.active.p, w.nrm.p,
-                                                                 w.nrm0.p, w.act2.p));
+                    DSC_TRY(launch_dependent(k_norm_finish, dim3(wb), dim3(256), 0, st, w.npart.p, nrb, F,
+                                             w.active.p, w.nrm.p, w.nrm0.p, w.act2.p));
                 else
-                    DSC_LAUNCH(k_norm_finish<<<wb, 256, 0, st>>>(w.npart.p, nrb, F, w.act2.p, w.nrm.p,
-                                                                 nullptr, nullptr));
+                    DSC_TRY(launch_dependent(k_norm_finish, dim3(wb), dim3(256), 0, st, w.npart.p, nrb, F,
+                                             w.act2.p, w.nrm.p, (const double *)nullptr, (int *)nullptr));
             }
             {
                 TimerScope ts(tm, kTKrylov, st);
