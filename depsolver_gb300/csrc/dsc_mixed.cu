@@ -958,6 +958,7 @@ __global__ void __launch_bounds__(256) k_apply_epilogue_splits(
     const float2 *__restrict__ cs, const float2 *__restrict__ cd, float2 *__restrict__ W, int N,
     size_t ld, int F, double *__restrict__ npart)
 {
+    grid_dep_wait();
     __shared__ float2 sh[8];
     const int i = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     const int f = blockIdx.y;
@@ -1140,9 +1141,8 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
             {
                 TimerScope ts(tm, kTKrylov, st);
                 const dim3 eg((N + 511) / 512, F);  // two rows per thread
-                DSC_LAUNCH(k_apply_epilogue_splits<<<eg, 256, 0, st>>>(w.Yp.p, w.S, ld * 2 * (size_t)F, vj,
-                                                                       w.cs32.p, w.cd32.p, w.W.p, N, ld, F,
-                                                                       w.npart.p));
+                DSC_TRY(launch_dependent(k_apply_epilogue_splits, eg, dim3(256), 0, st, w.Yp.p, w.S,
+                                         ld * 2 * (size_t)F, vj, w.cs32.p, w.cd32.p, w.W.p, N, ld, F, w.npart.p));
                 DSC_CUDA(cudaMemsetAsync(w.hacc.p, 0, (size_t)(j + 1) * F * sizeof(double2), st));
                 DSC_LAUNCH(k_norm_finish<<<(F * 32 + 255) / 256, 256, 0, st>>>(w.npart.p, (int)eg.x, F, w.active.p,
                                                                                 w.nrm0.p, nullptr, nullptr));

@@ -135,6 +135,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                uint32_t acc_stride, const float *__restrict__ rsc, const float *__restrict__ csc,
                int gj_k, int *err)
 {
+    grid_dep_wait();  // launched as a programmatic dependent of the kernel before
     // ntn: column tiles of BN columns (1 unless the product is the
     // Gauss-Jordan update); GJ selects that update's epilogue with gj_k:
     // Y[column][row] -= the product (Y = -the product in column tile gj_k),
@@ -536,8 +537,8 @@ static int tc_launch(int amode, const CUtensorMap &ah, const CUtensorMap &al, co
             DSC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             if (dev < kDevs) smem_set[dev][slot] = (int)smem;
         }
-        DSC_LAUNCH(kern<<<grid, kTcThreads, smem, st>>>(ah, al, bh, bl, M, Nc, BN, ntn, nkb, kps, splits, Y, ldy,
-                                                 ldy * (size_t)Nc, tmem_cols, acc_stride, rsc, csc, gj_k, d_err));
+        DSC_TRY(launch_dependent(kern, grid, dim3(kTcThreads), smem, st, ah, al, bh, bl, M, Nc, BN, ntn, nkb, kps,
+                                 splits, Y, ldy, ldy * (size_t)Nc, tmem_cols, acc_stride, rsc, csc, gj_k, d_err));
         return kOk;
     };
     if (gj_k >= 0) DSC_TRY(launch(k_tc_gemm3<3, true>, 4));
