@@ -168,6 +168,7 @@ __device__ __forceinline__ void load_tile128(const float *__restrict__ base, siz
 // between two buffers by the parity of j: two barriers a pivot.
 __global__ void __launch_bounds__(256) k_gj_pivot(GJArgs g, int nb, int k)
 {
+    grid_dep_wait();  // a programmatic dependent of the previous step's update
     const int b = blockIdx.x;
     if (b >= nb || k >= g.nbk[b]) return;
     const float *X = g.X[b];
@@ -264,6 +265,7 @@ __device__ __forceinline__ void pre_row_pair(const float *v, __half *h, __half *
 // shared memory ([row][col + 1]).
 __global__ void __launch_bounds__(256) k_gj_row(GJArgs g, int nb, int k)
 {
+    grid_dep_wait();  // a programmatic dependent of the pivot inversion
     const int b = blockIdx.z, J = blockIdx.x;
     if (b >= nb || k >= g.nbk[b] || J >= g.nbk[b]) return;
     float *X = g.X[b];
@@ -435,8 +437,9 @@ int precond_build(Session &s)
         for (int t = 0; t < nseq; t++) {
             cudaStream_t ss = t ? s.side : st;
             for (int k = 0; k < nbk_sub[t]; k++) {
-                DSC_LAUNCH(k_gj_pivot<<<nsub[t], 256, 0, ss>>>(gsub[t], nsub[t], k));
-                DSC_LAUNCH(k_gj_row<<<dim3(nbk_sub[t], 2, nsub[t]), 256, rsmem, ss>>>(gsub[t], nsub[t], k));
+                DSC_TRY(launch_dependent(k_gj_pivot, dim3(nsub[t]), dim3(256), 0, ss, gsub[t], nsub[t], k));
+                DSC_TRY(launch_dependent(k_gj_row, dim3(nbk_sub[t], 2, nsub[t]), dim3(256), rsmem, ss, gsub[t],
+                                         nsub[t], k));
                 for (int q : which[t])
                     if (k < ga.nbk[q]) DSC_TRY(tc_gj_run(plans[q], k, ss));
             }
