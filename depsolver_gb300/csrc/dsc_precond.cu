@@ -521,6 +521,7 @@ int precond_reserve(Session &s, int F)
 __global__ void k_pre_gather_v(const float2 *__restrict__ V, size_t ld, const int *__restrict__ nodes, int n,
                                __half *__restrict__ Bh, __half *__restrict__ Bl, int ldb)
 {
+    grid_dep_wait();
     const int r = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
     if (r >= n) return;
     const float2 v = V[(size_t)c * ld + nodes[r]];
@@ -540,6 +541,7 @@ __global__ void k_pre_combine(const float2 *__restrict__ V, size_t ld, int N, co
                               const long long *__restrict__ yinfo, const unsigned *__restrict__ zbound,
                               __half *__restrict__ Zh, __half *__restrict__ Zl, float *__restrict__ cz)
 {
+    grid_dep_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
     const int sh = max(-100, min(100, 14 - ((int)(*zbound >> 23) - 127)));
     if (i == 0) cz[c] = pre_pow2(-sh);
@@ -601,8 +603,8 @@ int precond_apply_v(Session &s, const float2 *V, int F, __half *Zh, __half *Zl, 
     for (int b = 0; b < pc.nb; b++) {
         const int n = pc.n[b], ldx = pc.ldx[b];
         cudaStream_t sb = two && (b & 1) ? s.side : st;
-        DSC_LAUNCH(k_pre_gather_v<<<dim3((n + 255) / 256, F2), 256, 0, sb>>>(
-            V, s.ld, pc.nodes.p + pc.noff[b], n, pc.Bh.p + pc.boff[b], pc.Bl.p + pc.boff[b], ldx));
+        DSC_TRY(launch_dependent(k_pre_gather_v, dim3((n + 255) / 256, F2), dim3(256), 0, sb, V, s.ld,
+                                 pc.nodes.p + pc.noff[b], n, pc.Bh.p + pc.boff[b], pc.Bl.p + pc.boff[b], ldx));
         DSC_TRY(tc_gemm_3xf16(pc.Xh.p + pc.xoff[b], pc.Xl.p + pc.xoff[b], ldx, pc.Bh.p + pc.boff[b],
                               pc.Bl.p + pc.boff[b], ldx, n, F2, n, pc.Y.p + pc.yoff[b], ldx, pc.S[b], d_err, sb,
                               pc.rs.p + pc.noff[b], cscK));
@@ -612,8 +614,8 @@ int precond_apply_v(Session &s, const float2 *V, int F, __half *Zh, __half *Zl, 
         DSC_TRY(sj.done(s.side));
         DSC_TRY(sj.join());
     }
-    DSC_LAUNCH(k_pre_combine<<<dim3((s.N + 255) / 256, F2), 256, 0, st>>>(
-        V, s.ld, s.N, pc.rblk.p, pc.rpos.p, pc.Y.p, pc.yinfo.p, pc.zbound.p, Zh, Zl, pc.cz.p));
+    DSC_TRY(launch_dependent(k_pre_combine, dim3((s.N + 255) / 256, F2), dim3(256), 0, st, V, s.ld, s.N,
+                             pc.rblk.p, pc.rpos.p, pc.Y.p, pc.yinfo.p, pc.zbound.p, Zh, Zl, pc.cz.p));
     DSC_CUDA(cudaGetLastError());
     *cz = pc.cz.p;
     return kOk;

@@ -950,6 +950,7 @@ int x_digits(const double *X, size_t ldx, int N, int ncol, __half *Xd, size_t ld
 __global__ void k_digit_accumulate(const float *__restrict__ P, int S, size_t ldp, int ncol, int nj, int i,
                                    int N, double *__restrict__ Y, size_t ldy, int first)
 {
+    grid_dep_wait();  // a programmatic dependent of the digit product
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     const int c = blockIdx.y;
     if (m >= N) return;
@@ -969,7 +970,8 @@ int digit_accumulate(const float *P, int S, size_t ldp, int ncol, int nj, int i,
                      bool first, cudaStream_t st)
 {
     dim3 g((N + 255) / 256, ncol);
-    DSC_LAUNCH(k_digit_accumulate<<<g, 256, 0, st>>>(P, S, ldp, ncol, nj, i, N, Y, ldy, first ? 1 : 0));
+    DSC_TRY(launch_dependent(k_digit_accumulate, g, dim3(256), 0, st, P, S, ldp, ncol, nj, i, N, Y, ldy,
+                             first ? 1 : 0));
     DSC_CUDA(cudaGetLastError());
     return kOk;
 }
