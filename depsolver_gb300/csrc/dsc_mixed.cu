@@ -101,6 +101,7 @@ __global__ void k_givens_step(GivensState gs, const double2 *__restrict__ hacc,
                               int *__restrict__ active, double *__restrict__ scale,
                               int *__restrict__ mcount)
 {
+    grid_dep_wait();
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= F) return;
     if (!active[f]) {
@@ -447,6 +448,7 @@ __global__ void k_scale_df(const float2 *__restrict__ W, float2 *__restrict__ V,
                            __half *__restrict__ Bh, __half *__restrict__ Bl, int N, size_t ld, int F,
                            const double *__restrict__ scale, const int *__restrict__ active)
 {
+    grid_dep_wait();
     __shared__ float2 s;
     const int f = blockIdx.y;
     if (threadIdx.x == 0) s = df_from(active[f] ? scale[f] : 0.0);
@@ -1179,8 +1181,8 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
             }
             {
                 TimerScope ts(tm, kTKrylov, st);
-                DSC_LAUNCH(k_givens_step<<<gb, 64, 0, st>>>(gst, w.hacc.p, w.nrm.p, j, F, w.betad.p, w.itold.p,
-                                                            w.active.p, w.scale.p, w.mcount.p));
+                DSC_TRY(launch_dependent(k_givens_step, gb, dim3(64), 0, st, gst, w.hacc.p, w.nrm.p, j, F, w.betad.p,
+                                         w.itold.p, w.active.p, w.scale.p, w.mcount.p));
             }
             DSC_CUDA(cudaGetLastError());
             if ((j + 1) % 4 == 0 || j + 1 == kInnerMax) {
@@ -1193,8 +1195,8 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
             }
             if (j + 1 < kInnerMax) {
                 TimerScope ts(tm, kTKrylov, st);
-                DSC_LAUNCH(k_scale_df<<<vg, 256, 0, st>>>(w.W.p, vn, w.Vh.p, w.Vl.p, N, ld, F, w.scale.p,
-                                                          w.active.p));
+                DSC_TRY(launch_dependent(k_scale_df, vg, dim3(256), 0, st, w.W.p, vn, w.Vh.p, w.Vl.p, N, ld, F,
+                                         w.scale.p, w.active.p));
             }
         }
         // triangular solves on the device, then x += V y below
