@@ -83,6 +83,8 @@ def lib() -> C.CDLL:
         L.dsc_session_set_mixed_assembly.restype = C.c_int
         L.dsc_session_set_mixed_assembly.argtypes = [C.c_void_p, C.c_int]
         L.dsc_session_set_preconditioner.argtypes = [C.c_void_p, C.c_int]
+        L.dsc_session_status.restype = C.c_int
+        L.dsc_session_status.argtypes = [C.c_void_p, C.c_void_p, C.c_uint]
         L.dsc_session_preconditioner_blocks.restype = C.c_int
         L.dsc_session_preconditioner_blocks.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
         L.dsc_session_timing.restype = C.c_int

@@ -107,6 +107,11 @@ def force_mst(sc: Scene, vB: np.ndarray, eps: float | None = None):
 
 MODE_FP64 = 1
 MODE_MIXED = 2
+ERR_NOCONVERGE = 5
+# outcome of one system of a sweep (Session.status)
+SYS_CONVERGED = 0
+SYS_CAPPED = 1
+SYS_STAGNATED = 2
 # arithmetic of the mixed mode's regular pairs (Session.set_mixed_assembly)
 ASM_DF32 = 1
 ASM_FP32 = 2
@@ -194,17 +199,31 @@ class Session:
         return {n: (float(ms[k]), int(cnt[k]), float(wk[k])) for k, n in enumerate(TIMER_NAMES)}
 
     def solve(self, freqs, mode: int = MODE_MIXED, tol: float = 1e-10, max_iters: int = 600,
-              want_sigma: bool = False):
-        """Returns (forces (F x 9): Fcm, Xcm, sum|Fce|; iterations; sigma or None)."""
+              want_sigma: bool = False, partial: bool = False):
+        """Returns (forces (F x 9): Fcm, Xcm, sum|Fce|; iterations; sigma or None).
+
+        A system that does not converge raises DscError (DSC_ERR_NOCONVERGE)
+        unless partial is true; then its forces and sigma are NaN and
+        :meth:`status` gives each system's outcome (SYS_*)."""
         fr = _f(np.atleast_1d(freqs))
         F = fr.shape[0]
         forces = np.zeros((F, 9))
         its = np.zeros(F, dtype=np.uint32)
         sig = np.zeros((F, 2 * self.scene.N)) if want_sigma else None
-        _native.check(self._L.dsc_session_solve(self._h, mode, F, fr, tol, max_iters,
-                                                sig.ctypes.data if sig is not None else None,
-                                                forces.ctypes.data, its.ctypes.data))
+        rc = self._L.dsc_session_solve(self._h, mode, F, fr, tol, max_iters,
+                                       sig.ctypes.data if sig is not None else None,
+                                       forces.ctypes.data, its.ctypes.data)
+        if not (partial and rc == ERR_NOCONVERGE):
+            _native.check(rc)
         return forces, its, sig
+
+    def status(self) -> np.ndarray:
+        """Outcome of each system of the last solve: SYS_CONVERGED,
+        SYS_CAPPED (max_iters reached) or SYS_STAGNATED."""
+        n = self._L.dsc_session_status(self._h, None, 0)
+        st = np.zeros(max(n, 1), dtype=np.int32)
+        self._L.dsc_session_status(self._h, st.ctypes.data, n)
+        return st[:n]
 
 
 def sweep(sc: Scene, freqs, mode: int = MODE_MIXED, tol: float = 1e-10, max_iters: int = 600,

@@ -442,21 +442,13 @@ int field_far_tc(const float *phl, int P, const float *ecent, const float *qoff,
     CUtensorMap bh, bl;
     DSC_TRY(tc_make_map(&bh, w.Ch.p, 2, kFtN, (int)ldq, ldq, kFtN));
     DSC_TRY(tc_make_map(&bl, w.Cl.p, 2, kFtN, (int)ldq, ldq, kFtN));
-    static int nsm = 0;
-    if (!nsm) {
-        int dev = 0;
-        DSC_CUDA(cudaGetDevice(&dev));
-        DSC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    }
+    int nsm = 0;
+    DSC_TRY(current_sm_count(&nsm));
     const int tiles = (P + kFtM - 1) / kFtM;
     int nsplit = std::max(1, std::min(nsplit_max, (4 * nsm + tiles - 1) / tiles));
     const int kps = (nkb + nsplit - 1) / nsplit;
     nsplit = (nkb + kps - 1) / kps;
-    static bool smem_set = false;
-    if (!smem_set) {
-        DSC_CUDA(cudaFuncSetAttribute(k_field_far_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFtSmem));
-        smem_set = true;
-    }
+    DSC_TRY(raise_smem_limit((const void *)k_field_far_tc, (int)kFtSmem));
     FieldTcArgs a{phl, ecent, w.q8.p, w.gsc.p, w.csc.p, part, P, E, F, nkb, kps, nsplit, tiles, d_err};
     const int units = tiles * nsplit;
     DSC_LAUNCH(k_field_far_tc<<<std::min(units, nsm), kFtThreads, kFtSmem, st>>>(bh, bl, a));

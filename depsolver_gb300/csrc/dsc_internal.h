@@ -23,6 +23,9 @@ enum Status {
     kErrMemory = 7,
 };
 
+// Outcome of one system of a sweep (dsc_session_status).
+enum SysStatus { kSysConverged = 0, kSysCapped = 1, kSysStagnated = 2 };
+
 void set_error(const char *fmt, ...);
 const char *last_error();
 
@@ -87,6 +90,13 @@ __device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.w
 // it uses cudaMalloc / cudaFree.
 cudaStream_t &alloc_stream();
 int alloc_pool_setup();  // once per device: the default pool keeps freed memory
+
+// Per-device facts cached for every thread (safe to call from several
+// threads at once, each on its own device or stream): the current device's
+// SM count, and raising a kernel's dynamic shared-memory limit on the
+// current device to at least `bytes` (set once per device and size).
+int current_sm_count(int *nsm);
+int raise_smem_limit(const void *kern, int bytes);
 
 struct AllocStreamScope {
     cudaStream_t prev;

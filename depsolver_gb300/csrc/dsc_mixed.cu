@@ -15,6 +15,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <limits>
 #include <vector>
 
 #include "../../include/depsolver_cuda.h"
@@ -94,12 +95,13 @@ __global__ void k_givens_init(GivensState gs, const double *__restrict__ beta, i
 // Column j of every active system: h[0..j] (complex, from the two Gram-
 // Schmidt passes) and h[j+1] = |w|; applies the previous rotations, forms
 // the new one, updates g, decides convergence (|g[j+1]| <= itol * beta)
-// and the scale of the next basis vector.
+// and the scale of the next basis vector; a system also stops once it has
+// taken icap[f] steps.
 __global__ void k_givens_step(GivensState gs, const double2 *__restrict__ hacc,
                               const double *__restrict__ hn, int j, int F,
                               const double *__restrict__ beta, const double *__restrict__ itol,
-                              int *__restrict__ active, double *__restrict__ scale,
-                              int *__restrict__ mcount)
+                              const int *__restrict__ icap, int *__restrict__ active,
+                              double *__restrict__ scale, int *__restrict__ mcount)
 {
     grid_dep_wait();
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
@@ -143,7 +145,9 @@ __global__ void k_givens_step(GivensState gs, const double2 *__restrict__ hacc,
     g[j] = cscale(gj, c);
     mcount[f] = j + 1;
     const double est = cabs2(g[j + 1]);
-    if (est <= itol[f] * beta[f] || b == 0.0) {
+    // icap[f]: the system's share of the caller's iteration cap left for
+    // this inner solve
+    if (est <= itol[f] * beta[f] || b == 0.0 || j + 1 >= icap[f]) {
         active[f] = 0;
         scale[f] = 0.0;
     } else {
@@ -910,7 +914,7 @@ struct Session::Mixed {
     DevBuf<float4> hdf;     // the update's coefficients (-Re h, Im h) in double-FP32
     DevBuf<double> nrm, nrm0, scale, betad, itold, gc;
     DevBuf<double2> gH, gsn, gg;  // Givens state per system
-    DevBuf<int> active, act0, act2, mcount;
+    DevBuf<int> active, act0, act2, mcount, icap;
     DevBuf<unsigned long long> cgsb;  // bytes the Gram-Schmidt kernels moved (timing on)
     DevBuf<double> npart;   // per-block partials of |w|^2
     int dots_grid = 0, upd_grid = 0;  // one resident wave of the Gram-Schmidt kernels
@@ -1054,9 +1058,13 @@ __global__ void k_prepare_systems(const int *__restrict__ iface_row, const doubl
     R[(size_t)(2 * f + 1) * ld + i] = r.y;
 }
 
-// One batch of F <= kMaxBatch frequencies.
+// One batch of F <= kMaxBatch frequencies.  status (F) receives each
+// system's outcome (kSysConverged, kSysCapped: max_iters inner iterations
+// taken without reaching tol, kSysStagnated: kOuterMax refinement steps
+// taken); the solution and forces of a system that did not converge are
+// NaN, the others are those of a batch of converged systems alone.
 static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsigned max_iters,
-                       double *sigma_host, double *tot_host, unsigned *iters)
+                       double *sigma_host, double *tot_host, unsigned *iters, int *status)
 {
     Session::Mixed &w = *s.mx;
     const int N = s.N;
@@ -1087,7 +1095,8 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
     DSC_CUDA(cudaMemsetAsync(w.Xs.p, 0, blk * sizeof(double), st));
     std::vector<double> bnorm(F, 0.0);
     const dim3 vg((N + 255) / 256, F);
-    std::vector<int> done(F, 0), total_it(F, 0);
+    constexpr int kRunning = -1;
+    std::vector<int> stat(F, kRunning), total_it(F, 0);
     std::vector<double> rn(F);
     for (int outer = 0; outer <= kOuterMax; outer++) {
         // residual norms
@@ -1095,21 +1104,28 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
         DSC_CUDA(cudaMemcpyAsync(rn.data(), w.nrm.p, F * sizeof(double), cudaMemcpyDeviceToHost, st));
         DSC_CUDA(cudaStreamSynchronize(st));
         if (outer == 0) bnorm = rn;
+        // a system leaves the batch once it has converged, used up its
+        // share of max_iters or the refinement steps; the others go on
         int nact = 0;
         for (int f = 0; f < F; f++) {
-            done[f] = rn[f] <= tol * bnorm[f];
-            nact += !done[f];
+            if (stat[f] != kRunning) continue;
+            if (rn[f] <= tol * bnorm[f]) stat[f] = kSysConverged;
+            else if ((unsigned)total_it[f] >= max_iters) stat[f] = kSysCapped;
+            else if (outer == kOuterMax || !(rn[f] == rn[f])) stat[f] = kSysStagnated;
+            else nact++;
         }
         if (nact == 0) break;
-        if (outer == kOuterMax) {
-            set_error("mixed solve: residual above tolerance after %d refinement steps", kOuterMax);
-            return kErrNoConverge;
-        }
-        // ---- inner GMRES on M e = r for the active systems
-        std::vector<int> act(F), mf(F, 0);
+        // ---- inner GMRES on M e = r for the active systems, each for at
+        // most what is left of its max_iters
+        std::vector<int> act(F), mf(F, 0), icap(F, 0);
         std::vector<double> beta(F), sc(F), itol(F);
+        int jcap = 0;
         for (int f = 0; f < F; f++) {
-            act[f] = !done[f];
+            act[f] = stat[f] == kRunning;
+            if (act[f]) {
+                icap[f] = (int)std::min<unsigned>(kInnerMax, max_iters - (unsigned)total_it[f]);
+                jcap = std::max(jcap, icap[f]);
+            }
             beta[f] = rn[f];
             sc[f] = act[f] && beta[f] > 0 ? 1.0 / beta[f] : 0.0;
             // reduce the residual to a tenth of the target, but not below
@@ -1121,13 +1137,14 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
         DSC_TRY(w.scale.upload(sc, st));
         DSC_TRY(w.betad.upload(beta, st));
         DSC_TRY(w.itold.upload(itol, st));
+        DSC_TRY(w.icap.upload(icap, st));
         DSC_LAUNCH(k_scale_from64<<<vg, 256, 0, st>>>(w.R.p, w.Vb.p, w.Vh.p, w.Vl.p, N, ld, F, w.scale.p,
                                                       w.active.p));
         GivensState gst{w.gH.p, w.gc.p, w.gsn.p, w.gg.p};
         const int gb = (F + 63) / 64;
         DSC_LAUNCH(k_givens_init<<<gb, 64, 0, st>>>(gst, w.betad.p, F, w.mcount.p));
         std::vector<int> hact(F);
-        for (int j = 0; j < kInnerMax; j++) {
+        for (int j = 0; j < jcap; j++) {
             const float2 *vj = w.Vb.p + (size_t)j * blk;
             float2 *vn = w.Vb.p + (size_t)(j + 1) * blk;
             const float *csc = w.cscK.p;
@@ -1182,10 +1199,10 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
             {
                 TimerScope ts(tm, kTKrylov, st);
                 DSC_TRY(launch_dependent(k_givens_step, gb, dim3(64), 0, st, gst, w.hacc.p, w.nrm.p, j, F, w.betad.p,
-                                         w.itold.p, w.active.p, w.scale.p, w.mcount.p));
+                                         w.itold.p, (const int *)w.icap.p, w.active.p, w.scale.p, w.mcount.p));
             }
             DSC_CUDA(cudaGetLastError());
-            if ((j + 1) % 4 == 0 || j + 1 == kInnerMax) {
+            if ((j + 1) % 4 == 0 || j + 1 == jcap) {
                 // poll the converged systems every few steps only
                 DSC_CUDA(cudaMemcpyAsync(hact.data(), w.active.p, F * sizeof(int), cudaMemcpyDeviceToHost, st));
                 DSC_CUDA(cudaStreamSynchronize(st));
@@ -1193,7 +1210,7 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
                 for (int f = 0; f < F; f++) still += hact[f];
                 if (still == 0) break;
             }
-            if (j + 1 < kInnerMax) {
+            if (j + 1 < jcap) {
                 TimerScope ts(tm, kTKrylov, st);
                 DSC_TRY(launch_dependent(k_scale_df, vg, dim3(256), 0, st, w.W.p, vn, w.Vh.p, w.Vl.p, N, ld, F,
                                          w.scale.p, w.active.p));
@@ -1247,7 +1264,7 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
     }
     if (iters)
         for (int f = 0; f < F; f++) iters[f] = (unsigned)total_it[f];
-    (void)max_iters;
+    for (int f = 0; f < F; f++) status[f] = stat[f] == kRunning ? kSysStagnated : stat[f];
     {
         int herr = 0;
         DSC_CUDA(cudaMemcpyAsync(&herr, w.err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -1379,6 +1396,13 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
         set_error("batched field: a shared-memory staging wait gave up (code %d)", herr);
         return kErrCuda;
     }
+    // no result for a system that did not converge
+    const double nan = std::numeric_limits<double>::quiet_NaN();
+    for (int f = 0; f < F; f++) {
+        if (status[f] == kSysConverged) continue;
+        if (tot_host) std::fill(tot_host + (size_t)f * 9, tot_host + (size_t)f * 9 + 9, nan);
+        if (sigma_host) std::fill(sigma_host + (size_t)f * 2 * N, sigma_host + (size_t)(f + 1) * 2 * N, nan);
+    }
     return kOk;
 }
 
@@ -1398,6 +1422,11 @@ int Session::collect_timing(double *ms, int *count, double *work)
 int Session::solve_mixed(unsigned nfreq, const double *freqs, double tol, unsigned max_iters,
                          double *sigma_host, double *forces_host, unsigned *iters)
 {
+    last_status.assign(nfreq, kSysStagnated);
+    if (max_iters == 0) {
+        set_error("mixed solve: max_iters must be at least 1");
+        return kErrArg;
+    }
     DSC_TRY(make_k16());
     if (!mx) mx = new Mixed();
     Mixed &w = *mx;
@@ -1444,6 +1473,7 @@ int Session::solve_mixed(unsigned nfreq, const double *freqs, double tol, unsign
         DSC_TRY(w.nrm0.alloc(Fmax));
         DSC_TRY(w.betad.alloc(Fmax));
         DSC_TRY(w.itold.alloc(Fmax));
+        DSC_TRY(w.icap.alloc(Fmax));
         DSC_TRY(w.gc.alloc((size_t)Fmax * kInnerMax));
         DSC_TRY(w.gsn.alloc((size_t)Fmax * kInnerMax));
         DSC_TRY(w.gg.alloc((size_t)Fmax * (kInnerMax + 1)));
@@ -1472,7 +1502,7 @@ int Session::solve_mixed(unsigned nfreq, const double *freqs, double tol, unsign
         DSC_TRY(mixed_batch(*this, F, freqs + f0, tol, max_iters,
                             sigma_host ? sigma_host + (size_t)f0 * 2 * N : nullptr,
                             forces_host ? forces_host + (size_t)f0 * 9 : nullptr,
-                            iters ? iters + f0 : nullptr));
+                            iters ? iters + f0 : nullptr, last_status.data() + f0));
     }
     return kOk;
 }

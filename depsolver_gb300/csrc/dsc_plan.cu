@@ -6,8 +6,12 @@
 
 #include <algorithm>
 #include <atomic>
+#include <map>
+#include <mutex>
 #include <numeric>
+#include <set>
 #include <thread>
+#include <utility>
 
 #include "dsc_common.cuh"
 #include "dsc_field.h"
@@ -341,17 +345,52 @@ cudaStream_t &alloc_stream()
     return s;
 }
 
+namespace {
+std::mutex g_dev_mu;  // guards the per-device caches below
+std::map<int, int> g_nsm;
+std::map<std::pair<int, const void *>, int> g_smem;
+std::set<int> g_pool_done;
+}  // namespace
+
 int alloc_pool_setup()
 {
-    static bool done[64] = {};
     int dev = 0;
     DSC_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 64 || done[dev]) return kOk;
+    std::lock_guard<std::mutex> lk(g_dev_mu);
+    if (g_pool_done.count(dev)) return kOk;
     cudaMemPool_t pool;
     DSC_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
     uint64_t keep = ~(uint64_t)0;
     DSC_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
-    done[dev] = true;
+    g_pool_done.insert(dev);
+    return kOk;
+}
+
+int current_sm_count(int *nsm)
+{
+    int dev = 0;
+    DSC_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_dev_mu);
+    auto it = g_nsm.find(dev);
+    if (it == g_nsm.end()) {
+        int n = 0;
+        DSC_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+        it = g_nsm.emplace(dev, n).first;
+    }
+    *nsm = it->second;
+    return kOk;
+}
+
+int raise_smem_limit(const void *kern, int bytes)
+{
+    int dev = 0;
+    DSC_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_dev_mu);
+    int &cur = g_smem[{dev, kern}];
+    if (cur < bytes) {
+        DSC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        cur = bytes;
+    }
     return kOk;
 }
 

@@ -18,6 +18,7 @@
 
 #include <algorithm>
 #include <complex>
+#include <limits>
 #include <memory>
 #include <vector>
 
@@ -410,6 +411,21 @@ extern "C" int dsc_session_geometric_matrix(dsc_session *s, int mode, double *K,
     return kOk;
 }
 
+// DSC_OK when every system of the sweep converged, else DSC_ERR_NOCONVERGE
+// naming how many did not (their outcomes: dsc_session_status).
+static int sweep_status(const std::vector<int> &st)
+{
+    int capped = 0, stag = 0;
+    for (int v : st) {
+        capped += v == kSysCapped;
+        stag += v == kSysStagnated;
+    }
+    if (capped + stag == 0) return kOk;
+    set_error("%d of %zu systems did not converge (%d reached max_iters, %d stagnated); their results are NaN",
+              capped + stag, st.size(), capped, stag);
+    return kErrNoConverge;
+}
+
 extern "C" int dsc_session_solve(dsc_session *sess, int mode, unsigned nfreq, const double *freqs,
                                  double tol, unsigned max_iters, double *sigma, double *forces,
                                  unsigned *iters)
@@ -420,16 +436,38 @@ extern "C" int dsc_session_solve(dsc_session *sess, int mode, unsigned nfreq, co
         set_error("dsc_session_solve: unknown mode %d", mode);
         return kErrArg;
     }
-    if (mode == DSC_MODE_MIXED) return s.solve_mixed(nfreq, freqs, tol, max_iters, sigma, forces, iters);
+    if (nfreq && !freqs) {
+        set_error("dsc_session_solve: freqs is NULL");
+        return kErrArg;
+    }
+    if (mode == DSC_MODE_MIXED) {
+        DSC_TRY(s.solve_mixed(nfreq, freqs, tol, max_iters, sigma, forces, iters));
+        return sweep_status(s.last_status);
+    }
     const size_t n2 = 2 * (size_t)s.N;
+    s.last_status.assign(nfreq, kSysStagnated);
     DevBuf<double> sig, tot;
     DSC_TRY(sig.alloc(n2));
     DSC_TRY(tot.alloc(9 * (size_t)std::max(1u, nfreq)));
+    const double nan = std::numeric_limits<double>::quiet_NaN();
     for (unsigned k = 0; k < nfreq; k++) {
         unsigned it = 0;
+        // a frequency whose GMRES stops short (cap or stagnation) gets NaN
+        // results and a status; the sweep goes on with the next one
         int rc = s.solve_fp64(freqs[k], tol, max_iters, sig.p, tot.p + 9 * (size_t)k, &it);
         if (iters) iters[k] = it;
+        if (rc == kErrNoConverge || rc == kErrStagnation) {
+            s.last_status[k] = rc == kErrNoConverge ? kSysCapped : kSysStagnated;
+            DSC_CUDA(cudaStreamSynchronize(s.st));
+            if (sigma) std::fill(sigma + n2 * k, sigma + n2 * (k + 1), nan);
+            std::vector<double> t9(9, nan);
+            DSC_CUDA(cudaMemcpyAsync(tot.p + 9 * (size_t)k, t9.data(), 9 * sizeof(double),
+                                     cudaMemcpyHostToDevice, s.st));
+            DSC_CUDA(cudaStreamSynchronize(s.st));
+            continue;
+        }
         if (rc != kOk) return rc;
+        s.last_status[k] = kSysConverged;
         if (sigma)
             DSC_CUDA(cudaMemcpyAsync(sigma + n2 * k, sig.p, n2 * sizeof(double), cudaMemcpyDeviceToHost,
                                      s.st));
@@ -438,7 +476,14 @@ extern "C" int dsc_session_solve(dsc_session *sess, int mode, unsigned nfreq, co
         DSC_CUDA(cudaMemcpyAsync(forces, tot.p, 9 * (size_t)nfreq * sizeof(double),
                                  cudaMemcpyDeviceToHost, s.st));
     DSC_CUDA(cudaStreamSynchronize(s.st));
-    return kOk;
+    return sweep_status(s.last_status);
+}
+
+extern "C" int dsc_session_status(dsc_session *sess, int *status, unsigned n)
+{
+    const std::vector<int> &st = sess->s.last_status;
+    for (unsigned k = 0; k < n && k < st.size() && status; k++) status[k] = st[k];
+    return (int)st.size();
 }
 
 extern "C" int dsc_sweep(int nen, unsigned N, unsigned E, const double *nodes, const unsigned *elems,

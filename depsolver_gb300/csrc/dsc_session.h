@@ -105,6 +105,8 @@ struct Session {
     int collect_timing(double *ms, int *count, double *work);
     int solve_mixed(unsigned nfreq, const double *freqs, double tol, unsigned max_iters,
                     double *sigma_host, double *forces_host, unsigned *iters);
+    // outcome of each system of the last solve (SysStatus)
+    std::vector<int> last_status;
 };
 
 }  // namespace dsc

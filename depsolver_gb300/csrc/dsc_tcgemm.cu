@@ -430,15 +430,18 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
 {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    if (!fn) {
+    // looked up once (a function-local static is initialised exactly once,
+    // whichever thread gets here first)
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
         void *p = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
                 cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
-    }
+            return (PFN_cuTensorMapEncodeTiled_v12000)p;
+        cudaGetLastError();
+        return (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
+    }();
     return fn;
 }
 
@@ -518,25 +521,15 @@ static int tc_launch(int amode, const CUtensorMap &ah, const CUtensorMap &al, co
     const int kps = (nkb + splits - 1) / splits;
     const size_t smem = 1024 + (size_t)kTcStages * (amode == 4 ? kTcBM + BN : 2 * kTcBM + 2 * BN) * kTcRowBytes + 256;
     // persistent: one CTA per SM walks the (row tile, split) units
-    static int nsm = 0;
-    if (!nsm) {
-        int dev = 0;
-        DSC_CUDA(cudaGetDevice(&dev));
-        DSC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    }
+    int nsm = 0;
+    DSC_TRY(current_sm_count(&nsm));
     const int units = (M + kTcBM - 1) / kTcBM * ntn * splits;
     const dim3 grid(std::min(units, nsm));
     // the shared-memory limit of each instantiation is raised to the largest
     // request seen on the device (once per size, not per launch)
-    constexpr int kDevs = 16;
-    static int smem_set[kDevs][6] = {};
-    int dev = 0;
-    DSC_CUDA(cudaGetDevice(&dev));
     auto launch = [&](auto kern, int slot) -> int {
-        if (dev >= kDevs || smem_set[dev][slot] < (int)smem) {
-            DSC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            if (dev < kDevs) smem_set[dev][slot] = (int)smem;
-        }
+        (void)slot;
+        DSC_TRY(raise_smem_limit((const void *)kern, (int)smem));
         DSC_TRY(launch_dependent(kern, grid, dim3(kTcThreads), smem, st, ah, al, bh, bl, M, Nc, BN, ntn, nkb, kps,
                                  splits, Y, ldy, ldy * (size_t)Nc, tmem_cols, acc_stride, rsc, csc, gj_k, d_err));
         return kOk;

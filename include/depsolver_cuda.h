@@ -165,7 +165,18 @@ int dsc_force_mst(int nen, unsigned N, unsigned E, const double *nodes, const un
  * forces receives 9 doubles per frequency: Fcm[3], Xcm[3] and the sum over
  * particle elements of |Fce| per component (the scale of the net force).
  * sigma (may be NULL) receives 2N doubles per frequency (Re then Im).
- * iters (may be NULL) receives the iteration count per frequency. */
+ * iters (may be NULL) receives the iteration count per frequency.
+ * max_iters caps each system's GMRES iterations: per frequency in the FP64
+ * mode (the reference's MAX_ITERS, src/gmres_el.c:42-50), and the inner
+ * iterations summed over the refinement steps in the mixed mode.
+ *
+ * A system that does not converge does not stop the sweep: its sigma and
+ * forces are NaN, the others are returned as usual, and the call returns
+ * DSC_ERR_NOCONVERGE (the reference's GMRES exits instead,
+ * src/gmres_el.c:123-126,233-236).  dsc_session_status gives each system's
+ * outcome: DSC_SYS_CONVERGED, DSC_SYS_CAPPED (max_iters reached) or
+ * DSC_SYS_STAGNATED (the FP64 GMRES's "CONVERGENCE RATE TOO SLOW", or the
+ * mixed mode's refinement steps used up). */
 #define DSC_MODE_FP64 1
 #define DSC_MODE_MIXED 2
 
@@ -211,6 +222,12 @@ int dsc_session_set_field_tensor(dsc_session *s, int on);
 int dsc_session_geometric_matrix(dsc_session *s, int mode, double *K, size_t ldk);
 int dsc_session_solve(dsc_session *s, int mode, unsigned nfreq, const double *freqs, double tol,
                       unsigned max_iters, double *sigma, double *forces, unsigned *iters);
+#define DSC_SYS_CONVERGED 0
+#define DSC_SYS_CAPPED 1
+#define DSC_SYS_STAGNATED 2
+/* Outcome of each system of the session's last solve: writes up to n of
+ * them to status (may be NULL) and returns how many systems it solved. */
+int dsc_session_status(dsc_session *s, int *status, unsigned n);
 /* CUDA-event timing of kernel classes (off by default).  Since the last
  * call: ms[k] the summed time of class k, count[k] its timed scopes and
  * work[k] its algorithmic work (any of the three may be NULL; n entries):
@@ -282,14 +299,16 @@ int dsc_tc_gemm(int M, int Nc, int Kd, const double *A, const double *B, double 
  * about 4 * Nc * (2 * round_up(Kd, 32) + splits * M) bytes, is rejected
  * with DSC_ERR_ARG and a message naming both sizes.
  *
- * The work runs on `stream` (a cudaStream_t; NULL = the default stream) and
- * the call returns once it has finished, with the status of the kernels'
- * bounded waits.  The first call on each device looks up the scratch's
- * address (cudaGetSymbolAddress) and keeps it: make that call during
- * set-up, before any stream capture begins, and do not call again on a
- * device after cudaDeviceReset.  All calls on a device share its scratch,
- * so two calls that overlapped would race on it; the library prevents that
- * with a process-wide lock held until a call's work has finished. */
+ * The call is synchronous: it queues its kernels on `stream` (a
+ * cudaStream_t; NULL = the default stream), then copies the kernels' status
+ * word back and synchronises `stream` on the host, so it returns only once
+ * Y is written, with the status of the kernels' bounded waits.  The first
+ * call on each device also looks up the scratch's address
+ * (cudaGetSymbolAddress) and keeps it: make that first call during set-up,
+ * before any stream capture begins, and do not call again on a device after
+ * cudaDeviceReset.  All calls on a device share its scratch, so two calls
+ * that overlapped would race on it; the library prevents that with a
+ * process-wide lock held until a call's work has finished. */
 #define DSC_NOALLOC_SCRATCH_BYTES 33554432u /* 32 MiB */
 int dsc_tc_gemm_noalloc(int M, int Nc, int Kd, const float *A, size_t lda, const double *B,
                         size_t ldb, double *Y, size_t ldy, int splits, void *stream);

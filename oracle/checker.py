@@ -22,7 +22,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libdsref.so")
-REF_SRC = os.environ.get("DSC_REFERENCE_SRC", "/root/reference/src")
+# the reference tree beside the repository (../reference from its root),
+# unless DSC_REFERENCE_SRC names its src directory
+REF_SRC = os.environ.get("DSC_REFERENCE_SRC",
+                         os.path.normpath(os.path.join(HERE, "..", "..", "reference", "src")))
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _up = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")

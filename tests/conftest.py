@@ -9,7 +9,9 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
-REFERENCE = os.environ.get("DSC_REFERENCE", "/root/reference")
+# the reference tree beside the repository (../reference from its root),
+# unless DSC_REFERENCE names it; tests that need it skip where it is absent
+REFERENCE = os.environ.get("DSC_REFERENCE", os.path.normpath(os.path.join(ROOT, "..", "reference")))
 
 
 def pytest_configure(config):

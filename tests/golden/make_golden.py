@@ -3,7 +3,10 @@
 Run where the reference sources exist (it builds oracle/_ref/libdsref.so
 from them):
 
-    python tests/golden/make_golden.py [--reference /root/reference]
+    python tests/golden/make_golden.py [--reference DIR]
+
+DIR defaults to the reference tree beside the repository (../reference from
+the repository's root).
 
 Fixtures (NumPy .npz, all FP64 bit patterns straight from the reference's
 own functions through oracle/ref_harness.c):
@@ -112,7 +115,8 @@ def dep_trap_2(ref, examples, path):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference",
+                    default=os.path.normpath(os.path.join(HERE, "..", "..", "..", "reference")))
     args = ap.parse_args()
     os.environ["DSC_REFERENCE_SRC"] = os.path.join(args.reference, "src")
     from oracle import checker

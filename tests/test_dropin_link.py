@@ -1,4 +1,4 @@
-"""The link recipe of INTEGRATION.md: the reference's own driver objects,
+"""The library's link recipe: the reference's own driver objects,
 its force.c with the MST functions renamed, and libdepsolver_cuda.so make a
 depSolver executable whose hot-path calls resolve to the library.
 

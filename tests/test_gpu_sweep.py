@@ -168,3 +168,47 @@ def test_field_tensor_cores_match_fp32_pipes(gpu):
         assert np.abs(f_tc[k, :3] - f_32[k, :3]).max() <= 1e-7 * scale, k
         assert np.allclose(f_tc[k, 6:9], f_32[k, 6:9], rtol=1e-5), k
         assert np.abs(f_tc[k, :3] - f64[k, :3]).max() <= FORCE_TOL * scale, k
+
+
+@pytest.mark.parametrize("mode", [api.MODE_MIXED, api.MODE_FP64])
+def test_iteration_cap_reports_capped_systems(gpu, mode):
+    """max_iters caps every system's GMRES iterations; systems that stop
+    short get the status SYS_CAPPED and NaN results (no fake solution), the
+    call reports DSC_ERR_NOCONVERGE, and the next uncapped sweep on the same
+    session is that of a fresh session."""
+    from depsolver_gb300 import _native
+    sc = scenes.small(nen=6)
+    freqs = [1e4, 1e6, 5e7]
+    s = api.Session(sc)
+    with pytest.raises(_native.DscError) as e:
+        s.solve(freqs, mode=mode, tol=1e-11, max_iters=1)
+    assert e.value.status == api.ERR_NOCONVERGE
+    f, its, sig = s.solve(freqs, mode=mode, tol=1e-11, max_iters=1, want_sigma=True, partial=True)
+    assert (s.status() == api.SYS_CAPPED).all(), s.status()
+    assert np.isnan(f).all() and np.isnan(sig).all()
+    assert (its == 1).all(), its
+    f2, it2, s2 = s.solve(freqs, mode=mode, tol=1e-11, want_sigma=True)
+    assert (s.status() == api.SYS_CONVERGED).all() and (it2 > 1).all()
+    f3, it3, s3 = api.Session(sc).solve(freqs, mode=mode, tol=1e-11, want_sigma=True)
+    assert np.array_equal(f2, f3) and np.array_equal(s2, s3) and np.array_equal(it2, it3)
+
+
+def test_iteration_cap_between_systems(gpu):
+    """A cap between the iteration counts of two systems of one batch stops
+    only the slower one: the faster one's result is that of an uncapped
+    sweep."""
+    sc = scenes.small(nen=6, sphere_level=2, plate_cells=4)
+    freqs = np.logspace(3, 8, 6)
+    s = api.Session(sc)
+    s.set_preconditioner(False)   # more spread in the iteration counts
+    f0, it0, s0 = s.solve(freqs, mode=api.MODE_MIXED, tol=1e-11, want_sigma=True)
+    assert it0.min() < it0.max(), it0
+    cap = int(it0.min())
+    f1, it1, s1 = s.solve(freqs, mode=api.MODE_MIXED, tol=1e-11, max_iters=cap, want_sigma=True,
+                          partial=True)
+    st = s.status()
+    fast = it0 <= cap
+    assert (st[fast] == api.SYS_CONVERGED).all() and (st[~fast] == api.SYS_CAPPED).all(), (st, it0)
+    assert np.isnan(f1[~fast]).all() and not np.isnan(f1[fast]).any()
+    for k in np.nonzero(fast)[0]:
+        assert relerr(s1[k], s0[k]) < 1e-9
