@@ -249,6 +249,112 @@ def cpu_baseline(sc, nthreads: int, sample_div: int = 8, full_first: bool = True
             "full": info}
 
 
+# ------------------------------------------------------------------ position sweep
+NPOS = 128
+
+
+def position_bench(args, with_cpu: bool):
+    """The batched frequency and position sweep on the config-0 plates: 128
+    seeded sphere centres (levels 2, 3, 4 drawn per position: N = 1524, 3444
+    or 11124) x the 64 frequencies, every system to 1e-10, in one
+    dsc_positions_solve call.  Timed by the host clock around the call with
+    the device synchronised on both sides (the positions' kernels run on
+    several streams); the systems' inputs are host arrays by construction
+    (each position's mesh is built and uploaded inside the call), so the
+    number is end to end."""
+    import torch
+
+    from depsolver_gb300 import api, scenes
+    fixed = scenes.plates_only(10)
+    lev, cen = scenes.cfg3_positions(NPOS)
+    ps = api.PositionSweep(fixed)
+    tid = {}
+    for lv in (2, 3, 4):
+        tid[lv] = ps.add_particle(*scenes.icosphere(lv, 1.0))
+    tm = np.array([tid[int(v)] for v in lev], dtype=np.uint32)
+    Ns = {lv: fixed.N + scenes.icosphere(lv, 1.0)[0].shape[0] for lv in (2, 3, 4)}
+    # warm-up: a few positions of every size (grows the device memory pool)
+    warm = [int(np.nonzero(lev == lv)[0][0]) for lv in (4, 3, 2)] * 2
+    for _ in range(max(1, args.warmup - 2)):
+        ps.solve(tm[warm], cen[warm], FREQS, tol=TOL)
+    ps.set_timing(True)
+    ps.timing()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    r = ps.solve(tm, cen, FREQS, tol=TOL)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    timing = ps.timing()
+    nsys = NPOS * NFREQ
+    value = nsys / wall
+    # roofline of the dominant class: the library counts the flops of every
+    # product (12 F N^2); a product moves 4 N^2 + 16 F N bytes, i.e.
+    # 1/(3F) + 4/(3N) bytes per flop -- nearly independent of N, so the
+    # positions' mean converts the summed flops to bytes
+    P = peaks()
+    hbm = P.get("hbm_gbs") or 6800.0
+    src = "MEASURED_PEAKS.json hbm_gbs, of measured" if P else "fallback"
+    ms, cnt, wk = timing["gemm_K"]
+    byts = 0.0
+    for lv, n in Ns.items():
+        k = int((lev == lv).sum())
+        byts += k * (4.0 * n * n + 16.0 * NFREQ * n) / (12.0 * NFREQ * n * n)
+    bpf = byts / NPOS
+    roof = None
+    if cnt and ms > 0:
+        ach = wk * bpf * 1e-9 / (ms / 1e3)
+        roof = {"kernel": "gemm_K", "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+                "frac": ach / hbm, "traffic": None, "peak_source": src, "ms": ms, "scopes": cnt,
+                "note": "kernels of several positions overlap on the GPU: per-kernel times include "
+                        "the sharing, so the fraction is a lower bound"}
+    # accuracy: one position of every size against FP64 solves of the same
+    # scene at 8 of the frequencies
+    chk = np.linspace(0, NFREQ - 1, 8).astype(int)
+    ferr, serr = [], []
+    for lv in (2, 3, 4):
+        q = int(np.nonzero(lev == lv)[0][0])
+        sc = scenes.sphere_between_plates(lv, 10, center=tuple(cen[q]))
+        s = api.Session(sc)
+        f64, _, _ = s.solve(FREQS[chk], mode=api.MODE_FP64, tol=1e-12)
+        s.close()
+        for j, k in enumerate(chk):
+            ferr.append(float(np.abs(r["forces"][q, k, :3] - f64[j, :3]).max() / f64[j, 6:9].sum()))
+    xo = r["crossover_hz"]
+    fin = np.isfinite(xo)
+    out = {"workload": "cfg3: 128 seeded sphere centres (uniform in [-4,4]^2 x [-3,3]) between the "
+                       "config-0 plates, sphere levels 2/3/4 drawn per position, x 64 frequencies "
+                       "1 kHz..100 MHz, tol 1e-10",
+           "value": value, "unit": UNIT, "systems": nsys, "wall_s": wall,
+           "positions_per_level": {str(lv): int((lev == lv).sum()) for lv in (2, 3, 4)},
+           "N_per_level": {str(lv): n for lv, n in Ns.items()},
+           "workers": 4, "conductor_inversions": ps.inversions(),
+           "e2e": {"value": value, "unit": UNIT, "note": "the call takes host arrays; same number"},
+           "roofline": roof,
+           "force_err_vs_fp64_max": max(ferr), "force_err_checked": len(ferr),
+           "inner_iterations_mean": float(r["iters"].mean()),
+           "crossover": {"positions_with_sign_change": int(fin.sum()),
+                         "median_hz": float(np.median(xo[fin])) if fin.any() else None,
+                         "per_position_hz": [None if not np.isfinite(v) else float(v) for v in xo]},
+           "kernels_ms": {k: v[0] for k, v in timing.items()}}
+    if with_cpu:
+        # the C restatement on the host cores, one position of each size
+        # (a full solve at 1e-6 then a 1/8 row sample), weighted by the
+        # positions per size
+        est = 0.0
+        for lv in (2, 3, 4):
+            q = int(np.nonzero(lev == lv)[0][0])
+            sc = scenes.sphere_between_plates(lv, 10, center=tuple(cen[q]))
+            cb = cpu_baseline(sc, os.cpu_count() or 1)
+            est += int((lev == lv).sum()) * cb["est_solve_s"]
+        est /= NPOS
+        out["cpu_baseline"] = {"value": 1.0 / est, "unit": UNIT, "cores": os.cpu_count() or 1,
+                               "kind": "port", "sample": "one position of each sphere level, one "
+                               "frequency each (full solve at the reference's 1e-6, then a 1/8 row "
+                               "sample scaled x8), weighted by the positions per level"}
+    ps.close()
+    return out
+
+
 # ------------------------------------------------------------------ ours
 def max_over_ranks(ms: float, world: int, device: str) -> float:
     """The slowest rank's time (every rank gets it): replicas share no data,
@@ -397,6 +503,7 @@ def run_ours(args, rank, world):
 
     if rank != 0:
         return
+    pos = position_bench(args, with_cpu=not args.no_cpu) if not args.no_positions else None
     # roofline of the dominant kernel class over the timed region: achieved
     # = algorithmic work (counted by the library per class) / CUDA-event time
     # of the class on the session's stream
@@ -421,6 +528,7 @@ def run_ours(args, rank, world):
                       "gmres_iters": int(itf[0])},
         "speedup_vs_fp64_path": value / world / (1.0 / fp64_s),
         "speedup_parts": ablation,
+        "position_sweep": pos,
         "inner_iterations": {"mean": float(np.mean(its)), "max": int(np.max(its)),
                              "products_per_step": timing["gemm_K"][1] // max(1, args.steps)},
         "accuracy": {"force_err_vs_fp64": float(ferrs.max()),
@@ -480,6 +588,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-positions", action="store_true", help="skip the position sweep (cfg3)")
     ap.add_argument("--scene", choices=["cfg1", "mid"], default="cfg1",
                     help="mid: a smaller scene for ncu captures (with --only-step)")
     ap.add_argument("--mixed-assembly", choices=["fp32", "df32"], default="fp32",

@@ -71,6 +71,27 @@ def lib() -> C.CDLL:
         L.dsc_tc_gemm_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_size_t,
                                           C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.c_int,
                                           C.c_void_p]
+        L.dsc_positions_create.restype = C.c_int
+        L.dsc_positions_create.argtypes = [C.c_int, C.c_uint, C.c_uint, _dp, _up, _up, _dp, C.c_uint,
+                                           C.c_void_p, C.c_uint, _dp, C.POINTER(C.c_void_p)]
+        L.dsc_positions_destroy.restype = None
+        L.dsc_positions_destroy.argtypes = [C.c_void_p]
+        L.dsc_positions_add_particle.restype = C.c_int
+        L.dsc_positions_add_particle.argtypes = [C.c_void_p, C.c_uint, C.c_uint, _dp, _up, C.c_uint]
+        for nm in ("dsc_positions_set_workers", "dsc_positions_set_mixed_assembly",
+                   "dsc_positions_set_timing"):
+            getattr(L, nm).restype = C.c_int
+            getattr(L, nm).argtypes = [C.c_void_p, C.c_int]
+        L.dsc_positions_timing.restype = C.c_int
+        L.dsc_positions_timing.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        L.dsc_positions_inversions.restype = C.c_int
+        L.dsc_positions_inversions.argtypes = [C.c_void_p]
+        L.dsc_positions_solve.restype = C.c_int
+        L.dsc_positions_solve.argtypes = [C.c_void_p, C.c_uint, _up, _dp, C.c_uint, _dp, C.c_double,
+                                          C.c_uint, _dp, C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.c_void_p]
+        L.dsc_force_crossover.restype = C.c_double
+        L.dsc_force_crossover.argtypes = [C.c_uint, _dp, _dp, C.c_void_p]
         L.dsc_session_stream.restype = C.c_void_p
         L.dsc_session_stream.argtypes = [C.c_void_p]
         L.dsc_kernel_launches.restype = C.c_ulonglong

@@ -242,3 +242,91 @@ def sweep(sc: Scene, freqs, mode: int = MODE_MIXED, tol: float = 1e-10, max_iter
                               sig.ctypes.data if sig is not None else None, forces.ctypes.data,
                               its.ctypes.data))
     return forces, its, sig
+
+
+class PositionSweep:
+    """Particle-position sweeps (dsc_positions_*): a fixed part of the scene
+    (electrodes) and particle meshes of any size, solved at many positions
+    and frequencies per call -- the work of many depSolver-sft runs
+    (src/depSolver-shift.c:129-133,212-217)."""
+
+    def __init__(self, fixed: Scene):
+        L = _native.lib()
+        self._L = L
+        self.fixed = fixed
+        self.sizes = []
+        h = C.c_void_p()
+        ifc = _u(fixed.ifaces)
+        _native.check(L.dsc_positions_create(fixed.nen, fixed.N, fixed.E, _f(fixed.nodes),
+                                             _u(fixed.elems), _u(fixed.bctype), _f(fixed.mbc),
+                                             fixed.n_if, ifc.ctypes.data if fixed.n_if else None,
+                                             fixed.mat.shape[0], _f(fixed.mat), C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if self._h:
+            self._L.dsc_positions_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_particle(self, nodes, elems0, iface: int = 1) -> int:
+        """A particle mesh: nodes about its own origin, 0-based elements."""
+        nodes = _f(nodes)
+        el = _u(np.asarray(elems0) + 1)
+        r = self._L.dsc_positions_add_particle(self._h, nodes.shape[0], el.shape[0], nodes, el, iface)
+        if r < 0:
+            _native.check(-r)
+        self.sizes.append(nodes.shape[0])
+        return r
+
+    def set_workers(self, n: int):
+        _native.check(self._L.dsc_positions_set_workers(self._h, int(n)))
+
+    def set_mixed_assembly(self, prec: int):
+        _native.check(self._L.dsc_positions_set_mixed_assembly(self._h, int(prec)))
+
+    def set_timing(self, on: bool):
+        _native.check(self._L.dsc_positions_set_timing(self._h, int(on)))
+
+    def timing(self):
+        ms = np.zeros(len(TIMER_NAMES))
+        cnt = np.zeros(len(TIMER_NAMES), dtype=np.int32)
+        wk = np.zeros(len(TIMER_NAMES))
+        _native.check(self._L.dsc_positions_timing(self._h, ms.ctypes.data, cnt.ctypes.data,
+                                                   wk.ctypes.data, len(TIMER_NAMES)))
+        return {n: (float(ms[k]), int(cnt[k]), float(wk[k])) for k, n in enumerate(TIMER_NAMES)}
+
+    def inversions(self) -> int:
+        return int(self._L.dsc_positions_inversions(self._h))
+
+    def solve(self, particles, centres, freqs, tol: float = 1e-10, max_iters: int = 600,
+              want_sigma: bool = False, partial: bool = False):
+        """Returns a dict: forces (P x F x 9), iters (P x F), status (P x F),
+        crossover_hz (P), sigma (list of F x 2N_q arrays, or None)."""
+        tp = _u(np.atleast_1d(particles))
+        ce = _f(np.asarray(centres, dtype=np.float64).reshape(-1, 3))
+        fr = _f(np.atleast_1d(freqs))
+        P, F = tp.shape[0], fr.shape[0]
+        forces = np.zeros((P, F, 9))
+        its = np.zeros((P, F), dtype=np.uint32)
+        st = np.zeros((P, F), dtype=np.int32)
+        xo = np.zeros(P)
+        Ns = [self.fixed.N + self.sizes[t] for t in tp]
+        sig = np.zeros(sum(2 * n * F for n in Ns)) if want_sigma else None
+        rc = self._L.dsc_positions_solve(self._h, P, tp, ce, F, fr, tol, max_iters, forces,
+                                         its.ctypes.data, st.ctypes.data, xo.ctypes.data,
+                                         sig.ctypes.data if sig is not None else None)
+        if not (partial and rc == ERR_NOCONVERGE):
+            _native.check(rc)
+        sigmas = None
+        if sig is not None:
+            sigmas, o = [], 0
+            for n in Ns:
+                sigmas.append(sig[o:o + 2 * n * F].reshape(F, 2 * n))
+                o += 2 * n * F
+        return {"forces": forces, "iters": its, "status": st, "crossover_hz": xo, "sigma": sigmas}

@@ -95,6 +95,7 @@ int precond_plan(Session &s)
         no += n;
         to += (size_t)kPB * ldx;
     }
+    pc.nodes_h = all;
     DSC_TRY(pc.nodes.upload(all, s.st));
     DSC_TRY(pc.rblk.upload(rblk, s.st));
     DSC_TRY(pc.rpos.upload(rpos, s.st));
@@ -480,12 +481,63 @@ int precond_build(Session &s)
     return kOk;
 }
 
+int precond_export(Session &s, PrecondShare &sh)
+{
+    Precond &pc = *s.pre;
+    if (!pc.ready) {
+        set_error("precond_export: the session's inverses are not built");
+        return kErrArg;
+    }
+    AllocStreamScope plain(nullptr);  // the share outlives the session's stream
+    sh.nb = pc.nb;
+    sh.n = pc.n;
+    sh.nodes_h = pc.nodes_h;
+    if (!pc.nb) return kOk;
+    sh.xtot = pc.xoff.back() + (size_t)pc.ldx.back() * pc.ldx.back();
+    sh.rtot = pc.noff.back() + pc.n.back();
+    DSC_TRY(sh.Xh.alloc(sh.xtot));
+    DSC_TRY(sh.Xl.alloc(sh.xtot));
+    DSC_TRY(sh.rs.alloc(sh.rtot));
+    DSC_TRY(sh.zbound.alloc(1));
+    DSC_CUDA(cudaMemcpyAsync(sh.Xh.p, pc.Xh.p, sh.xtot * sizeof(__half), cudaMemcpyDeviceToDevice, s.st));
+    DSC_CUDA(cudaMemcpyAsync(sh.Xl.p, pc.Xl.p, sh.xtot * sizeof(__half), cudaMemcpyDeviceToDevice, s.st));
+    DSC_CUDA(cudaMemcpyAsync(sh.rs.p, pc.rs.p, sh.rtot * sizeof(float), cudaMemcpyDeviceToDevice, s.st));
+    DSC_CUDA(cudaMemcpyAsync(sh.zbound.p, pc.zbound.p, sizeof(unsigned), cudaMemcpyDeviceToDevice, s.st));
+    DSC_CUDA(cudaStreamSynchronize(s.st));
+    return kOk;
+}
+
+int precond_adopt(Session &s, const PrecondShare &sh)
+{
+    Precond &pc = *s.pre;
+    if (sh.nb != pc.nb || sh.n != pc.n || sh.nodes_h != pc.nodes_h) {
+        set_error("precond_adopt: the session's conductor blocks differ from the shared ones");
+        return kErrArg;
+    }
+    if (pc.nb) {
+        DSC_TRY(pc.Xh.alloc(sh.xtot));
+        DSC_TRY(pc.Xl.alloc(sh.xtot));
+        DSC_TRY(pc.rs.alloc(sh.rtot));
+        DSC_TRY(pc.zbound.alloc(1));
+        DSC_CUDA(cudaMemcpyAsync(pc.Xh.p, sh.Xh.p, sh.xtot * sizeof(__half), cudaMemcpyDeviceToDevice, s.st));
+        DSC_CUDA(cudaMemcpyAsync(pc.Xl.p, sh.Xl.p, sh.xtot * sizeof(__half), cudaMemcpyDeviceToDevice, s.st));
+        DSC_CUDA(cudaMemcpyAsync(pc.rs.p, sh.rs.p, sh.rtot * sizeof(float), cudaMemcpyDeviceToDevice, s.st));
+        DSC_CUDA(cudaMemcpyAsync(pc.zbound.p, sh.zbound.p, sizeof(unsigned), cudaMemcpyDeviceToDevice, s.st));
+    }
+    pc.ready = true;
+    pc.adopted = true;
+    return kOk;
+}
+
 // ------------------------------------------------------------------ apply
 
 int precond_reserve(Session &s, int F)
 {
     Precond &pc = *s.pre;
-    if (!pc.nb || pc.F >= F) return kOk;
+    // the partial tiles' layout follows F (split stride ldx x 2F), so it is
+    // laid out again whenever a batch has another size than the last one;
+    // the buffers only grow
+    if (!pc.nb || pc.F == F) return kOk;
     pc.S.clear();
     pc.yoff.clear();
     pc.boff.clear();

@@ -34,7 +34,7 @@ struct Precond {
     std::vector<int> S;               // split count of block b's product
     std::vector<size_t> yoff;         // block b's partial tiles in Y
     std::vector<size_t> boff;         // block b's operand pairs in Bh, Bl, G
-    int F = 0;                        // systems the apply workspace is sized for
+    int F = 0;                        // systems the apply workspace is laid out for
     DevBuf<int> nodes;                // rows of each block, ascending
     DevBuf<int> rblk, rpos;           // per row: its block (-1: none) and position
     DevBuf<float> X;                  // scaled blocks (column-major), inverted in place
@@ -52,7 +52,26 @@ struct Precond {
     DevBuf<long long> yinfo;          // per block: Y offset, split stride, S (device copy)
     DevBuf<unsigned> zbound;          // FP32 bits of a bound on |P^-1 v| for |v| <= 1
     DevBuf<float> cz;                 // the K product's column factors of z's pair
+    std::vector<int> nodes_h;         // host copy of `nodes`
     bool ready = false;               // the inverses match the current K
+    // the inverses were copied from a PrecondShare (blocks of a part of the
+    // scene that every assembly of this session leaves unchanged): a new
+    // assembly of K keeps them
+    bool adopted = false;
+};
+
+// The inverses of one session's blocks, kept apart from any session so that
+// sessions of other scenes with the same conductor blocks (the fixed
+// electrodes of a position sweep: the same nodes, elements and rows) can
+// take them instead of inverting again.  Device memory from cudaMalloc,
+// tied to no stream.
+struct PrecondShare {
+    int nb = 0;
+    std::vector<int> n, nodes_h;
+    size_t xtot = 0, rtot = 0;
+    DevBuf<__half> Xh, Xl;
+    DevBuf<float> rs;
+    DevBuf<unsigned> zbound;
 };
 
 // Blocks from the mesh and the conductor rows (once per session; no blocks
@@ -60,6 +79,11 @@ struct Precond {
 int precond_plan(Session &s);
 // The inverses for the current K64 (after each assembly).
 int precond_build(Session &s);
+// Copies a built session's inverses into sh (waits for the copies).
+int precond_export(Session &s, PrecondShare &sh);
+// Takes sh's inverses for s when s has the same blocks (same rows in the
+// same order); returns kErrArg, touching nothing, when it has not.
+int precond_adopt(Session &s, const PrecondShare &sh);
 // Workspace of the apply calls for F systems.
 int precond_reserve(Session &s, int F);
 // z = P^-1 v for the 2F columns of the double-FP32 block V (Re, Im of each

@@ -204,7 +204,7 @@ int Session::assemble64(bool need_fp64)
     const int want = need_fp64 ? kAsmF64 : mixed_asm;
     if (k64_ready && k64_prec <= want) return kOk;
     k16_ready = false;  // the fp16 copies and the preconditioner follow K
-    if (pre) pre->ready = false;
+    if (pre && !pre->adopted) pre->ready = false;
     DSC_TRY(K64.alloc(ld * N));
     // the force plan is joined only before the singular pairs, which store
     // the gradients its points take

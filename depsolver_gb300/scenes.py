@@ -308,6 +308,38 @@ def quadrupole_trap(nen: int = 6, seed: int = 7, levels=(3, 3, 4, 4),
     return _assemble(parts, nen, mat, ifaces, freq, f"quadrupole-trap-tria{nen}")
 
 
+def plates_only(plate_cells: int = 10, *, nen: int = 6, plate_side: float = 20.0,
+                plate_z: float = 5.0, volts: float = 1.0, freq: float = 1.0e6,
+                medium=(1.0e-4, 78.0), particle=(1.0e-3, 2.5)) -> Scene:
+    """The fixed part of a position sweep: the two plate electrodes of
+    :func:`sphere_between_plates` (materials and interface 1 = medium /
+    particle as there), without the sphere."""
+    top_n, top_e = plate(plate_side, plate_side, plate_cells, plate_cells, (0, 0, plate_z), nen)
+    bot_n, bot_e = plate(plate_side, plate_side, plate_cells, plate_cells, (0, 0, -plate_z), nen)
+    parts = [(top_n, top_e, "conductor", volts), (bot_n, bot_e, "conductor", -volts)]
+    return _assemble(parts, nen, [list(medium), list(particle)], [[1, 2]], freq,
+                     f"plates-{plate_cells}x{plate_cells}-tria{nen}")
+
+
+def cfg3_positions(n: int = 128, seed: int = 3, levels=(2, 3, 4), radius: float = 1.0,
+                   box=((-4.0, 4.0), (-4.0, 4.0), (-3.0, 3.0)), plate_z: float = 5.0):
+    """Seeded sphere positions of the batched position sweep on the config-0
+    plates: centres uniform in the box, each sphere's mesh level drawn
+    uniformly from `levels`; centres whose sphere would reach a plate are
+    drawn again.  Returns (levels (n,), centres (n, 3))."""
+    rng = np.random.default_rng(seed)
+    lev = np.empty(n, dtype=np.int64)
+    cen = np.empty((n, 3))
+    for q in range(n):
+        while True:
+            c = np.array([rng.uniform(*box[0]), rng.uniform(*box[1]), rng.uniform(*box[2])])
+            if abs(c[2]) + radius < plate_z - 0.05:
+                break
+        cen[q] = c
+        lev[q] = rng.choice(np.asarray(levels))
+    return lev, cen
+
+
 def shifted(scene: Scene, first_node: int, delta) -> Scene:
     """Rigid shift of nodes first_node.. (0-based) by delta, as the
     reference's position-sweep driver does (src/depSolver-shift.c:212-217)."""

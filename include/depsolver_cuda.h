@@ -313,6 +313,63 @@ int dsc_tc_gemm(int M, int Nc, int Kd, const double *A, const double *B, double 
 int dsc_tc_gemm_noalloc(int M, int Nc, int Kd, const float *A, size_t lda, const double *B,
                         size_t ldb, double *Y, size_t ldy, int splits, void *stream);
 
+/* ------------------------------------------------------- position sweeps
+ * Replaces a series of depSolver-sft runs, each of which shifts nodes
+ * pNodes..nNodes-1 (the particle) rigidly by the REPOSITION vector and
+ * solves the whole system again (src/depSolver-shift.c:129-133,212-217).
+ * A position-sweep object holds a fixed part of the scene -- N nodes, E
+ * elements, bctype (2N), mbc (2N x 3), materials and interfaces, in the
+ * reference's input model as for dsc_session_create -- and particle meshes
+ * added with dsc_positions_add_particle (any number of nodes each, node
+ * coordinates about the particle's own origin, elements 1-based within the
+ * particle, one interface id; its nodes get boundary type 6, so its
+ * Maxwell-stress force is computed).
+ *
+ * dsc_positions_solve solves, for each of npos positions q (particle
+ * tmpl[q] with its origin at centres[3q..3q+2]), the scene "fixed part's
+ * nodes, then the particle's nodes + centre" at nfreq frequencies, every
+ * system in the mixed mode to relative residual tol (DSC_MODE_MIXED of
+ * dsc_session_solve).  The fixed part's conductor-block inverses are
+ * computed once and reused by every position.  Outputs, position-major:
+ * forces (npos x nfreq x 9, as dsc_session_solve), iters (npos x nfreq, may
+ * be NULL), status (npos x nfreq, DSC_SYS_*), crossover_hz (npos, may be
+ * NULL: the frequency where the force's component along its lowest-
+ * frequency direction first changes sign, interpolated in log f; NaN when
+ * it keeps its sign), sigma (may be NULL: for each position in turn
+ * nfreq x 2N_q doubles, N_q its node count).  Systems that do not converge
+ * get NaN results and a status, and the call returns DSC_ERR_NOCONVERGE
+ * after solving all the others.  Positions run on a pool of host workers
+ * (dsc_positions_set_workers, default 4), each with its own CUDA stream,
+ * largest systems first. */
+typedef struct dsc_positions dsc_positions;
+int dsc_positions_create(int nen, unsigned N, unsigned E, const double *nodes, const unsigned *elems,
+                         const unsigned *bctype, const double *mbc, unsigned nIf,
+                         const unsigned *ifaces, unsigned nMat, const double *mat,
+                         dsc_positions **out);
+void dsc_positions_destroy(dsc_positions *p);
+/* Returns the particle's index (>= 0), or minus a status code. */
+int dsc_positions_add_particle(dsc_positions *p, unsigned N, unsigned E, const double *nodes,
+                               const unsigned *elems, unsigned iface);
+int dsc_positions_set_workers(dsc_positions *p, int workers);
+int dsc_positions_set_mixed_assembly(dsc_positions *p, int prec);
+/* Timing of kernel classes summed over the positions' solves, as
+ * dsc_session_set_timing / dsc_session_timing (resets on read). */
+int dsc_positions_set_timing(dsc_positions *p, int on);
+int dsc_positions_timing(dsc_positions *p, double *ms, int *count, double *work, int n);
+/* How many positions inverted the conductor blocks themselves (at most the
+ * number of workers; the others copied the shared inverses). */
+int dsc_positions_inversions(dsc_positions *p);
+int dsc_positions_solve(dsc_positions *p, unsigned npos, const unsigned *tmpl, const double *centres,
+                        unsigned nfreq, const double *freqs, double tol, unsigned max_iters,
+                        double *forces, unsigned *iters, int *status, double *crossover_hz,
+                        double *sigma);
+
+/* The crossover_hz of dsc_positions_solve for one force spectrum (forces:
+ * nfreq x 9 as dsc_session_solve writes them, freqs ascending; status may
+ * be NULL, else a system that did not converge gives NaN).  Host only. */
+double dsc_force_crossover(unsigned nfreq, const double *freqs, const double *forces,
+                           const int *status);
+
 /* One-call sweep from host arrays (session created and destroyed inside). */
 int dsc_sweep(int nen, unsigned N, unsigned E, const double *nodes, const unsigned *elems,
               const unsigned *bctype, const double *mbc, unsigned nIf, const unsigned *ifaces,

@@ -36,3 +36,24 @@ def test_no_cpu_fallback_without_device(native):
     with pytest.raises(_native.DscError) as ei:
         api.electric_form(sc)
     assert ei.value.status == 1 and "device" in str(ei.value)
+
+
+def test_force_crossover_host_logic(native):
+    """dsc_force_crossover (the position sweep's crossover_hz): first sign
+    change of the force along its lowest-frequency direction, interpolated
+    linearly in log f; NaN without a sign change or past an unconverged
+    system."""
+    L = _native.lib()
+    f = np.logspace(3, 8, 6)
+    F = np.zeros((6, 9))
+    p = np.array([3.0, 2.0, 1.0, -1.0, -2.0, -3.0])     # changes sign between f[2] and f[3]
+    d = np.array([0.6, 0.0, 0.8])
+    F[:, :3] = p[:, None] * d
+    x = L.dsc_force_crossover(6, f, F, None)
+    assert np.isclose(x, np.exp(0.5 * (np.log(f[2]) + np.log(f[3]))), rtol=1e-14)
+    st = np.zeros(6, dtype=np.int32)
+    st[1] = 1
+    assert np.isnan(L.dsc_force_crossover(6, f, F, st.ctypes.data))
+    F[:, :3] = np.abs(p)[:, None] * d
+    assert np.isnan(L.dsc_force_crossover(6, f, F, None))
+    assert np.isnan(L.dsc_force_crossover(1, f, F, None))

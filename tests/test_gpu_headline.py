@@ -40,7 +40,8 @@ def test_fp64_path_matches_reference_gmres_at_12k_nodes(gpu, port):
     pel = sc.bctype[sc.elems[:, 0] - 1] == 6
     scale = np.abs(Fce[pel]).sum()
     assert np.abs(forces[0, :3] - Fcm).max() <= 1e-9 * scale
-    assert relerr(forces[0, 3:6], Xcm) < 1e-13
+    # Xcm, the mean of the particle's nodes, is ~1e-17 for this centred sphere
+    assert np.abs(forces[0, 3:6] - Xcm).max() < 1e-13
 
 
 def _mixed_vs_fp64(sc, freqs):
