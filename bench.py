@@ -268,6 +268,7 @@ def position_bench(args, with_cpu: bool):
     fixed = scenes.plates_only(10)
     lev, cen = scenes.cfg3_positions(NPOS)
     ps = api.PositionSweep(fixed)
+    ps.set_workers(args.pos_workers)
     tid = {}
     for lv in (2, 3, 4):
         tid[lv] = ps.add_particle(*scenes.icosphere(lv, 1.0))
@@ -327,7 +328,7 @@ def position_bench(args, with_cpu: bool):
            "value": value, "unit": UNIT, "systems": nsys, "wall_s": wall,
            "positions_per_level": {str(lv): int((lev == lv).sum()) for lv in (2, 3, 4)},
            "N_per_level": {str(lv): n for lv, n in Ns.items()},
-           "workers": 4, "conductor_inversions": ps.inversions(),
+           "workers": args.pos_workers, "conductor_inversions": ps.inversions(),
            "e2e": {"value": value, "unit": UNIT, "note": "the call takes host arrays; same number"},
            "roofline": roof,
            "force_err_vs_fp64_max": max(ferr), "force_err_checked": len(ferr),
@@ -352,6 +353,230 @@ def position_bench(args, with_cpu: bool):
                                "frequency each (full solve at the reference's 1e-6, then a 1/8 row "
                                "sample scaled x8), weighted by the positions per level"}
     ps.close()
+    return out
+
+
+# ------------------------------------------------------------------ direct solve
+def gauss_bench(with_cpu: bool):
+    """gaussBksb through the C ABI (dsc_gauss: host matrix in, solution out)
+    on the full 2N x 2N real form of two scenes: config 0 (2N = 3048) and the
+    size of the reference's capacitor-1/quadratic Gauss run (two 25 x 25-cell
+    plates, 2N = 10404; 371 s on one x86 core in the survey's re-run).  The
+    tensor-core block LU with FP64 refinement against the FP64 LU; the
+    factorisation's rate is (2/3) n^3 flops over its CUDA-event time."""
+    from depsolver_gb300 import api, scenes
+    P = peaks()
+    bf16 = P.get("bf16_tflops") or 1900.0
+    out = {}
+    for name, sc in (("cfg0", scenes.cfg0(center=(0.0, 0.0, 1.0))), ("capacitor25", scenes.capacitor(25))):
+        Af, Bf = api.electric_form(sc, full=True)
+        n = Af.shape[0]
+        api.gauss_bksb(Af, Bf, mode=api.GAUSS_MIXED)        # warm-up
+        best, xm, inf = None, None, None
+        for _ in range(3):
+            t0 = time.perf_counter()
+            xm = api.gauss_bksb(Af, Bf, mode=api.GAUSS_MIXED)
+            dt = time.perf_counter() - t0
+            if best is None or dt < best:
+                best, inf = dt, api.gauss_info(times=True)
+        t0 = time.perf_counter()
+        x64 = api.gauss_bksb(Af, Bf, mode=api.GAUSS_FP64)
+        t64 = time.perf_counter() - t0
+        flops = 2.0 / 3.0 * n ** 3
+        tf = flops / (inf[4] * 1e-3) * 1e-12 if inf[4] > 0 else None
+        out[name] = {"unknowns": n, "e2e_s": best, "factor_ms": inf[4], "refine_ms": inf[5],
+                     "refinements": inf[1], "rel_residual": inf[2], "fell_back_to_fp64": inf[3],
+                     "fp64_lu_e2e_s": t64, "sol_rel_diff_vs_fp64_lu": float(np.abs(xm - x64).max() / np.abs(x64).max()),
+                     "factor_tflops": tf, "factor_frac_of_bf16_peak": tf / bf16 if tf else None,
+                     "peak_source": "MEASURED_PEAKS.json bf16_tflops, of measured" if P else "fallback",
+                     "speedup_vs_fp64_lu": t64 / best}
+        if with_cpu and name == "cfg0":
+            from oracle.checker import Port
+            t0 = time.perf_counter()
+            Port().gauss(Af, Bf)
+            tc = time.perf_counter() - t0
+            out[name]["cpu_port_gauss_s"] = tc
+            out[name]["cpu_cores"] = 1
+        del Af
+    out["cpu_note"] = ("cfg0: the C restatement's elimination (the reference's loop order) on one host "
+                       "core; capacitor25: the survey's x86 re-run of the reference took 371 s")
+    return out
+
+
+# ------------------------------------------------------------------ multi-material trap
+def trap_bench():
+    """Config 2: four 4 x 4 pads (16 x 16 cells, phases 0/90/180/270 deg, 1 V,
+    100 kHz) and four spheres of their own materials (levels 3/3/4/4):
+    the mixed solve at 100 kHz against the FP64 path, with the force and
+    torque of every particle."""
+    import torch
+
+    from depsolver_gb300 import api, scenes
+    sc = scenes.quadrupole_trap()
+    s = api.Session(sc)
+    fm, itm, _ = s.solve([sc.freq], mode=api.MODE_MIXED, tol=TOL)   # assembles
+    pm = s.particles()[0]
+    t = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.assemble(api.MODE_MIXED)
+        s.solve([sc.freq], mode=api.MODE_MIXED, tol=TOL)
+        torch.cuda.synchronize()
+        t.append(time.perf_counter() - t0)
+    # the FP64 check with the imaginary right-hand side scaled too: the
+    # pads' boundary values are complex, where the reference's Jacobi step
+    # (which scales only the real half) solves a different system
+    s.set_fp64_jacobi(True)
+    f64, it64, _ = s.solve([sc.freq], mode=api.MODE_FP64, tol=1e-12)
+    p64 = s.particles()[0]
+    s.close()
+    parts = []
+    for k in range(pm.shape[0]):
+        scale = p64[k, 6:9].sum()
+        parts.append({"force": pm[k, :3].tolist(), "torque": pm[k, 9:12].tolist(), "centre": pm[k, 3:6].tolist(),
+                      "force_err_vs_fp64": float(np.abs(pm[k, :3] - p64[k, :3]).max() / scale),
+                      "torque_err_vs_fp64": float(np.abs(pm[k, 9:12] - p64[k, 9:12]).max() / scale)})
+    return {"workload": "cfg2: quadrupole trap, 4 pads + 4 spheres (levels 3/3/4/4, own eps_r and sigma), "
+                        "100 kHz, tol 1e-10", "N": sc.N, "E": sc.E,
+            "s_per_solve": min(t), "inner_iterations": int(itm[0]), "fp64_gmres_iters": int(it64[0]),
+            "particles": parts}
+
+
+# ------------------------------------------------------------------ large scene
+def large_bench():
+    """Config 4: the castellated trap (two interdigitated combs of 10
+    fingers, 8 x 32 cells each, and a chain of 8 level-4 spheres: N = 104036,
+    E = 51200) at 1 MHz.  K in FP64 (87 GB) and its fp16 pair (43 GB) on the
+    device; K's digits (173 GB) do not fit, so the first residual is an FP64
+    GEMV.  Reported: the mixed solve (assembly included), the K product's
+    HBM rate, the assembly's (row, element) pairs/s and the force error
+    against the FP64 GMRES of the same scene."""
+    import torch
+
+    from depsolver_gb300 import api, scenes
+    free, total = torch.cuda.mem_get_info()
+    if total < 200e9:
+        return {"unavailable": f"needs about 135 GB of device memory; the device has {total / 1e9:.0f} GB"}
+    sc = scenes.comb_trap()
+    s = api.Session(sc)
+    try:
+        s.set_timing(True)
+        s.solve([1e6], mode=api.MODE_MIXED, tol=TOL)     # first solve: assembly, conversion, inverses
+        s.timing()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.assemble(api.MODE_MIXED)
+        fm, itm, _ = s.solve([1e6], mode=api.MODE_MIXED, tol=TOL)
+        torch.cuda.synchronize()
+        t_mixed = time.perf_counter() - t0
+        timing = s.timing()
+        free2, _ = torch.cuda.mem_get_info()
+        pm = s.particles()[0]
+        t0 = time.perf_counter()
+        f64, it64, _ = s.solve([1e6], mode=api.MODE_FP64, tol=TOL)
+        torch.cuda.synchronize()
+        t64 = time.perf_counter() - t0
+        p64 = s.particles()[0]
+    except Exception as e:  # an allocation the device refused, reported as such
+        s.close()
+        return {"unavailable": str(e)[:300]}
+    s.close()
+    P = peaks()
+    hbm = P.get("hbm_gbs") or 6800.0
+    N = sc.N
+    ms, cnt, wk = timing["gemm_K"]
+    bpf = (4.0 * N * N + 16.0 * N) / (12.0 * N * N)   # one system: 2 columns
+    gemm = {"achieved": wk * bpf * 1e-9 / (ms / 1e3), "unit": "GB/s", "peak": hbm,
+            "frac": wk * bpf * 1e-9 / (ms / 1e3) / hbm, "ms": ms, "launches": cnt} if cnt else None
+    ams, acnt, awk = timing["asm_regular"]
+    gms, gcnt, gwk = timing["gemv_K64"]
+    pe = [float(np.abs(pm[k, :3] - p64[k, :3]).max() / p64[k, 6:9].sum()) for k in range(pm.shape[0])]
+    return {"workload": "cfg4: castellated trap, 2 x 10 interdigitated fingers (2 x 8, 8 x 32 cells, "
+                        "+-1 V) + chain of 8 level-4 spheres (r = 1), 1 MHz, tol 1e-10",
+            "N": N, "E": sc.E, "device_memory_used_gb": (total - free2) / 1e9,
+            "mixed_s": t_mixed, "inner_iterations": int(itm[0]), "fp64_gmres_s": t64,
+            "fp64_gmres_iters": int(it64[0]),
+            "force_err_vs_fp64": float(np.abs(fm[0, :3] - f64[0, :3]).max() / f64[0, 6:9].sum()),
+            "particle_force_err_vs_fp64_max": max(pe),
+            "k_product_hbm": gemm,
+            "fp64_residual_gemv": {"achieved": gwk * 1e-9 / (gms / 1e3), "unit": "GB/s", "peak": hbm,
+                                   "frac": gwk * 1e-9 / (gms / 1e3) / hbm} if gcnt else None,
+            "assembly_pairs_per_s": awk / (ams / 1e3) if acnt else None,
+            "kernels_ms": {k: v[0] for k, v in timing.items()}}
+
+
+# ------------------------------------------------------------------ drop-in sequence
+def dropin_bench():
+    """The reference's own call sequence through the drop-in entry points on
+    host row-pointer buffers (src/depSolver.c:284-310, src/postProcess.c:
+    398-445): electricFormA_tria6 -> solverGMRES_el(1, 0) (tolerance 1e-6,
+    gmres.log written) -> forceMST_tria6, then field_tria6 at 2646 internal
+    points one call each (the point count of the dep-trap-1 example)."""
+    import ctypes as C
+    import tempfile
+
+    from depsolver_gb300 import _native, api, scenes
+    L = _native.lib()
+    out = {}
+    for name, sc in (("cfg0", scenes.cfg0(center=(0.0, 0.0, 1.0))), ("cfg1", scenes.cfg1())):
+        N, E = sc.N, sc.E
+        C.c_uint.in_dll(L, "nNodes").value = N
+        C.c_uint.in_dll(L, "nElems").value = E
+        C.c_uint.in_dll(L, "nInterfaces").value = sc.n_if
+        nodes = np.ascontiguousarray(sc.nodes)
+        elems = np.ascontiguousarray(sc.elems, dtype=np.uint32)
+        mat = np.ascontiguousarray(sc.mat)
+        ifc = np.ascontiguousarray(sc.ifaces, dtype=np.uint32)
+        mbc = np.ascontiguousarray(sc.mbc)
+        bct = np.ascontiguousarray(sc.bctype, dtype=np.uint32)
+        prob = np.array([sc.freq])
+        A = np.zeros((N, 2 * N))
+        B = np.zeros(2 * N)
+        rn, re_, rA = api.row_pointers(nodes), api.row_pointers(elems), api.row_pointers(A)
+        L.electricFormA_tria6.restype = C.c_int
+        t0 = time.perf_counter()
+        L.electricFormA_tria6(rn, re_, bct.ctypes.data_as(C.c_void_p), api.row_pointers(ifc),
+                              api.row_pointers(mat), prob.ctypes.data_as(C.c_void_p), rA,
+                              api.row_pointers(mbc), B.ctypes.data_as(C.c_void_p))
+        t1 = time.perf_counter()
+        cwd = os.getcwd()
+        with tempfile.TemporaryDirectory() as d:
+            os.chdir(d)
+            try:
+                L.solverGMRES_el(C.c_uint(1), C.c_uint(0), rA, B.ctypes.data_as(C.c_void_p))
+                t2 = time.perf_counter()
+                its = sum(1 for ln in open("gmres.log") if ln[:8].strip().isdigit())
+            finally:
+                os.chdir(cwd)
+        del A, rA
+        Fce = np.zeros((E, 3))
+        Xce = np.zeros((E, 3))
+        Fcm = np.zeros(3)
+        Xcm = np.zeros(3)
+        t2b = time.perf_counter()
+        L.forceMST_tria6(rn, re_, bct.ctypes.data_as(C.c_void_p), B.ctypes.data_as(C.c_void_p),
+                         C.c_double(sc.eps_medium), api.row_pointers(Fce), api.row_pointers(Xce),
+                         Fcm.ctypes.data_as(C.c_void_p), Xcm.ctypes.data_as(C.c_void_p))
+        t3 = time.perf_counter()
+        xs, zs = np.linspace(-4.0, 4.0, 63), np.linspace(-3.0, 3.0, 42)
+        pts = np.ascontiguousarray([[x, 0.3, z] for z in zs for x in xs])
+        mE = np.zeros(6)
+        t4 = time.perf_counter()
+        for p in pts:
+            L.field_tria6(p.ctypes.data_as(C.c_void_p), rn, re_, B.ctypes.data_as(C.c_void_p),
+                          mE.ctypes.data_as(C.c_void_p))
+        t5 = time.perf_counter()
+        out[name] = {"N": N, "E": E, "assembly_s": t1 - t0, "gmres_s": t2 - t1, "gmres_iters": its,
+                     "force_s": t3 - t2b, "field_points": len(pts), "field_s": t5 - t4,
+                     "field_us_per_point": (t5 - t4) / len(pts) * 1e6, "total_s": (t1 - t0) + (t2 - t1) + (t3 - t2b) + (t5 - t4)}
+        if name == "cfg0":
+            from oracle.checker import Port
+            nt = os.cpu_count() or 1
+            t6 = time.perf_counter()
+            Port().field(sc, B, pts, nthreads=nt)
+            out[name]["cpu_port_field_s"] = time.perf_counter() - t6
+            out[name]["cpu_port_threads"] = nt
     return out
 
 
@@ -504,6 +729,10 @@ def run_ours(args, rank, world):
     if rank != 0:
         return
     pos = position_bench(args, with_cpu=not args.no_cpu) if not args.no_positions else None
+    gauss = gauss_bench(with_cpu=not args.no_cpu) if not args.no_extras else None
+    trap = trap_bench() if not args.no_extras else None
+    large = large_bench() if not args.no_extras else None
+    dropin = dropin_bench() if not args.no_extras else None
     # roofline of the dominant kernel class over the timed region: achieved
     # = algorithmic work (counted by the library per class) / CUDA-event time
     # of the class on the session's stream
@@ -529,6 +758,10 @@ def run_ours(args, rank, world):
         "speedup_vs_fp64_path": value / world / (1.0 / fp64_s),
         "speedup_parts": ablation,
         "position_sweep": pos,
+        "gauss": gauss,
+        "trap": trap,
+        "large": large,
+        "dropin": dropin,
         "inner_iterations": {"mean": float(np.mean(its)), "max": int(np.max(its)),
                              "products_per_step": timing["gemm_K"][1] // max(1, args.steps)},
         "accuracy": {"force_err_vs_fp64": float(ferrs.max()),
@@ -541,6 +774,7 @@ def run_ours(args, rank, world):
         "kernels_ms": {k: {"ms": v[0], "scopes": v[1], "share": v[0] / total_ms if total_ms else 0}
                        for k, v in timing.items()},
         "roofline_classes": roof_all,
+        "autotuned_splits": [{"N": r[0], "columns": r[1], "splits": r[2]} for r in api.autotune_table()],
         "gpu_launches": launches,
         "clocks": clk,
     }
@@ -589,6 +823,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-positions", action="store_true", help="skip the position sweep (cfg3)")
+    ap.add_argument("--no-extras", action="store_true", help="skip the direct-solve and trap sections")
+    ap.add_argument("--pos-workers", type=int, default=4, help="host workers (streams) of the position sweep")
     ap.add_argument("--scene", choices=["cfg1", "mid"], default="cfg1",
                     help="mid: a smaller scene for ncu captures (with --only-step)")
     ap.add_argument("--mixed-assembly", choices=["fp32", "df32"], default="fp32",

@@ -43,6 +43,11 @@ def lib() -> C.CDLL:
                                    _dp]
         L.dsc_gauss.restype = C.c_int
         L.dsc_gauss.argtypes = [C.c_uint, _dp, C.c_size_t, _dp]
+        L.dsc_set_gauss_mode.restype = C.c_int
+        L.dsc_set_gauss_mode.argtypes = [C.c_int]
+        L.dsc_gauss_info.restype = C.c_int
+        L.dsc_gauss_info.argtypes = [C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_int),
+                                     C.c_void_p]
         L.dsc_gmres.restype = C.c_int
         L.dsc_gmres.argtypes = [C.c_uint, C.c_uint, C.c_double, C.c_uint, _dp, C.c_size_t, _dp,
                                 C.c_void_p, C.c_char_p, C.POINTER(C.c_uint)]
@@ -99,11 +104,21 @@ def lib() -> C.CDLL:
         L.dsc_session_set_timing.restype = C.c_int
         L.dsc_session_set_timing.argtypes = [C.c_void_p, C.c_int]
         L.dsc_session_set_preconditioner.restype = C.c_int
+        L.dsc_session_set_fp64_jacobi.restype = C.c_int
+        L.dsc_session_set_fp64_jacobi.argtypes = [C.c_void_p, C.c_int]
+        L.dsc_session_set_residual.restype = C.c_int
+        L.dsc_session_set_residual.argtypes = [C.c_void_p, C.c_int]
         L.dsc_session_set_field_tensor.restype = C.c_int
         L.dsc_session_set_field_tensor.argtypes = [C.c_void_p, C.c_int]
         L.dsc_session_set_mixed_assembly.restype = C.c_int
         L.dsc_session_set_mixed_assembly.argtypes = [C.c_void_p, C.c_int]
         L.dsc_session_set_preconditioner.argtypes = [C.c_void_p, C.c_int]
+        L.dsc_session_particles.restype = C.c_int
+        L.dsc_session_particles.argtypes = [C.c_void_p, C.c_void_p, C.c_uint]
+        L.dsc_set_autotune.restype = C.c_int
+        L.dsc_set_autotune.argtypes = [C.c_int]
+        L.dsc_autotune_table.restype = C.c_int
+        L.dsc_autotune_table.argtypes = [C.c_void_p, C.c_int]
         L.dsc_session_status.restype = C.c_int
         L.dsc_session_status.argtypes = [C.c_void_p, C.c_void_p, C.c_uint]
         L.dsc_session_preconditioner_blocks.restype = C.c_int

@@ -30,6 +30,19 @@ def _f(a):
     return np.ascontiguousarray(a, dtype=np.float64)
 
 
+def row_pointers(arr: np.ndarray):
+    """The reference's row-pointer view (double** / unsigned**) of a
+    C-contiguous 2-D array, for the drop-in entry points; the array must
+    outlive the view."""
+    T = C.c_double if arr.dtype == np.float64 else C.c_uint
+    ptrs = (C.POINTER(T) * arr.shape[0])()
+    base = arr.ctypes.data
+    step = arr.strides[0]
+    for i in range(arr.shape[0]):
+        ptrs[i] = C.cast(base + i * step, C.POINTER(T))
+    return ptrs
+
+
 def _u(a):
     return np.ascontiguousarray(a, dtype=np.uint32)
 
@@ -51,11 +64,40 @@ def electric_form(sc: Scene, full: bool = False, A: np.ndarray | None = None):
     return A, B
 
 
-def gauss_bksb(A: np.ndarray, B: np.ndarray) -> np.ndarray:
+GAUSS_MIXED = 0
+GAUSS_FP64 = 1
+
+
+def gauss_bksb(A: np.ndarray, B: np.ndarray, mode: int | None = None) -> np.ndarray:
+    """Direct solve (gaussBksb).  mode: GAUSS_MIXED (tensor-core block LU
+    with FP64 refinement, the library's default), GAUSS_FP64, or None (the
+    current process-wide mode)."""
+    L = _native.lib()
     A = _f(A)
     x = _f(B).copy()
-    _native.check(_native.lib().dsc_gauss(A.shape[0], A, A.shape[1], x))
+    old = None
+    if mode is not None:
+        old = L.dsc_gauss_info(None, None, None, None)
+        _native.check(L.dsc_set_gauss_mode(int(mode)))
+    try:
+        _native.check(L.dsc_gauss(A.shape[0], A, A.shape[1], x))
+    finally:
+        if old is not None:
+            L.dsc_set_gauss_mode(old)
     return x
+
+
+def gauss_info(times: bool = False):
+    """(mode, refinement steps, relative residual, fell back to FP64) of the
+    last direct solve; with times, also (factorisation ms, refinement ms)
+    of its device work."""
+    it = C.c_int(0)
+    rr = C.c_double(0.0)
+    fb = C.c_int(0)
+    ms = np.zeros(2)
+    mode = _native.lib().dsc_gauss_info(C.byref(it), C.byref(rr), C.byref(fb), ms.ctypes.data)
+    out = (mode, it.value, rr.value, bool(fb.value))
+    return out + (float(ms[0]), float(ms[1])) if times else out
 
 
 def solver_gmres_el(A: np.ndarray, B: np.ndarray, preCond: int = 1, tol: float = 1.0e-6,
@@ -108,6 +150,9 @@ def force_mst(sc: Scene, vB: np.ndarray, eps: float | None = None):
 MODE_FP64 = 1
 MODE_MIXED = 2
 ERR_NOCONVERGE = 5
+RESIDUAL_AUTO = 0
+RESIDUAL_DIGITS = 1
+RESIDUAL_FP64 = 2
 # outcome of one system of a sweep (Session.status)
 SYS_CONVERGED = 0
 SYS_CAPPED = 1
@@ -118,6 +163,20 @@ ASM_FP32 = 2
 TIMER_NAMES = ("asm_regular", "asm_fixup", "asm_singular", "gemv_K64", "gemm_K", "field", "mst",
                "residual_fp64", "krylov", "gram_schmidt", "convert_K", "precond_build",
                "precond_apply")
+
+
+def set_autotune(on: bool):
+    """Split-count autotuner of the mixed sweep's tensor-core product."""
+    _native.check(_native.lib().dsc_set_autotune(int(on)))
+
+
+def autotune_table():
+    """[(N, columns, splits)] of the sizes tuned so far in this process."""
+    L = _native.lib()
+    n = L.dsc_autotune_table(None, 0)
+    rows = np.zeros((max(n, 1), 3), dtype=np.int32)
+    L.dsc_autotune_table(rows.ctypes.data, n)
+    return [tuple(int(v) for v in r) for r in rows[:n]]
 
 
 class Session:
@@ -177,6 +236,17 @@ class Session:
         (default on) or on the FP32 pipes."""
         _native.check(self._L.dsc_session_set_field_tensor(self._h, int(on)))
 
+    def set_fp64_jacobi(self, full: bool):
+        """FP64 mode: also scale the imaginary right-hand side in the Jacobi
+        step (the reference scales only the real half; they differ for
+        complex boundary values)."""
+        _native.check(self._L.dsc_session_set_fp64_jacobi(self._h, int(full)))
+
+    def set_residual(self, how: int):
+        """Mixed mode's first FP64 residual: RESIDUAL_AUTO, RESIDUAL_DIGITS
+        (tensor-core digit products) or RESIDUAL_FP64 (FP64 GEMV)."""
+        _native.check(self._L.dsc_session_set_residual(self._h, int(how)))
+
     def set_preconditioner(self, on: bool):
         """Mixed mode: the conductor-block right preconditioner (default on)."""
         _native.check(self._L.dsc_session_set_preconditioner(self._h, int(on)))
@@ -216,6 +286,15 @@ class Session:
         if not (partial and rc == ERR_NOCONVERGE):
             _native.check(rc)
         return forces, its, sig
+
+    def particles(self) -> np.ndarray:
+        """Per-particle results of the last solve: (F, P, 12) -- force[3],
+        centre[3], sum|Fce|[3], torque[3] about the centre."""
+        n = self._L.dsc_session_status(self._h, None, 0)
+        P = self._L.dsc_session_particles(self._h, None, 0)
+        out = np.zeros((n, P, 12))
+        self._L.dsc_session_particles(self._h, out.ctypes.data, n)
+        return out
 
     def status(self) -> np.ndarray:
         """Outcome of each system of the last solve: SYS_CONVERGED,

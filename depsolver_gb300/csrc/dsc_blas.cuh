@@ -56,4 +56,42 @@ __device__ __forceinline__ void finish_reduction(double v, RedWork rw, double *o
     }
 }
 
+// part[s][0/1][i] = sum over the column split s of K[c][i] * x{re,im}[c];
+// K column-major; thread per row, x chunks staged in shared memory.
+template <typename T>
+__global__ void __launch_bounds__(256) k_gemv_K2(const T *__restrict__ K, size_t ld, int N,
+                                                 const double *__restrict__ xr,
+                                                 const double *__restrict__ xi, int cols,
+                                                 double *__restrict__ part, const int *skip = nullptr)
+{
+    if (skip && *skip) return;
+    __shared__ double sxr[256], sxi[256];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = blockIdx.y;
+    const int c0 = s * cols, c1 = min(N, c0 + cols);
+    double ar = 0.0, ai = 0.0;
+    for (int cb = c0; cb < c1; cb += 256) {
+        __syncthreads();
+        if (cb + (int)threadIdx.x < c1) {
+            sxr[threadIdx.x] = xr[cb + threadIdx.x];
+            sxi[threadIdx.x] = xi[cb + threadIdx.x];
+        }
+        __syncthreads();
+        const int cn = min(256, c1 - cb);
+        if (i < N) {
+            const T *kp = K + (size_t)cb * ld + i;
+#pragma unroll 8
+            for (int c = 0; c < cn; c++) {
+                double k = (double)kp[(size_t)c * ld];
+                ar += k * sxr[c];
+                ai += k * sxi[c];
+            }
+        }
+    }
+    if (i < N) {
+        part[((size_t)s * 2) * N + i] = ar;
+        part[((size_t)s * 2 + 1) * N + i] = ai;
+    }
+}
+
 }  // namespace dsc

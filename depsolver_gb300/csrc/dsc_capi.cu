@@ -39,8 +39,19 @@ struct Context {
     std::unique_ptr<MeshEntry> mesh;
     uint64_t sigma_key = 0;
     DevBuf<double> sigma;
+    std::vector<double> sigma_host;  // host copy of the solution on the device
+    // point evaluations: one point set and output buffer kept between calls
+    // (the reference's post-processing evaluates one point per call)
+    PointSet pts;
+    DevBuf<double> pout;
     double *pinned = nullptr;
     size_t pinned_bytes = 0;
+    // direct solve: the tensor-core block LU with FP64 refinement (default)
+    // or the FP64 LU; the last solve's refinement steps, relative residual
+    // and whether it fell back to the FP64 LU
+    int gauss_mode = DSC_GAUSS_MIXED;
+    LuMixedInfo gauss_info;
+    int gauss_fell_back = 0;
 };
 
 static Context &ctx()
@@ -119,15 +130,37 @@ static int get_mesh(int nen, int N, int E, const double *nodes, const int *elems
 
 static int get_sigma(int N, const double *vB, const double **dsig)
 {
+    // the solution goes up again only when it differs from the copy on the
+    // device (compared value by value with its host copy)
     Context &c = ctx();
-    uint64_t key = hash_bytes(0x13198a2e03707344ULL ^ c.mesh->key, vB, (size_t)2 * N * sizeof(double));
-    if (c.sigma_key != key) {
-        DSC_TRY(c.sigma.upload(vB, (size_t)2 * N, c.st));
+    const size_t n2 = 2 * (size_t)N;
+    if (c.sigma_key != c.mesh->key || c.sigma_host.size() != n2 ||
+        memcmp(c.sigma_host.data(), vB, n2 * sizeof(double)) != 0) {
+        c.sigma_host.assign(vB, vB + n2);
+        DSC_TRY(c.sigma.upload(c.sigma_host.data(), n2, c.st));
         DSC_CUDA(cudaStreamSynchronize(c.st));
-        c.sigma_key = key;
+        c.sigma_key = c.mesh->key;
     }
     *dsig = c.sigma.p;
     return kOk;
+}
+
+// The cached mesh when it holds exactly these row-pointer inputs (checked
+// value by value against its flattened copy, without allocating), else
+// null: the reference's post-processing calls field_* once per point with
+// the same mesh, which then needs neither a new flat copy nor a hash.
+static MeshEntry *cached_rows(int nen, int N, int E, double **mNodes, unsigned **mElems)
+{
+    MeshEntry *m = ctx().mesh.get();
+    if (!m || m->plan.nen != nen || m->plan.N != N || m->plan.E != E) return nullptr;
+    const double *x = m->plan.nodes.data();
+    for (int i = 0; i < N; i++)
+        if (memcmp(mNodes[i], x + 3 * (size_t)i, 3 * sizeof(double)) != 0) return nullptr;
+    const int *el = m->plan.elems.data();
+    for (int e = 0; e < E; e++)
+        for (int k = 0; k < nen; k++)
+            if ((int)mElems[e][k] - 1 != el[(size_t)e * nen + k]) return nullptr;
+    return m;
 }
 
 // Flattened copies of the reference's row-pointer inputs.
@@ -306,10 +339,22 @@ static int gauss_impl(unsigned n, const double *const *rows, const double *flat,
                                  cudaMemcpyHostToDevice, st));
         DSC_CUDA(cudaStreamSynchronize(st));
     }
-    DSC_TRY(lu_solve_augmented_fp64((int)n, A.p, ldd, bad_row, st));
     DevBuf<double> x;
     DSC_TRY(x.alloc(n));
-    DSC_TRY(lu_extract_solution((int)n, A.p, ldd, x.p, st));
+    Context &c = ctx();
+    c.gauss_info = LuMixedInfo();
+    c.gauss_fell_back = 0;
+    bool done = false;
+    if (c.gauss_mode == DSC_GAUSS_MIXED) {
+        const int rc = lu_solve_mixed((int)n, A.p, ldd, x.p, 1e-15, &c.gauss_info, bad_row, st);
+        if (rc == kOk) done = true;
+        else if (rc == kErrStagnation) c.gauss_fell_back = 1;  // the matrix needs the FP64 factors
+        else return rc;
+    }
+    if (!done) {
+        DSC_TRY(lu_solve_augmented_fp64((int)n, A.p, ldd, bad_row, st));
+        DSC_TRY(lu_extract_solution((int)n, A.p, ldd, x.p, st));
+    }
     DSC_CUDA(cudaMemcpyAsync(B, x.p, n * sizeof(double), cudaMemcpyDeviceToHost, st));
     DSC_CUDA(cudaStreamSynchronize(st));
     return kOk;
@@ -347,24 +392,29 @@ static int gmres_impl(unsigned N, unsigned preCond, double tol, unsigned maxit,
     return rc;
 }
 
+// Points on a mesh already on the device; the point set and the output
+// buffer are the context's, reused (grown only) from call to call.
+static int points_on(MeshEntry *m, const double *vB, unsigned npts, const double *pts, int field, double *out)
+{
+    Context &c = ctx();
+    const double *dsig;
+    DSC_TRY(get_sigma(m->plan.N, vB, &dsig));
+    cudaStream_t st = c.st;
+    DSC_TRY(c.pts.build(m->plan, (int)npts, pts));
+    const int nv = field ? 6 : 2;
+    DSC_TRY(c.pout.alloc((size_t)npts * nv));
+    DSC_TRY(eval_points(m->dev, c.pts, dsig, field, c.pout.p, st));
+    DSC_CUDA(cudaMemcpyAsync(out, c.pout.p, (size_t)npts * nv * sizeof(double), cudaMemcpyDeviceToHost, st));
+    DSC_CUDA(cudaStreamSynchronize(st));
+    return kOk;
+}
+
 static int points_impl(int nen, unsigned N, unsigned E, const double *nodes, const int *elems0,
                        const double *vB, unsigned npts, const double *pts, int field, double *out)
 {
     MeshEntry *m;
     DSC_TRY(get_mesh(nen, (int)N, (int)E, nodes, elems0, &m));
-    const double *dsig;
-    DSC_TRY(get_sigma((int)N, vB, &dsig));
-    cudaStream_t st = ctx().st;
-    PointSet ps;
-    DSC_TRY(ps.build(m->plan, (int)npts, pts));
-    DevBuf<double> dout;
-    const int nv = field ? 6 : 2;
-    DSC_TRY(dout.alloc((size_t)npts * nv));
-    DSC_TRY(eval_points(m->dev, ps, dsig, field, dout.p, st));
-    DSC_CUDA(cudaMemcpyAsync(out, dout.p, (size_t)npts * nv * sizeof(double), cudaMemcpyDeviceToHost,
-                             st));
-    DSC_CUDA(cudaStreamSynchronize(st));
-    return kOk;
+    return points_on(m, vB, npts, pts, field, out);
 }
 
 static int force_impl(int nen, unsigned N, unsigned E, const double *nodes, const int *elems0,
@@ -524,6 +574,11 @@ static int field_dropin(int nen, int field, double *Xin, double **mNodes, unsign
                         double *vB, double *out)
 {
     std::lock_guard<std::mutex> lk(ctx().mu);
+    check_or_die(ensure_stream());
+    if (MeshEntry *m = cached_rows(nen, (int)nNodes, (int)nElems, mNodes, mElems)) {
+        check_or_die(points_on(m, vB, 1, Xin, field, out));
+        return 0;
+    }
     FlatMesh f;
     flatten(nen, (int)nNodes, (int)nElems, mNodes, mElems, f);
     check_or_die(points_impl(nen, nNodes, nElems, f.nodes.data(), f.elems0.data(), vB, 1, Xin, field, out));
@@ -632,6 +687,31 @@ extern "C" int dsc_gauss(unsigned n, const double *A, size_t lda, double *B)
     }
     int bad = -1;
     return gauss_impl(n, nullptr, A, lda, B, &bad);
+}
+
+extern "C" int dsc_set_gauss_mode(int mode)
+{
+    if (mode != DSC_GAUSS_MIXED && mode != DSC_GAUSS_FP64) {
+        set_error("dsc_set_gauss_mode: unknown mode %d", mode);
+        return kErrArg;
+    }
+    std::lock_guard<std::mutex> lk(ctx().mu);
+    ctx().gauss_mode = mode;
+    return kOk;
+}
+
+extern "C" int dsc_gauss_info(int *refinements, double *rel_residual, int *fell_back, double *ms)
+{
+    std::lock_guard<std::mutex> lk(ctx().mu);
+    const Context &c = ctx();
+    if (refinements) *refinements = c.gauss_info.refinements;
+    if (rel_residual) *rel_residual = c.gauss_info.rel_residual;
+    if (fell_back) *fell_back = c.gauss_fell_back;
+    if (ms) {
+        ms[0] = c.gauss_info.factor_ms;
+        ms[1] = c.gauss_info.refine_ms;
+    }
+    return c.gauss_mode;
 }
 
 extern "C" int dsc_gmres(unsigned N, unsigned preCond, double tol, unsigned max_iters,

@@ -18,6 +18,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <numeric>
 #include <thread>
 
 #include "dsc_common.cuh"
@@ -352,6 +353,124 @@ __global__ void k_mst_totals(const double *__restrict__ Fce, int npel, const dou
     }
 }
 
+// Per-particle results (see mst_particles): block per (particle, system),
+// thread-strided sums in a fixed order, then warp sums and the warps' sums
+// in order.
+constexpr int kPartThreads = 256;
+__device__ __forceinline__ void part_block_sum(double *v, int n, double (*sh)[kPartThreads / 32])
+{
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    for (int k = 0; k < n; k++) v[k] = warp_sum(v[k]);
+    __syncthreads();
+    if (lane == 0)
+        for (int k = 0; k < n; k++) sh[k][wp] = v[k];
+    __syncthreads();
+    for (int k = 0; k < n; k++) {
+        double t = 0.0;
+        for (int w = 0; w < kPartThreads / 32; w++) t += sh[k][w];
+        v[k] = t;
+    }
+}
+
+__global__ void __launch_bounds__(kPartThreads) k_mst_particles(
+    const double *__restrict__ Fce, size_t fstride, const double *__restrict__ Xce, int npel,
+    const int *__restrict__ pel_part, const double *__restrict__ X, const double *__restrict__ Y,
+    const double *__restrict__ Z, const int *__restrict__ ids, const int *__restrict__ ids_part, int P, int npart,
+    double *__restrict__ out)
+{
+    __shared__ double sh[9][kPartThreads / 32];
+    const int p = blockIdx.x, f = blockIdx.y;
+    double c[4] = {0, 0, 0, 0};
+    for (int q = threadIdx.x; q < P; q += kPartThreads)
+        if (ids_part[q] == p) {
+            const int v = ids[q];
+            c[0] += X[v];
+            c[1] += Y[v];
+            c[2] += Z[v];
+            c[3] += 1.0;
+        }
+    part_block_sum(c, 4, sh);
+    const double cx = c[0] / c[3], cy = c[1] / c[3], cz = c[2] / c[3];
+    const double *Fc = Fce + (size_t)f * fstride;
+    double s[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int t = threadIdx.x; t < npel; t += kPartThreads)
+        if (pel_part[t] == p) {
+            const double fx = Fc[3 * (size_t)t], fy = Fc[3 * (size_t)t + 1], fz = Fc[3 * (size_t)t + 2];
+            const double rx = Xce[3 * (size_t)t] - cx, ry = Xce[3 * (size_t)t + 1] - cy,
+                         rz = Xce[3 * (size_t)t + 2] - cz;
+            s[0] += fx;
+            s[1] += fy;
+            s[2] += fz;
+            s[3] += fabs(fx);
+            s[4] += fabs(fy);
+            s[5] += fabs(fz);
+            s[6] += ry * fz - rz * fy;
+            s[7] += rz * fx - rx * fz;
+            s[8] += rx * fy - ry * fx;
+        }
+    part_block_sum(s, 9, sh);
+    if (threadIdx.x == 0) {
+        double *o = out + ((size_t)f * npart + p) * kPartVals;
+        o[0] = s[0];
+        o[1] = s[1];
+        o[2] = s[2];
+        o[3] = cx;
+        o[4] = cy;
+        o[5] = cz;
+        o[6] = s[3];
+        o[7] = s[4];
+        o[8] = s[5];
+        o[9] = s[6];
+        o[10] = s[7];
+        o[11] = s[8];
+    }
+}
+
+template <int NEN>
+__global__ void k_mst_centres(const double *__restrict__ X, const double *__restrict__ Y,
+                              const double *__restrict__ Z, const int *__restrict__ elems,
+                              const int *__restrict__ pel, int npel, double *__restrict__ Xce)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= npel) return;
+    const int e = pel[t];
+    double Xe[NEN][3], N6[NEN], XL[3];
+#pragma unroll
+    for (int k = 0; k < NEN; k++) {
+        const int v = elems[(size_t)e * NEN + k];
+        Xe[k][0] = X[v];
+        Xe[k][1] = Y[v];
+        Xe[k][2] = Z[v];
+    }
+    shape<NEN>(0.25, 0.25, N6);
+    map_point<NEN>(Xe, 0.25, 0.25, N6, XL);
+    Xce[3 * (size_t)t] = XL[0];
+    Xce[3 * (size_t)t + 1] = XL[1];
+    Xce[3 * (size_t)t + 2] = XL[2];
+}
+
+int mst_particles(const ForcePlan &fp, const double *X, const double *Y, const double *Z, const double *Fce,
+                  size_t fstride, const double *Xce, int nsys, double *out, cudaStream_t st)
+{
+    if (fp.npart == 0 || nsys == 0) return kOk;
+    DSC_LAUNCH(k_mst_particles<<<dim3(fp.npart, nsys), kPartThreads, 0, st>>>(
+        Fce, fstride, Xce, fp.npel, fp.pel_part.p, X, Y, Z, fp.ids.p, fp.ids_part.p, fp.P, fp.npart, out));
+    DSC_CUDA(cudaGetLastError());
+    return kOk;
+}
+
+int mst_centres(const DeviceMesh &m, const ForcePlan &fp, double *Xce, cudaStream_t st)
+{
+    if (fp.npel == 0) return kOk;
+    const int g = (fp.npel + 127) / 128;
+    if (m.nen == 6)
+        DSC_LAUNCH(k_mst_centres<6><<<g, 128, 0, st>>>(m.x.p, m.y.p, m.z.p, m.elems.p, fp.pel.p, fp.npel, Xce));
+    else
+        DSC_LAUNCH(k_mst_centres<3><<<g, 128, 0, st>>>(m.x.p, m.y.p, m.z.p, m.elems.p, fp.pel.p, fp.npel, Xce));
+    DSC_CUDA(cudaGetLastError());
+    return kOk;
+}
+
 // ------------------------------------------------------------------ host
 
 int PointSet::build(const HostPlan &plan, int P, const double *pts, const int *node_ids)
@@ -625,6 +744,36 @@ int ForcePlan::build(const HostPlan &plan, const unsigned *bctype, cudaStream_t 
         }
         DSC_TRY(tmap.upload(tm, st));
         DSC_TRY(row_grad.upload(rg, st));
+    }
+    {
+        // particles: union of the nodes of every particle element
+        std::vector<int> par(plan.N);
+        std::iota(par.begin(), par.end(), 0);
+        auto find = [&](int a) {
+            while (par[a] != a) {
+                par[a] = par[par[a]];
+                a = par[a];
+            }
+            return a;
+        };
+        for (int e : pel_host)
+            for (int k = 1; k < plan.nen; k++) {
+                const int a = find(plan.elems[(size_t)e * plan.nen]), b = find(plan.elems[(size_t)e * plan.nen + k]);
+                if (a != b) par[std::max(a, b)] = std::min(a, b);
+            }
+        std::vector<int> pid(plan.N, -1), ip(P), ep(std::max(npel, 1), 0);
+        npart = 0;
+        for (int i = 0; i < plan.N; i++)  // numbered by their lowest node
+            if (bctype[i] == 6 && pid[find(i)] < 0) pid[find(i)] = npart++;
+        for (int e : pel_host) {  // a first node of type 6 whose element has no type-6 peers
+            const int r = find(plan.elems[(size_t)e * plan.nen]);
+            if (pid[r] < 0) pid[r] = npart++;
+        }
+        for (int t = 0; t < P; t++) ip[t] = pid[find(idv[t])];
+        for (int t = 0; t < npel; t++) ep[t] = pid[find(plan.elems[(size_t)pel_host[t] * plan.nen])];
+        DSC_TRY(ids_part.upload(ip, st));
+        DSC_TRY(pel_part.upload(ep, st));
+        DSC_CUDA(cudaStreamSynchronize(st));  // ip, ep go out of scope
     }
     DSC_TRY(ids.upload(idv, st));
     DSC_TRY(pel.upload(pel_host.empty() ? std::vector<int>{0} : pel_host, st));

@@ -47,8 +47,27 @@ struct ForcePlan {
     DevBuf<int> tmap, row_grad;
     std::vector<int> pel_host;
     DevBuf<double> Ept, Enode, Fce, Xce;
+    // particles: the connected sets of particle elements (elements sharing
+    // a node belong to one particle), numbered by their lowest node; the
+    // particle of each force point (ids order) and of each particle element
+    int npart = 0;
+    DevBuf<int> ids_part, pel_part;
     int build(const HostPlan &plan, const unsigned *bctype, cudaStream_t st);
 };
+
+// Values per particle and system of the per-particle Maxwell-stress results.
+constexpr int kPartVals = 12;
+// out[(f * npart + p) * kPartVals + ...] for the nsys systems whose element
+// forces are Fce + f * fstride (npel x 3 each; Xce npel x 3 shared):
+//   [0..2] the particle's force (sum of its elements' Fce), [3..5] its
+//   centre (mean of its force points), [6..8] sum of |Fce| per component,
+//   [9..11] torque about the centre, sum over its elements of
+//   (Xce - centre) x Fce.
+int mst_particles(const ForcePlan &fp, const double *X, const double *Y, const double *Z, const double *Fce,
+                  size_t fstride, const double *Xce, int nsys, double *out, cudaStream_t st);
+// Xce (npel x 3) = X(1/4, 1/4) of each particle element, where the reference
+// reports an element's force (src/force.c:486-487,531-541).
+int mst_centres(const DeviceMesh &m, const ForcePlan &fp, double *Xce, cudaStream_t st);
 
 // Force for one nodal solution dsigma (device, 2N); d_tot (device, 9):
 // Fcm[3], Xcm[3], sum over elements of |Fce| per component[3].  Fce/Xce

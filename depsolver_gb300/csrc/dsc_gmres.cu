@@ -23,8 +23,9 @@ namespace dsc {
 // y = (A1 - i A2) x on the compact row-major form: one warp per row, lanes
 // stride over the columns (matVectProd_el src/gmres_el.c:323-337).
 __global__ void k_matvec_compact(const double *__restrict__ A, size_t lda, int N,
-                                 const double *__restrict__ x, double *__restrict__ y)
+                                 const double *__restrict__ x, double *__restrict__ y, const int *skip)
 {
+    if (skip && *skip) return;  // the GMRES has stopped: nothing to do
     const int i = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (i >= N) return;
@@ -117,6 +118,146 @@ __global__ void k_update_x(double *__restrict__ x, const double *__restrict__ V,
     }
 }
 
+// ---- one Arnoldi column in one launch: a cluster of kMgsCta CTAs holds
+// the new vector w in shared memory (a contiguous slice per CTA) and runs
+// the whole modified Gram-Schmidt sequence of the reference's column i
+// (src/gmres_el.c:190-200): h_j = v_j . w then w -= h_j v_j for j = 0..i in
+// that order, then |w| and w / |w| (written to V[i + 1]).  Each dot product
+// is a block sum per CTA and the CTAs' sums added in rank order through
+// distributed shared memory between cluster barriers (hardware barriers: no
+// polling); the partial-sum slots alternate by parity, so one barrier per
+// dot product suffices.  ww (the reference's |w|^2 before the
+// orthogonalisation, its zero test) and h[0..i+1] go to global memory.
+constexpr int kMgsCta = 8;         // CTAs per cluster (the portable maximum)
+constexpr int kMgsThreads = 1024;
+constexpr size_t kMgsMaxSlice = 26 * 1024;  // doubles of w per CTA (208 KB of shared memory)
+
+__device__ __forceinline__ void cluster_sync_all()
+{
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ unsigned cluster_rank()
+{
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+
+// The cluster-wide sum of every thread's v, identical in all threads of all
+// CTAs (fixed order: warps, then CTAs by rank).  slot: 2 x kMgsCta partials
+// of this CTA's shared memory (its own in slot[p][0]).
+__device__ __forceinline__ double cluster_sum(double v, double *wsum, double *slot, int p)
+{
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    if (lane == 0) wsum[wp] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int q = 0; q < kMgsThreads / 32; q++) t += wsum[q];
+        slot[p] = t;
+    }
+    cluster_sync_all();  // every CTA's partial of this parity is written
+    double t = 0.0;
+    const unsigned local = (unsigned)__cvta_generic_to_shared(&slot[p]);
+    for (unsigned r = 0; r < kMgsCta; r++) {
+        unsigned remote;
+        double x;
+        asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(remote) : "r"(local), "r"(r));
+        asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(x) : "r"(remote) : "memory");
+        t += x;
+    }
+    return t;
+}
+
+__global__ void __launch_bounds__(kMgsThreads, 1) k_mgs_cluster(double *__restrict__ V, int n, int i,
+                                                                 double *__restrict__ h, double *__restrict__ ww,
+                                                                 const int *__restrict__ done)
+{
+    extern __shared__ double ws[];                    // this CTA's slice of w
+    __shared__ double wsum[kMgsThreads / 32], slot[2];
+    if (*done) return;  // the whole cluster reads the same flag
+    const unsigned rank = cluster_rank();
+    const int L = (n + kMgsCta - 1) / kMgsCta;
+    const int lo = (int)rank * L, hi = min(n, lo + L);
+    double *w = V + (size_t)(i + 1) * n;
+    double s = 0.0;
+    for (int t = lo + threadIdx.x; t < hi; t += kMgsThreads) {
+        const double x = w[t];
+        ws[t - lo] = x;
+        s += x * x;
+    }
+    int p = 0;
+    const double w2 = cluster_sum(s, wsum, slot, p);
+    if (rank == 0 && threadIdx.x == 0) *ww = w2;
+    for (int j = 0; j <= i + 1; j++) {
+        const double *v = V + (size_t)j * n;
+        double d = 0.0;
+        if (j <= i)
+            for (int t = lo + threadIdx.x; t < hi; t += kMgsThreads) d += v[t] * ws[t - lo];
+        else
+            for (int t = lo + threadIdx.x; t < hi; t += kMgsThreads) d += ws[t - lo] * ws[t - lo];
+        p ^= 1;
+        const double hj = cluster_sum(d, wsum, slot, p);
+        if (j <= i) {
+            for (int t = lo + threadIdx.x; t < hi; t += kMgsThreads) ws[t - lo] = ws[t - lo] - hj * v[t];
+            if (rank == 0 && threadIdx.x == 0) h[j] = hj;
+        } else {
+            const double nr = sqrt(hj);
+            if (rank == 0 && threadIdx.x == 0) h[i + 1] = nr;
+            for (int t = lo + threadIdx.x; t < hi; t += kMgsThreads) w[t] = nr != 0.0 ? ws[t - lo] / nr : ws[t - lo];
+        }
+    }
+    cluster_sync_all();  // no CTA leaves while another may still read its slots
+}
+
+// ---- the reference's Givens step for column i on the device (one thread;
+// src/gmres_el.c:202-237), in its operation order without fused
+// multiply-adds; the iteration's residual estimate goes to err[i + 1], the
+// outcome to st[0] (0 running, 1 converged, 2 "CONVERGENCE RATE TOO SLOW")
+// and st[1] = iterations done.
+struct GivensDev {
+    double *H;     // (M + 2) x (M + 2), row-major
+    double *c, *s, *res, *err;
+    int *st;       // [0] status, [1] iterations
+    double *e0;    // err0
+    int M;
+};
+
+__global__ void k_givens64(GivensDev g, const double *__restrict__ hcol, const double *__restrict__ ww, int i,
+                           double tolerance)
+{
+    if (g.st[0] != 0) return;
+    const int ld = g.M + 2;
+    double *H = g.H;
+    for (int j = 0; j <= i + 1; j++) H[(size_t)j * ld + i] = hcol[j];
+    for (int j = 0; j + 1 <= i; j++) {
+        const double a = H[(size_t)j * ld + i], b = H[(size_t)(j + 1) * ld + i];
+        const double h1 = __dadd_rn(__dmul_rn(g.c[j], a), __dmul_rn(g.s[j], b));
+        const double h2 = __dadd_rn(__dmul_rn(-g.s[j], a), __dmul_rn(g.c[j], b));
+        H[(size_t)j * ld + i] = h1;
+        H[(size_t)(j + 1) * ld + i] = h2;
+    }
+    const double htmp = H[(size_t)(i + 1) * ld + i] / H[(size_t)i * ld + i];
+    if (sqrt(*ww) != 0.0) {
+        const double ci = 1.0 / sqrt(__dadd_rn(1.0, __dmul_rn(htmp, htmp)));
+        const double si = __dmul_rn(ci, htmp);
+        g.c[i] = ci;
+        g.s[i] = si;
+        H[(size_t)i * ld + i] = __dadd_rn(__dmul_rn(ci, H[(size_t)i * ld + i]), __dmul_rn(si, H[(size_t)(i + 1) * ld + i]));
+        H[(size_t)(i + 1) * ld + i] = 0.0;
+        g.res[i + 1] = __dmul_rn(-si, g.res[i]);
+        g.res[i] = __dmul_rn(ci, g.res[i]);
+    }
+    const double err1 = fabs(g.res[i + 1]);
+    g.err[i + 1] = err1;
+    g.st[1] = i + 1;
+    if (err1 < tolerance) g.st[0] = 1;
+    else if (fabs(__ddiv_rn(__dsub_rn(err1, *g.e0), *g.e0)) < 1.0e-6 * tolerance) g.st[0] = 2;
+    *g.e0 = err1;
+}
+
 // The compact N x 2N matrix as an operator.
 struct CompactOp : RealOp {
     const double *A;
@@ -124,7 +265,7 @@ struct CompactOp : RealOp {
     int N;
     int apply(const double *x, double *y, cudaStream_t st) override
     {
-        DSC_LAUNCH(k_matvec_compact<<<(N * 32 + 255) / 256, 256, 0, st>>>(A, lda, N, x, y));
+        DSC_LAUNCH(k_matvec_compact<<<(N * 32 + 255) / 256, 256, 0, st>>>(A, lda, N, x, y, skip));
         DSC_CUDA(cudaGetLastError());
         return kOk;
     }
@@ -201,8 +342,78 @@ int gmres_real_fp64(int n, RealOp &op, double *dB, const double *dx0, double tol
     double err0 = r0, err1 = r0;
     int status = 1;
     unsigned it = 0;
+    const size_t mgs_slice = ((size_t)n + kMgsCta - 1) / kMgsCta;
     if (err0 < tolerance) {
         status = 0;
+    } else if (mgs_slice <= kMgsMaxSlice) {
+        // Arnoldi columns in one cluster launch each and the Givens step on
+        // the device; the host only looks at the outcome every kPoll
+        // iterations (iterations queued after the stop return at once)
+        constexpr unsigned kPoll = 4;
+        DevBuf<double> dH, dcs, derr, de0;
+        DevBuf<int> dst;
+        DSC_TRY(dH.alloc((size_t)(M + 2) * (M + 2)));
+        DSC_TRY(dcs.alloc(3 * (size_t)(M + 2)));
+        DSC_TRY(derr.alloc(M + 2));
+        DSC_TRY(de0.alloc(1));
+        DSC_TRY(dst.alloc(2));
+        DSC_CUDA(cudaMemsetAsync(dH.p, 0, (size_t)(M + 2) * (M + 2) * sizeof(double), st));
+        DSC_CUDA(cudaMemsetAsync(dcs.p, 0, 3 * (size_t)(M + 2) * sizeof(double), st));
+        DSC_CUDA(cudaMemsetAsync(dst.p, 0, 2 * sizeof(int), st));
+        DSC_CUDA(cudaMemcpyAsync(dcs.p + 2 * (M + 2), &r0, sizeof(double), cudaMemcpyHostToDevice, st));
+        DSC_CUDA(cudaMemcpyAsync(de0.p, &r0, sizeof(double), cudaMemcpyHostToDevice, st));
+        GivensDev gd{dH.p, dcs.p, dcs.p + (M + 2), dcs.p + 2 * (M + 2), derr.p, dst.p, de0.p, (int)M};
+        const size_t smem = mgs_slice * sizeof(double);
+        DSC_TRY(raise_smem_limit((const void *)k_mgs_cluster, (int)smem));
+        op.skip = dst.p;  // status != 0: the operator's kernels return at once
+        int hst[2] = {0, 0};
+        for (unsigned i0 = 0; i0 < M && hst[0] == 0; i0 += kPoll) {
+            for (unsigned i = i0; i < std::min(M, i0 + kPoll); i++) {
+                double *vi = V.p + (size_t)i * n, *w = V.p + (size_t)(i + 1) * n;
+                DSC_TRY(op.apply(vi, w, st));
+                cudaLaunchConfig_t cfg = {};
+                cfg.gridDim = dim3(kMgsCta);
+                cfg.blockDim = dim3(kMgsThreads);
+                cfg.dynamicSmemBytes = smem;
+                cfg.stream = st;
+                cudaLaunchAttribute at[1];
+                at[0].id = cudaLaunchAttributeClusterDimension;
+                at[0].val.clusterDim.x = kMgsCta;
+                at[0].val.clusterDim.y = 1;
+                at[0].val.clusterDim.z = 1;
+                cfg.attrs = at;
+                cfg.numAttrs = 1;
+                note_launch();
+                DSC_CUDA(cudaLaunchKernelEx(&cfg, k_mgs_cluster, V.p, n, (int)i, hcol, aux, (const int *)dst.p));
+                DSC_LAUNCH(k_givens64<<<1, 1, 0, st>>>(gd, hcol, aux, (int)i, tolerance));
+                DSC_CUDA(cudaGetLastError());
+            }
+            DSC_CUDA(cudaMemcpyAsync(hst, dst.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+            DSC_CUDA(cudaStreamSynchronize(st));
+        }
+        op.skip = nullptr;
+        it = (unsigned)hst[1];
+        status = hst[0] == 1 ? 0 : hst[0] == 2 ? 2 : 1;
+        // the log lines and what the back substitution needs
+        std::vector<double> errs(M + 2);
+        DSC_CUDA(cudaMemcpyAsync(errs.data(), derr.p, (M + 2) * sizeof(double), cudaMemcpyDeviceToHost, st));
+        DSC_CUDA(cudaMemcpyAsync(h.data(), dH.p, (size_t)(it + 1) * (M + 2) * sizeof(double), cudaMemcpyDeviceToHost,
+                                 st));
+        DSC_CUDA(cudaMemcpyAsync(res.data(), dcs.p + 2 * (M + 2), (it + 1) * sizeof(double), cudaMemcpyDeviceToHost,
+                                 st));
+        DSC_CUDA(cudaStreamSynchronize(st));
+        if (log)
+            for (unsigned q = 1; q <= it; q++) fprintf(log, "%8d%25.4e\n", (int)q, errs[q]);
+        if (log) fflush(log);
+        if (status != 2) {
+            for (int i = (int)it - 1; i >= 0; i--) {
+                for (unsigned j = (unsigned)i + 1; j <= it; j++) res[i] -= H(i, j) * res[j];
+                res[i] = res[i] / H(i, i);
+            }
+            DSC_CUDA(cudaMemcpyAsync(resd.p, res.data(), it * sizeof(double), cudaMemcpyHostToDevice, st));
+            DSC_LAUNCH(k_update_x<<<vblocks, 256, 0, st>>>(x.p, V.p, n, resd.p, (int)it, n));
+            DSC_CUDA(cudaGetLastError());
+        }
     } else {
         for (unsigned i = 0; i < M; i++) {
             it++;

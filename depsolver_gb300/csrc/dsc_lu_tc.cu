@@ -1,0 +1,370 @@
+// dsc_lu_tc.cu -- the dense direct solve (gaussBksb, src/gaussBksb.c:39-108)
+// as a low-precision block LU on the tensor cores with FP64-residual
+// iterative refinement.
+//
+// Factorisation, without pivoting like the reference (which only swaps rows
+// when a pivot is within 1e-9 of zero), in 128 x 128 tiles of an FP32
+// working copy W of A (column-major, padded with the identity to a multiple
+// of 128).  Step k of the block LU A = L U (L unit lower by blocks, U upper
+// by blocks with the Schur complement's diagonal tiles):
+//   P_k = W_kk^-1                 Gauss-Jordan of the tile in registers of one
+//                                 CTA (gj_invert_tile); a pivot within 1e-9 of
+//                                 zero is reported with its row, as the
+//                                 reference's "Singularity in row" exit
+//   R_kJ = P_k W_kJ  (J > k)      FP32 pipes; R replaces row block k
+//   W_IJ -= W_Ik R_kJ (I, J > k)  the trailing update: one 3xFP16 product on
+//                                 the tensor cores (k_tc_gemm3's read-modify-
+//                                 write epilogue on the trailing sub-matrix),
+//                                 operands as row-scaled fp16 pairs
+// so that L_Ik = W_Ik P_k, U_kk = P_k^-1, U_kJ = P_k^-1 R_kJ, and a solve is
+//   forward:  z_k = P_k (r_k - sum_{j<k} W_kj z_j)
+//   backward: x_k = z_k - sum_{J>k} R_kJ x_J
+// (one kernel per tile step, FP32, each updating the remaining rows with the
+// finished tile's values).  The FP32-accurate factors solve the correction
+// equation of an FP64 iterative refinement: x = 0, r = b; d = LU^-1 r (on r
+// scaled to unit norm), x += d, r = b - A x with A in FP64; until |r| <=
+// tol |b|, the correction is below 1e-14 |x|, or the residual stops falling.
+#include <math.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "dsc_blas.cuh"
+#include "dsc_common.cuh"
+#include "dsc_gjtile.cuh"
+#include "dsc_gmres.h"
+#include "dsc_internal.h"
+#include "dsc_tcgemm.h"
+
+namespace dsc {
+
+constexpr float kLuPivTol = 1.0E-9f;  // the reference's singular-pivot threshold (src/gaussBksb.c:46)
+constexpr int kLuMaxRefine = 30;
+
+// W (column-major FP32, np x np) = A (row-major FP64, n x n, stride lda),
+// the identity on the padding; 32 x 32 tiles through shared memory.
+__global__ void k_lu_load(const double *__restrict__ A, size_t lda, int n, float *__restrict__ W, int np)
+{
+    __shared__ float t[32][33];
+    const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
+    for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+        const int r = r0 + y, c = c0 + threadIdx.x;
+        t[y][threadIdx.x] = (r < n && c < n) ? (float)A[(size_t)r * lda + c] : (r == c ? 1.0f : 0.0f);
+    }
+    __syncthreads();
+    for (int y = threadIdx.y; y < 32; y += blockDim.y) W[(size_t)(c0 + y) * np + r0 + threadIdx.x] = t[threadIdx.x][y];
+}
+
+// P_k = the inverse of the diagonal tile of step k.
+__global__ void __launch_bounds__(256) k_lu_pivot(const float *__restrict__ W, int np, int k, float *__restrict__ P,
+                                                   int *bad)
+{
+    grid_dep_wait();  // a programmatic dependent of the previous step's update
+    gj_invert_tile(W + (size_t)k * kPB * np + k * kPB, np, P + (size_t)k * kPB * kPB, kLuPivTol, bad, k * kPB);
+}
+
+// Step k, tile J = k + 1 + blockIdx.x: blockIdx.y = 0: R_kJ = P_k W_kJ
+// written into row block k and, transposed, as the update's B rows (the
+// tile's columns, 128 k-values each, at Bh + (J - k - 1) * 128 * 128);
+// blockIdx.y = 1: the column block's tile I = J as the update's A rows.
+__global__ void __launch_bounds__(256) k_lu_row(float *__restrict__ W, int np, int k, const float *__restrict__ P,
+                                                __half *__restrict__ Ah, __half *__restrict__ Al,
+                                                float *__restrict__ ra, __half *__restrict__ Bh,
+                                                __half *__restrict__ Bl, float *__restrict__ rb)
+{
+    grid_dep_wait();  // a programmatic dependent of the pivot inversion
+    const int J = k + 1 + blockIdx.x, o = blockIdx.x * kPB;
+    extern __shared__ float sm[];
+    float(*T)[129] = (float(*)[129])sm;  // T[r][c]
+    const int warp = threadIdx.x >> 5;
+    if (blockIdx.y == 1) {
+        // A row i of tile I = J: A[i][kk] = W(J*128 + i, k*128 + kk)
+        load_tile128(W + (size_t)k * kPB * np + J * kPB, (size_t)np, [&](int kk, int i, float v) { T[i][kk] = v; });
+        __syncthreads();
+        for (int i = warp; i < kPB; i += 8)
+            pre_row_pair(&T[i][0], Ah + (size_t)(o + i) * kPB, Al + (size_t)(o + i) * kPB, &ra[o + i]);
+        return;
+    }
+    const float *Pk = P + (size_t)k * kPB * kPB;
+    float(*Pt)[128] = (float(*)[128])(sm + kPB * 129);               // Pt[q][kk] = P[kk][q]
+    float(*Xs)[129] = (float(*)[129])(sm + kPB * 129 + kPB * 128);  // Xs[j][q] = W(k*128 + q, J*128 + j)
+    load_tile128(Pk, kPB, [&](int r, int c, float v) { Pt[c][r] = v; });
+    load_tile128(W + (size_t)J * kPB * np + k * kPB, (size_t)np, [&](int r, int c, float v) { Xs[r][c] = v; });
+    __syncthreads();
+    // thread (ty, tx): kk = 8 ty + u, j = tx + 16 v (u, v < 8)
+    const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
+    float acc[8][8];
+#pragma unroll
+    for (int u = 0; u < 8; u++)
+#pragma unroll
+        for (int v = 0; v < 8; v++) acc[u][v] = 0.0f;
+#pragma unroll 4
+    for (int q = 0; q < kPB; q++) {
+        const float4 p0 = *(const float4 *)&Pt[q][8 * ty], p1 = *(const float4 *)&Pt[q][8 * ty + 4];
+        const float pa[8] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w};
+        float xb[8];
+#pragma unroll
+        for (int v = 0; v < 8; v++) xb[v] = Xs[tx + 16 * v][q];
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+#pragma unroll
+            for (int v = 0; v < 8; v++) acc[u][v] = fmaf(pa[u], xb[v], acc[u][v]);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; u++)
+#pragma unroll
+        for (int v = 0; v < 8; v++) T[tx + 16 * v][8 * ty + u] = acc[u][v];
+    __syncthreads();
+    for (int t = threadIdx.x; t < kPB * kPB; t += blockDim.x) {
+        const int j = t >> 7, kk = t & 127;
+        W[(size_t)(J * kPB + j) * np + k * kPB + kk] = T[j][kk];
+    }
+    for (int jj = warp; jj < kPB; jj += 8)
+        pre_row_pair(&T[jj][0], Bh + (size_t)(o + jj) * kPB, Bl + (size_t)(o + jj) * kPB, &rb[o + jj]);
+}
+
+// Forward step k: z_k = P_k y_k (every block forms it from the finished y_k;
+// block 0 stores it), then y_r -= sum_c W(r, k*128 + c) z_k[c] for the rows
+// r >= (k + 1) * 128 of this block.
+__global__ void __launch_bounds__(256) k_lu_fwd(const float *__restrict__ W, int np, int k,
+                                                const float *__restrict__ P, float *__restrict__ y,
+                                                float *__restrict__ z)
+{
+    grid_dep_wait();
+    __shared__ float yk[kPB], zk[kPB];
+    const int kb = k * kPB;
+    if (threadIdx.x < kPB) yk[threadIdx.x] = y[kb + threadIdx.x];
+    __syncthreads();
+    const float *Pk = P + (size_t)k * kPB * kPB;
+    {
+        // row i of P_k by two threads (halves of the row), then a shuffle
+        const int i = threadIdx.x >> 1, h = threadIdx.x & 1;
+        float s = 0.0f;
+        const float *pr = Pk + (size_t)i * kPB + 64 * h;
+#pragma unroll 8
+        for (int q = 0; q < 64; q++) s = fmaf(pr[q], yk[64 * h + q], s);
+        s += __shfl_xor_sync(0xffffffffu, s, 1);
+        if (h == 0) zk[i] = s;
+    }
+    __syncthreads();
+    if (blockIdx.x == 0 && threadIdx.x < kPB) z[kb + threadIdx.x] = zk[threadIdx.x];
+    const int r = (k + 1) * kPB + blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= np) return;
+    float s = 0.0f;
+    const float *w = W + (size_t)kb * np + r;
+#pragma unroll 8
+    for (int c = 0; c < kPB; c++) s = fmaf(w[(size_t)c * np], zk[c], s);
+    y[r] -= s;
+}
+
+// Backward step k: x_k = z_k is final; z_r -= sum_c R(r, k*128 + c) x_k[c]
+// for the rows r < k * 128 of this block.
+__global__ void __launch_bounds__(256) k_lu_bwd(const float *__restrict__ W, int np, int k, float *__restrict__ z)
+{
+    grid_dep_wait();
+    __shared__ float xk[kPB];
+    const int kb = k * kPB;
+    if (threadIdx.x < kPB) xk[threadIdx.x] = z[kb + threadIdx.x];
+    __syncthreads();
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= kb) return;
+    float s = 0.0f;
+    const float *w = W + (size_t)kb * np + r;
+#pragma unroll 8
+    for (int c = 0; c < kPB; c++) s = fmaf(w[(size_t)c * np], xk[c], s);
+    z[r] -= s;
+}
+
+// y = r / scale (FP32), zero on the padding.
+__global__ void k_lu_scale_in(const double *__restrict__ r, int n, int np, const double *__restrict__ nrm2,
+                              float *__restrict__ y)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    const double s = sqrt(*nrm2);
+    y[i] = (i < n && s > 0.0) ? (float)(r[i] / s) : 0.0f;
+}
+
+// x += scale * z; dn2 partial = |scale z|^2 (reduction as k_dot)
+__global__ void k_lu_update(double *__restrict__ x, const float *__restrict__ z, int n,
+                            const double *__restrict__ nrm2, RedWork rw, double *__restrict__ dn2)
+{
+    __shared__ double sh[32];
+    const double s = sqrt(*nrm2);
+    double acc = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double d = s * (double)z[i];
+        x[i] += d;
+        acc += d * d;
+    }
+    finish_reduction(acc, rw, dn2, sh);
+}
+
+// r = b - A x (A row-major FP64, stride lda); one warp per row.
+__global__ void k_lu_residual(const double *__restrict__ A, size_t lda, int n, const double *__restrict__ b,
+                              const double *__restrict__ x, double *__restrict__ r)
+{
+    const int row = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (row >= n) return;
+    const double *a = A + (size_t)row * lda;
+    double s = 0.0;
+    for (int c = lane; c < n; c += 32) s = fma(a[c], x[c], s);
+    s = warp_sum(s);
+    if (lane == 0) r[row] = b[row] - s;
+}
+
+__global__ void k_lu_dot(const double *__restrict__ a, int n, RedWork rw, double *__restrict__ out)
+{
+    __shared__ double sh[32];
+    double acc = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) acc += a[i] * a[i];
+    finish_reduction(acc, rw, out, sh);
+}
+
+__global__ void k_lu_copy_b(const double *__restrict__ A, size_t lda, int n, double *__restrict__ b)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = A[(size_t)i * lda + n];
+}
+
+int lu_solve_mixed(int n, const double *dA, size_t lda, double *dx, double tol, LuMixedInfo *info, int *bad_row,
+                   cudaStream_t st)
+{
+    const int np = (n + kPB - 1) / kPB * kPB, nb = np / kPB;
+    DevBuf<float> W, P, y, z;
+    DevBuf<__half> gAh, gAl, gBh, gBl;
+    DevBuf<float> ra, rb;
+    DevBuf<int> bad, err;
+    DevBuf<double> b, r, scal, part;
+    DevBuf<unsigned> cnt;
+    DSC_TRY(W.alloc((size_t)np * np));
+    DSC_TRY(P.alloc((size_t)nb * kPB * kPB));
+    DSC_TRY(gAh.alloc((size_t)np * kPB));
+    DSC_TRY(gAl.alloc((size_t)np * kPB));
+    DSC_TRY(gBh.alloc((size_t)np * kPB));
+    DSC_TRY(gBl.alloc((size_t)np * kPB));
+    DSC_TRY(ra.alloc(np));
+    DSC_TRY(rb.alloc(np));
+    DSC_TRY(bad.alloc(1));
+    DSC_TRY(err.alloc(1));
+    DSC_TRY(y.alloc(np));
+    DSC_TRY(z.alloc(np));
+    DSC_TRY(b.alloc(n));
+    DSC_TRY(r.alloc(n));
+    DSC_TRY(scal.alloc(4));
+    DSC_TRY(part.alloc(kRedBlocks));
+    DSC_TRY(cnt.alloc(1));
+    const int big = 0x7FFFFFFF;
+    DSC_CUDA(cudaMemcpyAsync(bad.p, &big, sizeof(int), cudaMemcpyHostToDevice, st));
+    DSC_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), st));
+    DSC_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(unsigned), st));
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    struct EvGuard {
+        cudaEvent_t *e;
+        ~EvGuard()
+        {
+            for (int q = 0; q < 3; q++)
+                if (e[q]) cudaEventDestroy(e[q]);
+        }
+    } evg{ev};
+    for (int q = 0; q < 3; q++) DSC_CUDA(cudaEventCreate(&ev[q]));
+    DSC_CUDA(cudaEventRecord(ev[0], st));
+    DSC_LAUNCH(k_lu_load<<<dim3(np / 32, np / 32), dim3(32, 8), 0, st>>>(dA, lda, n, W.p, np));
+    DSC_CUDA(cudaGetLastError());
+    // ---- factorisation
+    const size_t rsmem = sizeof(float) * (2 * kPB * 129 + kPB * 128);
+    DSC_TRY(raise_smem_limit((const void *)k_lu_row, (int)rsmem));
+    for (int k = 0; k < nb; k++) {
+        DSC_TRY(launch_dependent(k_lu_pivot, dim3(1), dim3(256), 0, st, (const float *)W.p, np, k, P.p, bad.p));
+        if (k + 1 == nb) break;
+        const int rest = nb - k - 1, k1 = (k + 1) * kPB, m = np - k1;
+        DSC_TRY(launch_dependent(k_lu_row, dim3(rest, 2), dim3(256), rsmem, st, W.p, np, k, (const float *)P.p,
+                                 gAh.p, gAl.p, ra.p, gBh.p, gBl.p, rb.p));
+        // W_IJ -= A_I B_J^T on the trailing sub-matrix (no tile excluded)
+        TcGjPlan plan;
+        DSC_TRY(tc_gj_plan(plan, gAh.p, gAl.p, kPB, gBh.p, gBl.p, kPB, m, m, W.p + (size_t)k1 * np + k1,
+                           (size_t)np, err.p, ra.p, rb.p));
+        DSC_TRY(tc_gj_run(plan, big, st));
+    }
+    DSC_CUDA(cudaEventRecord(ev[1], st));
+    int hbad = big, herr = 0;
+    DSC_CUDA(cudaMemcpyAsync(&hbad, bad.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    DSC_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    DSC_CUDA(cudaStreamSynchronize(st));
+    if (herr) {
+        set_error("block LU: a pipeline wait of the tensor-core update gave up (code %d)", herr);
+        return kErrCuda;
+    }
+    if (hbad < n) {
+        if (bad_row) *bad_row = hbad;
+        set_error("Singularity in row %d in system matrix", hbad);
+        return kErrSingular;
+    }
+    if (info) info->factor_done = true;
+    // ---- refinement: x = 0, r = b
+    RedWork rw{part.p, cnt.p};
+    DSC_LAUNCH(k_lu_copy_b<<<(n + 255) / 256, 256, 0, st>>>(dA, lda, n, b.p));
+    DSC_CUDA(cudaMemcpyAsync(r.p, b.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    DSC_CUDA(cudaMemsetAsync(dx, 0, n * sizeof(double), st));
+    double *rn2 = scal.p, *dn2 = scal.p + 1;
+    DSC_LAUNCH(k_lu_dot<<<kRedBlocks, kRedThreads, 0, st>>>(b.p, n, rw, rn2));
+    double h[2];
+    DSC_CUDA(cudaMemcpyAsync(h, rn2, sizeof(double), cudaMemcpyDeviceToHost, st));
+    DSC_CUDA(cudaStreamSynchronize(st));
+    const double bnorm = sqrt(h[0]);
+    double rprev = bnorm;
+    int it = 0, status = 1;  // 1 running, 0 converged, 2 the residual stopped falling
+    if (bnorm == 0.0) status = 0;
+    const int vg = (np + 255) / 256;
+    while (status == 1 && it < kLuMaxRefine) {
+        it++;
+        // d = LU^-1 (r / |r|) |r|
+        DSC_LAUNCH(k_lu_scale_in<<<vg, 256, 0, st>>>(r.p, n, np, rn2, y.p));
+        for (int k = 0; k < nb; k++) {
+            const int rows = np - (k + 1) * kPB;
+            DSC_TRY(launch_dependent(k_lu_fwd, dim3(std::max(1, (rows + 255) / 256)), dim3(256), 0, st,
+                                     (const float *)W.p, np, k, (const float *)P.p, y.p, z.p));
+        }
+        for (int k = nb - 1; k >= 0; k--)
+            if (k > 0)
+                DSC_TRY(launch_dependent(k_lu_bwd, dim3((k * kPB + 255) / 256), dim3(256), 0, st,
+                                         (const float *)W.p, np, k, z.p));
+        DSC_LAUNCH(k_lu_update<<<kRedBlocks, kRedThreads, 0, st>>>(dx, z.p, n, rn2, rw, dn2));
+        DSC_LAUNCH(k_lu_residual<<<(n * 32 + 255) / 256, 256, 0, st>>>(dA, lda, n, b.p, dx, r.p));
+        DSC_LAUNCH(k_lu_dot<<<kRedBlocks, kRedThreads, 0, st>>>(r.p, n, rw, rn2));
+        DSC_LAUNCH(k_lu_dot<<<kRedBlocks, kRedThreads, 0, st>>>(dx, n, rw, scal.p + 2));
+        DSC_CUDA(cudaGetLastError());
+        double hv[3];
+        DSC_CUDA(cudaMemcpyAsync(hv, scal.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        DSC_CUDA(cudaStreamSynchronize(st));
+        const double rnorm = sqrt(hv[0]), dnorm = sqrt(hv[1]), xnorm = sqrt(hv[2]);
+        // converged: the residual is below the tolerance or the correction
+        // at the rounding level of x (1e-14 |x|); a residual that stops
+        // falling is accepted once the corrections are within 1e-12 |x|
+        // (the FP64 residual's own rounding), else the factors are too
+        // inaccurate for this matrix
+        if (rnorm <= tol * bnorm || dnorm <= 1e-14 * xnorm) status = 0;
+        else if (it >= 3 && rnorm > 0.5 * rprev) status = dnorm <= 1e-12 * xnorm ? 0 : 2;
+        if (info) {
+            info->refinements = it;
+            info->rel_residual = rnorm / bnorm;
+            info->last_correction = xnorm > 0.0 ? dnorm / xnorm : dnorm;
+        }
+        rprev = rnorm;
+    }
+    if (status == 1) status = 2;
+    DSC_CUDA(cudaEventRecord(ev[2], st));
+    DSC_CUDA(cudaEventSynchronize(ev[2]));
+    if (info) {
+        DSC_CUDA(cudaEventElapsedTime(&info->factor_ms, ev[0], ev[1]));
+        DSC_CUDA(cudaEventElapsedTime(&info->refine_ms, ev[1], ev[2]));
+    }
+    if (status != 0) {
+        set_error("block LU refinement: relative residual %.3e after %d steps (tolerance %.1e)",
+                  info ? info->rel_residual : 0.0, it, tol);
+        return kErrStagnation;
+    }
+    return kOk;
+}
+
+}  // namespace dsc

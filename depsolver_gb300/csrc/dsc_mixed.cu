@@ -16,6 +16,9 @@
 
 #include <algorithm>
 #include <limits>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "../../include/depsolver_cuda.h"
@@ -55,6 +58,21 @@ __global__ void k_residual(const double *__restrict__ Y, const double *__restric
     const double2 s = cs[(size_t)f * N + i], d = cd[(size_t)f * N + i], b = bt[(size_t)f * N + i];
     R[(size_t)(2 * f) * ld + i] = b.x - (s.x * yr - s.y * yi + d.x * xr - d.y * xi);
     R[(size_t)(2 * f + 1) * ld + i] = b.y - (s.x * yi + s.y * yr + d.x * xi + d.y * xr);
+}
+
+// y{re,im}[i] = the sum of k_gemv_K2's S split partials (FP64, in split order).
+__global__ void k_gemv_parts(const double *__restrict__ part, int S, int N, double *__restrict__ yr,
+                             double *__restrict__ yi)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    double tr = 0.0, ti = 0.0;
+    for (int s = 0; s < S; s++) {
+        tr += part[((size_t)s * 2) * N + i];
+        ti += part[((size_t)s * 2 + 1) * N + i];
+    }
+    yr[i] = tr;
+    yi[i] = ti;
 }
 
 // ---- Givens rotations and triangular solves on the device, one thread per
@@ -919,7 +937,8 @@ struct Session::Mixed {
     DevBuf<double> npart;   // per-block partials of |w|^2
     int dots_grid = 0, upd_grid = 0;  // one resident wave of the Gram-Schmidt kernels
     // batched field
-    DevBuf<double> sing, Enode, Fce, tot;
+    DevBuf<double> sing, Enode, Fce, tot, Xce, ptot;
+    DevBuf<double> gpart;  // split partials of the FP64 GEMV residual (no digits)
     DevBuf<double4> mst_geo;  // per (particle element, point): w J and the unit normal
     DevBuf<float> part;  // field partials per element group (FP32)
     // FP32 far-field pass: element centroids / offsets, split points, weights
@@ -935,16 +954,28 @@ int Session::make_k16()
     if (k16_ready && k64_ready) return kOk;
     DSC_TRY(assemble64(false));
     {
+        // K's row digits for the tensor-core first residual take 16 bytes
+        // per entry: kept when they fill at most a quarter of the device
+        // (a 100k-node scene's 173 GB do not), else the first residual is
+        // an FP64 GEMV over K64 per system
+        digits = residual_mode == kResidDigits;
+        if (residual_mode == kResidAuto) {
+            size_t fr = 0, tot = 0;
+            DSC_CUDA(cudaMemGetInfo(&fr, &tot));
+            digits = 2.0 * kKDigits * (double)ld * N <= 0.25 * (double)tot;
+        }
         TimerScope ts(&timer, kTConvertK, st);
         DSC_TRY(Kh16.alloc(ld * N));
         DSC_TRY(Kl16.alloc(ld * N));
-        DSC_TRY(Kdig.alloc(kKDigits * ld * N));
+        if (digits) DSC_TRY(Kdig.alloc(kKDigits * ld * N));
+        else Kdig.release();
         DSC_TRY(rowE.alloc(N));
         DSC_TRY(rsK.alloc(N));
         DSC_TRY(k16_row_scales(K64.p, ld, N, rowE.p, rsK.p, st));
-        DSC_TRY(split_transpose_K16(K64.p, ld, N, rowE.p, Kh16.p, Kl16.p, Kdig.p, ld * N, ld, st));
+        DSC_TRY(split_transpose_K16(K64.p, ld, N, rowE.p, Kh16.p, Kl16.p, digits ? Kdig.p : nullptr, ld * N, ld,
+                                    st));
         // bytes: K read (8), the fp16 pair and the digits written (2 each)
-        timer.add_work(kTConvertK, (8.0 + 2.0 * (2 + kKDigits)) * N * N);
+        timer.add_work(kTConvertK, (8.0 + 2.0 * (2 + (digits ? kKDigits : 0))) * N * N);
     }
     if (pre_on) DSC_TRY(precond_build(*this));
     k16_ready = true;
@@ -1058,13 +1089,116 @@ __global__ void k_prepare_systems(const int *__restrict__ iface_row, const doubl
     R[(size_t)(2 * f + 1) * ld + i] = r.y;
 }
 
+// ------------------------------------------------------------ autotuner
+// Split count of the sweep's tensor-core product K V (M = k = N, 2F
+// columns), chosen by measurement: the candidates around the heuristic
+// (tc_gemm_f16_splits_for: about eleven waves of one CTA per SM) are each
+// timed as the product plus the epilogue that sums its partial tiles, three
+// times with CUDA events on the session's stream, and the fastest median
+// wins.  Results are kept per (device, N, columns) for the whole process,
+// so a size is tuned once, by the first solve that meets it.
+static std::mutex g_tune_mu;
+static std::map<std::tuple<int, int, int>, int> g_tuned;
+static bool g_autotune = true;
+
+static int tuned_splits(Session &s, int F, int *out)
+{
+    Session::Mixed &w = *s.mx;
+    const int N = s.N, Nc = 2 * F;
+    const size_t ld = s.ld, blk = ld * (size_t)Nc;
+    const int h = tc_gemm_f16_splits_for(N, N);
+    int dev = 0;
+    DSC_CUDA(cudaGetDevice(&dev));
+    const auto key = std::make_tuple(dev, N, Nc);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        if (!g_autotune) {
+            *out = h;
+            return kOk;
+        }
+        auto it = g_tuned.find(key);
+        if (it != g_tuned.end()) {
+            *out = it->second;
+            return kOk;
+        }
+    }
+    std::vector<int> cand;
+    for (int c : {h / 3, h / 2, (2 * h) / 3, h, (3 * h) / 2, 2 * h, 3 * h}) {
+        const int v = tc_gemm_f16_splits_norm(N, std::max(1, c));
+        if (std::find(cand.begin(), cand.end(), v) == cand.end()) cand.push_back(v);
+    }
+    const int smax = *std::max_element(cand.begin(), cand.end());
+    DSC_TRY(w.Yp.alloc(blk * smax));
+    cudaEvent_t e0, e1;
+    DSC_CUDA(cudaEventCreate(&e0));
+    DSC_CUDA(cudaEventCreate(&e1));
+    int best = h;
+    float best_ms = 1e30f;
+    int rc = kOk;
+    for (int S : cand) {
+        float t[3];
+        for (int r = 0; r < 4 && rc == kOk; r++) {
+            cudaEventRecord(e0, s.st);
+            rc = tc_gemm_3xf16(s.Kh16.p, s.Kl16.p, ld, w.Vh.p, w.Vl.p, ld, N, Nc, N, w.Yp.p, ld, S, w.err.p, s.st,
+                               s.rsK.p, w.cscK.p);
+            if (rc != kOk) break;
+            const dim3 eg((N + 511) / 512, F);
+            rc = launch_dependent(k_apply_epilogue_splits, eg, dim3(256), 0, s.st, (const float *)w.Yp.p, S,
+                                  blk, (const float2 *)w.Vb.p, (const float2 *)w.cs32.p, (const float2 *)w.cd32.p,
+                                  w.W.p, N, ld, F, w.npart.p);
+            cudaEventRecord(e1, s.st);
+            if (rc == kOk && cudaEventSynchronize(e1) != cudaSuccess) rc = kErrCuda;
+            if (r > 0 && rc == kOk) cudaEventElapsedTime(&t[r - 1], e0, e1);  // the first run warms up
+        }
+        if (rc != kOk) break;
+        std::sort(t, t + 3);
+        if (t[1] < best_ms) {
+            best_ms = t[1];
+            best = S;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc == kErrCuda) set_error("split autotuner: %s", cudaGetErrorString(cudaGetLastError()));
+    DSC_TRY(rc);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tuned[key] = best;
+    }
+    *out = best;
+    return kOk;
+}
+
+int autotune_set(int on)
+{
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_autotune = on != 0;
+    return kOk;
+}
+
+// (N, columns, splits) of every tuned size, up to n of them; returns the count.
+int autotune_table(int *rows, int n)
+{
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    int k = 0;
+    for (const auto &kv : g_tuned) {
+        if (rows && k < n) {
+            rows[3 * k] = std::get<1>(kv.first);
+            rows[3 * k + 1] = std::get<2>(kv.first);
+            rows[3 * k + 2] = kv.second;
+        }
+        k++;
+    }
+    return k;
+}
+
 // One batch of F <= kMaxBatch frequencies.  status (F) receives each
 // system's outcome (kSysConverged, kSysCapped: max_iters inner iterations
 // taken without reaching tol, kSysStagnated: kOuterMax refinement steps
 // taken); the solution and forces of a system that did not converge are
 // NaN, the others are those of a batch of converged systems alone.
 static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsigned max_iters,
-                       double *sigma_host, double *tot_host, unsigned *iters, int *status)
+                       double *sigma_host, double *tot_host, unsigned *iters, int *status, double *part_host)
 {
     Session::Mixed &w = *s.mx;
     const int N = s.N;
@@ -1072,6 +1206,9 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
     const size_t blk = ld * 2 * (size_t)F;  // one N x 2F block
     cudaStream_t st = s.st;
     Timer *tm = &s.timer;
+    // the product's split count for this size (measured once per process)
+    DSC_TRY(tuned_splits(s, F, &w.S));
+    DSC_TRY(w.Yp.alloc(blk * w.S));
     if (s.pre_on) DSC_TRY(precond_build(s));  // no-op when built for this K
     const bool pre = s.pre_on && s.pre && s.pre->nb > 0 && s.pre->ready;
     if (pre) DSC_TRY(precond_reserve(s, F));
@@ -1226,7 +1363,22 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
         DSC_LAUNCH(k_update_solution<<<vg, 256, 0, st>>>(w.D.p, w.Vb.p, blk, N, ld, F, w.ycoef.p, w.mcount.p));
         if (pre) DSC_TRY(precond_apply_d(s, w.D.p, F, w.err.p));
         DSC_LAUNCH(k_axpy_blocks<<<vg, 256, 0, st>>>(w.Xs.p, w.D.p, N, ld, F));
-        if (outer == 0) {
+        if (outer == 0 && !s.digits) {
+            // the first residual in FP64 without K's digits: K x by an FP64
+            // GEMV over K64 for each system (K read once per system)
+            TimerScope ts(tm, kTGemvK, st);
+            const int rowblocks = (N + 255) / 256;
+            const int S = std::max(1, std::min(64, 4 * 152 / rowblocks)), cols = (N + S - 1) / S;
+            DSC_TRY(w.gpart.alloc((size_t)S * 2 * N));
+            for (int f = 0; f < F; f++) {
+                DSC_LAUNCH(k_gemv_K2<double><<<dim3(rowblocks, S), 256, 0, st>>>(
+                    s.K64.p, ld, N, w.Xs.p + (size_t)(2 * f) * ld, w.Xs.p + (size_t)(2 * f + 1) * ld, cols, w.gpart.p));
+                DSC_LAUNCH(k_gemv_parts<<<(N + 255) / 256, 256, 0, st>>>(w.gpart.p, S, N, w.Y64.p + (size_t)(2 * f) * ld,
+                                                                         w.Y64.p + (size_t)(2 * f + 1) * ld));
+                tm->add_work(kTGemvK, 8.0 * N * N);  // bytes of K read
+            }
+            DSC_LAUNCH(k_residual<<<vg, 256, 0, st>>>(w.Y64.p, w.Xs.p, w.cs.p, w.cd.p, w.bt.p, w.R.p, N, ld, F));
+        } else if (outer == 0) {
             // the first residual in FP64: r = bt - M x, with K x from
             //   K's row digits times x's column digits (fixed point, the
             //     21 digit products whose weight is within 2^-48 of the
@@ -1375,6 +1527,16 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
         if (tot_host)
             DSC_CUDA(cudaMemcpyAsync(tot_host, w.tot.p, (size_t)F * 9 * sizeof(double),
                                      cudaMemcpyDeviceToHost, st));
+        if (part_host && fp.npart > 0) {
+            // per particle: force, centre, scale, torque of every system
+            DSC_TRY(w.Xce.alloc((size_t)std::max(fp.npel, 1) * 3));
+            DSC_TRY(w.ptot.alloc((size_t)F * fp.npart * kPartVals));
+            DSC_TRY(mst_centres(s.dev, fp, w.Xce.p, st));
+            DSC_TRY(mst_particles(fp, s.dev.x.p, s.dev.y.p, s.dev.z.p, w.Fce.p, (size_t)fp.npel * 3, w.Xce.p, F,
+                                  w.ptot.p, st));
+            DSC_CUDA(cudaMemcpyAsync(part_host, w.ptot.p, (size_t)F * fp.npart * kPartVals * sizeof(double),
+                                     cudaMemcpyDeviceToHost, st));
+        }
     } else if (tot_host) {
         memset(tot_host, 0, (size_t)F * 9 * sizeof(double));
     }
@@ -1401,6 +1563,9 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
     for (int f = 0; f < F; f++) {
         if (status[f] == kSysConverged) continue;
         if (tot_host) std::fill(tot_host + (size_t)f * 9, tot_host + (size_t)f * 9 + 9, nan);
+        if (part_host && s.force.npart > 0)
+            std::fill(part_host + (size_t)f * s.force.npart * kPartVals,
+                      part_host + (size_t)(f + 1) * s.force.npart * kPartVals, nan);
         if (sigma_host) std::fill(sigma_host + (size_t)f * 2 * N, sigma_host + (size_t)(f + 1) * 2 * N, nan);
     }
     return kOk;
@@ -1423,11 +1588,15 @@ int Session::solve_mixed(unsigned nfreq, const double *freqs, double tol, unsign
                          double *sigma_host, double *forces_host, unsigned *iters)
 {
     last_status.assign(nfreq, kSysStagnated);
+    last_particles.clear();
     if (max_iters == 0) {
         set_error("mixed solve: max_iters must be at least 1");
         return kErrArg;
     }
     DSC_TRY(make_k16());
+    // the force plan (its particles) is joined by the assembly
+    DSC_TRY(force_wait());
+    last_particles.assign((size_t)nfreq * force.npart * kPartVals, std::numeric_limits<double>::quiet_NaN());
     if (!mx) mx = new Mixed();
     Mixed &w = *mx;
     const int Fmax = (int)std::min<unsigned>(nfreq, kMaxBatch);
@@ -1502,7 +1671,8 @@ int Session::solve_mixed(unsigned nfreq, const double *freqs, double tol, unsign
         DSC_TRY(mixed_batch(*this, F, freqs + f0, tol, max_iters,
                             sigma_host ? sigma_host + (size_t)f0 * 2 * N : nullptr,
                             forces_host ? forces_host + (size_t)f0 * 9 : nullptr,
-                            iters ? iters + f0 : nullptr, last_status.data() + f0));
+                            iters ? iters + f0 : nullptr, last_status.data() + f0,
+                            last_particles.data() + (size_t)f0 * force.npart * kPartVals));
     }
     return kOk;
 }

@@ -34,49 +34,13 @@ namespace dsc {
 
 // ---------------------------------------------------------------- kernels
 
-// part[s][0/1][i] = sum over the column split s of K[c][i] * x{re,im}[c];
-// K column-major; thread per row, x chunks staged in shared memory.
-template <typename T>
-__global__ void __launch_bounds__(256) k_gemv_K2(const T *__restrict__ K, size_t ld, int N,
-                                                 const double *__restrict__ xr,
-                                                 const double *__restrict__ xi, int cols,
-                                                 double *__restrict__ part)
-{
-    __shared__ double sxr[256], sxi[256];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int s = blockIdx.y;
-    const int c0 = s * cols, c1 = min(N, c0 + cols);
-    double ar = 0.0, ai = 0.0;
-    for (int cb = c0; cb < c1; cb += 256) {
-        __syncthreads();
-        if (cb + (int)threadIdx.x < c1) {
-            sxr[threadIdx.x] = xr[cb + threadIdx.x];
-            sxi[threadIdx.x] = xi[cb + threadIdx.x];
-        }
-        __syncthreads();
-        const int cn = min(256, c1 - cb);
-        if (i < N) {
-            const T *kp = K + (size_t)cb * ld + i;
-#pragma unroll 8
-            for (int c = 0; c < cn; c++) {
-                double k = (double)kp[(size_t)c * ld];
-                ar += k * sxr[c];
-                ai += k * sxi[c];
-            }
-        }
-    }
-    if (i < N) {
-        part[((size_t)s * 2) * N + i] = ar;
-        part[((size_t)s * 2 + 1) * N + i] = ai;
-    }
-}
-
 // y = K-form operator applied to x (real 2N layout), from the split sums.
 __global__ void k_kform_epilogue(const double *__restrict__ part, int S, int N,
                                  const double *__restrict__ ca, const double *__restrict__ cb,
                                  const double *__restrict__ cd, const double *__restrict__ x,
-                                 double *__restrict__ y)
+                                 double *__restrict__ y, const int *skip)
 {
+    if (skip && *skip) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     double tr = 0.0, ti = 0.0;
@@ -109,10 +73,10 @@ struct KFormOp : RealOp {
         {
             TimerScope ts(tm, kTGemvK, st);
             dim3 g((N + 255) / 256, S);
-            DSC_LAUNCH(k_gemv_K2<double><<<g, 256, 0, st>>>(K, ld, N, x, x + N, cols, part));
+            DSC_LAUNCH(k_gemv_K2<double><<<g, 256, 0, st>>>(K, ld, N, x, x + N, cols, part, skip));
             if (tm) tm->add_work(kTGemvK, 8.0 * N * N);  // bytes of K read
         }
-        DSC_LAUNCH(k_kform_epilogue<<<(N + 255) / 256, 256, 0, st>>>(part, S, N, ca, cb, cd, x, y));
+        DSC_LAUNCH(k_kform_epilogue<<<(N + 255) / 256, 256, 0, st>>>(part, S, N, ca, cb, cd, x, y, skip));
         DSC_CUDA(cudaGetLastError());
         return kOk;
     }
@@ -266,13 +230,18 @@ int Session::solve_fp64(double f, double tol, unsigned max_iters, double *sigma_
         B[i + N] = mbc[3 * (size_t)(i + N)];
     }
     // Jacobi scaling of the reference: row i (both halves) and B[i] (real
-    // part only) times 1 / A1[i][i] (src/gmres_el.c:87-93)
+    // part only) times 1 / A1[i][i] (src/gmres_el.c:87-93).  The imaginary
+    // right-hand side B[N + i] stays unscaled there, so with a complex
+    // boundary value (a phase-shifted electrode) the reference solves for an
+    // imaginary part off by the factor A1[i][i]; jacobi_full scales it too
+    // (the system the mixed mode solves)
     for (int i = 0; i < N; i++) {
         double p = 1.0 / (a[i] * Kdiag_host[i] + d[i]);
         a[i] *= p;
         b[i] *= p;
         d[i] *= p;
         B[i] *= p;
+        if (jacobi_full) B[i + N] *= p;
     }
     DSC_TRY(ca.upload(a, st));
     DSC_TRY(cb.upload(b, st));
@@ -342,6 +311,27 @@ extern "C" int dsc_session_set_timing(dsc_session *s, int on)
 extern "C" int dsc_session_set_preconditioner(dsc_session *s, int on)
 {
     s->s.pre_on = on != 0;
+    return kOk;
+}
+
+extern "C" int dsc_set_autotune(int on) { return autotune_set(on); }
+
+extern "C" int dsc_autotune_table(int *rows, int n) { return autotune_table(rows, n); }
+
+extern "C" int dsc_session_set_fp64_jacobi(dsc_session *s, int full)
+{
+    s->s.jacobi_full = full != 0;
+    return kOk;
+}
+
+extern "C" int dsc_session_set_residual(dsc_session *s, int how)
+{
+    if (how != DSC_RESIDUAL_AUTO && how != DSC_RESIDUAL_DIGITS && how != DSC_RESIDUAL_FP64) {
+        set_error("dsc_session_set_residual: unknown choice %d", how);
+        return kErrArg;
+    }
+    if (how != s->s.residual_mode) s->s.k16_ready = false;  // the digits follow the choice
+    s->s.residual_mode = how;
     return kOk;
 }
 
@@ -446,16 +436,25 @@ extern "C" int dsc_session_solve(dsc_session *sess, int mode, unsigned nfreq, co
     }
     const size_t n2 = 2 * (size_t)s.N;
     s.last_status.assign(nfreq, kSysStagnated);
-    DevBuf<double> sig, tot;
+    s.last_particles.clear();
+    DevBuf<double> sig, tot, ptot;
     DSC_TRY(sig.alloc(n2));
     DSC_TRY(tot.alloc(9 * (size_t)std::max(1u, nfreq)));
     const double nan = std::numeric_limits<double>::quiet_NaN();
+    size_t pv = 0;
     for (unsigned k = 0; k < nfreq; k++) {
         unsigned it = 0;
         // a frequency whose GMRES stops short (cap or stagnation) gets NaN
         // results and a status; the sweep goes on with the next one
         int rc = s.solve_fp64(freqs[k], tol, max_iters, sig.p, tot.p + 9 * (size_t)k, &it);
         if (iters) iters[k] = it;
+        if (k == 0) {
+            // the force plan (its particles) is joined by the first assembly
+            DSC_TRY(s.force_wait());
+            pv = (size_t)s.force.npart * kPartVals;
+            DSC_TRY(ptot.alloc(std::max<size_t>(1, pv * nfreq)));
+            s.last_particles.assign(pv * nfreq, nan);
+        }
         if (rc == kErrNoConverge || rc == kErrStagnation) {
             s.last_status[k] = rc == kErrNoConverge ? kSysCapped : kSysStagnated;
             DSC_CUDA(cudaStreamSynchronize(s.st));
@@ -468,6 +467,8 @@ extern "C" int dsc_session_solve(dsc_session *sess, int mode, unsigned nfreq, co
         }
         if (rc != kOk) return rc;
         s.last_status[k] = kSysConverged;
+        DSC_TRY(mst_particles(s.force, s.dev.x.p, s.dev.y.p, s.dev.z.p, s.force.Fce.p, 0, s.force.Xce.p, 1,
+                              ptot.p + pv * k, s.st));
         if (sigma)
             DSC_CUDA(cudaMemcpyAsync(sigma + n2 * k, sig.p, n2 * sizeof(double), cudaMemcpyDeviceToHost,
                                      s.st));
@@ -475,8 +476,24 @@ extern "C" int dsc_session_solve(dsc_session *sess, int mode, unsigned nfreq, co
     if (forces)
         DSC_CUDA(cudaMemcpyAsync(forces, tot.p, 9 * (size_t)nfreq * sizeof(double),
                                  cudaMemcpyDeviceToHost, s.st));
+    std::vector<double> ph(pv * nfreq);
+    if (pv) DSC_CUDA(cudaMemcpyAsync(ph.data(), ptot.p, ph.size() * sizeof(double), cudaMemcpyDeviceToHost, s.st));
     DSC_CUDA(cudaStreamSynchronize(s.st));
+    for (unsigned k = 0; k < nfreq; k++)
+        if (s.last_status[k] == kSysConverged)
+            std::copy(ph.begin() + pv * k, ph.begin() + pv * (k + 1), s.last_particles.begin() + pv * k);
     return sweep_status(s.last_status);
+}
+
+extern "C" int dsc_session_particles(dsc_session *sess, double *out, unsigned n)
+{
+    const Session &s = sess->s;
+    const size_t pv = (size_t)s.force.npart * kPartVals;
+    if (out && pv) {
+        const size_t nf = pv ? s.last_particles.size() / pv : 0;
+        std::copy(s.last_particles.begin(), s.last_particles.begin() + pv * std::min<size_t>(n, nf), out);
+    }
+    return s.force.npart;
 }
 
 extern "C" int dsc_session_status(dsc_session *sess, int *status, unsigned n)

@@ -68,14 +68,21 @@ struct Session {
     DevBuf<double> Wsing;
     DevBuf<double> K64, Kdiag;
     std::vector<double> Kdiag_host;
-    // plain FP64 path workspace
+    // plain FP64 path workspace; jacobi_full: its Jacobi scaling also
+    // scales the imaginary right-hand side (the reference scales B[i] only)
     DevBuf<double> ca, cb, cd, gemv_part;
+    bool jacobi_full = false;
 
     // mixed path: K as row-major scaled fp16 pairs (2^s_i fl32(K) per row i)
     // for the tensor-core products, K's fixed-point row digits (kKDigits
     // fp16 matrices) for the first FP64-accurate residual, the epilogue's
     // row factors, and the batched-solver workspace
     bool k16_ready = false;
+    // the first residual's K x: from K's digits on the tensor cores, or by
+    // an FP64 GEMV over K64 (residual_mode: kResidAuto decides by size)
+    enum { kResidAuto = 0, kResidDigits = 1, kResidFp64 = 2 };
+    int residual_mode = kResidAuto;
+    bool digits = true;
     DevBuf<__half> Kh16, Kl16, Kdig;
     DevBuf<int> rowE;           // biased FP64 exponent of each row's largest entry
     DevBuf<float> rsK;          // 2^-s_i
@@ -105,8 +112,15 @@ struct Session {
     int collect_timing(double *ms, int *count, double *work);
     int solve_mixed(unsigned nfreq, const double *freqs, double tol, unsigned max_iters,
                     double *sigma_host, double *forces_host, unsigned *iters);
-    // outcome of each system of the last solve (SysStatus)
+    // outcome of each system of the last solve (SysStatus), and the
+    // per-particle results of its systems (nfreq x force.npart x kPartVals)
     std::vector<int> last_status;
+    std::vector<double> last_particles;
 };
+
+// The split-count autotuner of the mixed sweep's tensor-core product
+// (dsc_mixed.cu): on/off, and its table of tuned sizes.
+int autotune_set(int on);
+int autotune_table(int *rows, int n);
 
 }  // namespace dsc

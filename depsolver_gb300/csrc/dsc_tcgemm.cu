@@ -647,6 +647,8 @@ int tc_gemm_splits_for(int M, int Kd) { return splits_for_bk(M, Kd, kTcBK); }
 
 int tc_gemm_f16_splits_for(int M, int Kd) { return splits_for_bk(M, Kd, kTcBK16); }
 
+int tc_gemm_f16_splits_norm(int Kd, int splits) { return splits_norm((Kd + kTcBK16 - 1) / kTcBK16, splits); }
+
 // ---------------------------------------------------------- operand split
 // tf32 pair of a value: hi = round-to-nearest tf32, lo = value - hi, also
 // rounded to tf32 (the tensor core would truncate it).

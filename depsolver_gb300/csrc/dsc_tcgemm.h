@@ -47,6 +47,9 @@ int tc_gemm_3xf16(const __half *Ah, const __half *Al, size_t lda, const __half *
                   size_t ldb, int M, int Nc, int Kd, float *Y, size_t ldy, int splits, int *d_err,
                   cudaStream_t st, const float *rsc, const float *csc);
 int tc_gemm_f16_splits_for(int M, int Kd);
+// The split count tc_gemm_3xf16 actually uses when asked for `splits` (the
+// k-blocks dealt evenly: the number of partial tiles it writes).
+int tc_gemm_f16_splits_norm(int Kd, int splits);
 // One fp16 product per split, for integer-valued operands ("digits"):
 // Y[s][n][m] = sum over split s's k-range of A[m][k] * B[n][k], each split
 // at most 4096 k long, so that with |A| <= 32 and |B| <= 128 (or any pair

@@ -308,6 +308,47 @@ def quadrupole_trap(nen: int = 6, seed: int = 7, levels=(3, 3, 4, 4),
     return _assemble(parts, nen, mat, ifaces, freq, f"quadrupole-trap-tria{nen}")
 
 
+def capacitor(cells: int = 25, *, nen: int = 6, side: float = 20.0, gap: float = 2.0,
+              volts: float = 1.0, eps_r: float = 80.0, freq: float = 1.0e6) -> Scene:
+    """Two parallel square plates (side x side, cells x cells quads split into
+    triangles) at z = +-gap/2 held at +-volts in one medium: conductors only,
+    a real system.  cells = 25, tria6: 2 x 2601 = 5202 nodes and 2500
+    elements, the size of the reference's capacitor-1/quadratic example."""
+    top_n, top_e = plate(side, side, cells, cells, (0, 0, gap / 2), nen)
+    bot_n, bot_e = plate(side, side, cells, cells, (0, 0, -gap / 2), nen)
+    parts = [(top_n, top_e, "conductor", volts), (bot_n, bot_e, "conductor", -volts)]
+    return _assemble(parts, nen, [[0.0, eps_r]], np.zeros((0, 2)), freq, f"capacitor-{cells}x{cells}-tria{nen}")
+
+
+def comb_trap(nen: int = 6, fingers: int = 10, finger=(2.0, 8.0), cells=(8, 32), pitch: float = 3.0,
+              overlap: float = 6.0, spheres: int = 8, sphere_level: int = 4, radius: float = 1.0,
+              spacing: float = 2.5, height: float = 2.0, volts: float = 1.0, freq: float = 1.0e6,
+              medium=(1.0e-4, 78.0), particle=(1.0e-3, 2.5)) -> Scene:
+    """Castellated trap: two interdigitated combs of `fingers` fingers each,
+    alternating in x at `pitch` in the plane z = 0 (each finger w x l,
+    cells[0] x cells[1] quads split into triangles; comb A's fingers, at
+    +volts, span y in [overlap/2 - l, overlap/2], comb B's, at -volts,
+    [-overlap/2, l - overlap/2]), and a chain of `spheres` spheres along x
+    at height z = height, all of one particle material on interface 1.
+    Defaults: 20 fingers of 8 x 32 cells (1105 tria6 nodes each) and 8
+    level-4 spheres: N = 104036, E = 51200."""
+    w, l = finger
+    parts = []
+    n_f = 2 * fingers
+    x0 = -(n_f - 1) * pitch / 2.0
+    for q in range(n_f):
+        a = q % 2 == 0
+        yc = (overlap / 2.0 - l / 2.0) if a else (l / 2.0 - overlap / 2.0)
+        n, e = plate(w, l, cells[0], cells[1], (x0 + q * pitch, yc, 0.0), nen)
+        parts.append((n, e, "conductor", volts if a else -volts))
+    xs = -(spheres - 1) * spacing / 2.0
+    for k in range(spheres):
+        n, e = icosphere(sphere_level, radius, (xs + k * spacing, 0.0, height), nen)
+        parts.append((n, e, "particle", 1))
+    return _assemble(parts, nen, [list(medium), list(particle)], [[1, 2]], freq,
+                     f"comb-trap-{fingers}x2-spheres{spheres}-L{sphere_level}-tria{nen}")
+
+
 def plates_only(plate_cells: int = 10, *, nen: int = 6, plate_side: float = 20.0,
                 plate_z: float = 5.0, volts: float = 1.0, freq: float = 1.0e6,
                 medium=(1.0e-4, 78.0), particle=(1.0e-3, 2.5)) -> Scene:

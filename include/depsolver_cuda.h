@@ -123,6 +123,27 @@ int dsc_assemble(int nen, int full, unsigned N, unsigned E, unsigned nIf, const 
  * the solution; A is left unchanged. */
 int dsc_gauss(unsigned n, const double *A, size_t lda, double *B);
 
+/* How gaussBksb and dsc_gauss solve (process-wide; no counterpart in the
+ * reference, whose gaussBksb is the FP64 elimination of src/gaussBksb.c):
+ *   DSC_GAUSS_MIXED (default) -- block LU without pivoting in FP32 tiles,
+ *     its trailing updates as 3xFP16 products on the tensor cores, then FP64
+ *     iterative refinement (residual b - A x with A in FP64) until the
+ *     correction is at FP64's rounding level of x; if the residual stops
+ *     falling first (factors too inaccurate for the matrix), the solve is
+ *     redone with the FP64 LU;
+ *   DSC_GAUSS_FP64 -- blocked FP64 LU without pivoting.
+ * Both report a pivot within 1e-9 of zero as the reference does
+ * ("Singularity in row"; DSC_ERR_SINGULAR for dsc_gauss).
+ * dsc_gauss_info gives the last mixed solve's refinement steps, final
+ * relative residual |b - A x| / |b|, whether it fell back to the FP64 LU,
+ * and in ms[0..1] (may be NULL) the device time of the factorisation
+ * (conversion to FP32 included) and of the refinement; it returns the mode.
+ * Any pointer may be NULL. */
+#define DSC_GAUSS_MIXED 0
+#define DSC_GAUSS_FP64 1
+int dsc_set_gauss_mode(int mode);
+int dsc_gauss_info(int *refinements, double *rel_residual, int *fell_back, double *ms);
+
 /* Flat form of solverGMRES_el with the tolerance (relative to |B|, the
  * reference compiles 1e-6) and the iteration cap (600) as arguments.
  * A (N x 2N, stride lda) is left unchanged; B is overwritten with the
@@ -216,6 +237,25 @@ int dsc_session_set_mixed_assembly(dsc_session *s, int prec);
  * every 64 quadrature points) and the near ones on the FP32 pipes; off
  * takes all of them on the FP32 pipes. */
 int dsc_session_set_field_tensor(dsc_session *s, int on);
+/* FP64 mode's Jacobi scaling.  The reference scales row i of the compact
+ * matrix and B[i] by 1 / A[i][i] but leaves B[N + i], the imaginary
+ * right-hand side, unscaled (src/gmres_el.c:87-93): with a complex boundary
+ * value (a phase-shifted electrode, e.g. a rotating-field trap) it solves
+ * for an imaginary part off by the factor A[i][i].  full = 0 (default)
+ * keeps that behaviour (parity with the reference); full = 1 scales B[N + i]
+ * as well, which solves the assembled system itself (what the mixed mode
+ * does).  With real boundary values the two are identical. */
+int dsc_session_set_fp64_jacobi(dsc_session *s, int full);
+/* Mixed mode's first FP64-accurate residual r = b - M x: K x either from
+ * K's eight fixed-point row digits on the tensor cores (exact integer digit
+ * products; the digits take 16 bytes per entry of K beside it) or by an
+ * FP64 GEMV over the FP64 K for each system (K read once per system).
+ * DSC_RESIDUAL_AUTO (default) keeps the digits when they fill at most a
+ * quarter of the device's memory (so a 100k-node scene takes the GEMV). */
+#define DSC_RESIDUAL_AUTO 0
+#define DSC_RESIDUAL_DIGITS 1
+#define DSC_RESIDUAL_FP64 2
+int dsc_session_set_residual(dsc_session *s, int how);
 /* The geometric matrix K (N x N) as assembled for `mode` (assembling it if
  * needed): K[c * ldk + i] = entry (row i, node c), i.e. C * int G N_c for
  * conductor rows and int H N_c for interface rows (src/assembly_el.c). */
@@ -228,6 +268,20 @@ int dsc_session_solve(dsc_session *s, int mode, unsigned nfreq, const double *fr
 /* Outcome of each system of the session's last solve: writes up to n of
  * them to status (may be NULL) and returns how many systems it solved. */
 int dsc_session_status(dsc_session *s, int *status, unsigned n);
+/* Maxwell-stress results per particle of the last solve (the reference
+ * sums every type-6 element into one force, src/force.c:516-547; the
+ * per-particle force is that sum over one particle's elements, i.e. its
+ * forceMST_* with vBCType masked to that particle).  A particle is a
+ * connected set of type-6 elements (elements sharing a node), numbered by
+ * their lowest node id.  Returns the number of particles P and writes, for
+ * the first n systems of the last solve, P x 12 doubles each to out (may be
+ * NULL): force[3], centre[3] (the mean of its type-6 nodes, as Xcm),
+ * sum |Fce|[3] over its elements, torque[3] about the centre: sum over its
+ * elements of (Xce - centre) x Fce, Xce the point X(1/4, 1/4) where the
+ * reference reports an element's force (an extension: the reference has no
+ * torque; like the force it is the stress of Re(E) only).  NaN for systems
+ * that did not converge. */
+int dsc_session_particles(dsc_session *s, double *out, unsigned n);
 /* CUDA-event timing of kernel classes (off by default).  Since the last
  * call: ms[k] the summed time of class k, count[k] its timed scopes and
  * work[k] its algorithmic work (any of the three may be NULL; n entries):
@@ -369,6 +423,18 @@ int dsc_positions_solve(dsc_positions *p, unsigned npos, const unsigned *tmpl, c
  * be NULL, else a system that did not converge gives NaN).  Host only. */
 double dsc_force_crossover(unsigned nfreq, const double *freqs, const double *forces,
                            const int *status);
+
+/* Autotuner of the mixed sweep's tensor-core product (no counterpart in the
+ * reference): the product of K with the 2F Krylov columns is split along k
+ * into partial tiles; the split count is chosen by timing the candidates
+ * around the built-in rule (about eleven waves of one CTA per SM) as the
+ * product plus the epilogue that sums the tiles, with CUDA events, the
+ * first time a solve meets a (device, N, 2F) size; the choice is kept for
+ * the process.  dsc_set_autotune(0) uses the rule alone (default on).
+ * dsc_autotune_table writes up to n rows of (N, columns, splits) to rows
+ * (3 ints each, may be NULL) and returns the number of tuned sizes. */
+int dsc_set_autotune(int on);
+int dsc_autotune_table(int *rows, int n);
 
 /* One-call sweep from host arrays (session created and destroyed inside). */
 int dsc_sweep(int nen, unsigned N, unsigned E, const double *nodes, const unsigned *elems,

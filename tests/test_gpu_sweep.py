@@ -229,3 +229,55 @@ def test_sweeps_of_different_sizes_on_one_session(gpu):
     f3, _, _ = api.Session(sc).solve(freqs, mode=api.MODE_MIXED, tol=1e-10)
     f4, _, _ = api.Session(sc).solve(freqs[64:], mode=api.MODE_MIXED, tol=1e-10)
     assert np.array_equal(f3[64:], f4)
+
+
+def test_fp64_gemv_first_residual_matches_digits(gpu):
+    """The mixed mode's first residual from an FP64 GEMV over K (the path of
+    scenes whose K digits would not fit the device) lands on the same
+    solution as the tensor-core digit product."""
+    sc = scenes.small(nen=6, sphere_level=2, plate_cells=4)
+    freqs = np.logspace(3, 8, 4)
+    s = api.Session(sc)
+    fd, _, sd = s.solve(freqs, mode=api.MODE_MIXED, tol=1e-11, want_sigma=True)
+    s.set_residual(api.RESIDUAL_FP64)
+    s.set_timing(True)
+    s.timing()
+    fg, _, sg = s.solve(freqs, mode=api.MODE_MIXED, tol=1e-11, want_sigma=True)
+    t = s.timing()
+    assert t["residual_fp64"][1] == 0 and t["gemv_K64"][1] >= 1   # no digit products: the GEMV ran
+    for k in range(len(freqs)):
+        assert relerr(sg[k], sd[k]) < 1e-9, k
+        assert np.abs(fg[k, :3] - fd[k, :3]).max() <= 1e-8 * fd[k, 6:9].sum(), k
+
+
+def test_comb_trap_mixed_matches_fp64(gpu):
+    """A small castellated trap (two interdigitated combs, a chain of
+    spheres): many conductor blocks and several particles in one solve."""
+    sc = scenes.comb_trap(fingers=3, cells=(2, 8), spheres=3, sphere_level=2, spacing=2.5)
+    s = api.Session(sc)
+    assert len(s.preconditioner_blocks()) == 6
+    fm, _, sm = s.solve([1e6], mode=api.MODE_MIXED, tol=1e-10, want_sigma=True)
+    pm = s.particles()[0]
+    f64, _, s64 = s.solve([1e6], mode=api.MODE_FP64, tol=1e-12, want_sigma=True)
+    p64 = s.particles()[0]
+    assert pm.shape == (3, 12)
+    assert np.abs(fm[0, :3] - f64[0, :3]).max() <= FORCE_TOL * f64[0, 6:9].sum()
+    for k in range(3):
+        assert np.abs(pm[k, :3] - p64[k, :3]).max() <= FORCE_TOL * p64[k, 6:9].sum(), k
+
+
+def test_autotuned_splits_keep_the_solution(gpu):
+    """The split count the autotuner picks for the tensor-core product only
+    changes the rounding of the products, not the solution."""
+    sc = scenes.small(nen=6, sphere_level=2, plate_cells=5)
+    freqs = np.logspace(3, 8, 5)
+    api.set_autotune(False)
+    try:
+        f0, _, s0 = api.Session(sc).solve(freqs, mode=api.MODE_MIXED, tol=1e-11, want_sigma=True)
+    finally:
+        api.set_autotune(True)
+    f1, _, s1 = api.Session(sc).solve(freqs, mode=api.MODE_MIXED, tol=1e-11, want_sigma=True)
+    assert any(r[0] == sc.N and r[1] == 2 * len(freqs) and r[2] >= 1 for r in api.autotune_table())
+    for k in range(len(freqs)):
+        assert relerr(s1[k], s0[k]) < 1e-9, k
+        assert np.abs(f1[k, :3] - f0[k, :3]).max() <= 1e-8 * f0[k, 6:9].sum(), k
