@@ -11,6 +11,7 @@
 
 #include <memory>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "../../include/depsolver_cuda.h"
@@ -85,6 +86,70 @@ static int ensure_pinned(size_t bytes)
     DSC_CUDA(cudaHostAlloc((void **)&c.pinned, bytes, cudaHostAllocDefault));
     c.pinned_bytes = bytes;
     return kOk;
+}
+
+// ---------------------------------------------------------------- row movers
+// The drop-ins' matrices are the reference's row-pointer arrays (or strided
+// flat rows), gigabytes at the 12k-node scene.  They move in chunks of rows
+// through two halves of one pinned buffer: host threads fill (or drain) one
+// half while the copy engine moves the other.
+constexpr size_t kMoverChunkBytes = (size_t)128 << 20;
+
+static int mover_threads()
+{
+    const unsigned h = std::thread::hardware_concurrency();
+    return (int)std::max(1u, std::min(16u, h ? h : 1u));
+}
+
+// fn(r) for r in [r0, r1) on the host threads (contiguous ranges).
+template <typename Fn>
+static void host_parallel_rows(size_t r0, size_t r1, Fn fn)
+{
+    const int T = mover_threads();
+    const size_t n = r1 - r0;
+    if (T == 1 || n < 64) {
+        for (size_t r = r0; r < r1; r++) fn(r);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (int t = 0; t < T; t++) {
+        const size_t a = r0 + n * t / T, b = r0 + n * (t + 1) / T;
+        th.emplace_back([=] {
+            for (size_t r = a; r < b; r++) fn(r);
+        });
+    }
+    for (auto &x : th) x.join();
+}
+
+// dst (device, row r at dst + r * ldd) row r = fill(r, host row of ldd
+// doubles) for r < nrows.
+template <typename Fill>
+static int rows_to_device(size_t nrows, size_t ldd, double *dst, Fill fill, cudaStream_t st)
+{
+    const size_t per = std::max<size_t>(1, kMoverChunkBytes / (ldd * sizeof(double)));
+    DSC_TRY(ensure_pinned(2 * per * ldd * sizeof(double)));
+    double *half[2] = {ctx().pinned, ctx().pinned + per * ldd};
+    cudaEvent_t ev[2];
+    DSC_CUDA(cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming));
+    DSC_CUDA(cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming));
+    int rc = kOk;
+    size_t q = 0;
+    for (size_t r0 = 0; r0 < nrows && rc == kOk; r0 += per, q++) {
+        const size_t r1 = std::min(nrows, r0 + per);
+        double *h = half[q & 1];
+        if (q >= 2 && cudaEventSynchronize(ev[q & 1]) != cudaSuccess) rc = kErrCuda;  // its last copy is done
+        if (rc != kOk) break;
+        host_parallel_rows(r0, r1, [&](size_t r) { fill(r, h + (r - r0) * ldd); });
+        if (cudaMemcpyAsync(dst + r0 * ldd, h, (r1 - r0) * ldd * sizeof(double), cudaMemcpyHostToDevice, st) !=
+                cudaSuccess ||
+            cudaEventRecord(ev[q & 1], st) != cudaSuccess)
+            rc = kErrCuda;
+    }
+    if (rc == kOk && cudaStreamSynchronize(st) != cudaSuccess) rc = kErrCuda;
+    if (rc != kOk) set_error("row upload: %s", cudaGetErrorString(cudaGetLastError()));
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    return rc;
 }
 
 static uint64_t mix(uint64_t h, uint64_t v)
@@ -273,23 +338,48 @@ static int assemble_impl(int nen, int full, unsigned N, unsigned E, unsigned nIf
 
     const size_t ncol = 2 * (size_t)N;
     const int nrows = full ? 2 * (int)N : (int)N;
-    // staging block of at most 64 MiB (and at least 32 rows)
-    int rows_per = (int)std::max<size_t>(32, ((size_t)64 << 20) / (ncol * sizeof(double)) / 32 * 32);
+    // chunks of rows formed on the device into one of two staging blocks,
+    // copied into one of two pinned halves; the host threads add chunk q - 1
+    // into the caller's rows while chunk q is formed and copied
+    int rows_per = (int)std::max<size_t>(32, kMoverChunkBytes / (ncol * sizeof(double)) / 32 * 32);
     rows_per = std::min(rows_per, (nrows + 31) / 32 * 32);
-    DSC_TRY(stage.alloc((size_t)rows_per * ncol));
-    DSC_TRY(ensure_pinned((size_t)rows_per * ncol * sizeof(double)));
-    double *host = ctx().pinned;
-    for (int r0 = 0; r0 < nrows; r0 += rows_per) {
-        const int r1 = std::min(nrows, r0 + rows_per);
-        dim3 grid(((int)N + 31) / 32, (r1 - r0 + 31) / 32), blk(32, 8);
-        DSC_LAUNCH(k_form_rows<<<grid, blk, 0, st>>>(K.p, ld, (int)N, full, r0, r1, dca.p, dcb.p, dcd.p, stage.p));
-        DSC_CUDA(cudaGetLastError());
-        DSC_CUDA(cudaMemcpyAsync(host, stage.p, (size_t)(r1 - r0) * ncol * sizeof(double),
-                                 cudaMemcpyDeviceToHost, st));
-        DSC_CUDA(cudaStreamSynchronize(st));
-        for (int r = r0; r < r1; r++) sink(user, r, host + (size_t)(r - r0) * ncol, ncol);
+    const size_t cb_ = (size_t)rows_per * ncol;
+    DSC_TRY(stage.alloc(2 * cb_));
+    DSC_TRY(ensure_pinned(2 * cb_ * sizeof(double)));
+    double *half[2] = {ctx().pinned, ctx().pinned + cb_};
+    cudaEvent_t ev[2];
+    DSC_CUDA(cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming));
+    DSC_CUDA(cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming));
+    int rc = kOk;
+    const int nq = (nrows + rows_per - 1) / rows_per;
+    for (int q = 0; q <= nq && rc == kOk; q++) {
+        if (q < nq) {
+            const int r0 = q * rows_per, r1 = std::min(nrows, r0 + rows_per);
+            double *sq = stage.p + (size_t)(q & 1) * cb_;
+            dim3 grid(((int)N + 31) / 32, (r1 - r0 + 31) / 32), blk(32, 8);
+            note_launch();
+            k_form_rows<<<grid, blk, 0, st>>>(K.p, ld, (int)N, full, r0, r1, dca.p, dcb.p, dcd.p, sq);
+            if (cudaGetLastError() != cudaSuccess ||
+                cudaMemcpyAsync(half[q & 1], sq, (size_t)(r1 - r0) * ncol * sizeof(double), cudaMemcpyDeviceToHost,
+                                st) != cudaSuccess ||
+                cudaEventRecord(ev[q & 1], st) != cudaSuccess)
+                rc = kErrCuda;
+        }
+        if (q >= 1 && rc == kOk) {
+            const int p = q - 1, r0 = p * rows_per, r1 = std::min(nrows, r0 + rows_per);
+            if (cudaEventSynchronize(ev[p & 1]) != cudaSuccess) {
+                rc = kErrCuda;
+                break;
+            }
+            const double *hp = half[p & 1];
+            host_parallel_rows((size_t)r0, (size_t)r1,
+                               [&](size_t r) { sink(user, (int)r, hp + (r - r0) * ncol, ncol); });
+        }
     }
-    return kOk;
+    if (rc != kOk) set_error("assembly rows to the host: %s", cudaGetErrorString(cudaGetLastError()));
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    return rc;
 }
 
 struct RowPtrSink {
@@ -323,22 +413,13 @@ static int gauss_impl(unsigned n, const double *const *rows, const double *flat,
     const size_t ldd = ((size_t)n + 1 + 31) / 32 * 32;
     DevBuf<double> A;
     DSC_TRY(A.alloc(ldd * n));
-    // pack rows (plus B as column n) through pinned memory, 64 MiB at a time
-    const size_t chunk = std::max<size_t>(1, ((size_t)64 << 20) / (ldd * sizeof(double)));
-    DSC_TRY(ensure_pinned(chunk * ldd * sizeof(double)));
-    double *host = ctx().pinned;
-    for (size_t r0 = 0; r0 < n; r0 += chunk) {
-        size_t r1 = std::min<size_t>(n, r0 + chunk);
-        for (size_t r = r0; r < r1; r++) {
-            const double *src = rows ? rows[r] : flat + r * lda;
-            double *dst = host + (r - r0) * ldd;
-            memcpy(dst, src, n * sizeof(double));
-            dst[n] = B[r];
-        }
-        DSC_CUDA(cudaMemcpyAsync(A.p + r0 * ldd, host, (r1 - r0) * ldd * sizeof(double),
-                                 cudaMemcpyHostToDevice, st));
-        DSC_CUDA(cudaStreamSynchronize(st));
-    }
+    // the rows, with B as column n
+    DSC_TRY(rows_to_device((size_t)n, ldd, A.p,
+                           [&](size_t r, double *dst) {
+                               memcpy(dst, rows ? rows[r] : flat + r * lda, n * sizeof(double));
+                               dst[n] = B[r];
+                           },
+                           st));
     DevBuf<double> x;
     DSC_TRY(x.alloc(n));
     Context &c = ctx();
@@ -370,17 +451,11 @@ static int gmres_impl(unsigned N, unsigned preCond, double tol, unsigned maxit,
     const size_t ldd = (ncol + 31) / 32 * 32;
     DevBuf<double> A, dB, dx0;
     DSC_TRY(A.alloc(ldd * N));
-    const size_t chunk = std::max<size_t>(1, ((size_t)64 << 20) / (ldd * sizeof(double)));
-    DSC_TRY(ensure_pinned(chunk * ldd * sizeof(double)));
-    double *host = ctx().pinned;
-    for (size_t r0 = 0; r0 < N; r0 += chunk) {
-        size_t r1 = std::min<size_t>(N, r0 + chunk);
-        for (size_t r = r0; r < r1; r++)
-            memcpy(host + (r - r0) * ldd, rows ? rows[r] : flat + r * lda, ncol * sizeof(double));
-        DSC_CUDA(cudaMemcpyAsync(A.p + r0 * ldd, host, (r1 - r0) * ldd * sizeof(double),
-                                 cudaMemcpyHostToDevice, st));
-        DSC_CUDA(cudaStreamSynchronize(st));
-    }
+    DSC_TRY(rows_to_device((size_t)N, ldd, A.p,
+                           [&](size_t r, double *dst) {
+                               memcpy(dst, rows ? rows[r] : flat + r * lda, ncol * sizeof(double));
+                           },
+                           st));
     DSC_TRY(dB.upload(B, ncol, st));
     if (x0) DSC_TRY(dx0.upload(x0, ncol, st));
     int rc = gmres_compact_fp64((int)N, A.p, ldd, dB.p, x0 ? dx0.p : nullptr, preCond, tol, maxit,

@@ -60,77 +60,73 @@ __device__ __forceinline__ void pre_row_pair(const float *v, __half *h, __half *
     if (lane == 0) *factor = pre_pow2(-sh);
 }
 
+// Threads of the CTA that inverts one tile (gj_invert_tile).
+constexpr int kGjThreads = 1024;
+
+// v[s] for a slot s known only at run time (selects, no local memory).
+__device__ __forceinline__ float gj_sel4(const float (&v)[4], int s)
+{
+    return s == 0 ? v[0] : s == 1 ? v[1] : s == 2 ? v[2] : v[3];
+}
+
 // P (row-major, 128 x 128) = inverse of the tile at T (column-major: element
 // (r, c) at T[c * ldt + r], 16-byte aligned columns) by Gauss-Jordan without
-// pivoting, in one CTA of 256 threads.  The tile lives in registers: thread
-// (tr, tc) = (t / 16, t % 16) owns rows 8 tr .. 8 tr + 7 and columns
-// 8 tc .. 8 tc + 7.  Per pivot j: the owners of column j publish it and
-// replace it by the unit vector e_j; the owners of row j scale it by
-// 1 / a_jj and publish it (a_jj becomes the reciprocal); then every thread
-// takes a_rc -= a_rj a_jc (with a_jj's row left alone) on its 64 entries
-// without branches.  Shared rows and columns alternate between two buffers
-// by the parity of j: two barriers a pivot.  With bad not null, a pivot
-// whose magnitude is at most tol sets *bad to row0 + j (the lowest such j
-// wins) and the inversion goes on.
+// pivoting, in one CTA of kGjThreads threads.  Warp w holds rows 4w .. 4w+3,
+// lane l columns 4l .. 4l+3 of them: 16 values in registers.  Per pivot j
+// the warp holding row j takes a_jj from the lane holding column j, replaces
+// it by 1, divides the row by the pivot and publishes it in shared memory;
+// after one barrier every other row i takes a_ic -= a_ij r_c with a_ij
+// replaced by 0 first (a_ij read from the lane that holds column j), and
+// row j becomes the published row.  The published rows alternate between
+// two buffers by the parity of j, so one barrier a pivot suffices.  With bad
+// not null, a pivot whose magnitude is at most tol sets *bad to row0 + j
+// (the lowest such j wins) and the inversion goes on.
 __device__ __forceinline__ void gj_invert_tile(const float *__restrict__ T, int ldt, float *__restrict__ P,
                                                float tol, int *bad, int row0)
 {
-    __shared__ __align__(16) float col[2][kPB], row[2][kPB];
-    const int tr = threadIdx.x >> 4, tc = threadIdx.x & 15;
-    float a[8][8];
+    __shared__ __align__(16) float prow[2][kPB];
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    float a[4][4];  // a[r][c] = A(4 w + r, 4 l + c)
 #pragma unroll
-    for (int c = 0; c < 8; c++) {
-        const float *src = T + (size_t)(8 * tc + c) * ldt + 8 * tr;
-        const float4 lo = *(const float4 *)src, hi = *(const float4 *)(src + 4);
-        a[0][c] = lo.x; a[1][c] = lo.y; a[2][c] = lo.z; a[3][c] = lo.w;
-        a[4][c] = hi.x; a[5][c] = hi.y; a[6][c] = hi.z; a[7][c] = hi.w;
+    for (int c = 0; c < 4; c++) {
+        const float4 v = *(const float4 *)(T + (size_t)(4 * l + c) * ldt + 4 * w);
+        a[0][c] = v.x;
+        a[1][c] = v.y;
+        a[2][c] = v.z;
+        a[3][c] = v.w;
     }
     for (int j = 0; j < kPB; j++) {
-        const int p = j & 1, jb = j >> 3, jo = j & 7;
-        if (tc == jb) {
+        const int jw = j >> 2, js = j & 3;  // warp and row slot of row j; lane jw, slot js hold column j
+        float *pr = prow[j & 1];
+        if (w == jw) {
+            float rv[4];
 #pragma unroll
-            for (int c = 0; c < 8; c++) {
-                if (c != jo) continue;
+            for (int c = 0; c < 4; c++) rv[c] = js == 0 ? a[0][c] : js == 1 ? a[1][c] : js == 2 ? a[2][c] : a[3][c];
+            const float pv = __shfl_sync(0xffffffffu, gj_sel4(rv, js), jw);
+            if (bad && l == 0 && !(fabsf(pv) > tol)) atomicMin(bad, row0 + j);
+            const float inv = __frcp_rn(pv);
 #pragma unroll
-                for (int i = 0; i < 8; i++) {
-                    col[p][8 * tr + i] = a[i][c];
-                    a[i][c] = (8 * tr + i == j) ? 1.0f : 0.0f;
-                }
-            }
+            for (int c = 0; c < 4; c++) rv[c] = (4 * l + c == j ? 1.0f : rv[c]) * inv;
+            *(float4 *)&pr[4 * l] = make_float4(rv[0], rv[1], rv[2], rv[3]);
         }
         __syncthreads();
-        if (tr == jb) {
-            const float pv = col[p][j];
-            if (bad && tc == 0 && !(fabsf(pv) > tol)) atomicMin(bad, row0 + j);
-            const float piv = __frcp_rn(pv);
+        const float4 q = *(const float4 *)&pr[4 * l];
+        const float qv[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
-            for (int i = 0; i < 8; i++) {
-                if (i != jo) continue;
+        for (int r = 0; r < 4; r++) {
+            const float f = __shfl_sync(0xffffffffu, gj_sel4(a[r], js), jw);
+            if (4 * w + r == j) {
 #pragma unroll
-                for (int c = 0; c < 8; c++) {
-                    a[i][c] *= piv;
-                    row[p][8 * tc + c] = a[i][c];
-                }
+                for (int c = 0; c < 4; c++) a[r][c] = qv[c];
+            } else {
+#pragma unroll
+                for (int c = 0; c < 4; c++) a[r][c] = fmaf(-f, qv[c], 4 * l + c == j ? 0.0f : a[r][c]);
             }
-        }
-        __syncthreads();
-        const float4 f0 = *(const float4 *)&col[p][8 * tr], f1 = *(const float4 *)&col[p][8 * tr + 4];
-        const float4 r0 = *(const float4 *)&row[p][8 * tc], r1 = *(const float4 *)&row[p][8 * tc + 4];
-        float f[8] = {f0.x, f0.y, f0.z, f0.w, f1.x, f1.y, f1.z, f1.w};
-        const float rv[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
-#pragma unroll
-        for (int i = 0; i < 8; i++) {
-            if (8 * tr + i == j) f[i] = 0.0f;
-#pragma unroll
-            for (int c = 0; c < 8; c++) a[i][c] = fmaf(-f[i], rv[c], a[i][c]);
         }
     }
 #pragma unroll
-    for (int i = 0; i < 8; i++) {
-        float *o = P + (size_t)(8 * tr + i) * kPB + 8 * tc;
-        *(float4 *)o = make_float4(a[i][0], a[i][1], a[i][2], a[i][3]);
-        *(float4 *)(o + 4) = make_float4(a[i][4], a[i][5], a[i][6], a[i][7]);
-    }
+    for (int r = 0; r < 4; r++)
+        *(float4 *)(P + (size_t)(4 * w + r) * kPB + 4 * l) = make_float4(a[r][0], a[r][1], a[r][2], a[r][3]);
 }
 
 }  // namespace dsc

@@ -56,7 +56,7 @@ __global__ void k_lu_load(const double *__restrict__ A, size_t lda, int n, float
 }
 
 // P_k = the inverse of the diagonal tile of step k.
-__global__ void __launch_bounds__(256) k_lu_pivot(const float *__restrict__ W, int np, int k, float *__restrict__ P,
+__global__ void __launch_bounds__(kGjThreads) k_lu_pivot(const float *__restrict__ W, int np, int k, float *__restrict__ P,
                                                    int *bad)
 {
     grid_dep_wait();  // a programmatic dependent of the previous step's update
@@ -275,7 +275,7 @@ int lu_solve_mixed(int n, const double *dA, size_t lda, double *dx, double tol, 
     const size_t rsmem = sizeof(float) * (2 * kPB * 129 + kPB * 128);
     DSC_TRY(raise_smem_limit((const void *)k_lu_row, (int)rsmem));
     for (int k = 0; k < nb; k++) {
-        DSC_TRY(launch_dependent(k_lu_pivot, dim3(1), dim3(256), 0, st, (const float *)W.p, np, k, P.p, bad.p));
+        DSC_TRY(launch_dependent(k_lu_pivot, dim3(1), dim3(kGjThreads), 0, st, (const float *)W.p, np, k, P.p, bad.p));
         if (k + 1 == nb) break;
         const int rest = nb - k - 1, k1 = (k + 1) * kPB, m = np - k1;
         DSC_TRY(launch_dependent(k_lu_row, dim3(rest, 2), dim3(256), rsmem, st, W.p, np, k, (const float *)P.p,

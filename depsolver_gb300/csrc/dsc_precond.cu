@@ -137,9 +137,9 @@ __global__ void k_pre_init(const double *__restrict__ K, size_t ld, const double
 }
 
 // tP = inverse of the 128 x 128 diagonal block k of each matrix, row-major
-// (Gauss-Jordan without pivoting, one CTA of 256 threads per matrix; see
+// (Gauss-Jordan without pivoting, one CTA of kGjThreads threads per matrix; see
 // gj_invert_tile).
-__global__ void __launch_bounds__(256) k_gj_pivot(GJArgs g, int nb, int k)
+__global__ void __launch_bounds__(kGjThreads) k_gj_pivot(GJArgs g, int nb, int k)
 {
     grid_dep_wait();  // a programmatic dependent of the previous step's update
     const int b = blockIdx.x;
@@ -326,7 +326,7 @@ int precond_build(Session &s)
         for (int t = 0; t < nseq; t++) {
             cudaStream_t ss = t ? s.side : st;
             for (int k = 0; k < nbk_sub[t]; k++) {
-                DSC_TRY(launch_dependent(k_gj_pivot, dim3(nsub[t]), dim3(256), 0, ss, gsub[t], nsub[t], k));
+                DSC_TRY(launch_dependent(k_gj_pivot, dim3(nsub[t]), dim3(kGjThreads), 0, ss, gsub[t], nsub[t], k));
                 DSC_TRY(launch_dependent(k_gj_row, dim3(nbk_sub[t], 2, nsub[t]), dim3(256), rsmem, ss, gsub[t],
                                          nsub[t], k));
                 for (int q : which[t])

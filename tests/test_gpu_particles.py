@@ -12,6 +12,7 @@ import dataclasses
 import numpy as np
 import pytest
 
+from conftest import relerr
 from depsolver_gb300 import api, scenes
 
 pytestmark = pytest.mark.gpu
