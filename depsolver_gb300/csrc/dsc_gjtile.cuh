@@ -63,10 +63,37 @@ __device__ __forceinline__ void pre_row_pair(const float *v, __half *h, __half *
 // Threads of the CTA that inverts one tile (gj_invert_tile).
 constexpr int kGjThreads = 1024;
 
-// v[s] for a slot s known only at run time (selects, no local memory).
-__device__ __forceinline__ float gj_sel4(const float (&v)[4], int s)
+// One pivot of gj_invert_tile: pivot j = 4 m + S (S a compile-time slot:
+// row S of warp m holds row j, slot S of lane m holds column j).
+template <int S>
+__device__ __forceinline__ void gj_pivot_step(float (&a)[4][4], int m, float *pr, float tol, int *bad, int row0)
 {
-    return s == 0 ? v[0] : s == 1 ? v[1] : s == 2 ? v[2] : v[3];
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (w == m) {
+        // row j: a_jj from lane m, replaced by 1, the row divided by it
+        const float pv = __shfl_sync(0xffffffffu, a[S][S], m);
+        if (bad && l == 0 && !(fabsf(pv) > tol)) atomicMin(bad, row0 + 4 * m + S);
+        const float inv = __frcp_rn(pv);
+        float rv[4];
+#pragma unroll
+        for (int c = 0; c < 4; c++) rv[c] = (c == S && l == m ? 1.0f : a[S][c]) * inv;
+        *(float4 *)&pr[4 * l] = make_float4(rv[0], rv[1], rv[2], rv[3]);
+    }
+    __syncthreads();
+    const float4 q = *(const float4 *)&pr[4 * l];
+    const float qv[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        const float f = __shfl_sync(0xffffffffu, a[r][S], m);  // a_ij of this row
+        if (r == S && w == m) {
+#pragma unroll
+            for (int c = 0; c < 4; c++) a[r][c] = qv[c];
+        } else {
+            if (l == m) a[r][S] = 0.0f;
+#pragma unroll
+            for (int c = 0; c < 4; c++) a[r][c] = fmaf(-f, qv[c], a[r][c]);
+        }
+    }
 }
 
 // P (row-major, 128 x 128) = inverse of the tile at T (column-major: element
@@ -76,11 +103,13 @@ __device__ __forceinline__ float gj_sel4(const float (&v)[4], int s)
 // the warp holding row j takes a_jj from the lane holding column j, replaces
 // it by 1, divides the row by the pivot and publishes it in shared memory;
 // after one barrier every other row i takes a_ic -= a_ij r_c with a_ij
-// replaced by 0 first (a_ij read from the lane that holds column j), and
-// row j becomes the published row.  The published rows alternate between
-// two buffers by the parity of j, so one barrier a pivot suffices.  With bad
-// not null, a pivot whose magnitude is at most tol sets *bad to row0 + j
-// (the lowest such j wins) and the inversion goes on.
+// replaced by 0 first (a_ij read by shuffle from the lane that holds column
+// j), and row j becomes the published row.  The pivot loop is unrolled by
+// four so that the row and column slot of every pivot is a compile-time
+// index.  The published rows alternate between two buffers by the parity of
+// j, so one barrier a pivot suffices.  With bad not null, a pivot whose
+// magnitude is at most tol sets *bad to row0 + j (the lowest such j wins)
+// and the inversion goes on.
 __device__ __forceinline__ void gj_invert_tile(const float *__restrict__ T, int ldt, float *__restrict__ P,
                                                float tol, int *bad, int row0)
 {
@@ -95,34 +124,11 @@ __device__ __forceinline__ void gj_invert_tile(const float *__restrict__ T, int 
         a[2][c] = v.z;
         a[3][c] = v.w;
     }
-    for (int j = 0; j < kPB; j++) {
-        const int jw = j >> 2, js = j & 3;  // warp and row slot of row j; lane jw, slot js hold column j
-        float *pr = prow[j & 1];
-        if (w == jw) {
-            float rv[4];
-#pragma unroll
-            for (int c = 0; c < 4; c++) rv[c] = js == 0 ? a[0][c] : js == 1 ? a[1][c] : js == 2 ? a[2][c] : a[3][c];
-            const float pv = __shfl_sync(0xffffffffu, gj_sel4(rv, js), jw);
-            if (bad && l == 0 && !(fabsf(pv) > tol)) atomicMin(bad, row0 + j);
-            const float inv = __frcp_rn(pv);
-#pragma unroll
-            for (int c = 0; c < 4; c++) rv[c] = (4 * l + c == j ? 1.0f : rv[c]) * inv;
-            *(float4 *)&pr[4 * l] = make_float4(rv[0], rv[1], rv[2], rv[3]);
-        }
-        __syncthreads();
-        const float4 q = *(const float4 *)&pr[4 * l];
-        const float qv[4] = {q.x, q.y, q.z, q.w};
-#pragma unroll
-        for (int r = 0; r < 4; r++) {
-            const float f = __shfl_sync(0xffffffffu, gj_sel4(a[r], js), jw);
-            if (4 * w + r == j) {
-#pragma unroll
-                for (int c = 0; c < 4; c++) a[r][c] = qv[c];
-            } else {
-#pragma unroll
-                for (int c = 0; c < 4; c++) a[r][c] = fmaf(-f, qv[c], 4 * l + c == j ? 0.0f : a[r][c]);
-            }
-        }
+    for (int m = 0; m < kPB / 4; m++) {
+        gj_pivot_step<0>(a, m, prow[0], tol, bad, row0);
+        gj_pivot_step<1>(a, m, prow[1], tol, bad, row0);
+        gj_pivot_step<2>(a, m, prow[0], tol, bad, row0);
+        gj_pivot_step<3>(a, m, prow[1], tol, bad, row0);
     }
 #pragma unroll
     for (int r = 0; r < 4; r++)

@@ -953,6 +953,11 @@ int Session::make_k16()
 {
     if (k16_ready && k64_ready) return kOk;
     DSC_TRY(assemble64(false));
+    // the conductor-block inverses need only K64: they run on side2 (and
+    // side) beside the conversion below on st, joined at the end
+    const bool pre_par = pre_on && pre && pre->nb > 0 && !pre->ready;
+    SideJoin pj;
+    if (pre_par) DSC_TRY(pj.fork(st, side2));
     {
         // K's row digits for the tensor-core first residual take 16 bytes
         // per entry: kept when they fill at most a quarter of the device
@@ -977,7 +982,16 @@ int Session::make_k16()
         // bytes: K read (8), the fp16 pair and the digits written (2 each)
         timer.add_work(kTConvertK, (8.0 + 2.0 * (2 + (digits ? kKDigits : 0))) * N * N);
     }
-    if (pre_on) DSC_TRY(precond_build(*this));
+    if (pre_par) {
+        {
+            AllocStreamScope ps(side2);  // its buffers ordered on the stream that first uses them
+            DSC_TRY(precond_build(*this, side2, side));
+        }
+        DSC_TRY(pj.done(side2));
+        DSC_TRY(pj.join());
+    } else if (pre_on) {
+        DSC_TRY(precond_build(*this));
+    }
     k16_ready = true;
     return kOk;
 }

@@ -247,11 +247,12 @@ __global__ void k_pre_transpose(const float *__restrict__ X, int ldx, float *__r
     for (int y = threadIdx.y; y < 32; y += blockDim.y) Xt[(size_t)(r0 + y) * ldx + c0 + threadIdx.x] = t[threadIdx.x][y];
 }
 
-int precond_build(Session &s)
+int precond_build(Session &s, cudaStream_t main, cudaStream_t aux)
 {
     Precond &pc = *s.pre;
     if (!pc.nb || pc.ready) return kOk;
-    cudaStream_t st = s.st;
+    cudaStream_t st = main ? main : s.st;
+    cudaStream_t side = main ? aux : s.side;
     TimerScope ts(&s.timer, kTPreBuild, st);
     const size_t xtot = pc.xoff.back() + (size_t)pc.ldx.back() * pc.ldx.back();
     const size_t ttot = pc.toff.back() + (size_t)kPB * pc.ldx.back();
@@ -302,7 +303,7 @@ int precond_build(Session &s)
         // blocks: even blocks on st, odd ones on the side stream, so that one
         // sequence's pivot inversion (one CTA) runs beside the other's
         // tensor-core update
-        const int nseq = (nb >= 2 && s.side) ? 2 : 1;
+        const int nseq = (nb >= 2 && side) ? 2 : 1;
         GJArgs gsub[2] = {};
         int nsub[2] = {0, 0}, nbk_sub[2] = {0, 0};
         std::vector<int> which[2];
@@ -322,9 +323,9 @@ int precond_build(Session &s)
             which[t].push_back(q);
         }
         SideJoin sj;
-        if (nseq == 2) DSC_TRY(sj.fork(st, s.side));
+        if (nseq == 2) DSC_TRY(sj.fork(st, side));
         for (int t = 0; t < nseq; t++) {
-            cudaStream_t ss = t ? s.side : st;
+            cudaStream_t ss = t ? side : st;
             for (int k = 0; k < nbk_sub[t]; k++) {
                 DSC_TRY(launch_dependent(k_gj_pivot, dim3(nsub[t]), dim3(kGjThreads), 0, ss, gsub[t], nsub[t], k));
                 DSC_TRY(launch_dependent(k_gj_row, dim3(nbk_sub[t], 2, nsub[t]), dim3(256), rsmem, ss, gsub[t],
@@ -334,7 +335,7 @@ int precond_build(Session &s)
             }
         }
         if (nseq == 2) {
-            DSC_TRY(sj.done(s.side));
+            DSC_TRY(sj.done(side));
             DSC_TRY(sj.join());
         }
     }

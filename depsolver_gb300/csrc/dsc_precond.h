@@ -77,8 +77,9 @@ struct PrecondShare {
 // Blocks from the mesh and the conductor rows (once per session; no blocks
 // when the scene has no conductor rows).
 int precond_plan(Session &s);
-// The inverses for the current K64 (after each assembly).
-int precond_build(Session &s);
+// The inverses for the current K64 (after each assembly), on main and aux
+// (default: the session's stream and side stream); waits for them.
+int precond_build(Session &s, cudaStream_t main = nullptr, cudaStream_t aux = nullptr);
 // Copies a built session's inverses into sh (waits for the copies).
 int precond_export(Session &s, PrecondShare &sh);
 // Takes sh's inverses for s when s has the same blocks (same rows in the

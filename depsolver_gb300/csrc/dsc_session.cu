@@ -94,6 +94,7 @@ int Session::create(int nen_, unsigned N_, unsigned E_, const double *nodes, con
     nIf = nIf_;
     DSC_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     DSC_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+    DSC_CUDA(cudaStreamCreateWithFlags(&side2, cudaStreamNonBlocking));
     AllocStreamScope as(st);
     std::vector<int> e0((size_t)E * nen);
     for (size_t t = 0; t < e0.size(); t++) e0[t] = (int)elems[t] - 1;

@@ -38,6 +38,10 @@ struct Session {
     // Gauss-Jordan sequences), joined back by events
     cudaStream_t side = nullptr;
     StreamGuard side_guard{&side};
+    // a third stream: the conductor-block inverses run on it (and on side)
+    // while K's conversion runs on st
+    cudaStream_t side2 = nullptr;
+    StreamGuard side2_guard{&side2};
     HostPlan plan;
     DeviceMesh dev;
     ForcePlan force;
