@@ -611,7 +611,9 @@ def run_ours(args, rank, world):
     L = _native.lib()
     # the 12k-node scene of the metric; --scene mid (level-3 sphere between
     # 25 x 25-cell plates, N = 7764) only for profiler captures of one step
-    sc = scenes.cfg1() if args.scene == "cfg1" else scenes.sphere_between_plates(3, 25, name="mid")
+    scene_of = {"cfg1": scenes.cfg1, "mid": lambda: scenes.sphere_between_plates(3, 25, name="mid"),
+                "cfg0": lambda: scenes.cfg0(center=(0.0, 0.0, 1.0)), "capacitor25": lambda: scenes.capacitor(25)}
+    sc = scene_of[args.scene]()
     N, E = sc.N, sc.E
     s = api.Session(sc)
     s.set_mixed_assembly(api.ASM_FP32 if args.mixed_assembly == "fp32" else api.ASM_DF32)
@@ -619,14 +621,32 @@ def run_ours(args, rank, world):
     if args.only_step:
         # one warm-up and one timed step only (for profiler launch lists);
         # --step-mode fp64: the plain FP64 path's step (FP64 assembly, the
-        # reference's GMRES at 1 MHz, force) instead
-        for _ in range(2):
-            if args.step_mode == "fp64":
-                s.assemble(api.MODE_FP64)
-                s.solve([1e6], mode=api.MODE_FP64, tol=TOL)
-            else:
-                s.assemble(api.MODE_MIXED)
-                s.solve(FREQS, mode=api.MODE_MIXED, tol=TOL)
+        # reference's GMRES at 1 MHz, force) instead; gauss: the direct
+        # solve of the scene's full 2N form (block LU + refinement);
+        # positions: 12 positions of the position sweep (levels 2/3/4)
+        s.close()
+        if args.step_mode == "gauss":
+            Af, Bf = api.electric_form(sc, full=True)
+            for _ in range(2):
+                api.gauss_bksb(Af, Bf, mode=api.GAUSS_MIXED)
+        elif args.step_mode == "positions":
+            ps = api.PositionSweep(scenes.plates_only(10))
+            lev, cen = scenes.cfg3_positions(12)
+            tid = {lv: ps.add_particle(*scenes.icosphere(lv, 1.0)) for lv in (2, 3, 4)}
+            tm = np.array([tid[int(v)] for v in lev], dtype=np.uint32)
+            for _ in range(2):
+                ps.solve(tm, cen, FREQS, tol=TOL)
+            ps.close()
+        else:
+            s = api.Session(sc)
+            s.set_mixed_assembly(api.ASM_FP32 if args.mixed_assembly == "fp32" else api.ASM_DF32)
+            for _ in range(2):
+                if args.step_mode == "fp64":
+                    s.assemble(api.MODE_FP64)
+                    s.solve([1e6], mode=api.MODE_FP64, tol=TOL)
+                else:
+                    s.assemble(api.MODE_MIXED)
+                    s.solve(FREQS, mode=api.MODE_MIXED, tol=TOL)
         torch.cuda.synchronize()
         print(json.dumps({"only_step": True, "launches": int(L.dsc_kernel_launches())}))
         return
@@ -825,12 +845,13 @@ def main():
     ap.add_argument("--no-positions", action="store_true", help="skip the position sweep (cfg3)")
     ap.add_argument("--no-extras", action="store_true", help="skip the direct-solve and trap sections")
     ap.add_argument("--pos-workers", type=int, default=4, help="host workers (streams) of the position sweep")
-    ap.add_argument("--scene", choices=["cfg1", "mid"], default="cfg1",
-                    help="mid: a smaller scene for ncu captures (with --only-step)")
+    ap.add_argument("--scene", choices=["cfg1", "mid", "cfg0", "capacitor25"], default="cfg1",
+                    help="mid, cfg0, capacitor25: other scenes for ncu captures (with --only-step)")
     ap.add_argument("--mixed-assembly", choices=["fp32", "df32"], default="fp32",
                     help="arithmetic of the mixed mode's regular pairs (FP32 far field, or double-FP32)")
-    ap.add_argument("--step-mode", choices=["mixed", "fp64"], default="mixed",
-                    help="with --only-step: profile the mixed sweep or the plain FP64 path")
+    ap.add_argument("--step-mode", choices=["mixed", "fp64", "gauss", "positions"], default="mixed",
+                    help="with --only-step: profile the mixed sweep, the plain FP64 path, the direct "
+                         "solve of the scene's full form, or a 12-position sample of the position sweep")
     ap.add_argument("--only-step", action="store_true",
                     help="run one warm-up and one step and nothing else (profiling)")
     args = ap.parse_args()
