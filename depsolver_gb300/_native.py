@@ -97,6 +97,16 @@ def lib() -> C.CDLL:
                                           C.c_void_p]
         L.dsc_force_crossover.restype = C.c_double
         L.dsc_force_crossover.argtypes = [C.c_uint, _dp, _dp, C.c_void_p]
+        L.dsc_bem_read.restype = C.c_int
+        L.dsc_bem_read.argtypes = [C.c_char_p, C.POINTER(C.c_void_p)]
+        L.dsc_bem_free.restype = None
+        L.dsc_bem_free.argtypes = [C.c_void_p]
+        L.dsc_bem_info.restype = C.c_int
+        L.dsc_bem_info.argtypes = [C.c_void_p] + [C.c_void_p] * 16
+        L.dsc_bem_arrays.restype = C.c_int
+        L.dsc_bem_arrays.argtypes = [C.c_void_p] + [C.c_void_p] * 8
+        L.dsc_node_normals.restype = C.c_int
+        L.dsc_node_normals.argtypes = [C.c_int, C.c_uint, C.c_uint, _dp, _up, _dp]
         L.dsc_session_stream.restype = C.c_void_p
         L.dsc_session_stream.argtypes = [C.c_void_p]
         L.dsc_kernel_launches.restype = C.c_ulonglong

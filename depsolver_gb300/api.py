@@ -409,3 +409,41 @@ class PositionSweep:
                 sigmas.append(sig[o:o + 2 * n * F].reshape(F, 2 * n))
                 o += 2 * n * F
         return {"forces": forces, "iters": its, "status": st, "crossover_hz": xo, "sigma": sigmas}
+
+
+def read_bem(directory: str) -> dict:
+    """The reference's input deck through the library's reader
+    (dsc_bem_read): a dict of the scene arrays (as Scene holds them) and
+    the deck's analysis settings."""
+    L = _native.lib()
+    h = C.c_void_p()
+    _native.check(L.dsc_bem_read(directory.encode(), C.byref(h)))
+    try:
+        nen, an, gm, rp = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        N, E, nm, ni, pc, nin, nint, nfp, pn = (C.c_uint() for _ in range(9))
+        fr = C.c_double()
+        dr = np.zeros(3)
+        ax = np.zeros(3)
+        refs = [nen, N, E, nm, ni, fr, an, gm, pc, nin, nint, nfp, rp, pn]
+        _native.check(L.dsc_bem_info(h, *[C.addressof(r) for r in refs], dr.ctypes.data, ax.ctypes.data))
+        out = {"nen": nen.value, "nodes": np.zeros((N.value, 3)),
+               "elems": np.zeros((E.value, nen.value), dtype=np.uint32),
+               "bctype": np.zeros(2 * N.value, dtype=np.uint32), "mbc": np.zeros((2 * N.value, 3)),
+               "mat": np.zeros((nm.value, 2)), "ifaces": np.zeros((ni.value, 2), dtype=np.uint32),
+               "internal": np.zeros((nint.value, 3)), "force_points": np.zeros((nfp.value, 3)),
+               "freq": fr.value, "analysis": an.value, "gmres": bool(gm.value), "precond": pc.value,
+               "ninit": nin.value, "reposition": bool(rp.value), "pnodes": pn.value, "dr": dr,
+               "axis": ax}
+        _native.check(L.dsc_bem_arrays(h, *[out[k].ctypes.data for k in
+                                            ("nodes", "elems", "bctype", "mbc", "mat", "ifaces",
+                                             "internal", "force_points")]))
+        return out
+    finally:
+        L.dsc_bem_free(h)
+
+
+def node_normals(sc: Scene) -> np.ndarray:
+    """Averaged unit normal at every node (N x 3): dsc_node_normals."""
+    out = np.zeros((sc.N, 3))
+    _native.check(_native.lib().dsc_node_normals(sc.nen, sc.N, sc.E, _f(sc.nodes), _u(sc.elems), out))
+    return out

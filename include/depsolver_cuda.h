@@ -436,6 +436,40 @@ double dsc_force_crossover(unsigned nfreq, const double *freqs, const double *fo
 int dsc_set_autotune(int on);
 int dsc_autotune_table(int *rows, int n);
 
+/* ---------------------------------------------------------- input decks
+ * The reference's input deck as a library call (host only): input.bem in
+ * directory dir and the node, element, boundary-condition, internal-point
+ * and force-point files it names, parsed as src/depSolver.c:98-252 and
+ * src/depSolver-shift.c:120-140,205-217 do ("//" comments stripped as
+ * comFilter does, src/preProcess.c:48-81; "C<k>" boundary types read as
+ * k + 5).  A REPOSITION section (depSolver-sft decks) shifts nodes pNodes..
+ * (0-based) by dr, as that driver does.  Element types other than tria3 and
+ * tria6 are rejected, as the reference's driver rejects them
+ * (src/depSolver.c:180-183).
+ *
+ * dsc_bem_info returns the sizes and scalars (any pointer may be NULL;
+ * analysis is the ANALYSIS type, gmres 1 for the GMRES solver with preCond
+ * and nInit, axis the sphere radius in axis[0] or the ellipsoid's
+ * semi-axes); dsc_bem_arrays copies the arrays (any may be NULL): nodes
+ * N x 3, elems E x nen (1-based), bctype 2N, mbc 2N x 3, mat nMat x 2,
+ * ifaces nIf x 2, internal points and force points nPoints x 3. */
+typedef struct dsc_bem dsc_bem;
+int dsc_bem_read(const char *dir, dsc_bem **out);
+void dsc_bem_free(dsc_bem *b);
+int dsc_bem_info(const dsc_bem *b, int *nen, unsigned *N, unsigned *E, unsigned *nMat, unsigned *nIf,
+                 double *freq, int *analysis, int *gmres, unsigned *preCond, unsigned *nInit,
+                 unsigned *nInternal, unsigned *nForcePoints, int *reposition, unsigned *pNodes,
+                 double *dr, double *axis);
+int dsc_bem_arrays(const dsc_bem *b, double *nodes, unsigned *elems, unsigned *bctype, double *mbc,
+                   double *mat, unsigned *ifaces, double *internal, double *force_points);
+
+/* Averaged unit normal at every node (normals: N x 3), replacing the
+ * reference's getNormal_tria3/6 (src/normals.c:120-319), which scans every
+ * element per node: the average over the elements containing the node of
+ * their local normals at it, normalised (host threads, O(N + E)). */
+int dsc_node_normals(int nen, unsigned N, unsigned E, const double *nodes, const unsigned *elems,
+                     double *normals);
+
 /* One-call sweep from host arrays (session created and destroyed inside). */
 int dsc_sweep(int nen, unsigned N, unsigned E, const double *nodes, const unsigned *elems,
               const unsigned *bctype, const double *mbc, unsigned nIf, const unsigned *ifaces,
