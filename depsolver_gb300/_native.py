@@ -55,6 +55,14 @@ def lib() -> C.CDLL:
             f = getattr(L, nm)
             f.restype = C.c_int
             f.argtypes = [C.c_int, C.c_uint, C.c_uint, _dp, _up, _dp, C.c_uint, _dp, _dp]
+        L.dsc_force_multipole.restype = C.c_int
+        L.dsc_force_multipole.argtypes = [C.c_int, C.c_uint, C.c_uint, _dp, _up, _dp, C.c_uint, _dp, C.c_uint,
+                                          C.c_double, _dp, C.c_double, _dp]
+        L.dsc_force_ellipsoid.restype = C.c_int
+        L.dsc_force_ellipsoid.argtypes = [C.c_int, C.c_uint, C.c_uint, _dp, _up, _dp, C.c_uint, _dp, C.c_uint,
+                                          C.c_void_p, _dp, C.c_double, _dp]
+        L.dsc_depolarization.restype = C.c_int
+        L.dsc_depolarization.argtypes = [_dp, _dp]
         L.dsc_force_mst.restype = C.c_int
         L.dsc_force_mst.argtypes = [C.c_int, C.c_uint, C.c_uint, _dp, _up, _up, _dp, C.c_double,
                                     C.c_void_p, C.c_void_p, _dp, _dp]

@@ -145,6 +145,35 @@ def force_mst(sc: Scene, vB: np.ndarray, eps: float | None = None):
     return Fce, Xce, Fcm, Xcm
 
 
+def force_multipole(sc: Scene, vB: np.ndarray, pts, order: int, R: float) -> np.ndarray:
+    """forceMultipole_* at each point (npts x 3): sphere of radius R,
+    materials 1 (medium) and 2 (particle) of the scene, its frequency."""
+    pts = _f(np.atleast_2d(pts))
+    F = np.zeros((pts.shape[0], 3))
+    _native.check(_native.lib().dsc_force_multipole(sc.nen, sc.N, sc.E, _f(sc.nodes), _u(sc.elems), _f(vB),
+                                                    pts.shape[0], pts, order, float(R), _f(sc.mat[:2]).ravel(),
+                                                    sc.freq, F))
+    return F
+
+
+def force_ellipsoid(sc: Scene, vB: np.ndarray, pts, analysis: int, axis) -> np.ndarray:
+    """forceEllipsoid_* (analysis 10 or 11) at each point (npts x 3)."""
+    pts = _f(np.atleast_2d(pts))
+    F = np.zeros((pts.shape[0], 3))
+    ax = _f(axis)
+    _native.check(_native.lib().dsc_force_ellipsoid(sc.nen, sc.N, sc.E, _f(sc.nodes), _u(sc.elems), _f(vB),
+                                                    pts.shape[0], pts, analysis, ax.ctypes.data,
+                                                    _f(sc.mat[:2]).ravel(), sc.freq, F))
+    return F
+
+
+def depolarization(axis) -> np.ndarray:
+    """Depolarisation factors of an ellipsoid of semi-axes `axis`."""
+    Ld = np.zeros(3)
+    _native.check(_native.lib().dsc_depolarization(_f(axis), Ld))
+    return Ld
+
+
 # ------------------------------------------------------------------ sweeps
 
 MODE_FP64 = 1

@@ -9,6 +9,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <memory>
 #include <mutex>
 #include <thread>
@@ -45,6 +46,9 @@ struct Context {
     // (the reference's post-processing evaluates one point per call)
     PointSet pts;
     DevBuf<double> pout;
+    // multipole / ellipsoid force points: their coordinates and workspace
+    DevBuf<double> dpts;
+    DerivWork deriv;
     double *pinned = nullptr;
     size_t pinned_bytes = 0;
     // direct solve: the tensor-core block LU with FP64 refinement (default)
@@ -682,6 +686,230 @@ extern "C" int potential_tria6(double *Xin, double **mNodes, unsigned int **mEle
     return field_dropin(6, 0, Xin, mNodes, mElems, vB, mPot);
 }
 
+// ---------------------------------------------------------- multipole forces
+// The multipole and ellipsoid DEP forces (src/force.c:65-322,572-825) from
+// the field and its derivatives at the evaluation point.  E_a is the
+// derivative tensor of point_derivatives (E_(1,0,0) = Re Ex, E_(2,0,0) =
+// dEx/dx, ...).  Sphere of radius R, order n <= 3 of the expansion:
+//   F_i = sum_n C_n sum_{|a| = n} (n! / a!) E_a E_{a + e_i},
+//   C_1 = 2 pi eps_m R^3 CM_1,  C_n = C_{n-1} R^2 / ((n - 1)(2n - 1)) with
+//   CM_n = Re[(e_p - e_m) / (n e_p + (n + 1) e_m)] in place of CM_{n-1},
+// e = eps + sigma / (i omega) (the reference's EpsDif / EpsPlus / SigDif /
+// SigPlus form).  The reference computes the order 4 and 5 coefficients but
+// adds only the terms up to n = 3 (src/force.c:814-826): orders 4 and 5 give
+// the order-3 force here too.  The tria6 form multiplies by 0.333...33 and
+// 0.1 where the tria3 form divides by 3 and 10 (src/force.c:636-642,773-779);
+// both are kept.
+static double deriv_E(const double *E, int p, int q, int r) { return E[deriv_index(p, q, r)]; }
+
+static double cm_factor(const double *mat, double freq, int n)
+{
+    const double w = freq * kPi2 * kEps0;
+    const double ed = w * (mat[3] - mat[1]), sd = mat[2] - mat[0];
+    const double ep = w * (n * mat[3] + (n + 1) * mat[1]), sp = n * mat[2] + (n + 1) * mat[0];
+    return (ed * ep + sd * sp) / (ep * ep + sp * sp);
+}
+
+static void multipole_from_derivs(int nen, const double *E, unsigned nOrder, double R, const double *mat,
+                                  double freq, double *F)
+{
+    const double Eps = mat[1] * kEps0;
+    double C[4];
+    C[1] = kPi2 * Eps * R * R * R;
+    C[2] = nen == 6 ? C[1] * R * R * 0.333333333333333333 : C[1] * R * R / 3.0;
+    C[3] = nen == 6 ? C[2] * R * R * 0.1 : C[2] * R * R / 10.0;
+    const int top = (int)std::min(3u, std::max(1u, nOrder));
+    for (int n = 1; n <= top; n++) C[n] *= cm_factor(mat, freq, n);
+    F[0] = F[1] = F[2] = 0.0;
+    for (int n = 1; n <= top; n++) {
+        double f[3] = {0.0, 0.0, 0.0};
+        for (int p = n; p >= 0; p--)
+            for (int q = n - p; q >= 0; q--) {
+                const int r = n - p - q;
+                double fact = 1.0;
+                for (int k = 2; k <= n; k++) fact *= k;
+                for (int k = 2; k <= p; k++) fact /= k;
+                for (int k = 2; k <= q; k++) fact /= k;
+                for (int k = 2; k <= r; k++) fact /= k;
+                const double ea = deriv_E(E, p, q, r);
+                f[0] += fact * ea * deriv_E(E, p + 1, q, r);
+                f[1] += fact * ea * deriv_E(E, p, q + 1, r);
+                f[2] += fact * ea * deriv_E(E, p, q, r + 1);
+            }
+        for (int i = 0; i < 3; i++) F[i] += C[n] * f[i];
+    }
+}
+
+// 64-point Gauss-Legendre rule on [-1, 1], ascending (Newton on P_64 from
+// the usual cosine guesses), for the depolarisation integrals.
+static const double (*gauss_legendre64())[2]
+{
+    static double rule[64][2];
+    static std::once_flag once;
+    std::call_once(once, [] {
+        const int n = 64;
+        for (int i = 0; i < n; i++) {
+            double x = cos(M_PI * (i + 0.75) / (n + 0.5)), dp = 1.0;
+            for (int it = 0; it < 100; it++) {
+                double p0 = 1.0, p1 = x;
+                for (int k = 2; k <= n; k++) {
+                    const double p2 = ((2.0 * k - 1.0) * x * p1 - (k - 1.0) * p0) / k;
+                    p0 = p1;
+                    p1 = p2;
+                }
+                dp = n * (x * p1 - p0) / (x * x - 1.0);
+                const double dx = p1 / dp;
+                x -= dx;
+                if (fabs(dx) < 1e-17) break;
+            }
+            rule[n - 1 - i][0] = x;  // ascending
+            rule[n - 1 - i][1] = 2.0 / ((1.0 - x * x) * dp * dp);
+        }
+    });
+    return rule;
+}
+
+// Depolarisation factors of an ellipsoid of semi-axes `axis`
+// (src/depolarization.c:44-115): L_k = (abc / 2) int_0^inf ds /
+// ((s + a_k^2) sqrt((s + a^2)(s + b^2)(s + c^2))), the range cut at
+// 100 a_k^2 and integrated with the 64-point rule.  Returns false when a
+// factor comes out negative (the reference's fatal error); *warn is set when
+// they do not add up to 1 within 0.05 (the reference's warning).
+static bool depolarization_factors(const double *axis, double *Ld, bool *warn)
+{
+    const double(*g)[2] = gauss_legendre64();
+    const double A = 0.5 * axis[0] * axis[1] * axis[2];
+    const double a2 = axis[0] * axis[0], b2 = axis[1] * axis[1], c2 = axis[2] * axis[2];
+    const double s2[3] = {a2, b2, c2};
+    for (int k = 0; k < 3; k++) {
+        const double X1 = 100 * s2[k], J = 0.5 * X1;
+        double acc = 0.0;
+        for (int i = 0; i < 64; i++) {
+            const double x = 0.5 * (1.0 + g[i][0]) * X1;  // the line from 0 to X1 at the rule's point
+            const double R = J * g[i][1] / sqrt((x + a2) * (x + b2) * (x + c2));
+            acc += R / (x + s2[k]);
+        }
+        Ld[k] = A * acc;
+    }
+    *warn = fabs(1.0 - Ld[0] - Ld[1] - Ld[2]) > 0.05;
+    return Ld[0] >= 0.0 && Ld[1] >= 0.0 && Ld[2] >= 0.0;
+}
+
+// The ellipsoid's dipole force (analysis 10: homogeneous; 11: single-shell
+// oblate, the particle's sigma and eps scaled by a c / (2 c + a) and divided
+// by each L_k), src/force.c:260-318.
+static void ellipsoid_from_derivs(const double *E, unsigned analysis, const double *axis, const double *Ld,
+                                  const double *mat, double freq, double *F)
+{
+    const double w = freq * kPi2 * kEps0, Eps = mat[1] * kEps0;
+    const double A = kPi2 * Eps * axis[0] * axis[1] * axis[2] / 3.0;
+    double K[3] = {0.0, 0.0, 0.0};
+    for (int d = 0; d < 3; d++) {
+        double ep = mat[3], sp = mat[2];
+        if (analysis == 11) {
+            const double Cs = axis[0] * axis[2] / (2.0 * axis[2] + axis[0]);
+            ep = mat[3] * Cs / Ld[d];
+            sp = mat[2] * Cs / Ld[d];
+        } else if (analysis != 10) {
+            break;
+        }
+        const double ed = w * (ep - mat[1]), sd = sp - mat[0];
+        const double epl = w * (mat[1] + (ep - mat[1]) * Ld[d]), spl = mat[0] + (sp - mat[0]) * Ld[d];
+        K[d] = (ed * epl + sd * spl) / (epl * epl + spl * spl);
+    }
+    const double Ex = deriv_E(E, 1, 0, 0), Ey = deriv_E(E, 0, 1, 0), Ez = deriv_E(E, 0, 0, 1);
+    F[0] = A * (K[0] * Ex * deriv_E(E, 2, 0, 0) + K[1] * Ey * deriv_E(E, 1, 1, 0) + K[2] * Ez * deriv_E(E, 1, 0, 1));
+    F[1] = A * (K[0] * Ex * deriv_E(E, 1, 1, 0) + K[1] * Ey * deriv_E(E, 0, 2, 0) + K[2] * Ez * deriv_E(E, 0, 1, 1));
+    F[2] = A * (K[0] * Ex * deriv_E(E, 1, 0, 1) + K[1] * Ey * deriv_E(E, 0, 1, 1) + K[2] * Ez * deriv_E(E, 0, 0, 2));
+}
+
+// E tensors at npts points on mesh m from the nodal solution vB.
+static int derivs_on(MeshEntry *m, const double *vB, unsigned npts, const double *pts, std::vector<double> &E)
+{
+    Context &c = ctx();
+    const double *dsig;
+    DSC_TRY(get_sigma(m->plan.N, vB, &dsig));
+    DSC_TRY(c.dpts.upload(pts, 3 * (size_t)npts, c.st));
+    E.assign((size_t)npts * kDerivCount, 0.0);
+    return point_derivatives(m->dev, dsig, (int)npts, c.dpts.p, c.deriv, E.data(), c.st);
+}
+
+static MeshEntry *mesh_of_rows(int nen, double **mNodes, unsigned **mElems)
+{
+    check_or_die(ensure_stream());
+    MeshEntry *m = cached_rows(nen, (int)nNodes, (int)nElems, mNodes, mElems);
+    if (m) return m;
+    FlatMesh f;
+    flatten(nen, (int)nNodes, (int)nElems, mNodes, mElems, f);
+    check_or_die(get_mesh(nen, (int)nNodes, (int)nElems, f.nodes.data(), f.elems0.data(), &m));
+    return m;
+}
+
+static int multipole_dropin(int nen, unsigned nOrder, double R, double *Xeval, double **mNodes, unsigned **mElems,
+                            double *vB, double **vMatParam, double *vProbParam, double *F)
+{
+    std::lock_guard<std::mutex> lk(ctx().mu);
+    MeshEntry *m = mesh_of_rows(nen, mNodes, mElems);
+    std::vector<double> E;
+    check_or_die(derivs_on(m, vB, 1, Xeval, E));
+    const double mat[4] = {vMatParam[0][0], vMatParam[0][1], vMatParam[1][0], vMatParam[1][1]};
+    multipole_from_derivs(nen, E.data(), nOrder, R, mat, vProbParam[0], F);
+    return 0;
+}
+
+static int ellipsoid_dropin(int nen, unsigned ANALYSIS, double *axis, double *Xeval, double **mNodes,
+                            unsigned **mElems, double *vB, double **vMatParam, double *vProbParam, double *F)
+{
+    std::lock_guard<std::mutex> lk(ctx().mu);
+    MeshEntry *m = mesh_of_rows(nen, mNodes, mElems);
+    std::vector<double> E;
+    check_or_die(derivs_on(m, vB, 1, Xeval, E));
+    double Ld[3];
+    bool warn = false;
+    if (!depolarization_factors(axis, Ld, &warn)) fatal("Error: depolarization() - factors must be positive!");
+    if (warn) printf("Warning: depolarization() - error is larger than 0.05");
+    const double mat[4] = {vMatParam[0][0], vMatParam[0][1], vMatParam[1][0], vMatParam[1][1]};
+    ellipsoid_from_derivs(E.data(), ANALYSIS, axis, Ld, mat, vProbParam[0], F);
+    if (ANALYSIS == 11) {
+        // the reference scales the particle's row of vMatParam in place
+        // (src/force.c:286-292), and its later calls see the scaled values
+        const double Cs = axis[0] * axis[2] / (2.0 * axis[2] + axis[0]);
+        vMatParam[1][1] *= Cs;
+        vMatParam[1][0] *= Cs;
+    }
+    return 0;
+}
+
+extern "C" int forceMultipole_tria3(unsigned int nOrder, double R, double *Xeval, double **mNodes,
+                                    unsigned int **mElems, double *vB, double **vMatParam, double *vProbParam,
+                                    double *F)
+{
+    return multipole_dropin(3, nOrder, R, Xeval, mNodes, mElems, vB, vMatParam, vProbParam, F);
+}
+
+extern "C" int forceMultipole_tria6(unsigned int nOrder, double R, double *Xeval, double **mNodes,
+                                    unsigned int **mElems, double *vB, double **vMatParam, double *vProbParam,
+                                    double *F)
+{
+    return multipole_dropin(6, nOrder, R, Xeval, mNodes, mElems, vB, vMatParam, vProbParam, F);
+}
+
+extern "C" int forceEllipsoid_tria3(unsigned int ANALYSIS, unsigned int nOrder, double *axis, double *Xeval,
+                                    double **mNodes, unsigned int **mElems, double *vB, double **vMatParam,
+                                    double *vProbParam, double *F)
+{
+    (void)nOrder;
+    return ellipsoid_dropin(3, ANALYSIS, axis, Xeval, mNodes, mElems, vB, vMatParam, vProbParam, F);
+}
+
+extern "C" int forceEllipsoid_tria6(unsigned int ANALYSIS, unsigned int nOrder, double *axis, double *Xeval,
+                                    double **mNodes, unsigned int **mElems, double *vB, double **vMatParam,
+                                    double *vProbParam, double *F)
+{
+    (void)nOrder;
+    return ellipsoid_dropin(6, ANALYSIS, axis, Xeval, mNodes, mElems, vB, vMatParam, vProbParam, F);
+}
+
 static int force_dropin(int nen, double **mNodes, unsigned **mElems, unsigned *vBCType, double *vB,
                         double Eps, double **Fce, double **Xce, double *Fcm, double *Xcm)
 {
@@ -822,6 +1050,68 @@ extern "C" int dsc_potential_points(int nen, unsigned N, unsigned E, const doubl
     std::vector<int> e0;
     elems_to0(nen, (int)E, elems, e0);
     return points_impl(nen, N, E, nodes, e0.data(), vB, npts, pts, 0, mPot);
+}
+
+extern "C" int dsc_force_multipole(int nen, unsigned N, unsigned E, const double *nodes, const unsigned *elems,
+                                   const double *vB, unsigned npts, const double *pts, unsigned order, double R,
+                                   const double *mat, double freq, double *F)
+{
+    std::lock_guard<std::mutex> lk(ctx().mu);
+    if ((nen != 3 && nen != 6) || !nodes || !elems || !vB || !pts || !mat || !F || order < 1) {
+        set_error("dsc_force_multipole: bad arguments");
+        return kErrArg;
+    }
+    std::vector<int> e0;
+    elems_to0(nen, (int)E, elems, e0);
+    MeshEntry *m;
+    DSC_TRY(get_mesh(nen, (int)N, (int)E, nodes, e0.data(), &m));
+    std::vector<double> Ed;
+    DSC_TRY(derivs_on(m, vB, npts, pts, Ed));
+    for (unsigned q = 0; q < npts; q++)
+        multipole_from_derivs(nen, Ed.data() + (size_t)q * kDerivCount, order, R, mat, freq, F + 3 * (size_t)q);
+    return kOk;
+}
+
+extern "C" int dsc_force_ellipsoid(int nen, unsigned N, unsigned E, const double *nodes, const unsigned *elems,
+                                   const double *vB, unsigned npts, const double *pts, unsigned analysis,
+                                   const double *axis, const double *mat, double freq, double *F)
+{
+    std::lock_guard<std::mutex> lk(ctx().mu);
+    if ((nen != 3 && nen != 6) || !nodes || !elems || !vB || !pts || !mat || !F || !axis ||
+        (analysis != 10 && analysis != 11)) {
+        set_error("dsc_force_ellipsoid: bad arguments");
+        return kErrArg;
+    }
+    double Ld[3];
+    bool warn = false;
+    if (!depolarization_factors(axis, Ld, &warn)) {
+        set_error("dsc_force_ellipsoid: negative depolarisation factors (%g %g %g)", Ld[0], Ld[1], Ld[2]);
+        return kErrArg;
+    }
+    std::vector<int> e0;
+    elems_to0(nen, (int)E, elems, e0);
+    MeshEntry *m;
+    DSC_TRY(get_mesh(nen, (int)N, (int)E, nodes, e0.data(), &m));
+    std::vector<double> Ed;
+    DSC_TRY(derivs_on(m, vB, npts, pts, Ed));
+    for (unsigned q = 0; q < npts; q++)
+        ellipsoid_from_derivs(Ed.data() + (size_t)q * kDerivCount, analysis, axis, Ld, mat, freq,
+                              F + 3 * (size_t)q);
+    return kOk;
+}
+
+extern "C" int dsc_depolarization(const double *axis, double *Ld)
+{
+    bool warn = false;
+    if (!axis || !Ld) {
+        set_error("dsc_depolarization: bad arguments");
+        return kErrArg;
+    }
+    if (!depolarization_factors(axis, Ld, &warn)) {
+        set_error("negative depolarisation factors");
+        return kErrArg;
+    }
+    return kOk;
 }
 
 extern "C" int dsc_force_mst(int nen, unsigned N, unsigned E, const double *nodes,

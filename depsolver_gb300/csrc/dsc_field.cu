@@ -813,3 +813,133 @@ int force_mst_dev(const DeviceMesh &m, ForcePlan &fp, const double *dsigma, doub
 }
 
 }  // namespace dsc
+
+// ------------------------------------------------------------ derivatives
+namespace dsc {
+
+// T[deriv_index(a)] = d^a (1/|d|) / dx^a for |a| <= kDerivOrder, by the
+// recurrence that follows from |d|^2 d_i(1/r) = -d_i / r differentiated
+// d^b times (a = b + e_i, i the first axis of a with a_i > 0):
+//   |d|^2 T_a = -d_i T_b - b_i T_{b - e_i}
+//               - sum_j [2 b_j d_j T_{b + e_i - e_j} + b_j (b_j - 1) T_{b + e_i - 2 e_j}].
+// The loops unroll completely, so every index is a constant.
+__device__ __forceinline__ void inv_r_derivs(const double d[3], double (&T)[kDerivCount])
+{
+    const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2], ir2 = 1.0 / r2;
+    T[0] = sqrt(ir2);
+#pragma unroll
+    for (int n = 1; n <= kDerivOrder; n++)
+#pragma unroll
+        for (int p = n; p >= 0; p--)
+#pragma unroll
+            for (int q = n - p; q >= 0; q--) {
+                const int a[3] = {p, q, n - p - q};
+                const int i = p > 0 ? 0 : (q > 0 ? 1 : 2);
+                int b[3] = {a[0], a[1], a[2]};
+                b[i]--;
+                double v = -d[i] * T[deriv_index(b[0], b[1], b[2])];
+                if (b[i] > 0) {
+                    int c[3] = {b[0], b[1], b[2]};
+                    c[i]--;
+                    v -= b[i] * T[deriv_index(c[0], c[1], c[2])];
+                }
+#pragma unroll
+                for (int j = 0; j < 3; j++) {
+                    if (b[j] > 0) {
+                        int c[3] = {b[0], b[1], b[2]};
+                        c[i]++;
+                        c[j]--;
+                        v -= 2.0 * b[j] * d[j] * T[deriv_index(c[0], c[1], c[2])];
+                    }
+                    if (b[j] > 1) {
+                        int c[3] = {b[0], b[1], b[2]};
+                        c[i]++;
+                        c[j] -= 2;
+                        v -= (double)(b[j] * (b[j] - 1)) * T[deriv_index(c[0], c[1], c[2])];
+                    }
+                }
+                T[deriv_index(a[0], a[1], a[2])] = v * ir2;
+            }
+}
+
+// part[(pt * nchunk + chunk) * kDerivCount + a] = sum over the chunk's
+// quadrature points (charge c = w J Re sigma, cq layout of k_charge_qp) of
+// c T_a(x_pt - y_q); block per (point, chunk), fixed-order reduction.
+constexpr int kDerivThreads = 128;
+__global__ void __launch_bounds__(kDerivThreads) k_point_derivs(const double *__restrict__ pts, int npts,
+                                                                const double *__restrict__ cq, int nq, int per,
+                                                                double *__restrict__ part)
+{
+    __shared__ double sh[kDerivThreads / 32][kDerivCount];
+    const int pt = blockIdx.x, chunk = blockIdx.y, nchunk = gridDim.y;
+    const double x = pts[3 * pt], y = pts[3 * pt + 1], z = pts[3 * pt + 2];
+    double S[kDerivCount];
+#pragma unroll
+    for (int a = 0; a < kDerivCount; a++) S[a] = 0.0;
+    const int q0 = chunk * per, q1 = min(nq, q0 + per);
+    for (int q = q0 + threadIdx.x; q < q1; q += kDerivThreads) {
+        const double *c = cq + (size_t)q * 5;
+        const double d[3] = {x - c[0], y - c[1], z - c[2]};
+        double T[kDerivCount];
+        inv_r_derivs(d, T);
+        const double w = c[3];
+#pragma unroll
+        for (int a = 0; a < kDerivCount; a++) S[a] = fma(w, T[a], S[a]);
+    }
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+#pragma unroll
+    for (int a = 0; a < kDerivCount; a++) {
+        const double v = warp_sum(S[a]);
+        if (lane == 0) sh[wp][a] = v;
+    }
+    __syncthreads();
+    for (int a = threadIdx.x; a < kDerivCount; a += kDerivThreads) {
+        double t = 0.0;
+        for (int w2 = 0; w2 < kDerivThreads / 32; w2++) t += sh[w2][a];
+        part[((size_t)pt * nchunk + chunk) * kDerivCount + a] = t;
+    }
+    (void)npts;
+}
+
+// E[pt][a] = -scale * sum over the chunks (in order) of part: the field
+// (|a| = 1) and its derivatives (|a| > 1) at the point, E = -grad phi.
+__global__ void k_point_derivs_sum(const double *__restrict__ part, int npts, int nchunk, double scale,
+                                   double *__restrict__ E)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= npts * kDerivCount) return;
+    const int pt = t / kDerivCount, a = t % kDerivCount;
+    double s = 0.0;
+    for (int c = 0; c < nchunk; c++) s += part[((size_t)pt * nchunk + c) * kDerivCount + a];
+    E[t] = -scale * s;
+}
+
+int point_derivatives(const DeviceMesh &m, const double *dsigma, int npts, const double *dpts, DerivWork &w,
+                      double *E_host, cudaStream_t st)
+{
+    const int nq = m.E * kTriPts;
+    DSC_TRY(w.cq.alloc((size_t)nq * 5));
+    if (m.nen == 6)
+        DSC_LAUNCH(k_charge_qp<6><<<(nq + 255) / 256, 256, 0, st>>>(m.x.p, m.y.p, m.z.p, m.elems.p, m.E, m.N, dsigma,
+                                                                    w.cq.p));
+    else
+        DSC_LAUNCH(k_charge_qp<3><<<(nq + 255) / 256, 256, 0, st>>>(m.x.p, m.y.p, m.z.p, m.elems.p, m.E, m.N, dsigma,
+                                                                    w.cq.p));
+    // about 4 blocks per SM over all points
+    int nsm = 0;
+    DSC_TRY(current_sm_count(&nsm));
+    const int nchunk = std::max(1, std::min((4 * nsm + npts - 1) / npts, (nq + kDerivThreads - 1) / kDerivThreads));
+    const int per = (nq + nchunk - 1) / nchunk;
+    DSC_TRY(w.part.alloc((size_t)npts * nchunk * kDerivCount));
+    DSC_TRY(w.E.alloc((size_t)npts * kDerivCount));
+    DSC_LAUNCH(k_point_derivs<<<dim3(npts, nchunk), kDerivThreads, 0, st>>>(dpts, npts, w.cq.p, nq, per, w.part.p));
+    const double B = 1.0 / (kPi4 * kEps0);  // src/force.c:232
+    DSC_LAUNCH(k_point_derivs_sum<<<(npts * kDerivCount + 255) / 256, 256, 0, st>>>(w.part.p, npts, nchunk, B, w.E.p));
+    DSC_CUDA(cudaGetLastError());
+    DSC_CUDA(cudaMemcpyAsync(E_host, w.E.p, (size_t)npts * kDerivCount * sizeof(double), cudaMemcpyDeviceToHost,
+                             st));
+    DSC_CUDA(cudaStreamSynchronize(st));
+    return kOk;
+}
+
+}  // namespace dsc

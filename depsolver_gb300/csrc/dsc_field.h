@@ -55,6 +55,35 @@ struct ForcePlan {
     int build(const HostPlan &plan, const unsigned *bctype, cudaStream_t st);
 };
 
+// Derivatives of the field at points (the reference's intDE_* tensors
+// summed over the mesh, src/forceIntegrals.c:61-619): for every multi-index
+// a with 1 <= |a| <= kDerivOrder, E_a = -d^a phi at the point with
+// phi = (1 / 4 pi eps0) sum over the elements of int Re(sigma) / r (so
+// E_(1,0,0) = Re Ex, E_(2,0,0) = dEx/dx, E_(1,1,0) = dEx/dy, ...), from the
+// 7-point rule of every element (the points are away from the surface).
+// Entries in the order of deriv_index (index 0, the potential's order 0, is
+// left at zero).
+constexpr int kDerivOrder = 4;
+constexpr int kDerivCount = (kDerivOrder + 1) * (kDerivOrder + 2) * (kDerivOrder + 3) / 6;
+// Index of the multi-index (p, q, r), p + q + r = n <= kDerivOrder, in the
+// flat derivative arrays: orders in turn, within an order p descending,
+// then q descending.
+__host__ __device__ constexpr int deriv_index(int p, int q, int r)
+{
+    const int n = p + q + r;
+    const int start = n * (n + 1) * (n + 2) / 6;
+    // entries of order n before (p, q): those with a larger p, then larger q
+    int before = 0;
+    for (int pp = n; pp > p; pp--) before += n - pp + 1;
+    return start + before + (n - p - q);
+}
+
+struct DerivWork {
+    DevBuf<double> cq, part, E;
+};
+int point_derivatives(const DeviceMesh &m, const double *dsigma, int npts, const double *dpts, DerivWork &w,
+                      double *E_host, cudaStream_t st);
+
 // Values per particle and system of the per-particle Maxwell-stress results.
 constexpr int kPartVals = 12;
 // out[(f * npart + p) * kPartVals + ...] for the nsys systems whose element

@@ -145,30 +145,35 @@ __device__ __forceinline__ unsigned cluster_rank()
 }
 
 // The cluster-wide sum of every thread's v, identical in all threads of all
-// CTAs (fixed order: warps, then CTAs by rank).  slot: 2 x kMgsCta partials
-// of this CTA's shared memory (its own in slot[p][0]).
-__device__ __forceinline__ double cluster_sum(double v, double *wsum, double *slot, int p)
+// CTAs (fixed order: a shuffle tree within each warp, one over the warps'
+// sums, one over the CTAs' sums by rank).  slot[p] holds this CTA's partial
+// of parity p (read by every CTA of the cluster through distributed shared
+// memory), sum[p] the cluster's sum for this CTA's threads.
+__device__ __forceinline__ double cluster_sum(double v, double *wsum, double *slot, double *sum, int p)
 {
+    static_assert(kMgsThreads / 32 == 32 && kMgsCta <= 32, "one warp reduces the warps' and the CTAs' sums");
     v = warp_sum(v);
     const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
     if (lane == 0) wsum[wp] = v;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (int q = 0; q < kMgsThreads / 32; q++) t += wsum[q];
-        slot[p] = t;
+    if (wp == 0) {
+        const double t = warp_sum(wsum[lane]);
+        if (lane == 0) slot[p] = t;
     }
     cluster_sync_all();  // every CTA's partial of this parity is written
-    double t = 0.0;
-    const unsigned local = (unsigned)__cvta_generic_to_shared(&slot[p]);
-    for (unsigned r = 0; r < kMgsCta; r++) {
-        unsigned remote;
-        double x;
-        asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(remote) : "r"(local), "r"(r));
-        asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(x) : "r"(remote) : "memory");
-        t += x;
+    if (wp == 0) {
+        double x = 0.0;
+        if (lane < kMgsCta) {
+            const unsigned local = (unsigned)__cvta_generic_to_shared(&slot[p]);
+            unsigned remote;
+            asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(remote) : "r"(local), "r"(lane));
+            asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(x) : "r"(remote) : "memory");
+        }
+        x = warp_sum(x);
+        if (lane == 0) sum[p] = x;
     }
-    return t;
+    __syncthreads();
+    return sum[p];
 }
 
 __global__ void __launch_bounds__(kMgsThreads, 1) k_mgs_cluster(double *__restrict__ V, int n, int i,
@@ -176,7 +181,7 @@ __global__ void __launch_bounds__(kMgsThreads, 1) k_mgs_cluster(double *__restri
                                                                  const int *__restrict__ done)
 {
     extern __shared__ double ws[];                    // this CTA's slice of w
-    __shared__ double wsum[kMgsThreads / 32], slot[2];
+    __shared__ double wsum[kMgsThreads / 32], slot[2], csum[2];
     if (*done) return;  // the whole cluster reads the same flag
     const unsigned rank = cluster_rank();
     const int L = (n + kMgsCta - 1) / kMgsCta;
@@ -189,7 +194,7 @@ __global__ void __launch_bounds__(kMgsThreads, 1) k_mgs_cluster(double *__restri
         s += x * x;
     }
     int p = 0;
-    const double w2 = cluster_sum(s, wsum, slot, p);
+    const double w2 = cluster_sum(s, wsum, slot, csum, p);
     if (rank == 0 && threadIdx.x == 0) *ww = w2;
     for (int j = 0; j <= i + 1; j++) {
         const double *v = V + (size_t)j * n;
@@ -199,7 +204,7 @@ __global__ void __launch_bounds__(kMgsThreads, 1) k_mgs_cluster(double *__restri
         else
             for (int t = lo + threadIdx.x; t < hi; t += kMgsThreads) d += ws[t - lo] * ws[t - lo];
         p ^= 1;
-        const double hj = cluster_sum(d, wsum, slot, p);
+        const double hj = cluster_sum(d, wsum, slot, csum, p);
         if (j <= i) {
             for (int t = lo + threadIdx.x; t < hi; t += kMgsThreads) ws[t - lo] = ws[t - lo] - hj * v[t];
             if (rank == 0 && threadIdx.x == 0) h[j] = hj;

@@ -87,6 +87,26 @@ int forceMST_tria3(double **mNodes, unsigned int **mElems, unsigned int *vBCType
                    double Eps, double **Fce, double **Xce, double *Fcm, double *Xcm);
 int forceMST_tria6(double **mNodes, unsigned int **mElems, unsigned int *vBCType, double *vB,
                    double Eps, double **Fce, double **Xce, double *Fcm, double *Xcm);
+/* forceMultipole_* replace src/force.c:572 / :709 (src/force.h): the DEP
+ * force on a sphere of radius R centred at Xeval by the multipole expansion
+ * of order nOrder (the reference adds the terms up to order 3; orders 4
+ * and 5 give the order-3 force), from Re(E) and its derivatives at Xeval;
+ * vMatParam rows 0 (medium) and 1 (particle), vProbParam[0] the frequency.
+ * forceEllipsoid_* replace src/force.c:65 / :204: the dipole force on an
+ * ellipsoid of semi-axes `axis` (ANALYSIS 10 homogeneous, 11 single-shell;
+ * for 11 the reference scales vMatParam[1] in place, and so does this). */
+int forceMultipole_tria3(unsigned int nOrder, double R, double *Xeval, double **mNodes,
+                         unsigned int **mElems, double *vB, double **vMatParam, double *vProbParam,
+                         double *F);
+int forceMultipole_tria6(unsigned int nOrder, double R, double *Xeval, double **mNodes,
+                         unsigned int **mElems, double *vB, double **vMatParam, double *vProbParam,
+                         double *F);
+int forceEllipsoid_tria3(unsigned int ANALYSIS, unsigned int nOrder, double *axis, double *Xeval,
+                         double **mNodes, unsigned int **mElems, double *vB, double **vMatParam,
+                         double *vProbParam, double *F);
+int forceEllipsoid_tria6(unsigned int ANALYSIS, unsigned int nOrder, double *axis, double *Xeval,
+                         double **mNodes, unsigned int **mElems, double *vB, double **vMatParam,
+                         double *vProbParam, double *F);
 
 /* ------------------------------------------------------------ flat dsc_ API */
 
@@ -159,6 +179,19 @@ int dsc_field_points(int nen, unsigned N, unsigned E, const double *nodes, const
 int dsc_potential_points(int nen, unsigned N, unsigned E, const double *nodes,
                          const unsigned *elems, const double *vB, unsigned npts,
                          const double *pts, double *mPot);
+
+/* Flat forms of forceMultipole_* and forceEllipsoid_* at npts points (pts
+ * npts x 3, F npts x 3); mat = {sigma_m, eps_m, sigma_p, eps_p}.  Unlike the
+ * reference's forceEllipsoid (ANALYSIS 11), the flat form leaves mat
+ * unchanged.  dsc_depolarization gives the ellipsoid's depolarisation
+ * factors (src/depolarization.c:44-115). */
+int dsc_force_multipole(int nen, unsigned N, unsigned E, const double *nodes, const unsigned *elems,
+                        const double *vB, unsigned npts, const double *pts, unsigned order, double R,
+                        const double *mat, double freq, double *F);
+int dsc_force_ellipsoid(int nen, unsigned N, unsigned E, const double *nodes, const unsigned *elems,
+                        const double *vB, unsigned npts, const double *pts, unsigned analysis,
+                        const double *axis, const double *mat, double freq, double *F);
+int dsc_depolarization(const double *axis, double *Ld);
 
 /* Flat form of forceMST_*: Fce, Xce are E x 3 (may be NULL). */
 int dsc_force_mst(int nen, unsigned N, unsigned E, const double *nodes, const unsigned *elems,

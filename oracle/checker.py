@@ -223,6 +223,10 @@ class Ref:
         L.ref_int.argtypes = [C.c_int, C.c_int, C.c_uint, C.c_uint, _dp, _dp, _dp, _dp]
         L.ref_node_normal.argtypes = [C.c_int, C.c_uint, C.c_uint, _dp, _up, C.c_uint, _dp]
         L.ref_set_sizes.argtypes = [C.c_uint, C.c_uint, C.c_uint]
+        L.ref_forceMultipole.argtypes = [C.c_int, C.c_uint, C.c_uint, _dp, _up, _dp, C.c_uint, C.c_double,
+                                         _dp, _dp, C.c_double, _dp]
+        L.ref_forceEllipsoid.argtypes = [C.c_int, C.c_uint, C.c_uint, _dp, _up, _dp, C.c_uint, _dp, _dp,
+                                         _dp, C.c_double, _dp]
 
     def assemble(self, sc, full=False):
         N = sc.N
@@ -286,6 +290,22 @@ class Ref:
         n = np.zeros(3)
         self.lib.ref_node_normal(sc.nen, sc.N, sc.E, _f(sc.nodes), _u(sc.elems), node0 + 1, n)
         return n
+
+    def force_multipole(self, sc, vB, order, R, xeval):
+        """forceMultipole_* at xeval (materials 1 and 2 of the scene)."""
+        F = np.zeros(3)
+        with _in_dir(self.workdir):
+            self.lib.ref_forceMultipole(sc.nen, sc.N, sc.E, _f(sc.nodes), _u(sc.elems), _f(vB), order, R,
+                                        _f(xeval), _f(sc.mat[:2]), sc.freq, F)
+        return F
+
+    def force_ellipsoid(self, sc, vB, analysis, axis, xeval):
+        """forceEllipsoid_* (analysis 10 or 11) at xeval."""
+        F = np.zeros(3)
+        with _in_dir(self.workdir):
+            self.lib.ref_forceEllipsoid(sc.nen, sc.N, sc.E, _f(sc.nodes), _u(sc.elems), _f(vB), analysis,
+                                        _f(axis), _f(xeval), _f(sc.mat[:2]), sc.freq, F)
+        return F
 
     def integral(self, which, nen, X, xe, flag=0, sin=0, normal=(0.0, 0.0, 1.0)):
         code = {"G": 0, "H": 1, "SG": 2, "SH": 3}[which]

@@ -53,6 +53,10 @@ int intSingularH_tria3(const unsigned, unsigned, double X[3][3], double*, double
 int intSingularH_tria6(const unsigned, unsigned, double X[6][3], double*, double*, double*);
 int getNormal_tria3(unsigned, double**, unsigned**, double*);
 int getNormal_tria6(unsigned, double**, unsigned**, double*);
+int forceMultipole_tria3(unsigned, double, double*, double**, unsigned**, double*, double**, double*, double*);
+int forceMultipole_tria6(unsigned, double, double*, double**, unsigned**, double*, double**, double*, double*);
+int forceEllipsoid_tria3(unsigned, unsigned, double*, double*, double**, unsigned**, double*, double**, double*, double*);
+int forceEllipsoid_tria6(unsigned, unsigned, double*, double*, double**, unsigned**, double*, double**, double*, double*);
 
 static double **rows_d(double *base, unsigned nrows, unsigned ld)
 {
@@ -175,6 +179,46 @@ int ref_forceMST(int nen, unsigned N, unsigned E, double *nodes, unsigned *elems
     int rc = nen == 3 ? forceMST_tria3(mNodes, mElems, bctype, vB, eps, mFce, mXce, Fcm, Xcm)
                       : forceMST_tria6(mNodes, mElems, bctype, vB, eps, mFce, mXce, Fcm, Xcm);
     free(mNodes); free(mElems); free(mFce); free(mXce);
+    return rc;
+}
+
+/* forceMultipole_* (src/force.c:572,709) at Xeval for a sphere of radius R:
+ * mat holds the medium's and the particle's (sigma, eps_r) rows. */
+int ref_forceMultipole(int nen, unsigned N, unsigned E, double *nodes, unsigned *elems,
+                       double *vB, unsigned order, double R, double *Xeval, double *mat,
+                       double freq, double *F)
+{
+    ref_set_sizes(N, E, nInterfaces);
+    double **mNodes = rows_d(nodes, N, 3);
+    unsigned **mElems = rows_u(elems, E, (unsigned)nen);
+    double m[4] = {mat[0], mat[1], mat[2], mat[3]};
+    double **vMat = rows_d(m, 2, 2);
+    double prob[1] = {freq};
+    double x[3] = {Xeval[0], Xeval[1], Xeval[2]};
+    int rc = nen == 3 ? forceMultipole_tria3(order, R, x, mNodes, mElems, vB, vMat, prob, F)
+                      : forceMultipole_tria6(order, R, x, mNodes, mElems, vB, vMat, prob, F);
+    free(mNodes); free(mElems); free(vMat);
+    return rc;
+}
+
+/* forceEllipsoid_* (src/force.c:65,204): analysis 10 (homogeneous) or 11
+ * (shelled); the reference rescales the particle's row of vMatParam in place
+ * for 11, so it works on a copy here. */
+int ref_forceEllipsoid(int nen, unsigned N, unsigned E, double *nodes, unsigned *elems,
+                       double *vB, unsigned analysis, double *axis, double *Xeval, double *mat,
+                       double freq, double *F)
+{
+    ref_set_sizes(N, E, nInterfaces);
+    double **mNodes = rows_d(nodes, N, 3);
+    unsigned **mElems = rows_u(elems, E, (unsigned)nen);
+    double m[4] = {mat[0], mat[1], mat[2], mat[3]};
+    double **vMat = rows_d(m, 2, 2);
+    double prob[1] = {freq};
+    double x[3] = {Xeval[0], Xeval[1], Xeval[2]};
+    double ax[3] = {axis[0], axis[1], axis[2]};
+    int rc = nen == 3 ? forceEllipsoid_tria3(analysis, 1, ax, x, mNodes, mElems, vB, vMat, prob, F)
+                      : forceEllipsoid_tria6(analysis, 1, ax, x, mNodes, mElems, vB, vMat, prob, F);
+    free(mNodes); free(mElems); free(vMat);
     return rc;
 }
 

@@ -19,6 +19,9 @@ own functions through oracle/ref_harness.c):
 * cfg0_tria6.npz -- the level-2 sphere between 10 x 10-cell plates
   (1524 nodes): Gauss (3048 unknowns) and GMRES at 1e-10 solutions, MST
   force from each.
+* multipole.npz -- forceMultipole_* (orders 1-5) and forceEllipsoid_*
+  (analyses 10 and 11) of both small scenes at three points, from their
+  Gauss solutions.
 * dep_trap_2.npz -- the reference's own example deck examples/dep-trap-2
   (956 nodes, 1676 tria3, nodes 537.. shifted by (1.25e-5, 0, 0) as its
   REPOSITION section asks), with the reference's solution, gmres.log and
@@ -113,21 +116,52 @@ def dep_trap_2(ref, examples, path):
     print("wrote", path, os.path.getsize(path), "bytes")
 
 
+MP_POINTS = np.array([[0.0, 0.0, 0.4], [0.05, -0.1, 0.3], [0.5, 0.5, -1.8]])
+MP_AXIS = np.array([1.0, 0.9, 0.8])
+
+
+def multipole_fixture(ref, path):
+    """forceMultipole_* (orders 1-5) and forceEllipsoid_* (analyses 10, 11)
+    of the reference at three points (the small scene's sphere centre, a
+    point inside the sphere and one in the medium), from the reference's
+    own Gauss solution of each small scene (radius 1; semi-axes MP_AXIS)."""
+    out = {"points": MP_POINTS, "axis": MP_AXIS, "R": np.float64(1.0)}
+    for nen in (6, 3):
+        sc = scenes.small(nen=nen)
+        g = np.load(os.path.join(HERE, f"small_tria{nen}.npz"))
+        x = g["x_gauss"]
+        out[f"x_{nen}"] = x
+        out[f"multipole_{nen}"] = np.array([[ref.force_multipole(sc, x, o, 1.0, p) for o in range(1, 6)]
+                                            for p in MP_POINTS])
+        out[f"ellipsoid_{nen}"] = np.array([[ref.force_ellipsoid(sc, x, a, MP_AXIS, p) for a in (10, 11)]
+                                            for p in MP_POINTS])
+    np.savez_compressed(path, **out)
+    print("wrote", path, os.path.getsize(path), "bytes")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference",
                     default=os.path.normpath(os.path.join(HERE, "..", "..", "..", "reference")))
+    ap.add_argument("--only", nargs="*", default=None,
+                    help="fixtures to write (small, cfg0, dep_trap_2, multipole; default: all)")
     args = ap.parse_args()
+    want = set(args.only) if args.only else {"small", "cfg0", "dep_trap_2", "multipole"}
     os.environ["DSC_REFERENCE_SRC"] = os.path.join(args.reference, "src")
     from oracle import checker
     checker.REF_SRC = os.environ["DSC_REFERENCE_SRC"]
     if checker.build_ref() is None:
         sys.exit("reference sources not found")
     ref = checker.Ref()
-    for nen in (6, 3):
-        scene_fixture(ref, scenes.small(nen=nen), os.path.join(HERE, f"small_tria{nen}.npz"))
-    scene_fixture(ref, scenes.cfg0(nen=6, center=(0.0, 0.0, 1.0)), os.path.join(HERE, "cfg0_tria6.npz"))
-    dep_trap_2(ref, os.path.join(args.reference, "examples"), os.path.join(HERE, "dep_trap_2.npz"))
+    if "small" in want:
+        for nen in (6, 3):
+            scene_fixture(ref, scenes.small(nen=nen), os.path.join(HERE, f"small_tria{nen}.npz"))
+    if "cfg0" in want:
+        scene_fixture(ref, scenes.cfg0(nen=6, center=(0.0, 0.0, 1.0)), os.path.join(HERE, "cfg0_tria6.npz"))
+    if "dep_trap_2" in want:
+        dep_trap_2(ref, os.path.join(args.reference, "examples"), os.path.join(HERE, "dep_trap_2.npz"))
+    if "multipole" in want:
+        multipole_fixture(ref, os.path.join(HERE, "multipole.npz"))
 
 
 if __name__ == "__main__":
