@@ -9,6 +9,9 @@
 namespace dsc {
 
 constexpr int kPB = 128;  // Gauss-Jordan / block-LU tile
+// SMs that the rest of a look-ahead update (a persistent grid on a side
+// stream) leaves free for the next step's pivot inverses and row blocks.
+constexpr int kGjReserveSms = 16;
 
 // A 128 x 128 FP32 tile at base (element (a, b) at base[a * stride + b], b
 // contiguous, 16-byte aligned rows) into shared memory through put(a, b,
@@ -62,58 +65,46 @@ __device__ __forceinline__ void pre_row_pair(const float *v, __half *h, __half *
 
 // Threads of the CTA that inverts one tile (gj_invert_tile).
 constexpr int kGjThreads = 1024;
-
-// One pivot of gj_invert_tile: pivot j = 4 m + S (S a compile-time slot:
-// row S of warp m holds row j, slot S of lane m holds column j).
+// P (row-major, 128 x 128) and PT (its transpose, row-major), each when not
+// null, = inverse of the tile at T (column-major: element (r, c) at
+// T[c * ldt + r], 16-byte aligned columns) by Gauss-Jordan without
+// pivoting, four pivots per block barrier, in one CTA of kGjThreads
+// threads.  Warp w holds rows 4w .. 4w+3, lane l columns 4l .. 4l+3 of
+// them: 16 values in registers.  Step m takes pivots 4m .. 4m+3, whose rows
+// are warp m's and whose columns are lane m's: warp m first eliminates
+// them among its own four rows (per pivot: the pivot from lane m, its row
+// scaled with the pivot's own entry replaced by 1, the other three rows
+// updated with their entries of the pivot column read from lane m and
+// replaced by 0 there), which leaves those rows final for the step, and
+// publishes them in shared memory; after one barrier every other warp reads
+// its rows' entries in the four pivot columns from lane m (where they are
+// then replaced by 0) and takes the rank-4 update a_ic -= sum_q a_iq r_qc.
+// The published rows alternate between two buffers by the parity of m.
+// With bad not null, a pivot whose magnitude is at most tol sets *bad to
+// row0 + its row (the lowest such row wins) and the inversion goes on.
 template <int S>
-__device__ __forceinline__ void gj_pivot_step(float (&a)[4][4], int m, float *pr, float tol, int *bad, int row0)
+__device__ __forceinline__ void gj_own_pivot(float (&a)[4][4], int m, float tol, int *bad, int row0)
 {
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    if (w == m) {
-        // row j: a_jj from lane m, replaced by 1, the row divided by it
-        const float pv = __shfl_sync(0xffffffffu, a[S][S], m);
-        if (bad && l == 0 && !(fabsf(pv) > tol)) atomicMin(bad, row0 + 4 * m + S);
-        const float inv = __frcp_rn(pv);
-        float rv[4];
+    const int l = threadIdx.x & 31;
+    const float pv = __shfl_sync(0xffffffffu, a[S][S], m);
+    if (bad && l == 0 && !(fabsf(pv) > tol)) atomicMin(bad, row0 + 4 * m + S);
+    const float inv = __frcp_rn(pv);
 #pragma unroll
-        for (int c = 0; c < 4; c++) rv[c] = (c == S && l == m ? 1.0f : a[S][c]) * inv;
-        *(float4 *)&pr[4 * l] = make_float4(rv[0], rv[1], rv[2], rv[3]);
-    }
-    __syncthreads();
-    const float4 q = *(const float4 *)&pr[4 * l];
-    const float qv[4] = {q.x, q.y, q.z, q.w};
+    for (int c = 0; c < 4; c++) a[S][c] = (c == S && l == m ? 1.0f : a[S][c]) * inv;
 #pragma unroll
     for (int r = 0; r < 4; r++) {
-        const float f = __shfl_sync(0xffffffffu, a[r][S], m);  // a_ij of this row
-        if (r == S && w == m) {
+        if (r == S) continue;
+        const float f = __shfl_sync(0xffffffffu, a[r][S], m);
+        if (l == m) a[r][S] = 0.0f;
 #pragma unroll
-            for (int c = 0; c < 4; c++) a[r][c] = qv[c];
-        } else {
-            if (l == m) a[r][S] = 0.0f;
-#pragma unroll
-            for (int c = 0; c < 4; c++) a[r][c] = fmaf(-f, qv[c], a[r][c]);
-        }
+        for (int c = 0; c < 4; c++) a[r][c] = fmaf(-f, a[S][c], a[r][c]);
     }
 }
 
-// P (row-major, 128 x 128) = inverse of the tile at T (column-major: element
-// (r, c) at T[c * ldt + r], 16-byte aligned columns) by Gauss-Jordan without
-// pivoting, in one CTA of kGjThreads threads.  Warp w holds rows 4w .. 4w+3,
-// lane l columns 4l .. 4l+3 of them: 16 values in registers.  Per pivot j
-// the warp holding row j takes a_jj from the lane holding column j, replaces
-// it by 1, divides the row by the pivot and publishes it in shared memory;
-// after one barrier every other row i takes a_ic -= a_ij r_c with a_ij
-// replaced by 0 first (a_ij read by shuffle from the lane that holds column
-// j), and row j becomes the published row.  The pivot loop is unrolled by
-// four so that the row and column slot of every pivot is a compile-time
-// index.  The published rows alternate between two buffers by the parity of
-// j, so one barrier a pivot suffices.  With bad not null, a pivot whose
-// magnitude is at most tol sets *bad to row0 + j (the lowest such j wins)
-// and the inversion goes on.
 __device__ __forceinline__ void gj_invert_tile(const float *__restrict__ T, int ldt, float *__restrict__ P,
-                                               float tol, int *bad, int row0)
+                                               float *__restrict__ PT, float tol, int *bad, int row0)
 {
-    __shared__ __align__(16) float prow[2][kPB];
+    __shared__ __align__(16) float prow[2][4][kPB];
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
     float a[4][4];  // a[r][c] = A(4 w + r, 4 l + c)
 #pragma unroll
@@ -124,15 +115,138 @@ __device__ __forceinline__ void gj_invert_tile(const float *__restrict__ T, int 
         a[2][c] = v.z;
         a[3][c] = v.w;
     }
+#pragma unroll 1
     for (int m = 0; m < kPB / 4; m++) {
-        gj_pivot_step<0>(a, m, prow[0], tol, bad, row0);
-        gj_pivot_step<1>(a, m, prow[1], tol, bad, row0);
-        gj_pivot_step<2>(a, m, prow[0], tol, bad, row0);
-        gj_pivot_step<3>(a, m, prow[1], tol, bad, row0);
-    }
+        float(*pr)[kPB] = prow[m & 1];
+        if (w == m) {
+            gj_own_pivot<0>(a, m, tol, bad, row0);
+            gj_own_pivot<1>(a, m, tol, bad, row0);
+            gj_own_pivot<2>(a, m, tol, bad, row0);
+            gj_own_pivot<3>(a, m, tol, bad, row0);
 #pragma unroll
-    for (int r = 0; r < 4; r++)
-        *(float4 *)(P + (size_t)(4 * w + r) * kPB + 4 * l) = make_float4(a[r][0], a[r][1], a[r][2], a[r][3]);
+            for (int r = 0; r < 4; r++)
+                *(float4 *)&pr[r][4 * l] = make_float4(a[r][0], a[r][1], a[r][2], a[r][3]);
+        }
+        __syncthreads();
+        if (w != m) {
+            float f[4][4];  // f[r][q] = A(4 w + r, 4 m + q) before the step
+#pragma unroll
+            for (int r = 0; r < 4; r++)
+#pragma unroll
+                for (int q = 0; q < 4; q++) f[r][q] = __shfl_sync(0xffffffffu, a[r][q], m);
+            if (l == m) {
+#pragma unroll
+                for (int r = 0; r < 4; r++)
+#pragma unroll
+                    for (int q = 0; q < 4; q++) a[r][q] = 0.0f;
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const float4 x = *(const float4 *)&pr[q][4 * l];
+                const float xv[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+                for (int r = 0; r < 4; r++)
+#pragma unroll
+                    for (int c = 0; c < 4; c++) a[r][c] = fmaf(-f[r][q], xv[c], a[r][c]);
+            }
+        }
+    }
+    if (P) {
+#pragma unroll
+        for (int r = 0; r < 4; r++)
+            *(float4 *)(P + (size_t)(4 * w + r) * kPB + 4 * l) = make_float4(a[r][0], a[r][1], a[r][2], a[r][3]);
+    }
+    if (PT) {
+#pragma unroll
+        for (int c = 0; c < 4; c++)
+            *(float4 *)(PT + (size_t)(4 * l + c) * kPB + 4 * w) = make_float4(a[0][c], a[1][c], a[2][c], a[3][c]);
+    }
+}
+
+// Shared memory of gj_row_product.
+constexpr int kGjRowXs = 36;  // row stride of the 32 X columns in shared memory (float4-aligned)
+constexpr size_t kGjRowSmem = sizeof(float) * (kPB * kPB + kPB * kGjRowXs);
+
+// R(kk, jj) = sum_q P(kk, q) X(q, j0 + jj) for 32 columns of one 128 x 128
+// tile, by 256 threads: PT is P transposed (PT[q * 128 + kk] = P(kk, q)),
+// X the tile, column-major with leading dimension ld (X(q, j) at
+// X[j * ld + q]).  sm holds kGjRowSmem bytes; the result is left in
+// T[jj * 129 + kk] (32 rows of 129 floats, in sm after P's copy) after a
+// block barrier.  Thread (ty, tx) forms kk = 4 ty + u, jj = 4 tx + v
+// (u, v < 4): per q one float4 of P's column and one of X's row.
+__device__ __forceinline__ float *gj_row_product(const float *__restrict__ PT, const float *__restrict__ X,
+                                                 size_t ld, int j0, float *sm)
+{
+    float *Ps = sm;              // Ps[q * 128 + kk] = P(kk, q)
+    float *Xs = sm + kPB * kPB;  // Xs[q * kGjRowXs + jj] = X(q, j0 + jj)
+#pragma unroll 4
+    for (int u = 0; u < kPB * kPB / 4 / 256; u++) {
+        const int t = threadIdx.x + 256 * u;
+        *(float4 *)&Ps[4 * t] = *(const float4 *)&PT[4 * t];
+    }
+    {
+        // lanes along q (coalesced columns of X), 16 values a thread
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        float v[16];
+#pragma unroll
+        for (int u = 0; u < 16; u++) {
+            const int jj = warp + 8 * (u >> 2), q = lane + 32 * (u & 3);
+            v[u] = X[(size_t)(j0 + jj) * ld + q];
+        }
+#pragma unroll
+        for (int u = 0; u < 16; u++) {
+            const int jj = warp + 8 * (u >> 2), q = lane + 32 * (u & 3);
+            Xs[q * kGjRowXs + jj] = v[u];
+        }
+    }
+    __syncthreads();
+    const int ty = threadIdx.x >> 3, tx = threadIdx.x & 7;
+    float acc[4][4];
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+#pragma unroll
+        for (int v = 0; v < 4; v++) acc[u][v] = 0.0f;
+#pragma unroll 8
+    for (int q = 0; q < kPB; q++) {
+        const float4 p = *(const float4 *)&Ps[q * kPB + 4 * ty];
+        const float4 x = *(const float4 *)&Xs[q * kGjRowXs + 4 * tx];
+        const float pv[4] = {p.x, p.y, p.z, p.w}, xv[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+#pragma unroll
+            for (int v = 0; v < 4; v++) acc[u][v] = fmaf(pv[u], xv[v], acc[u][v]);
+    }
+    __syncthreads();  // every read of Xs is done: T takes its place
+    float *T = Xs;
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+#pragma unroll
+        for (int v = 0; v < 4; v++) T[(4 * tx + v) * 129 + 4 * ty + u] = acc[u][v];
+    __syncthreads();
+    return T;
+}
+
+// The tile (column-major, leading dimension ld) as T[i * 129 + kk] = X(i,
+// kk) (in sm, 128 rows of 129 floats) after a block barrier, by 256
+// threads: lanes along i (coalesced columns), conflict-free stores.
+__device__ __forceinline__ void gj_load_rows(const float *__restrict__ X, size_t ld, float *T)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll 1
+    for (int kb = 0; kb < kPB; kb += 32) {
+        float v[16];
+#pragma unroll
+        for (int u = 0; u < 16; u++) {
+            const int kk = kb + warp + 8 * (u >> 2), i = lane + 32 * (u & 3);
+            v[u] = X[(size_t)kk * ld + i];
+        }
+#pragma unroll
+        for (int u = 0; u < 16; u++) {
+            const int kk = kb + warp + 8 * (u >> 2), i = lane + 32 * (u & 3);
+            T[i * 129 + kk] = v[u];
+        }
+    }
+    __syncthreads();
 }
 
 }  // namespace dsc

@@ -196,6 +196,23 @@ struct Timer {
 // main stream by join() -- or by the destructor, on every early return, so
 // that nothing queued on the main stream later (a free of a buffer the side
 // work uses) overtakes it.
+// Two events without timing (the look-ahead sequences of the blocked
+// Gauss-Jordan and block LU: one stream signals the other).
+struct EventPair {
+    cudaEvent_t a = nullptr, b = nullptr;
+    int create()
+    {
+        DSC_CUDA(cudaEventCreateWithFlags(&a, cudaEventDisableTiming));
+        DSC_CUDA(cudaEventCreateWithFlags(&b, cudaEventDisableTiming));
+        return kOk;
+    }
+    ~EventPair()
+    {
+        if (a) cudaEventDestroy(a);
+        if (b) cudaEventDestroy(b);
+    }
+};
+
 struct SideJoin {
     cudaStream_t main = nullptr;
     cudaEvent_t ev = nullptr;

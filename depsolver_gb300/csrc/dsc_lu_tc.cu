@@ -55,72 +55,47 @@ __global__ void k_lu_load(const double *__restrict__ A, size_t lda, int n, float
     for (int y = threadIdx.y; y < 32; y += blockDim.y) W[(size_t)(c0 + y) * np + r0 + threadIdx.x] = t[threadIdx.x][y];
 }
 
-// P_k = the inverse of the diagonal tile of step k.
+// P_k = the inverse of the diagonal tile of step k (and its transpose).
 __global__ void __launch_bounds__(kGjThreads) k_lu_pivot(const float *__restrict__ W, int np, int k, float *__restrict__ P,
-                                                   int *bad)
+                                                   float *__restrict__ PT, int *bad)
 {
     grid_dep_wait();  // a programmatic dependent of the previous step's update
-    gj_invert_tile(W + (size_t)k * kPB * np + k * kPB, np, P + (size_t)k * kPB * kPB, kLuPivTol, bad, k * kPB);
+    gj_invert_tile(W + (size_t)k * kPB * np + k * kPB, np, P + (size_t)k * kPB * kPB, PT + (size_t)k * kPB * kPB,
+                   kLuPivTol, bad, k * kPB);
 }
 
-// Step k, tile J = k + 1 + blockIdx.x: blockIdx.y = 0: R_kJ = P_k W_kJ
-// written into row block k and, transposed, as the update's B rows (the
-// tile's columns, 128 k-values each, at Bh + (J - k - 1) * 128 * 128);
-// blockIdx.y = 1: the column block's tile I = J as the update's A rows.
-__global__ void __launch_bounds__(256) k_lu_row(float *__restrict__ W, int np, int k, const float *__restrict__ P,
+// Step k, tile J = k + 1 + blockIdx.x: blockIdx.y < 4: columns 32 y ..
+// 32 y + 31 of R_kJ = P_k W_kJ (PT: every step's P transposed, tile k at
+// PT + k * 128 * 128) written into row block k and, transposed, as the
+// update's B rows (the tile's columns, 128 k-values each, at Bh + (J - k -
+// 1) * 128 * 128); blockIdx.y = 4: the column block's tile I = J as the
+// update's A rows.  256 threads.
+__global__ void __launch_bounds__(256) k_lu_row(float *__restrict__ W, int np, int k, const float *__restrict__ PT,
                                                 __half *__restrict__ Ah, __half *__restrict__ Al,
                                                 float *__restrict__ ra, __half *__restrict__ Bh,
                                                 __half *__restrict__ Bl, float *__restrict__ rb)
 {
     grid_dep_wait();  // a programmatic dependent of the pivot inversion
     const int J = k + 1 + blockIdx.x, o = blockIdx.x * kPB;
-    extern __shared__ float sm[];
-    float(*T)[129] = (float(*)[129])sm;  // T[r][c]
+    extern __shared__ __align__(16) float sm[];
     const int warp = threadIdx.x >> 5;
-    if (blockIdx.y == 1) {
+    if (blockIdx.y == 4) {
         // A row i of tile I = J: A[i][kk] = W(J*128 + i, k*128 + kk)
-        load_tile128(W + (size_t)k * kPB * np + J * kPB, (size_t)np, [&](int kk, int i, float v) { T[i][kk] = v; });
-        __syncthreads();
+        gj_load_rows(W + (size_t)k * kPB * np + J * kPB, (size_t)np, sm);
         for (int i = warp; i < kPB; i += 8)
-            pre_row_pair(&T[i][0], Ah + (size_t)(o + i) * kPB, Al + (size_t)(o + i) * kPB, &ra[o + i]);
+            pre_row_pair(&sm[i * 129], Ah + (size_t)(o + i) * kPB, Al + (size_t)(o + i) * kPB, &ra[o + i]);
         return;
     }
-    const float *Pk = P + (size_t)k * kPB * kPB;
-    float(*Pt)[128] = (float(*)[128])(sm + kPB * 129);               // Pt[q][kk] = P[kk][q]
-    float(*Xs)[129] = (float(*)[129])(sm + kPB * 129 + kPB * 128);  // Xs[j][q] = W(k*128 + q, J*128 + j)
-    load_tile128(Pk, kPB, [&](int r, int c, float v) { Pt[c][r] = v; });
-    load_tile128(W + (size_t)J * kPB * np + k * kPB, (size_t)np, [&](int r, int c, float v) { Xs[r][c] = v; });
-    __syncthreads();
-    // thread (ty, tx): kk = 8 ty + u, j = tx + 16 v (u, v < 8)
-    const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
-    float acc[8][8];
-#pragma unroll
-    for (int u = 0; u < 8; u++)
-#pragma unroll
-        for (int v = 0; v < 8; v++) acc[u][v] = 0.0f;
-#pragma unroll 4
-    for (int q = 0; q < kPB; q++) {
-        const float4 p0 = *(const float4 *)&Pt[q][8 * ty], p1 = *(const float4 *)&Pt[q][8 * ty + 4];
-        const float pa[8] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w};
-        float xb[8];
-#pragma unroll
-        for (int v = 0; v < 8; v++) xb[v] = Xs[tx + 16 * v][q];
-#pragma unroll
-        for (int u = 0; u < 8; u++)
-#pragma unroll
-            for (int v = 0; v < 8; v++) acc[u][v] = fmaf(pa[u], xb[v], acc[u][v]);
+    const int j0 = 32 * blockIdx.y;
+    const float *T =
+        gj_row_product(PT + (size_t)k * kPB * kPB, W + (size_t)J * kPB * np + k * kPB, (size_t)np, j0, sm);
+    for (int t = threadIdx.x; t < 32 * kPB; t += blockDim.x) {
+        const int jj = t >> 7, kk = t & 127;
+        W[(size_t)(J * kPB + j0 + jj) * np + k * kPB + kk] = T[jj * 129 + kk];
     }
-#pragma unroll
-    for (int u = 0; u < 8; u++)
-#pragma unroll
-        for (int v = 0; v < 8; v++) T[tx + 16 * v][8 * ty + u] = acc[u][v];
-    __syncthreads();
-    for (int t = threadIdx.x; t < kPB * kPB; t += blockDim.x) {
-        const int j = t >> 7, kk = t & 127;
-        W[(size_t)(J * kPB + j) * np + k * kPB + kk] = T[j][kk];
-    }
-    for (int jj = warp; jj < kPB; jj += 8)
-        pre_row_pair(&T[jj][0], Bh + (size_t)(o + jj) * kPB, Bl + (size_t)(o + jj) * kPB, &rb[o + jj]);
+    for (int jj = warp; jj < 32; jj += 8)
+        pre_row_pair(&T[jj * 129], Bh + (size_t)(o + j0 + jj) * kPB, Bl + (size_t)(o + j0 + jj) * kPB,
+                     &rb[o + j0 + jj]);
 }
 
 // Forward step k: z_k = P_k y_k (every block forms it from the finished y_k;
@@ -231,7 +206,7 @@ int lu_solve_mixed(int n, const double *dA, size_t lda, double *dx, double tol, 
                    cudaStream_t st)
 {
     const int np = (n + kPB - 1) / kPB * kPB, nb = np / kPB;
-    DevBuf<float> W, P, y, z;
+    DevBuf<float> W, P, PT, y, z;
     DevBuf<__half> gAh, gAl, gBh, gBl;
     DevBuf<float> ra, rb;
     DevBuf<int> bad, err;
@@ -239,12 +214,15 @@ int lu_solve_mixed(int n, const double *dA, size_t lda, double *dx, double tol, 
     DevBuf<unsigned> cnt;
     DSC_TRY(W.alloc((size_t)np * np));
     DSC_TRY(P.alloc((size_t)nb * kPB * kPB));
-    DSC_TRY(gAh.alloc((size_t)np * kPB));
-    DSC_TRY(gAl.alloc((size_t)np * kPB));
-    DSC_TRY(gBh.alloc((size_t)np * kPB));
-    DSC_TRY(gBl.alloc((size_t)np * kPB));
-    DSC_TRY(ra.alloc(np));
-    DSC_TRY(rb.alloc(np));
+    DSC_TRY(PT.alloc((size_t)nb * kPB * kPB));
+    // the update operands: two halves, alternating by the parity of the step
+    const size_t oh = (size_t)np * kPB;
+    DSC_TRY(gAh.alloc(2 * oh));
+    DSC_TRY(gAl.alloc(2 * oh));
+    DSC_TRY(gBh.alloc(2 * oh));
+    DSC_TRY(gBl.alloc(2 * oh));
+    DSC_TRY(ra.alloc(2 * (size_t)np));
+    DSC_TRY(rb.alloc(2 * (size_t)np));
     DSC_TRY(bad.alloc(1));
     DSC_TRY(err.alloc(1));
     DSC_TRY(y.alloc(np));
@@ -272,20 +250,66 @@ int lu_solve_mixed(int n, const double *dA, size_t lda, double *dx, double tol, 
     DSC_LAUNCH(k_lu_load<<<dim3(np / 32, np / 32), dim3(32, 8), 0, st>>>(dA, lda, n, W.p, np));
     DSC_CUDA(cudaGetLastError());
     // ---- factorisation
-    const size_t rsmem = sizeof(float) * (2 * kPB * 129 + kPB * 128);
+    const size_t rsmem = std::max(kGjRowSmem, sizeof(float) * kPB * 129);
     DSC_TRY(raise_smem_limit((const void *)k_lu_row, (int)rsmem));
+    // Step k on a high-priority stream (hp, forked from st): the pivot
+    // inverse and row block k, then (after the rest of step k - 1) the cross
+    // of the trailing matrix's first tile -- the next pivot tile, row block
+    // and column block -- and on a side stream the rest of the trailing
+    // update (after row block k) on all but kGjReserveSms SMs, which step
+    // k + 1's pivot and row block have to themselves.  The operands of step
+    // k + 1 go to the other half of the buffers.
+    struct OwnStream {
+        cudaStream_t s = nullptr;
+        ~OwnStream()
+        {
+            if (s) cudaStreamDestroy(s);
+        }
+    } side, hp;
+    {
+        int least = 0, greatest = 0;
+        DSC_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        DSC_CUDA(cudaStreamCreateWithPriority(&side.s, cudaStreamNonBlocking, least));
+        DSC_CUDA(cudaStreamCreateWithPriority(&hp.s, cudaStreamNonBlocking, greatest));
+    }
+    SideJoin hj;
+    DSC_TRY(hj.fork(st, hp.s));
+    EventPair evs;  // a: row block k is done; b: the rest of the last update is
+    DSC_TRY(evs.create());
+    int nsm = 0;
+    DSC_TRY(current_sm_count(&nsm));
+    const int rest_ctas = std::max(1, nsm - kGjReserveSms);
+    bool rest_pending = false;
     for (int k = 0; k < nb; k++) {
-        DSC_TRY(launch_dependent(k_lu_pivot, dim3(1), dim3(kGjThreads), 0, st, (const float *)W.p, np, k, P.p, bad.p));
+        DSC_TRY(launch_dependent(k_lu_pivot, dim3(1), dim3(kGjThreads), 0, hp.s, (const float *)W.p, np, k, P.p, PT.p,
+                                 bad.p));
         if (k + 1 == nb) break;
         const int rest = nb - k - 1, k1 = (k + 1) * kPB, m = np - k1;
-        DSC_TRY(launch_dependent(k_lu_row, dim3(rest, 2), dim3(256), rsmem, st, W.p, np, k, (const float *)P.p,
-                                 gAh.p, gAl.p, ra.p, gBh.p, gBl.p, rb.p));
+        const size_t h = (size_t)(k & 1);
+        __half *Ah = gAh.p + h * oh, *Al = gAl.p + h * oh, *Bh = gBh.p + h * oh, *Bl = gBl.p + h * oh;
+        float *rah = ra.p + h * np, *rbh = rb.p + h * np;
+        DSC_TRY(launch_dependent(k_lu_row, dim3(rest, 5), dim3(256), rsmem, hp.s, W.p, np, k, (const float *)PT.p,
+                                 Ah, Al, rah, Bh, Bl, rbh));
+        DSC_CUDA(cudaEventRecord(evs.a, hp.s));
+        if (rest_pending) DSC_CUDA(cudaStreamWaitEvent(hp.s, evs.b, 0));
         // W_IJ -= A_I B_J^T on the trailing sub-matrix (no tile excluded)
         TcGjPlan plan;
-        DSC_TRY(tc_gj_plan(plan, gAh.p, gAl.p, kPB, gBh.p, gBl.p, kPB, m, m, W.p + (size_t)k1 * np + k1,
-                           (size_t)np, err.p, ra.p, rb.p));
-        DSC_TRY(tc_gj_run(plan, big, st));
+        DSC_TRY(tc_gj_plan(plan, Ah, Al, kPB, Bh, Bl, kPB, m, m, W.p + (size_t)k1 * np + k1, (size_t)np, err.p,
+                           rah, rbh));
+        if (rest >= 2) {
+            DSC_TRY(tc_gj_run(plan, big, hp.s, 1, 0));
+            DSC_CUDA(cudaStreamWaitEvent(side.s, evs.a, 0));
+            DSC_TRY(tc_gj_run(plan, big, side.s, 2, 0, rest_ctas));
+            DSC_CUDA(cudaEventRecord(evs.b, side.s));
+            rest_pending = true;
+        } else {
+            DSC_TRY(tc_gj_run(plan, big, hp.s));
+            rest_pending = false;
+        }
     }
+    if (rest_pending) DSC_CUDA(cudaStreamWaitEvent(hp.s, evs.b, 0));
+    DSC_TRY(hj.done(hp.s));
+    DSC_TRY(hj.join());
     DSC_CUDA(cudaEventRecord(ev[1], st));
     int hbad = big, herr = 0;
     DSC_CUDA(cudaMemcpyAsync(&hbad, bad.p, sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -136,22 +136,22 @@ __global__ void k_pre_init(const double *__restrict__ K, size_t ld, const double
     X[(size_t)c * ldx + a] = v;
 }
 
-// tP = inverse of the 128 x 128 diagonal block k of each matrix, row-major
-// (Gauss-Jordan without pivoting, one CTA of kGjThreads threads per matrix; see
-// gj_invert_tile).
+// tP = the transposed inverse of the 128 x 128 diagonal block k of each
+// matrix (blocked Gauss-Jordan without pivoting, one CTA of kGjThreads
+// threads per matrix; see gj_invert_tile).
 __global__ void __launch_bounds__(kGjThreads) k_gj_pivot(GJArgs g, int nb, int k)
 {
     grid_dep_wait();  // a programmatic dependent of the previous step's update
     const int b = blockIdx.x;
     if (b >= nb || k >= g.nbk[b]) return;
-    gj_invert_tile(g.X[b] + (size_t)k * kPB * g.ldx[b] + k * kPB, g.ldx[b], g.tP[b], 0.0f, nullptr, 0);
+    gj_invert_tile(g.X[b] + (size_t)k * kPB * g.ldx[b] + k * kPB, g.ldx[b], nullptr, g.tP[b], 0.0f, nullptr, 0);
 }
 
-// Step k, per matrix: blockIdx.y = 0, tile J: R_J = P X_kJ (P itself for
-// J = k) written into row block k of X and, transposed, as the update's B
-// rows; blockIdx.y = 1, tile I != k: the old column block's rows as the
-// update's A rows (zero rows for I = k).  256 threads; the 128 x 128 tile in
-// shared memory ([row][col + 1]).
+// Step k, per matrix (blockIdx.z), tile J = blockIdx.x: blockIdx.y < 4:
+// columns 32 y .. 32 y + 31 of R_J = P X_kJ (P itself for J = k) written
+// into row block k of X and, transposed, as the update's B rows;
+// blockIdx.y = 4: tile I = J of the old column block as the update's A
+// rows (zero rows for I = k).  256 threads.
 __global__ void __launch_bounds__(256) k_gj_row(GJArgs g, int nb, int k)
 {
     grid_dep_wait();  // a programmatic dependent of the pivot inversion
@@ -159,10 +159,9 @@ __global__ void __launch_bounds__(256) k_gj_row(GJArgs g, int nb, int k)
     if (b >= nb || k >= g.nbk[b] || J >= g.nbk[b]) return;
     float *X = g.X[b];
     const int ldx = g.ldx[b];
-    extern __shared__ float sm[];
-    float(*T)[129] = (float(*)[129])sm;  // T[r][c]
+    extern __shared__ __align__(16) float sm[];
     const int warp = threadIdx.x >> 5;
-    if (blockIdx.y == 1) {
+    if (blockIdx.y == 4) {
         // A rows: row i of tile J of column block k, A[i][kk] = X(J*128 + i, k*128 + kk)
         __half *Ah = g.Ah[b] + (size_t)J * kPB * kPB, *Al = g.Al[b] + (size_t)J * kPB * kPB;
         if (J == k) {
@@ -173,55 +172,34 @@ __global__ void __launch_bounds__(256) k_gj_row(GJArgs g, int nb, int k)
             if (threadIdx.x < kPB) g.ra[b][J * kPB + threadIdx.x] = 1.0f;
             return;
         }
-        load_tile128(X + (size_t)k * kPB * ldx + J * kPB, (size_t)ldx, [&](int kk, int i, float v) { T[i][kk] = v; });
-        __syncthreads();
+        gj_load_rows(X + (size_t)k * kPB * ldx + J * kPB, (size_t)ldx, sm);
         for (int i = warp; i < kPB; i += 8)
-            pre_row_pair(&T[i][0], Ah + (size_t)i * kPB, Al + (size_t)i * kPB, &g.ra[b][J * kPB + i]);
+            pre_row_pair(&sm[i * 129], Ah + (size_t)i * kPB, Al + (size_t)i * kPB, &g.ra[b][J * kPB + i]);
         return;
     }
-    // R_J[kk][j] = sum_q P[kk][q] X(k*128 + q, J*128 + j); T[j][kk] = R_J[kk][j]
-    const float *P = g.tP[b];
+    const int j0 = 32 * blockIdx.y;
+    const float *PT = g.tP[b];
+    const float *T;
     if (J == k) {
-        load_tile128(P, kPB, [&](int kk, int j, float v) { T[j][kk] = v; });
-    } else {
-        float(*Pt)[128] = (float(*)[128])(sm + kPB * 129);       // Pt[q][kk] = P[kk][q]
-        float(*Xs)[129] = (float(*)[129])(sm + kPB * 129 + kPB * 128);  // Xs[j][q] = X(k*128 + q, J*128 + j)
-        load_tile128(P, kPB, [&](int r, int c, float v) { Pt[c][r] = v; });
-        load_tile128(X + (size_t)J * kPB * ldx + k * kPB, (size_t)ldx, [&](int r, int c, float v) { Xs[r][c] = v; });
-        __syncthreads();
-        // thread (ty, tx): kk = 8 ty + u, j = tx + 16 v (u, v < 8)
-        const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
-        float acc[8][8];
-#pragma unroll
-        for (int u = 0; u < 8; u++)
-#pragma unroll
-            for (int v = 0; v < 8; v++) acc[u][v] = 0.0f;
-#pragma unroll 4
-        for (int q = 0; q < kPB; q++) {
-            const float4 p0 = *(const float4 *)&Pt[q][8 * ty], p1 = *(const float4 *)&Pt[q][8 * ty + 4];
-            const float pa[8] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w};
-            float xb[8];
-#pragma unroll
-            for (int v = 0; v < 8; v++) xb[v] = Xs[tx + 16 * v][q];
-#pragma unroll
-            for (int u = 0; u < 8; u++)
-#pragma unroll
-                for (int v = 0; v < 8; v++) acc[u][v] = fmaf(pa[u], xb[v], acc[u][v]);
+        // R_k = P: T[jj][kk] = P(kk, j0 + jj) = PT[(j0 + jj) * 128 + kk]
+        for (int t = threadIdx.x; t < 32 * kPB; t += blockDim.x) {
+            const int jj = t >> 7, kk = t & 127;
+            sm[jj * 129 + kk] = PT[(size_t)(j0 + jj) * kPB + kk];
         }
-#pragma unroll
-        for (int u = 0; u < 8; u++)
-#pragma unroll
-            for (int v = 0; v < 8; v++) T[tx + 16 * v][8 * ty + u] = acc[u][v];
+        __syncthreads();
+        T = sm;
+    } else {
+        T = gj_row_product(PT, X + (size_t)J * kPB * ldx + k * kPB, (size_t)ldx, j0, sm);
     }
-    __syncthreads();
-    // row block k of X takes R_J (P for J = k): X(k*128 + kk, J*128 + j)
-    for (int t = threadIdx.x; t < kPB * kPB; t += blockDim.x) {
-        const int j = t >> 7, kk = t & 127;
-        X[(size_t)(J * kPB + j) * ldx + k * kPB + kk] = T[j][kk];
+    // row block k of X takes R_J: X(k*128 + kk, J*128 + j)
+    for (int t = threadIdx.x; t < 32 * kPB; t += blockDim.x) {
+        const int jj = t >> 7, kk = t & 127;
+        X[(size_t)(J * kPB + j0 + jj) * ldx + k * kPB + kk] = T[jj * 129 + kk];
     }
     __half *Bh = g.Bh[b] + (size_t)J * kPB * kPB, *Bl = g.Bl[b] + (size_t)J * kPB * kPB;
-    for (int jj = warp; jj < kPB; jj += 8)
-        pre_row_pair(&T[jj][0], Bh + (size_t)jj * kPB, Bl + (size_t)jj * kPB, &g.rb[b][J * kPB + jj]);
+    for (int jj = warp; jj < 32; jj += 8)
+        pre_row_pair(&T[jj * 129], Bh + (size_t)(j0 + jj) * kPB, Bl + (size_t)(j0 + jj) * kPB,
+                     &g.rb[b][J * kPB + j0 + jj]);
 }
 
 // *bound = max(*bound, largest row sum of |Xt| over the first n rows and
@@ -262,12 +240,12 @@ int precond_build(Session &s, cudaStream_t main, cudaStream_t aux)
     DSC_TRY(pc.Xl.alloc(xtot));
     DSC_TRY(pc.rs.alloc(pc.noff.back() + pc.n.back()));
     DSC_TRY(pc.tP.alloc((size_t)kPreMaxBlocks * kPB * kPB));
-    DSC_TRY(pc.gAh.alloc(ttot));
-    DSC_TRY(pc.gAl.alloc(ttot));
-    DSC_TRY(pc.gBh.alloc(ttot));
-    DSC_TRY(pc.gBl.alloc(ttot));
-    DSC_TRY(pc.gra.alloc(ttot / kPB));
-    DSC_TRY(pc.grb.alloc(ttot / kPB));
+    DSC_TRY(pc.gAh.alloc(2 * ttot));  // two halves: see the step loop
+    DSC_TRY(pc.gAl.alloc(2 * ttot));
+    DSC_TRY(pc.gBh.alloc(2 * ttot));
+    DSC_TRY(pc.gBl.alloc(2 * ttot));
+    DSC_TRY(pc.gra.alloc(2 * ttot / kPB));
+    DSC_TRY(pc.grb.alloc(2 * ttot / kPB));
     DSC_TRY(pc.err.alloc(1));
     DSC_CUDA(cudaMemsetAsync(pc.err.p, 0, sizeof(int), st));
     double flops = 0.0;
@@ -277,7 +255,7 @@ int precond_build(Session &s, cudaStream_t main, cudaStream_t aux)
                                                  pc.X.p + pc.xoff[b], pc.ldx[b]));
         flops += 2.0 * pc.ldx[b] * (double)pc.ldx[b] * pc.ldx[b];
     }
-    const size_t rsmem = sizeof(float) * (2 * kPB * 129 + kPB * 128);
+    const size_t rsmem = std::max(kGjRowSmem, sizeof(float) * kPB * 129);
     DSC_CUDA(cudaFuncSetAttribute(k_gj_row, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem));
     for (int b0 = 0; b0 < pc.nb; b0 += kPreMaxBlocks) {
         const int nb = std::min(kPreMaxBlocks, pc.nb - b0);
@@ -295,49 +273,66 @@ int precond_build(Session &s, cudaStream_t main, cudaStream_t aux)
             ga.ldx[q] = pc.ldx[b];
             ga.nbk[q] = pc.nbk[b];
         }
-        std::vector<TcGjPlan> plans(nb);
-        for (int q = 0; q < nb; q++)
-            DSC_TRY(tc_gj_plan(plans[q], ga.Ah[q], ga.Al[q], kPB, ga.Bh[q], ga.Bl[q], kPB, ga.ldx[q], ga.ldx[q],
-                               ga.X[q], (size_t)ga.ldx[q], pc.err.p, ga.ra[q], ga.rb[q]));
-        // two interleaved Gauss-Jordan sequences when there are two or more
-        // blocks: even blocks on st, odd ones on the side stream, so that one
-        // sequence's pivot inversion (one CTA) runs beside the other's
-        // tensor-core update
-        const int nseq = (nb >= 2 && side) ? 2 : 1;
-        GJArgs gsub[2] = {};
-        int nsub[2] = {0, 0}, nbk_sub[2] = {0, 0};
-        std::vector<int> which[2];
+        // the update operands alternate between two halves of the buffers
+        // by the parity of the step (the rest of step k is still reading
+        // its half while step k + 1's row blocks are formed)
+        GJArgs gp[2] = {ga, ga};
         for (int q = 0; q < nb; q++) {
-            const int t = q % nseq, i = nsub[t]++;
-            gsub[t].X[i] = ga.X[q];
-            gsub[t].tP[i] = ga.tP[q];
-            gsub[t].Ah[i] = ga.Ah[q];
-            gsub[t].Al[i] = ga.Al[q];
-            gsub[t].Bh[i] = ga.Bh[q];
-            gsub[t].Bl[i] = ga.Bl[q];
-            gsub[t].ra[i] = ga.ra[q];
-            gsub[t].rb[i] = ga.rb[q];
-            gsub[t].ldx[i] = ga.ldx[q];
-            gsub[t].nbk[i] = ga.nbk[q];
-            nbk_sub[t] = std::max(nbk_sub[t], ga.nbk[q]);
-            which[t].push_back(q);
+            const size_t o = ttot;
+            gp[1].Ah[q] += o;
+            gp[1].Al[q] += o;
+            gp[1].Bh[q] += o;
+            gp[1].Bl[q] += o;
+            gp[1].ra[q] += o / kPB;
+            gp[1].rb[q] += o / kPB;
         }
-        SideJoin sj;
-        if (nseq == 2) DSC_TRY(sj.fork(st, side));
-        for (int t = 0; t < nseq; t++) {
-            cudaStream_t ss = t ? side : st;
-            for (int k = 0; k < nbk_sub[t]; k++) {
-                DSC_TRY(launch_dependent(k_gj_pivot, dim3(nsub[t]), dim3(kGjThreads), 0, ss, gsub[t], nsub[t], k));
-                DSC_TRY(launch_dependent(k_gj_row, dim3(nbk_sub[t], 2, nsub[t]), dim3(256), rsmem, ss, gsub[t],
-                                         nsub[t], k));
-                for (int q : which[t])
-                    if (k < ga.nbk[q]) DSC_TRY(tc_gj_run(plans[q], k, ss));
+        int nbk_max = 0;
+        for (int q = 0; q < nb; q++) nbk_max = std::max(nbk_max, ga.nbk[q]);
+        std::vector<TcGjPlan> plans(2 * (size_t)nb);
+        for (int h = 0; h < 2; h++)
+            for (int q = 0; q < nb; q++)
+                DSC_TRY(tc_gj_plan(plans[2 * q + h], gp[h].Ah[q], gp[h].Al[q], kPB, gp[h].Bh[q], gp[h].Bl[q], kPB,
+                                   ga.ldx[q], ga.ldx[q], ga.X[q], (size_t)ga.ldx[q], pc.err.p, gp[h].ra[q],
+                                   gp[h].rb[q]));
+        // Step k on st: the pivot inverses and row blocks of every block,
+        // then (after the rest of step k - 1) the cross of tile k + 1 of the
+        // update -- the next pivot tile, row block and column block -- and
+        // on the side stream the rest of the update (after step k's row
+        // blocks), on all but kGjReserveSms SMs, which step k + 1's pivots
+        // and row blocks have to themselves.  A block's last step updates
+        // everything on st.  Without a side stream every update is whole.
+        const bool la = side != nullptr;
+        EventPair ev;  // a: step k's row blocks are done; b: the rest of the last step is
+        if (la) DSC_TRY(ev.create());
+        int nsm = 0;
+        DSC_TRY(current_sm_count(&nsm));
+        const int rest_ctas = std::max(1, nsm - kGjReserveSms);
+        bool rest_pending = false;
+        for (int k = 0; k < nbk_max; k++) {
+            const GJArgs &g = gp[k & 1];
+            DSC_TRY(launch_dependent(k_gj_pivot, dim3(nb), dim3(kGjThreads), 0, st, g, nb, k));
+            DSC_TRY(launch_dependent(k_gj_row, dim3(nbk_max, 5, nb), dim3(256), rsmem, st, g, nb, k));
+            if (la) {
+                DSC_CUDA(cudaEventRecord(ev.a, st));
+                if (rest_pending) DSC_CUDA(cudaStreamWaitEvent(st, ev.b, 0));
             }
+            bool any_rest = false;
+            for (int q = 0; q < nb; q++) {
+                if (k >= ga.nbk[q]) continue;
+                const TcGjPlan &pl = plans[2 * q + (k & 1)];
+                if (la && k + 1 < ga.nbk[q]) {
+                    DSC_TRY(tc_gj_run(pl, k, st, 1, k + 1));
+                    if (!any_rest) DSC_CUDA(cudaStreamWaitEvent(side, ev.a, 0));
+                    DSC_TRY(tc_gj_run(pl, k, side, 2, k + 1, rest_ctas));
+                    any_rest = true;
+                } else {
+                    DSC_TRY(tc_gj_run(pl, k, st));
+                }
+            }
+            if (any_rest) DSC_CUDA(cudaEventRecord(ev.b, side));
+            rest_pending = any_rest;
         }
-        if (nseq == 2) {
-            DSC_TRY(sj.done(side));
-            DSC_TRY(sj.join());
-        }
+        if (rest_pending) DSC_CUDA(cudaStreamWaitEvent(st, ev.b, 0));
     }
     // the inverses as row-scaled fp16 pairs for the products (X is
     // column-major: its transpose's rows are X's columns; the products take

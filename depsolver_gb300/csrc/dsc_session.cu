@@ -94,7 +94,13 @@ int Session::create(int nen_, unsigned N_, unsigned E_, const double *nodes, con
     nIf = nIf_;
     DSC_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     DSC_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
-    DSC_CUDA(cudaStreamCreateWithFlags(&side2, cudaStreamNonBlocking));
+    {
+        // side2 runs the conductor-block inverses' chain of small dependent
+        // kernels: it goes first whenever SMs free up
+        int least = 0, greatest = 0;
+        DSC_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        DSC_CUDA(cudaStreamCreateWithPriority(&side2, cudaStreamNonBlocking, greatest));
+    }
     AllocStreamScope as(st);
     std::vector<int> e0((size_t)E * nen);
     for (size_t t = 0; t < e0.size(); t++) e0[t] = (int)elems[t] - 1;

@@ -126,6 +126,50 @@ __device__ __forceinline__ float tf32_lo_biased(float s)
 // products out of the main accumulator: the tensor core's FP32 accumulation
 // truncates (sums of positive products come out low), so every MMA added
 // into an accumulator costs up to one of its units in the last place.
+// Row and column tile of unit u.  Every product but the Gauss-Jordan
+// update with sel != 0: row tile u % tiles, column tile (u / tiles) % ntn.
+// The update with sel = 1 takes the cross of tile la: row tile la with every
+// column tile (u < ntn), then column tile la with every row tile other than
+// la and gk; with sel = 2 every other tile (row tiles other than la and gk,
+// column tiles other than la).  A gk outside [0, tiles) excludes nothing.
+// Together sel 1 and sel 2 cover the tiles of sel 0 but row tile gk (which
+// the update leaves alone).
+__device__ __forceinline__ void unit_tile(int u, int tiles, int ntn, int sel, int la, int gk, int &tm, int &tn)
+{
+    if (sel == 0) {
+        tm = u % tiles;
+        tn = (u / tiles) % ntn;
+        return;
+    }
+    const bool gv = gk >= 0 && gk < tiles && gk != la;
+    const int e1 = gv ? min(la, gk) : la, e2 = gv ? max(la, gk) : 0x7FFFFFFF;
+    if (sel == 1 && u < ntn) {
+        tm = la;
+        tn = u;
+        return;
+    }
+    const int nr = tiles - 1 - (gv ? 1 : 0);
+    int i = sel == 1 ? u - ntn : u % nr;  // the i-th row tile other than e1, e2
+    if (i >= e1) i++;
+    if (i >= e2) i++;
+    tm = i;
+    if (sel == 1) {
+        tn = la;
+    } else {
+        const int c = u / nr;
+        tn = c >= la ? c + 1 : c;
+    }
+}
+
+// Units of the update's tile selection sel (see unit_tile).
+__host__ __device__ inline int gj_sel_units(int tiles, int ntn, int sel, int la, int gk)
+{
+    if (sel == 0) return tiles * ntn;
+    const bool gv = gk >= 0 && gk < tiles && gk != la;
+    const int nr = tiles - 1 - (gv ? 1 : 0);
+    return sel == 1 ? ntn + nr : nr * (ntn - 1);
+}
+
 template <int AMODE, bool GJ = false>
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_tc_gemm3(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
@@ -133,7 +177,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                int M, int Nc, int BN, int ntn, int nkb_total, int kb_per_split, int nsplit,
                float *__restrict__ Y, size_t ldy, size_t split_stride, int tmem_cols,
                uint32_t acc_stride, const float *__restrict__ rsc, const float *__restrict__ csc,
-               int gj_k, int *err)
+               int gj_k, int gj_sel, int gj_la, int *err)
 {
     grid_dep_wait();  // launched as a programmatic dependent of the kernel before
     // ntn: column tiles of BN columns (1 unless the product is the
@@ -164,7 +208,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     uint32_t *tmem_slot = (uint32_t *)(done + 1);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int tiles = (M + kTcBM - 1) / kTcBM;
-    const int units = tiles * ntn * nsplit;  // unit u: row tile u % tiles, then column tile, then split
+    // unit u: row tile u % tiles, then column tile, then split (the
+    // Gauss-Jordan update: one split, tiles by unit_tile)
+    const int units = GJ && gj_sel ? gj_sel_units(tiles, ntn, gj_sel, gj_la, gj_k) : tiles * ntn * nsplit;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < kTcStages; s++) {
@@ -201,8 +247,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             uint32_t g = 0;
             bool ok = true;
             for (int u = blockIdx.x; ok && u < units; u += gridDim.x) {
-                const int m0 = (u % tiles) * kTcBM, n0 = ((u / tiles) % ntn) * BN;
-                const int kb0 = (u / tiles / ntn) * kb_per_split;
+                int tmu, tnu;
+                unit_tile(u, tiles, ntn, GJ ? gj_sel : 0, gj_la, gj_k, tmu, tnu);
+                const int m0 = tmu * kTcBM, n0 = tnu * BN;
+                const int kb0 = GJ ? 0 : (u / tiles / ntn) * kb_per_split;
                 const int nkb = min(nkb_total, kb0 + kb_per_split) - kb0;
                 for (int i = 0; i < nkb; i++, g++) {
                     const uint32_t s = g % kTcStages, n = g / kTcStages;
@@ -241,7 +289,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             bool ok = true;
             int j = 0;
             for (int u = blockIdx.x; ok && u < units; u += gridDim.x, j++) {
-                const int kb0 = (u / tiles / ntn) * kb_per_split;
+                const int kb0 = GJ ? 0 : (u / tiles / ntn) * kb_per_split;
                 const int nkb = min(nkb_total, kb0 + kb_per_split) - kb0;
                 const uint32_t buf = j % nbuf, q = j / nbuf;
                 if (q > 0 && !mbar_wait(&acc_empty[buf], (q - 1) & 1, err, 5)) break;
@@ -351,13 +399,34 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         const int cend = GJ && warp < 2 + kTcSplitWarps ? BN / 2 : BN;
         int j = 0;
         for (int u = blockIdx.x; u < units; u += gridDim.x, j++) {
-            const int tm = u % tiles, tn = (u / tiles) % ntn, split = u / tiles / ntn;
+            int tm, tn;
+            unit_tile(u, tiles, ntn, GJ ? gj_sel : 0, gj_la, gj_k, tm, tn);
+            const int split = GJ ? 0 : u / tiles / ntn;
             const int m0 = tm * kTcBM, n0 = tn * BN;
             const uint32_t buf = j % nbuf, q = j / nbuf;
             bool have = mbar_wait(&acc_full[buf], q & 1, err, 3);
             // tcgen05.ld is warp-collective: the whole warp reads or none of it
             if (!__all_sync(0xffffffffu, have)) break;
             tc_fence_after();
+            if (GJ) {
+                // the old values of this warp's rows and columns of the next
+                // unit (and, before the first, of this one) into L2 while
+                // the accumulator is formed or written back: lane t asks for
+                // column cbeg + t (and + 32), 32 rows (128 bytes) each
+                for (int u2 = j ? u + gridDim.x : u; u2 <= u + (int)gridDim.x && u2 < units; u2 += gridDim.x) {
+                    int tm2, tn2;
+                    unit_tile(u2, tiles, ntn, gj_sel, gj_la, gj_k, tm2, tn2);
+                    const int r0 = tm2 * kTcBM + ew * 32;
+                    if (tm2 != gj_k && tn2 != gj_k && r0 < M) {
+#pragma unroll
+                        for (int h = 0; h < 64; h += 32) {
+                            const int n = tn2 * BN + cbeg + h + lane;
+                            if (cbeg + h + lane < cend && n < Nc)
+                                asm volatile("prefetch.global.L2 [%0];" ::"l"(Y + (size_t)n * ldy + r0));
+                        }
+                    }
+                }
+            }
             const uint32_t acc = tmem + ((uint32_t)(ew * 32) << 16) + buf * acc_stride;
             const int m = m0 + ew * 32 + lane;
             const float rs = (rsc && m < M) ? rsc[m] : 1.0f;
@@ -503,7 +572,8 @@ static int splits_for_bk(int M, int Kd, int bk)
 // Launch of the persistent kernel on encoded maps (bk: elements per k-block).
 static int tc_launch(int amode, const CUtensorMap &ah, const CUtensorMap &al, const CUtensorMap &bh,
                      const CUtensorMap &bl, int M, int Nc, int Kd, int bk, float *Y, size_t ldy, int splits,
-                     int *d_err, cudaStream_t st, const float *rsc, const float *csc, int gj_k = -1)
+                     int *d_err, cudaStream_t st, const float *rsc, const float *csc, int gj_k = -1,
+                     int gj_sel = 0, int gj_la = 0, int max_ctas = 0)
 {
     // one column tile of all Nc columns, or tiles of 128 (the Gauss-Jordan
     // update); above 256 columns (digits) a multiple of 32 (two halves)
@@ -523,15 +593,19 @@ static int tc_launch(int amode, const CUtensorMap &ah, const CUtensorMap &al, co
     // persistent: one CTA per SM walks the (row tile, split) units
     int nsm = 0;
     DSC_TRY(current_sm_count(&nsm));
-    const int units = (M + kTcBM - 1) / kTcBM * ntn * splits;
-    const dim3 grid(std::min(units, nsm));
+    const int units = gj_k >= 0 && gj_sel ? gj_sel_units((M + kTcBM - 1) / kTcBM, ntn, gj_sel, gj_la, gj_k)
+                                          : (M + kTcBM - 1) / kTcBM * ntn * splits;
+    if (units < 1) return kOk;
+    // max_ctas > 0: at most that many CTAs (SMs left for other streams)
+    const dim3 grid(std::min(units, max_ctas > 0 ? std::min(max_ctas, nsm) : nsm));
     // the shared-memory limit of each instantiation is raised to the largest
     // request seen on the device (once per size, not per launch)
     auto launch = [&](auto kern, int slot) -> int {
         (void)slot;
         DSC_TRY(raise_smem_limit((const void *)kern, (int)smem));
         DSC_TRY(launch_dependent(kern, grid, dim3(kTcThreads), smem, st, ah, al, bh, bl, M, Nc, BN, ntn, nkb, kps,
-                                 splits, Y, ldy, ldy * (size_t)Nc, tmem_cols, acc_stride, rsc, csc, gj_k, d_err));
+                                 splits, Y, ldy, ldy * (size_t)Nc, tmem_cols, acc_stride, rsc, csc, gj_k, gj_sel,
+                                 gj_la, d_err));
         return kOk;
     };
     if (gj_k >= 0) DSC_TRY(launch(k_tc_gemm3<3, true>, 4));
@@ -633,14 +707,19 @@ int tc_gj_plan(TcGjPlan &p, const __half *Ah, const __half *Al, size_t lda, cons
     return kOk;
 }
 
-int tc_gj_run(const TcGjPlan &p, int k, cudaStream_t st)
+int tc_gj_run(const TcGjPlan &p, int k, cudaStream_t st, int sel, int la, int max_ctas)
 {
-    if (!p.maps || k < 0) {
-        set_error("tc_gj_run: no plan or negative step");
+    if (!p.maps || k < 0 || sel < 0 || sel > 2) {
+        set_error("tc_gj_run: no plan, negative step or bad tile selection");
+        return kErrArg;
+    }
+    const int tiles = (p.M + kTcBM - 1) / kTcBM, ntn = (p.Nc + 127) / 128;
+    if (sel && (la < 0 || la >= tiles || la >= ntn || la == k)) {
+        set_error("tc_gj_run: look-ahead tile %d outside the update", la);
         return kErrArg;
     }
     return tc_launch(3, p.maps->ah, p.maps->al, p.maps->bh, p.maps->bl, p.M, p.Nc, 128, kTcBK16, p.C, p.ldc, 1,
-                     p.err, st, p.rsc, p.csc, k);
+                     p.err, st, p.rsc, p.csc, k, sel, la, max_ctas);
 }
 
 int tc_gemm_splits_for(int M, int Kd) { return splits_for_bk(M, Kd, kTcBK); }

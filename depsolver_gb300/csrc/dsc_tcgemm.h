@@ -85,7 +85,13 @@ struct TcGjPlan {
 int tc_gj_plan(TcGjPlan &p, const __half *Ah, const __half *Al, size_t lda, const __half *Bh,
                const __half *Bl, size_t ldb, int M, int Nc, float *C, size_t ldc, int *d_err,
                const float *rsc, const float *csc);
-int tc_gj_run(const TcGjPlan &p, int k, cudaStream_t st);
+// sel = 0: every tile of the update; sel = 1: only the cross of tile la
+// (row tile la and column tile la, la != k), sel = 2: every other tile --
+// so that the next step's pivot tile, row block and column block (la = k +
+// 1) can be ready while the rest is updated.  max_ctas > 0 sets the
+// persistent grid (below the SM count: SMs left for kernels of other
+// streams).
+int tc_gj_run(const TcGjPlan &p, int k, cudaStream_t st, int sel = 0, int la = 0, int max_ctas = 0);
 // Row scales of column-major FP64 K (stride ld): rowE (N ints) the biased
 // exponent of each row's largest entry, rsK = 2^-s_i.
 int k16_row_scales(const double *K, size_t ld, int N, int *rowE, float *rsK, cudaStream_t st);

@@ -22,7 +22,8 @@ def test_mixed_lu_matches_fp64_lu_and_checker(gpu, port, nen):
     x64 = api.gauss_bksb(Af, Bf, mode=api.GAUSS_FP64)
     xm = api.gauss_bksb(Af, Bf, mode=api.GAUSS_MIXED)
     mode, it, rr, fb = api.gauss_info()
-    assert mode == api.GAUSS_MIXED and not fb and 1 <= it <= 30, (it, rr, fb)
+    # an FP32-accurate factor needs a few refinements, not tens
+    assert mode == api.GAUSS_MIXED and not fb and 1 <= it <= 5, (it, rr, fb)
     assert relerr(xm, x64) < 1e-11
     assert relerr(xm, port.gauss(Af, Bf)) < 1e-11
 
@@ -35,7 +36,7 @@ def test_mixed_lu_at_config0_full_form(gpu):
     Af, Bf = api.electric_form(sc, full=True)
     xm = api.gauss_bksb(Af, Bf, mode=api.GAUSS_MIXED)
     _, it, rr, fb = api.gauss_info()
-    assert not fb, (it, rr)
+    assert not fb and it <= 5, (it, rr)
     assert relerr(xm, g["x_gauss"]) < 1e-10
     assert rr < 1e-12
 
