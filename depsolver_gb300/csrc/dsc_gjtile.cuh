@@ -64,102 +64,152 @@ __device__ __forceinline__ void pre_row_pair(const float *v, __half *h, __half *
 }
 
 // Threads of the CTA that inverts one tile (gj_invert_tile).
-constexpr int kGjThreads = 1024;
-// P (row-major, 128 x 128) and PT (its transpose, row-major), each when not
-// null, = inverse of the tile at T (column-major: element (r, c) at
-// T[c * ldt + r], 16-byte aligned columns) by Gauss-Jordan without
-// pivoting, four pivots per block barrier, in one CTA of kGjThreads
-// threads.  Warp w holds rows 4w .. 4w+3, lane l columns 4l .. 4l+3 of
-// them: 16 values in registers.  Step m takes pivots 4m .. 4m+3, whose rows
-// are warp m's and whose columns are lane m's: warp m first eliminates
-// them among its own four rows (per pivot: the pivot from lane m, its row
-// scaled with the pivot's own entry replaced by 1, the other three rows
-// updated with their entries of the pivot column read from lane m and
-// replaced by 0 there), which leaves those rows final for the step, and
-// publishes them in shared memory; after one barrier every other warp reads
-// its rows' entries in the four pivot columns from lane m (where they are
-// then replaced by 0) and takes the rank-4 update a_ic -= sum_q a_iq r_qc.
-// The published rows alternate between two buffers by the parity of m.
-// With bad not null, a pivot whose magnitude is at most tol sets *bad to
-// row0 + its row (the lowest such row wins) and the inversion goes on.
-template <int S>
-__device__ __forceinline__ void gj_own_pivot(float (&a)[4][4], int m, float tol, int *bad, int row0)
+constexpr int kGjThreads = 512;
+
+// 1 / x to within an ulp (the pivots of the FP32 factors and inverses,
+// which iterative refinement or the Krylov solver correct).
+__device__ __forceinline__ float gj_rcp(float x)
 {
-    const int l = threadIdx.x & 31;
-    const float pv = __shfl_sync(0xffffffffu, a[S][S], m);
-    if (bad && l == 0 && !(fabsf(pv) > tol)) atomicMin(bad, row0 + 4 * m + S);
-    const float inv = __frcp_rn(pv);
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// One pivot of warp m's elimination among its own eight rows: pivot
+// 8 m + S, whose column is slot S & 3 of lane 2 m + (S >> 2).  The pivot
+// comes from that lane; every lane scales its entries of row S (the pivot's
+// own entry replaced by 1) and takes, for each other row r, a_rc -= a_rS r_c
+// with a_rS read from that lane (and replaced by 0 there).
+template <int S>
+__device__ __forceinline__ void gj_own_pivot8(float (&a)[8][4], int m, float tol, int *bad, int row0)
+{
+    constexpr int C = S & 3;
+    const int l = threadIdx.x & 31, L = 2 * m + (S >> 2);
+    const float pv = __shfl_sync(0xffffffffu, a[S][C], L);
+    if (bad && l == 0 && !(fabsf(pv) > tol)) atomicMin(bad, row0 + 8 * m + S);
+    const float inv = gj_rcp(pv);
 #pragma unroll
-    for (int c = 0; c < 4; c++) a[S][c] = (c == S && l == m ? 1.0f : a[S][c]) * inv;
+    for (int c = 0; c < 4; c++) a[S][c] = (c == C && l == L ? 1.0f : a[S][c]) * inv;
 #pragma unroll
-    for (int r = 0; r < 4; r++) {
+    for (int r = 0; r < 8; r++) {
         if (r == S) continue;
-        const float f = __shfl_sync(0xffffffffu, a[r][S], m);
-        if (l == m) a[r][S] = 0.0f;
+        const float f = __shfl_sync(0xffffffffu, a[r][C], L);
+        if (l == L) a[r][C] = 0.0f;
 #pragma unroll
         for (int c = 0; c < 4; c++) a[r][c] = fmaf(-f, a[S][c], a[r][c]);
     }
 }
 
+// P (row-major, 128 x 128) and PT (its transpose, row-major), each when not
+// null, = inverse of the tile at T (column-major: element (r, c) at
+// T[c * ldt + r], 16-byte aligned columns) by Gauss-Jordan without
+// pivoting, eight pivots per block barrier, in one CTA of kGjThreads
+// threads.  Warp w holds rows 8w .. 8w+7, lane l columns 4l .. 4l+3 of
+// them: 32 values in registers.  Step m takes pivots 8m .. 8m+7, whose rows
+// are warp m's and whose columns are lanes 2m and 2m+1's: warp m eliminates
+// them among its own rows (gj_own_pivot8), which leaves those rows final
+// for the step, and publishes them in shared memory; after one barrier
+// every other warp takes the rank-8 update a_ic -= sum_q a_iq r_qc, its
+// entries a_iq in the pivot columns read from shared memory (staged there
+// by lanes 2m and 2m+1 at the end of the step before) and replaced by 0
+// first.  The published rows alternate between two buffers by the parity
+// of m.  With bad not null, a pivot whose magnitude is at most tol sets
+// *bad to row0 + its row (the lowest such row wins) and the inversion goes
+// on.
 __device__ __forceinline__ void gj_invert_tile(const float *__restrict__ T, int ldt, float *__restrict__ P,
                                                float *__restrict__ PT, float tol, int *bad, int row0)
 {
-    __shared__ __align__(16) float prow[2][4][kPB];
+    constexpr int kW = kGjThreads / 32;                  // 16 warps of 8 rows
+    __shared__ __align__(16) float prow[2][8][kPB];     // the published rows
+    __shared__ __align__(16) float fsl[kW][8][8];       // per warp: its rows' entries in the step's pivot columns
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    float a[4][4];  // a[r][c] = A(4 w + r, 4 l + c)
+    float a[8][4];  // a[r][c] = A(8 w + r, 4 l + c)
 #pragma unroll
     for (int c = 0; c < 4; c++) {
-        const float4 v = *(const float4 *)(T + (size_t)(4 * l + c) * ldt + 4 * w);
-        a[0][c] = v.x;
-        a[1][c] = v.y;
-        a[2][c] = v.z;
-        a[3][c] = v.w;
+        const float4 v0 = *(const float4 *)(T + (size_t)(4 * l + c) * ldt + 8 * w);
+        const float4 v1 = *(const float4 *)(T + (size_t)(4 * l + c) * ldt + 8 * w + 4);
+        a[0][c] = v0.x;
+        a[1][c] = v0.y;
+        a[2][c] = v0.z;
+        a[3][c] = v0.w;
+        a[4][c] = v1.x;
+        a[5][c] = v1.y;
+        a[6][c] = v1.z;
+        a[7][c] = v1.w;
+    }
+    // step 0's pivot columns are lanes 0 and 1's
+    if ((l >> 1) == 0) {
+#pragma unroll
+        for (int r = 0; r < 8; r++)
+            *(float4 *)&fsl[w][r][4 * (l & 1)] = make_float4(a[r][0], a[r][1], a[r][2], a[r][3]);
     }
 #pragma unroll 1
-    for (int m = 0; m < kPB / 4; m++) {
+    for (int m = 0; m < kW; m++) {
         float(*pr)[kPB] = prow[m & 1];
         if (w == m) {
-            gj_own_pivot<0>(a, m, tol, bad, row0);
-            gj_own_pivot<1>(a, m, tol, bad, row0);
-            gj_own_pivot<2>(a, m, tol, bad, row0);
-            gj_own_pivot<3>(a, m, tol, bad, row0);
+            gj_own_pivot8<0>(a, m, tol, bad, row0);
+            gj_own_pivot8<1>(a, m, tol, bad, row0);
+            gj_own_pivot8<2>(a, m, tol, bad, row0);
+            gj_own_pivot8<3>(a, m, tol, bad, row0);
+            gj_own_pivot8<4>(a, m, tol, bad, row0);
+            gj_own_pivot8<5>(a, m, tol, bad, row0);
+            gj_own_pivot8<6>(a, m, tol, bad, row0);
+            gj_own_pivot8<7>(a, m, tol, bad, row0);
 #pragma unroll
-            for (int r = 0; r < 4; r++)
+            for (int r = 0; r < 8; r++)
                 *(float4 *)&pr[r][4 * l] = make_float4(a[r][0], a[r][1], a[r][2], a[r][3]);
         }
         __syncthreads();
         if (w != m) {
-            float f[4][4];  // f[r][q] = A(4 w + r, 4 m + q) before the step
+            if ((l >> 1) == m) {
 #pragma unroll
-            for (int r = 0; r < 4; r++)
+                for (int r = 0; r < 8; r++)
 #pragma unroll
-                for (int q = 0; q < 4; q++) f[r][q] = __shfl_sync(0xffffffffu, a[r][q], m);
-            if (l == m) {
-#pragma unroll
-                for (int r = 0; r < 4; r++)
-#pragma unroll
-                    for (int q = 0; q < 4; q++) a[r][q] = 0.0f;
+                    for (int c = 0; c < 4; c++) a[r][c] = 0.0f;
             }
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const float4 x = *(const float4 *)&pr[q][4 * l];
-                const float xv[4] = {x.x, x.y, x.z, x.w};
+            for (int hq = 0; hq < 2; hq++) {
+                float F[8][4];  // F[r][q] = A(8 w + r, 8 m + 4 hq + q) before the step
 #pragma unroll
-                for (int r = 0; r < 4; r++)
+                for (int r = 0; r < 8; r++) {
+                    const float4 v = *(const float4 *)&fsl[w][r][4 * hq];
+                    F[r][0] = v.x;
+                    F[r][1] = v.y;
+                    F[r][2] = v.z;
+                    F[r][3] = v.w;
+                }
 #pragma unroll
-                    for (int c = 0; c < 4; c++) a[r][c] = fmaf(-f[r][q], xv[c], a[r][c]);
+                for (int q = 0; q < 4; q++) {
+                    const float4 x = *(const float4 *)&pr[4 * hq + q][4 * l];
+                    const float xv[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+                    for (int r = 0; r < 8; r++)
+#pragma unroll
+                        for (int c = 0; c < 4; c++) a[r][c] = fmaf(-F[r][q], xv[c], a[r][c]);
+                }
+            }
+        }
+        // the next step's pivot columns, once every lane has read fsl[w]
+        if (m + 1 < kW) {
+            __syncwarp();
+            if ((l >> 1) == m + 1) {
+#pragma unroll
+                for (int r = 0; r < 8; r++)
+                    *(float4 *)&fsl[w][r][4 * (l & 1)] = make_float4(a[r][0], a[r][1], a[r][2], a[r][3]);
             }
         }
     }
     if (P) {
 #pragma unroll
-        for (int r = 0; r < 4; r++)
-            *(float4 *)(P + (size_t)(4 * w + r) * kPB + 4 * l) = make_float4(a[r][0], a[r][1], a[r][2], a[r][3]);
+        for (int r = 0; r < 8; r++)
+            *(float4 *)(P + (size_t)(8 * w + r) * kPB + 4 * l) = make_float4(a[r][0], a[r][1], a[r][2], a[r][3]);
     }
     if (PT) {
 #pragma unroll
-        for (int c = 0; c < 4; c++)
-            *(float4 *)(PT + (size_t)(4 * l + c) * kPB + 4 * w) = make_float4(a[0][c], a[1][c], a[2][c], a[3][c]);
+        for (int c = 0; c < 4; c++) {
+            *(float4 *)(PT + (size_t)(4 * l + c) * kPB + 8 * w) = make_float4(a[0][c], a[1][c], a[2][c], a[3][c]);
+            *(float4 *)(PT + (size_t)(4 * l + c) * kPB + 8 * w + 4) = make_float4(a[4][c], a[5][c], a[6][c], a[7][c]);
+        }
     }
 }
 
