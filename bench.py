@@ -570,13 +570,23 @@ def dropin_bench():
         out[name] = {"N": N, "E": E, "assembly_s": t1 - t0, "gmres_s": t2 - t1, "gmres_iters": its,
                      "force_s": t3 - t2b, "field_points": len(pts), "field_s": t5 - t4,
                      "field_us_per_point": (t5 - t4) / len(pts) * 1e6, "total_s": (t1 - t0) + (t2 - t1) + (t3 - t2b) + (t5 - t4)}
+        # the C restatement at the same points: batched on every host core,
+        # and one point per call on one core as the reference's post-
+        # processing runs (a sample of the points at the larger scene)
+        from oracle.checker import Port
+        nt = os.cpu_count() or 1
         if name == "cfg0":
-            from oracle.checker import Port
-            nt = os.cpu_count() or 1
             t6 = time.perf_counter()
             Port().field(sc, B, pts, nthreads=nt)
             out[name]["cpu_port_field_s"] = time.perf_counter() - t6
             out[name]["cpu_port_threads"] = nt
+        sample = pts[:: (1 if name == "cfg0" else 40)]
+        port = Port()
+        t7 = time.perf_counter()
+        for p in sample:
+            port.field(sc, B, p[None], nthreads=1)
+        out[name]["cpu_port_1core_us_per_point"] = (time.perf_counter() - t7) / len(sample) * 1e6
+        out[name]["cpu_port_1core_points"] = len(sample)
     return out
 
 

@@ -127,13 +127,14 @@ __global__ void __launch_bounds__(128) k_point_regular(PointArgs a, double *__re
     for (int v = 0; v < NV; v++) o[v] = acc[v];
 }
 
-// Few points: thread per element, block reduction per point.
+// Few points: thread per element of chunk `chunk` (blockDim.x elements),
+// block reduction per point.
 template <int NEN, int FIELD>
-__global__ void __launch_bounds__(128) k_point_regular_few(PointArgs a, double *__restrict__ part)
+__device__ __forceinline__ void point_regular_few(const PointArgs &a, int chunk, double *__restrict__ part)
 {
     constexpr int NV = FIELD ? 6 : 2;
     __shared__ double sh[32];
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    const int e = chunk * blockDim.x + threadIdx.x;
     for (int p = 0; p < a.P; p++) {
         double acc[NV];
 #pragma unroll
@@ -166,24 +167,31 @@ __global__ void __launch_bounds__(128) k_point_regular_few(PointArgs a, double *
             if (threadIdx.x == 0) {
                 double t = 0.0;
                 for (int u = 0; u < (int)(blockDim.x >> 5); u++) t += sh[u];
-                part[((size_t)blockIdx.x * a.P + p) * NV + v] = t;
+                part[((size_t)chunk * a.P + p) * NV + v] = t;
             }
             __syncthreads();
         }
     }
 }
 
-// Singular pairs of each point: tuples (element, local position s of the
-// coincident node, node whose averaged normal is used), in element order.
 template <int NEN, int FIELD>
-__global__ void __launch_bounds__(128) k_point_singular(
-    PointArgs a, const double *__restrict__ X, const double *__restrict__ Y,
-    const double *__restrict__ Z, const double *__restrict__ normals, int N,
-    const double *__restrict__ sigma, const int *__restrict__ sp_ptr, const int4 *__restrict__ sp,
-    double *__restrict__ out)
+__global__ void __launch_bounds__(128) k_point_regular_few(PointArgs a, double *__restrict__ part)
+{
+    point_regular_few<NEN, FIELD>(a, blockIdx.x, part);
+}
+
+// Singular pairs of each point: tuples (element, local position s of the
+// coincident node, node whose averaged normal is used), in element order;
+// warp p of the grid (block b of blockDim.x threads) takes point p.
+template <int NEN, int FIELD>
+__device__ __forceinline__ void point_singular(const PointArgs &a, int b, const double *__restrict__ X,
+                                               const double *__restrict__ Y, const double *__restrict__ Z,
+                                               const double *__restrict__ normals, int N,
+                                               const double *__restrict__ sigma, const int *__restrict__ sp_ptr,
+                                               const int4 *__restrict__ sp, double *__restrict__ out)
 {
     constexpr int NV = FIELD ? 6 : 2;
-    const int p = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    const int p = (int)((b * (size_t)blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (p >= a.P) return;
     const double xe[3] = {a.px[p], a.py[p], a.pz[p]};
@@ -242,6 +250,16 @@ __global__ void __launch_bounds__(128) k_point_singular(
     }
 }
 
+template <int NEN, int FIELD>
+__global__ void __launch_bounds__(128) k_point_singular(
+    PointArgs a, const double *__restrict__ X, const double *__restrict__ Y,
+    const double *__restrict__ Z, const double *__restrict__ normals, int N,
+    const double *__restrict__ sigma, const int *__restrict__ sp_ptr, const int4 *__restrict__ sp,
+    double *__restrict__ out)
+{
+    point_singular<NEN, FIELD>(a, blockIdx.x, X, Y, Z, normals, N, sigma, sp_ptr, sp, out);
+}
+
 // result[p] = 1/(4 pi eps0) * sum_chunks part + singular part.
 template <int NV>
 __global__ void k_point_reduce(const double *__restrict__ part, int nchunk, int P,
@@ -253,6 +271,41 @@ __global__ void k_point_reduce(const double *__restrict__ part, int nchunk, int 
     double s = 0.0;
     for (int c = 0; c < nchunk; c++) s += part[(size_t)c * P * NV + t];
     out[t] = A * s + sing[t];
+}
+
+// The few-point pass in one launch: blocks [0, nchunk) the regular parts
+// (point_regular_few), the blocks after them the singular parts (a warp per
+// point); the last block to finish (a ticket taken after each block's
+// results are visible) sums the chunks as k_point_reduce does and returns
+// the ticket to zero for the next launch.
+template <int NEN, int FIELD>
+__global__ void __launch_bounds__(128) k_point_few(PointArgs a, int nchunk, const double *__restrict__ X,
+                                                   const double *__restrict__ Y, const double *__restrict__ Z,
+                                                   const double *__restrict__ normals, int N,
+                                                   const double *__restrict__ sigma, const int *__restrict__ sp_ptr,
+                                                   const int4 *__restrict__ sp, double *__restrict__ part,
+                                                   double *__restrict__ sing, unsigned *ticket,
+                                                   double *__restrict__ out)
+{
+    constexpr int NV = FIELD ? 6 : 2;
+    if ((int)blockIdx.x < nchunk) point_regular_few<NEN, FIELD>(a, blockIdx.x, part);
+    else point_singular<NEN, FIELD>(a, blockIdx.x - nchunk, X, Y, Z, normals, N, sigma, sp_ptr, sp, sing);
+    __shared__ bool last;
+    __threadfence();  // every thread's partial results, before the ticket
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    const double A = FIELD ? 0.5 / kEps0 / kPi2 : 1.0 / (kPi4 * kEps0);
+    for (int t = threadIdx.x; t < a.P * NV; t += blockDim.x) {
+        double s = 0.0;
+        for (int c = 0; c < nchunk; c++) s += ((volatile const double *)part)[(size_t)c * a.P * NV + t];
+        out[t] = A * s + ((volatile const double *)sing)[t];
+    }
+    if (threadIdx.x == 0) *ticket = 0u;
 }
 
 // Maxwell stress on the particle elements (first node of type 6):
@@ -473,13 +526,19 @@ int mst_centres(const DeviceMesh &m, const ForcePlan &fp, double *Xce, cudaStrea
 
 // ------------------------------------------------------------------ host
 
-int PointSet::build(const HostPlan &plan, int P, const double *pts, const int *node_ids)
+// Host classification of P points: coordinates, up to four coincident
+// mesh nodes each (-1 padded) and the singular tuples (element, local
+// position, node) in point order, ptr their offsets.
+static int classify_points(const HostPlan &plan, int P, const double *pts, const int *node_ids,
+                           std::vector<double> &xs, std::vector<double> &ys, std::vector<double> &zs,
+                           std::vector<int4> &co, std::vector<int> &ptr, std::vector<int4> &tup)
 {
-    this->P = P;
-    std::vector<double> xs(P), ys(P), zs(P);
-    std::vector<int4> co(P, make_int4(-1, -1, -1, -1));
-    std::vector<int> ptr(1, 0);
-    std::vector<int4> tup;
+    xs.assign(P, 0.0);
+    ys.assign(P, 0.0);
+    zs.assign(P, 0.0);
+    co.assign(P, make_int4(-1, -1, -1, -1));
+    ptr.assign(1, 0);
+    tup.clear();
     const int nen = plan.nen;
     // points that are mesh nodes: each node's group of nodes with identical
     // coordinates (a run of the coordinate order), found in one pass
@@ -568,6 +627,16 @@ int PointSet::build(const HostPlan &plan, int P, const double *pts, const int *n
         }
     for (int p = 0; p < P; p++) ptr.push_back(ptr.back() + cnt[p]);
     for (int t = 0; t < nth; t++) tup.insert(tup.end(), tups[t].begin(), tups[t].end());
+    return kOk;
+}
+
+int PointSet::build(const HostPlan &plan, int P, const double *pts, const int *node_ids)
+{
+    this->P = P;
+    std::vector<double> xs, ys, zs;
+    std::vector<int4> co, tup;
+    std::vector<int> ptr;
+    DSC_TRY(classify_points(plan, P, pts, node_ids, xs, ys, zs, co, ptr, tup));
     cudaStream_t st = 0;
     DSC_TRY(px.upload(xs, st));
     DSC_TRY(py.upload(ys, st));
@@ -619,6 +688,98 @@ static int eval_points_impl(const DeviceMesh &m, PointSet &ps, const double *dsi
     else DSC_LAUNCH(k_point_reduce<2><<<(ps.P * 2 + 255) / 256, 256, 0, st>>>(part.p, nchunk, ps.P, sing.p, dout));
     DSC_CUDA(cudaGetLastError());
     if (sync) DSC_CUDA(cudaStreamSynchronize(st));
+    return kOk;
+}
+
+FewPointWork::~FewPointWork()
+{
+    if (host) cudaFreeHost(host);
+}
+
+int point_charges(const DeviceMesh &m, const double *dsigma, DevBuf<double> &cq, cudaStream_t st)
+{
+    DSC_TRY(cq.alloc((size_t)m.E * kTriPts * 5));
+    if (m.nen == 6)
+        DSC_LAUNCH(k_charge_qp<6><<<(m.E * kTriPts + 255) / 256, 256, 0, st>>>(m.x.p, m.y.p, m.z.p, m.elems.p, m.E,
+                                                                            m.N, dsigma, cq.p));
+    else
+        DSC_LAUNCH(k_charge_qp<3><<<(m.E * kTriPts + 255) / 256, 256, 0, st>>>(m.x.p, m.y.p, m.z.p, m.elems.p, m.E,
+                                                                            m.N, dsigma, cq.p));
+    DSC_CUDA(cudaGetLastError());
+    return kOk;
+}
+
+template <int NEN, int FIELD>
+static int few_kernels(const DeviceMesh &m, const PointArgs &a, const double *dsigma, const int *sp_ptr,
+                       const int4 *sp, FewPointWork &w, cudaStream_t st)
+{
+    constexpr int NV = FIELD ? 6 : 2;
+    const int nchunk = (m.E + 127) / 128, nsing = (a.P * 32 + 127) / 128;
+    DSC_TRY(w.part.alloc((size_t)nchunk * a.P * NV));
+    DSC_TRY(w.sing.alloc((size_t)a.P * NV));
+    DSC_TRY(w.out.alloc((size_t)a.P * NV));
+    if (!w.ticket.p) {
+        DSC_TRY(w.ticket.alloc(1));
+        DSC_CUDA(cudaMemsetAsync(w.ticket.p, 0, sizeof(unsigned), st));
+    }
+    DSC_LAUNCH(k_point_few<NEN, FIELD><<<nchunk + nsing, 128, 0, st>>>(a, nchunk, m.x.p, m.y.p, m.z.p, m.normals.p,
+                                                                      m.N, dsigma, sp_ptr, sp, w.part.p, w.sing.p,
+                                                                      w.ticket.p, w.out.p));
+    DSC_CUDA(cudaGetLastError());
+    return kOk;
+}
+
+int eval_few_points(const DeviceMesh &m, const HostPlan &plan, const double *cq, const double *dsigma, int P,
+                    const double *pts, int field, double *out, FewPointWork &w, cudaStream_t st)
+{
+    if (P < 1 || P > kFewPoints) {
+        set_error("eval_few_points: %d points (1 .. %d)", P, kFewPoints);
+        return kErrArg;
+    }
+    std::vector<double> xs, ys, zs;
+    std::vector<int4> co, tup;
+    std::vector<int> ptr;
+    DSC_TRY(classify_points(plan, P, pts, nullptr, xs, ys, zs, co, ptr, tup));
+    if (tup.empty()) tup.push_back(make_int4(0, 0, 0, 0));
+    // one packed upload: x, y, z (P doubles each), coincident nodes (P int4),
+    // tuple offsets (P + 1 ints), tuples; 16-byte aligned parts
+    auto al = [](size_t b) { return (b + 15) & ~(size_t)15; };
+    const size_t o_co = al(24 * (size_t)P), o_ptr = o_co + 16 * (size_t)P, o_sp = al(o_ptr + 4 * ((size_t)P + 1));
+    const size_t up = o_sp + 16 * tup.size(), o_out = al(up);
+    const int NV = field ? 6 : 2;
+    const size_t need = o_out + sizeof(double) * P * NV;
+    if (w.host_bytes < need) {
+        if (w.host) cudaFreeHost(w.host);
+        w.host = nullptr;
+        w.host_bytes = 0;
+        const size_t cap = std::max(need, (size_t)64 << 10);
+        DSC_CUDA(cudaHostAlloc((void **)&w.host, cap, cudaHostAllocDefault));
+        w.host_bytes = cap;
+    }
+    unsigned char *h = w.host;
+    memcpy(h, xs.data(), 8 * (size_t)P);
+    memcpy(h + 8 * (size_t)P, ys.data(), 8 * (size_t)P);
+    memcpy(h + 16 * (size_t)P, zs.data(), 8 * (size_t)P);
+    memcpy(h + o_co, co.data(), 16 * (size_t)P);
+    memcpy(h + o_ptr, ptr.data(), 4 * ((size_t)P + 1));
+    memcpy(h + o_sp, tup.data(), 16 * tup.size());
+    DSC_TRY(w.pack.alloc(up));
+    DSC_CUDA(cudaMemcpyAsync(w.pack.p, h, up, cudaMemcpyHostToDevice, st));
+    const unsigned char *d = w.pack.p;
+    const PointArgs a{(const double *)d, (const double *)(d + 8 * (size_t)P), (const double *)(d + 16 * (size_t)P),
+                      (const int4 *)(d + o_co), P, m.elems.p, cq, m.E};
+    const int *sp_ptr = (const int *)(d + o_ptr);
+    const int4 *sp = (const int4 *)(d + o_sp);
+    if (m.nen == 6) {
+        if (field) DSC_TRY((few_kernels<6, 1>(m, a, dsigma, sp_ptr, sp, w, st)));
+        else DSC_TRY((few_kernels<6, 0>(m, a, dsigma, sp_ptr, sp, w, st)));
+    } else {
+        if (field) DSC_TRY((few_kernels<3, 1>(m, a, dsigma, sp_ptr, sp, w, st)));
+        else DSC_TRY((few_kernels<3, 0>(m, a, dsigma, sp_ptr, sp, w, st)));
+    }
+    DSC_CUDA(cudaMemcpyAsync(h + o_out, w.out.p, sizeof(double) * P * NV, cudaMemcpyDeviceToHost, st));
+    DSC_CUDA(cudaStreamSynchronize(st));
+    memcpy(out, h + o_out, sizeof(double) * P * NV);
     return kOk;
 }
 

@@ -29,6 +29,30 @@ struct PointSet {
     int build(const HostPlan &plan, int P, const double *pts, const int *node_ids = nullptr);
 };
 
+// Few points at a time (the reference's post-processing evaluates one point
+// per call): the quadrature points' charges stay on the device while the
+// solution does not change (point_charges), and each call moves its points,
+// coincident nodes and singular tuples up in one copy and its results down
+// in one, through a pinned staging buffer.
+constexpr int kFewPoints = 64;
+struct FewPointWork {
+    DevBuf<unsigned char> pack;
+    DevBuf<double> part, sing, out;
+    DevBuf<unsigned> ticket;  // k_point_few's count of finished blocks (zero between launches)
+    unsigned char *host = nullptr;  // pinned
+    size_t host_bytes = 0;
+    FewPointWork() = default;
+    FewPointWork(const FewPointWork &) = delete;
+    FewPointWork &operator=(const FewPointWork &) = delete;
+    ~FewPointWork();
+};
+// cq (E x 7 x 5: the point and both charges of every quadrature point).
+int point_charges(const DeviceMesh &m, const double *dsigma, DevBuf<double> &cq, cudaStream_t st);
+// Field (field = 1: P x 6) or potential (P x 2) at P <= kFewPoints points,
+// into host memory, with cq from point_charges for dsigma.
+int eval_few_points(const DeviceMesh &m, const HostPlan &plan, const double *cq, const double *dsigma, int P,
+                    const double *pts, int field, double *out, FewPointWork &w, cudaStream_t st);
+
 // field = 1: dout = P x 6 (Re Ex, Im Ex, Re Ey, Im Ey, Re Ez, Im Ez);
 // field = 0: dout = P x 2 (Re, Im potential).  dsigma: device, 2N.
 // sync = false leaves the work queued on st.

@@ -112,6 +112,26 @@ def test_field_off_mesh_and_on_nodes_vs_checker(gpu, port):
     assert relerr(api.potential(sc, x, pts), port.potential(sc, x, pts)) < SOL_TOL
 
 
+def test_few_point_calls_match_batched_and_follow_the_solution(gpu, port):
+    """Calls of at most 64 points (the reference's post-processing asks for
+    one point per call) keep the solution's quadrature charges on the device
+    and move each call's data in one packed copy: they must agree with one
+    batched call, on and off the mesh, and after the solution changes."""
+    sc = scenes.small(nen=6)
+    A, B = port.assemble(sc)
+    x, _, _ = port.gmres(A, B)
+    p0 = sc.particles[0][0]
+    pts = np.vstack([sc.nodes[p0:p0 + 40], sc.nodes[:3], np.random.default_rng(5).uniform(-2, 2, (30, 3))])
+    for xs in (x, 2.0 * x + 1e-3, x):
+        for fn in (api.field, api.potential):
+            full = fn(sc, xs, pts)   # 73 points: the batched path
+            one = np.vstack([fn(sc, xs, p[None]) for p in pts[::7]])
+            chunks = np.vstack([fn(sc, xs, pts[i:i + 50]) for i in range(0, len(pts), 50)])
+            assert relerr(one, full[::7]) < 1e-13
+            assert relerr(chunks, full) < 1e-13
+        assert relerr(api.field(sc, xs, pts[:5]), port.field(sc, xs, pts[:5])) < SOL_TOL
+
+
 def test_assembly_accumulates_like_reference(gpu, port):
     sc = scenes.small(nen=3)
     A0 = np.full((sc.N, 2 * sc.N), 0.25)
