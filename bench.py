@@ -540,6 +540,14 @@ def dropin_bench():
                               api.row_pointers(mat), prob.ctypes.data_as(C.c_void_p), rA,
                               api.row_pointers(mbc), B.ctypes.data_as(C.c_void_p))
         t1 = time.perf_counter()
+        asm_first = t1 - t0
+        # the same call again: the rows' pages now exist (the first call
+        # pays the host's first touch of the caller's fresh allocation)
+        L.electricFormA_tria6(rn, re_, bct.ctypes.data_as(C.c_void_p), api.row_pointers(ifc),
+                              api.row_pointers(mat), prob.ctypes.data_as(C.c_void_p), rA,
+                              api.row_pointers(mbc), B.ctypes.data_as(C.c_void_p))
+        asm_again = time.perf_counter() - t1
+        t1 = time.perf_counter()
         cwd = os.getcwd()
         with tempfile.TemporaryDirectory() as d:
             os.chdir(d)
@@ -567,9 +575,11 @@ def dropin_bench():
             L.field_tria6(p.ctypes.data_as(C.c_void_p), rn, re_, B.ctypes.data_as(C.c_void_p),
                           mE.ctypes.data_as(C.c_void_p))
         t5 = time.perf_counter()
-        out[name] = {"N": N, "E": E, "assembly_s": t1 - t0, "gmres_s": t2 - t1, "gmres_iters": its,
+        out[name] = {"N": N, "E": E, "assembly_s": asm_first, "assembly_again_s": asm_again,
+                     "assembly_bytes": 8.0 * N * 2 * N, "gmres_s": t2 - t1, "gmres_iters": its,
                      "force_s": t3 - t2b, "field_points": len(pts), "field_s": t5 - t4,
-                     "field_us_per_point": (t5 - t4) / len(pts) * 1e6, "total_s": (t1 - t0) + (t2 - t1) + (t3 - t2b) + (t5 - t4)}
+                     "field_us_per_point": (t5 - t4) / len(pts) * 1e6,
+                     "total_s": asm_first + (t2 - t1) + (t3 - t2b) + (t5 - t4)}
         # the C restatement at the same points: batched on every host core,
         # and one point per call on one core as the reference's post-
         # processing runs (a sample of the points at the larger scene)
