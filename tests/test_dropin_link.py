@@ -1,6 +1,7 @@
-"""The library's link recipe: the reference's own driver objects,
-its force.c with the MST functions renamed, and libdepsolver_cuda.so make a
-depSolver executable whose hot-path calls resolve to the library.
+"""The library's link recipe: the reference's own driver objects (without
+its assembly, solvers, field, potential and force objects) and
+libdepsolver_cuda.so make a depSolver executable whose hot-path calls,
+the multipole and ellipsoid force models included, resolve to the library.
 
 Needs the reference sources (built into oracle/_ref/); skipped elsewhere.
 Without a GPU the executable must stop at its first library call (matrix
@@ -16,7 +17,8 @@ from conftest import REFERENCE, ROOT
 
 DROPIN = ["electricFormA_tria3", "electricFormA_tria6", "electricFormFullA_tria3",
           "electricFormFullA_tria6", "gaussBksb", "solverGMRES_el", "field_tria3", "field_tria6",
-          "potential_tria3", "potential_tria6", "forceMST_tria3", "forceMST_tria6"]
+          "potential_tria3", "potential_tria6", "forceMST_tria3", "forceMST_tria6",
+          "forceMultipole_tria3", "forceMultipole_tria6", "forceEllipsoid_tria3", "forceEllipsoid_tria6"]
 
 
 @pytest.fixture(scope="module")
@@ -37,7 +39,8 @@ def test_hot_path_symbols_come_from_the_library(exe):
     for name in DROPIN:
         assert name in undef, name          # resolved at run time ...
         assert name not in defined, name    # ... and not by an object of the reference
-    assert "forceMST_tria6_cpu" in defined  # the CPU MST stays linked, renamed
+    for cpu_only in ("intDE_tria6", "intF_tria6", "depolarization"):
+        assert cpu_only not in defined, cpu_only   # no reference force code is linked
     ldd = subprocess.run(["ldd", exe], capture_output=True, text=True).stdout
     assert "libdepsolver_cuda.so" in ldd
 
