@@ -18,6 +18,7 @@
 #include "../../include/depsolver_cuda.h"
 #include "dsc_common.cuh"
 #include "dsc_field.h"
+#include "dsc_quad8.h"
 #include "dsc_gmres.h"
 #include "dsc_internal.h"
 
@@ -51,6 +52,11 @@ struct Context {
     uint64_t sigma_gen = 0, cq_gen = ~(uint64_t)0, cq_key = 0;
     DevBuf<double> cq;
     FewPointWork few;
+    // the quad8 family: its mesh (rebuilt when the content changes), the
+    // solution and the point results on the device
+    std::unique_ptr<Q8Mesh> q8;
+    uint64_t q8_key = 0;
+    DevBuf<double> q8_sigma, q8_out;
     // multipole / ellipsoid force points: their coordinates and workspace
     DevBuf<double> dpts;
     DerivWork deriv;
@@ -202,6 +208,23 @@ static int get_mesh(int nen, int N, int E, const double *nodes, const int *elems
     return kOk;
 }
 
+static int get_q8_mesh(int N, int E, const double *nodes, const int *elems0, Q8Mesh **out)
+{
+    DSC_TRY(ensure_stream());
+    Context &c = ctx();
+    uint64_t key = mix(mix(mix(0x243f6a8885a308d3ULL, 8), N), E);
+    key = hash_bytes(key, nodes, (size_t)N * 3 * sizeof(double));
+    key = hash_bytes(key, elems0, (size_t)E * 8 * sizeof(int));
+    if (!c.q8 || c.q8_key != key) {
+        auto m = std::make_unique<Q8Mesh>();
+        DSC_TRY(m->build(N, E, nodes, elems0, c.st));
+        c.q8 = std::move(m);
+        c.q8_key = key;
+    }
+    *out = c.q8.get();
+    return kOk;
+}
+
 static int get_sigma(int N, const double *vB, const double **dsig)
 {
     // the solution goes up again only when it differs from the copy on the
@@ -322,11 +345,25 @@ static int assemble_impl(int nen, int full, unsigned N, unsigned E, unsigned nIf
                          const unsigned *ifaces, const double *mat, double freq, const double *mbc,
                          RowSinkFn sink, void *user)
 {
-    MeshEntry *m;
-    DSC_TRY(get_mesh(nen, (int)N, (int)E, nodes, elems0, &m));
-    DSC_TRY(set_rows(m->plan, bctype));
     cudaStream_t st = ctx().st;
-    DSC_TRY(m->dev.upload_rows(m->plan, st));
+    const size_t ld = ((size_t)N + 31) / 32 * 32;
+    DevBuf<double> K;
+    std::vector<int> row_kind(N);
+    if (nen == 8) {
+        Q8Mesh *q;
+        DSC_TRY(get_q8_mesh((int)N, (int)E, nodes, elems0, &q));
+        DSC_TRY(K.alloc(ld * N));
+        DSC_TRY(q8_assemble_K(*q, bctype, K.p, ld, st));
+        for (unsigned i = 0; i < N; i++) row_kind[i] = bctype[i] == 1 ? 0 : 1;
+    } else {
+        MeshEntry *m;
+        DSC_TRY(get_mesh(nen, (int)N, (int)E, nodes, elems0, &m));
+        DSC_TRY(set_rows(m->plan, bctype));
+        DSC_TRY(m->dev.upload_rows(m->plan, st));
+        DSC_TRY(K.alloc(ld * N));
+        DSC_TRY(assemble_K_fp64(m->dev, K.p, ld, st));
+        row_kind = m->plan.row_kind;
+    }
     // Per-row coefficients: conductor rows a = 1 (K holds C int G N);
     // interface rows a = A_k, b = B_k, d = -1/(2 eps0) with k the row's
     // interface id mBC[i][1] (src/assembly_el.c:245-256).
@@ -334,7 +371,7 @@ static int assemble_impl(int nen, int full, unsigned N, unsigned E, unsigned nIf
     if (nIf) interface_coeffs(nIf, ifaces, mat, freq, Ak.data(), Bk.data());
     std::vector<double> ca(N), cb(N), cd(N);
     for (unsigned i = 0; i < N; i++) {
-        if (m->plan.row_kind[i] == 0) {
+        if (row_kind[i] == 0) {
             ca[i] = 1.0;
             cb[i] = 0.0;
             cd[i] = 0.0;
@@ -349,13 +386,10 @@ static int assemble_impl(int nen, int full, unsigned N, unsigned E, unsigned nIf
             cd[i] = -0.5 / kEps0;
         }
     }
-    DevBuf<double> dca, dcb, dcd, K, stage;
+    DevBuf<double> dca, dcb, dcd, stage;
     DSC_TRY(dca.upload(ca, st));
     DSC_TRY(dcb.upload(cb, st));
     DSC_TRY(dcd.upload(cd, st));
-    const size_t ld = ((size_t)N + 31) / 32 * 32;
-    DSC_TRY(K.alloc(ld * N));
-    DSC_TRY(assemble_K_fp64(m->dev, K.p, ld, st));
 
     const size_t ncol = 2 * (size_t)N;
     const int nrows = full ? 2 * (int)N : (int)N;
@@ -983,14 +1017,16 @@ extern "C" int dsc_device_count(void)
     return n;
 }
 
+// Element families of the flat calls: tria3, tria6 and the quad8 extension.
+static bool family_ok(int nen) { return nen == 3 || nen == 6 || nen == 8; }
+
 extern "C" int dsc_assemble(int nen, int full, unsigned N, unsigned E, unsigned nIf,
                             const double *nodes, const unsigned *elems, const unsigned *bctype,
                             const unsigned *ifaces, const double *mat, double freq,
                             const double *mbc, double *A, size_t lda, double *B)
 {
     std::lock_guard<std::mutex> lk(ctx().mu);
-    if ((nen != 3 && nen != 6) || !nodes || !elems || !bctype || !mbc || !A || !B ||
-        lda < 2 * (size_t)N) {
+    if (!family_ok(nen) || !nodes || !elems || !bctype || !mbc || !A || !B || lda < 2 * (size_t)N) {
         set_error("dsc_assemble: bad arguments");
         return kErrArg;
     }
@@ -1057,13 +1093,35 @@ extern "C" int dsc_gmres(unsigned N, unsigned preCond, double tol, unsigned max_
     return rc;
 }
 
+// Field or potential of a quad8 mesh at host points (out: npts x 6 or 2).
+static int q8_points_host(unsigned N, unsigned E, const double *nodes, const int *elems0, const double *vB,
+                          unsigned npts, const double *pts, int field, double *out)
+{
+    Context &c = ctx();
+    Q8Mesh *q;
+    DSC_TRY(get_q8_mesh((int)N, (int)E, nodes, elems0, &q));
+    if (npts == 0) return kOk;
+    const int NV = field ? 6 : 2;
+    DSC_TRY(c.q8_sigma.upload(vB, 2 * (size_t)N, c.st));
+    DSC_TRY(c.q8_out.alloc((size_t)npts * NV));
+    DSC_TRY(q8_points(*q, c.q8_sigma.p, (int)npts, pts, field, c.q8_out.p, c.st));
+    DSC_CUDA(cudaMemcpyAsync(out, c.q8_out.p, (size_t)npts * NV * sizeof(double), cudaMemcpyDeviceToHost, c.st));
+    DSC_CUDA(cudaStreamSynchronize(c.st));
+    return kOk;
+}
+
 extern "C" int dsc_field_points(int nen, unsigned N, unsigned E, const double *nodes,
                                 const unsigned *elems, const double *vB, unsigned npts,
                                 const double *pts, double *mE)
 {
     std::lock_guard<std::mutex> lk(ctx().mu);
+    if (!family_ok(nen) || !nodes || !elems || !vB || (npts && (!pts || !mE))) {
+        set_error("dsc_field_points: bad arguments");
+        return kErrArg;
+    }
     std::vector<int> e0;
     elems_to0(nen, (int)E, elems, e0);
+    if (nen == 8) return q8_points_host(N, E, nodes, e0.data(), vB, npts, pts, 1, mE);
     return points_impl(nen, N, E, nodes, e0.data(), vB, npts, pts, 1, mE);
 }
 
@@ -1072,8 +1130,13 @@ extern "C" int dsc_potential_points(int nen, unsigned N, unsigned E, const doubl
                                     const double *pts, double *mPot)
 {
     std::lock_guard<std::mutex> lk(ctx().mu);
+    if (!family_ok(nen) || !nodes || !elems || !vB || (npts && (!pts || !mPot))) {
+        set_error("dsc_potential_points: bad arguments");
+        return kErrArg;
+    }
     std::vector<int> e0;
     elems_to0(nen, (int)E, elems, e0);
+    if (nen == 8) return q8_points_host(N, E, nodes, e0.data(), vB, npts, pts, 0, mPot);
     return points_impl(nen, N, E, nodes, e0.data(), vB, npts, pts, 0, mPot);
 }
 
@@ -1144,7 +1207,18 @@ extern "C" int dsc_force_mst(int nen, unsigned N, unsigned E, const double *node
                              double eps, double *Fce, double *Xce, double *Fcm, double *Xcm)
 {
     std::lock_guard<std::mutex> lk(ctx().mu);
+    if (!family_ok(nen) || !nodes || !elems || !bctype || !vB || !Fcm || !Xcm) {
+        set_error("dsc_force_mst: bad arguments");
+        return kErrArg;
+    }
     std::vector<int> e0;
     elems_to0(nen, (int)E, elems, e0);
+    if (nen == 8) {
+        Context &c = ctx();
+        Q8Mesh *q;
+        DSC_TRY(get_q8_mesh((int)N, (int)E, nodes, e0.data(), &q));
+        DSC_TRY(c.q8_sigma.upload(vB, 2 * (size_t)N, c.st));
+        return q8_force_mst(*q, bctype, c.q8_sigma.p, eps, Fce, Xce, Fcm, Xcm, c.st);
+    }
     return force_impl(nen, N, E, nodes, e0.data(), bctype, vB, eps, Fce, Xce, Fcm, Xcm);
 }

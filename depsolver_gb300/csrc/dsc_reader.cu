@@ -29,6 +29,7 @@
 
 #include "../../include/depsolver_cuda.h"
 #include "dsc_internal.h"
+#include "dsc_quad8.h"
 
 namespace dsc {
 
@@ -123,10 +124,13 @@ static int read_deck(const std::string &dir, BemDeck &d)
     std::string etype = c.next();
     for (char &ch : etype) ch = (char)tolower((unsigned char)ch);
     const std::string elem_file = c.next();
+    // the reference's names (src/preProcess.c:110-146); its driver takes
+    // tria3 and tria6 (src/depSolver.c:180-183), this library also quad8
     if (etype.compare(0, 5, "tria6") == 0) d.nen = 6;
     else if (etype.compare(0, 5, "tria3") == 0) d.nen = 3;
+    else if (etype.compare(0, 5, "quad8") == 0) d.nen = 8;
     else {
-        set_error("element type %s: the path handles tria3 and tria6 (src/depSolver.c:180-183)", etype.c_str());
+        set_error("element type %s: the path handles tria3, tria6 and quad8", etype.c_str());
         return kErrArg;
     }
     c.next();  // MATERIALS
@@ -339,7 +343,7 @@ extern "C" int dsc_bem_arrays(const dsc_bem *b, double *nodes, unsigned *elems, 
 extern "C" int dsc_node_normals(int nen, unsigned N, unsigned E, const double *nodes, const unsigned *elems,
                                 double *normals)
 {
-    if ((nen != 3 && nen != 6) || !nodes || !elems || !normals || N == 0) {
+    if ((nen != 3 && nen != 6 && nen != 8) || !nodes || !elems || !normals || N == 0) {
         set_error("dsc_node_normals: bad arguments");
         return kErrArg;
     }
@@ -351,6 +355,7 @@ extern "C" int dsc_node_normals(int nen, unsigned N, unsigned E, const double *n
         }
         e0[t] = (int)elems[t] - 1;
     }
-    node_normals(nen, (int)N, (int)E, nodes, e0.data(), normals);
+    if (nen == 8) q8_node_normals((int)N, (int)E, nodes, e0.data(), normals);
+    else node_normals(nen, (int)N, (int)E, nodes, e0.data(), normals);
     return kOk;
 }

@@ -126,6 +126,62 @@ def _orient_outward(v: np.ndarray, f: np.ndarray) -> np.ndarray:
     return f
 
 
+def _drop_unused(nodes: np.ndarray, elems: np.ndarray):
+    """Nodes that no element names removed (quad8 grids have no node at a
+    cell's centre), the rest renumbered in their order."""
+    used = np.zeros(nodes.shape[0], bool)
+    used[elems.ravel()] = True
+    new = np.cumsum(used) - 1
+    return nodes[used], new[elems].astype(np.int64)
+
+
+def cubed_sphere(cells: int, radius: float = 1.0, center=(0.0, 0.0, 0.0)):
+    """Sphere of quad8 elements: each face of the cube [-1, 1]^3 cut into
+    cells x cells quads, every node (corners and mid-sides) projected onto
+    the sphere, nodes shared across faces merged, elements oriented with
+    their normal outward.  Returns (nodes, 0-based elems)."""
+    g = 2 * cells + 1
+    t = np.linspace(-1.0, 1.0, g)
+    faces = []
+    for axis in range(3):
+        for sign in (-1.0, 1.0):
+            U, V = np.meshgrid(t, t, indexing="xy")
+            P = np.zeros((g, g, 3))
+            a, b = [d for d in range(3) if d != axis]
+            P[..., axis] = sign
+            P[..., a] = U
+            P[..., b] = V
+            faces.append(P)
+    key_id, nodes = {}, []
+
+    def node(p):
+        q = p / np.linalg.norm(p)
+        k = tuple(np.round(p, 12))
+        if k not in key_id:
+            key_id[k] = len(nodes)
+            nodes.append(q)
+        return key_id[k]
+
+    el = []
+    for P in faces:
+        ids = [[node(P[j, i]) for i in range(g)] for j in range(g)]
+        for j in range(cells):
+            for i in range(cells):
+                I, J = 2 * i, 2 * j
+                e = [ids[J][I], ids[J][I + 2], ids[J + 2][I + 2], ids[J + 2][I],
+                     ids[J][I + 1], ids[J + 1][I + 2], ids[J + 2][I + 1], ids[J + 1][I]]
+                el.append(e)
+    nodes = np.asarray(nodes)
+    elems = np.asarray(el, dtype=np.int64)
+    # outward: the corners' diagonal cross product along the centroid
+    c0, c1, c2, c3 = (nodes[elems[:, k]] for k in range(4))
+    n = np.cross(c2 - c0, c3 - c1)
+    flip = np.einsum("ij,ij->i", n, c0 + c1 + c2 + c3) < 0
+    elems[flip] = elems[flip][:, [0, 3, 2, 1, 7, 6, 5, 4]]
+    nodes, elems = _drop_unused(nodes, elems)
+    return nodes * radius + np.asarray(center, dtype=np.float64), elems
+
+
 def icosphere(level: int, radius: float = 1.0, center=(0.0, 0.0, 0.0), nen: int = 6):
     """Unit icosphere subdivided `level` times, as (nodes, 0-based elems).
 
@@ -163,8 +219,10 @@ def icosphere(level: int, radius: float = 1.0, center=(0.0, 0.0, 0.0), nen: int 
 def plate(side_x: float, side_y: float, ncell_x: int, ncell_y: int, center=(0.0, 0.0, 0.0),
           nen: int = 6):
     """Flat rectangle in the plane z = center[2], meshed as ncell_x x ncell_y
-    quads, each split into two triangles along its (0,0)-(1,1) diagonal.
-    Returns (nodes, 0-based elems); normals point along +z."""
+    quads, each split into two triangles along its (0,0)-(1,1) diagonal, or
+    kept as one quad8 (nen = 8: corners counter-clockwise, then the
+    mid-sides of edges 1-2, 2-3, 3-4, 4-1).  Returns (nodes, 0-based elems);
+    normals point along +z."""
     cx, cy, cz = center
     if nen == 3:
         gx, gy = ncell_x + 1, ncell_y + 1
@@ -185,13 +243,20 @@ def plate(side_x: float, side_y: float, ncell_x: int, ncell_y: int, center=(0.0,
                 p00, p10, p11, p01 = idx(i, j), idx(i + 1, j), idx(i + 1, j + 1), idx(i, j + 1)
                 el.append([p00, p10, p11])
                 el.append([p00, p11, p01])
+            elif nen == 8:
+                I, J = 2 * i, 2 * j
+                el.append([idx(I, J), idx(I + 2, J), idx(I + 2, J + 2), idx(I, J + 2),
+                           idx(I + 1, J), idx(I + 2, J + 1), idx(I + 1, J + 2), idx(I, J + 1)])
             else:
                 I, J = 2 * i, 2 * j
                 p00, p10, p11, p01 = idx(I, J), idx(I + 2, J), idx(I + 2, J + 2), idx(I, J + 2)
                 cc = idx(I + 1, J + 1)
                 el.append([p00, idx(I + 1, J), p10, idx(I + 2, J + 1), p11, cc])
                 el.append([p00, cc, p11, idx(I + 1, J + 2), p01, idx(I, J + 1)])
-    return nodes, np.asarray(el, dtype=np.int64)
+    elems = np.asarray(el, dtype=np.int64)
+    if nen == 8:
+        nodes, elems = _drop_unused(nodes, elems)
+    return nodes, elems
 
 
 # ---------------------------------------------------------------- scenes
@@ -240,8 +305,12 @@ def sphere_between_plates(sphere_level: int, plate_cells: int, *, nen: int = 6,
                           name: Optional[str] = None) -> Scene:
     """One dielectric sphere between two square plate electrodes at
     z = +-plate_z held at +-volts.  Material 1 = medium, 2 = sphere;
-    interface 1 = (1, 2); sphere nodes carry boundary type 6."""
-    s_nodes, s_el = icosphere(sphere_level, radius, center, nen)
+    interface 1 = (1, 2); sphere nodes carry boundary type 6.  nen = 8: quad8
+    plates and a cubed sphere of 2^sphere_level cells per face edge."""
+    if nen == 8:
+        s_nodes, s_el = cubed_sphere(2 ** sphere_level, radius, center)
+    else:
+        s_nodes, s_el = icosphere(sphere_level, radius, center, nen)
     top_n, top_e = plate(plate_side, plate_side, plate_cells, plate_cells, (0, 0, plate_z), nen)
     bot_n, bot_e = plate(plate_side, plate_side, plate_cells, plate_cells, (0, 0, -plate_z), nen)
     parts = [(top_n, top_e, "conductor", volts), (bot_n, bot_e, "conductor", -volts),
@@ -249,6 +318,20 @@ def sphere_between_plates(sphere_level: int, plate_cells: int, *, nen: int = 6,
     mat = [list(medium), list(particle)]
     return _assemble(parts, nen, mat, [[1, 2]], freq,
                      name or f"sphere-L{sphere_level}-plates-{plate_cells}x{plate_cells}-tria{nen}")
+
+
+def conductor_sphere(cells: int = 4, *, nen: int = 8, radius: float = 1.0, volts: float = 1.0,
+                     eps_r: float = 1.0, freq: float = 1.0e6) -> Scene:
+    """One sphere held at `volts` alone in one medium (a real system whose
+    potential outside is volts * radius / r and whose field on the surface
+    is volts / radius along the normal): a quad8 cubed sphere of `cells`
+    cells per face edge, or (nen = 3, 6) an icosphere of level `cells`."""
+    if nen == 8:
+        n, e = cubed_sphere(cells, radius)
+    else:
+        n, e = icosphere(cells, radius, nen=nen)
+    return _assemble([(n, e, "conductor", volts)], nen, [[0.0, eps_r]], np.zeros((0, 2)), freq,
+                     f"conductor-sphere-{cells}-n{nen}")
 
 
 def cfg0(nen: int = 6, center=(0.0, 0.0, 0.0)) -> Scene:
@@ -410,7 +493,7 @@ def write_bem(scene: Scene, directory: str, solver: str = "gmres 1 0", analysis:
                 f.write(f"{j + 1}\t{t}\t{scene.mbc[j, 0]:.17e}\t{int(scene.mbc[j, 1])}\n")
             else:
                 f.write(f"{j + 1}\t{t}\t{scene.mbc[j, 0]:.17e}\n")
-    etype = "tria6" if scene.nen == 6 else "tria3"
+    etype = {3: "tria3", 6: "tria6", 8: "quad8"}[scene.nen]
     with open(os.path.join(directory, "input.bem"), "w") as f:
         f.write(f"NODES\n{scene.N}\nnodes.bem\n\nELEMS\n{scene.E}\n{etype}\nelems.bem\n\n")
         f.write(f"MATERIALS\n{scene.mat.shape[0]}\n")
@@ -445,7 +528,7 @@ def read_bem(directory: str) -> Scene:
     for _ in range(n_if):
         next(it); ifaces.append([int(next(it)), int(next(it))])
     next(it); freq = float(next(it)); bc_file = next(it)
-    nen = 6 if etype.startswith("tria6") else 3
+    nen = 6 if etype.startswith("tria6") else 8 if etype.startswith("quad8") else 3
 
     def table(fname):
         return _strip_comments(open(os.path.join(directory, fname)).read()).split()

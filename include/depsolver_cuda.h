@@ -132,7 +132,9 @@ unsigned long long dsc_kernel_launches(void);
 /* Flat form of electricFormA_* (full = 0; A is N x 2N) and
  * electricFormFullA_* (full = 1; A is 2N x 2N); rows of A are lda doubles
  * apart and receive A += assembled values; B (2N) = boundary values.
- * nen = 3 or 6; elems 1-based (E x nen); bctype 2N; ifaces nIf x 2; mat
+ * nen = 3 or 6 (tria3, tria6) or 8 (quad8, an extension: the reference
+ * has no quad8 integrals; see dsc_field_points); elems 1-based (E x nen);
+ * bctype 2N; ifaces nIf x 2; mat
  * has at least max(ifaces) rows of (sigma, eps_r); mbc 2N x 3. */
 int dsc_assemble(int nen, int full, unsigned N, unsigned E, unsigned nIf, const double *nodes,
                  const unsigned *elems, const unsigned *bctype, const unsigned *ifaces,
@@ -173,7 +175,15 @@ int dsc_gmres(unsigned N, unsigned preCond, double tol, unsigned max_iters, cons
               size_t lda, double *B, const double *x0, const char *log_path, unsigned *iters);
 
 /* Field (mE: npts x 6) or potential (mPot: npts x 2) at npts points
- * (pts: npts x 3), from the nodal solution vB (2N). */
+ * (pts: npts x 3), from the nodal solution vB (2N).  nen = 3, 6 or 8.
+ * quad8 (nen = 8) is this library's extension of the element families:
+ * serendipity element on [-1, 1]^2, nodes 1-4 the corners (-1,-1),
+ * (1,-1), (1,1), (-1,1), nodes 5-8 the mid-sides of edges 1-2, 2-3, 3-4,
+ * 4-1; 3 x 3 Gauss points for regular pairs; singular pairs on triangles
+ * with their apex at the collocation node, with the triangle path's Duffy
+ * and subdivision schemes; on a node the field adds the jump
+ * sigma / (2 eps0) n once with that node's sigma (the triangle families
+ * keep the reference's jump per singular element). */
 int dsc_field_points(int nen, unsigned N, unsigned E, const double *nodes, const unsigned *elems,
                      const double *vB, unsigned npts, const double *pts, double *mE);
 int dsc_potential_points(int nen, unsigned N, unsigned E, const double *nodes,
@@ -193,7 +203,8 @@ int dsc_force_ellipsoid(int nen, unsigned N, unsigned E, const double *nodes, co
                         const double *axis, const double *mat, double freq, double *F);
 int dsc_depolarization(const double *axis, double *Ld);
 
-/* Flat form of forceMST_*: Fce, Xce are E x 3 (may be NULL). */
+/* Flat form of forceMST_*: Fce, Xce are E x 3 (may be NULL); nen = 3, 6
+ * or 8 (quad8: the 3 x 3 Gauss points, Xce at the element's centre). */
 int dsc_force_mst(int nen, unsigned N, unsigned E, const double *nodes, const unsigned *elems,
                   const unsigned *bctype, const double *vB, double eps, double *Fce, double *Xce,
                   double *Fcm, double *Xcm);
@@ -499,7 +510,8 @@ int dsc_bem_arrays(const dsc_bem *b, double *nodes, unsigned *elems, unsigned *b
 /* Averaged unit normal at every node (normals: N x 3), replacing the
  * reference's getNormal_tria3/6 (src/normals.c:120-319), which scans every
  * element per node: the average over the elements containing the node of
- * their local normals at it, normalised (host threads, O(N + E)). */
+ * their local normals at it, normalised (host threads, O(N + E)); nen = 3,
+ * 6 or 8. */
 int dsc_node_normals(int nen, unsigned N, unsigned E, const double *nodes, const unsigned *elems,
                      double *normals);
 

@@ -96,6 +96,18 @@ class Port:
         L.orc_interface_coeffs.argtypes = [C.c_uint, C.c_void_p, C.c_void_p, C.c_double, _dp, _dp]
         L.orc_matvec_rows.restype = None
         L.orc_matvec_rows.argtypes = [C.c_uint, C.c_void_p, _dp, _dp, C.c_uint, C.c_uint, C.c_int]
+        # the quad8 extension (oracle/port/quad8.c)
+        L.orc_q8_assemble.restype = C.c_int
+        L.orc_q8_assemble.argtypes = [C.c_int, C.c_uint, C.c_uint, C.c_uint, _dp, _up, _up, C.c_void_p,
+                                      C.c_void_p, C.c_double, _dp, C.c_void_p, C.c_size_t, _dp]
+        L.orc_q8_field.restype = None
+        L.orc_q8_field.argtypes = [C.c_uint, C.c_uint, _dp, _up, _dp, _dp, _dp]
+        L.orc_q8_potential.restype = None
+        L.orc_q8_potential.argtypes = [C.c_uint, C.c_uint, _dp, _up, _dp, _dp, _dp]
+        L.orc_q8_forceMST.restype = None
+        L.orc_q8_forceMST.argtypes = [C.c_uint, C.c_uint, _dp, _up, _up, _dp, C.c_double, _dp, _dp, _dp, _dp]
+        L.orc_q8_node_normal.restype = None
+        L.orc_q8_node_normal.argtypes = [C.c_uint, _dp, _up, C.c_uint, _dp]
 
     # -- assembly -------------------------------------------------------
     def assemble(self, sc, full: bool = False, rows=None, nthreads: int = 1):
@@ -107,6 +119,13 @@ class Port:
         r0, r1 = rows if rows is not None else (0, N)
         ifc = _u(sc.ifaces)
         mat = _f(sc.mat)
+        if sc.nen == 8:
+            rc = self.lib.orc_q8_assemble(int(full), N, sc.E, sc.n_if, _f(sc.nodes), _u(sc.elems),
+                                          _u(sc.bctype), ifc.ctypes.data if sc.n_if else None,
+                                          mat.ctypes.data, sc.freq, _f(sc.mbc), A.ctypes.data, 2 * N, B)
+            if rc:
+                raise ValueError("boundary type other than 0, 1, 6 in the scene")
+            return A, B
         rc = self.lib.orc_assemble(sc.nen, int(full), N, sc.E, sc.n_if, _f(sc.nodes), _u(sc.elems),
                                    _u(sc.bctype), ifc.ctypes.data if sc.n_if else None,
                                    mat.ctypes.data, sc.freq, _f(sc.mbc), r0, r1,
@@ -155,6 +174,12 @@ class Port:
     def field(self, sc, vB, pts, nthreads=1):
         pts = _f(np.atleast_2d(pts))
         out = np.zeros((pts.shape[0], 6))
+        if sc.nen == 8:
+            for i in range(pts.shape[0]):
+                r = np.zeros(6)
+                self.lib.orc_q8_field(sc.N, sc.E, _f(sc.nodes), _u(sc.elems), _f(vB), _f(pts[i]), r)
+                out[i] = r
+            return out
         self.lib.orc_field_points(sc.nen, sc.N, sc.E, _f(sc.nodes), _u(sc.elems), _f(vB),
                                   pts.shape[0], pts, out, nthreads)
         return out
@@ -164,6 +189,10 @@ class Port:
         out = np.zeros((pts.shape[0], 2))
         for i in range(pts.shape[0]):
             r = np.zeros(2)
+            if sc.nen == 8:
+                self.lib.orc_q8_potential(sc.N, sc.E, _f(sc.nodes), _u(sc.elems), _f(vB), _f(pts[i]), r)
+                out[i] = r
+                continue
             self.lib.orc_potential(sc.nen, sc.N, sc.E, _f(sc.nodes), _u(sc.elems), _f(vB),
                                    _f(pts[i]), r)
             out[i] = r
@@ -175,12 +204,19 @@ class Port:
         Xce = np.zeros((sc.E, 3))
         Fcm = np.zeros(3)
         Xcm = np.zeros(3)
+        if sc.nen == 8:
+            self.lib.orc_q8_forceMST(sc.N, sc.E, _f(sc.nodes), _u(sc.elems), _u(sc.bctype), _f(vB), eps,
+                                     Fce, Xce, Fcm, Xcm)
+            return Fce, Xce, Fcm, Xcm
         self.lib.orc_forceMST(sc.nen, sc.N, sc.E, _f(sc.nodes), _u(sc.elems), _u(sc.bctype),
                               _f(vB), eps, Fce, Xce, Fcm, Xcm, nthreads)
         return Fce, Xce, Fcm, Xcm
 
     def node_normal(self, sc, node0):
         n = np.zeros(3)
+        if sc.nen == 8:
+            self.lib.orc_q8_node_normal(sc.E, _f(sc.nodes), _u(sc.elems), node0 + 1, n)
+            return n
         self.lib.orc_node_normal(sc.nen, sc.E, _f(sc.nodes), _u(sc.elems), node0 + 1, n)
         return n
 

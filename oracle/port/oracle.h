@@ -119,6 +119,27 @@ int orc_forceMST(int nen, unsigned N, unsigned E, const double *nodes, const uns
 /* Per-element MST integral (src/forceIntegrals.c:632-723). */
 void orc_intF(int nen, const double *X, const double *Enodes, double Int[3]);
 
+/* The quad8 extension (quad8.c; no reference counterpart): element
+ * integrals (X 8 x 3, s the 0-based singular node), node normals, the
+ * assembled rows as orc_assemble forms them, field, potential and
+ * Maxwell-stress force. */
+void orc_q8_shape(double xi, double eta, double N[8], double Nx[8], double Ne[8]);
+double orc_q8_map(const double *X, double xi, double eta, double XL[3], double N[8], double *n);
+void orc_q8_intG(const double *X, const double *Xe, double Int[8]);
+void orc_q8_intH(int flag, const double *X, const double *Xe, double *Int, const double *n);
+void orc_q8_intSingularG(int s, const double *X, const double *Xe, double Int[8]);
+void orc_q8_intSingularH(int flag, int s, const double *X, const double *Xe, double *Int, const double *n);
+void orc_q8_node_normal(unsigned E, const double *nodes, const unsigned *elems, unsigned node1, double n[3]);
+int orc_q8_assemble(int full, unsigned N, unsigned E, unsigned nIf, const double *nodes, const unsigned *elems,
+                    const unsigned *bctype, const unsigned *ifaces, const double *mat, double freq,
+                    const double *mbc, double *A, size_t lda, double *B);
+void orc_q8_field(unsigned N, unsigned E, const double *nodes, const unsigned *elems, const double *vB,
+                  const double *Xin, double mE[6]);
+void orc_q8_potential(unsigned N, unsigned E, const double *nodes, const unsigned *elems, const double *vB,
+                      const double *Xin, double mPot[2]);
+void orc_q8_forceMST(unsigned N, unsigned E, const double *nodes, const unsigned *elems, const unsigned *bctype,
+                     const double *vB, double eps, double *Fce, double *Xce, double Fcm[3], double Xcm[3]);
+
 #ifdef __cplusplus
 }
 #endif
