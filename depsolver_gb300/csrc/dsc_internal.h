@@ -175,8 +175,8 @@ struct Timer {
     };
     std::vector<Rec> recs;
     std::vector<cudaEvent_t> pool;
-    int open_id = -1;
-    cudaEvent_t open_a = nullptr;
+    // scopes begun and not yet ended, innermost last (scopes nest)
+    std::vector<std::pair<int, cudaEvent_t>> open;
     // algorithmic work per id since the last collect (units per id in the
     // C ABI's dsc_session_timing)
     double work[kTCount] = {};
@@ -192,10 +192,6 @@ struct Timer {
     ~Timer();
 };
 
-// Work on a second stream between fork() and done(), joined back into the
-// main stream by join() -- or by the destructor, on every early return, so
-// that nothing queued on the main stream later (a free of a buffer the side
-// work uses) overtakes it.
 // Two events without timing (the look-ahead sequences of the blocked
 // Gauss-Jordan and block LU: one stream signals the other).
 struct EventPair {
@@ -213,6 +209,10 @@ struct EventPair {
     }
 };
 
+// Work on a second stream between fork() and done(), joined back into the
+// main stream by join() -- or by the destructor, on every early return, so
+// that nothing queued on the main stream later (a free of a buffer the side
+// work uses) overtakes it.
 struct SideJoin {
     cudaStream_t main = nullptr;
     cudaEvent_t ev = nullptr;

@@ -408,17 +408,18 @@ cudaEvent_t Timer::take()
 
 void Timer::begin(int id, cudaStream_t st)
 {
-    open_id = id;
-    open_a = take();
-    cudaEventRecord(open_a, st);
+    cudaEvent_t a = take();
+    cudaEventRecord(a, st);
+    open.emplace_back(id, a);
 }
 
 void Timer::end(cudaStream_t st)
 {
+    if (open.empty()) return;
     cudaEvent_t b = take();
     cudaEventRecord(b, st);
-    recs.push_back({open_id, open_a, b});
-    open_id = -1;
+    recs.push_back({open.back().first, open.back().second, b});
+    open.pop_back();
 }
 
 int Timer::collect(double *ms, int *count, double *wk)
@@ -433,8 +434,10 @@ int Timer::collect(double *ms, int *count, double *wk)
         DSC_CUDA(cudaEventSynchronize(r.b));
         float t = 0.0f;
         DSC_CUDA(cudaEventElapsedTime(&t, r.a, r.b));
-        ms[r.id] += t;
-        count[r.id] += 1;
+        if (r.id >= 0 && r.id < kTCount) {
+            ms[r.id] += t;
+            count[r.id] += 1;
+        }
         pool.push_back(r.a);
         pool.push_back(r.b);
     }
@@ -444,6 +447,7 @@ int Timer::collect(double *ms, int *count, double *wk)
 
 Timer::~Timer()
 {
+    for (auto &o : open) pool.push_back(o.second);
     for (auto &r : recs) {
         pool.push_back(r.a);
         pool.push_back(r.b);
