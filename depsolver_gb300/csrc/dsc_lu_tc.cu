@@ -29,6 +29,7 @@
 #include <algorithm>
 #include <vector>
 
+#include "dsc_async.cuh"
 #include "dsc_blas.cuh"
 #include "dsc_common.cuh"
 #include "dsc_gjtile.cuh"
@@ -148,6 +149,146 @@ __global__ void __launch_bounds__(256) k_lu_bwd(const float *__restrict__ W, int
 #pragma unroll 8
     for (int c = 0; c < kPB; c++) s = fmaf(w[(size_t)c * np], xk[c], s);
     z[r] -= s;
+}
+
+// ---- the triangular sweeps in one cooperative launch each (CTA k: tile
+// row k, every CTA resident at once).  A tile's values are published with
+// a release store of the sweep's epoch into its flag; a CTA that needs them
+// waits (thread 0, an acquire load; bounded: after kSpin cycles, or once
+// another CTA has given up, it sets *err and returns) and reads them past
+// L1.  Rows by two threads, on the two halves of each tile's 128 columns.
+
+__device__ __forceinline__ int lu_ld_acquire(const int *p)
+{
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void lu_st_release(int *p, int v)
+{
+    asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Thread 0 waits for flag == epoch; true for the whole CTA when it came.
+__device__ __forceinline__ bool lu_wait(const int *flag, int epoch, int *err, int code)
+{
+    __shared__ int ok;
+    if (threadIdx.x == 0) {
+        const long long t0 = clock64();
+        int good = 1;
+        while (lu_ld_acquire(flag) != epoch) {
+            if (clock64() - t0 > kSpin || *(volatile int *)err) {
+                atomicCAS(err, 0, code);
+                good = 0;
+                break;
+            }
+            __nanosleep(32);
+        }
+        ok = good;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// acc[r] += sum over the 16 columns c0 .. c0+15 of tile column block (at
+// col, leading dimension ld: element (row, c) at col[c * ld + row]) of
+// element (4 lane + r, c) times v[c - c0]: 16 float4 loads issued together.
+// GLOBAL_V: v is a published vector in global memory, read past L1; else v
+// is in shared memory.
+template <bool GLOBAL_V>
+__device__ __forceinline__ void lu_tile_mv16(const float *__restrict__ col, size_t ld, int lane,
+                                             const float *__restrict__ v, float (&acc)[4])
+{
+    float4 w[16];
+#pragma unroll
+    for (int c = 0; c < 16; c++) w[c] = *(const float4 *)(col + (size_t)c * ld + 4 * lane);
+    float x[16];
+#pragma unroll
+    for (int c = 0; c < 16; c += 4) {
+        const float4 q = GLOBAL_V ? __ldcg((const float4 *)(v + c)) : *(const float4 *)(v + c);
+        x[c] = q.x;
+        x[c + 1] = q.y;
+        x[c + 2] = q.z;
+        x[c + 3] = q.w;
+    }
+#pragma unroll
+    for (int c = 0; c < 16; c++) {
+        acc[0] = fmaf(w[c].x, x[c], acc[0]);
+        acc[1] = fmaf(w[c].y, x[c], acc[1]);
+        acc[2] = fmaf(w[c].z, x[c], acc[2]);
+        acc[3] = fmaf(w[c].w, x[c], acc[3]);
+    }
+}
+
+// The 8 column groups' partial sums of rows 4 lane .. 4 lane + 3 (thread
+// group g = threadIdx.x >> 5) summed into out[128] (shared), g order.
+__device__ __forceinline__ void lu_reduce8(const float (&acc)[4], float (*red)[kPB], float *out)
+{
+    const int g = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    *(float4 *)&red[g][4 * lane] = make_float4(acc[0], acc[1], acc[2], acc[3]);
+    __syncthreads();
+    if (threadIdx.x < kPB) {
+        float s = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 8; q++) s += red[q][threadIdx.x];
+        out[threadIdx.x] = s;
+    }
+    __syncthreads();
+}
+
+// Forward: y_k -= sum_{j < k} W_kj z_j as each z_j is published, then
+// z_k = P_k y_k (PT: every step's P transposed), published.  Thread (g,
+// lane): rows 4 lane .. 4 lane + 3 of the tile row, columns 16 g .. 16 g + 15
+// of each tile.
+__global__ void __launch_bounds__(256, 1) k_lu_fwd_all(const float *__restrict__ W, int np,
+                                                    const float *__restrict__ PT, const float *__restrict__ y,
+                                                    float *__restrict__ z, int *flags, int epoch, int *err)
+{
+    __shared__ __align__(16) float red[8][kPB];
+    __shared__ __align__(16) float yk[kPB];
+    const int k = blockIdx.x, g = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    for (int j = 0; j < k; j++) {
+        if (!lu_wait(&flags[j], epoch, err, 11)) return;
+        lu_tile_mv16<true>(W + (size_t)(j * kPB + 16 * g) * np + (size_t)k * kPB, (size_t)np, lane,
+                           z + (size_t)j * kPB + 16 * g, acc);
+    }
+    lu_reduce8(acc, red, yk);
+    if (threadIdx.x < kPB) yk[threadIdx.x] = y[(size_t)k * kPB + threadIdx.x] - yk[threadIdx.x];
+    __syncthreads();
+    float a2[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    lu_tile_mv16<false>(PT + (size_t)k * kPB * kPB + (size_t)(16 * g) * kPB, kPB, lane, yk + 16 * g, a2);
+    lu_reduce8(a2, red, yk);
+    if (threadIdx.x < kPB) z[(size_t)k * kPB + threadIdx.x] = yk[threadIdx.x];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        lu_st_release(&flags[k], epoch);
+    }
+}
+
+// Backward, in place on z: x_k = z_k - sum_{J > k} R_kJ x_J as each x_J is
+// published (R: row block k of W), then x_k published over z_k.
+__global__ void __launch_bounds__(256, 1) k_lu_bwd_all(const float *__restrict__ W, int np, int nb,
+                                                    float *__restrict__ z, int *flags, int epoch, int *err)
+{
+    __shared__ __align__(16) float red[8][kPB];
+    __shared__ __align__(16) float s[kPB];
+    const int k = blockIdx.x, g = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    for (int J = nb - 1; J > k; J--) {
+        if (!lu_wait(&flags[J], epoch, err, 12)) return;
+        lu_tile_mv16<true>(W + (size_t)(J * kPB + 16 * g) * np + (size_t)k * kPB, (size_t)np, lane,
+                           z + (size_t)J * kPB + 16 * g, acc);
+    }
+    lu_reduce8(acc, red, s);
+    if (threadIdx.x < kPB) z[(size_t)k * kPB + threadIdx.x] -= s[threadIdx.x];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        lu_st_release(&flags[k], epoch);
+    }
 }
 
 // y = r / scale (FP32), zero on the padding.
@@ -340,27 +481,67 @@ int lu_solve_mixed(int n, const double *dA, size_t lda, double *dx, double tol, 
     int it = 0, status = 1;  // 1 running, 0 converged, 2 the residual stopped falling
     if (bnorm == 0.0) status = 0;
     const int vg = (np + 255) / 256;
+    // the one-launch sweeps need every tile row's CTA resident at once
+    bool coop = false;
+    DevBuf<int> flags;
+    int epoch = 0;
+    {
+        int dev = 0, can = 0, per = 0, nsm = 0;
+        DSC_CUDA(cudaGetDevice(&dev));
+        DSC_CUDA(cudaDeviceGetAttribute(&can, cudaDevAttrCooperativeLaunch, dev));
+        DSC_TRY(current_sm_count(&nsm));
+        int per_b = 0;
+        DSC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_lu_fwd_all, 256, 0));
+        DSC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_b, k_lu_bwd_all, 256, 0));
+        coop = can && (long long)std::min(per, per_b) * nsm >= nb;
+        if (coop) {
+            DSC_TRY(flags.alloc(nb));
+            DSC_CUDA(cudaMemsetAsync(flags.p, 0, nb * sizeof(int), st));
+        }
+    }
     while (status == 1 && it < kLuMaxRefine) {
         it++;
         // d = LU^-1 (r / |r|) |r|
         DSC_LAUNCH(k_lu_scale_in<<<vg, 256, 0, st>>>(r.p, n, np, rn2, y.p));
-        for (int k = 0; k < nb; k++) {
-            const int rows = np - (k + 1) * kPB;
-            DSC_TRY(launch_dependent(k_lu_fwd, dim3(std::max(1, (rows + 255) / 256)), dim3(256), 0, st,
-                                     (const float *)W.p, np, k, (const float *)P.p, y.p, z.p));
+        if (coop) {
+            // one cooperative launch per sweep, tiles handed on by flags
+            const float *Wc = W.p, *Pc = PT.p, *yc = y.p;
+            float *zc = z.p;
+            int *fl = flags.p, *er = err.p;
+            int ef = ++epoch;
+            void *fa[] = {(void *)&Wc, (void *)&np, (void *)&Pc, (void *)&yc, (void *)&zc, (void *)&fl, (void *)&ef,
+                          (void *)&er};
+            note_launch();
+            DSC_CUDA(cudaLaunchCooperativeKernel((const void *)k_lu_fwd_all, dim3(nb), dim3(256), fa, 0, st));
+            int eb = ++epoch;
+            void *ba[] = {(void *)&Wc, (void *)&np, (void *)&nb, (void *)&zc, (void *)&fl, (void *)&eb, (void *)&er};
+            note_launch();
+            DSC_CUDA(cudaLaunchCooperativeKernel((const void *)k_lu_bwd_all, dim3(nb), dim3(256), ba, 0, st));
+        } else {
+            for (int k = 0; k < nb; k++) {
+                const int rows = np - (k + 1) * kPB;
+                DSC_TRY(launch_dependent(k_lu_fwd, dim3(std::max(1, (rows + 255) / 256)), dim3(256), 0, st,
+                                         (const float *)W.p, np, k, (const float *)P.p, y.p, z.p));
+            }
+            for (int k = nb - 1; k >= 0; k--)
+                if (k > 0)
+                    DSC_TRY(launch_dependent(k_lu_bwd, dim3((k * kPB + 255) / 256), dim3(256), 0, st,
+                                             (const float *)W.p, np, k, z.p));
         }
-        for (int k = nb - 1; k >= 0; k--)
-            if (k > 0)
-                DSC_TRY(launch_dependent(k_lu_bwd, dim3((k * kPB + 255) / 256), dim3(256), 0, st,
-                                         (const float *)W.p, np, k, z.p));
         DSC_LAUNCH(k_lu_update<<<kRedBlocks, kRedThreads, 0, st>>>(dx, z.p, n, rn2, rw, dn2));
         DSC_LAUNCH(k_lu_residual<<<(n * 32 + 255) / 256, 256, 0, st>>>(dA, lda, n, b.p, dx, r.p));
         DSC_LAUNCH(k_lu_dot<<<kRedBlocks, kRedThreads, 0, st>>>(r.p, n, rw, rn2));
         DSC_LAUNCH(k_lu_dot<<<kRedBlocks, kRedThreads, 0, st>>>(dx, n, rw, scal.p + 2));
         DSC_CUDA(cudaGetLastError());
         double hv[3];
+        int herr_s = 0;
         DSC_CUDA(cudaMemcpyAsync(hv, scal.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        if (coop) DSC_CUDA(cudaMemcpyAsync(&herr_s, err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
         DSC_CUDA(cudaStreamSynchronize(st));
+        if (herr_s) {
+            set_error("block LU: a triangular sweep's wait for a tile gave up (code %d)", herr_s);
+            return kErrCuda;
+        }
         const double rnorm = sqrt(hv[0]), dnorm = sqrt(hv[1]), xnorm = sqrt(hv[2]);
         // converged: the residual is below the tolerance or the correction
         // at the rounding level of x (1e-14 |x|); a residual that stops
