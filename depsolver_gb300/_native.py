@@ -45,6 +45,8 @@ def lib() -> C.CDLL:
         L.dsc_gauss.argtypes = [C.c_uint, _dp, C.c_size_t, _dp]
         L.dsc_set_gauss_mode.restype = C.c_int
         L.dsc_set_gauss_mode.argtypes = [C.c_int]
+        L.dsc_set_host_direct.restype = C.c_int
+        L.dsc_set_host_direct.argtypes = [C.c_int]
         L.dsc_gauss_info.restype = C.c_int
         L.dsc_gauss_info.argtypes = [C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_int),
                                      C.c_void_p]

@@ -87,6 +87,12 @@ def gauss_bksb(A: np.ndarray, B: np.ndarray, mode: int | None = None) -> np.ndar
     return x
 
 
+def set_host_direct(on: bool) -> None:
+    """Host matrices read in place by the device where it can (default) or
+    copied through pinned staging (on = False)."""
+    _native.check(_native.lib().dsc_set_host_direct(int(bool(on))))
+
+
 def gauss_info(times: bool = False):
     """(mode, refinement steps, relative residual, fell back to FP64) of the
     last direct solve; with times, also (factorisation ms, refinement ms)

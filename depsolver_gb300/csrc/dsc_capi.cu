@@ -167,6 +167,52 @@ static int rows_to_device(size_t nrows, size_t ldd, double *dst, Fill fill, cuda
     return rc;
 }
 
+// ---------------------------------------------------------------- host rows read by the device
+// On a device that reads pageable host memory through the host's page
+// tables (Grace-Blackwell over NVLink-C2C), the drop-ins' row-pointer
+// matrices go to the device in one gather kernel that reads the caller's
+// rows where they are, instead of host threads copying them into pinned
+// halves first.  dsc_set_host_direct(0) keeps the staged copy.
+static int g_host_direct = 1;
+
+static bool host_direct()
+{
+    if (!g_host_direct) return false;
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return v != 0;
+}
+
+// dst row r (stride ldd) = the caller's row r (rows[r], or flat + r * lda)
+// for r in [r0, r1), and dst[r][ncopy] = extra[r] when extra is not null;
+// a block per row.
+__global__ void k_rows_from_host(const double *const *rows, const double *flat, size_t lda, size_t ncopy,
+                                 const double *extra, double *__restrict__ dst, size_t ldd, size_t r0)
+{
+    const size_t r = r0 + blockIdx.x;
+    const double *src = rows ? rows[r] : flat + r * lda;
+    double *d = dst + r * ldd;
+    for (size_t c = threadIdx.x; c < ncopy; c += blockDim.x) d[c] = src[c];
+    if (extra && threadIdx.x == 0) d[ncopy] = extra[r];
+}
+
+static int rows_from_host(size_t nrows, size_t ncopy, const double *const *rows, const double *flat, size_t lda,
+                          const double *extra, double *dst, size_t ldd, cudaStream_t st)
+{
+    constexpr size_t kChunk = 65535;  // rows per launch (grid limit kept small)
+    for (size_t r0 = 0; r0 < nrows; r0 += kChunk) {
+        const size_t m = std::min(kChunk, nrows - r0);
+        DSC_LAUNCH(k_rows_from_host<<<(unsigned)m, 256, 0, st>>>(rows, flat, lda, ncopy, extra, dst, ldd, r0));
+    }
+    DSC_CUDA(cudaGetLastError());
+    DSC_CUDA(cudaStreamSynchronize(st));
+    return kOk;
+}
+
 static uint64_t mix(uint64_t h, uint64_t v)
 {
     h ^= v + 0x9e3779b97f4a7c15ULL + (h << 6) + (h >> 2);
@@ -300,9 +346,13 @@ static int elems_to0(int nen, int E, const unsigned *elems1, std::vector<int> &o
 // top rows i:    [a_i K_i + d_i e_i | b_i K_i]
 // bottom rows N+i (full only): [-b_i K_i | a_i K_i + d_i e_(N+i)]
 // K is column-major; a 32 x 32 shared tile turns its columns into rows.
+// out: the staging block (rows from r0); or, with hrows or hflat not null,
+// the caller's host rows themselves (rows[r] or hflat + r * hlda), added
+// to in place (a device that reads and writes pageable host memory).
 __global__ void k_form_rows(const double *__restrict__ K, size_t ld, int N, int full, int r0,
                             int r1, const double *__restrict__ ca, const double *__restrict__ cb,
-                            const double *__restrict__ cd, double *__restrict__ out)
+                            const double *__restrict__ cd, double *__restrict__ out,
+                            double *const *hrows = nullptr, double *hflat = nullptr, size_t hlda = 0)
 {
     __shared__ double t[32][33];
     const int c0 = blockIdx.x * 32, rr0 = r0 + blockIdx.y * 32;
@@ -329,9 +379,15 @@ __global__ void k_form_rows(const double *__restrict__ K, size_t ld, int N, int 
             left = -b * kv;
             right = a * kv + (c == i ? d : 0.0);
         }
-        double *o = out + (size_t)(r - r0) * ncol;
-        o[c] = left;
-        o[c + N] = right;
+        if (hrows || hflat) {
+            double *o = hrows ? hrows[r] : hflat + (size_t)r * hlda;
+            o[c] += left;
+            o[c + N] += right;
+        } else {
+            double *o = out + (size_t)(r - r0) * ncol;
+            o[c] = left;
+            o[c + N] = right;
+        }
     }
 }
 
@@ -343,7 +399,7 @@ typedef void (*RowSinkFn)(void *user, int row, const double *vals, size_t n);
 static int assemble_impl(int nen, int full, unsigned N, unsigned E, unsigned nIf,
                          const double *nodes, const int *elems0, const unsigned *bctype,
                          const unsigned *ifaces, const double *mat, double freq, const double *mbc,
-                         RowSinkFn sink, void *user)
+                         RowSinkFn sink, void *user, double *const *drows, double *dflat, size_t dlda)
 {
     cudaStream_t st = ctx().st;
     const size_t ld = ((size_t)N + 31) / 32 * 32;
@@ -393,6 +449,15 @@ static int assemble_impl(int nen, int full, unsigned N, unsigned E, unsigned nIf
 
     const size_t ncol = 2 * (size_t)N;
     const int nrows = full ? 2 * (int)N : (int)N;
+    if ((drows || dflat) && host_direct()) {
+        // the caller's rows take the form in place, read and written by the device
+        dim3 grid(((int)N + 31) / 32, (nrows + 31) / 32), blk(32, 8);
+        DSC_LAUNCH(k_form_rows<<<grid, blk, 0, st>>>(K.p, ld, (int)N, full, 0, nrows, dca.p, dcb.p, dcd.p, nullptr,
+                                                     drows, dflat, dlda));
+        DSC_CUDA(cudaGetLastError());
+        DSC_CUDA(cudaStreamSynchronize(st));
+        return kOk;
+    }
     // chunks of rows formed on the device into one of two staging blocks,
     // copied into one of two pinned halves; the host threads add chunk q - 1
     // into the caller's rows while chunk q is formed and copied
@@ -469,12 +534,16 @@ static int gauss_impl(unsigned n, const double *const *rows, const double *flat,
     DevBuf<double> A;
     DSC_TRY(A.alloc(ldd * n));
     // the rows, with B as column n
-    DSC_TRY(rows_to_device((size_t)n, ldd, A.p,
-                           [&](size_t r, double *dst) {
-                               memcpy(dst, rows ? rows[r] : flat + r * lda, n * sizeof(double));
-                               dst[n] = B[r];
-                           },
-                           st));
+    if (host_direct()) {
+        DSC_TRY(rows_from_host(n, n, rows, flat, lda, B, A.p, ldd, st));
+    } else {
+        DSC_TRY(rows_to_device((size_t)n, ldd, A.p,
+                               [&](size_t r, double *dst) {
+                                   memcpy(dst, rows ? rows[r] : flat + r * lda, n * sizeof(double));
+                                   dst[n] = B[r];
+                               },
+                               st));
+    }
     DevBuf<double> x;
     DSC_TRY(x.alloc(n));
     Context &c = ctx();
@@ -506,11 +575,15 @@ static int gmres_impl(unsigned N, unsigned preCond, double tol, unsigned maxit,
     const size_t ldd = (ncol + 31) / 32 * 32;
     DevBuf<double> A, dB, dx0;
     DSC_TRY(A.alloc(ldd * N));
-    DSC_TRY(rows_to_device((size_t)N, ldd, A.p,
-                           [&](size_t r, double *dst) {
-                               memcpy(dst, rows ? rows[r] : flat + r * lda, ncol * sizeof(double));
-                           },
-                           st));
+    if (host_direct()) {
+        DSC_TRY(rows_from_host(N, ncol, rows, flat, lda, nullptr, A.p, ldd, st));
+    } else {
+        DSC_TRY(rows_to_device((size_t)N, ldd, A.p,
+                               [&](size_t r, double *dst) {
+                                   memcpy(dst, rows ? rows[r] : flat + r * lda, ncol * sizeof(double));
+                               },
+                               st));
+    }
     DSC_TRY(dB.upload(B, ncol, st));
     if (x0) DSC_TRY(dx0.upload(x0, ncol, st));
     int rc = gmres_compact_fp64((int)N, A.p, ldd, dB.p, x0 ? dx0.p : nullptr, preCond, tol, maxit,
@@ -619,7 +692,7 @@ static int electric_form(int nen, int full, double **mNodes, unsigned **mElems, 
     RowPtrSink sink{mA};
     check_or_die(assemble_impl(nen, full, N, E, nIf, f.nodes.data(), f.elems0.data(), vBCType,
                                ifc.data(), mat.data(), vProbParam[0], mbc.data(), add_to_rowptr,
-                               &sink));
+                               &sink, mA, nullptr, 0));
     // right-hand side (src/assembly_el.c:296-298)
     for (unsigned i = 0; i < N; i++) {
         vB[i] = mBC[i][0];
@@ -1034,7 +1107,7 @@ extern "C" int dsc_assemble(int nen, int full, unsigned N, unsigned E, unsigned 
     elems_to0(nen, (int)E, elems, e0);
     FlatSink sink{A, lda};
     DSC_TRY(assemble_impl(nen, full, N, E, nIf, nodes, e0.data(), bctype, ifaces, mat, freq, mbc,
-                          add_to_flat, &sink));
+                          add_to_flat, &sink, nullptr, A, lda));
     for (unsigned i = 0; i < N; i++) {
         B[i] = mbc[3 * (size_t)i];
         B[i + N] = mbc[3 * (size_t)(i + N)];
@@ -1051,6 +1124,13 @@ extern "C" int dsc_gauss(unsigned n, const double *A, size_t lda, double *B)
     }
     int bad = -1;
     return gauss_impl(n, nullptr, A, lda, B, &bad);
+}
+
+extern "C" int dsc_set_host_direct(int on)
+{
+    std::lock_guard<std::mutex> lk(ctx().mu);
+    g_host_direct = on ? 1 : 0;
+    return kOk;
 }
 
 extern "C" int dsc_set_gauss_mode(int mode)

@@ -164,6 +164,13 @@ int dsc_gauss(unsigned n, const double *A, size_t lda, double *B);
 #define DSC_GAUSS_MIXED 0
 #define DSC_GAUSS_FP64 1
 int dsc_set_gauss_mode(int mode);
+
+/* Host matrices of gaussBksb / dsc_gauss and solverGMRES_el / dsc_gmres
+ * (row pointers or flat rows) reach the device through one gather kernel
+ * that reads them in place when the device can read pageable host memory
+ * (Grace-Blackwell, through the host's page tables), else through pinned
+ * staging by host threads.  on = 0 forces the staged copy (default 1). */
+int dsc_set_host_direct(int on);
 int dsc_gauss_info(int *refinements, double *rel_residual, int *fell_back, double *ms);
 
 /* Flat form of solverGMRES_el with the tolerance (relative to |B|, the

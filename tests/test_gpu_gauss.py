@@ -60,3 +60,29 @@ def test_mixed_lu_reports_singular_pivot(gpu):
     with pytest.raises(_native.DscError) as ei:
         api.gauss_bksb(A, np.ones(200), mode=api.GAUSS_FP64)
     assert ei.value.status == 4
+
+
+@pytest.mark.parametrize("n", [129, 1000])
+def test_host_matrix_read_in_place_or_staged(gpu, n):
+    """The host matrix reaches the device read in place by a kernel (where
+    the device reads pageable memory) or staged by host threads: the same
+    bytes either way, so the same solutions."""
+    rng = np.random.default_rng(n)
+    A = rng.standard_normal((n, n)) + n * np.eye(n)
+    b = rng.standard_normal(n)
+    A2 = rng.standard_normal((n // 2, n)) * 0.01
+    A2[:, : n // 2] += np.eye(n // 2) * 3.0
+    b2 = rng.standard_normal(n)
+    try:
+        out = []
+        for on in (True, False):
+            api.set_host_direct(on)
+            x = api.gauss_bksb(A, b, mode=api.GAUSS_MIXED)
+            y, it = api.solver_gmres_el(A2, b2, tol=1e-10)
+            out.append((x, y, it))
+    finally:
+        api.set_host_direct(True)
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1]) and out[0][2] == out[1][2]
+    assert relerr(A @ out[0][0], b) < 1e-13
+

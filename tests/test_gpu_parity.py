@@ -132,6 +132,25 @@ def test_few_point_calls_match_batched_and_follow_the_solution(gpu, port):
         assert relerr(api.field(sc, xs, pts[:5]), port.field(sc, xs, pts[:5])) < SOL_TOL
 
 
+@pytest.mark.parametrize("full", [False, True])
+def test_assembly_rows_in_place_or_staged(gpu, full):
+    """The assembled rows reach the caller's matrix added in place by the
+    device (where it writes pageable host memory) or through pinned staging
+    and host threads: the same values either way, accumulated into what the
+    matrix held."""
+    sc = scenes.small(nen=6)
+    out = []
+    try:
+        for on in (True, False):
+            api.set_host_direct(on)
+            A0 = np.full((2 * sc.N if full else sc.N, 2 * sc.N), 0.25)
+            A, B = api.electric_form(sc, full=full, A=A0)
+            out.append(A.copy())
+    finally:
+        api.set_host_direct(True)
+    assert np.array_equal(out[0], out[1])
+
+
 def test_assembly_accumulates_like_reference(gpu, port):
     sc = scenes.small(nen=3)
     A0 = np.full((sc.N, 2 * sc.N), 0.25)
