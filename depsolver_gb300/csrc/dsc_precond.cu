@@ -296,13 +296,13 @@ int precond_build(Session &s, cudaStream_t main, cudaStream_t aux)
                                    gp[h].rb[q]));
         // Step k on st: the pivot inverses and row blocks of every block,
         // then (after the rest of step k - 1) the cross of tile k + 1 of the
-        // update -- the next pivot tile, row block and column block -- and
-        // on the side stream the rest of the update (after step k's row
-        // blocks), on all but kGjReserveSms SMs, which step k + 1's pivots
-        // and row blocks have to themselves.  A block's last step updates
+        // update -- the next pivot tile, row block and column block -- on
+        // every SM, and after it, on the side stream, the rest of the update
+        // on all but kGjReserveSms SMs, which step k + 1's pivots and row
+        // blocks have to themselves.  A block's last step updates
         // everything on st.  Without a side stream every update is whole.
         const bool la = side != nullptr;
-        EventPair ev;  // a: step k's row blocks are done; b: the rest of the last step is
+        EventPair ev;  // a: step k's cross is done; b: the rest of the last step is
         if (la) DSC_TRY(ev.create());
         int nsm = 0;
         DSC_TRY(current_sm_count(&nsm));
@@ -312,24 +312,28 @@ int precond_build(Session &s, cudaStream_t main, cudaStream_t aux)
             const GJArgs &g = gp[k & 1];
             DSC_TRY(launch_dependent(k_gj_pivot, dim3(nb), dim3(kGjThreads), 0, st, g, nb, k));
             DSC_TRY(launch_dependent(k_gj_row, dim3(nbk_max, 5, nb), dim3(256), rsmem, st, g, nb, k));
-            if (la) {
-                DSC_CUDA(cudaEventRecord(ev.a, st));
-                if (rest_pending) DSC_CUDA(cudaStreamWaitEvent(st, ev.b, 0));
-            }
-            bool any_rest = false;
+            if (rest_pending) DSC_CUDA(cudaStreamWaitEvent(st, ev.b, 0));
+            // the blocks' updates in one launch per kind: split into cross
+            // and rest, or (a block's last step) whole
+            const TcGjPlan *sp[kPreMaxBlocks], *wp[kPreMaxBlocks];
+            int ns = 0, nw = 0;
             for (int q = 0; q < nb; q++) {
                 if (k >= ga.nbk[q]) continue;
-                const TcGjPlan &pl = plans[2 * q + (k & 1)];
-                if (la && k + 1 < ga.nbk[q]) {
-                    DSC_TRY(tc_gj_run(pl, k, st, 1, k + 1));
-                    if (!any_rest) DSC_CUDA(cudaStreamWaitEvent(side, ev.a, 0));
-                    DSC_TRY(tc_gj_run(pl, k, side, 2, k + 1, rest_ctas));
-                    any_rest = true;
-                } else {
-                    DSC_TRY(tc_gj_run(pl, k, st));
-                }
+                const TcGjPlan *pl = &plans[2 * q + (k & 1)];
+                if (la && k + 1 < ga.nbk[q]) sp[ns++] = pl;
+                else wp[nw++] = pl;
             }
-            if (any_rest) DSC_CUDA(cudaEventRecord(ev.b, side));
+            constexpr int G = kTcGjMaxProblems;
+            for (int i = 0; i < ns; i += G) DSC_TRY(tc_gj_run_batch(sp + i, std::min(G, ns - i), k, st, 1, k + 1));
+            for (int i = 0; i < nw; i += G) DSC_TRY(tc_gj_run_batch(wp + i, std::min(G, nw - i), k, st));
+            const bool any_rest = ns > 0;
+            if (any_rest) {
+                DSC_CUDA(cudaEventRecord(ev.a, st));
+                DSC_CUDA(cudaStreamWaitEvent(side, ev.a, 0));
+                for (int i = 0; i < ns; i += G)
+                    DSC_TRY(tc_gj_run_batch(sp + i, std::min(G, ns - i), k, side, 2, k + 1, rest_ctas));
+                DSC_CUDA(cudaEventRecord(ev.b, side));
+            }
             rest_pending = any_rest;
         }
         if (rest_pending) DSC_CUDA(cudaStreamWaitEvent(st, ev.b, 0));

@@ -93,12 +93,13 @@ int Session::create(int nen_, unsigned N_, unsigned E_, const double *nodes, con
     E = (int)E_;
     nIf = nIf_;
     DSC_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-    DSC_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
     {
         // side2 runs the conductor-block inverses' chain of small dependent
-        // kernels: it goes first whenever SMs free up
+        // kernels and side the rest of their updates, beside K's conversion
+        // on st: they go first whenever SMs free up
         int least = 0, greatest = 0;
         DSC_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        DSC_CUDA(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, greatest));
         DSC_CUDA(cudaStreamCreateWithPriority(&side2, cudaStreamNonBlocking, greatest));
     }
     AllocStreamScope as(st);

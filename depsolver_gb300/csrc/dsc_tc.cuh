@@ -26,6 +26,35 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, u
         : "memory");
 }
 
+// 2-D TMA store of the box at (x, y) from shared src (the tensor map's box
+// layout); out-of-range parts of the box are not written.  The caller
+// fences its generic writes to src (fence.proxy.async.shared::cta) first.
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, const void *src, int x, int y)
+{
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];" ::"l"(
+                     (uint64_t)map),
+                 "r"(su32(src)), "r"(x), "r"(y)
+                 : "memory");
+}
+
+// Prefetch of the box at (x, y) into L2 (no shared memory, no completion).
+__device__ __forceinline__ void tma_prefetch_2d(const CUtensorMap *map, int x, int y)
+{
+    asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global [%0, {%1, %2}];" ::"l"((uint64_t)map), "r"(x), "r"(y)
+                 : "memory");
+}
+
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+
+// this thread's committed bulk stores have read their shared sources
+__device__ __forceinline__ void bulk_wait_read0()
+{
+    asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+
+// this thread's committed bulk stores are complete
+__device__ __forceinline__ void bulk_wait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
 // Shared-memory matrix descriptor of a K-major tile in the swizzled
 // canonical layout: rows of kTcRowBytes bytes (the swizzle width), 8-row
 // groups 8 rows apart.
@@ -100,21 +129,8 @@ __device__ __forceinline__ void tc_fence_after()
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
-// 32 consecutive accumulator columns of this warp's 32 TMEM lanes.
-// 16 consecutive accumulator columns of this warp's 32 TMEM lanes (one per
-// thread), waited for.
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t *r)
-{
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-          "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-}
-
+// 32 consecutive accumulator columns of this warp's 32 TMEM lanes, waited
+// for.
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t *r)
 {
     asm volatile(

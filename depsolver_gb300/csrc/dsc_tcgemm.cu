@@ -17,7 +17,8 @@
 // k) u = blockIdx.x, + gridDim.x, ...  Warp 0 lane 0 streams k-blocks (one
 // 128-byte swizzle row: 32 tf32 or 64 fp16 values) of A and Bh, Bl into a
 // 3-stage shared-memory ring with TMA (128B swizzle) without pausing between
-// units; warps 2-5 split a plain FP32 A in shared memory; warp 1 lane 0
+// units (the Gauss-Jordan update: one stage, and the old values of its
+// tiles in a ring of their own); warps 2-5 split a plain FP32 A in shared memory; warp 1 lane 0
 // issues tcgen05.mma (M = 128, 32 bytes of k per instruction: K = 8 tf32 or
 // K = 16 fp16) into one of two FP32 accumulator buffers in tensor memory and
 // releases each stage with tcgen05.commit; warps 6-9 read the finished
@@ -57,6 +58,17 @@ constexpr long long kTcSpin = kSpin;  // clock cycles before a wait gives up
 // columns (3 stages of a 16 KB A tile and a 48 KB B tile)
 constexpr int kTcDigitKBlocks = 64;
 constexpr int kTcMaxDigitCols = 384;
+// The Gauss-Jordan update (rank 128 on 128 x 128 tiles: two k-blocks per
+// unit) keeps one stage of operands and a ring of kGjXSlots half tiles (128
+// rows x 64 columns, FP32) of the old values, which the producer fetches by
+// TMA when it starts a unit; each epilogue warp rewrites its 32 x 64 box in
+// place and stores it back by TMA.  Four slots are two units: the old
+// values of the next unit stream in while this one is formed.
+constexpr int kGjStages = 1;
+constexpr int kGjXSlots = 4;
+constexpr int kGjXBoxRows = 32, kGjXBoxCols = 64;
+constexpr uint32_t kGjXBoxBytes = kGjXBoxRows * kGjXBoxCols * 4;
+constexpr uint32_t kGjXHalfBytes = 4 * kGjXBoxBytes;
 
 // The tf32 value the tensor core reads from an FP32 word: the top 19 bits
 // (the low 13 mantissa bits are ignored).
@@ -170,20 +182,17 @@ __host__ __device__ inline int gj_sel_units(int tiles, int ntn, int sel, int la,
     return sel == 1 ? ntn + nr : nr * (ntn - 1);
 }
 
-template <int AMODE, bool GJ = false>
+template <int AMODE>
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_tc_gemm3(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
                const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl,
                int M, int Nc, int BN, int ntn, int nkb_total, int kb_per_split, int nsplit,
                float *__restrict__ Y, size_t ldy, size_t split_stride, int tmem_cols,
                uint32_t acc_stride, const float *__restrict__ rsc, const float *__restrict__ csc,
-               int gj_k, int gj_sel, int gj_la, int *err)
+               int *err)
 {
     grid_dep_wait();  // launched as a programmatic dependent of the kernel before
-    // ntn: column tiles of BN columns (1 unless the product is the
-    // Gauss-Jordan update); GJ selects that update's epilogue with gj_k:
-    // Y[column][row] -= the product (Y = -the product in column tile gj_k),
-    // row tile gj_k left alone.
+    // ntn: column tiles of BN columns
     // acc_stride: TMEM columns of one accumulator buffer, a power of two of
     // at least the columns it holds (so each buffer's MMAs start aligned)
     constexpr bool SPLIT_A = AMODE == 1 || AMODE == 2;
@@ -208,9 +217,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     uint32_t *tmem_slot = (uint32_t *)(done + 1);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int tiles = (M + kTcBM - 1) / kTcBM;
-    // unit u: row tile u % tiles, then column tile, then split (the
-    // Gauss-Jordan update: one split, tiles by unit_tile)
-    const int units = GJ && gj_sel ? gj_sel_units(tiles, ntn, gj_sel, gj_la, gj_k) : tiles * ntn * nsplit;
+    // unit u: row tile u % tiles, then column tile, then split
+    const int units = tiles * ntn * nsplit;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < kTcStages; s++) {
@@ -220,9 +228,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
         for (int b = 0; b < 2; b++) {
             mbar_init(&acc_full[b], 1);
-            // one lane of each epilogue warp (the Gauss-Jordan update's
-            // read-modify-write epilogue also runs on the splitter warps)
-            mbar_init(&acc_empty[b], GJ ? 4 + kTcSplitWarps : 4);
+            mbar_init(&acc_empty[b], 4);  // one lane of each epilogue warp
         }
         mbar_init(done, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -247,10 +253,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             uint32_t g = 0;
             bool ok = true;
             for (int u = blockIdx.x; ok && u < units; u += gridDim.x) {
-                int tmu, tnu;
-                unit_tile(u, tiles, ntn, GJ ? gj_sel : 0, gj_la, gj_k, tmu, tnu);
-                const int m0 = tmu * kTcBM, n0 = tnu * BN;
-                const int kb0 = GJ ? 0 : (u / tiles / ntn) * kb_per_split;
+                const int m0 = (u % tiles) * kTcBM, n0 = ((u / tiles) % ntn) * BN;
+                const int kb0 = (u / tiles / ntn) * kb_per_split;
                 const int nkb = min(nkb_total, kb0 + kb_per_split) - kb0;
                 for (int i = 0; i < nkb; i++, g++) {
                     const uint32_t s = g % kTcStages, n = g / kTcStages;
@@ -274,11 +278,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             }
             // drain: the last loads of every stage have landed before the CTA
             // may exit (immediate in the normal path, bounded otherwise)
-            for (uint32_t h = g > (uint32_t)kTcStages ? g - kTcStages : 0; h < g; h++) {
-                const long long t0 = clock64();
-                while (!mbar_try(&full[h % kTcStages], (h / kTcStages) & 1) && clock64() - t0 < kTcSpin) {
-                }
-            }
+            for (uint32_t h = g > (uint32_t)kTcStages ? g - kTcStages : 0; h < g; h++)
+                mbar_drain(&full[h % kTcStages], (h / kTcStages) & 1);
         }
     } else if (warp == 1) {
         if (lane == 0) {
@@ -289,7 +290,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             bool ok = true;
             int j = 0;
             for (int u = blockIdx.x; ok && u < units; u += gridDim.x, j++) {
-                const int kb0 = GJ ? 0 : (u / tiles / ntn) * kb_per_split;
+                const int kb0 = (u / tiles / ntn) * kb_per_split;
                 const int nkb = min(nkb_total, kb0 + kb_per_split) - kb0;
                 const uint32_t buf = j % nbuf, q = j / nbuf;
                 if (q > 0 && !mbar_wait(&acc_empty[buf], (q - 1) & 1, err, 5)) break;
@@ -350,7 +351,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             }
             mma_commit(done);  // arrives when every MMA issued above has completed
         }
-    } else if (warp < 2 + kTcSplitWarps && !GJ) {
+    } else if (warp < 2 + kTcSplitWarps) {
         if (SPLIT_A) {
             // ---- splitters: the lo slot of each stage
             const int tid = threadIdx.x - 64;
@@ -391,47 +392,22 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
     } else {
         // ---- epilogue (the last 4 warps: TMEM lanes 32 (warp % 4) .. + 31 =
-        // rows; for the Gauss-Jordan update warps 2 .. 9, two per lane
-        // group, each on half of the tile's columns)
-        static_assert(kTcSplitWarps == 4, "the Gauss-Jordan epilogue pairs the splitter and epilogue warps");
+        // rows)
         const int ew = warp & 3;
-        const int cbeg = GJ && warp >= 2 + kTcSplitWarps ? BN / 2 : 0;
-        const int cend = GJ && warp < 2 + kTcSplitWarps ? BN / 2 : BN;
         int j = 0;
         for (int u = blockIdx.x; u < units; u += gridDim.x, j++) {
-            int tm, tn;
-            unit_tile(u, tiles, ntn, GJ ? gj_sel : 0, gj_la, gj_k, tm, tn);
-            const int split = GJ ? 0 : u / tiles / ntn;
-            const int m0 = tm * kTcBM, n0 = tn * BN;
+            const int split = u / tiles / ntn;
+            const int m0 = (u % tiles) * kTcBM, n0 = ((u / tiles) % ntn) * BN;
             const uint32_t buf = j % nbuf, q = j / nbuf;
             bool have = mbar_wait(&acc_full[buf], q & 1, err, 3);
             // tcgen05.ld is warp-collective: the whole warp reads or none of it
             if (!__all_sync(0xffffffffu, have)) break;
             tc_fence_after();
-            if (GJ) {
-                // the old values of this warp's rows and columns of the next
-                // unit (and, before the first, of this one) into L2 while
-                // the accumulator is formed or written back: lane t asks for
-                // column cbeg + t (and + 32), 32 rows (128 bytes) each
-                for (int u2 = j ? u + gridDim.x : u; u2 <= u + (int)gridDim.x && u2 < units; u2 += gridDim.x) {
-                    int tm2, tn2;
-                    unit_tile(u2, tiles, ntn, gj_sel, gj_la, gj_k, tm2, tn2);
-                    const int r0 = tm2 * kTcBM + ew * 32;
-                    if (tm2 != gj_k && tn2 != gj_k && r0 < M) {
-#pragma unroll
-                        for (int h = 0; h < 64; h += 32) {
-                            const int n = tn2 * BN + cbeg + h + lane;
-                            if (cbeg + h + lane < cend && n < Nc)
-                                asm volatile("prefetch.global.L2 [%0];" ::"l"(Y + (size_t)n * ldy + r0));
-                        }
-                    }
-                }
-            }
             const uint32_t acc = tmem + ((uint32_t)(ew * 32) << 16) + buf * acc_stride;
             const int m = m0 + ew * 32 + lane;
             const float rs = (rsc && m < M) ? rsc[m] : 1.0f;
             float *Ys = Y + (size_t)split * split_stride;
-            for (int c0 = cbeg; c0 < cend; c0 += 32) {
+            for (int c0 = 0; c0 < BN; c0 += 32) {
                 uint32_t r[32];
                 tmem_ld32(acc + (uint32_t)c0, r);
                 if (comb) {
@@ -440,7 +416,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
                     for (int t = 0; t < 32; t++) r[t] = __float_as_uint(__uint_as_float(r[t]) + __uint_as_float(r2[t]));
                 }
-                if (m < M && !GJ) {
+                if (m < M) {
 #pragma unroll
                     for (int t = 0; t < 32; t++) {
                         const int n = n0 + c0 + t;
@@ -448,26 +424,6 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                             // powers of two: the scaling is exact
                             const float cn = csc ? csc[n] : 1.0f;
                             Ys[(size_t)n * ldy + m] = __uint_as_float(r[t]) * rs * cn;
-                        }
-                    }
-                } else if (m < M && tm != gj_k) {
-                    // 16 old values at a time first (independent loads in
-                    // flight together), then their stores
-#pragma unroll
-                    for (int h = 0; h < 32; h += 16) {
-                        float old[16];
-#pragma unroll
-                        for (int t = 0; t < 16; t++) {
-                            const int n = n0 + c0 + h + t;
-                            old[t] = (n < Nc && tn != gj_k) ? Ys[(size_t)n * ldy + m] : 0.0f;
-                        }
-#pragma unroll
-                        for (int t = 0; t < 16; t++) {
-                            const int n = n0 + c0 + h + t;
-                            if (n < Nc) {
-                                const float cn = csc ? csc[n] : 1.0f;
-                                Ys[(size_t)n * ldy + m] = old[t] - __uint_as_float(r[h + t]) * rs * cn;
-                            }
                         }
                     }
                 }
@@ -493,6 +449,276 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tmem_cols)
                      : "memory");
+}
+
+// ------------------------------------------------ the Gauss-Jordan update
+//
+// C -= A B^T on 128 x 128 tiles of up to kTcGjMaxProblems column-major FP32
+// matrices C in one launch (rank 128: A = the old column block, B = the
+// row block, scaled fp16 pairs, 3xFP16 with the two Ah products in one
+// MMA of N = 256); per problem: row tile gk left alone, column tile gk
+// overwritten with -A B^T, tiles chosen by sel / la (unit_tile).  The units
+// of the problems follow one another; one persistent CTA per SM walks them.
+// Warp 0 lane 0 streams each unit's old values into a ring of kGjXSlots
+// half tiles (TMA, 4 boxes of 32 rows x 64 columns each) and its two
+// k-blocks of operands through one stage; warp 1 lane 0 issues the MMAs
+// into one of two TMEM accumulators; warps 2 .. 9 (two per TMEM lane
+// group, one per half of the columns) rewrite their 32 x 64 box of old
+// values in shared memory and store it back by TMA.
+
+struct TcGjProblem {
+    CUtensorMap ah, al, bh, bl, c;  // A, B: rows x 128 k; c: the matrix in 32 x 64 boxes
+    float *C;
+    const float *rsc, *csc;  // power-of-two row scales of A and B
+    int M, Nc, tiles, ntn;
+    int gk, sel, la, units;
+};
+
+struct TcGjBatch {
+    TcGjProblem p[kTcGjMaxProblems];
+    int np, units;
+};
+
+// problem and tiles of unit u of the batch
+__device__ __forceinline__ const TcGjProblem &gj_locate(const TcGjBatch &B, int u, int &tm, int &tn)
+{
+    int pi = 0;
+    while (pi + 1 < B.np && u >= B.p[pi].units) u -= B.p[pi++].units;
+    const TcGjProblem &P = B.p[pi];
+    unit_tile(u, P.tiles, P.ntn, P.sel, P.la, P.gk, tm, tn);
+    return P;
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1) k_tc_gj(const __grid_constant__ TcGjBatch B, int *err)
+{
+    grid_dep_wait();  // launched as a programmatic dependent of the kernel before
+    constexpr int BN = 128;
+    constexpr uint32_t a_bytes = kTcBM * kTcRowBytes, b_bytes = BN * kTcRowBytes;
+    constexpr uint32_t stage_bytes = 2 * a_bytes + 2 * b_bytes;
+    constexpr uint32_t acc_stride = 2 * BN;  // Ah [Bh | Bl] in [0, 2 BN); Al Bh added to [BN, 2 BN)
+    constexpr int nkb = 128 / kTcBK16;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t *xbuf = smem + kGjStages * stage_bytes;
+    uint64_t *full = (uint64_t *)(xbuf + kGjXSlots * kGjXHalfBytes);
+    uint64_t *empty = full + kGjStages;
+    uint64_t *acc_full = empty + kGjStages;  // [2]
+    uint64_t *acc_empty = acc_full + 2;      // [2]
+    uint64_t *done = acc_empty + 2;
+    uint64_t *xfull = done + 1;            // [kGjXSlots]
+    uint64_t *xempty = xfull + kGjXSlots;  // [kGjXSlots]
+    uint32_t *tmem_slot = (uint32_t *)(xempty + kGjXSlots);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int units = B.units;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kGjStages; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; b++) {
+            mbar_init(&acc_full[b], 1);
+            mbar_init(&acc_empty[b], 8);  // one lane of each epilogue warp
+        }
+        mbar_init(done, 1);
+        for (int s = 0; s < kGjXSlots; s++) {
+            mbar_init(&xfull[s], 1);
+            mbar_init(&xempty[s], 4);  // the four warps on that half of the columns
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         su32(tmem_slot)),
+                     "r"(512)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    // Every role walks the same units u = blockIdx.x, + gridDim.x, ...; g
+    // counts k-blocks (stage g % kGjStages), xh half-tile slot uses (slot
+    // xh % kGjXSlots; unit j of this CTA takes uses 2 j and 2 j + 1).
+    if (warp == 0) {
+        if (lane == 0) {
+            // ---- producer
+            uint32_t g = 0, xh = 0;
+            bool ok = true;
+            for (int u = blockIdx.x; ok && u < units; u += gridDim.x) {
+                int tm, tn;
+                const TcGjProblem &P = gj_locate(B, u, tm, tn);
+                const int m0 = tm * kTcBM, n0 = tn * BN;
+                // the old values (none in row tile gk, which stays, nor in
+                // column tile gk, which is overwritten)
+                const bool old = tm != P.gk && tn != P.gk;
+                for (int h = 0; h < 2; h++, xh++) {
+                    const uint32_t s = xh % kGjXSlots, n = xh / kGjXSlots;
+                    if (n > 0 && !mbar_wait(&xempty[s], (n - 1) & 1, err, 6)) {
+                        ok = false;
+                        break;
+                    }
+                    if (!old) {
+                        mbar_arrive(&xfull[s]);
+                        continue;
+                    }
+                    uint8_t *xb = xbuf + s * kGjXHalfBytes;
+                    mbar_expect_tx(&xfull[s], kGjXHalfBytes);
+                    for (int r = 0; r < 4; r++)
+                        tma_load_2d(xb + r * kGjXBoxBytes, &P.c, &xfull[s], m0 + r * kGjXBoxRows, n0 + h * kGjXBoxCols);
+                }
+                if (!ok) break;
+                // and those of the unit after it into L2
+                if (u + (int)gridDim.x < units) {
+                    int tm2, tn2;
+                    const TcGjProblem &P2 = gj_locate(B, u + (int)gridDim.x, tm2, tn2);
+                    if (tm2 != P2.gk && tn2 != P2.gk)
+                        for (int b = 0; b < 8; b++)
+                            tma_prefetch_2d(&P2.c, tm2 * kTcBM + (b & 3) * kGjXBoxRows, tn2 * BN + (b >> 2) * kGjXBoxCols);
+                }
+                for (int i = 0; i < nkb; i++, g++) {
+                    const uint32_t s = g % kGjStages, n = g / kGjStages;
+                    if (n > 0 && !mbar_wait(&empty[s], (n - 1) & 1, err, 1)) {
+                        ok = false;
+                        break;
+                    }
+                    uint8_t *st = smem + s * stage_bytes;
+                    mbar_expect_tx(&full[s], stage_bytes);
+                    const int kx = i * kTcBK16;
+                    tma_load_2d(st, &P.ah, &full[s], kx, m0);
+                    tma_load_2d(st + a_bytes, &P.al, &full[s], kx, m0);
+                    tma_load_2d(st + 2 * a_bytes, &P.bh, &full[s], kx, n0);
+                    tma_load_2d(st + 2 * a_bytes + b_bytes, &P.bl, &full[s], kx, n0);
+                }
+            }
+            // drain: the last loads of every stage and slot have landed
+            // before the CTA may exit (immediate in the normal path, bounded
+            // otherwise)
+            for (uint32_t h = g > (uint32_t)kGjStages ? g - kGjStages : 0; h < g; h++)
+                mbar_drain(&full[h % kGjStages], (h / kGjStages) & 1);
+            for (uint32_t h = xh > (uint32_t)kGjXSlots ? xh - kGjXSlots : 0; h < xh; h++)
+                mbar_drain(&xfull[h % kGjXSlots], (h / kGjXSlots) & 1);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            // ---- MMA issuer
+            const uint32_t idesc = idesc_f16(BN, kTcBM), idesc2 = idesc_f16(2 * BN, kTcBM);
+            uint32_t g = 0;
+            bool ok = true;
+            int j = 0;
+            for (int u = blockIdx.x; ok && u < units; u += gridDim.x, j++) {
+                const uint32_t buf = j & 1, q = j >> 1;
+                if (q > 0 && !mbar_wait(&acc_empty[buf], (q - 1) & 1, err, 5)) break;
+                tc_fence_after();
+                const uint32_t acc = tmem + buf * acc_stride;
+                for (int i = 0; i < nkb; i++, g++) {
+                    const uint32_t s = g % kGjStages, n = g / kGjStages;
+                    if (!mbar_wait(&full[s], n & 1, err, 2)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    uint8_t *st = smem + s * stage_bytes;
+                    const uint64_t dah = sw_desc(st), dal = sw_desc(st + a_bytes);
+                    const uint64_t dbh = sw_desc(st + 2 * a_bytes);
+#pragma unroll
+                    for (int kk = 0; kk < kTcRowBytes / 32; kk++) {
+                        // 32 bytes of k per MMA (16 fp16): Ah against Bh and
+                        // the adjacent Bl, then Al against Bh
+                        const uint64_t off = (uint64_t)(kk * 32) >> 4;
+                        mma_op<true>(acc, dah + off, dbh + off, idesc2, (i | kk) != 0);
+                    }
+#pragma unroll
+                    for (int kk = 0; kk < kTcRowBytes / 32; kk++) {
+                        const uint64_t off = (uint64_t)(kk * 32) >> 4;
+                        mma_op<true>(acc + BN, dal + off, dbh + off, idesc, 1);
+                    }
+                    mma_commit(&empty[s]);
+                }
+                if (ok) mma_commit(&acc_full[buf]);
+            }
+            mma_commit(done);  // arrives when every MMA issued above has completed
+        }
+    } else {
+        // ---- epilogue (warps 2 .. 9: TMEM lanes 32 (warp % 4) .. + 31 =
+        // rows, the first four on columns 0 .. 63, the others on 64 .. 127):
+        // C = old - the product (-the product in column tile gk), row tile
+        // gk left alone.  The warp's 32 x 64 box of the unit's half-tile
+        // slot is column-major (a column's 32 rows are 128 contiguous
+        // bytes, lane = row); the TMA store drops rows >= M and columns >=
+        // Nc.
+        const int ew = warp & 3, hh = warp >= 6 ? 1 : 0;
+        const int cbeg = hh * kGjXBoxCols;
+        int j = 0;
+        for (int u = blockIdx.x; u < units; u += gridDim.x, j++) {
+            int tm, tn;
+            const TcGjProblem &P = gj_locate(B, u, tm, tn);
+            const int m0 = tm * kTcBM, n0 = tn * BN;
+            const uint32_t buf = j & 1, q = j >> 1;
+            const uint32_t xs = (2 * j + hh) % kGjXSlots, xn = (2 * j + hh) / kGjXSlots;
+            // the row's scale and (lane t) those of columns t and t + 32 of
+            // this half, read before the waits
+            const int m = m0 + ew * 32 + lane;
+            const float rs = (P.rsc && m < P.M) ? P.rsc[m] : 1.0f;
+            float cl[2];
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int n = n0 + cbeg + 32 * h + lane;
+                cl[h] = (P.csc && n < P.Nc) ? P.csc[n] : 1.0f;
+            }
+            bool have = mbar_wait(&acc_full[buf], q & 1, err, 3);
+            have = have && mbar_wait(&xfull[xs], xn & 1, err, 7);
+            // tcgen05.ld is warp-collective: the whole warp reads or none of it
+            if (!__all_sync(0xffffffffu, have)) break;
+            tc_fence_after();
+            if (tm != P.gk) {
+                float *xw = (float *)(xbuf + xs * kGjXHalfBytes + ew * kGjXBoxBytes) + lane;
+                const uint32_t acc = tmem + ((uint32_t)(ew * 32) << 16) + buf * acc_stride;
+                const bool keep = tn != P.gk;
+#pragma unroll
+                for (int c0 = 0; c0 < kGjXBoxCols; c0 += 32) {
+                    uint32_t r[32], r2[32];
+                    tmem_ld32(acc + (uint32_t)(cbeg + c0), r);
+                    tmem_ld32(acc + (uint32_t)(BN + cbeg + c0), r2);
+#pragma unroll
+                    for (int t = 0; t < 32; t++) {
+                        // powers of two: the scaling is exact
+                        const float cn = __shfl_sync(0xffffffffu, cl[c0 / 32], t);
+                        const float v = (__uint_as_float(r[t]) + __uint_as_float(r2[t])) * rs * cn;
+                        float *x = xw + (c0 + t) * kGjXBoxRows;
+                        *x = (keep ? *x : 0.0f) - v;
+                    }
+                }
+                // the box's generic writes before the TMA engine reads it
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) {
+                    tma_store_2d(&P.c, xw, m0 + ew * kGjXBoxRows, n0 + cbeg);
+                    bulk_commit();
+                    bulk_wait_read0();  // the slot may be refilled once the store has read it
+                }
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) {
+                mbar_arrive(&acc_empty[buf]);
+                mbar_arrive(&xempty[xs]);
+            }
+        }
+        if (lane == 0) bulk_wait0();  // the stores are complete before the CTA exits
+    }
+    __syncwarp();
+    if (warp == 0) {
+        // every MMA has completed before the accumulator memory is freed
+        if (lane == 0) mbar_drain(done, 0);
+        __syncwarp();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
 }
 
 // ---------------------------------------------------------------- host
@@ -545,6 +771,35 @@ static int make_map(CUtensorMap *map, const void *base, int esize, int rows, int
     return kOk;
 }
 
+// Column-major FP32 matrix (rows x cols, entry (r, c) at c * ld + r) in
+// unswizzled boxes of box_rows x box_cols (rows innermost); loads fill zeros
+// outside, stores drop what falls outside.
+static int make_box_map(CUtensorMap *map, const float *base, int rows, int cols, size_t ld, int box_rows,
+                        int box_cols)
+{
+    auto fn = encode_fn();
+    if (!fn) {
+        set_error("cuTensorMapEncodeTiled is not available");
+        return kErrCuda;
+    }
+    if (((uintptr_t)base & 15) || ((ld * 4) & 15)) {
+        set_error("TMA matrix not 16-byte aligned (base and column stride)");
+        return kErrArg;
+    }
+    cuuint64_t dims[2] = {(cuuint64_t)rows, (cuuint64_t)cols};
+    cuuint64_t strides[1] = {(cuuint64_t)(ld * 4)};
+    cuuint32_t box[2] = {(cuuint32_t)box_rows, (cuuint32_t)box_cols};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)base, dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+        return kErrCuda;
+    }
+    return kOk;
+}
+
 int tc_make_map(CUtensorMap *map, const void *base, int esize, int rows, int k, size_t ld, int box_rows)
 {
     return make_map(map, base, esize, rows, k, ld, box_rows);
@@ -572,12 +827,11 @@ static int splits_for_bk(int M, int Kd, int bk)
 // Launch of the persistent kernel on encoded maps (bk: elements per k-block).
 static int tc_launch(int amode, const CUtensorMap &ah, const CUtensorMap &al, const CUtensorMap &bh,
                      const CUtensorMap &bl, int M, int Nc, int Kd, int bk, float *Y, size_t ldy, int splits,
-                     int *d_err, cudaStream_t st, const float *rsc, const float *csc, int gj_k = -1,
-                     int gj_sel = 0, int gj_la = 0, int max_ctas = 0)
+                     int *d_err, cudaStream_t st, const float *rsc, const float *csc)
 {
-    // one column tile of all Nc columns, or tiles of 128 (the Gauss-Jordan
-    // update); above 256 columns (digits) a multiple of 32 (two halves)
-    int BN = gj_k >= 0 ? 128 : (Nc + 15) / 16 * 16;
+    // one column tile of all Nc columns; above 256 columns (digits) a
+    // multiple of 32 (two halves)
+    int BN = (Nc + 15) / 16 * 16;
     if (BN > 256) BN = (Nc + 31) / 32 * 32;
     const int ntn = (Nc + BN - 1) / BN;
     // two accumulator buffers of 2 BN (COMB) or BN columns, each rounded up
@@ -593,23 +847,18 @@ static int tc_launch(int amode, const CUtensorMap &ah, const CUtensorMap &al, co
     // persistent: one CTA per SM walks the (row tile, split) units
     int nsm = 0;
     DSC_TRY(current_sm_count(&nsm));
-    const int units = gj_k >= 0 && gj_sel ? gj_sel_units((M + kTcBM - 1) / kTcBM, ntn, gj_sel, gj_la, gj_k)
-                                          : (M + kTcBM - 1) / kTcBM * ntn * splits;
-    if (units < 1) return kOk;
-    // max_ctas > 0: at most that many CTAs (SMs left for other streams)
-    const dim3 grid(std::min(units, max_ctas > 0 ? std::min(max_ctas, nsm) : nsm));
+    const int units = (M + kTcBM - 1) / kTcBM * ntn * splits;
+    const dim3 grid(std::min(units, nsm));
     // the shared-memory limit of each instantiation is raised to the largest
     // request seen on the device (once per size, not per launch)
     auto launch = [&](auto kern, int slot) -> int {
         (void)slot;
         DSC_TRY(raise_smem_limit((const void *)kern, (int)smem));
         DSC_TRY(launch_dependent(kern, grid, dim3(kTcThreads), smem, st, ah, al, bh, bl, M, Nc, BN, ntn, nkb, kps,
-                                 splits, Y, ldy, ldy * (size_t)Nc, tmem_cols, acc_stride, rsc, csc, gj_k, gj_sel,
-                                 gj_la, d_err));
+                                 splits, Y, ldy, ldy * (size_t)Nc, tmem_cols, acc_stride, rsc, csc, d_err));
         return kOk;
     };
-    if (gj_k >= 0) DSC_TRY(launch(k_tc_gemm3<3, true>, 4));
-    else switch (amode) {
+    switch (amode) {
     case 0: DSC_TRY(launch(k_tc_gemm3<0>, 0)); break;
     case 1: DSC_TRY(launch(k_tc_gemm3<1>, 1)); break;
     case 2: DSC_TRY(launch(k_tc_gemm3<2>, 2)); break;
@@ -679,7 +928,7 @@ int tc_digit_splits(int Kd)
 }
 
 struct TcGjPlan::Maps {
-    CUtensorMap ah, al, bh, bl;
+    TcGjProblem pr;  // the maps, matrix and scales; the step's fields set per launch
 };
 
 TcGjPlan::~TcGjPlan() { delete maps; }
@@ -693,10 +942,19 @@ int tc_gj_plan(TcGjPlan &p, const __half *Ah, const __half *Al, size_t lda, cons
         return kErrArg;
     }
     if (!p.maps) p.maps = new TcGjPlan::Maps();
-    DSC_TRY(make_map(&p.maps->ah, Ah, 2, M, 128, lda, kTcBM));
-    DSC_TRY(make_map(&p.maps->al, Al, 2, M, 128, lda, kTcBM));
-    DSC_TRY(make_map(&p.maps->bh, Bh, 2, Nc, 128, ldb, 128));
-    DSC_TRY(make_map(&p.maps->bl, Bl, 2, Nc, 128, ldb, 128));
+    TcGjProblem &pr = p.maps->pr;
+    DSC_TRY(make_map(&pr.ah, Ah, 2, M, 128, lda, kTcBM));
+    DSC_TRY(make_map(&pr.al, Al, 2, M, 128, lda, kTcBM));
+    DSC_TRY(make_map(&pr.bh, Bh, 2, Nc, 128, ldb, 128));
+    DSC_TRY(make_map(&pr.bl, Bl, 2, Nc, 128, ldb, 128));
+    DSC_TRY(make_box_map(&pr.c, C, M, Nc, ldc, kGjXBoxRows, kGjXBoxCols));
+    pr.C = C;
+    pr.rsc = rsc;
+    pr.csc = csc;
+    pr.M = M;
+    pr.Nc = Nc;
+    pr.tiles = (M + kTcBM - 1) / kTcBM;
+    pr.ntn = (Nc + 127) / 128;
     p.M = M;
     p.Nc = Nc;
     p.C = C;
@@ -707,19 +965,47 @@ int tc_gj_plan(TcGjPlan &p, const __half *Ah, const __half *Al, size_t lda, cons
     return kOk;
 }
 
+int tc_gj_run_batch(const TcGjPlan *const *plans, int np, int k, cudaStream_t st, int sel, int la, int max_ctas)
+{
+    if (np < 1 || np > kTcGjMaxProblems || k < 0 || sel < 0 || sel > 2) {
+        set_error("tc_gj_run: %d problems (at most %d), step %d, tile selection %d", np, kTcGjMaxProblems, k, sel);
+        return kErrArg;
+    }
+    TcGjBatch B{};
+    B.np = np;
+    for (int q = 0; q < np; q++) {
+        const TcGjPlan &p = *plans[q];
+        if (!p.maps || p.err != plans[0]->err) {
+            set_error("tc_gj_run: problem %d has no plan or another error word", q);
+            return kErrArg;
+        }
+        TcGjProblem &pr = B.p[q];
+        pr = p.maps->pr;
+        if (sel && (la < 0 || la >= pr.tiles || la >= pr.ntn || la == k)) {
+            set_error("tc_gj_run: look-ahead tile %d outside the update", la);
+            return kErrArg;
+        }
+        pr.gk = k;
+        pr.sel = sel;
+        pr.la = la;
+        pr.units = gj_sel_units(pr.tiles, pr.ntn, sel, la, k);
+        B.units += pr.units;
+    }
+    if (B.units < 1) return kOk;
+    int nsm = 0;
+    DSC_TRY(current_sm_count(&nsm));
+    const dim3 grid(std::min(B.units, max_ctas > 0 ? std::min(max_ctas, nsm) : nsm));
+    const size_t smem = 1024 + (size_t)kGjStages * 4 * kTcBM * kTcRowBytes + (size_t)kGjXSlots * kGjXHalfBytes + 256;
+    DSC_TRY(raise_smem_limit((const void *)k_tc_gj, (int)smem));
+    DSC_TRY(launch_dependent(k_tc_gj, grid, dim3(kTcThreads), smem, st, B, plans[0]->err));
+    DSC_CUDA(cudaGetLastError());
+    return kOk;
+}
+
 int tc_gj_run(const TcGjPlan &p, int k, cudaStream_t st, int sel, int la, int max_ctas)
 {
-    if (!p.maps || k < 0 || sel < 0 || sel > 2) {
-        set_error("tc_gj_run: no plan, negative step or bad tile selection");
-        return kErrArg;
-    }
-    const int tiles = (p.M + kTcBM - 1) / kTcBM, ntn = (p.Nc + 127) / 128;
-    if (sel && (la < 0 || la >= tiles || la >= ntn || la == k)) {
-        set_error("tc_gj_run: look-ahead tile %d outside the update", la);
-        return kErrArg;
-    }
-    return tc_launch(3, p.maps->ah, p.maps->al, p.maps->bh, p.maps->bl, p.M, p.Nc, 128, kTcBK16, p.C, p.ldc, 1,
-                     p.err, st, p.rsc, p.csc, k, sel, la, max_ctas);
+    const TcGjPlan *pl = &p;
+    return tc_gj_run_batch(&pl, 1, k, st, sel, la, max_ctas);
 }
 
 int tc_gemm_splits_for(int M, int Kd) { return splits_for_bk(M, Kd, kTcBK); }

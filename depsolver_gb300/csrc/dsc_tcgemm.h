@@ -64,11 +64,12 @@ int tc_digit_splits(int Kd);
 // values, rows x k (k contiguous, row stride ld elements, 16-byte aligned),
 // boxes of one 128-byte swizzle row of k by box_rows rows, zero fill.
 int tc_make_map(CUtensorMap *map, const void *base, int esize, int rows, int k, size_t ld, int box_rows);
-// The Gauss-Jordan update of step k on the same kernel (3xFP16, K = 128):
-// for every 128 x 128 tile (I, J) of C (column-major, M x Nc, stride ldc)
-// with I != k: C_IJ -= A_I B_J^T (C_Ik = -A_I B_k^T); A (M x 128) and B
-// (Nc x 128) K-major scaled fp16 pairs with row factors rsc, csc.  The
-// operands' tensor maps are encoded once (tc_gj_plan) for all steps.
+// The Gauss-Jordan update of step k (3xFP16, K = 128): for every 128 x 128
+// tile (I, J) of C (column-major, M x Nc, stride ldc a multiple of 4, C
+// 16-byte aligned) with I != k: C_IJ -= A_I B_J^T (C_Ik = -A_I B_k^T); A
+// (M x 128) and B (Nc x 128) K-major scaled fp16 pairs with row factors
+// rsc, csc.  The tensor maps are encoded once (tc_gj_plan) for all steps.
+constexpr int kTcGjMaxProblems = 4;
 struct TcGjPlan {
     struct Maps;
     Maps *maps = nullptr;
@@ -92,6 +93,10 @@ int tc_gj_plan(TcGjPlan &p, const __half *Ah, const __half *Al, size_t lda, cons
 // persistent grid (below the SM count: SMs left for kernels of other
 // streams).
 int tc_gj_run(const TcGjPlan &p, int k, cudaStream_t st, int sel = 0, int la = 0, int max_ctas = 0);
+// The same step of up to kTcGjMaxProblems plans (sharing one error word) in
+// one launch.
+int tc_gj_run_batch(const TcGjPlan *const *plans, int np, int k, cudaStream_t st, int sel = 0, int la = 0,
+                    int max_ctas = 0);
 // Row scales of column-major FP64 K (stride ld): rowE (N ints) the biased
 // exponent of each row's largest entry, rsK = 2^-s_i.
 int k16_row_scales(const double *K, size_t ld, int N, int *rowE, float *rsK, cudaStream_t st);
