@@ -431,8 +431,15 @@ int precond_reserve(Session &s, int F)
     pc.boff.clear();
     size_t yo = 0, bo = 0;
     std::vector<long long> info;
+    // splits: about two waves of units over all blocks' products (more
+    // splits cost partial tiles written and summed; fewer leave SMs idle)
+    int nsm = 0;
+    DSC_TRY(current_sm_count(&nsm));
+    int tiles = 0;
+    for (int b = 0; b < pc.nb; b++) tiles += (pc.n[b] + kPB - 1) / kPB;
     for (int b = 0; b < pc.nb; b++) {
-        const int S = tc_gemm_f16_splits_for(pc.n[b], pc.n[b]);
+        const int nkb = (pc.n[b] + 63) / 64;  // fp16 k-blocks
+        const int S = tc_gemm_f16_splits_norm(pc.n[b], std::max(1, std::min(2 * nsm / tiles, nkb / 4)));
         pc.S.push_back(S);
         pc.yoff.push_back(yo);
         pc.boff.push_back(bo);
