@@ -87,10 +87,11 @@ def gauss_bksb(A: np.ndarray, B: np.ndarray, mode: int | None = None) -> np.ndar
     return x
 
 
-def set_host_direct(on: bool) -> None:
-    """Host matrices read in place by the device where it can (default) or
-    copied through pinned staging (on = False)."""
-    _native.check(_native.lib().dsc_set_host_direct(int(bool(on))))
+def set_host_direct(mode: int) -> None:
+    """Host matrices read in place by the device where it can (mode 1, the
+    default), the assembled rows also written in place (2), or every copy
+    through pinned staging (0)."""
+    _native.check(_native.lib().dsc_set_host_direct(int(mode)))
 
 
 def gauss_info(times: bool = False):

@@ -172,12 +172,16 @@ static int rows_to_device(size_t nrows, size_t ldd, double *dst, Fill fill, cuda
 // tables (Grace-Blackwell over NVLink-C2C), the drop-ins' row-pointer
 // matrices go to the device in one gather kernel that reads the caller's
 // rows where they are, instead of host threads copying them into pinned
-// halves first.  dsc_set_host_direct(0) keeps the staged copy.
+// halves first (mode 1, the default).  Mode 2 also adds the assembled rows
+// into the caller's rows from the device; on the 12k-node scene that took
+// 0.12 to 0.59 s from one box and run to the next for 5 GB of rows (the
+// device's first writes to the caller's pages), the staged copy a steady
+// 0.18 s, so it is not the default.  Mode 0: staged both ways.
 static int g_host_direct = 1;
 
-static bool host_direct()
+static bool host_direct(bool write)
 {
-    if (!g_host_direct) return false;
+    if (g_host_direct < (write ? 2 : 1)) return false;
     int dev = 0, v = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) {
@@ -449,7 +453,7 @@ static int assemble_impl(int nen, int full, unsigned N, unsigned E, unsigned nIf
 
     const size_t ncol = 2 * (size_t)N;
     const int nrows = full ? 2 * (int)N : (int)N;
-    if ((drows || dflat) && host_direct()) {
+    if ((drows || dflat) && host_direct(true)) {
         // the caller's rows take the form in place, read and written by the device
         dim3 grid(((int)N + 31) / 32, (nrows + 31) / 32), blk(32, 8);
         DSC_LAUNCH(k_form_rows<<<grid, blk, 0, st>>>(K.p, ld, (int)N, full, 0, nrows, dca.p, dcb.p, dcd.p, nullptr,
@@ -534,7 +538,7 @@ static int gauss_impl(unsigned n, const double *const *rows, const double *flat,
     DevBuf<double> A;
     DSC_TRY(A.alloc(ldd * n));
     // the rows, with B as column n
-    if (host_direct()) {
+    if (host_direct(false)) {
         DSC_TRY(rows_from_host(n, n, rows, flat, lda, B, A.p, ldd, st));
     } else {
         DSC_TRY(rows_to_device((size_t)n, ldd, A.p,
@@ -575,7 +579,7 @@ static int gmres_impl(unsigned N, unsigned preCond, double tol, unsigned maxit,
     const size_t ldd = (ncol + 31) / 32 * 32;
     DevBuf<double> A, dB, dx0;
     DSC_TRY(A.alloc(ldd * N));
-    if (host_direct()) {
+    if (host_direct(false)) {
         DSC_TRY(rows_from_host(N, ncol, rows, flat, lda, nullptr, A.p, ldd, st));
     } else {
         DSC_TRY(rows_to_device((size_t)N, ldd, A.p,
@@ -1126,10 +1130,14 @@ extern "C" int dsc_gauss(unsigned n, const double *A, size_t lda, double *B)
     return gauss_impl(n, nullptr, A, lda, B, &bad);
 }
 
-extern "C" int dsc_set_host_direct(int on)
+extern "C" int dsc_set_host_direct(int mode)
 {
+    if (mode < 0 || mode > 2) {
+        set_error("dsc_set_host_direct: mode %d (0, 1 or 2)", mode);
+        return kErrArg;
+    }
     std::lock_guard<std::mutex> lk(ctx().mu);
-    g_host_direct = on ? 1 : 0;
+    g_host_direct = mode;
     return kOk;
 }
 

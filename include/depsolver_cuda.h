@@ -169,8 +169,11 @@ int dsc_set_gauss_mode(int mode);
  * (row pointers or flat rows) reach the device through one gather kernel
  * that reads them in place when the device can read pageable host memory
  * (Grace-Blackwell, through the host's page tables), else through pinned
- * staging by host threads.  on = 0 forces the staged copy (default 1). */
-int dsc_set_host_direct(int on);
+ * staging by host threads.  mode 0: staged copies both ways; 1 (default):
+ * host matrices read in place, the assembled rows of electricFormA_* /
+ * dsc_assemble staged; 2: the assembled rows also added into the caller's
+ * rows by the device.  Every mode gives the same bytes. */
+int dsc_set_host_direct(int mode);
 int dsc_gauss_info(int *refinements, double *rel_residual, int *fell_back, double *ms);
 
 /* Flat form of solverGMRES_el with the tolerance (relative to |B|, the

@@ -75,13 +75,13 @@ def test_host_matrix_read_in_place_or_staged(gpu, n):
     b2 = rng.standard_normal(n)
     try:
         out = []
-        for on in (True, False):
-            api.set_host_direct(on)
+        for mode in (1, 0):
+            api.set_host_direct(mode)
             x = api.gauss_bksb(A, b, mode=api.GAUSS_MIXED)
             y, it = api.solver_gmres_el(A2, b2, tol=1e-10)
             out.append((x, y, it))
     finally:
-        api.set_host_direct(True)
+        api.set_host_direct(1)
     assert np.array_equal(out[0][0], out[1][0])
     assert np.array_equal(out[0][1], out[1][1]) and out[0][2] == out[1][2]
     assert relerr(A @ out[0][0], b) < 1e-13

@@ -141,13 +141,13 @@ def test_assembly_rows_in_place_or_staged(gpu, full):
     sc = scenes.small(nen=6)
     out = []
     try:
-        for on in (True, False):
-            api.set_host_direct(on)
+        for mode in (2, 0):
+            api.set_host_direct(mode)
             A0 = np.full((2 * sc.N if full else sc.N, 2 * sc.N), 0.25)
             A, B = api.electric_form(sc, full=full, A=A0)
             out.append(A.copy())
     finally:
-        api.set_host_direct(True)
+        api.set_host_direct(1)
     assert np.array_equal(out[0], out[1])
 
 
