@@ -413,8 +413,7 @@ int dsc_tc_gemm(int M, int Nc, int Kd, const double *A, const double *B, double 
  * Y is written, with the status of the kernels' bounded waits.  The first
  * call on each device also looks up the scratch's address
  * (cudaGetSymbolAddress) and keeps it: make that first call during set-up,
- * before any stream capture begins, and do not call again on a device after
- * cudaDeviceReset.  All calls on a device share its scratch, so two calls
+ * and do not call again on a device after cudaDeviceReset.  All calls on a device share its scratch, so two calls
  * that overlapped would race on it; the library prevents that with a
  * process-wide lock held until a call's work has finished. */
 #define DSC_NOALLOC_SCRATCH_BYTES 33554432u /* 32 MiB */
