@@ -19,6 +19,7 @@
 #include "dsc_df32.cuh"
 #include "dsc_internal.h"
 #include "dsc_singular.cuh"
+#include "dsc_singular_df.cuh"
 
 namespace dsc {
 
@@ -645,15 +646,27 @@ __global__ void __launch_bounds__(128) k_asm_singular(const double *__restrict__
             Xe[k][2] = Z[v];
         }
         double g[4 * NEN];  // FLAG 2: out's values, then the gradient
-        if (kind == 0) {
-            warp_singular_G<NEN, FAST>(s, Xe, xe, out);
-            if (grad) warp_singular_H<NEN, 1, FAST>(s, Xe, xe, n, g + NEN);
+        if (FAST) {
+            // the mixed mode: double-FP32 on the FP32 pipes
+            if (kind == 0) {
+                warp_singular_G_df<NEN>(s, Xe, xe, out);
+                if (grad) warp_singular_H_df<NEN, 1>(s, Xe, xe, n, g + NEN);
+            } else if (grad) {
+                warp_singular_H_df<NEN, 2>(s, Xe, xe, n, g);
+#pragma unroll
+                for (int k = 0; k < NEN; k++) out[k] = g[k];
+            } else {
+                warp_singular_H_df<NEN, 0>(s, Xe, xe, n, out);
+            }
+        } else if (kind == 0) {
+            warp_singular_G<NEN, false>(s, Xe, xe, out);
+            if (grad) warp_singular_H<NEN, 1, false>(s, Xe, xe, n, g + NEN);
         } else if (grad) {
-            warp_singular_H<NEN, 2, FAST>(s, Xe, xe, n, g);
+            warp_singular_H<NEN, 2, false>(s, Xe, xe, n, g);
 #pragma unroll
             for (int k = 0; k < NEN; k++) out[k] = g[k];
         } else {
-            warp_singular_H<NEN, 0, FAST>(s, Xe, xe, n, out);
+            warp_singular_H<NEN, 0, false>(s, Xe, xe, n, out);
         }
         if (lane == 0) {
 #pragma unroll
