@@ -1306,30 +1306,49 @@ int x_digits(const double *X, size_t ldx, int N, int ncol, __half *Xd, size_t ld
 // j < nj of 2^(kXDigitBits (kXDigits - 1 - j)) * (the S partial tiles of the
 // product of K digit i with x digit j; column j * ncol + c of the tiles).
 // The tiles hold integers below 2^24: they are summed as integers (exact),
-// then added in FP64.
+// then added in FP64.  Four rows per thread (ldp a multiple of 4: float4
+// loads, all S nj of them issued before the sums).
 __global__ void k_digit_accumulate(const float *__restrict__ P, int S, size_t ldp, int ncol, int nj, int i,
                                    int N, double *__restrict__ Y, size_t ldy, int first)
 {
     grid_dep_wait();  // a programmatic dependent of the digit product
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    const int m0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
     const int c = blockIdx.y;
-    if (m >= N) return;
+    if (m0 >= N) return;
     const size_t split_stride = ldp * (size_t)(nj * ncol);
-    long long t = 0;
+    long long t[4] = {0, 0, 0, 0};
     for (int j = 0; j < nj; j++) {
-        int s = 0;
-        for (int k = 0; k < S; k++) s += __float2int_rn(P[k * split_stride + (size_t)(j * ncol + c) * ldp + m]);
-        t += (long long)s * (1ll << (kXDigitBits * (kXDigits - 1 - j)));
+        int sum[4] = {0, 0, 0, 0};
+        const float *pj = P + (size_t)(j * ncol + c) * ldp + m0;
+#pragma unroll 4
+        for (int k = 0; k < S; k++) {
+            const float4 v = __ldg((const float4 *)(pj + k * split_stride));
+            sum[0] += __float2int_rn(v.x);
+            sum[1] += __float2int_rn(v.y);
+            sum[2] += __float2int_rn(v.z);
+            sum[3] += __float2int_rn(v.w);
+        }
+        const long long w = 1ll << (kXDigitBits * (kXDigits - 1 - j));
+#pragma unroll
+        for (int r = 0; r < 4; r++) t[r] += (long long)sum[r] * w;
     }
-    const double v = ldexp((double)t, kKDigitBits * (kKDigits - 1 - i));
-    double *y = Y + (size_t)c * ldy + m;
-    *y = first ? v : *y + v;
+    double *y = Y + (size_t)c * ldy + m0;
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        if (m0 + r >= N) break;
+        const double v = ldexp((double)t[r], kKDigitBits * (kKDigits - 1 - i));
+        y[r] = first ? v : y[r] + v;
+    }
 }
 
 int digit_accumulate(const float *P, int S, size_t ldp, int ncol, int nj, int i, int N, double *Y, size_t ldy,
                      bool first, cudaStream_t st)
 {
-    dim3 g((N + 255) / 256, ncol);
+    if (ldp % 4 || ((uintptr_t)P & 15)) {
+        set_error("digit_accumulate: the partial tiles' stride must be a multiple of 4 floats, 16-byte aligned");
+        return kErrArg;
+    }
+    dim3 g((N + 1023) / 1024, ncol);
     DSC_TRY(launch_dependent(k_digit_accumulate, g, dim3(256), 0, st, P, S, ldp, ncol, nj, i, N, Y, ldy,
                              first ? 1 : 0));
     DSC_CUDA(cudaGetLastError());
@@ -1488,16 +1507,18 @@ int f32_to_tf32_pair(const float *x, float *h, float *l, size_t n, cudaStream_t 
     return kOk;
 }
 
-// Y[n * ldy + m] (FP64, column n) += the S partial tiles, in split order.
+// Y[n * ldy + m] (FP64, column n) += the S partial tiles, in split order,
+// summed in double-FP32 (about 2^-48 of the largest partial; the FP64 pipe
+// only for the final addition).
 __global__ void k_add_splits(const float *__restrict__ P, int S, size_t split_stride, size_t ldp,
                              int M, double *__restrict__ Y, size_t ldy)
 {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = blockIdx.y;
     if (m >= M) return;
-    double s = 0.0;
-    for (int k = 0; k < S; k++) s += (double)P[(size_t)k * split_stride + (size_t)n * ldp + m];
-    Y[(size_t)n * ldy + m] += s;
+    float2 s = make_float2(0.0f, 0.0f);
+    for (int k = 0; k < S; k++) s = df_add(s, make_float2(P[(size_t)k * split_stride + (size_t)n * ldp + m], 0.0f));
+    Y[(size_t)n * ldy + m] += df_to(s);
 }
 
 int add_splits(const float *P, int S, size_t split_stride, size_t ldp, int M, int Nc, double *Y,
