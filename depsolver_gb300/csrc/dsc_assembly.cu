@@ -606,8 +606,8 @@ __global__ void k_asm_fixup(const int *__restrict__ fix_ptr, const int *__restri
 // sums, 3 NEN per tuple t of ne_ptr's numbering) at Wg + t * 3 NEN: the
 // field's singular part at that node, taken from the same points as the
 // row's H integral.  FAST: the singular quadrature's points from the
-// polynomial element map and 1/r^3 by rsqrt (the mixed mode); else summed
-// as the reference sums them (the FP64 mode).
+// polynomial element map and 1/r^3 by rsqrt; else summed as the reference
+// sums them (the FP64 mode).  The mixed mode takes k_asm_singular_df.
 template <int NEN, typename T, bool FAST>
 __global__ void __launch_bounds__(128) k_asm_singular(const double *__restrict__ X,
                                                       const double *__restrict__ Y,
@@ -646,27 +646,15 @@ __global__ void __launch_bounds__(128) k_asm_singular(const double *__restrict__
             Xe[k][2] = Z[v];
         }
         double g[4 * NEN];  // FLAG 2: out's values, then the gradient
-        if (FAST) {
-            // the mixed mode: double-FP32 on the FP32 pipes
-            if (kind == 0) {
-                warp_singular_G_df<NEN>(s, Xe, xe, out);
-                if (grad) warp_singular_H_df<NEN, 1>(s, Xe, xe, n, g + NEN);
-            } else if (grad) {
-                warp_singular_H_df<NEN, 2>(s, Xe, xe, n, g);
-#pragma unroll
-                for (int k = 0; k < NEN; k++) out[k] = g[k];
-            } else {
-                warp_singular_H_df<NEN, 0>(s, Xe, xe, n, out);
-            }
-        } else if (kind == 0) {
-            warp_singular_G<NEN, false>(s, Xe, xe, out);
-            if (grad) warp_singular_H<NEN, 1, false>(s, Xe, xe, n, g + NEN);
+        if (kind == 0) {
+            warp_singular_G<NEN, FAST>(s, Xe, xe, out);
+            if (grad) warp_singular_H<NEN, 1, FAST>(s, Xe, xe, n, g + NEN);
         } else if (grad) {
-            warp_singular_H<NEN, 2, false>(s, Xe, xe, n, g);
+            warp_singular_H<NEN, 2, FAST>(s, Xe, xe, n, g);
 #pragma unroll
             for (int k = 0; k < NEN; k++) out[k] = g[k];
         } else {
-            warp_singular_H<NEN, 0, false>(s, Xe, xe, n, out);
+            warp_singular_H<NEN, 0, FAST>(s, Xe, xe, n, out);
         }
         if (lane == 0) {
 #pragma unroll
@@ -680,6 +668,88 @@ __global__ void __launch_bounds__(128) k_asm_singular(const double *__restrict__
         }
         __syncwarp();
     }
+}
+
+// k_asm_singular<NEN, double, true> in double-FP32 (the mixed mode): node
+// coordinates and normals from Xd / Nd (double-FP32, 3 per node), the
+// integrals by warp_singular_G_df / warp_singular_H_df; lane k adds output
+// k into K (FP64) and stores gradient entry k, so that each pair takes one
+// FP64 operation per lane.
+template <int NEN>
+__global__ void __launch_bounds__(128) k_asm_singular_df(const float2 *__restrict__ Xd,
+                                                         const float2 *__restrict__ Nd,
+                                                         const int *__restrict__ row_kind,
+                                                         const double *__restrict__ row_fac,
+                                                         const int *__restrict__ elems,
+                                                         const int *__restrict__ ne_ptr,
+                                                         const int *__restrict__ ne_elem,
+                                                         const int *__restrict__ ne_pos, int row_lo, int row_hi,
+                                                         double *__restrict__ K, size_t ld,
+                                                         const int *__restrict__ row_grad, double *__restrict__ Wg)
+{
+    const int i = row_lo + (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (i >= row_hi) return;
+    const bool grad = row_grad && row_grad[i];
+    const float2 xe[3] = {Xd[3 * (size_t)i], Xd[3 * (size_t)i + 1], Xd[3 * (size_t)i + 2]};
+    const float2 nd[3] = {Nd[3 * (size_t)i], Nd[3 * (size_t)i + 1], Nd[3 * (size_t)i + 2]};
+    const int kind = row_kind[i];
+    const double fac = kind == 0 ? row_fac[i] : 1.0;  // as in k_asm_singular
+    for (int t = ne_ptr[i]; t < ne_ptr[i + 1]; t++) {
+        const int e = ne_elem[t], s = ne_pos[t] + 1;
+        float2 Xe[NEN][3];
+        int v[NEN];
+#pragma unroll
+        for (int k = 0; k < NEN; k++) {
+            v[k] = elems[(size_t)e * NEN + k];
+#pragma unroll
+            for (int d = 0; d < 3; d++) Xe[k][d] = Xd[3 * (size_t)v[k] + d];
+        }
+        float2 g[4 * NEN];  // out's values, then the gradient
+        if (kind == 0) {
+            warp_singular_G_df<NEN>(s, Xe, xe, g);
+            if (grad) warp_singular_H_df<NEN, 1>(s, Xe, xe, nd, g + NEN);
+        } else if (grad) {
+            warp_singular_H_df<NEN, 2>(s, Xe, xe, nd, g);
+        } else {
+            warp_singular_H_df<NEN, 0>(s, Xe, xe, nd, g);
+        }
+        // every lane holds every sum: lane k takes value k
+        float2 mine = g[0];
+        int dst = v[0];
+#pragma unroll
+        for (int k = 1; k < NEN; k++)
+            if (lane == k) {
+                mine = g[k];
+                dst = v[k];
+            }
+        if (lane < NEN) {
+            double *o = K + (size_t)dst * ld + i;
+            *o += fac * df_to(mine);
+        }
+        if (grad) {
+            float2 gj = g[NEN];
+#pragma unroll
+            for (int j = 1; j < 3 * NEN; j++)
+                if (lane == j) gj = g[NEN + j];
+            if (lane < 3 * NEN) Wg[(size_t)t * 3 * NEN + lane] = df_to(gj);
+        }
+        __syncwarp();
+    }
+}
+
+// Xd, Nd = the node coordinates and normals in double-FP32 (3 per node).
+__global__ void k_nodes_df(const double *__restrict__ X, const double *__restrict__ Y,
+                           const double *__restrict__ Z, const double *__restrict__ normals, int N,
+                           float2 *__restrict__ Xd, float2 *__restrict__ Nd)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    Xd[3 * (size_t)i] = df_from(X[i]);
+    Xd[3 * (size_t)i + 1] = df_from(Y[i]);
+    Xd[3 * (size_t)i + 2] = df_from(Z[i]);
+#pragma unroll
+    for (int d = 0; d < 3; d++) Nd[3 * (size_t)i + d] = df_from(normals[3 * (size_t)i + d]);
 }
 
 static size_t regular_smem(int nen)
@@ -731,6 +801,12 @@ static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStr
     AsmArgs a{m.x.p, m.y.p, m.z.p, m.normals.p, m.row_fac.p, m.qp.p, m.row_kind.p, m.elems.p,
               m.grp_elem.p, m.fp_ptr.p, m.fp_dest.p, m.fp_sl_ptr.p, m.fp_sl.p, m.N, 0, 0, ld,
               (size_t)rc};
+    if (prec != kAsmF64) {
+        // the singular pairs' nodes and normals in double-FP32
+        DSC_TRY(w.nodes_df.alloc((size_t)m.N * 6));
+        DSC_LAUNCH(k_nodes_df<<<(m.N + 255) / 256, 256, 0, st>>>(m.x.p, m.y.p, m.z.p, m.normals.p, m.N,
+                                                                w.nodes_df.p, w.nodes_df.p + 3 * (size_t)m.N));
+    }
     for (int lo = 0; lo < m.N; lo += rc) {
         int hi = std::min(m.N, lo + rc);
         a.row_lo = lo;
@@ -765,10 +841,16 @@ static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStr
         }
         int warps = hi - lo;
         TimerScope ts(tm, kTAsmSingular, st);
-        auto sing = prec == kAsmF64 ? k_asm_singular<NEN, double, false> : k_asm_singular<NEN, double, true>;
-        DSC_LAUNCH(sing<<<(warps * 32 + 127) / 128, 128, 0, st>>>(
-            m.x.p, m.y.p, m.z.p, m.normals.p, m.row_kind.p, m.row_fac.p, m.elems.p, m.ne_ptr.p,
-            m.ne_elem.p, m.ne_pos.p, lo, hi, K, ld, Wg ? row_grad : nullptr, Wg));
+        if (prec == kAsmF64) {
+            DSC_LAUNCH(k_asm_singular<NEN, double, false><<<(warps * 32 + 127) / 128, 128, 0, st>>>(
+                m.x.p, m.y.p, m.z.p, m.normals.p, m.row_kind.p, m.row_fac.p, m.elems.p, m.ne_ptr.p,
+                m.ne_elem.p, m.ne_pos.p, lo, hi, K, ld, Wg ? row_grad : nullptr, Wg));
+        } else {
+            // the mixed mode: double-FP32 on the FP32 pipes
+            DSC_LAUNCH(k_asm_singular_df<NEN><<<(warps * 32 + 127) / 128, 128, 0, st>>>(
+                w.nodes_df.p, w.nodes_df.p + 3 * (size_t)m.N, m.row_kind.p, m.row_fac.p, m.elems.p, m.ne_ptr.p,
+                m.ne_elem.p, m.ne_pos.p, lo, hi, K, ld, Wg ? row_grad : nullptr, Wg));
+        }
         DSC_CUDA(cudaGetLastError());
     }
     // a local workspace is released at scope exit: wait for the kernels

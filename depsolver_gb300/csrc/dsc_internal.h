@@ -332,6 +332,7 @@ struct AsmWorkspace {
     DevBuf<float2> cen;
     DevBuf<float4> qloc;
     DevBuf<unsigned char> rows;  // per-row FP32 data of the FP32 assembly
+    DevBuf<float2> nodes_df;     // node coordinates, then normals, in double-FP32 (singular pairs)
 };
 
 // Arithmetic of the regular pairs, most accurate first: FP64 (the

@@ -6,10 +6,14 @@
 // |J| / r^k from one reciprocal square root), taken in double-FP32 (a
 // 48-bit significand, dsc_df32.cuh): about 1e-13 of the FP64 values, at a
 // fraction of the FP64 pipe's time (the FP32 pipes issue 64 times as many
-// operations per clock on sm_103a).  Each pair is evaluated in coordinates
-// scaled by a power of two near the element's size, so that r^6 J^2 stays
-// inside FP32's exponent range for meshes in any unit; G comes back times
-// that power of two, H and the gradient are scale-free.
+// operations per clock on sm_103a).  The node coordinates and normals come
+// in double-FP32 (converted once per assembly), the element's polynomial is
+// formed from them in double-FP32, and the sums go back in double-FP32
+// (every lane holds them): nothing per point or per pair runs on the FP64
+// pipe.  Each pair is evaluated in coordinates scaled by a power of two
+// near the element's size, so that r^6 J^2 stays inside FP32's exponent
+// range for meshes in any unit; G comes back times that power of two, H
+// and the gradient are scale-free.
 #pragma once
 
 #include "dsc_common.cuh"
@@ -83,31 +87,50 @@ __device__ __forceinline__ float2 df_ld(const DfC &c)
     return v;
 }
 
-// Power of two near the element's size (from its first tangent), as the
-// factor s = 2^-e that brings the pair's coordinates to order one.
-template <int NEN>
-__device__ __forceinline__ double sing_scale(const ElemMap<NEN> &em)
-{
-    const double h = fabs(em.k1[0]) + fabs(em.k1[1]) + fabs(em.k1[2]);
-    int e = 0;
-    frexp(h > 0.0 ? h : 1.0, &e);
-    return ldexp(1.0, -e);
-}
-
-// ElemMap's polynomial in double-FP32, scaled by s.
+// ElemMap's polynomial in double-FP32 from the nodes in double-FP32,
+// scaled by sc, a power of two near the element's size (from its first
+// tangent: the factor that brings the pair's coordinates to order one).
 template <int NEN>
 struct ElemMapDf {
-    float2 k1[3], k2[3], d11[3], k12[3], d22[3];
-    __device__ __forceinline__ void init(const ElemMap<NEN> &em, double s)
+    float2 k0[3], k1[3], k2[3], d11[3], k12[3], d22[3];
+    float sc;
+    __device__ __forceinline__ void init(const float2 (*X)[3])
     {
 #pragma unroll
         for (int d = 0; d < 3; d++) {
-            k1[d] = df_from(em.k1[d] * s);
-            k2[d] = df_from(em.k2[d] * s);
-            d11[d] = df_from(em.d11[d] * s);
-            k12[d] = df_from(em.k12[d] * s);
-            d22[d] = df_from(em.d22[d] * s);
+            if (NEN == 3) {
+                k0[d] = X[2][d];
+                k1[d] = df_sub(X[0][d], X[2][d]);
+                k2[d] = df_sub(X[1][d], X[2][d]);
+                d11[d] = k12[d] = d22[d] = make_float2(0.0f, 0.0f);
+            } else {
+                k0[d] = X[4][d];
+                const float2 t3 = df_mulf(X[4][d], 3.0f);
+                k1[d] = df_sub(df_sub(df_pow2(X[5][d], 4.0f), X[0][d]), t3);
+                k2[d] = df_sub(df_sub(df_pow2(X[3][d], 4.0f), X[2][d]), t3);
+                d11[d] = df_pow2(df_sub(df_add(X[0][d], X[4][d]), df_pow2(X[5][d], 2.0f)), 4.0f);
+                k12[d] = df_pow2(df_sub(df_add(df_sub(X[1][d], X[3][d]), X[4][d]), X[5][d]), 4.0f);
+                d22[d] = df_pow2(df_sub(df_add(X[2][d], X[4][d]), df_pow2(X[3][d], 2.0f)), 4.0f);
+            }
         }
+        const float h = fabsf(k1[0].x) + fabsf(k1[1].x) + fabsf(k1[2].x);
+        int e = 0;
+        frexpf(h > 0.0f ? h : 1.0f, &e);
+        sc = ldexpf(1.0f, -e);
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            k1[d] = df_pow2(k1[d], sc);
+            k2[d] = df_pow2(k2[d], sc);
+            d11[d] = df_pow2(d11[d], sc);
+            k12[d] = df_pow2(k12[d], sc);
+            d22[d] = df_pow2(d22[d], sc);
+        }
+    }
+    // e0 = (xe - k0) sc
+    __device__ __forceinline__ void offset(const float2 *xe, float2 *e0) const
+    {
+#pragma unroll
+        for (int d = 0; d < 3; d++) e0[d] = df_pow2(df_sub(xe[d], k0[d]), sc);
     }
     // dd = xe - X(l1, l2) given e0 = xe - k0; returns |t1 x t2|^2
     __device__ __forceinline__ float2 at_sq(float2 l1, float2 l2, const float2 *e0, float2 *dd) const
@@ -191,18 +214,15 @@ __device__ __forceinline__ int duffy_df(int s, float2 u1, float2 u2, float2 *La,
 }
 
 // warp_singular_G<NEN, true> in double-FP32: out[k] (every lane) = sum
-// over 8 x 8 (x2) points of w1 w2 J B N_k / r.
+// over 8 x 8 (x2) points of w1 w2 J B N_k / r; X and xe in double-FP32.
 template <int NEN>
-__device__ void warp_singular_G_df(int s, const double (*X)[3], const double *xe, double *out)
+__device__ void warp_singular_G_df(int s, const float2 (*X)[3], const float2 *xe, float2 *out)
 {
     const int lane = threadIdx.x & 31;
-    ElemMap<NEN> em;
-    em.init(X);
-    const double sc = sing_scale<NEN>(em);
     ElemMapDf<NEN> ed;
-    ed.init(em, sc);
-    const float2 e0[3] = {df_from((xe[0] - em.k0[0]) * sc), df_from((xe[1] - em.k0[1]) * sc),
-                          df_from((xe[2] - em.k0[2]) * sc)};
+    ed.init(X);
+    float2 e0[3];
+    ed.offset(xe, e0);
     float2 acc[NEN];
 #pragma unroll
     for (int k = 0; k < NEN; k++) acc[k] = make_float2(0.0f, 0.0f);
@@ -225,32 +245,29 @@ __device__ void warp_singular_G_df(int s, const double (*X)[3], const double *xe
 #pragma unroll
         for (int k = 0; k < NEN; k++) df_mac(acc[k], A, N[k]);
     }
-    const double back = 1.0 / sc;  // G scales with the length (a power of two: exact)
+    const float back = 1.0f / ed.sc;  // G scales with the length (a power of two: exact)
 #pragma unroll
-    for (int k = 0; k < NEN; k++) out[k] = df_to(df_warp_sum(acc[k])) * back;
+    for (int k = 0; k < NEN; k++) out[k] = df_pow2(df_warp_sum(acc[k]), back);
 }
 
-// warp_singular_H<NEN, FLAG, true> in double-FP32 (the same outputs).
+// warp_singular_H<NEN, FLAG, true> in double-FP32 (the same outputs, in
+// double-FP32 in every lane); X0, xe and the normal n in double-FP32.
 template <int NEN, int FLAG>
-__device__ void warp_singular_H_df(int s, const double (*X0)[3], const double *xe, const double *n,
-                                   double *out)
+__device__ void warp_singular_H_df(int s, const float2 (*X0)[3], const float2 *xe, const float2 *nd,
+                                   float2 *out)
 {
     constexpr int NOUT = FLAG == 2 ? 4 * NEN : FLAG ? 3 * NEN : NEN;
     constexpr int G0 = FLAG == 2 ? NEN : 0;
     const int lane = threadIdx.x & 31;
-    double X[NEN][3];
+    float2 X[NEN][3];
 #pragma unroll
     for (int p = 0; p < NEN; p++)
 #pragma unroll
         for (int d = 0; d < 3; d++) X[p][d] = X0[singular_perm<NEN>(s, p)][d];
-    ElemMap<NEN> em;
-    em.init(X);
-    const double sc = sing_scale<NEN>(em);
     ElemMapDf<NEN> ed;
-    ed.init(em, sc);
-    const float2 e0[3] = {df_from((xe[0] - em.k0[0]) * sc), df_from((xe[1] - em.k0[1]) * sc),
-                          df_from((xe[2] - em.k0[2]) * sc)};
-    const float2 nd[3] = {df_from(n[0]), df_from(n[1]), df_from(n[2])};
+    ed.init(X);
+    float2 e0[3];
+    ed.offset(xe, e0);
     float2 acc[NOUT];
 #pragma unroll
     for (int k = 0; k < NOUT; k++) acc[k] = make_float2(0.0f, 0.0f);
@@ -319,9 +336,9 @@ __device__ void warp_singular_H_df(int s, const double (*X0)[3], const double *x
             }
         }
     }
-    double red[NOUT];
+    float2 red[NOUT];
 #pragma unroll
-    for (int k = 0; k < NOUT; k++) red[k] = df_to(df_warp_sum(acc[k]));
+    for (int k = 0; k < NOUT; k++) red[k] = df_warp_sum(acc[k]);
 #pragma unroll
     for (int p = 0; p < NEN; p++) {
         const int o = singular_perm<NEN>(s, p);
