@@ -15,6 +15,7 @@
 namespace dsc {
 
 constexpr int kPreMaxBlocks = 16;     // preconditioner blocks per Gauss-Jordan launch
+constexpr int kPreOneStream = 1024;   // blocks up to this size applied on one stream
 constexpr int kPreMinRows = 32;       // smaller electrodes keep the Jacobi scaling only
 constexpr int kPreMaxRows = 6144;     // larger ones are cut into pieces of at most this
 constexpr float kPreVScale = 16384.0f;  // 2^14: fp16 scale of unit Krylov vectors
@@ -543,9 +544,13 @@ int precond_apply_v(Session &s, const float2 *V, int F, __half *Zh, __half *Zl, 
     TimerScope ts(&s.timer, kTPreApply, st);
     const int F2 = 2 * F;
     // odd blocks on the side stream: each block's product is a small GEMM
-    // (tens of CTAs), two of them fill more of the GPU
+    // (tens of CTAs), two of them fill more of the GPU; blocks of at most
+    // kPreOneStream rows stay on st (the products take microseconds, less
+    // than the streams' fork and join)
     SideJoin sj;
-    const bool two = pc.nb >= 2 && s.side;
+    int nmax = 0;
+    for (int b = 0; b < pc.nb; b++) nmax = std::max(nmax, pc.n[b]);
+    const bool two = pc.nb >= 2 && s.side && nmax > kPreOneStream;
     if (two) DSC_TRY(sj.fork(st, s.side));
     for (int b = 0; b < pc.nb; b++) {
         const int n = pc.n[b], ldx = pc.ldx[b];
@@ -574,9 +579,12 @@ int precond_apply_d(Session &s, double *D, int F, int *d_err)
     cudaStream_t st = s.st;
     TimerScope ts(&s.timer, kTPreApply, st);
     const int F2 = 2 * F;
-    // blocks' rows are disjoint: odd blocks on the side stream
+    // blocks' rows are disjoint: odd blocks on the side stream (large
+    // blocks only, as above)
     SideJoin sj;
-    const bool two = pc.nb >= 2 && s.side;
+    int nmax = 0;
+    for (int b = 0; b < pc.nb; b++) nmax = std::max(nmax, pc.n[b]);
+    const bool two = pc.nb >= 2 && s.side && nmax > kPreOneStream;
     if (two) DSC_TRY(sj.fork(st, s.side));
     for (int b = 0; b < pc.nb; b++) {
         const int n = pc.n[b], ldx = pc.ldx[b];
