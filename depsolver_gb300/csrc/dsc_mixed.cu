@@ -654,6 +654,22 @@ __global__ void __launch_bounds__(128) k_field_batched_mixed(
         const int e0 = (group * nloop + cl) * kBChunk;
         if (e0 >= E) break;  // uniform over the block
         const int ne = min(kBChunk, E - e0);
+        if (!far_on) {
+            // the far pairs go to the tensor cores: skip a chunk with no
+            // element near any of the block's points (the same test, from
+            // the centroids alone, as below)
+            bool any = false;
+            if (valid)
+                for (int e = 0; e < ne; e++) {
+                    const float4 ca = __ldg((const float4 *)(ecent + (size_t)(e0 + e) * 8));
+                    const float4 cb = __ldg((const float4 *)(ecent + (size_t)(e0 + e) * 8 + 4));
+                    const float d0x = (ph[0] - ca.x) + (pl[0] - ca.w);
+                    const float d0y = (ph[1] - ca.y) + (pl[1] - cb.x);
+                    const float d0z = (ph[2] - ca.z) + (pl[2] - cb.y);
+                    any |= __fmaf_rn(d0z, d0z, __fmaf_rn(d0y, d0y, __fmul_rn(d0x, d0x))) < cb.z;
+                }
+            if (!__syncthreads_or(any)) continue;
+        }
         __syncthreads();  // the previous chunk is no longer read (and the barrier is initialised)
         if (threadIdx.x == 0) {
             mbar_expect_tx(&bar, kBytes);
