@@ -17,15 +17,15 @@
 // k) u = blockIdx.x, + gridDim.x, ...  Warp 0 lane 0 streams k-blocks (one
 // 128-byte swizzle row: 32 tf32 or 64 fp16 values) of A and Bh, Bl into a
 // 3-stage shared-memory ring with TMA (128B swizzle) without pausing between
-// units (the Gauss-Jordan update: one stage, and the old values of its
-// tiles in a ring of their own); warps 2-5 split a plain FP32 A in shared memory; warp 1 lane 0
+// units; warps 2-5 split a plain FP32 A in shared memory; warp 1 lane 0
 // issues tcgen05.mma (M = 128, 32 bytes of k per instruction: K = 8 tf32 or
 // K = 16 fp16) into one of two FP32 accumulator buffers in tensor memory and
 // releases each stage with tcgen05.commit; warps 6-9 read the finished
 // buffer back (tcgen05.ld, one TMEM lane per row) and store the partial tile
 // while the next unit accumulates in the other buffer.  Every wait on an
 // mbarrier gives up after ~2 s of clock, sets *err and lets the CTA drain
-// and free its tensor memory.
+// and free its tensor memory.  The Gauss-Jordan / block-LU update is a
+// kernel of its own on the same building blocks (k_tc_gj, below).
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_fp16.h>
@@ -138,9 +138,8 @@ __device__ __forceinline__ float tf32_lo_biased(float s)
 // products out of the main accumulator: the tensor core's FP32 accumulation
 // truncates (sums of positive products come out low), so every MMA added
 // into an accumulator costs up to one of its units in the last place.
-// Row and column tile of unit u.  Every product but the Gauss-Jordan
-// update with sel != 0: row tile u % tiles, column tile (u / tiles) % ntn.
-// The update with sel = 1 takes the cross of tile la: row tile la with every
+// Row and column tile of unit u of the Gauss-Jordan update.  sel = 0: row
+// tile u % tiles, column tile (u / tiles) % ntn.  sel = 1 takes the cross of tile la: row tile la with every
 // column tile (u < ntn), then column tile la with every row tile other than
 // la and gk; with sel = 2 every other tile (row tiles other than la and gk,
 // column tiles other than la).  A gk outside [0, tiles) excludes nothing.
