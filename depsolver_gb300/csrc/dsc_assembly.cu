@@ -605,10 +605,9 @@ __global__ void k_asm_fixup(const int *__restrict__ fix_ptr, const int *__restri
 // integral of each of their singular elements (warp_singular_H's FLAG 1
 // sums, 3 NEN per tuple t of ne_ptr's numbering) at Wg + t * 3 NEN: the
 // field's singular part at that node, taken from the same points as the
-// row's H integral.  FAST: the singular quadrature's points from the
-// polynomial element map and 1/r^3 by rsqrt; else summed as the reference
-// sums them (the FP64 mode).  The mixed mode takes k_asm_singular_df.
-template <int NEN, typename T, bool FAST>
+// row's H integral.  Summed as the reference sums them (the FP64 mode; the
+// mixed mode takes k_asm_singular_df).
+template <int NEN, typename T>
 __global__ void __launch_bounds__(128) k_asm_singular(const double *__restrict__ X,
                                                       const double *__restrict__ Y,
                                                       const double *__restrict__ Z,
@@ -647,14 +646,14 @@ __global__ void __launch_bounds__(128) k_asm_singular(const double *__restrict__
         }
         double g[4 * NEN];  // FLAG 2: out's values, then the gradient
         if (kind == 0) {
-            warp_singular_G<NEN, FAST>(s, Xe, xe, out);
-            if (grad) warp_singular_H<NEN, 1, FAST>(s, Xe, xe, n, g + NEN);
+            warp_singular_G<NEN>(s, Xe, xe, out);
+            if (grad) warp_singular_H<NEN, 1>(s, Xe, xe, n, g + NEN);
         } else if (grad) {
-            warp_singular_H<NEN, 2, FAST>(s, Xe, xe, n, g);
+            warp_singular_H<NEN, 2>(s, Xe, xe, n, g);
 #pragma unroll
             for (int k = 0; k < NEN; k++) out[k] = g[k];
         } else {
-            warp_singular_H<NEN, 0, FAST>(s, Xe, xe, n, out);
+            warp_singular_H<NEN, 0>(s, Xe, xe, n, out);
         }
         if (lane == 0) {
 #pragma unroll
@@ -842,7 +841,7 @@ static int assemble_fp64_impl(const DeviceMesh &m, double *K, size_t ld, cudaStr
         int warps = hi - lo;
         TimerScope ts(tm, kTAsmSingular, st);
         if (prec == kAsmF64) {
-            DSC_LAUNCH(k_asm_singular<NEN, double, false><<<(warps * 32 + 127) / 128, 128, 0, st>>>(
+            DSC_LAUNCH(k_asm_singular<NEN, double><<<(warps * 32 + 127) / 128, 128, 0, st>>>(
                 m.x.p, m.y.p, m.z.p, m.normals.p, m.row_kind.p, m.row_fac.p, m.elems.p, m.ne_ptr.p,
                 m.ne_elem.p, m.ne_pos.p, lo, hi, K, ld, Wg ? row_grad : nullptr, Wg));
         } else {

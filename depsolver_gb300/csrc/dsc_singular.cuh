@@ -40,79 +40,13 @@ __device__ __forceinline__ int duffy(int s, double u1, double u2, double *La, do
     }
 }
 
-// The element's map X(l1, l2) = sum N_k(l) X_k as its polynomial about
-// local (0, 0): X = k0 + k1 l1 + k2 l2 (+ d11 l1^2 / 2 + k12 l1 l2 +
-// d22 l2^2 / 2 for tria6), with the tangents dX/dl1 = k1 + d11 l1 + k12 l2,
-// dX/dl2 = k2 + k12 l1 + d22 l2.  X - k0 = (l1 (t1 + k1) + l2 (t2 + k2)) / 2,
-// so a point's offset from the collocation point comes from the tangents in
-// a few FMAs (the same map as shape() / tangents(), summed differently).
-template <int NEN>
-struct ElemMap {
-    double k0[3], k1[3], k2[3], d11[3], k12[3], d22[3];
-    __device__ __forceinline__ void init(const double (*X)[3])
-    {
-#pragma unroll
-        for (int d = 0; d < 3; d++) {
-            if (NEN == 3) {
-                k0[d] = X[2][d];
-                k1[d] = X[0][d] - X[2][d];
-                k2[d] = X[1][d] - X[2][d];
-                d11[d] = k12[d] = d22[d] = 0.0;
-            } else {
-                k0[d] = X[4][d];
-                k1[d] = 4.0 * X[5][d] - X[0][d] - 3.0 * X[4][d];
-                k2[d] = 4.0 * X[3][d] - X[2][d] - 3.0 * X[4][d];
-                d11[d] = 4.0 * (X[0][d] + X[4][d] - 2.0 * X[5][d]);
-                k12[d] = 4.0 * (X[1][d] - X[3][d] + X[4][d] - X[5][d]);
-                d22[d] = 4.0 * (X[2][d] + X[4][d] - 2.0 * X[3][d]);
-            }
-        }
-    }
-    // dd = xe - X(l1, l2), given e0 = xe - k0; returns the squared Jacobian
-    // |t1 x t2|^2.
-    __device__ __forceinline__ double at_sq(double l1, double l2, const double *e0, double *dd) const
-    {
-        double t1[3], t2[3];
-        const double h1 = 0.5 * l1, h2 = 0.5 * l2;
-#pragma unroll
-        for (int d = 0; d < 3; d++) {
-            if (NEN == 3) {
-                t1[d] = k1[d];
-                t2[d] = k2[d];
-                dd[d] = e0[d] - fma(l1, k1[d], l2 * k2[d]);
-            } else {
-                t1[d] = fma(d11[d], l1, fma(k12[d], l2, k1[d]));
-                t2[d] = fma(k12[d], l1, fma(d22[d], l2, k2[d]));
-                dd[d] = e0[d] - fma(h1, t1[d] + k1[d], h2 * (t2[d] + k2[d]));
-            }
-        }
-        const double j1 = t1[1] * t2[2] - t2[1] * t1[2];
-        const double j2 = t2[0] * t1[2] - t1[0] * t2[2];
-        const double j3 = t1[0] * t2[1] - t2[0] * t1[1];
-        return j1 * j1 + j2 * j2 + j3 * j3;
-    }
-    __device__ __forceinline__ double at(double l1, double l2, const double *e0, double *dd) const
-    {
-        return sqrt(at_sq(l1, l2, e0, dd));
-    }
-};
-
-// |J| / r^3 from the squared Jacobian and squared distance in one
-// reciprocal square root: |J| / r^3 = J^2 / sqrt(J^2 r^6).
-__device__ __forceinline__ double jac_over_r3(double j2, double rsq)
-{
-    return j2 * rsqrt(j2 * (rsq * rsq * rsq));
-}
-
 // A point of the singular quadrature: dd = xe - X(l1, l2), returns the
-// Jacobian.  FAST: from the polynomial map; else as the reference sums it
-// (nodal shape functions, N the shape values at (l1, l2)), which the FP64
-// mode keeps so that its K follows the reference's rounding.
-template <int NEN, bool FAST>
-__device__ __forceinline__ double sing_point(const ElemMap<NEN> &em, const double (*X)[3], const double *xe,
-                                             const double *e0, double l1, double l2, const double *N, double *dd)
+// Jacobian, summed as the reference sums it (nodal shape functions, N the
+// shape values at (l1, l2)), so that K follows the reference's rounding.
+template <int NEN>
+__device__ __forceinline__ double sing_point(const double (*X)[3], const double *xe, double l1, double l2,
+                                             const double *N, double *dd)
 {
-    if (FAST) return em.at(l1, l2, e0, dd);
     double XL[3];
     const double J = map_point<NEN>(X, l1, l2, N, XL);
 #pragma unroll
@@ -120,15 +54,10 @@ __device__ __forceinline__ double sing_point(const ElemMap<NEN> &em, const doubl
     return J;
 }
 
-// c / r^3 at squared distance rsq: FAST by the reciprocal square root, else
-// by the reference's division.
-template <int NEN, bool FAST>
+// c / r^3 at squared distance rsq, by the reference's division.
+template <int NEN>
 __device__ __forceinline__ double over_r3(double c, double rsq)
 {
-    if (FAST) {
-        const double ri = rsqrt(rsq);
-        return c * (ri * ri * ri);
-    }
     if (NEN == 3) return c / (rsq * sqrt(rsq));
     const double dr = sqrt(rsq);
     return c / (dr * dr * dr);
@@ -137,14 +66,11 @@ __device__ __forceinline__ double over_r3(double c, double rsq)
 // Warp-cooperative weakly singular G: out[k] (lane 0 valid after the call,
 // every lane holds the reduced value) = sum over 8 x 8 (x2) points of
 // w1 w2 J B N_k / r, B = 1/8 (one sub-triangle) or 1/16 (two).
-template <int NEN, bool FAST = false>
+template <int NEN>
 __device__ void warp_singular_G(int s, const double (*X)[3], const double *xe, double *out)
 {
     const int lane = threadIdx.x & 31;
     double La[2], Lb[2], N[6], dd[3];
-    ElemMap<NEN> em;
-    em.init(X);
-    const double e0[3] = {xe[0] - em.k0[0], xe[1] - em.k0[1], xe[2] - em.k0[2]};
     double acc[NEN];
 #pragma unroll
     for (int k = 0; k < NEN; k++) acc[k] = 0.0;
@@ -158,17 +84,9 @@ __device__ void warp_singular_G(int s, const double (*X)[3], const double *xe, d
         duffy<NEN>(s, u1, u2, La, Lb);
         const double *L = t == 0 ? La : Lb;
         shape<NEN>(L[0], L[1], N);
-        double A;
-        if (FAST) {
-            // |J| / r = J^2 / sqrt(J^2 r^2)
-            const double j2 = em.at_sq(L[0], L[1], e0, dd);
-            const double rsq = dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2];
-            A = w1 * w2 * B * (j2 * rsqrt(j2 * rsq));
-        } else {
-            const double J = sing_point<NEN, FAST>(em, X, xe, e0, L[0], L[1], N, dd);
-            const double dx = dd[0], dy = dd[1], dz = dd[2];
-            A = w1 * w2 * J * B / sqrt(dx * dx + dy * dy + dz * dz);
-        }
+        const double J = sing_point<NEN>(X, xe, L[0], L[1], N, dd);
+        const double dx = dd[0], dy = dd[1], dz = dd[2];
+        const double A = w1 * w2 * J * B / sqrt(dx * dx + dy * dy + dz * dz);
 #pragma unroll
         for (int k = 0; k < NEN; k++) acc[k] += A * N[k];
     }
@@ -179,8 +97,9 @@ __device__ void warp_singular_G(int s, const double (*X)[3], const double *xe, d
 // The subdivision's points at level 0 (level m: times 2^-m, exact): for
 // sub-triangle i and point q of the 7-point rule, l[i][q] = (l1, l2); for
 // the tria6 mid-side rotations s = 2, 4, 6, ab[s / 2 - 1][i][q] = the two
-// mapped points (a1, a2, b1, b2).  The same sums as the loop below takes
-// per point, evaluated once at compile time.
+// mapped points (a1, a2, b1, b2).  The same sums as warp_singular_H takes
+// per point, evaluated once at compile time (the table of the double-FP32
+// form, dsc_singular_df.cuh).
 struct SubdivPts {
     double l[3][kTriPts][2];
     double ab[3][3][kTriPts][4];
@@ -212,8 +131,6 @@ constexpr SubdivPts make_subdiv_pts()
     return t;
 }
 
-// in global memory: the lanes of a warp read different entries
-__device__ const SubdivPts g_subdiv = make_subdiv_pts();
 
 // Position p of the rotated element holds original node perm[p]
 // (src/kernelIntegrals.c:494-499, :636-647).
@@ -230,51 +147,6 @@ __device__ __forceinline__ int singular_perm(int s, int p)
     return p;
 }
 
-// One point's (two mapped points') terms of warp_singular_H: FLAG != 1 the
-// normal derivative (acc[k] -= A (d . n) N_k), FLAG != 0 the gradient
-// (acc[G0 + 3 k + c] += A d_c N_k; the second mapped point's z term with its
-// y distance, as in the reference, src/kernelIntegrals.c:762).
-template <int NEN, int FLAG>
-__device__ __forceinline__ void singular_H_add(double A, double dx, double dy, double dz, const double *n,
-                                               const double *N1, double *acc)
-{
-    constexpr int G0 = FLAG == 2 ? NEN : 0;
-    if (FLAG != 1) {
-        const double An = A * (dx * n[0] + dy * n[1] + dz * n[2]);
-#pragma unroll
-        for (int k = 0; k < NEN; k++) acc[k] -= An * N1[k];
-    }
-    if (FLAG != 0) {
-#pragma unroll
-        for (int k = 0; k < NEN; k++) {
-            acc[G0 + 3 * k + 0] += A * dx * N1[k];
-            acc[G0 + 3 * k + 1] += A * dy * N1[k];
-            acc[G0 + 3 * k + 2] += A * dz * N1[k];
-        }
-    }
-}
-
-template <int NEN, int FLAG>
-__device__ __forceinline__ void singular_H_add2(double A1, const double *D1, const double *N1, double A2,
-                                                const double *D2, const double *N2, const double *n, double *acc)
-{
-    constexpr int G0 = FLAG == 2 ? NEN : 0;
-    if (FLAG != 1) {
-        const double An1 = A1 * (D1[0] * n[0] + D1[1] * n[1] + D1[2] * n[2]);
-        const double An2 = A2 * (D2[0] * n[0] + D2[1] * n[1] + D2[2] * n[2]);
-#pragma unroll
-        for (int k = 0; k < NEN; k++) acc[k] -= An1 * N1[k] + An2 * N2[k];
-    }
-    if (FLAG != 0) {
-#pragma unroll
-        for (int k = 0; k < NEN; k++) {
-            acc[G0 + 3 * k + 0] += A1 * D1[0] * N1[k] + A2 * D2[0] * N2[k];
-            acc[G0 + 3 * k + 1] += A1 * D1[1] * N1[k] + A2 * D2[1] * N2[k];
-            acc[G0 + 3 * k + 2] += A1 * D1[2] * N1[k] + A2 * D2[1] * N2[k];
-        }
-    }
-}
-
 // Warp-cooperative strongly singular H (FLAG = 0: normal derivative with
 // the node normal n, out[k]; FLAG = 1: gradient, out[3k + c]; FLAG = 2:
 // both from the same points, out[k] and out[NEN + 3k + c], each summed as
@@ -284,7 +156,7 @@ __device__ __forceinline__ void singular_H_add2(double A1, const double *D1, con
 // mid-side nodes each point is split into two mapped points with weight
 // 1/2; the gradient's z-component of the second one uses its y-distance,
 // as in the reference (:762).
-template <int NEN, int FLAG, bool FAST = false>
+template <int NEN, int FLAG>
 __device__ void warp_singular_H(int s, const double (*X0)[3], const double *xe, const double *n,
                                 double *out)
 {
@@ -296,9 +168,6 @@ __device__ void warp_singular_H(int s, const double (*X0)[3], const double *xe, 
     for (int p = 0; p < NEN; p++)
 #pragma unroll
         for (int d = 0; d < 3; d++) X[p][d] = X0[singular_perm<NEN>(s, p)][d];
-    ElemMap<NEN> em;
-    em.init(X);
-    const double e0[3] = {xe[0] - em.k0[0], xe[1] - em.k0[1], xe[2] - em.k0[2]};
     double acc[NOUT];
 #pragma unroll
     for (int k = 0; k < NOUT; k++) acc[k] = 0.0;
@@ -314,30 +183,6 @@ __device__ void warp_singular_H(int s, const double (*X0)[3], const double *xe, 
         double J = ldexp(1.0, -2 * (m + 1));    // 0.25^(m+1) (exact)
         double M1 = c_tri7[q][0], M2 = c_tri7[q][1];
         double M3 = 1.0 - M1 - M2, W = c_tri7[q][2];
-        if (FAST) {
-            if (!two) {
-                const double2 L = __ldg((const double2 *)g_subdiv.l[i][q]);
-                const double l1 = L.x * scale, l2 = L.y * scale;
-                shape<NEN>(l1, l2, N1);
-                const double j2 = em.at_sq(l1, l2, e0, D1);
-                const double dx = D1[0], dy = D1[1], dz = D1[2];
-                const double A = J * W * jac_over_r3(j2, dx * dx + dy * dy + dz * dz);
-                singular_H_add<NEN, FLAG>(A, dx, dy, dz, n, N1, acc);
-            } else {
-                const double2 *ab = (const double2 *)g_subdiv.ab[s / 2 - 1][i][q];
-                const double2 P1 = __ldg(ab), P2 = __ldg(ab + 1);
-                const double a1 = P1.x * scale, a2 = P1.y * scale, b1 = P2.x * scale, b2 = P2.y * scale;
-                shape<NEN>(a1, a2, N1);
-                shape<NEN>(b1, b2, N2);
-                const double j21 = em.at_sq(a1, a2, e0, D1);
-                const double j22 = em.at_sq(b1, b2, e0, D2);
-                const double hJW = 0.5 * J * W;
-                const double A1 = hJW * jac_over_r3(j21, D1[0] * D1[0] + D1[1] * D1[1] + D1[2] * D1[2]);
-                const double A2 = hJW * jac_over_r3(j22, D2[0] * D2[0] + D2[1] * D2[1] + D2[2] * D2[2]);
-                singular_H_add2<NEN, FLAG>(A1, D1, N1, A2, D2, N2, n, acc);
-            }
-            continue;
-        }
         double x00 = xs0[i][0][0] * scale, x01 = xs0[i][0][1] * scale;
         double x10 = xs0[i][1][0] * scale, x11 = xs0[i][1][1] * scale;
         double x20 = xs0[i][2][0] * scale, x21 = xs0[i][2][1] * scale;
@@ -345,9 +190,9 @@ __device__ void warp_singular_H(int s, const double (*X0)[3], const double *xe, 
             double l1 = x00 * M1 + x10 * M2 + x20 * M3;
             double l2 = x01 * M1 + x11 * M2 + x21 * M3;
             shape<NEN>(l1, l2, N1);
-            const double JL = sing_point<NEN, FAST>(em, X, xe, e0, l1, l2, N1, D1);
+            const double JL = sing_point<NEN>(X, xe, l1, l2, N1, D1);
             const double dx = D1[0], dy = D1[1], dz = D1[2];
-            const double A = over_r3<NEN, FAST>(J * JL * W, dx * dx + dy * dy + dz * dz);
+            const double A = over_r3<NEN>(J * JL * W, dx * dx + dy * dy + dz * dz);
             if (FLAG != 1) {
                 const double An = A * (dx * n[0] + dy * n[1] + dz * n[2]);
 #pragma unroll
@@ -371,12 +216,12 @@ __device__ void warp_singular_H(int s, const double (*X0)[3], const double *xe, 
             double b1 = x00 * V1 + x10 * V2 + x20 * V3, b2 = x01 * V1 + x11 * V2 + x21 * V3;
             shape<NEN>(a1, a2, N1);
             shape<NEN>(b1, b2, N2);
-            const double JL1 = sing_point<NEN, FAST>(em, X, xe, e0, a1, a2, N1, D1);
-            const double JL2 = sing_point<NEN, FAST>(em, X, xe, e0, b1, b2, N2, D2);
+            const double JL1 = sing_point<NEN>(X, xe, a1, a2, N1, D1);
+            const double JL2 = sing_point<NEN>(X, xe, b1, b2, N2, D2);
             const double dx1 = D1[0], dy1 = D1[1], dz1 = D1[2];
             const double dx2 = D2[0], dy2 = D2[1], dz2 = D2[2];
-            const double A1 = over_r3<NEN, FAST>(0.5 * J * JL1 * W, dx1 * dx1 + dy1 * dy1 + dz1 * dz1);
-            const double A2 = over_r3<NEN, FAST>(0.5 * J * JL2 * W, dx2 * dx2 + dy2 * dy2 + dz2 * dz2);
+            const double A1 = over_r3<NEN>(0.5 * J * JL1 * W, dx1 * dx1 + dy1 * dy1 + dz1 * dz1);
+            const double A2 = over_r3<NEN>(0.5 * J * JL2 * W, dx2 * dx2 + dy2 * dy2 + dz2 * dz2);
             if (FLAG != 1) {
                 const double An1 = A1 * (dx1 * n[0] + dy1 * n[1] + dz1 * n[2]);
                 const double An2 = A2 * (dx2 * n[0] + dy2 * n[1] + dz2 * n[2]);

@@ -1,9 +1,14 @@
 // dsc_singular_df.cuh -- the mixed mode's singular element integrals in
 // double-FP32 on the FP32 pipes.
 //
-// The same sums as the FAST forms of warp_singular_G / warp_singular_H
-// (dsc_singular.cuh: the element's polynomial map about the singular node,
-// |J| / r^k from one reciprocal square root), taken in double-FP32 (a
+// The integrals of warp_singular_G / warp_singular_H (dsc_singular.cuh:
+// the same points, weights, node rotation and sums) with the element's map
+// written as a polynomial about its node at local (0, 0) -- X = k0 + k1 l1 +
+// k2 l2 (+ d11 l1^2 / 2 + k12 l1 l2 + d22 l2^2 / 2 for tria6), tangents
+// dX/dl1 = k1 + d11 l1 + k12 l2, dX/dl2 = k2 + k12 l1 + d22 l2, and X - k0
+// = (l1 (t1 + k1) + l2 (t2 + k2)) / 2, so that a point's offset from the
+// collocation point comes from the tangents without cancellation -- and
+// |J| / r^k from one reciprocal square root, taken in double-FP32 (a
 // 48-bit significand, dsc_df32.cuh): about 1e-13 of the FP64 values, at a
 // fraction of the FP64 pipe's time (the FP32 pipes issue 64 times as many
 // operations per clock on sm_103a).  The node coordinates and normals come
@@ -87,8 +92,8 @@ __device__ __forceinline__ float2 df_ld(const DfC &c)
     return v;
 }
 
-// ElemMap's polynomial in double-FP32 from the nodes in double-FP32,
-// scaled by sc, a power of two near the element's size (from its first
+// The element's polynomial map in double-FP32 from the nodes in
+// double-FP32, scaled by sc, a power of two near the element's size (from its first
 // tangent: the factor that brings the pair's coordinates to order one).
 template <int NEN>
 struct ElemMapDf {
@@ -213,7 +218,7 @@ __device__ __forceinline__ int duffy_df(int s, float2 u1, float2 u2, float2 *La,
     }
 }
 
-// warp_singular_G<NEN, true> in double-FP32: out[k] (every lane) = sum
+// warp_singular_G in double-FP32: out[k] (every lane) = sum
 // over 8 x 8 (x2) points of w1 w2 J B N_k / r; X and xe in double-FP32.
 template <int NEN>
 __device__ void warp_singular_G_df(int s, const float2 (*X)[3], const float2 *xe, float2 *out)
@@ -250,7 +255,7 @@ __device__ void warp_singular_G_df(int s, const float2 (*X)[3], const float2 *xe
     for (int k = 0; k < NEN; k++) out[k] = df_pow2(df_warp_sum(acc[k]), back);
 }
 
-// warp_singular_H<NEN, FLAG, true> in double-FP32 (the same outputs, in
+// warp_singular_H<NEN, FLAG> in double-FP32 (the same outputs, in
 // double-FP32 in every lane); X0, xe and the normal n in double-FP32.
 template <int NEN, int FLAG>
 __device__ void warp_singular_H_df(int s, const float2 (*X0)[3], const float2 *xe, const float2 *nd,
