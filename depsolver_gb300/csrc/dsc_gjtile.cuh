@@ -180,12 +180,20 @@ __device__ __forceinline__ void gj_invert_tile(const float *__restrict__ T, int 
                 }
 #pragma unroll
                 for (int q = 0; q < 4; q++) {
+                    // packed FP32x2 FMAs (each half rounded as an FMA)
                     const float4 x = *(const float4 *)&pr[4 * hq + q][4 * l];
-                    const float xv[4] = {x.x, x.y, x.z, x.w};
+                    const float2 x01 = make_float2(x.x, x.y), x23 = make_float2(x.z, x.w);
 #pragma unroll
-                    for (int r = 0; r < 8; r++)
-#pragma unroll
-                        for (int c = 0; c < 4; c++) a[r][c] = fmaf(-F[r][q], xv[c], a[r][c]);
+                    for (int r = 0; r < 8; r++) {
+                        const float2 nf = make_float2(-F[r][q], -F[r][q]);
+                        float2 a01 = make_float2(a[r][0], a[r][1]), a23 = make_float2(a[r][2], a[r][3]);
+                        a01 = __ffma2_rn(nf, x01, a01);
+                        a23 = __ffma2_rn(nf, x23, a23);
+                        a[r][0] = a01.x;
+                        a[r][1] = a01.y;
+                        a[r][2] = a23.x;
+                        a[r][3] = a23.y;
+                    }
                 }
             }
         }

@@ -602,6 +602,42 @@ __global__ void k_points_split(const double *__restrict__ px, const double *__re
     }
 }
 
+// near_mask[b * ngroup + g] bit c: some point of block b (128 points) lies
+// within the near radius of some element of chunk c of group g (nloop
+// chunks of kBChunk elements) -- the near test of k_field_batched_mixed,
+// from the centroids, with the same rounding.  One block of 128 threads per
+// (point block, group); geometry only: once per session.
+__global__ void __launch_bounds__(128) k_near_masks(const float *__restrict__ phl, int P,
+                                                    const float *__restrict__ ecent, int E, int nloop,
+                                                    unsigned *__restrict__ near_mask)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x, group = blockIdx.y;
+    const bool valid = p < P;
+    const int pp = valid ? p : 0;
+    const float ph[3] = {phl[(size_t)pp * 6], phl[(size_t)pp * 6 + 1], phl[(size_t)pp * 6 + 2]};
+    const float pl[3] = {phl[(size_t)pp * 6 + 3], phl[(size_t)pp * 6 + 4], phl[(size_t)pp * 6 + 5]};
+    unsigned mask = 0;
+    for (int cl = 0; cl < nloop && cl < 32; cl++) {
+        const int e0 = (group * nloop + cl) * kBChunk;
+        if (e0 >= E) break;
+        const int ne = min(kBChunk, E - e0);
+        bool any = false;
+        if (valid) {
+#pragma unroll 8
+            for (int e = 0; e < ne; e++) {
+                const float4 ca = __ldg((const float4 *)(ecent + (size_t)(e0 + e) * 8));
+                const float4 cb = __ldg((const float4 *)(ecent + (size_t)(e0 + e) * 8 + 4));
+                const float d0x = (ph[0] - ca.x) + (pl[0] - ca.w);
+                const float d0y = (ph[1] - ca.y) + (pl[1] - cb.x);
+                const float d0z = (ph[2] - ca.z) + (pl[2] - cb.y);
+                any |= __fmaf_rn(d0z, d0z, __fmaf_rn(d0y, d0y, __fmul_rn(d0x, d0x))) < cb.z;
+            }
+        }
+        if (__syncthreads_or(any)) mask |= 1u << cl;
+    }
+    if (threadIdx.x == 0) near_mask[(size_t)blockIdx.x * gridDim.y + group] = mask;
+}
+
 // part[group][f][p][3] (FP32): regular contributions of one group of
 // kBLoop x kBChunk elements to the field at point p for system f.  Far
 // pairs in FP32 (rsqrt with a Newton step, coordinates as centroid-relative
@@ -618,7 +654,7 @@ __global__ void __launch_bounds__(128) k_field_batched_mixed(
     const float *__restrict__ phl, const int4 *__restrict__ coinc, int P, const int *__restrict__ en_pad,
     int E, int E7p, const float *__restrict__ ecent, const float *__restrict__ qoff,
     const float *__restrict__ cT, const float2 *__restrict__ qdf, int F, float *__restrict__ part, int *err,
-    int far_on, int nloop)
+    int far_on, int nloop, const unsigned *__restrict__ near_mask)
 {
     __shared__ __align__(16) float s_c[kBChunk * kTriPts][kBF];
     __shared__ __align__(16) float s_cent[kBChunk * 8];
@@ -654,22 +690,10 @@ __global__ void __launch_bounds__(128) k_field_batched_mixed(
         const int e0 = (group * nloop + cl) * kBChunk;
         if (e0 >= E) break;  // uniform over the block
         const int ne = min(kBChunk, E - e0);
-        if (!far_on) {
-            // the far pairs go to the tensor cores: skip a chunk with no
-            // element near any of the block's points (the same test, from
-            // the centroids alone, as below)
-            bool any = false;
-            if (valid)
-                for (int e = 0; e < ne; e++) {
-                    const float4 ca = __ldg((const float4 *)(ecent + (size_t)(e0 + e) * 8));
-                    const float4 cb = __ldg((const float4 *)(ecent + (size_t)(e0 + e) * 8 + 4));
-                    const float d0x = (ph[0] - ca.x) + (pl[0] - ca.w);
-                    const float d0y = (ph[1] - ca.y) + (pl[1] - cb.x);
-                    const float d0z = (ph[2] - ca.z) + (pl[2] - cb.y);
-                    any |= __fmaf_rn(d0z, d0z, __fmaf_rn(d0y, d0y, __fmul_rn(d0x, d0x))) < cb.z;
-                }
-            if (!__syncthreads_or(any)) continue;
-        }
+        // the far pairs on the tensor cores: chunks with no element near any
+        // of the block's points are skipped (bit cl of the block's mask;
+        // uniform over the block)
+        if (near_mask && !((near_mask[(size_t)blockIdx.x * gridDim.y + group] >> cl) & 1u)) continue;
         __syncthreads();  // the previous chunk is no longer read (and the barrier is initialised)
         if (threadIdx.x == 0) {
             mbar_expect_tx(&bar, kBytes);
@@ -960,6 +984,7 @@ struct Session::Mixed {
     // FP32 far-field pass: element centroids / offsets, split points, weights
     bool far_ready = false;
     DevBuf<float> ecent, qoff, phl, cf32;  // cf32: the charges, kBF systems innermost
+    DevBuf<unsigned> near_mask;            // per (point block, element group): chunks with near pairs
     DevBuf<int> en_pad;                    // element nodes, padded to whole chunks (-1)
     FieldTcWork ftc;                       // the tensor-core far pass
     DevBuf<float2> qdf;  // quadrature points in double-FP32 (near pairs)
@@ -1501,6 +1526,13 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
                                                                           w.qdf.p));
                 DSC_LAUNCH(k_points_split<<<(P + 127) / 128, 128, 0, st>>>(fp.ps.px.p, fp.ps.py.p, fp.ps.pz.p,
                                                                            P, w.phl.p));
+                if (tc && nloop <= 32) {
+                    DSC_TRY(w.near_mask.alloc((size_t)fg.x * fg.y));
+                    DSC_LAUNCH(k_near_masks<<<dim3(fg.x, fg.y), 128, 0, st>>>(w.phl.p, P, w.ecent.p, E, nloop,
+                                                                           w.near_mask.p));
+                } else {
+                    w.near_mask.release();
+                }
                 w.far_ready = true;
             }
             // far pairs on the tensor cores (partials after the FP32 pass's
@@ -1514,12 +1546,12 @@ static int mixed_batch(Session &s, int F, const double *freqs, double tol, unsig
                 DSC_LAUNCH(k_field_batched_mixed<6><<<fg, 128, 0, st>>>(w.phl.p, fp.ps.coinc.p, P, w.en_pad.p, E,
                                                                         E7p, w.ecent.p, w.qoff.p, w.cf32.p,
                                                                         w.qdf.p, F, w.part.p, w.err.p, tc ? 0 : 1,
-                                                                        nloop));
+                                                                        nloop, tc ? w.near_mask.p : nullptr));
             else
                 DSC_LAUNCH(k_field_batched_mixed<3><<<fg, 128, 0, st>>>(w.phl.p, fp.ps.coinc.p, P, w.en_pad.p, E,
                                                                         E7p, w.ecent.p, w.qoff.p, w.cf32.p,
                                                                         w.qdf.p, F, w.part.p, w.err.p, tc ? 0 : 1,
-                                                                        nloop));
+                                                                        nloop, tc ? w.near_mask.p : nullptr));
             const int sb = (P * 32 + 127) / 128;
             if (s.nen == 6)
                 DSC_LAUNCH(k_field_singular_apply<6><<<sb, 128, 0, st>>>(P, s.dev.elems.p, s.dev.normals.p,
