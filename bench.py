@@ -173,7 +173,7 @@ def cpu_baseline(sc, nthreads: int, sample_div: int = 8, full_first: bool = True
     rows' share of every GMRES matrix-vector product (times that count) and
     1/sample_div of the particle-node fields, scaled to one full solve;
     Gram-Schmidt and the MST integral are timed in full."""
-    from oracle.checker import Port
+    from oracle.oracle import Port
     P = Port()
     N = sc.N
     info = {}
@@ -391,7 +391,7 @@ def gauss_bench(with_cpu: bool):
                      "peak_source": "MEASURED_PEAKS.json bf16_tflops, of measured" if P else "fallback",
                      "speedup_vs_fp64_lu": t64 / best}
         if with_cpu and name == "cfg0":
-            from oracle.checker import Port
+            from oracle.oracle import Port
             t0 = time.perf_counter()
             Port().gauss(Af, Bf)
             tc = time.perf_counter() - t0
@@ -583,7 +583,7 @@ def dropin_bench():
         # the C restatement at the same points: batched on every host core,
         # and one point per call on one core as the reference's post-
         # processing runs (a sample of the points at the larger scene)
-        from oracle.checker import Port
+        from oracle.oracle import Port
         nt = os.cpu_count() or 1
         if name == "cfg0":
             t6 = time.perf_counter()

@@ -1,4 +1,4 @@
-"""ctypes front-ends of the two CPU checkers (test infrastructure only).
+"""ctypes front-ends of the two CPU oracles (test infrastructure only).
 
 ``Port`` drives ``oracle/liboracle.so`` (the C restatement, builds anywhere);
 ``Ref`` drives ``oracle/_ref/libdsref.so`` (the reference's own objects plus

@@ -1,7 +1,7 @@
 /*
  * oracle.h -- CPU restatement of depSolver's BEM hot path (test infrastructure).
  *
- * This library is the checker for the GPU library and the CPU baseline of the
+ * This library is the oracle for the GPU library and the CPU baseline of the
  * benchmark.  It is NOT part of the product: only tests, the smoke check and
  * the benchmark's CPU leg load it.  Every function restates one reference
  * function (cited by file:line in the reference tree) in plain C99 on flat

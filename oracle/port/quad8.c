@@ -3,7 +3,7 @@
  *
  * The reference has no quad8 integrals (it recognises the element type,
  * src/preProcess.c:142-146, and its driver rejects it), so this is the
- * checker of the GPU library's quad8 extension, written independently in
+ * oracle of the GPU library's quad8 extension, written independently in
  * plain loops from the same definitions:
  *   - serendipity element on [-1, 1]^2, nodes 1-4 the corners (-1,-1),
  *     (1,-1), (1,1), (-1,1), nodes 5-8 the mid-sides of edges 1-2, 2-3,

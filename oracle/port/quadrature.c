@@ -4,7 +4,7 @@
  *
  * The three rules are standard published ones, written to the same 15
  * significant digits the reference tabulates (src/gaussData.h:38-73) so that
- * the checker reproduces the reference's sums to rounding:
+ * the oracle reproduces the reference's sums to rounding:
  *   - 8-point Gauss-Legendre on [-1, 1];
  *   - 8-point Gauss-Jacobi on [-1, 1] with weight (1 + x) (alpha 0, beta 1);
  *   - Dunavant's 7-point degree-5 triangle rule, weights summing to 1/2:

@@ -20,17 +20,17 @@ def pytest_configure(config):
 
 @pytest.fixture(scope="session")
 def port():
-    from oracle.checker import Port, build_port
+    from oracle.oracle import Port, build_port
     build_port()
     return Port()
 
 
 @pytest.fixture(scope="session")
 def ref():
-    from oracle import checker
-    if checker.build_ref() is None:
+    from oracle import oracle as orc
+    if orc.build_ref() is None:
         pytest.skip("reference sources not present")
-    return checker.Ref()
+    return orc.Ref()
 
 
 @pytest.fixture(scope="session")

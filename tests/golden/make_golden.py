@@ -148,11 +148,11 @@ def main():
     args = ap.parse_args()
     want = set(args.only) if args.only else {"small", "cfg0", "dep_trap_2", "multipole"}
     os.environ["DSC_REFERENCE_SRC"] = os.path.join(args.reference, "src")
-    from oracle import checker
-    checker.REF_SRC = os.environ["DSC_REFERENCE_SRC"]
-    if checker.build_ref() is None:
+    from oracle import oracle as orc
+    orc.REF_SRC = os.environ["DSC_REFERENCE_SRC"]
+    if orc.build_ref() is None:
         sys.exit("reference sources not found")
-    ref = checker.Ref()
+    ref = orc.Ref()
     if "small" in want:
         for nen in (6, 3):
             scene_fixture(ref, scenes.small(nen=nen), os.path.join(HERE, f"small_tria{nen}.npz"))

@@ -1,6 +1,6 @@
 """The direct solve (gaussBksb, src/gaussBksb.c:39-108) as a block LU on the
 tensor cores with FP64 iterative refinement, against the FP64 LU, the
-checker's elimination and the reference's own Gauss fixtures.
+oracle's elimination and the reference's own Gauss fixtures.
 
 The reference eliminates without pivoting; so do both GPU factorisations,
 and both stop on a pivot within 1e-9 of zero with the reference's message.
@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("nen", [6, 3])
-def test_mixed_lu_matches_fp64_lu_and_checker(gpu, port, nen):
+def test_mixed_lu_matches_fp64_lu_and_oracle(gpu, port, nen):
     sc = scenes.small(nen=nen)
     Af, Bf = api.electric_form(sc, full=True)
     x64 = api.gauss_bksb(Af, Bf, mode=api.GAUSS_FP64)

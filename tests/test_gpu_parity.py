@@ -31,7 +31,7 @@ def _probe(A, g, prefix, tol=ASM_TOL):
 
 @pytest.mark.parametrize("nen", [6, 3])
 @pytest.mark.parametrize("full", [False, True])
-def test_assembly_matches_checker(gpu, port, nen, full):
+def test_assembly_matches_oracle(gpu, port, nen, full):
     sc = scenes.small(nen=nen)
     A, B = api.electric_form(sc, full=full)
     Ap, Bp = port.assemble(sc, full=full)
@@ -101,7 +101,7 @@ def test_cfg0_gauss_and_tight_gmres(gpu):
     assert np.abs(Fcm - g["Fcm_tight"]).max() <= 1e-9 * np.abs(g["Fce"]).sum()
 
 
-def test_field_off_mesh_and_on_nodes_vs_checker(gpu, port):
+def test_field_off_mesh_and_on_nodes_vs_oracle(gpu, port):
     sc = scenes.small(nen=6)
     A, B = port.assemble(sc)
     x, _, _ = port.gmres(A, B)
@@ -169,7 +169,7 @@ def test_pure_conductor_scene(gpu, port):
     Ap, Bp = port.assemble(sc)
     assert relerr(A, Ap) < ASM_TOL
     # At the compiled 1e-6 tolerance this scene converges on a tie: the
-    # checker's residual at step 11 is within 9% of the tolerance and a
+    # oracle's residual at step 11 is within 9% of the tolerance and a
     # different summation order stops one step earlier, so compare the
     # tight-tolerance and direct solutions instead.
     x, it = api.solver_gmres_el(A, B, tol=1e-12)

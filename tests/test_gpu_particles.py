@@ -3,9 +3,9 @@
 The reference sums every type-6 element into one force (src/force.c:516-547);
 a particle's own force is that sum over its elements alone, which is what
 the reference's forceMST_* returns with vBCType masked to that particle (the
-field at its nodes comes from the same solution).  The checker does exactly
+field at its nodes comes from the same solution).  The oracle does exactly
 that; the torque (an extension: the reference has none) is checked against
-sum (Xce - Xcm) x Fce of the checker's own per-element output.
+sum (Xce - Xcm) x Fce of the oracle's own per-element output.
 """
 import dataclasses
 
@@ -56,7 +56,7 @@ def test_per_particle_force_and_torque_match_masked_reference(gpu, port, nen):
     # the reference's Jacobi step leaves the imaginary right-hand side
     # unscaled (src/gmres_el.c:87-93): its solution is not that of the
     # assembled system.  The FP64 path with the full scaling is, as the
-    # checker's GMRES without Jacobi scaling confirms; the mixed sweep's
+    # oracle's GMRES without Jacobi scaling confirms; the mixed sweep's
     # per-particle results follow that one.
     s.set_fp64_jacobi(True)
     f2, _, sig2 = s.solve([sc.freq], mode=api.MODE_FP64, tol=1e-12, want_sigma=True)

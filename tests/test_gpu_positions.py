@@ -50,7 +50,7 @@ def test_positions_match_separate_sweeps(gpu, port):
         st = np.zeros(len(freqs), dtype=np.int32)
         xo = L.dsc_force_crossover(len(freqs), freqs, np.ascontiguousarray(r["forces"][q]), st.ctypes.data)
         assert (np.isnan(xo) and np.isnan(r["crossover_hz"][q])) or xo == r["crossover_hz"][q]
-    # one position against the checker's GMRES (FP64, tol 1e-12) at one frequency
+    # one position against the oracle's GMRES (FP64, tol 1e-12) at one frequency
     sc = _position_scene(levels[tm[0]], cen[0]).with_freq(freqs[3])
     A, B = port.assemble(sc)
     xp, _, stp = port.gmres(A, B, tol=1e-12)

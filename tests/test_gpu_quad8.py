@@ -1,4 +1,4 @@
-"""The quad8 extension on the GPU, against the checker's quad8 restatement
+"""The quad8 extension on the GPU, against the oracle's quad8 restatement
 (oracle/port/quad8.c; the reference has no quad8 integrals) and against
 closed-form fields: assembly of both forms, the solve, field and potential
 off and on the mesh, the Maxwell-stress force; a conducting sphere and a
@@ -16,14 +16,14 @@ SOL_TOL = 1e-10
 
 
 @pytest.mark.parametrize("full", [False, True])
-def test_quad8_assembly_matches_checker(gpu, port, full):
+def test_quad8_assembly_matches_oracle(gpu, port, full):
     sc = scenes.small(nen=8)
     A, B = api.electric_form(sc, full=full)
     Ap, Bp = port.assemble(sc, full=full)
     assert relerr(A, Ap) < ASM_TOL and np.array_equal(B, Bp)
 
 
-def test_quad8_pipeline_matches_checker(gpu, port):
+def test_quad8_pipeline_matches_oracle(gpu, port):
     sc = scenes.small(nen=8)
     A, B = api.electric_form(sc)
     x, _ = api.solver_gmres_el(A, B, tol=1e-12)

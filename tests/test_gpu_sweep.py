@@ -1,7 +1,7 @@
 """Frequency sweeps on a device-resident scene (dsc_session_* / dsc_sweep).
 
 The plain FP64 path must reproduce the reference's GMRES (through the
-strict compact path and the checker); the mixed path must reach the FP64
+strict compact path and the oracle); the mixed path must reach the FP64
 solution: Maxwell-stress force within 1e-6 of the force scale (sum over
 particle elements of |Fce|), and the nodal solution within 1e-9 relative
 when the matrix's regular pairs are assembled in double-FP32, within 1e-5
@@ -49,7 +49,7 @@ def test_mixed_matches_fp64_across_frequencies(gpu, port, nen, asm, sig_tol):
         assert relerr(smx[k], s64[k]) < sig_tol, k
         scale = f64[k, 6:9].sum()
         assert np.abs(fmx[k, :3] - f64[k, :3]).max() <= FORCE_TOL * scale, k
-    # the reference's own solution at one frequency, by the checker
+    # the reference's own solution at one frequency, by the oracle
     scf = sc.with_freq(freqs[2])
     Ap, Bp = port.assemble(scf)
     xp, _, st = port.gmres(Ap, Bp, tol=1e-12)
@@ -102,7 +102,7 @@ def test_double_fp32_assembly_matches_fp64(gpu, port, nen):
     scale = np.abs(K64).max()
     assert np.abs(Kd - K64).max() <= 1e-13 * scale
     assert not np.array_equal(Kd, K64)            # it is a different computation
-    # the FP64 K against the checker's compact matrix (conductor rows: C int G)
+    # the FP64 K against the oracle's compact matrix (conductor rows: C int G)
     A, _ = port.assemble(sc)
     N = sc.N
     cond = sc.bctype[:N] != 6

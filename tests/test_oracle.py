@@ -1,4 +1,4 @@
-"""Pins the CPU checker (oracle/port, a C restatement of the reference) to
+"""Pins the CPU oracle (oracle/port, a C restatement of the reference) to
 the reference: committed golden fixtures made by the reference itself, the
 reference's 2008 example outputs, and -- where the reference sources exist --
 the reference compiled here, bit for bit."""

@@ -1,5 +1,5 @@
 """The quad8 extension without a GPU.  The reference has no quad8 integrals,
-so the checker's quad8 restatement (oracle/port/quad8.c) is pinned here to
+so the oracle's quad8 restatement (oracle/port/quad8.c) is pinned here to
 fields known in closed form instead of reference outputs: a sphere held at
 1 V alone (potential R / r outside, normal field V / R on the surface) and
 a dielectric sphere in a near-uniform field (induced dipole with the
@@ -21,7 +21,7 @@ def test_cubed_sphere_mesh():
     assert (out > 0).all()                                       # normals outward
 
 
-def test_checker_conducting_sphere(port):
+def test_oracle_conducting_sphere(port):
     sc = scenes.conductor_sphere(4)
     A, B = port.assemble(sc, full=True)
     x = port.gauss(A, B)
@@ -36,7 +36,7 @@ def test_checker_conducting_sphere(port):
     assert np.abs(En - 1.0).max() < 0.12
 
 
-def test_checker_dielectric_sphere_dipole(port):
+def test_oracle_dielectric_sphere_dipole(port):
     ep, em = 10.0, 1.0
     sc = scenes.sphere_between_plates(2, 4, nen=8, plate_side=40.0, plate_z=8.0, medium=(0.0, em),
                                       particle=(0.0, ep), freq=1e6)

@@ -1,7 +1,7 @@
 """The input-deck reader and the node normals as library calls (host code,
 no GPU): dsc_bem_read against decks written from the scene generator and
 against the reference's own example decks (where the reference tree is
-present), dsc_node_normals against the checker's getNormal restatement
+present), dsc_node_normals against the oracle's getNormal restatement
 (src/normals.c:120-319) and, where present, the reference's own."""
 import os
 
@@ -70,7 +70,7 @@ def test_reader_reads_reference_examples(native, deck):
 
 
 @pytest.mark.parametrize("nen", [6, 3])
-def test_node_normals_match_checker(native, port, nen):
+def test_node_normals_match_oracle(native, port, nen):
     sc = scenes.small(nen=nen)
     n = api.node_normals(sc)
     ref = np.array([port.node_normal(sc, i) for i in range(sc.N)])
