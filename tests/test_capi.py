@@ -57,3 +57,14 @@ def test_force_crossover_host_logic(native):
     F[:, :3] = np.abs(p)[:, None] * d
     assert np.isnan(L.dsc_force_crossover(6, f, F, None))
     assert np.isnan(L.dsc_force_crossover(1, f, F, None))
+
+
+def test_host_direct_modes(native):
+    """dsc_set_host_direct takes 0 (staged both ways), 1 (host matrices read
+    in place, the default) or 2 (the assembled rows also written in place),
+    and rejects anything else without changing the mode."""
+    L = _native.lib()
+    assert L.dsc_set_host_direct(C.c_int(3)) == 2  # DSC_ERR_ARG
+    assert b"mode 3" in L.dsc_last_error()
+    for mode in (0, 2, 1):
+        assert L.dsc_set_host_direct(C.c_int(mode)) == 0
