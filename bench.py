@@ -3,7 +3,7 @@
 
 A step is one batch: assemble the geometric matrix of the scene (regular
 pairs in FP32 from centroid-relative offsets: the far-field assembly in
-FP32; singular pairs in FP64) and
+FP32; singular pairs in double-FP32, about 1e-13 of FP64) and
 solve a 64-frequency sweep (1 kHz .. 100 MHz, log-spaced) to a relative
 residual of 1e-10 with the mixed-precision batched path, then the
 Maxwell-stress DEP force of every system.  value = systems solved per
@@ -786,7 +786,7 @@ def run_ours(args, rank, world):
         "config": {"workload": "cfg1: level-4 tria6 sphere (r=1, eps_r 2.5, sigma 1e-3) between "
                                "30x30-cell tria6 plates at z=+-5, +-1 V; medium eps_r 78, sigma 1e-4",
                    "N": N, "E": E, "freqs_per_step": NFREQ, "freq_range_hz": [1e3, 1e8],
-                   "tol": TOL, "step": f"assemble K ({args.mixed_assembly.upper()} regular / FP64 singular pairs) + 64-system mixed sweep + MST forces",
+                   "tol": TOL, "step": f"assemble K ({args.mixed_assembly.upper()} regular / double-FP32 singular pairs) + 64-system mixed sweep + MST forces",
                    "l2": "inputs larger than L2 (K 2.5 GB FP64 + its 1.25 GB fp16 pair + 5 GB digits)",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": NFREQ / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),

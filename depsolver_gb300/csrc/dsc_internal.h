@@ -341,7 +341,7 @@ struct AsmWorkspace {
 enum { kAsmF64 = 0, kAsmDf32 = 1, kAsmF32 = 2 };
 
 // prec: one of the above for the regular pairs.  Singular pairs are FP64
-// whatever prec is; K is FP64.  ws (may be null: a local one, freed before
+// (the reference's sums) with kAsmF64, else double-FP32; K is FP64.  ws (may be null: a local one, freed before
 // returning) holds the scratch.  With Wg not null, the rows flagged in
 // row_grad (N flags) also leave the gradient integrals of their singular
 // elements there: 3 nen doubles per (node, element) tuple of the plan's

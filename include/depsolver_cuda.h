@@ -234,9 +234,12 @@ int dsc_force_mst(int nen, unsigned N, unsigned E, const double *nodes, const un
  *                     tolerance `tol`) one frequency at a time, FP64 field
  *                     and Maxwell-stress force.
  *   DSC_MODE_MIXED -- all frequencies at once: complex GMRES whose matrix
- *                     products run on an FP32 copy of the matrix, FP64
- *                     Arnoldi, FP64-residual iterative refinement to `tol`
- *                     (relative residual), batched field and force.
+ *                     products run on the tensor cores (3xFP16 on a scaled
+ *                     fp16 pair of the matrix: about FP32 accuracy),
+ *                     double-FP32 Arnoldi, right preconditioning by the
+ *                     electrodes' blocks, iterative refinement on an
+ *                     FP64-accurate residual to `tol` (relative residual),
+ *                     batched field and force.
  * forces receives 9 doubles per frequency: Fcm[3], Xcm[3] and the sum over
  * particle elements of |Fce| per component (the scale of the net force).
  * sigma (may be NULL) receives 2N doubles per frequency (Re then Im).
@@ -270,7 +273,8 @@ void dsc_session_destroy(dsc_session *s);
  * mode DSC_MODE_FP64: regular pairs in FP64, the reference's arithmetic;
  * DSC_MODE_MIXED: regular pairs in the arithmetic dsc_session_set_mixed_
  * assembly chose, and the fp16 copies for the tensor cores.  Singular pairs
- * are FP64 in both.  An FP64 solve on a matrix assembled for the mixed mode
+ * are FP64 in the FP64 mode and double-FP32 (about 1e-13 of FP64) in the
+ * mixed mode.  An FP64 solve on a matrix assembled for the mixed mode
  * assembles it again in FP64; a mixed solve keeps a more accurate matrix. */
 int dsc_session_assemble(dsc_session *s, int mode);
 /* Arithmetic of the mixed mode's regular (non-singular) pairs:
