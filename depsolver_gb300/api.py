@@ -244,7 +244,9 @@ class Session:
 
     def assemble(self, mode: int = MODE_FP64):
         """Assemble K now: MODE_FP64 in FP64, MODE_MIXED with the regular
-        pairs in double-FP32 (and the tensor cores' FP32 copy)."""
+        pairs in the arithmetic set_mixed_assembly chose (FP32 by default),
+        the singular pairs in double-FP32, and the tensor cores' fp16
+        pair."""
         _native.check(self._L.dsc_session_assemble(self._h, mode))
 
     def geometric_matrix(self, mode: int = MODE_FP64) -> np.ndarray:
