@@ -28,19 +28,11 @@ struct Shape7 {
     double v[kTriPts][6];
 };
 
-constexpr double kT7[kTriPts][2] = {
-    {0.333333333333333, 0.333333333333333}, {0.470142064105115, 0.470142064105115},
-    {0.0597158717897700, 0.470142064105115}, {0.470142064105115, 0.0597158717897700},
-    {0.101286507323456, 0.101286507323456}, {0.797426985353088, 0.101286507323456},
-    {0.101286507323456, 0.797426985353088}};
-constexpr double kW7[kTriPts] = {0.1125, 0.066197076394253, 0.066197076394253, 0.066197076394253,
-                                 0.062969590272414, 0.062969590272414, 0.062969590272414};
-
 constexpr Shape7 make_shape(int nen)
 {
     Shape7 s{};
     for (int q = 0; q < kTriPts; q++) {
-        double l1 = kT7[q][0], l2 = kT7[q][1], l3 = 1.0 - l1 - l2;
+        double l1 = kTri7.v[q][0], l2 = kTri7.v[q][1], l3 = 1.0 - l1 - l2;
         if (nen == 3) {
             s.v[q][0] = l1;
             s.v[q][1] = l2;

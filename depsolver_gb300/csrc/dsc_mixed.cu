@@ -839,12 +839,18 @@ __global__ void k_field_batched_reduce(const float *__restrict__ part, int nchun
     Enode[((size_t)f * N + ids[p]) * 3 + d] = A * s + sing[t];
 }
 
+// w J of a particle element's quadrature point and the unit normal there
+// (one 32-byte load)
+struct alignas(32) MstGeo {
+    double wj, nx, ny, nz;
+};
+
 // Frequency-independent geometry of the Maxwell-stress integrals: per
 // (particle element t, point q) the weight w_q J_q and the unit normal.
 template <int NEN>
 __global__ void k_mst_geometry(const double *__restrict__ X, const double *__restrict__ Y,
                                const double *__restrict__ Z, const int *__restrict__ elems,
-                               const int *__restrict__ pel, int npel, double4 *__restrict__ geo)
+                               const int *__restrict__ pel, int npel, MstGeo *__restrict__ geo)
 {
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
     if (u >= npel * kTriPts) return;
@@ -862,14 +868,14 @@ __global__ void k_mst_geometry(const double *__restrict__ X, const double *__res
     shape<NEN>(l1, l2, N6);
     const double J = map_point<NEN>(Xe, l1, l2, N6, XL);
     local_normal<NEN>(Xe, l1, l2, n);
-    geo[u] = make_double4(J * c_tri7[q][2], n[0], n[1], n[2]);
+    geo[u] = MstGeo{J * c_tri7[q][2], n[0], n[1], n[2]};
 }
 
 // Maxwell stress per (particle element, frequency), from the element's
 // geometry (k_mst_geometry) and the nodal field of that frequency.
 template <int NEN>
 __global__ void k_mst_batched(const int *__restrict__ elems, const int *__restrict__ pel, int npel,
-                              const double4 *__restrict__ geo, const double *__restrict__ Enode, int N, int F,
+                              const MstGeo *__restrict__ geo, const double *__restrict__ Enode, int N, int F,
                               double eps, double *__restrict__ Fce)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -889,7 +895,7 @@ __global__ void k_mst_batched(const int *__restrict__ elems, const int *__restri
 #pragma unroll
     for (int q = 0; q < kTriPts; q++) {
         shape<NEN>(c_tri7[q][0], c_tri7[q][1], N6);
-        const double4 g = geo[(size_t)t * kTriPts + q];
+        const MstGeo g = geo[(size_t)t * kTriPts + q];
         double Ex = 0.0, Ey = 0.0, Ez = 0.0;
 #pragma unroll
         for (int k = 0; k < NEN; k++) {
@@ -897,11 +903,11 @@ __global__ void k_mst_batched(const int *__restrict__ elems, const int *__restri
             Ey += En[k][1] * N6[k];
             Ez += En[k][2] * N6[k];
         }
-        const double NE = Ex * g.y + Ey * g.z + Ez * g.w;
+        const double NE = Ex * g.nx + Ey * g.ny + Ez * g.nz;
         const double Esq = Ex * Ex + Ey * Ey + Ez * Ez;
-        I0 += g.x * (Ex * NE - 0.5 * Esq * g.y);
-        I1 += g.x * (Ey * NE - 0.5 * Esq * g.z);
-        I2 += g.x * (Ez * NE - 0.5 * Esq * g.w);
+        I0 += g.wj * (Ex * NE - 0.5 * Esq * g.nx);
+        I1 += g.wj * (Ey * NE - 0.5 * Esq * g.ny);
+        I2 += g.wj * (Ez * NE - 0.5 * Esq * g.nz);
     }
     const double A = 0.5 * eps;
     double *o = Fce + ((size_t)f * npel + t) * 3;
@@ -979,7 +985,7 @@ struct Session::Mixed {
     // batched field
     DevBuf<double> sing, Enode, Fce, tot, Xce, ptot;
     DevBuf<double> gpart;  // split partials of the FP64 GEMV residual (no digits)
-    DevBuf<double4> mst_geo;  // per (particle element, point): w J and the unit normal
+    DevBuf<MstGeo> mst_geo;  // per (particle element, point): w J and the unit normal
     DevBuf<float> part;  // field partials per element group (FP32)
     // FP32 far-field pass: element centroids / offsets, split points, weights
     bool far_ready = false;
