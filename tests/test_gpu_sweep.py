@@ -91,8 +91,10 @@ def test_session_timing_counts_kernels(gpu):
 
 @pytest.mark.parametrize("nen", [6, 3])
 def test_double_fp32_assembly_matches_fp64(gpu, port, nen):
-    """K with the regular pairs in double-FP32 (the mixed mode's assembly)
-    against the FP64 assembly and the C restatement of the reference."""
+    """K with the regular pairs in double-FP32 (the mixed mode's
+    double-FP32 assembly; its singular pairs are double-FP32 in every mixed
+    assembly) against the FP64 assembly, to 1e-13 of the matrix's scale, and
+    the FP64 K against the C restatement of the reference."""
     sc = scenes.small(nen=nen)
     s = api.Session(sc)
     s.set_mixed_assembly(api.ASM_DF32)
